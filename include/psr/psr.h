@@ -1,0 +1,130 @@
+/*
+ * psr.h - C ABI of the GB300 Poisson surface reconstruction path.
+ *
+ * Drop-in replacement for the data-parallel path of the reference's
+ * SparseSurfelFusion::PoissonReconstruction (mesh/PoissonReconstruction.h:63-184):
+ * oriented (optionally coloured) points in, triangle mesh out.  The reference's
+ * compile-time configuration (base/GlobalConfigs.h) becomes a runtime psr_config; all
+ * state lives in a handle (no process-global __constant__ state), every call returns a
+ * status instead of exiting, and no call allocates device memory after psr_create.
+ *
+ * Plain C types only: pointers, sizes and a CUDA stream passed as void*.
+ */
+#ifndef PSR_PSR_H_
+#define PSR_PSR_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PSR_ABI_VERSION 1
+
+typedef enum psr_status {
+    PSR_OK = 0,
+    PSR_OUT_OF_CAPACITY = 1, /* a count exceeded its configured capacity */
+    PSR_INVALID_INPUT = 2,   /* bad argument, empty cloud, non-finite coordinate */
+    PSR_NONCONVERGED = 3,    /* CG hit its iteration limit above tolerance (informational) */
+    PSR_DEVICE_TIMEOUT = 4,  /* a bounded device-side wait gave up */
+    PSR_CUDA_ERROR = 5       /* CUDA runtime error (message via psr_last_error) */
+} psr_status;
+
+typedef enum psr_location { PSR_HOST = 0, PSR_DEVICE = 1 } psr_location;
+
+/* Capacities and solver settings; replaces base/GlobalConfigs.h:7-53. */
+typedef struct psr_config {
+    int max_depth;             /* MAX_DEPTH_OCTREE (base/GlobalConfigs.h:34); 2..9 */
+    int max_points;            /* MAX_SURFEL_COUNT (:7) */
+    int max_triangles;         /* MAX_MESH_TRIANGLE_COUNT (:8) */
+    int max_mesh_vertices;     /* MeshTriangleVertex capacity (mesh/ComputeTriangleIndices.cpp:32) */
+    int max_nodes;             /* 0: 10 x max_points (TOTAL_NODEARRAY_MAX_COUNT, :42) */
+    int max_subdivision_nodes; /* 0: 16 x max_points */
+    float bbox_scale;          /* 1.25 (mesh/BuildOctree.cpp:91) */
+    int cg_max_iterations;     /* 10000 (mesh/solver/CGAlgorithm.cu:15) */
+    float cg_tolerance;        /* 1e-5, absolute on ||r|| (mesh/solver/CGAlgorithm.cu:298) */
+    int compute_colors;        /* per-vertex colour transfer (mesh/DrawMesh.cu:179-214) */
+    int compute_normals;       /* per-vertex normals (mesh/DrawMesh.cu:102-177) */
+    int device;                /* CUDA device ordinal */
+} psr_config;
+
+/* Oriented input cloud (the fields of DepthSurfel, base/CommonTypes.h:113-118, as SoA). */
+typedef struct psr_points {
+    const float* xyz;      /* 3 * count, x y z interleaved */
+    const float* normals;  /* 3 * count */
+    const uint8_t* rgb;    /* 3 * count, or NULL; colour = rgb / 255 */
+    int count;
+    int location;          /* psr_location of the three arrays */
+} psr_points;
+
+/* Per-call options. */
+typedef struct psr_options {
+    int depth;             /* octree depth of this call, <= max_depth (0: max_depth) */
+    int cg_iterations;     /* > 0: per-depth iteration limit instead of cg_max_iterations */
+} psr_options;
+
+/* Output mesh: vertices in the normalised unit cube of the reference
+ * (mesh/ComputeTriangleIndices.h:331-342); world = center + vertex * scale. */
+typedef struct psr_mesh {
+    float* vertices;       /* 3 * vertex_capacity */
+    int32_t* triangles;    /* 3 * triangle_capacity */
+    float* colors;         /* 3 * vertex_capacity, or NULL */
+    float* normals;        /* 3 * vertex_capacity, or NULL */
+    int vertex_capacity;
+    int triangle_capacity;
+    int location;          /* psr_location of the output arrays */
+    int vertex_count;      /* out */
+    int triangle_count;    /* out */
+    float center[3];       /* out: bounding-box origin */
+    float scale;           /* out: bounding-box edge (1.25 x largest extent) */
+} psr_mesh;
+
+/* Counts of the last reconstruction. */
+typedef struct psr_stats {
+    int points, unique_leaves, nodes, depth;
+    int level_count[10];
+    int vertices, edges, faces;
+    int crossings, triangles;
+    int subdivision_roots, subdivision_nodes;
+    int mesh_vertices, mesh_triangles;
+    int cg_iterations[10];
+    double cg_residual[10];
+    float iso_value;
+    unsigned error_bits;
+    float stage_ms[6];     /* octree, field, solve, mesh, transfer, total (device time) */
+} psr_stats;
+
+typedef struct psr_handle psr_handle;
+
+/* Fills the reference defaults. */
+psr_status psr_config_default(psr_config* cfg);
+
+/* Allocates every device buffer from the capacities (replaces the constructor,
+ * mesh/PoissonReconstruction.cpp:10-30, and ComputeVectorField::BuildInnerProductTable,
+ * mesh/ComputeVectorField.cpp:77-121). */
+psr_status psr_create(const psr_config* cfg, psr_handle** out);
+
+psr_status psr_destroy(psr_handle* h);
+
+/* One reconstruction (replaces SolvePoissionReconstructionMesh,
+ * mesh/PoissonReconstruction.cpp:195-245, and the mesh read-back of DrawRebuildMesh,
+ * :248-252).  `stream` is a cudaStream_t or NULL for the handle's own stream.  The call
+ * returns once the mesh counts are known and the mesh has been written. */
+psr_status psr_reconstruct(psr_handle* h, const psr_points* points, const psr_options* options,
+                           psr_mesh* mesh, void* stream);
+
+psr_status psr_get_stats(const psr_handle* h, psr_stats* out);
+
+/* Copies an internal device array of the last reconstruction to host memory (testing
+ * and inspection).  Returns the byte size in *bytes; dst may be NULL to query it. */
+psr_status psr_debug_array(psr_handle* h, const char* name, void* dst, size_t dst_bytes, size_t* bytes);
+
+const char* psr_status_string(psr_status s);
+const char* psr_last_error(const psr_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PSR_PSR_H_ */

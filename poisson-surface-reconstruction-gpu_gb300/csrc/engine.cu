@@ -1,0 +1,454 @@
+// Handle, workspace allocation and the C ABI (include/psr/psr.h).
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/psr/psr.h"
+#include "workspace.h"
+
+namespace psr {
+cudaError_t upload_tables_octree();
+cudaError_t upload_tables_field();
+cudaError_t upload_tables_solver();
+cudaError_t upload_tables_mesh();
+cudaError_t upload_tables_transfer();
+void build_dff_table(int depth, std::vector<double>& dff);
+void build_stencil(int depth, std::vector<float>& st);
+}  // namespace psr
+
+using namespace psr;
+
+struct DebugArray {
+    const void* ptr;
+    int elem;        // bytes per element
+    int kind;        // 0 int32, 1 float32, 2 float64, 3 uint8, 4 uint16
+    const int* count_field;   // device counter (nullptr: fixed count)
+    long long fixed;
+    int mult;        // elements per counted item
+};
+
+struct psr_handle {
+    psr_config cfg;
+    Workspace ws;
+    void* arena = nullptr;
+    size_t arena_bytes = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaEvent_t ev[6] = {};
+    Counters host_cnt;
+    bool have_result = false;
+    std::string last_error;
+    psr_stats stats;
+};
+
+namespace {
+
+struct Arena {
+    size_t bytes = 0;
+    std::vector<std::pair<void**, size_t>> items;
+    template <class T>
+    void add(T*& p, size_t count) {
+        items.push_back({(void**)&p, count * sizeof(T)});
+        bytes += (count * sizeof(T) + 255) & ~(size_t)255;
+    }
+    void assign(char* base) {
+        size_t off = 0;
+        for (auto& it : items) {
+            *it.first = base + off;
+            off += (it.second + 255) & ~(size_t)255;
+        }
+    }
+};
+
+psr_status fail(psr_handle* h, psr_status s, const char* msg) {
+    if (h) h->last_error = msg ? msg : "";
+    return s;
+}
+
+psr_status cuda_fail(psr_handle* h, cudaError_t e, const char* where) {
+    if (h) h->last_error = std::string(where) + ": " + cudaGetErrorString(e);
+    return PSR_CUDA_ERROR;
+}
+
+}  // namespace
+
+extern "C" {
+
+psr_status psr_config_default(psr_config* c) {
+    if (!c) return PSR_INVALID_INPUT;
+    memset(c, 0, sizeof(*c));
+    c->max_depth = 7;
+    c->max_points = 300000;
+    c->max_triangles = 1000000;
+    c->max_mesh_vertices = 300000;
+    c->max_nodes = 0;
+    c->max_subdivision_nodes = 0;
+    c->bbox_scale = 1.25f;
+    c->cg_max_iterations = 10000;
+    c->cg_tolerance = 1e-5f;
+    c->compute_colors = 0;
+    c->compute_normals = 0;
+    c->device = 0;
+    return PSR_OK;
+}
+
+const char* psr_status_string(psr_status s) {
+    switch (s) {
+        case PSR_OK: return "ok";
+        case PSR_OUT_OF_CAPACITY: return "out of capacity";
+        case PSR_INVALID_INPUT: return "invalid input";
+        case PSR_NONCONVERGED: return "not converged";
+        case PSR_DEVICE_TIMEOUT: return "device timeout";
+        case PSR_CUDA_ERROR: return "cuda error";
+    }
+    return "unknown";
+}
+
+const char* psr_last_error(const psr_handle* h) { return h ? h->last_error.c_str() : ""; }
+
+psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
+    if (!out) return PSR_INVALID_INPUT;
+    *out = nullptr;
+    psr_config cfg;
+    if (cfg_in) cfg = *cfg_in;
+    else psr_config_default(&cfg);
+    if (cfg.max_depth < 2 || cfg.max_depth > kMaxDepth || cfg.max_points <= 0 || cfg.max_triangles <= 0 ||
+        cfg.max_mesh_vertices <= 0)
+        return PSR_INVALID_INPUT;
+    if (cfg.bbox_scale <= 0.0f) cfg.bbox_scale = 1.25f;
+    if (cfg.cg_max_iterations <= 0) cfg.cg_max_iterations = 10000;
+    psr_handle* h = new (std::nothrow) psr_handle();
+    if (!h) return PSR_CUDA_ERROR;
+    h->cfg = cfg;
+    cudaError_t e = cudaSetDevice(cfg.device);
+    if (e != cudaSuccess) { psr_status st = cuda_fail(h, e, "cudaSetDevice"); delete h; return st; }
+    Workspace& ws = h->ws;
+    memset(&ws, 0, sizeof(ws));
+    cudaDeviceGetAttribute(&ws.num_sms, cudaDevAttrMultiProcessorCount, cfg.device);
+    if (ws.num_sms <= 0) ws.num_sms = 148;
+
+    const long long N = cfg.max_points;
+    const long long nodes = cfg.max_nodes > 0 ? cfg.max_nodes : 10 * N;
+    const long long dnodes = std::min(nodes, 8 * N);
+    const long long subn = cfg.max_subdivision_nodes > 0 ? cfg.max_subdivision_nodes : 16 * N;
+    const long long subd = subn;   // D-level subdivision nodes are a subset
+    Caps& cap = ws.cap;
+    cap.points = (int)N;
+    cap.nodes = (int)nodes;
+    cap.dnodes = (int)dnodes;
+    cap.vertices = (int)std::min(4 * nodes, (long long)1 << 30);
+    cap.edges = (int)std::min(6 * dnodes, (long long)1 << 30);
+    cap.faces = (int)std::min(4 * nodes, (long long)1 << 30);
+    cap.sub_nodes = (int)subn;
+    cap.sub_dnodes = (int)subd;
+    cap.mesh_vertices = cfg.max_mesh_vertices;
+    cap.mesh_tris = cfg.max_triangles;
+    ws.part_cap_v = 2 * cfg.max_mesh_vertices + 4096;
+    ws.part_cap_t = 2 * cfg.max_triangles + 4096;
+    long long max_scan = std::max({N + 1, nodes, (long long)cap.edges, (long long)cap.faces, (long long)cap.vertices,
+                                   subd * 12, (long long)ws.part_cap_v, (long long)ws.part_cap_t,
+                                   256LL * ((N + kSortTile - 1) / kSortTile)});
+    cap.scan_tiles = (int)((max_scan + kScanTile - 1) / kScanTile) + 1;
+    const int sort_tiles = (int)((N + kSortTile - 1) / kSortTile) + 1;
+    const int D = cfg.max_depth;
+    ws.res = (1 << (D + 1)) - 1;
+
+    Arena A;
+    A.add(ws.cnt, 1);
+    A.add(ws.scan.words, (size_t)cap.scan_tiles + 1);
+    A.add(ws.sort.hist, (size_t)kRadix * sort_tiles + 16);
+    A.add(ws.sort.keys_alt, (size_t)N);
+    A.add(ws.sort.vals_alt, (size_t)N);
+    A.add(ws.in_xyz, 3 * (size_t)N);
+    A.add(ws.in_nrm, 3 * (size_t)N);
+    A.add(ws.in_rgb, 3 * (size_t)N);
+    A.add(ws.code, (size_t)N);
+    A.add(ws.sidx, (size_t)N);
+    A.add(ws.px, (size_t)N); A.add(ws.py, (size_t)N); A.add(ws.pz, (size_t)N);
+    A.add(ws.nx, (size_t)N); A.add(ws.ny, (size_t)N); A.add(ws.nz, (size_t)N);
+    A.add(ws.cr, (size_t)N); A.add(ws.cg, (size_t)N); A.add(ws.cb, (size_t)N);
+    A.add(ws.point2node, (size_t)N);
+    A.add(ws.puid, (size_t)N);
+    A.add(ws.ucode, (size_t)N);
+    A.add(ws.ufirst, (size_t)N + 1);
+    A.add(ws.uslot, (size_t)N);
+    A.add(ws.uaddr, (size_t)N);
+    A.add(ws.tkey, (size_t)nodes); A.add(ws.tpidx, (size_t)nodes); A.add(ws.tpnum, (size_t)nodes);
+    A.add(ws.tdidx, (size_t)nodes); A.add(ws.tdnum, (size_t)nodes); A.add(ws.tchild, (size_t)nodes);
+    A.add(ws.tparent_slot, (size_t)nodes / 8 + 8);
+    A.add(ws.gkey, (size_t)dnodes / 8 + 8); A.add(ws.gpidx, (size_t)dnodes / 8 + 8);
+    A.add(ws.gpnum, (size_t)dnodes / 8 + 8); A.add(ws.gdidx, (size_t)dnodes / 8 + 8);
+    A.add(ws.gdnum, (size_t)dnodes / 8 + 8); A.add(ws.gaddr, (size_t)dnodes / 8 + 8);
+    A.add(ws.key, (size_t)nodes); A.add(ws.pidx, (size_t)nodes); A.add(ws.pnum, (size_t)nodes);
+    A.add(ws.parent, (size_t)nodes); A.add(ws.first_child, (size_t)nodes); A.add(ws.didx, (size_t)nodes);
+    A.add(ws.dnum, (size_t)nodes); A.add(ws.ndepth, (size_t)nodes); A.add(ws.enc, (size_t)nodes);
+    A.add(ws.ctr_x, (size_t)nodes); A.add(ws.ctr_y, (size_t)nodes); A.add(ws.ctr_z, (size_t)nodes);
+    A.add(ws.neigh, 27 * (size_t)nodes);
+    A.add(ws.node_vtx, 8 * (size_t)nodes);
+    A.add(ws.node_edge, 12 * (size_t)nodes);
+    A.add(ws.node_face, 6 * (size_t)nodes);
+    A.add(ws.dff, (size_t)ws.res * ws.res);
+    A.add(ws.stencil, (size_t)(kMaxDepth + 1) * 27);
+    A.add(ws.vfield, 3 * (size_t)dnodes);
+    A.add(ws.divg, (size_t)nodes);
+    A.add(ws.xsol, (size_t)nodes);
+    A.add(ws.cg_r, (size_t)nodes); A.add(ws.cg_p, (size_t)nodes); A.add(ws.cg_ap, (size_t)nodes);
+    A.add(ws.cg_partial, std::max((size_t)nodes, (size_t)4096 * (kMaxDepth + 1)));
+    A.add(ws.point_val, (size_t)N);
+    A.add(ws.iso_partial, (size_t)ws.num_sms * 8 + 64);
+    A.add(ws.vmask, (size_t)nodes);
+    A.add(ws.emask16, (size_t)dnodes);
+    A.add(ws.fmask, (size_t)nodes);
+    A.add(ws.v_x, (size_t)cap.vertices); A.add(ws.v_y, (size_t)cap.vertices); A.add(ws.v_z, (size_t)cap.vertices);
+    A.add(ws.v_owner, (size_t)cap.vertices); A.add(ws.v_kind, (size_t)cap.vertices); A.add(ws.v_depth, (size_t)cap.vertices);
+    A.add(ws.e_owner, (size_t)cap.edges); A.add(ws.e_kind, (size_t)cap.edges);
+    A.add(ws.f_owner, (size_t)cap.faces); A.add(ws.f_kind, (size_t)cap.faces); A.add(ws.f_hasparent, (size_t)cap.faces);
+    A.add(ws.vvalue, (size_t)cap.vertices);
+    A.add(ws.e_cross, (size_t)cap.edges);
+    A.add(ws.cube_class, (size_t)dnodes);
+    A.add(ws.face_hit, (size_t)cap.faces);
+    A.add(ws.sub_root, (size_t)nodes);
+    A.add(ws.sub_root_depth, (size_t)nodes);
+    A.add(ws.node_subslot, (size_t)nodes);
+    A.add(ws.node_subgroup, (size_t)nodes);
+    A.add(ws.s_key, (size_t)subn); A.add(ws.s_parent, (size_t)subn); A.add(ws.s_first_child, (size_t)subn);
+    A.add(ws.s_neigh, 27 * (size_t)subn); A.add(ws.s_depth, (size_t)subn); A.add(ws.s_root, (size_t)subn);
+    A.add(ws.s_group, (size_t)subn);
+    A.add(ws.s_cx, (size_t)subn); A.add(ws.s_cy, (size_t)subn); A.add(ws.s_cz, (size_t)subn);
+    A.add(ws.s_vtx, 8 * (size_t)subd); A.add(ws.s_edge, 12 * (size_t)subd);
+    A.add(ws.s_vmask, (size_t)subd); A.add(ws.s_emask, (size_t)subd);
+    A.add(ws.sv_x, 8 * (size_t)subd); A.add(ws.sv_y, 8 * (size_t)subd); A.add(ws.sv_z, 8 * (size_t)subd);
+    A.add(ws.sv_owner, 8 * (size_t)subd); A.add(ws.sv_kind, 8 * (size_t)subd); A.add(ws.sv_value, 8 * (size_t)subd);
+    A.add(ws.se_owner, 12 * (size_t)subd); A.add(ws.se_kind, 12 * (size_t)subd); A.add(ws.se_cross, 12 * (size_t)subd);
+    A.add(ws.s_cube_class, (size_t)subd);
+    A.add(ws.mesh_v, 3 * (size_t)cap.mesh_vertices);
+    A.add(ws.mesh_t, 3 * (size_t)cap.mesh_tris);
+    A.add(ws.mesh_c, 3 * (size_t)cap.mesh_vertices);
+    A.add(ws.mesh_n, 3 * (size_t)cap.mesh_vertices);
+    A.add(ws.nacc, 3 * (size_t)cap.mesh_vertices);
+    A.add(ws.vcount, (size_t)cap.mesh_vertices);
+    A.add(ws.cell_start, (size_t)(1 << 18) + 16);
+    A.add(ws.part_v, 3 * (size_t)ws.part_cap_v);
+    A.add(ws.part_t, 3 * (size_t)ws.part_cap_t);
+    ws.mb.max_groups = (int)nodes;
+    A.add(ws.mb.ov_group, 8 * (size_t)nodes);
+    A.add(ws.mb.ov_sub, 8 * (size_t)nodes);
+    A.add(ws.mb.groups, 8 * (size_t)nodes);
+    A.add(ws.mb.edge_of_dnode, (size_t)subd);
+    A.add(ws.mb.tri_of_dnode, (size_t)subd);
+    A.add(ws.mb.group_cross0, (size_t)nodes);
+    A.add(ws.mb.parts, 4 * (size_t)nodes + 8);
+    A.add(ws.mb.kept_prefix, (size_t)ws.part_cap_v);
+    A.add(ws.mb.misc, 16);
+
+    e = cudaMalloc(&h->arena, A.bytes);
+    if (e != cudaSuccess) { psr_status st = cuda_fail(h, e, "cudaMalloc workspace"); delete h; return st; }
+    h->arena_bytes = A.bytes;
+    A.assign((char*)h->arena);
+    ws.scan.max_tiles = cap.scan_tiles;
+    ws.sort.max_tiles = sort_tiles;
+    ws.sort.scan = ws.scan;   // sort shares the scan scratch (scans are sequential on one stream)
+    e = cudaMallocHost(&ws.cnt_host, sizeof(Counters));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
+    for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&h->ev[i]);
+    // tables
+    if (e == cudaSuccess) e = upload_tables_octree();
+    if (e == cudaSuccess) e = upload_tables_field();
+    if (e == cudaSuccess) e = upload_tables_solver();
+    if (e == cudaSuccess) e = upload_tables_mesh();
+    if (e == cudaSuccess) e = upload_tables_transfer();
+    if (e == cudaSuccess) {
+        std::vector<double> dff;
+        build_dff_table(D, dff);
+        std::vector<float> st;
+        build_stencil(kMaxDepth, st);
+        e = cudaMemcpy(ws.dff, dff.data(), dff.size() * sizeof(double), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(ws.stencil, st.data(), st.size() * sizeof(float), cudaMemcpyHostToDevice);
+    }
+    if (e != cudaSuccess) {
+        psr_status st = cuda_fail(h, e, "psr_create");
+        psr_destroy(h);
+        return st;
+    }
+    *out = h;
+    return PSR_OK;
+}
+
+psr_status psr_destroy(psr_handle* h) {
+    if (!h) return PSR_OK;
+    if (h->arena) cudaFree(h->arena);
+    if (h->ws.cnt_host) cudaFreeHost(h->ws.cnt_host);
+    for (int i = 0; i < 6; ++i) if (h->ev[i]) cudaEventDestroy(h->ev[i]);
+    if (h->own_stream) cudaStreamDestroy(h->own_stream);
+    delete h;
+    return PSR_OK;
+}
+
+psr_status psr_reconstruct(psr_handle* h, const psr_points* pts, const psr_options* opt, psr_mesh* mesh,
+                           void* stream) {
+    if (!h) return PSR_INVALID_INPUT;
+    h->have_result = false;
+    if (!pts || !mesh || !pts->xyz || !pts->normals) return fail(h, PSR_INVALID_INPUT, "null argument");
+    const int n = pts->count;
+    if (n <= 0) return fail(h, PSR_INVALID_INPUT, "empty point cloud");
+    if (n > h->ws.cap.points) return fail(h, PSR_OUT_OF_CAPACITY, "more points than max_points");
+    int depth = (opt && opt->depth > 0) ? opt->depth : h->cfg.max_depth;
+    if (depth < 2 || depth > h->cfg.max_depth) return fail(h, PSR_INVALID_INPUT, "depth outside [2, max_depth]");
+    const int cg_iters = (opt && opt->cg_iterations > 0) ? opt->cg_iterations : 0;
+    Workspace& ws = h->ws;
+    ws.depth = depth;
+    cudaStream_t s = stream ? (cudaStream_t)stream : h->own_stream;
+    ws.stream = s;
+    cudaError_t e = cudaSetDevice(h->cfg.device);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaSetDevice");
+    // inputs
+    const cudaMemcpyKind kind = (pts->location == PSR_DEVICE) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    e = cudaMemcpyAsync(ws.in_xyz, pts->xyz, 3 * sizeof(float) * (size_t)n, kind, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ws.in_nrm, pts->normals, 3 * sizeof(float) * (size_t)n, kind, s);
+    const bool has_rgb = pts->rgb != nullptr;
+    if (e == cudaSuccess && has_rgb) e = cudaMemcpyAsync(ws.in_rgb, pts->rgb, 3 * (size_t)n, kind, s);
+    if (e != cudaSuccess) return cuda_fail(h, e, "input copy");
+    uint8_t* saved_rgb = ws.in_rgb;
+    if (!has_rgb) ws.in_rgb = nullptr;
+    cudaEventRecord(h->ev[0], s);
+    e = octree_build(ws, n);
+    if (e == cudaSuccess) { cudaEventRecord(h->ev[1], s); e = field_build(ws); }
+    if (e == cudaSuccess) {
+        cudaEventRecord(h->ev[2], s);
+        e = solve_build(ws, cg_iters > 0 ? 1 : 0, cg_iters, h->cfg.cg_tolerance, h->cfg.cg_max_iterations);
+    }
+    if (e == cudaSuccess) { cudaEventRecord(h->ev[3], s); e = mesh_build(ws); }
+    const int want_colour = h->cfg.compute_colors && mesh->colors;
+    const int want_normals = h->cfg.compute_normals && mesh->normals;
+    if (e == cudaSuccess) { cudaEventRecord(h->ev[4], s); e = transfer_build(ws, want_colour, want_normals); }
+    ws.in_rgb = saved_rgb;
+    if (e == cudaSuccess) { cudaEventRecord(h->ev[5], s); e = cudaMemcpyAsync(ws.cnt_host, ws.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, s); }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(h, e, "reconstruct");
+    Counters& c = *ws.cnt_host;
+    h->host_cnt = c;
+    h->have_result = true;
+    // stats
+    psr_stats& st = h->stats;
+    memset(&st, 0, sizeof(st));
+    st.points = c.n_points; st.unique_leaves = c.n_unique; st.nodes = c.n_nodes; st.depth = depth;
+    for (int d = 0; d <= kMaxDepth; ++d) { st.level_count[d] = c.level_count[d]; st.cg_iterations[d] = c.cg_iters[d]; st.cg_residual[d] = c.cg_rr[d] > 0 ? sqrt(c.cg_rr[d]) : 0.0; }
+    st.vertices = c.n_vertices; st.edges = c.n_edges; st.faces = c.n_faces;
+    st.crossings = c.n_cross; st.triangles = c.n_tri;
+    st.subdivision_roots = c.n_subroots; st.subdivision_nodes = c.n_sub_nodes;
+    st.mesh_vertices = c.n_mesh_vertices; st.mesh_triangles = c.n_mesh_triangles;
+    st.iso_value = c.iso;
+    st.error_bits = c.error;
+    for (int i = 0; i < 5; ++i) cudaEventElapsedTime(&st.stage_ms[i], h->ev[i], h->ev[i + 1]);
+    cudaEventElapsedTime(&st.stage_ms[5], h->ev[0], h->ev[5]);
+    if (c.error & kErrInvalid) return fail(h, PSR_INVALID_INPUT, "non-finite input or malformed octree");
+    if (c.error & kErrCapacity) return fail(h, PSR_OUT_OF_CAPACITY, "a device count exceeded its capacity");
+    if (c.error & kErrSpinTimeout) return fail(h, PSR_DEVICE_TIMEOUT, "a bounded device wait gave up");
+    // outputs
+    mesh->vertex_count = c.n_mesh_vertices;
+    mesh->triangle_count = c.n_mesh_triangles;
+    for (int a = 0; a < 3; ++a) mesh->center[a] = c.center[a];
+    mesh->scale = c.max_edge;
+    if (c.n_mesh_vertices > mesh->vertex_capacity || c.n_mesh_triangles > mesh->triangle_capacity)
+        return fail(h, PSR_OUT_OF_CAPACITY, "output mesh buffers too small");
+    const cudaMemcpyKind ok = (mesh->location == PSR_DEVICE) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if (mesh->vertices && c.n_mesh_vertices)
+        e = cudaMemcpyAsync(mesh->vertices, ws.mesh_v, 3 * sizeof(float) * (size_t)c.n_mesh_vertices, ok, s);
+    if (e == cudaSuccess && mesh->triangles && c.n_mesh_triangles)
+        e = cudaMemcpyAsync(mesh->triangles, ws.mesh_t, 3 * sizeof(int) * (size_t)c.n_mesh_triangles, ok, s);
+    if (e == cudaSuccess && want_colour && c.n_mesh_vertices)
+        e = cudaMemcpyAsync(mesh->colors, ws.mesh_c, 3 * sizeof(float) * (size_t)c.n_mesh_vertices, ok, s);
+    if (e == cudaSuccess && want_normals && c.n_mesh_vertices)
+        e = cudaMemcpyAsync(mesh->normals, ws.mesh_n, 3 * sizeof(float) * (size_t)c.n_mesh_vertices, ok, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(h, e, "output copy");
+    return PSR_OK;
+}
+
+psr_status psr_get_stats(const psr_handle* h, psr_stats* out) {
+    if (!h || !out) return PSR_INVALID_INPUT;
+    *out = h->stats;
+    return PSR_OK;
+}
+
+psr_status psr_debug_array(psr_handle* h, const char* name, void* dst, size_t dst_bytes, size_t* bytes) {
+    if (!h || !name) return PSR_INVALID_INPUT;
+    if (!h->have_result) return fail(h, PSR_INVALID_INPUT, "no reconstruction yet");
+    const Workspace& ws = h->ws;
+    const Counters& c = h->host_cnt;
+    const int D = ws.depth;
+    const size_t M = (size_t)c.n_nodes, N = (size_t)c.n_points, MD = (size_t)c.level_count[D];
+    struct Item { const void* p; size_t bytes; size_t stride_bytes; int rows; };
+    std::string nm(name);
+    std::vector<Item> items;
+    auto one = [&](const void* p, size_t b) { items.push_back({p, b, 0, 1}); };
+    auto rows = [&](const void* p, int r, size_t row_bytes, size_t stride_bytes) { items.push_back({p, row_bytes, stride_bytes, r}); };
+    const size_t S = (size_t)ws.cap.nodes;
+    if (nm == "px") one(ws.px, 4 * N);
+    else if (nm == "py") one(ws.py, 4 * N);
+    else if (nm == "pz") one(ws.pz, 4 * N);
+    else if (nm == "nx") one(ws.nx, 4 * N);
+    else if (nm == "ny") one(ws.ny, 4 * N);
+    else if (nm == "nz") one(ws.nz, 4 * N);
+    else if (nm == "point2node") one(ws.point2node, 4 * N);
+    else if (nm == "key") one(ws.key, 4 * M);
+    else if (nm == "pidx") one(ws.pidx, 4 * M);
+    else if (nm == "pnum") one(ws.pnum, 4 * M);
+    else if (nm == "parent") one(ws.parent, 4 * M);
+    else if (nm == "first_child") one(ws.first_child, 4 * M);
+    else if (nm == "didx") one(ws.didx, 4 * M);
+    else if (nm == "dnum") one(ws.dnum, 4 * M);
+    else if (nm == "depth") one(ws.ndepth, 4 * M);
+    else if (nm == "enc") one(ws.enc, 4 * M);
+    else if (nm == "ctr_x") one(ws.ctr_x, 4 * M);
+    else if (nm == "ctr_y") one(ws.ctr_y, 4 * M);
+    else if (nm == "ctr_z") one(ws.ctr_z, 4 * M);
+    else if (nm == "neigh") rows(ws.neigh, 27, 4 * M, 4 * S);
+    else if (nm == "node_vtx") rows(ws.node_vtx, 8, 4 * M, 4 * S);
+    else if (nm == "node_edge") rows(ws.node_edge, 12, 4 * M, 4 * S);
+    else if (nm == "node_face") rows(ws.node_face, 6, 4 * M, 4 * S);
+    else if (nm == "vfield") rows(ws.vfield, 3, 4 * MD, 4 * (size_t)ws.cap.dnodes);
+    else if (nm == "divg") one(ws.divg, 4 * M);
+    else if (nm == "x") one(ws.xsol, 4 * M);
+    else if (nm == "point_val") one(ws.point_val, 4 * N);
+    else if (nm == "v_x") one(ws.v_x, 4 * (size_t)c.n_vertices);
+    else if (nm == "v_y") one(ws.v_y, 4 * (size_t)c.n_vertices);
+    else if (nm == "v_z") one(ws.v_z, 4 * (size_t)c.n_vertices);
+    else if (nm == "v_owner") one(ws.v_owner, 4 * (size_t)c.n_vertices);
+    else if (nm == "v_kind") one(ws.v_kind, 4 * (size_t)c.n_vertices);
+    else if (nm == "v_depth") one(ws.v_depth, 4 * (size_t)c.n_vertices);
+    else if (nm == "vvalue") one(ws.vvalue, 4 * (size_t)c.n_vertices);
+    else if (nm == "e_owner") one(ws.e_owner, 4 * (size_t)c.n_edges);
+    else if (nm == "e_kind") one(ws.e_kind, 4 * (size_t)c.n_edges);
+    else if (nm == "f_owner") one(ws.f_owner, 4 * (size_t)c.n_faces);
+    else if (nm == "f_kind") one(ws.f_kind, 4 * (size_t)c.n_faces);
+    else if (nm == "f_hasparent") one(ws.f_hasparent, 4 * (size_t)c.n_faces);
+    else if (nm == "cube_class") one(ws.cube_class, 4 * MD);
+    else if (nm == "sub_root") one(ws.sub_root, 4 * (size_t)c.n_subroots);
+    else if (nm == "mesh_v") one(ws.mesh_v, 12 * (size_t)c.n_mesh_vertices);
+    else if (nm == "mesh_t") one(ws.mesh_t, 12 * (size_t)c.n_mesh_triangles);
+    else if (nm == "mesh_c") one(ws.mesh_c, 12 * (size_t)c.n_mesh_vertices);
+    else if (nm == "mesh_n") one(ws.mesh_n, 12 * (size_t)c.n_mesh_vertices);
+    else if (nm == "counters") { if (bytes) *bytes = sizeof(Counters); if (dst && dst_bytes >= sizeof(Counters)) memcpy(dst, &c, sizeof(Counters)); return PSR_OK; }
+    else return fail(h, PSR_INVALID_INPUT, "unknown array name");
+    size_t total = 0;
+    for (auto& it : items) total += it.bytes * it.rows;
+    if (bytes) *bytes = total;
+    if (!dst) return PSR_OK;
+    if (dst_bytes < total) return fail(h, PSR_OUT_OF_CAPACITY, "destination too small");
+    char* d = (char*)dst;
+    cudaError_t e = cudaSuccess;
+    for (auto& it : items)
+        for (int r = 0; r < it.rows && e == cudaSuccess; ++r) {
+            e = cudaMemcpy(d, (const char*)it.p + r * it.stride_bytes, it.bytes, cudaMemcpyDeviceToHost);
+            d += it.bytes;
+        }
+    if (e != cudaSuccess) return cuda_fail(h, e, "debug copy");
+    return PSR_OK;
+}
+
+}  // extern "C"

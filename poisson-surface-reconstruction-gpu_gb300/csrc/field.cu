@@ -1,0 +1,234 @@
+// Stage (b): B-spline vector-field splat at the finest depth and per-node divergence.
+//
+// Vector field (mesh/ComputeVectorField.cu:61-100): for every D-level node o
+//     V[o] = sum_{27 neighbours nb} sum_{points p in nb} B(p - c_o) n_p,
+// B the separable normalised quadratic B-spline of width 2^-D, evaluated in the node's
+// local coordinate (the reference expands shifted polynomials in float, which loses
+// ~1e-4 relative accuracy at depth 7; the value is the same function).
+// Divergence (mesh/ComputeNodesDivergence.cu:25-136): for every node o
+//     div[o] = sum_{27 neighbours nb} sum_{D-level l under nb} V[l] . dff(o, l)
+// with float terms accumulated in FP64, as in the reference's finer-depth kernel.  The
+// reference's coarse-depth host loop (one node at a time, :159-207) is replaced by one
+// chunked reduction over all coarse nodes.
+#include "workspace.h"
+#include "tables.cuh"
+
+PSR_DEFINE_CONST_TABLES(upload_tables_field)
+
+namespace psr {
+
+__device__ __forceinline__ float bspline32(float t) {
+    const float kF43 = 1.33333337306976318359375f;
+    const float kF23 = 0.666666686534881591796875f;
+    float a = fabsf(t);
+    if (a < 0.5f) return __fmul_rn(__fsub_rn(0.75f, __fmul_rn(t, t)), kF43);
+    if (a < 1.5f) { float u = __fsub_rn(1.5f, a); return __fmul_rn(__fmul_rn(u, u), kF23); }
+    return 0.0f;
+}
+
+__global__ void __launch_bounds__(kBlock) k_vector_field(const Counters* c, int depth, const float* px, const float* py,
+                                                         const float* pz, const float* nx, const float* ny,
+                                                         const float* nz, const int* pidx, const int* pnum,
+                                                         const float* cx, const float* cy, const float* cz,
+                                                         const int* neigh, size_t stride, float* vx, float* vy,
+                                                         float* vz) {
+    const int md = c->level_count[depth];
+    const int b = c->level_base[depth];
+    const float s = (float)(1 << depth);
+    PSR_GRID_STRIDE(o, md) {
+        const int i = b + o;
+        const float ox = cx[i], oy = cy[i], oz = cz[i];
+        float ax = 0.f, ay = 0.f, az = 0.f;
+        for (int k = 0; k < 27; ++k) {
+            const int nb = neigh[(size_t)k * stride + i];
+            if (nb < 0) continue;
+            const int p0 = pidx[nb], pn = pnum[nb];
+            for (int p = p0; p < p0 + pn; ++p) {
+                float w = bspline32((px[p] - ox) * s) * bspline32((py[p] - oy) * s) * bspline32((pz[p] - oz) * s);
+                ax = fmaf(w, nx[p], ax);
+                ay = fmaf(w, ny[p], ay);
+                az = fmaf(w, nz[p], az);
+            }
+        }
+        vx[o] = ax;
+        vy[o] = ay;
+        vz[o] = az;
+    }
+}
+
+__device__ __forceinline__ void decode3(int e, int depth, int& ix, int& iy, int& iz) {
+    const int o1 = 1 << (depth + 1);
+    ix = e & (o1 - 1);
+    iy = (e >> (depth + 1)) & (o1 - 1);
+    iz = e >> (2 * (depth + 1));
+}
+
+// contribution of D-level leaves [l0, l1) to node o's divergence
+__device__ __forceinline__ double div_terms(int l0, int l1, int step, int ox, int oy, int oz, int depth, int res,
+                                            int bD, const int* enc, const float* vx, const float* vy, const float* vz,
+                                            const double* dff) {
+    double acc = 0.0;
+    for (int l = l0; l < l1; l += step) {
+        int lx, ly, lz;
+        decode3(enc[bD + l], depth, lx, ly, lz);
+        float ux = (float)dff[(size_t)ox + (size_t)res * lx];
+        float uy = (float)dff[(size_t)oy + (size_t)res * ly];
+        float uz = (float)dff[(size_t)oz + (size_t)res * lz];
+        float t = vx[l] * ux;
+        t = fmaf(vy[l], uy, t);
+        t = fmaf(vz[l], uz, t);
+        acc += (double)t;
+    }
+    return acc;
+}
+
+// one warp per node for depths >= dsplit
+__global__ void __launch_bounds__(kBlock) k_div_fine(const Counters* c, int depth, int dsplit, int res,
+                                                     const int* enc, const int* didx, const int* dnum,
+                                                     const int* neigh, size_t stride, const float* vx,
+                                                     const float* vy, const float* vz, const double* dff,
+                                                     float* divg) {
+    const int b0 = c->level_base[dsplit];
+    const int M = c->n_nodes;
+    const int bD = c->level_base[depth];
+    const int lane = lane_id();
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int i = b0 + warp; i < M; i += nwarps) {
+        int ox, oy, oz;
+        decode3(enc[i], depth, ox, oy, oz);
+        double acc = 0.0;
+        for (int k = 0; k < 27; ++k) {
+            const int nb = neigh[(size_t)k * stride + i];
+            if (nb < 0) continue;
+            const int l0 = didx[nb];
+            acc += div_terms(l0 + lane, l0 + dnum[nb], 32, ox, oy, oz, depth, res, bD, enc, vx, vy, vz, dff);
+        }
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) divg[i] = (float)acc;
+    }
+}
+
+constexpr int kDivChunk = 512;
+
+// chunk count of every coarse node (depth < dsplit)
+struct DivChunkLoad {
+    const int* neigh;
+    size_t stride;
+    const int* dnum;
+    __device__ unsigned operator()(int i) const {
+        unsigned n = 0;
+        for (int k = 0; k < 27; ++k) {
+            int nb = neigh[(size_t)k * stride + i];
+            if (nb >= 0) n += (unsigned)((dnum[nb] + kDivChunk - 1) / kDivChunk);
+        }
+        return n;
+    }
+};
+
+__global__ void k_div_chunk_count(Counters* c, int dsplit, const unsigned* total, int cap, int* n_items) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        int n = (int)*total;
+        if (n > cap) { atomicOr(&c->error, kErrCapacity); n = 0; }
+        *n_items = n;
+    }
+}
+
+// one warp per chunk: partial sum of up to kDivChunk leaves of one neighbour of one node
+__global__ void __launch_bounds__(kBlock) k_div_chunks(const Counters* c, int depth, int dsplit, int res,
+                                                       const int* n_items_ptr, const unsigned* item_start,
+                                                       const int* enc, const int* didx, const int* dnum,
+                                                       const int* neigh, size_t stride, const float* vx,
+                                                       const float* vy, const float* vz, const double* dff,
+                                                       double* partial) {
+    const int n_nodes = c->level_base[dsplit];
+    const int n_items = *n_items_ptr;
+    const int bD = c->level_base[depth];
+    const int lane = lane_id();
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int it = warp; it < n_items; it += nwarps) {
+        // node owning this item: last node with item_start <= it
+        int lo = 0, hi = n_nodes - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if ((int)item_start[mid] <= it) lo = mid;
+            else hi = mid - 1;
+        }
+        const int i = lo;
+        int rem = it - (int)item_start[i];
+        int nb = -1, ch = 0;
+        for (int k = 0; k < 27; ++k) {
+            int q = neigh[(size_t)k * stride + i];
+            if (q < 0) continue;
+            int nc = (dnum[q] + kDivChunk - 1) / kDivChunk;
+            if (rem < nc) { nb = q; ch = rem; break; }
+            rem -= nc;
+        }
+        double acc = 0.0;
+        if (nb >= 0) {
+            int ox, oy, oz;
+            decode3(enc[i], depth, ox, oy, oz);
+            const int l0 = didx[nb] + ch * kDivChunk;
+            const int l1 = min(didx[nb] + dnum[nb], l0 + kDivChunk);
+            acc = div_terms(l0 + lane, l1, 32, ox, oy, oz, depth, res, bD, enc, vx, vy, vz, dff);
+        }
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) partial[it] = acc;
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_div_coarse_reduce(const Counters* c, int dsplit, const unsigned* item_start,
+                                                              const int* n_items_ptr, const double* partial,
+                                                              float* divg) {
+    const int n_nodes = c->level_base[dsplit];
+    const int n_items = *n_items_ptr;
+    PSR_GRID_STRIDE(i, n_nodes) {
+        int a = (int)item_start[i];
+        int b = (i + 1 < n_nodes) ? (int)item_start[i + 1] : n_items;
+        double s = 0.0;
+        for (int t = a; t < b; ++t) s += partial[t];
+        divg[i] = (float)s;
+    }
+}
+
+static inline int grid_for(const Workspace& ws, long long work) {
+    long long g = (work + kBlock - 1) / kBlock;
+    long long cap = (long long)ws.num_sms * 8;
+    if (g > cap) g = cap;
+    return (int)(g < 1 ? 1 : g);
+}
+
+cudaError_t field_build(Workspace& ws) {
+    cudaStream_t s = ws.stream;
+    const int D = ws.depth;
+    Counters* c = ws.cnt;
+    const size_t stride = (size_t)ws.cap.nodes;
+    float* vx = ws.vfield;
+    float* vy = ws.vfield + ws.cap.dnodes;
+    float* vz = ws.vfield + 2 * (size_t)ws.cap.dnodes;
+    k_vector_field<<<grid_for(ws, ws.cap.dnodes), kBlock, 0, s>>>(c, D, ws.px, ws.py, ws.pz, ws.nx, ws.ny, ws.nz,
+                                                                    ws.pidx, ws.pnum, ws.ctr_x, ws.ctr_y, ws.ctr_z,
+                                                                    ws.neigh, stride, vx, vy, vz);
+    const int dsplit = D >= 2 ? D - 2 : 0;
+    k_div_fine<<<ws.num_sms * 8, kBlock, 0, s>>>(c, D, dsplit, ws.res, ws.enc, ws.didx, ws.dnum, ws.neigh, stride, vx,
+                                                 vy, vz, ws.dff, ws.divg);
+    if (dsplit > 0) {
+        // item_start / n_items / partial live in the (otherwise idle) CG scratch
+        unsigned* item_start = (unsigned*)ws.cg_r;
+        int* n_items = (int*)&c->n_groups;
+        unsigned* total = (unsigned*)&c->scan_total;
+        cudaError_t e = launch_scan(DivChunkLoad{ws.neigh, stride, ws.dnum}, StoreExclusive{item_start},
+                                    &c->level_base[dsplit], 0, ws.scan, total, &c->error, s);
+        if (e != cudaSuccess) return e;
+        const int item_cap = ws.cap.nodes;   // partial buffer holds cap.nodes doubles
+        k_div_chunk_count<<<1, 1, 0, s>>>(c, dsplit, total, item_cap, n_items);
+        k_div_chunks<<<ws.num_sms * 8, kBlock, 0, s>>>(c, D, dsplit, ws.res, n_items, item_start, ws.enc, ws.didx,
+                                                       ws.dnum, ws.neigh, stride, vx, vy, vz, ws.dff, ws.cg_partial);
+        k_div_coarse_reduce<<<grid_for(ws, 1 << 16), kBlock, 0, s>>>(c, dsplit, item_start, n_items, ws.cg_partial,
+                                                                    ws.divg);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace psr

@@ -1,0 +1,1307 @@
+// Stage (d): vertex / edge / face arrays, marching cubes at the finest depth, subdivision
+// of coarser leaves that carry surface, and compaction of the output mesh.
+//
+// Reference: mesh/BuildMeshGeometry.cu:42-546 and mesh/ComputeTriangleIndices.cu:346-2194.
+// The reference processes each coarse subdivision root in its own host iteration and the
+// finer roots in one host iteration per depth, temporarily redirecting the parent's child
+// pointer to the subdivided copy.  Here every root group (one coarse root, or all finer
+// roots of one depth) owns a region of one subdivision-space array and an overlay of the
+// redirected child pointers that only its own lookups see, so all groups run in one
+// batched pass with the same results as the sequential reference.
+#include "workspace.h"
+#include "tables.cuh"
+
+PSR_DEFINE_CONST_TABLES(upload_tables_mesh)
+
+namespace psr {
+
+__device__ __forceinline__ float sqdist3(float ax, float ay, float az, float bx, float by, float bz) {
+    float dx = __fsub_rn(ax, bx), dy = __fsub_rn(ay, by), dz = __fsub_rn(az, bz);
+    return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+}
+
+// value behind a 1-based back-pointer; a missing pointer (0) flags the tree as malformed
+// and reads as +1 instead of touching memory outside the array
+__device__ __forceinline__ float ptr_value(const float* vals, int ptr1, unsigned* err) {
+    if (ptr1 <= 0) { atomicOr(err, kErrInvalid); return 1.0f; }
+    return vals[ptr1 - 1];
+}
+
+__device__ __forceinline__ void decode3m(int e, int depth, int& ix, int& iy, int& iz) {
+    const int o1 = 1 << (depth + 1);
+    ix = e & (o1 - 1);
+    iy = (e >> (depth + 1)) & (o1 - 1);
+    iz = e >> (2 * (depth + 1));
+}
+
+// vertex slot of a neighbour centre relative to a vertex (mesh/BuildMeshGeometry.cu:133-144)
+__device__ __forceinline__ int vertex_slot(float ncx, float ncy, float ncz, float vx, float vy, float vz) {
+    int idx = 0;
+    if (__fsub_rn(ncx, vx) < 0) idx |= 1;
+    if (__fsub_rn(ncz, vz) < 0) idx |= 4;
+    if (__fsub_rn(ncy, vy) < 0) idx += (idx & 1) ? 1 : 3;
+    return idx;
+}
+
+__device__ __forceinline__ void edge_center(float cx, float cy, float cz, int e, float hw, float out[3]) {
+    const int orient = e >> 2;
+    const int off[2] = {e & 1, (e & 2) >> 1};
+    const float c[3] = {cx, cy, cz};
+    int dim = 0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        int m = 0;
+        if (orient != a) { m = 2 * off[dim] - 1; dim++; }
+        out[a] = __fadd_rn(c[a], (float)m * hw);
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// octree vertex / edge / face records
+// ------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_mesh_reset(const Counters* c, int* node_vtx, int* node_edge,
+                                                       int* node_face, int* ov_group, int* ov_sub, size_t stride) {
+    const int M = c->n_nodes;
+    PSR_GRID_STRIDE(i, M) {
+        for (int k = 0; k < 8; ++k) node_vtx[(size_t)k * stride + i] = 0;
+        for (int k = 0; k < 12; ++k) node_edge[(size_t)k * stride + i] = 0;
+        for (int k = 0; k < 6; ++k) node_face[(size_t)k * stride + i] = 0;
+        for (int k = 0; k < 8; ++k) { ov_group[(size_t)k * stride + i] = -1; ov_sub[(size_t)k * stride + i] = -1; }
+    }
+}
+
+// vertex ownership (initVertexOwner, mesh/BuildMeshGeometry.cu:42-101)
+__global__ void __launch_bounds__(kBlock) k_vertex_owner(const Counters* c, const int* key, const int* ndepth,
+                                                         const float* cx, const float* cy, const float* cz,
+                                                         const int* neigh, size_t stride, unsigned char* vmask) {
+    const int M = c->n_nodes;
+    PSR_GRID_STRIDE(i, M) {
+        const int d = ndepth[i];
+        const float hw = 1.0f / (float)(1 << (d + 1)), w = 1.0f / (float)(1 << d), w2 = __fmul_rn(w, w);
+        const float ox = cx[i], oy = cy[i], oz = cz[i];
+        int okey[8], oidx[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) { okey[q] = 0x7fffffff; oidx[q] = -1; }
+        for (int k = 0; k < 27; ++k) {
+            const int nb = neigh[(size_t)k * stride + i];
+            if (nb == -1) continue;
+            const float nx = cx[nb], ny = cy[nb], nz = cz[nb];
+            const int nk = key[nb];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                float vx = __fadd_rn(ox, (float)(2 * (q & 1) - 1) * hw);
+                float vy = __fadd_rn(oy, (float)(2 * ((q >> 1) & 1) - 1) * hw);
+                float vz = __fadd_rn(oz, (float)(2 * ((q >> 2) & 1) - 1) * hw);
+                if (sqdist3(vx, vy, vz, nx, ny, nz) < w2 && okey[q] > nk) { okey[q] = nk; oidx[q] = nb; }
+            }
+        }
+        unsigned m = 0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) if (oidx[q] == i) m |= 1u << q;
+        vmask[i] = (unsigned char)m;
+    }
+}
+
+struct PopcLoad8 {
+    const unsigned char* m;
+    __device__ unsigned operator()(int i) const { return __popc((unsigned)m[i]); }
+};
+
+struct VertexStore {
+    const unsigned char* vmask;
+    const int* ndepth;
+    const float *cx, *cy, *cz;
+    float *vx, *vy, *vz;
+    int *vowner, *vkind, *vdepth;
+    int cap;
+    unsigned* err;
+    __device__ void operator()(int i, unsigned pre, unsigned cnt) const {
+        if (!cnt) return;
+        if ((int)(pre + cnt) > cap) { atomicOr(err, kErrCapacity); return; }
+        const unsigned m = vmask[i];
+        const int d = ndepth[i];
+        const float hw = 1.0f / (float)(1 << (d + 1));
+        int o = (int)pre;
+        for (int q = 0; q < 8; ++q) {
+            if (!((m >> q) & 1)) continue;
+            vx[o] = __fadd_rn(cx[i], (float)(2 * (q & 1) - 1) * hw);
+            vy[o] = __fadd_rn(cy[i], (float)(2 * ((q >> 1) & 1) - 1) * hw);
+            vz[o] = __fadd_rn(cz[i], (float)(2 * ((q >> 2) & 1) - 1) * hw);
+            vowner[o] = i;
+            vkind[o] = q;
+            vdepth[o] = d;
+            ++o;
+        }
+    }
+};
+
+__global__ void k_set_count(int* dst, const unsigned* total, int cap, unsigned* err) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        int n = (int)*total;
+        if (n > cap) { atomicOr(err, kErrCapacity); n = cap; }
+        *dst = n;
+    }
+}
+
+// maintainVertexNodePointer (mesh/BuildMeshGeometry.cu:108-147)
+__global__ void __launch_bounds__(kBlock) k_vertex_maintain(const Counters* c, const int* ndepth, const float* cx,
+                                                            const float* cy, const float* cz, const int* neigh,
+                                                            size_t stride, const float* vx, const float* vy,
+                                                            const float* vz, const int* vowner, int* node_vtx) {
+    const int V = c->n_vertices;
+    PSR_GRID_STRIDE(v, V) {
+        const int ow = vowner[v];
+        const int d = ndepth[ow];
+        const float w = 1.0f / (float)(1 << d), w2 = __fmul_rn(w, w);
+        const float px = vx[v], py = vy[v], pz = vz[v];
+        for (int k = 0; k < 27; ++k) {
+            const int nb = neigh[(size_t)k * stride + ow];
+            if (nb == -1) continue;
+            const float nx = cx[nb], ny = cy[nb], nz = cz[nb];
+            if (sqdist3(px, py, pz, nx, ny, nz) < w2)
+                node_vtx[(size_t)vertex_slot(nx, ny, nz, px, py, pz) * stride + nb] = v + 1;
+        }
+    }
+}
+
+// edge ownership for D-level nodes (initEdgeArray, mesh/BuildMeshGeometry.cu:149-220)
+__global__ void __launch_bounds__(kBlock) k_edge_owner(const Counters* c, int depth, const int* key, const float* cx,
+                                                       const float* cy, const float* cz, const int* neigh,
+                                                       size_t stride, unsigned short* emask) {
+    const int md = c->level_count[depth];
+    const int b = c->level_base[depth];
+    const float hw = 1.0f / (float)(1 << (depth + 1)), w = 1.0f / (float)(1 << depth), w2 = __fmul_rn(w, w);
+    PSR_GRID_STRIDE(o, md) {
+        const int i = b + o;
+        float ec[12][3];
+#pragma unroll
+        for (int e = 0; e < 12; ++e) edge_center(cx[i], cy[i], cz[i], e, hw, ec[e]);
+        int okey[12], oidx[12];
+#pragma unroll
+        for (int e = 0; e < 12; ++e) { okey[e] = 0x7fffffff; oidx[e] = -1; }
+        for (int k = 0; k < 27; ++k) {
+            const int nb = neigh[(size_t)k * stride + i];
+            if (nb == -1) continue;
+            const float nx = cx[nb], ny = cy[nb], nz = cz[nb];
+            const int nk = key[nb];
+#pragma unroll
+            for (int e = 0; e < 12; ++e)
+                if (sqdist3(ec[e][0], ec[e][1], ec[e][2], nx, ny, nz) < w2 && okey[e] > nk) { okey[e] = nk; oidx[e] = nb; }
+        }
+        unsigned m = 0;
+#pragma unroll
+        for (int e = 0; e < 12; ++e) if (oidx[e] == i) m |= 1u << e;
+        emask[o] = (unsigned short)m;
+    }
+}
+
+struct PopcLoad16 {
+    const unsigned short* m;
+    __device__ unsigned operator()(int i) const { return __popc((unsigned)m[i]); }
+};
+
+struct EdgeStore {
+    const unsigned short* emask;
+    const int* base_ptr;   // first D-level node
+    int *eowner, *ekind;
+    int cap;
+    unsigned* err;
+    __device__ void operator()(int o, unsigned pre, unsigned cnt) const {
+        if (!cnt) return;
+        if ((int)(pre + cnt) > cap) { atomicOr(err, kErrCapacity); return; }
+        const unsigned m = emask[o];
+        const int i = *base_ptr + o;
+        int q = (int)pre;
+        for (int e = 0; e < 12; ++e)
+            if ((m >> e) & 1) { eowner[q] = i; ekind[q] = e; ++q; }
+    }
+};
+
+// maintainEdgeNodePointer (mesh/BuildMeshGeometry.cu:222-280)
+__global__ void __launch_bounds__(kBlock) k_edge_maintain(const Counters* c, int depth, const float* cx, const float* cy,
+                                                          const float* cz, const int* neigh, size_t stride,
+                                                          const int* eowner, const int* ekind, int* node_edge) {
+    const int E = c->n_edges;
+    const float hw = 1.0f / (float)(1 << (depth + 1)), w = 1.0f / (float)(1 << depth), w2 = __fmul_rn(w, w);
+    PSR_GRID_STRIDE(ei, E) {
+        const int ow = eowner[ei], kind = ekind[ei];
+        float ec[3];
+        edge_center(cx[ow], cy[ow], cz[ow], kind, hw, ec);
+        const int orient = kind >> 2;
+        for (int k = 0; k < 27; ++k) {
+            const int nb = neigh[(size_t)k * stride + ow];
+            if (nb == -1) continue;
+            const float nc[3] = {cx[nb], cy[nb], cz[nb]};
+            if (sqdist3(ec[0], ec[1], ec[2], nc[0], nc[1], nc[2]) < w2) {
+                int idx = orient << 2, dim = 0;
+                for (int a = 0; a < 3; ++a)
+                    if (orient != a) { if (__fsub_rn(nc[a], ec[a]) < 0) idx |= (1 << dim); dim++; }
+                node_edge[(size_t)idx * stride + nb] = ei + 1;
+            }
+        }
+    }
+}
+
+// face ownership (initFaceArray, mesh/BuildMeshGeometry.cu:282-354)
+__global__ void __launch_bounds__(kBlock) k_face_owner(const Counters* c, const int* key, const int* ndepth,
+                                                       const float* cx, const float* cy, const float* cz,
+                                                       const int* neigh, size_t stride, unsigned char* fmask) {
+    const int M = c->n_nodes;
+    PSR_GRID_STRIDE(i, M) {
+        const int d = ndepth[i];
+        const float hw = 1.0f / (float)(1 << (d + 1)), w = 1.0f / (float)(1 << d), w2 = __fmul_rn(w, w);
+        float fc[6][3];
+#pragma unroll
+        for (int f = 0; f < 6; ++f) {
+            fc[f][0] = cx[i]; fc[f][1] = cy[i]; fc[f][2] = cz[i];
+            fc[f][f >> 1] = __fadd_rn(fc[f][f >> 1], (float)(2 * (f & 1) - 1) * hw);
+        }
+        int okey[6], oidx[6];
+#pragma unroll
+        for (int f = 0; f < 6; ++f) { okey[f] = 0x7fffffff; oidx[f] = -1; }
+        for (int k = 0; k < 27; ++k) {
+            const int nb = neigh[(size_t)k * stride + i];
+            if (nb == -1) continue;
+            const float nx = cx[nb], ny = cy[nb], nz = cz[nb];
+            const int nk = key[nb];
+#pragma unroll
+            for (int f = 0; f < 6; ++f)
+                if (sqdist3(fc[f][0], fc[f][1], fc[f][2], nx, ny, nz) < w2 && okey[f] > nk) { okey[f] = nk; oidx[f] = nb; }
+        }
+        unsigned m = 0;
+#pragma unroll
+        for (int f = 0; f < 6; ++f) if (oidx[f] == i) m |= 1u << f;
+        fmask[i] = (unsigned char)m;
+    }
+}
+
+struct FaceStore {
+    const unsigned char* fmask;
+    const int* key;
+    const int* ndepth;
+    const int* parent;
+    int depth;
+    int *fowner, *fkind, *fhas;
+    int cap;
+    unsigned* err;
+    __device__ void operator()(int i, unsigned pre, unsigned cnt) const {
+        if (!cnt) return;
+        if ((int)(pre + cnt) > cap) { atomicOr(err, kErrCapacity); return; }
+        const unsigned m = fmask[i];
+        const int d = ndepth[i];
+        const int son = (key[i] >> (3 * (depth - d))) & 7;
+        int q = (int)pre;
+        for (int f = 0; f < 6; ++f) {
+            if (!((m >> f) & 1)) continue;
+            fowner[q] = i;
+            fkind[q] = f;
+            fhas[q] = (parent[i] == -1) ? -1 : ((c_tab.parent_face_kind[son][f] != -1) ? 1 : -1);
+            ++q;
+        }
+    }
+};
+
+// maintainFaceNodePointer (mesh/BuildMeshGeometry.cu:356-400)
+__global__ void __launch_bounds__(kBlock) k_face_maintain(const Counters* c, const int* ndepth, const float* cx,
+                                                          const float* cy, const float* cz, const int* neigh,
+                                                          size_t stride, const int* fowner, const int* fkind,
+                                                          int* node_face) {
+    const int F = c->n_faces;
+    PSR_GRID_STRIDE(fi, F) {
+        const int ow = fowner[fi], kind = fkind[fi];
+        const int d = ndepth[ow];
+        const float hw = 1.0f / (float)(1 << (d + 1)), w = 1.0f / (float)(1 << d), w2 = __fmul_rn(w, w);
+        float fc[3] = {cx[ow], cy[ow], cz[ow]};
+        const int orient = kind >> 1;
+        fc[orient] = __fadd_rn(fc[orient], (float)(2 * (kind & 1) - 1) * hw);
+        for (int k = 0; k < 27; ++k) {
+            const int nb = neigh[(size_t)k * stride + ow];
+            if (nb == -1) continue;
+            const float nc[3] = {cx[nb], cy[nb], cz[nb]};
+            if (sqdist3(fc[0], fc[1], fc[2], nc[0], nc[1], nc[2]) < w2) {
+                int idx = orient << 1;
+                if (__fsub_rn(nc[orient], fc[orient]) < 0) idx++;
+                node_face[(size_t)idx * stride + nb] = fi + 1;
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// implicit values at the octree vertices (mesh/ComputeTriangleIndices.cu:346-399)
+// ------------------------------------------------------------------------------------
+__device__ __forceinline__ float node_terms(int node, float val, float qx, float qy, float qz, int depth,
+                                            const int* neigh, size_t stride, const int* enc, const float* x) {
+    for (int k = 0; k < 27; ++k) {
+        int nb = neigh[(size_t)k * stride + node];
+        if (nb == -1) continue;
+        int ix, iy, iz;
+        decode3m(enc[nb], depth, ix, iy, iz);
+        float t = __fmul_rn(x[nb], basis32(ix, qx));
+        t = __fmul_rn(t, basis32(iy, qy));
+        t = __fmul_rn(t, basis32(iz, qz));
+        val = __fadd_rn(val, t);
+    }
+    return val;
+}
+
+__global__ void __launch_bounds__(kBlock) k_vertex_values(const Counters* c, int depth, const float* vx,
+                                                          const float* vy, const float* vz, const int* vowner,
+                                                          const int* vkind, const int* vdepth, const int* neigh,
+                                                          size_t stride, const int* parent, const int* first_child,
+                                                          const int* enc, const float* x, float* vvalue) {
+    const int V = c->n_vertices;
+    const float iso = c->iso;
+    PSR_GRID_STRIDE(v, V) {
+        float val = 0.0f;
+        const int ow = vowner[v];
+        if (ow > 0) {
+            const float qx = vx[v], qy = vy[v], qz = vz[v];
+            int node = ow;
+            while (node != -1) {
+                val = node_terms(node, val, qx, qy, qz, depth, neigh, stride, enc, x);
+                node = parent[node];
+            }
+            node = ow;
+            int d = vdepth[v];
+            const int ec = c_tab.children_vertex_kind[vkind[v]];
+            while (d < depth) {
+                d++;
+                const int fc = first_child[node];
+                node = (fc == -1) ? -1 : fc + ec;
+                if (node == -1) break;
+                val = node_terms(node, val, qx, qy, qz, depth, neigh, stride, enc, x);
+            }
+        }
+        vvalue[v] = __fsub_rn(val, iso);
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// marching cubes at depth D (mesh/ComputeTriangleIndices.cu:401-526)
+// ------------------------------------------------------------------------------------
+__device__ __forceinline__ void interp_point(float p1x, float p1y, float p1z, float p2x, float p2y, float p2z, int dim,
+                                             float v1, float v2, float* out) {
+    out[0] = p1x; out[1] = p1y; out[2] = p1z;
+    const float p1[3] = {p1x, p1y, p1z}, p2[3] = {p2x, p2y, p2z};
+    float pivot = __fdiv_rn(v1, __fsub_rn(v1, v2));
+    float other = __fsub_rn(1.0f, pivot);
+    out[dim] = __fadd_rn(__fmul_rn(p2[dim], pivot), __fmul_rn(p1[dim], other));
+}
+
+struct CrossLoad {
+    const int* eowner;
+    const int* ekind;
+    const int* node_vtx;
+    size_t stride;
+    const float* vvalue;
+    unsigned* err;
+    __device__ unsigned operator()(int e) const {
+        const int ow = eowner[e], kind = ekind[e];
+        const float a = ptr_value(vvalue, node_vtx[(size_t)c_tab.edge_vertex[kind][0] * stride + ow], err);
+        const float b = ptr_value(vvalue, node_vtx[(size_t)c_tab.edge_vertex[kind][1] * stride + ow], err);
+        return (__fmul_rn(a, b) <= 0.0f) ? 1u : 0u;
+    }
+};
+
+struct CrossStore {
+    const int* eowner;
+    const int* ekind;
+    const int* node_vtx;
+    size_t stride;
+    const float* vvalue;
+    const float *vx, *vy, *vz;
+    unsigned* ecross;   // per edge: staged vertex index (valid when the edge crosses)
+    float* part_v;      // staged vertices (3 floats each)
+    int voff;
+    int cap;
+    unsigned* err;
+    __device__ void operator()(int e, unsigned pre, unsigned flag) const {
+        ecross[e] = pre;
+        if (!flag) return;
+        const int at = voff + (int)pre;
+        if (at >= cap) { atomicOr(err, kErrCapacity); return; }
+        const int ow = eowner[e], kind = ekind[e];
+        const int v1 = node_vtx[(size_t)c_tab.edge_vertex[kind][0] * stride + ow] - 1;
+        const int v2 = node_vtx[(size_t)c_tab.edge_vertex[kind][1] * stride + ow] - 1;
+        if (v1 < 0 || v2 < 0) return;   // only reachable for a malformed tree (flagged in the load)
+        interp_point(vx[v1], vy[v1], vz[v1], vx[v2], vy[v2], vz[v2], kind >> 2, vvalue[v1], vvalue[v2],
+                     &part_v[3 * (size_t)at]);
+    }
+};
+
+struct CubeLoad {
+    const int* node_vtx;
+    size_t stride;
+    const int* base_ptr;
+    const float* vvalue;
+    int* cube_class;
+    unsigned* err;
+    __device__ unsigned operator()(int o) const {
+        const int i = *base_ptr + o;
+        int cls = 0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+            if (ptr_value(vvalue, node_vtx[(size_t)q * stride + i], err) < 0.0f) cls |= 1 << q;
+        cube_class[o] = cls;
+        return (unsigned)c_tab.mc_count[cls];
+    }
+};
+
+// emits the triangles of a D-level cube and marks surface-edge intersections on faces,
+// propagating them to the parent faces (generateTrianglePos, :476-526)
+struct CubeStore {
+    const int* cube_class;
+    const int* base_ptr;
+    const int* node_edge;
+    const int* node_face;
+    size_t stride;
+    const unsigned* ecross;
+    const int* parent;
+    const int* fhas;
+    int* face_hit;
+    int* part_t;
+    int toff;
+    int cap;
+    unsigned* err;
+    __device__ void operator()(int o, unsigned pre, unsigned cnt) const {
+        if (!cnt) return;
+        const int i = *base_ptr + o;
+        const int cls = cube_class[o];
+        const unsigned long long tri = c_tab.mc_tri[cls];
+        unsigned used = 0;
+        for (int t = 0; t < (int)cnt; ++t) {
+            const int at = toff + (int)pre + t;
+            for (int a = 0; a < 3; ++a) {
+                const int e = (int)((tri >> (4 * (3 * t + a))) & 0xF);
+                used |= 1u << e;
+                const int ei = node_edge[(size_t)e * stride + i] - 1;
+                if (at < cap) part_t[3 * (size_t)at + a] = (ei >= 0) ? (int)ecross[ei] : -1;
+            }
+            if (at >= cap) atomicOr(err, kErrCapacity);
+        }
+        for (int f = 0; f < 6; ++f) {
+            unsigned mark = 0;
+            for (int j = 0; j < 4; ++j) mark |= (used >> c_tab.face_edges[f][j]) & 1u;
+            if (!mark) continue;
+            int pn = parent[i];
+            int cf = node_face[(size_t)f * stride + i] - 1;
+            if (cf < 0) continue;
+            face_hit[cf] = 1;
+            int guard = 0;
+            while (fhas[cf] != -1 && pn >= 0 && guard++ < 32) {
+                cf = node_face[(size_t)f * stride + pn] - 1;
+                if (cf < 0) break;
+                pn = parent[pn];
+                face_hit[cf] = 1;
+            }
+        }
+    }
+};
+
+// ------------------------------------------------------------------------------------
+// subdivision roots (ProcessLeafNodesAtOtherDepth :555-587, selection :1284-1346)
+// ------------------------------------------------------------------------------------
+struct RootLoad {
+    const int* node_vtx;
+    const int* node_face;
+    size_t stride;
+    const float* vvalue;
+    const int* face_hit;
+    const int* first_child;
+    unsigned* err;
+    __device__ unsigned operator()(int i) const {
+        const float v0 = ptr_value(vvalue, node_vtx[i], err);
+        const float s = (v0 < 0.0f) ? -1.0f : 1.0f;
+        int ht = 0;
+        for (int q = 1; q < 8; ++q)
+            if (__fmul_rn(s, ptr_value(vvalue, node_vtx[(size_t)q * stride + i], err)) < 0.0f) { ht = 1; break; }
+        int hi = 0;
+        for (int f = 0; f < 6; ++f) {
+            const int fp = node_face[(size_t)f * stride + i] - 1;
+            if (fp >= 0 && face_hit[fp]) { hi = 1; break; }
+        }
+        return (first_child[i] == -1 && (ht || hi)) ? 1u : 0u;
+    }
+};
+struct RootStore {
+    int* sub_root;
+    int cap;
+    unsigned* err;
+    __device__ void operator()(int i, unsigned pre, unsigned f) const {
+        if (!f) return;
+        if ((int)pre >= cap) { atomicOr(err, kErrCapacity); return; }
+        sub_root[pre] = i;
+    }
+};
+
+// Group table (one thread).  Group record (ints): 0 root depth, 1 first root, 2 root count,
+// 3 node offset, 4 node count, 5 D-level node offset (in the D-level sub numbering),
+// 6 D-level node count.
+constexpr int kGroupRec = 8;
+
+__global__ void k_build_groups(Counters* c, int depth, const int* sub_root, const int* ndepth, const int* key,
+                               const int* parent, int* sub_root_depth, int* groups, int max_groups, int node_cap,
+                               int dnode_cap, int* node_subgroup, int* node_subslot, int* ov_group, int* ov_sub,
+                               size_t stride) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int R = c->n_subroots;
+    const int finer = depth - 4;
+    int ng = 0;
+    long long noff = 0, doff = 0;
+    int r = 0;
+    bool overflow = false;
+    while (r < R) {
+        const int rd = ndepth[sub_root[r]];
+        int n = 1;
+        if (rd >= finer) {
+            while (r + n < R && ndepth[sub_root[r + n]] == rd) ++n;
+        }
+        long long per = 0, dper = 1;
+        for (int d = rd; d <= depth; ++d) { per += dper; if (d < depth) dper *= 8; }
+        if (ng >= max_groups || noff + per * n > node_cap || doff + dper * n > dnode_cap) { overflow = true; break; }
+        int* g = groups + (size_t)ng * kGroupRec;
+        g[0] = rd; g[1] = r; g[2] = n; g[3] = (int)noff; g[4] = (int)(per * n); g[5] = (int)doff; g[6] = (int)(dper * n);
+        g[7] = 0;
+        for (int q = 0; q < n; ++q) {
+            const int node = sub_root[r + q];
+            sub_root_depth[r + q] = rd;
+            node_subgroup[node] = ng;
+            node_subslot[node] = q;
+            const int son = (key[node] >> (3 * (depth - rd))) & 7;
+            const int pa = parent[node];
+            if (pa >= 0) {
+                ov_group[(size_t)son * stride + pa] = ng;
+                ov_sub[(size_t)son * stride + pa] = q;
+            }
+        }
+        noff += per * n;
+        doff += dper * n;
+        ++ng;
+        r += n;
+    }
+    if (overflow) atomicOr(&c->error, kErrCapacity);
+    c->n_sub_nodes = overflow ? 0 : (int)noff;
+    c->n_sub_dnodes = overflow ? 0 : (int)doff;
+    c->n_groups = overflow ? 0 : ng;
+}
+
+// subdivision node geometry (singleRebuildArray :599-635 / wholeRebuildArray :1110-1168)
+__device__ __forceinline__ int find_group(const int* groups, int ng, int field, int v) {
+    int lo = 0, hi = ng - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (groups[(size_t)mid * kGroupRec + field] <= v) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// local index inside a group -> (depth, root slot q, rel)
+__device__ __forceinline__ void sub_locate(int local, int rd, int n, int depth, int& d, int& q, int& rel) {
+    int off = 0, cnt = n;
+    d = rd;
+    while (d < depth && local >= off + cnt) { off += cnt; cnt *= 8; ++d; }
+    const int per = cnt / n;
+    q = (local - off) / per;
+    rel = (local - off) - q * per;
+}
+__device__ __forceinline__ int sub_level_off(int rd, int n, int d) {
+    int off = 0, cnt = n;
+    for (int e = rd; e < d; ++e) { off += cnt; cnt *= 8; }
+    return off;
+}
+
+__global__ void __launch_bounds__(kBlock) k_sub_build(const Counters* c, int depth, const int* groups,
+                                                      const int* sub_root, const int* key, const int* parent,
+                                                      const int* neigh, size_t stride, int* s_key, int* s_parent,
+                                                      int* s_first_child, int* s_depth, int* s_group, int* s_root,
+                                                      float* s_cx, float* s_cy, float* s_cz, int na) {
+    const int S = c->n_sub_nodes;
+    const int ng = c->n_groups;
+    PSR_GRID_STRIDE(s, S) {
+        const int g = find_group(groups, ng, 3, s);
+        const int* G = groups + (size_t)g * kGroupRec;
+        const int rd = G[0], n = G[2], goff = G[3];
+        const int local = s - goff;
+        int d, q, rel;
+        sub_locate(local, rd, n, depth, d, q, rel);
+        const int root_node = sub_root[G[1] + q];
+        const int k = key[root_node] | (rel << (3 * (depth - d)));
+        s_key[s] = k;
+        s_depth[s] = d;
+        s_group[s] = g;
+        // root: the octree node it replaces (its neighs[13] in the reference)
+        int self = neigh[(size_t)13 * stride + root_node];
+        if (self == -1) self = root_node;
+        s_root[s] = (d == rd) ? self : -1;
+        if (d == rd) s_parent[s] = parent[root_node];
+        else s_parent[s] = na + goff + sub_level_off(rd, n, d - 1) + q * (1 << (3 * (d - 1 - rd))) + (rel >> 3);
+        s_first_child[s] = (d < depth) ? na + goff + sub_level_off(rd, n, d + 1) + q * (1 << (3 * (d + 1 - rd))) + (rel << 3)
+                                       : -1;
+        float cc[3] = {0.5f, 0.5f, 0.5f};
+        float w = 0.25f;
+        for (int l = depth - 1; l >= depth - d; --l) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                if ((k >> (3 * l + 2 - a)) & 1) cc[a] = __fadd_rn(cc[a], w);
+                else cc[a] = __fsub_rn(cc[a], w);
+            }
+            w = __fdiv_rn(w, 2.0f);
+        }
+        s_cx[s] = cc[0];
+        s_cy[s] = cc[1];
+        s_cz[s] = cc[2];
+    }
+}
+
+// computeRebuildNeighbor (:669-696) for all subdivision nodes at depth d
+__global__ void __launch_bounds__(kBlock) k_sub_neighbours(const Counters* c, int d, int depth, const int* groups,
+                                                           const int* neigh, size_t stride, const int* first_child,
+                                                           const int* ov_group, const int* ov_sub, const int* s_key,
+                                                           const int* s_parent, const int* s_first_child,
+                                                           const int* s_depth, const int* s_group, int* s_neigh,
+                                                           size_t sstride, int na) {
+    const int S = c->n_sub_nodes;
+    PSR_GRID_STRIDE(s, S) {
+        if (s_depth[s] != d) continue;
+        const int g = s_group[s];
+        const int* G = groups + (size_t)g * kGroupRec;
+        const int son = (s_key[s] >> (3 * (depth - d))) & 7;
+        const int pa = s_parent[s];
+        for (int k = 0; k < 27; ++k) {
+            const int lp = c_tab.lut_parent[son][k];
+            const int np = (pa < na) ? neigh[(size_t)lp * stride + pa] : s_neigh[(size_t)lp * sstride + (pa - na)];
+            int v = -1;
+            if (np != -1) {
+                const int lc = c_tab.lut_child[son][k];
+                if (np < na) {
+                    if (ov_group[(size_t)lc * stride + np] == g) {
+                        // redirected child pointer of this group's root
+                        v = na + G[3] + ov_sub[(size_t)lc * stride + np];
+                    } else {
+                        const int fc = first_child[np];
+                        v = (fc == -1) ? -1 : fc + lc;
+                    }
+                } else {
+                    const int fc = s_first_child[np - na];
+                    v = (fc == -1) ? -1 : fc + lc;
+                }
+            }
+            s_neigh[(size_t)k * sstride + s] = v;
+        }
+    }
+}
+
+__device__ __forceinline__ void sub_center(int nb, int na, const float* cx, const float* cy, const float* cz,
+                                           const float* s_cx, const float* s_cy, const float* s_cz, float& x, float& y,
+                                           float& z) {
+    if (nb < na) { x = cx[nb]; y = cy[nb]; z = cz[nb]; }
+    else { x = s_cx[nb - na]; y = s_cy[nb - na]; z = s_cz[nb - na]; }
+}
+
+// D-level subdivision node o (0..n_sub_dnodes) -> subdivision node index
+__device__ __forceinline__ int sub_dnode_to_node(int o, const int* groups, int ng, int depth) {
+    const int g = find_group(groups, ng, 5, o);
+    const int* G = groups + (size_t)g * kGroupRec;
+    return G[3] + sub_level_off(G[0], G[2], depth) + (o - G[5]);
+}
+
+// vertex ownership among subdivision nodes only (initSubdivideVertexOwner :698-763)
+__global__ void __launch_bounds__(kBlock) k_sub_vertex_owner(const Counters* c, int depth, const int* groups,
+                                                             const int* s_key, const int* s_neigh, size_t sstride,
+                                                             const float* s_cx, const float* s_cy, const float* s_cz,
+                                                             unsigned char* s_vmask, int na) {
+    const int SD = c->n_sub_dnodes;
+    const int ng = c->n_groups;
+    const float hw = 1.0f / (float)(1 << (depth + 1)), w = 1.0f / (float)(1 << depth), w2 = __fmul_rn(w, w);
+    PSR_GRID_STRIDE(o, SD) {
+        const int s = sub_dnode_to_node(o, groups, ng, depth);
+        const float ox = s_cx[s], oy = s_cy[s], oz = s_cz[s];
+        int okey[8], oidx[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) { okey[q] = 0x7fffffff; oidx[q] = -1; }
+        for (int k = 0; k < 27; ++k) {
+            const int nb = s_neigh[(size_t)k * sstride + s];
+            if (nb < na) continue;
+            const float nx = s_cx[nb - na], ny = s_cy[nb - na], nz = s_cz[nb - na];
+            const int nk = s_key[nb - na];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                float vx = __fadd_rn(ox, (float)(2 * (q & 1) - 1) * hw);
+                float vy = __fadd_rn(oy, (float)(2 * ((q >> 1) & 1) - 1) * hw);
+                float vz = __fadd_rn(oz, (float)(2 * ((q >> 2) & 1) - 1) * hw);
+                if (sqdist3(vx, vy, vz, nx, ny, nz) < w2 && okey[q] > nk) { okey[q] = nk; oidx[q] = nb; }
+            }
+        }
+        unsigned m = 0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) if (oidx[q] == na + s) m |= 1u << q;
+        s_vmask[o] = (unsigned char)m;
+    }
+}
+
+struct SubVertexStore {
+    const unsigned char* vmask;
+    const int* groups;
+    const int* ng_ptr;
+    int depth;
+    const float *s_cx, *s_cy, *s_cz;
+    float *vx, *vy, *vz;
+    int *vowner, *vkind;
+    int cap;
+    int na;
+    unsigned* err;
+    __device__ void operator()(int o, unsigned pre, unsigned cnt) const {
+        if (!cnt) return;
+        if ((int)(pre + cnt) > cap) { atomicOr(err, kErrCapacity); return; }
+        const int s = sub_dnode_to_node(o, groups, *ng_ptr, depth);
+        const unsigned m = vmask[o];
+        const float hw = 1.0f / (float)(1 << (depth + 1));
+        int q = (int)pre;
+        for (int k = 0; k < 8; ++k) {
+            if (!((m >> k) & 1)) continue;
+            vx[q] = __fadd_rn(s_cx[s], (float)(2 * (k & 1) - 1) * hw);
+            vy[q] = __fadd_rn(s_cy[s], (float)(2 * ((k >> 1) & 1) - 1) * hw);
+            vz[q] = __fadd_rn(s_cz[s], (float)(2 * ((k >> 2) & 1) - 1) * hw);
+            vowner[q] = na + s;
+            vkind[q] = k;
+            ++q;
+        }
+    }
+};
+
+// D-level subdivision node index of subdivision node s (s must be at depth D)
+__device__ __forceinline__ int sub_node_to_dnode(int s, const int* groups, int ng, int depth) {
+    const int g = find_group(groups, ng, 3, s);
+    const int* G = groups + (size_t)g * kGroupRec;
+    return G[5] + (s - G[3] - sub_level_off(G[0], G[2], depth));
+}
+
+// maintainSubdivideVertexNodePointer (:765-810): s_vtx indexed by D-level sub node
+__global__ void __launch_bounds__(kBlock) k_sub_vertex_maintain(const Counters* c, int depth, const int* groups,
+                                                                const float* cx, const float* cy, const float* cz,
+                                                                const int* s_neigh, size_t sstride,
+                                                                const float* s_cx, const float* s_cy,
+                                                                const float* s_cz, const int* s_depth,
+                                                                const float* vx, const float* vy, const float* vz,
+                                                                const int* vowner, int* s_vtx, size_t dstride, int na) {
+    const int V = c->n_sub_vertices;
+    const int ng = c->n_groups;
+    const float w = 1.0f / (float)(1 << depth), w2 = __fmul_rn(w, w);
+    PSR_GRID_STRIDE(v, V) {
+        const int ow = vowner[v] - na;
+        const float px = vx[v], py = vy[v], pz = vz[v];
+        for (int k = 0; k < 27; ++k) {
+            const int nb = s_neigh[(size_t)k * sstride + ow];
+            if (nb == -1) continue;
+            float nx, ny, nz;
+            sub_center(nb, na, cx, cy, cz, s_cx, s_cy, s_cz, nx, ny, nz);
+            if (sqdist3(px, py, pz, nx, ny, nz) < w2 && nb >= na && s_depth[nb - na] == depth) {
+                const int dn = sub_node_to_dnode(nb - na, groups, ng, depth);
+                s_vtx[(size_t)vertex_slot(nx, ny, nz, px, py, pz) * dstride + dn] = v + 1;
+            }
+        }
+    }
+}
+
+// edge ownership among subdivision nodes only (initSubdivideEdgeArray :812-886)
+__global__ void __launch_bounds__(kBlock) k_sub_edge_owner(const Counters* c, int depth, const int* groups,
+                                                           const int* s_key, const int* s_neigh, size_t sstride,
+                                                           const float* s_cx, const float* s_cy, const float* s_cz,
+                                                           unsigned short* s_emask, int na) {
+    const int SD = c->n_sub_dnodes;
+    const int ng = c->n_groups;
+    const float hw = 1.0f / (float)(1 << (depth + 1)), w = 1.0f / (float)(1 << depth), w2 = __fmul_rn(w, w);
+    PSR_GRID_STRIDE(o, SD) {
+        const int s = sub_dnode_to_node(o, groups, ng, depth);
+        float ec[12][3];
+#pragma unroll
+        for (int e = 0; e < 12; ++e) edge_center(s_cx[s], s_cy[s], s_cz[s], e, hw, ec[e]);
+        int okey[12], oidx[12];
+#pragma unroll
+        for (int e = 0; e < 12; ++e) { okey[e] = 0x7fffffff; oidx[e] = -1; }
+        for (int k = 0; k < 27; ++k) {
+            const int nb = s_neigh[(size_t)k * sstride + s];
+            if (nb < na) continue;
+            const float nx = s_cx[nb - na], ny = s_cy[nb - na], nz = s_cz[nb - na];
+            const int nk = s_key[nb - na];
+#pragma unroll
+            for (int e = 0; e < 12; ++e)
+                if (sqdist3(ec[e][0], ec[e][1], ec[e][2], nx, ny, nz) < w2 && okey[e] > nk) { okey[e] = nk; oidx[e] = nb; }
+        }
+        unsigned m = 0;
+#pragma unroll
+        for (int e = 0; e < 12; ++e) if (oidx[e] == na + s) m |= 1u << e;
+        s_emask[o] = (unsigned short)m;
+    }
+}
+
+struct SubEdgeStore {
+    const unsigned short* emask;
+    const int* groups;
+    const int* ng_ptr;
+    int depth;
+    int *eowner, *ekind;
+    int cap;
+    int na;
+    unsigned* err;
+    __device__ void operator()(int o, unsigned pre, unsigned cnt) const {
+        if (!cnt) return;
+        if ((int)(pre + cnt) > cap) { atomicOr(err, kErrCapacity); return; }
+        const int s = sub_dnode_to_node(o, groups, *ng_ptr, depth);
+        const unsigned m = emask[o];
+        int q = (int)pre;
+        for (int e = 0; e < 12; ++e)
+            if ((m >> e) & 1) { eowner[q] = na + s; ekind[q] = e; ++q; }
+    }
+};
+
+// maintainSubdivideEdgeNodePointer (:888-949)
+__global__ void __launch_bounds__(kBlock) k_sub_edge_maintain(const Counters* c, int depth, const int* groups,
+                                                              const float* cx, const float* cy, const float* cz,
+                                                              const int* s_neigh, size_t sstride, const float* s_cx,
+                                                              const float* s_cy, const float* s_cz,
+                                                              const int* s_depth, const int* eowner,
+                                                              const int* ekind, int* s_edge, size_t dstride, int na) {
+    const int E = c->n_sub_edges;
+    const int ng = c->n_groups;
+    const float hw = 1.0f / (float)(1 << (depth + 1)), w = 1.0f / (float)(1 << depth), w2 = __fmul_rn(w, w);
+    PSR_GRID_STRIDE(ei, E) {
+        const int ow = eowner[ei] - na, kind = ekind[ei];
+        float ec[3];
+        edge_center(s_cx[ow], s_cy[ow], s_cz[ow], kind, hw, ec);
+        const int orient = kind >> 2;
+        for (int k = 0; k < 27; ++k) {
+            const int nb = s_neigh[(size_t)k * sstride + ow];
+            if (nb == -1) continue;
+            float nc[3];
+            sub_center(nb, na, cx, cy, cz, s_cx, s_cy, s_cz, nc[0], nc[1], nc[2]);
+            if (sqdist3(ec[0], ec[1], ec[2], nc[0], nc[1], nc[2]) < w2 && nb >= na && s_depth[nb - na] == depth) {
+                int idx = orient << 2, dim = 0;
+                for (int a = 0; a < 3; ++a)
+                    if (orient != a) { if (__fsub_rn(nc[a], ec[a]) < 0) idx |= (1 << dim); dim++; }
+                const int dn = sub_node_to_dnode(nb - na, groups, ng, depth);
+                s_edge[(size_t)idx * dstride + dn] = ei + 1;
+            }
+        }
+    }
+}
+
+// implicit values of subdivision vertices (:956-1038): x = 0 inside subdivision space,
+// a root stands for the octree node it replaces
+__global__ void __launch_bounds__(kBlock) k_sub_vertex_values(const Counters* c, int depth, const float* vx,
+                                                              const float* vy, const float* vz, const int* vowner,
+                                                              const int* neigh, size_t stride, const int* parent,
+                                                              const int* s_neigh, size_t sstride,
+                                                              const int* s_parent, const int* s_root,
+                                                              const int* enc, const float* x, float* vvalue, int na) {
+    const int V = c->n_sub_vertices;
+    const float iso = c->iso;
+    PSR_GRID_STRIDE(v, V) {
+        float val = 0.0f;
+        int now = vowner[v];
+        const float qx = vx[v], qy = vy[v], qz = vz[v];
+        if (now > 0) {
+            while (now != -1) {
+                for (int k = 0; k < 27; ++k) {
+                    int nb = (now < na) ? neigh[(size_t)k * stride + now] : s_neigh[(size_t)k * sstride + (now - na)];
+                    if (nb == -1) continue;
+                    if (nb >= na) {
+                        nb = s_root[nb - na];
+                        if (nb < 0) continue;
+                    }
+                    int ix, iy, iz;
+                    decode3m(enc[nb], depth, ix, iy, iz);
+                    float t = __fmul_rn(x[nb], basis32(ix, qx));
+                    t = __fmul_rn(t, basis32(iy, qy));
+                    t = __fmul_rn(t, basis32(iz, qz));
+                    val = __fadd_rn(val, t);
+                }
+                now = (now < na) ? parent[now] : s_parent[now - na];
+            }
+        }
+        vvalue[v] = __fsub_rn(val, iso);
+    }
+}
+
+struct SubCrossLoad {
+    const int* eowner;
+    const int* ekind;
+    const int* s_vtx;
+    size_t dstride;
+    const int* groups;
+    const int* ng_ptr;
+    int depth;
+    const float* vvalue;
+    int na;
+    unsigned* err;
+    __device__ unsigned operator()(int e) const {
+        const int dn = sub_node_to_dnode(eowner[e] - na, groups, *ng_ptr, depth);
+        const int kind = ekind[e];
+        const float a = ptr_value(vvalue, s_vtx[(size_t)c_tab.edge_vertex[kind][0] * dstride + dn], err);
+        const float b = ptr_value(vvalue, s_vtx[(size_t)c_tab.edge_vertex[kind][1] * dstride + dn], err);
+        return (__fmul_rn(a, b) <= 0.0f) ? 1u : 0u;
+    }
+};
+struct SubCrossStore {
+    const int* eowner;
+    const int* ekind;
+    const int* s_vtx;
+    size_t dstride;
+    const int* groups;
+    const int* ng_ptr;
+    int depth;
+    const float* vvalue;
+    const float *vx, *vy, *vz;
+    unsigned* ecross;
+    float* part_v;
+    const int* voff_ptr;
+    int cap;
+    int na;
+    unsigned* err;
+    __device__ void operator()(int e, unsigned pre, unsigned flag) const {
+        ecross[e] = pre;
+        if (!flag) return;
+        const int at = *voff_ptr + (int)pre;
+        if (at >= cap) { atomicOr(err, kErrCapacity); return; }
+        const int dn = sub_node_to_dnode(eowner[e] - na, groups, *ng_ptr, depth);
+        const int kind = ekind[e];
+        const int v1 = s_vtx[(size_t)c_tab.edge_vertex[kind][0] * dstride + dn] - 1;
+        const int v2 = s_vtx[(size_t)c_tab.edge_vertex[kind][1] * dstride + dn] - 1;
+        if (v1 < 0 || v2 < 0) return;
+        interp_point(vx[v1], vy[v1], vz[v1], vx[v2], vy[v2], vz[v2], kind >> 2, vvalue[v1], vvalue[v2],
+                     &part_v[3 * (size_t)at]);
+    }
+};
+
+struct SubCubeLoad {
+    const int* s_vtx;
+    size_t dstride;
+    const float* vvalue;
+    int* cube_class;
+    unsigned* err;
+    __device__ unsigned operator()(int o) const {
+        int cls = 0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+            if (ptr_value(vvalue, s_vtx[(size_t)q * dstride + o], err) < 0.0f) cls |= 1 << q;
+        cube_class[o] = cls;
+        return (unsigned)c_tab.mc_count[cls];
+    }
+};
+
+// group-local first crossing index of group g: ecross of the group's first sub edge
+struct SubCubeStore {
+    const int* cube_class;
+    const int* s_edge;
+    size_t dstride;
+    const unsigned* ecross;
+    const unsigned* group_cross0;   // per group: crossing prefix at its first edge
+    const int* groups;
+    const int* ng_ptr;
+    int* part_t;
+    const int* toff_ptr;
+    int cap;
+    unsigned* err;
+    __device__ void operator()(int o, unsigned pre, unsigned cnt) const {
+        if (!cnt) return;
+        const int g = find_group(groups, *ng_ptr, 5, o);
+        const unsigned base = group_cross0[g];
+        const int cls = cube_class[o];
+        const unsigned long long tri = c_tab.mc_tri[cls];
+        for (int t = 0; t < (int)cnt; ++t) {
+            const int at = *toff_ptr + (int)pre + t;
+            if (at >= cap) { atomicOr(err, kErrCapacity); continue; }
+            for (int a = 0; a < 3; ++a) {
+                const int e = (int)((tri >> (4 * (3 * t + a))) & 0xF);
+                const int ei = s_edge[(size_t)e * dstride + o] - 1;
+                part_t[3 * (size_t)at + a] = (ei >= 0) ? (int)(ecross[ei] - base) : -1;
+            }
+        }
+    }
+};
+
+// per-group first sub edge / first crossing / first triangle -> part table
+// parts: [0] main, [1 + g] group g.  part record: vstart, vcount, tstart, tcount
+__global__ void k_part_table(Counters* c, const int* groups, const unsigned* edge_of_dnode, const unsigned* ecross_sub, const unsigned* tri_of_dnode,
+                             unsigned* group_cross0, int* parts) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int ng = c->n_groups;
+    const int nE = c->n_sub_edges;
+    const int nSD = c->n_sub_dnodes;
+    parts[0] = 0;
+    parts[1] = c->n_cross;
+    parts[2] = 0;
+    parts[3] = c->n_tri;
+    for (int g = 0; g < ng; ++g) {
+        const int* G = groups + (size_t)g * kGroupRec;
+        const int d0 = G[5], d1 = G[5] + G[6];
+        // first sub edge of the group = edge prefix at its first D-level sub node
+        const int e0 = (d0 < nSD) ? (int)edge_of_dnode[d0] : nE;
+        const int e1 = (d1 < nSD) ? (int)edge_of_dnode[d1] : nE;
+        const unsigned x0 = (e0 < nE) ? ecross_sub[e0] : (unsigned)c->n_sub_cross;
+        const unsigned x1 = (e1 < nE) ? ecross_sub[e1] : (unsigned)c->n_sub_cross;
+        const unsigned t0 = (d0 < nSD) ? tri_of_dnode[d0] : (unsigned)c->n_sub_tri;
+        const unsigned t1 = (d1 < nSD) ? tri_of_dnode[d1] : (unsigned)c->n_sub_tri;
+        group_cross0[g] = x0;
+        int* P = parts + 4 * (size_t)(g + 1);
+        P[0] = c->n_cross + (int)x0;
+        P[1] = (int)(x1 - x0);
+        P[2] = c->n_tri + (int)t0;
+        P[3] = (int)(t1 - t0);
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// insertion (insertTriangle :1247-1282): drop vertices with |x| < 1e-6, offset triangle
+// indices by the vertices kept before the part, drop triangles out of the part's range
+// ------------------------------------------------------------------------------------
+struct KeepVertexLoad {
+    const float* part_v;
+    __device__ unsigned operator()(int v) const { return (fabsf(part_v[3 * (size_t)v]) < 1e-6f) ? 0u : 1u; }
+};
+struct KeepVertexStore {
+    const float* part_v;
+    float* mesh_v;
+    unsigned* kept_prefix;
+    int cap;
+    unsigned* err;
+    __device__ void operator()(int v, unsigned pre, unsigned keep) const {
+        kept_prefix[v] = pre;
+        if (!keep) return;
+        if ((int)pre >= cap) { atomicOr(err, kErrCapacity); return; }
+        mesh_v[3 * (size_t)pre] = part_v[3 * (size_t)v];
+        mesh_v[3 * (size_t)pre + 1] = part_v[3 * (size_t)v + 1];
+        mesh_v[3 * (size_t)pre + 2] = part_v[3 * (size_t)v + 2];
+    }
+};
+
+__device__ __forceinline__ int find_part(const int* parts, int np, int t) {
+    int lo = 0, hi = np - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (parts[4 * mid + 2] <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+struct KeepTriLoad {
+    const int* part_t;
+    const int* parts;
+    const int* np_ptr;
+    __device__ unsigned operator()(int t) const {
+        const int p = find_part(parts, *np_ptr, t);
+        const int vc = parts[4 * p + 1];
+        for (int a = 0; a < 3; ++a) {
+            int l = part_t[3 * (size_t)t + a];
+            if (l < 0 || l >= vc) return 0u;
+        }
+        return 1u;
+    }
+};
+struct KeepTriStore {
+    const int* part_t;
+    const int* parts;
+    const int* np_ptr;
+    const unsigned* kept_prefix;
+    const int* n_staged_v;
+    const int* n_kept_v;
+    int* mesh_t;
+    int cap;
+    unsigned* err;
+    __device__ void operator()(int t, unsigned pre, unsigned keep) const {
+        if (!keep) return;
+        if ((int)pre >= cap) { atomicOr(err, kErrCapacity); return; }
+        const int p = find_part(parts, *np_ptr, t);
+        const int vs = parts[4 * p];
+        const int prev = (vs < *n_staged_v) ? (int)kept_prefix[vs] : *n_kept_v;
+        for (int a = 0; a < 3; ++a) mesh_t[3 * (size_t)pre + a] = part_t[3 * (size_t)t + a] + prev;
+    }
+};
+
+__global__ void k_count_parts(Counters* c, int* n_parts, int* n_staged_v, int* n_staged_t, int cap_v, int cap_t) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        *n_parts = 1 + c->n_groups;
+        int nv = c->n_cross + c->n_sub_cross, nt = c->n_tri + c->n_sub_tri;
+        if (nv > cap_v || nt > cap_t) atomicOr(&c->error, kErrCapacity);
+        *n_staged_v = nv < cap_v ? nv : cap_v;
+        *n_staged_t = nt < cap_t ? nt : cap_t;
+    }
+}
+
+static inline int grid_for(const Workspace& ws, long long work) {
+    long long g = (work + kBlock - 1) / kBlock;
+    long long cap = (long long)ws.num_sms * 8;
+    if (g > cap) g = cap;
+    return (int)(g < 1 ? 1 : g);
+}
+
+cudaError_t mesh_build_impl(Workspace& ws, const MeshBufs& mb) {
+    cudaStream_t s = ws.stream;
+    const int D = ws.depth;
+    Counters* c = ws.cnt;
+    unsigned* err = &c->error;
+    unsigned* total = (unsigned*)&c->scan_total;
+    const size_t stride = (size_t)ws.cap.nodes;
+    const int gm = grid_for(ws, ws.cap.nodes);
+    cudaError_t e;
+    k_mesh_reset<<<gm, kBlock, 0, s>>>(c, ws.node_vtx, ws.node_edge, ws.node_face, mb.ov_group, mb.ov_sub, stride);
+    // vertices
+    k_vertex_owner<<<gm, kBlock, 0, s>>>(c, ws.key, ws.ndepth, ws.ctr_x, ws.ctr_y, ws.ctr_z, ws.neigh, stride, ws.vmask);
+    e = launch_scan(PopcLoad8{ws.vmask},
+                    VertexStore{ws.vmask, ws.ndepth, ws.ctr_x, ws.ctr_y, ws.ctr_z, ws.v_x, ws.v_y, ws.v_z, ws.v_owner,
+                                ws.v_kind, ws.v_depth, ws.cap.vertices, err},
+                    &c->n_nodes, 0, ws.scan, total, err, s);
+    if (e != cudaSuccess) return e;
+    k_set_count<<<1, 1, 0, s>>>(&c->n_vertices, total, ws.cap.vertices, err);
+    k_vertex_maintain<<<gm, kBlock, 0, s>>>(c, ws.ndepth, ws.ctr_x, ws.ctr_y, ws.ctr_z, ws.neigh, stride, ws.v_x, ws.v_y,
+                                            ws.v_z, ws.v_owner, ws.node_vtx);
+    // edges (D level)
+    k_edge_owner<<<gm, kBlock, 0, s>>>(c, D, ws.key, ws.ctr_x, ws.ctr_y, ws.ctr_z, ws.neigh, stride, ws.emask16);
+    e = launch_scan(PopcLoad16{ws.emask16},
+                    EdgeStore{ws.emask16, &c->level_base[D], ws.e_owner, ws.e_kind, ws.cap.edges, err},
+                    &c->level_count[D], 0, ws.scan, total, err, s);
+    if (e != cudaSuccess) return e;
+    k_set_count<<<1, 1, 0, s>>>(&c->n_edges, total, ws.cap.edges, err);
+    k_edge_maintain<<<gm, kBlock, 0, s>>>(c, D, ws.ctr_x, ws.ctr_y, ws.ctr_z, ws.neigh, stride, ws.e_owner, ws.e_kind,
+                                          ws.node_edge);
+    // faces
+    k_face_owner<<<gm, kBlock, 0, s>>>(c, ws.key, ws.ndepth, ws.ctr_x, ws.ctr_y, ws.ctr_z, ws.neigh, stride, ws.fmask);
+    e = launch_scan(PopcLoad8{ws.fmask},
+                    FaceStore{ws.fmask, ws.key, ws.ndepth, ws.parent, D, ws.f_owner, ws.f_kind, ws.f_hasparent,
+                              ws.cap.faces, err},
+                    &c->n_nodes, 0, ws.scan, total, err, s);
+    if (e != cudaSuccess) return e;
+    k_set_count<<<1, 1, 0, s>>>(&c->n_faces, total, ws.cap.faces, err);
+    k_face_maintain<<<gm, kBlock, 0, s>>>(c, ws.ndepth, ws.ctr_x, ws.ctr_y, ws.ctr_z, ws.neigh, stride, ws.f_owner,
+                                          ws.f_kind, ws.node_face);
+    // implicit values
+    k_vertex_values<<<gm, kBlock, 0, s>>>(c, D, ws.v_x, ws.v_y, ws.v_z, ws.v_owner, ws.v_kind, ws.v_depth, ws.neigh,
+                                          stride, ws.parent, ws.first_child, ws.enc, ws.xsol, ws.vvalue);
+    // crossings -> staged vertices of the main part
+    e = launch_scan(CrossLoad{ws.e_owner, ws.e_kind, ws.node_vtx, stride, ws.vvalue, err},
+                    CrossStore{ws.e_owner, ws.e_kind, ws.node_vtx, stride, ws.vvalue, ws.v_x, ws.v_y, ws.v_z,
+                               ws.e_cross, ws.part_v, 0, ws.part_cap_v, err},
+                    &c->n_edges, 0, ws.scan, total, err, s);
+    if (e != cudaSuccess) return e;
+    k_set_count<<<1, 1, 0, s>>>(&c->n_cross, total, ws.part_cap_v, err);
+    // face hits must start cleared
+    cudaMemsetAsync(ws.face_hit, 0, sizeof(int) * (size_t)ws.cap.faces, s);
+    e = launch_scan(CubeLoad{ws.node_vtx, stride, &c->level_base[D], ws.vvalue, ws.cube_class, err},
+                    CubeStore{ws.cube_class, &c->level_base[D], ws.node_edge, ws.node_face, stride, ws.e_cross,
+                              ws.parent, ws.f_hasparent, ws.face_hit, ws.part_t, 0, ws.part_cap_t, err},
+                    &c->level_count[D], 0, ws.scan, total, err, s);
+    if (e != cudaSuccess) return e;
+    k_set_count<<<1, 1, 0, s>>>(&c->n_tri, total, ws.part_cap_t, err);
+    // subdivision roots among nodes of depth < D
+    e = launch_scan(RootLoad{ws.node_vtx, ws.node_face, stride, ws.vvalue, ws.face_hit, ws.first_child, err},
+                    RootStore{ws.sub_root, ws.cap.nodes, err}, &c->level_base[D], 0, ws.scan, total, err, s);
+    if (e != cudaSuccess) return e;
+    k_set_count<<<1, 1, 0, s>>>(&c->n_subroots, total, ws.cap.nodes, err);
+    k_build_groups<<<1, 1, 0, s>>>(c, D, ws.sub_root, ws.ndepth, ws.key, ws.parent, ws.sub_root_depth, mb.groups,
+                                   mb.max_groups, ws.cap.sub_nodes, ws.cap.sub_dnodes, ws.node_subgroup,
+                                   ws.node_subslot, mb.ov_group, mb.ov_sub, stride);
+    return cudaGetLastError();
+}
+
+// Subdivision-space nodes are numbered cap.nodes + local index: every such number is
+// larger than any octree index, which is all the kernels compare against.
+cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
+    cudaStream_t s = ws.stream;
+    const int D = ws.depth;
+    Counters* c = ws.cnt;
+    unsigned* err = &c->error;
+    unsigned* total = (unsigned*)&c->scan_total;
+    const size_t stride = (size_t)ws.cap.nodes;
+    const size_t sstride = (size_t)ws.cap.sub_nodes;
+    const size_t dstride = (size_t)ws.cap.sub_dnodes;
+    const int na = ws.cap.nodes;
+    const int gs = grid_for(ws, ws.cap.sub_nodes);
+    cudaError_t e;
+    k_sub_build<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.sub_root, ws.key, ws.parent, ws.neigh, stride, ws.s_key,
+                                      ws.s_parent, ws.s_first_child, ws.s_depth, ws.s_group, ws.s_root, ws.s_cx,
+                                      ws.s_cy, ws.s_cz, na);
+    for (int d = 1; d <= D; ++d)
+        k_sub_neighbours<<<gs, kBlock, 0, s>>>(c, d, D, mb.groups, ws.neigh, stride, ws.first_child, mb.ov_group,
+                                               mb.ov_sub, ws.s_key, ws.s_parent, ws.s_first_child, ws.s_depth,
+                                               ws.s_group, ws.s_neigh, sstride, na);
+    cudaMemsetAsync(ws.s_vtx, 0, sizeof(int) * 8 * dstride, s);
+    cudaMemsetAsync(ws.s_edge, 0, sizeof(int) * 12 * dstride, s);
+    k_sub_vertex_owner<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.s_key, ws.s_neigh, sstride, ws.s_cx, ws.s_cy, ws.s_cz,
+                                             ws.s_vmask, na);
+    e = launch_scan(PopcLoad8{ws.s_vmask},
+                    SubVertexStore{ws.s_vmask, mb.groups, &c->n_groups, D, ws.s_cx, ws.s_cy, ws.s_cz, ws.sv_x, ws.sv_y,
+                                   ws.sv_z, ws.sv_owner, ws.sv_kind, 8 * ws.cap.sub_dnodes, na, err},
+                    &c->n_sub_dnodes, 0, ws.scan, total, err, s);
+    if (e != cudaSuccess) return e;
+    k_set_count<<<1, 1, 0, s>>>(&c->n_sub_vertices, total, 8 * ws.cap.sub_dnodes, err);
+    k_sub_vertex_maintain<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.ctr_x, ws.ctr_y, ws.ctr_z, ws.s_neigh, sstride,
+                                                ws.s_cx, ws.s_cy, ws.s_cz, ws.s_depth, ws.sv_x, ws.sv_y, ws.sv_z,
+                                                ws.sv_owner, ws.s_vtx, dstride, na);
+    k_sub_edge_owner<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.s_key, ws.s_neigh, sstride, ws.s_cx, ws.s_cy, ws.s_cz,
+                                           ws.s_emask, na);
+    e = launch_scan(PopcLoad16{ws.s_emask},
+                    SubEdgeStore{ws.s_emask, mb.groups, &c->n_groups, D, ws.se_owner, ws.se_kind,
+                                 12 * ws.cap.sub_dnodes, na, err},
+                    &c->n_sub_dnodes, 0, ws.scan, total, err, s);
+    if (e != cudaSuccess) return e;
+    k_set_count<<<1, 1, 0, s>>>(&c->n_sub_edges, total, 12 * ws.cap.sub_dnodes, err);
+    // edge prefix per D-level sub node (for the part table): recompute via a scan of popcounts
+    e = launch_scan(PopcLoad16{ws.s_emask}, StoreExclusive{mb.edge_of_dnode}, &c->n_sub_dnodes, 0, ws.scan, total,
+                    err, s);
+    if (e != cudaSuccess) return e;
+    k_sub_edge_maintain<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.ctr_x, ws.ctr_y, ws.ctr_z, ws.s_neigh, sstride,
+                                              ws.s_cx, ws.s_cy, ws.s_cz, ws.s_depth, ws.se_owner, ws.se_kind, ws.s_edge,
+                                              dstride, na);
+    k_sub_vertex_values<<<gs, kBlock, 0, s>>>(c, D, ws.sv_x, ws.sv_y, ws.sv_z, ws.sv_owner, ws.neigh, stride, ws.parent,
+                                              ws.s_neigh, sstride, ws.s_parent, ws.s_root, ws.enc, ws.xsol,
+                                              ws.sv_value, na);
+    // crossings: staged after the main part's vertices
+    e = launch_scan(SubCrossLoad{ws.se_owner, ws.se_kind, ws.s_vtx, dstride, mb.groups, &c->n_groups, D, ws.sv_value, na, err},
+                    SubCrossStore{ws.se_owner, ws.se_kind, ws.s_vtx, dstride, mb.groups, &c->n_groups, D, ws.sv_value,
+                                  ws.sv_x, ws.sv_y, ws.sv_z, ws.se_cross, ws.part_v, &c->n_cross, ws.part_cap_v, na,
+                                  err},
+                    &c->n_sub_edges, 0, ws.scan, total, err, s);
+    if (e != cudaSuccess) return e;
+    k_set_count<<<1, 1, 0, s>>>(&c->n_sub_cross, total, ws.part_cap_v, err);
+    // triangle prefix per D-level sub node
+    e = launch_scan(SubCubeLoad{ws.s_vtx, dstride, ws.sv_value, ws.s_cube_class, err}, StoreExclusive{mb.tri_of_dnode},
+                    &c->n_sub_dnodes, 0, ws.scan, total, err, s);
+    if (e != cudaSuccess) return e;
+    k_set_count<<<1, 1, 0, s>>>(&c->n_sub_tri, total, ws.part_cap_t, err);
+    k_part_table<<<1, 1, 0, s>>>(c, mb.groups, mb.edge_of_dnode, ws.se_cross, mb.tri_of_dnode,
+                                 mb.group_cross0, mb.parts);
+    e = launch_scan(SubCubeLoad{ws.s_vtx, dstride, ws.sv_value, ws.s_cube_class, err},
+                    SubCubeStore{ws.s_cube_class, ws.s_edge, dstride, ws.se_cross, mb.group_cross0, mb.groups,
+                                 &c->n_groups, ws.part_t, &c->n_tri, ws.part_cap_t, err},
+                    &c->n_sub_dnodes, 0, ws.scan, total, err, s);
+    if (e != cudaSuccess) return e;
+    // insertion of all parts
+    int* n_parts = mb.misc;
+    int* n_staged_v = mb.misc + 1;
+    int* n_staged_t = mb.misc + 2;
+    k_count_parts<<<1, 1, 0, s>>>(c, n_parts, n_staged_v, n_staged_t, ws.part_cap_v, ws.part_cap_t);
+    e = launch_scan(KeepVertexLoad{ws.part_v}, KeepVertexStore{ws.part_v, ws.mesh_v, mb.kept_prefix, ws.cap.mesh_vertices, err},
+                    n_staged_v, 0, ws.scan, total, err, s);
+    if (e != cudaSuccess) return e;
+    k_set_count<<<1, 1, 0, s>>>(&c->n_mesh_vertices, total, ws.cap.mesh_vertices, err);
+    e = launch_scan(KeepTriLoad{ws.part_t, mb.parts, n_parts},
+                    KeepTriStore{ws.part_t, mb.parts, n_parts, mb.kept_prefix, n_staged_v, &c->n_mesh_vertices,
+                                 ws.mesh_t, ws.cap.mesh_tris, err},
+                    n_staged_t, 0, ws.scan, total, err, s);
+    if (e != cudaSuccess) return e;
+    k_set_count<<<1, 1, 0, s>>>(&c->n_mesh_triangles, total, ws.cap.mesh_tris, err);
+    return cudaGetLastError();
+}
+
+}  // namespace psr
+
+namespace psr {
+cudaError_t mesh_build(Workspace& ws) {
+    cudaError_t e = mesh_build_impl(ws, ws.mb);
+    if (e != cudaSuccess) return e;
+    return mesh_build_sub(ws, ws.mb);
+}
+}  // namespace psr

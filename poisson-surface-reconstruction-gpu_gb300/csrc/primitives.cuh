@@ -1,0 +1,195 @@
+// Hand-written device-wide primitives: single-pass prefix scan with fused load / store
+// functors (decoupled look-back, dynamic tile ids, bounded waits) and a stable LSD radix
+// sort of (32-bit key, 32-bit value) pairs.  Problem sizes are read from device memory.
+#pragma once
+#include "psr_common.cuh"
+
+namespace psr {
+
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kBlock * kScanItems;   // 2048 elements per tile
+
+// Scratch of one scan call: tile counter + one 64-bit status word per tile
+// (bit 62: aggregate published, bit 63: inclusive prefix published, low 32 bits value).
+struct ScanScratch {
+    unsigned long long* words;   // [0] = tile counter, [1 + t] = status of tile t
+    int max_tiles;
+};
+
+constexpr unsigned long long kFlagAgg = 1ull << 62;
+constexpr unsigned long long kFlagIncl = 1ull << 63;
+
+__device__ __forceinline__ unsigned long long load_status(const unsigned long long* p) {
+    return *((volatile const unsigned long long*)p);
+}
+
+// Block-wide exclusive scan of one value per thread; returns the block total.
+__device__ __forceinline__ unsigned block_exclusive_scan(unsigned v, unsigned& excl, unsigned* smem_warp) {
+    const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+    unsigned x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= (unsigned)o) x += y;
+    }
+    if (lane == 31) smem_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned w = (lane < (kBlock / 32)) ? smem_warp[lane] : 0u;
+        unsigned s = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= (unsigned)o) s += y;
+        }
+        if (lane < (kBlock / 32)) smem_warp[lane] = s - w;   // exclusive warp offsets
+        if (lane == (kBlock / 32) - 1) smem_warp[kBlock / 32] = s;
+    }
+    __syncthreads();
+    excl = smem_warp[warp] + x - v;
+    unsigned total = smem_warp[kBlock / 32];
+    __syncthreads();
+    return total;
+}
+
+// Generic scan.  Load(i) -> unsigned value of element i; Store(i, prefix, value) gets the
+// exclusive prefix of element i.  *total receives the sum of all n elements.
+template <class Load, class Store>
+__global__ void __launch_bounds__(kBlock) k_scan(Load load, Store store, const int* count_ptr, int count_add,
+                                                 ScanScratch sc, unsigned* total, unsigned* err) {
+    __shared__ unsigned s_warp[kBlock / 32 + 1];
+    __shared__ int s_tile;
+    __shared__ unsigned s_prefix;
+    const int n = *count_ptr + count_add;
+    const int ntiles = (n + kScanTile - 1) / kScanTile;
+    if (n <= 0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) *total = 0u;
+        return;
+    }
+    if (ntiles > sc.max_tiles) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(err, kErrCapacity);
+        return;
+    }
+    while (true) {
+        if (threadIdx.x == 0) s_tile = (int)atomicAdd(sc.words, 1ull);
+        __syncthreads();
+        const int t = s_tile;
+        __syncthreads();
+        if (t >= ntiles) break;
+        const int base = t * kScanTile + threadIdx.x * kScanItems;
+        unsigned v[kScanItems];
+        unsigned sum = 0;
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) {
+            int i = base + k;
+            v[k] = (i < n) ? load(i) : 0u;
+            sum += v[k];
+        }
+        unsigned excl;
+        const unsigned agg = block_exclusive_scan(sum, excl, s_warp);
+        // look-back by warp 0
+        if (threadIdx.x < 32) {
+            const unsigned lane = lane_id();
+            unsigned long long* st = sc.words + 1;
+            if (t == 0) {
+                if (lane == 0) {
+                    atomicExch(st, kFlagIncl | (unsigned long long)agg);
+                    s_prefix = 0u;
+                }
+            } else {
+                if (lane == 0) atomicExch(st + t, kFlagAgg | (unsigned long long)agg);
+                unsigned run = 0;
+                int pred = t - 1;
+                bool timeout = false;
+                while (true) {
+                    int idx = pred - (int)lane;
+                    unsigned long long s = kFlagIncl;   // "prefix 0" past the first tile
+                    if (idx >= 0) {
+                        int it = 0;
+                        s = load_status(st + idx);
+                        while (!(s & (kFlagAgg | kFlagIncl))) {
+                            if (++it > kSpinLimit) { timeout = true; s = kFlagIncl; break; }
+                            __nanosleep(20);
+                            s = load_status(st + idx);
+                        }
+                    }
+                    unsigned incl_mask = __ballot_sync(0xffffffffu, (s & kFlagIncl) != 0);
+                    unsigned val = (unsigned)(s & 0xffffffffull);
+                    if (incl_mask) {
+                        int first = __ffs(incl_mask) - 1;
+                        unsigned contrib = ((int)lane <= first) ? val : 0u;
+#pragma unroll
+                        for (int o = 16; o > 0; o >>= 1) contrib += __shfl_xor_sync(0xffffffffu, contrib, o);
+                        run += contrib;
+                        break;
+                    }
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
+                    run += val;
+                    pred -= 32;
+                }
+                if (__any_sync(0xffffffffu, timeout) && lane == 0) atomicOr(err, kErrSpinTimeout);
+                if (lane == 0) {
+                    atomicExch(st + t, kFlagIncl | (unsigned long long)(run + agg));
+                    s_prefix = run;
+                }
+            }
+        }
+        __syncthreads();
+        unsigned pre = s_prefix + excl;
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) {
+            int i = base + k;
+            if (i < n) store(i, pre, v[k]);
+            pre += v[k];
+        }
+        if (t == ntiles - 1 && threadIdx.x == kBlock - 1) *total = s_prefix + agg;
+        __syncthreads();
+    }
+}
+
+// host launcher (declared here, defined in primitives.cu)
+struct Device;
+int scan_grid(int max_tiles);
+
+template <class Load, class Store>
+inline cudaError_t launch_scan(Load load, Store store, const int* count_ptr, int count_add, ScanScratch sc,
+                               unsigned* total, unsigned* err, cudaStream_t stream) {
+    cudaError_t e = cudaMemsetAsync(sc.words, 0, sizeof(unsigned long long) * (size_t)(sc.max_tiles + 1), stream);
+    if (e != cudaSuccess) return e;
+    k_scan<Load, Store><<<scan_grid(sc.max_tiles), kBlock, 0, stream>>>(load, store, count_ptr, count_add, sc, total, err);
+    return cudaGetLastError();
+}
+
+// ---- common load / store functors ----------------------------------------------------
+struct LoadArray {
+    const unsigned* a;
+    __device__ unsigned operator()(int i) const { return a[i]; }
+};
+struct StoreExclusive {
+    unsigned* out;
+    __device__ void operator()(int i, unsigned pre, unsigned) const { out[i] = pre; }
+};
+struct StoreInclusive {
+    unsigned* out;
+    __device__ void operator()(int i, unsigned pre, unsigned v) const { out[i] = pre + v; }
+};
+
+// ---- radix sort ------------------------------------------------------------------------
+constexpr int kRadixBits = 8;
+constexpr int kRadix = 1 << kRadixBits;
+constexpr int kSortItems = 8;
+constexpr int kSortTile = kBlock * kSortItems;   // 2048 keys per tile
+
+struct SortScratch {
+    unsigned* hist;          // [kRadix][max_tiles]
+    unsigned* keys_alt;
+    unsigned* vals_alt;
+    int max_tiles;
+    ScanScratch scan;
+};
+
+cudaError_t radix_sort_pairs(unsigned* keys, unsigned* vals, const int* count_ptr, int key_bits, SortScratch sc,
+                             unsigned* err, cudaStream_t stream, bool* result_in_alt);
+
+}  // namespace psr

@@ -1,0 +1,98 @@
+// Common device definitions for the Poisson reconstruction kernels (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace psr {
+
+constexpr int kMaxDepth = 9;      // the encoded function index packs 3 x (D+1) bits in int32
+constexpr int kBlock = 256;
+
+// Device error word bits (read back by the host after a run).
+enum : unsigned {
+    kErrSpinTimeout = 1u,   // a bounded wait gave up
+    kErrCapacity = 2u,      // a device-side count exceeded its buffer capacity
+    kErrInvalid = 4u,       // non-finite input
+};
+
+// Device-resident counts: every kernel reads its problem size from here, so the whole
+// pipeline can be replayed from a CUDA graph without host round trips.
+struct Counters {
+    int n_points;
+    int n_unique;
+    int n_groups;                 // scratch: group count of the level being built
+    int level_count[kMaxDepth + 1];
+    int level_base[kMaxDepth + 1];
+    int level_tmp_off[kMaxDepth + 1];   // offset of each level inside the build buffer
+    int n_nodes;
+    int n_vertices, n_edges, n_faces;
+    int n_cross, n_tri;
+    int n_subroots;
+    int sub_depth_count[kMaxDepth + 1];
+    int sub_depth_start[kMaxDepth + 1];
+    int n_sub_nodes;              // all subdivision-space nodes over all groups
+    int n_sub_dnodes;             // D-level subdivision nodes
+    int n_sub_vertices, n_sub_edges, n_sub_cross, n_sub_tri;
+    int n_mesh_vertices, n_mesh_triangles;
+    int scan_total;               // scratch total written by scans
+    unsigned error;
+    float bbox_min[3], bbox_max[3];
+    float center[3];
+    float max_edge;
+    double iso_sum;
+    float iso;
+    int cg_iters[kMaxDepth + 1];
+    double cg_rr[kMaxDepth + 1];
+};
+
+// Look-up tables shared by the kernels (values derived in tables.cpp).
+struct ConstTables {
+    int lut_parent[8][27];
+    int lut_child[8][27];
+    int edge_vertex[12][2];
+    int face_edges[6][4];
+    int parent_face_kind[8][6];
+    int children_vertex_kind[8];
+    unsigned long long mc_tri[256];
+    int mc_count[256];
+};
+
+#ifdef __CUDACC__
+#define PSR_GRID_STRIDE(i, n) for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += gridDim.x * blockDim.x)
+
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+// ordered-int encoding of floats for atomic min / max
+__device__ __forceinline__ int float_to_ordered(float f) {
+    int i = __float_as_int(f);
+    return i >= 0 ? i : i ^ 0x7fffffff;
+}
+__device__ __forceinline__ float ordered_to_float(int i) {
+    return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff);
+}
+
+__device__ __forceinline__ int ilog2_dev(int v) { return 31 - __clz(v); }
+
+// Normalised quadratic B-spline of the 1-D function index `idx` (centre (o+1/2)/2^d,
+// width 2^-d) at x.  Operation order is fixed (no contraction) so the host mirror in
+// the oracle reproduces it bit for bit.
+__device__ __forceinline__ float basis32(int idx, float x) {
+    const float kF43 = 1.33333337306976318359375f;
+    const float kF23 = 0.666666686534881591796875f;
+    int d = ilog2_dev(idx + 1);
+    int off = idx + 1 - (1 << d);
+    float s = (float)(1 << d);
+    float c = __fdiv_rn(__fadd_rn((float)off, 0.5f), s);
+    float t = __fmul_rn(__fsub_rn(x, c), s);
+    float a = fabsf(t);
+    if (a < 0.5f) return __fmul_rn(__fsub_rn(0.75f, __fmul_rn(t, t)), kF43);
+    if (a < 1.5f) { float u = __fsub_rn(1.5f, a); return __fmul_rn(__fmul_rn(u, u), kF23); }
+    return 0.0f;
+}
+
+#endif  // __CUDACC__
+
+// Iteration limit of every device-side wait; exceeding it sets kErrSpinTimeout.
+constexpr int kSpinLimit = 1 << 22;
+
+}  // namespace psr

@@ -1,0 +1,310 @@
+// Stage (c): per-depth Laplacian conjugate gradients and the iso-value.
+//
+// System of depth d (mesh/solver/LaplacianSolver.cu:27-74,120-267): rows are the nodes of
+// depth d, columns their same-depth neighbours, entry ff_x ff_y ff_z (d2_x + d2_y + d2_z)
+// stored in FP32 and dropped when |value| <= 1e-6.  Same-depth entries depend only on
+// the neighbour offset, so the operator is applied matrix-free from a 27-entry stencil
+// per depth and the neighbour table.  Right-hand side: the divergence of the depth.
+//
+// CG (mesh/solver/CGAlgorithm.cu:10-80): x0 = 0, r0 = b, stops when r.r <= tol^2 or after
+// max_iter iterations (or after a fixed count).  All depths are independent and are solved
+// together in one cooperative launch: every iteration performs the SpMV of all depths,
+// per-depth FP64 reductions in a fixed order (deterministic), and per-depth updates.
+//
+// Iso-value (:269-305): mean of the implicit function at the sample points, evaluated in
+// FP32 per point and averaged in FP64.
+#include <cooperative_groups.h>
+#include "workspace.h"
+#include "tables.cuh"
+
+PSR_DEFINE_CONST_TABLES(upload_tables_solver)
+
+namespace cg = cooperative_groups;
+
+namespace psr {
+
+constexpr int kCgBlock = 256;
+
+struct CgArgs {
+    const Counters* c;
+    Counters* cw;
+    int depth;
+    const int* ndepth;
+    const int* neigh;
+    size_t stride;
+    const float* stencil;
+    const float* b;
+    float* x;
+    float* r;
+    float* p;
+    float* ap;
+    double* partial;   // [gridDim][kMaxDepth + 1]
+    double tol2;       // compared against a float copy of r.r, as the reference does
+    int max_iter;
+};
+
+// Sum the per-depth values of all threads of the block into smem[depth]; then every
+// block reduces the grid partials of every depth in the same fixed order.
+__device__ __forceinline__ void block_depth_reduce(double (&acc)[kMaxDepth + 1], int nd, double* smem, double* out_row) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int d = 0; d <= kMaxDepth; ++d) {
+        if (d >= nd) break;
+        double v = acc[d];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) smem[warp * (kMaxDepth + 1) + d] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < nd) {
+        double s = 0.0;
+        for (int w = 0; w < kCgBlock / 32; ++w) s += smem[w * (kMaxDepth + 1) + threadIdx.x];
+        out_row[threadIdx.x] = s;
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ void grid_depth_sum(const double* partial, int nblocks, int nd, double* result) {
+    // warp w sums depth w over all blocks (fixed order)
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int d = warp; d < nd; d += kCgBlock / 32) {
+        double s = 0.0;
+        for (int bi = lane; bi < nblocks; bi += 32) s += partial[(size_t)bi * (kMaxDepth + 1) + d];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) result[d] = s;
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(kCgBlock) k_cg(CgArgs a) {
+    cg::grid_group grid = cg::this_grid();
+    __shared__ double s_red[(kCgBlock / 32) * (kMaxDepth + 1)];
+    __shared__ double s_rr[kMaxDepth + 1], s_pap[kMaxDepth + 1], s_new[kMaxDepth + 1];
+    __shared__ float s_alpha[kMaxDepth + 1], s_beta[kMaxDepth + 1];
+    __shared__ int s_active[kMaxDepth + 1];
+    __shared__ float s_st[(kMaxDepth + 1) * 27];
+    const int nd = a.depth + 1;
+    const int M = a.c->n_nodes;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nthr = gridDim.x * blockDim.x;
+    for (int q = threadIdx.x; q < nd * 27; q += blockDim.x) s_st[q] = a.stencil[q];
+    __syncthreads();
+    double* my_row = a.partial + (size_t)blockIdx.x * (kMaxDepth + 1);
+
+    // r = b, x = 0, p = r, rr = r.r
+    double acc[kMaxDepth + 1];
+#pragma unroll
+    for (int d = 0; d <= kMaxDepth; ++d) acc[d] = 0.0;
+    for (int i = tid; i < M; i += nthr) {
+        float bi = a.b[i];
+        a.r[i] = bi;
+        a.p[i] = bi;
+        a.x[i] = 0.0f;
+        const int d = a.ndepth[i];
+#pragma unroll
+        for (int q = 0; q <= kMaxDepth; ++q) if (q == d) acc[q] += (double)(bi * bi);
+    }
+    block_depth_reduce(acc, nd, s_red, my_row);
+    grid.sync();
+    grid_depth_sum(a.partial, gridDim.x, nd, s_rr);
+    if (threadIdx.x < nd) {
+        const int d = threadIdx.x;
+        // the reference compares a float copy of r.r (mesh/solver/CGAlgorithm.cu:19,36)
+        s_active[d] = ((double)(float)s_rr[d] > a.tol2) ? 1 : 0;
+    }
+    __syncthreads();
+    int it = 1;
+    const int maxit = a.max_iter;
+    int any = 0;
+    for (int d = 0; d < nd; ++d) any |= s_active[d];
+    while (any && it <= maxit) {
+        grid.sync();   // p complete everywhere; partial rows free
+        // Ap and p.Ap
+#pragma unroll
+        for (int d = 0; d <= kMaxDepth; ++d) acc[d] = 0.0;
+        for (int i = tid; i < M; i += nthr) {
+            const int d = a.ndepth[i];
+            if (!s_active[d]) continue;
+            const float* st = &s_st[d * 27];
+            float y = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 27; ++k) {
+                int nb = a.neigh[(size_t)k * a.stride + i];
+                if (nb >= 0) y = fmaf(st[k], a.p[nb], y);
+            }
+            a.ap[i] = y;
+            const float pi = a.p[i];
+#pragma unroll
+            for (int q = 0; q <= kMaxDepth; ++q) if (q == d) acc[q] += (double)(pi * y);
+        }
+        block_depth_reduce(acc, nd, s_red, my_row);
+        grid.sync();
+        grid_depth_sum(a.partial, gridDim.x, nd, s_pap);
+        if (threadIdx.x < nd) {
+            const int d = threadIdx.x;
+            s_alpha[d] = (s_active[d] && s_pap[d] != 0.0) ? (float)(s_rr[d] / s_pap[d]) : 0.0f;
+        }
+        __syncthreads();
+        grid.sync();   // every block has read the p.Ap partials
+#pragma unroll
+        for (int d = 0; d <= kMaxDepth; ++d) acc[d] = 0.0;
+        for (int i = tid; i < M; i += nthr) {
+            const int d = a.ndepth[i];
+            if (!s_active[d]) continue;
+            const float al = s_alpha[d];
+            a.x[i] = fmaf(al, a.p[i], a.x[i]);
+            const float ri = fmaf(-al, a.ap[i], a.r[i]);
+            a.r[i] = ri;
+#pragma unroll
+            for (int q = 0; q <= kMaxDepth; ++q) if (q == d) acc[q] += (double)(ri * ri);
+        }
+        block_depth_reduce(acc, nd, s_red, my_row);
+        grid.sync();
+        grid_depth_sum(a.partial, gridDim.x, nd, s_new);
+        if (threadIdx.x < nd) {
+            const int d = threadIdx.x;
+            if (s_active[d]) {
+                s_beta[d] = (s_rr[d] != 0.0) ? (float)(s_new[d] / s_rr[d]) : 0.0f;
+                s_rr[d] = s_new[d];
+                if (blockIdx.x == 0) {
+                    a.cw->cg_iters[d] = it;
+                    a.cw->cg_rr[d] = s_new[d];
+                }
+                bool go = ((double)(float)s_new[d] > a.tol2) && s_pap[d] != 0.0;
+                s_active[d] = (go && it + 1 <= maxit) ? 1 : 0;
+            } else {
+                s_beta[d] = 0.0f;
+            }
+        }
+        __syncthreads();
+        for (int i = tid; i < M; i += nthr) {
+            const int d = a.ndepth[i];
+            if (!s_active[d]) continue;
+            a.p[i] = fmaf(s_beta[d], a.p[i], a.r[i]);
+        }
+        any = 0;
+        for (int d = 0; d < nd; ++d) any |= s_active[d];
+        ++it;
+    }
+}
+
+// ---- implicit function at the sample points and the iso-value ----------------------
+__device__ __forceinline__ void decode3s(int e, int depth, int& ix, int& iy, int& iz) {
+    const int o1 = 1 << (depth + 1);
+    ix = e & (o1 - 1);
+    iy = (e >> (depth + 1)) & (o1 - 1);
+    iz = e >> (2 * (depth + 1));
+}
+
+// chain value: every ancestor of `node` (itself first), 27 neighbours each, terms
+// ((x * Fx) * Fy) * Fz accumulated in order (mirrored by the oracle's float mode)
+__device__ __forceinline__ float chain_value(int node, float qx, float qy, float qz, int depth, const int* neigh,
+                                             size_t stride, const int* parent, const int* enc, const float* x) {
+    float val = 0.0f;
+    while (node != -1) {
+        for (int k = 0; k < 27; ++k) {
+            int nb = neigh[(size_t)k * stride + node];
+            if (nb == -1) continue;
+            int ix, iy, iz;
+            decode3s(enc[nb], depth, ix, iy, iz);
+            float t = __fmul_rn(x[nb], basis32(ix, qx));
+            t = __fmul_rn(t, basis32(iy, qy));
+            t = __fmul_rn(t, basis32(iz, qz));
+            val = __fadd_rn(val, t);
+        }
+        node = parent[node];
+    }
+    return val;
+}
+
+__global__ void __launch_bounds__(kBlock) k_point_values(const Counters* c, int depth, const float* px,
+                                                         const float* py, const float* pz, const int* point2node,
+                                                         const int* neigh, size_t stride, const int* parent,
+                                                         const int* enc, const float* x, float* out,
+                                                         double* block_sums) {
+    __shared__ double s_w[kBlock / 32];
+    const int n = c->n_points;
+    const int bD = c->level_base[depth];
+    double acc = 0.0;
+    PSR_GRID_STRIDE(i, n) {
+        float v = chain_value(bD + point2node[i], px[i], py[i], pz[i], depth, neigh, stride, parent, enc, x);
+        out[i] = v;
+        acc += (double)v;
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane_id() == 0) s_w[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < kBlock / 32; ++w) s += s_w[w];
+        block_sums[blockIdx.x] = s;
+    }
+}
+
+__global__ void k_iso_finalize(Counters* c, const double* block_sums, int nblocks) {
+    __shared__ double s_w[32];
+    double s = 0.0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) s += block_sums[b];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane_id() == 0) s_w[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s_w[w];
+        c->iso_sum = t;
+        c->iso = (c->n_points > 0) ? (float)(t / (double)c->n_points) : 0.0f;
+    }
+}
+
+static int g_cg_grid = 0;
+
+cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, int cg_max_iter) {
+    cudaStream_t s = ws.stream;
+    if (g_cg_grid == 0) {
+        int per_sm = 0;
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg, kCgBlock, 0);
+        if (e != cudaSuccess) return e;
+        if (per_sm < 1) return cudaErrorLaunchOutOfResources;
+        g_cg_grid = ws.num_sms * (per_sm < 2 ? per_sm : 2);
+    }
+    CgArgs a;
+    a.c = ws.cnt;
+    a.cw = ws.cnt;
+    a.depth = ws.depth;
+    a.ndepth = ws.ndepth;
+    a.neigh = ws.neigh;
+    a.stride = (size_t)ws.cap.nodes;
+    a.stencil = ws.stencil;
+    a.b = ws.divg;
+    a.x = ws.xsol;
+    a.r = ws.cg_r;
+    a.p = ws.cg_p;
+    a.ap = ws.cg_ap;
+    a.partial = ws.cg_partial;
+    float t2 = cg_tol * cg_tol;
+    a.tol2 = (double)t2;
+    // a fixed iteration count replaces the reference's max_iter (10000); the tolerance
+    // test of the loop is kept (mesh/solver/CGAlgorithm.cu:36)
+    a.max_iter = (cg_mode == 1 && cg_iters > 0) ? cg_iters : cg_max_iter;
+    void* args[] = {&a};
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(g_cg_grid);
+    cfg.blockDim = dim3(kCgBlock);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaError_t e = cudaLaunchKernelExC(&cfg, (const void*)k_cg, args);
+    if (e != cudaSuccess) return e;
+    // iso-value
+    const int nb = ws.num_sms * 4;
+    k_point_values<<<nb, kBlock, 0, s>>>(ws.cnt, ws.depth, ws.px, ws.py, ws.pz, ws.point2node, ws.neigh,
+                                         (size_t)ws.cap.nodes, ws.parent, ws.enc, ws.xsol, ws.point_val,
+                                         ws.iso_partial);
+    k_iso_finalize<<<1, 256, 0, s>>>(ws.cnt, ws.iso_partial, nb);
+    return cudaGetLastError();
+}
+
+}  // namespace psr

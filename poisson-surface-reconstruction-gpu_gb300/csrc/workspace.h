@@ -1,0 +1,159 @@
+// Device workspace of one reconstruction handle.  Every buffer is allocated once at
+// handle creation from the configured capacities; a reconstruction never allocates.
+//
+// HBM layout (structure of arrays, one array per field):
+//   points   : sorted positions / scaled normals / colours, 3 x N floats each
+//   nodes    : key, pidx, pnum, parent, first_child, didx, dnum, depth, enc (int32 x M),
+//              centre (3 x M floats), neighbour table [27][M] int32,
+//              vertex / edge / face back-pointers [8|12|6][M] int32
+//   build    : level-by-level staging arrays used while the octree is assembled
+//   mesh     : vertex / edge / face records, implicit values, output vertices/triangles
+#pragma once
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+#include "primitives.cuh"
+
+namespace psr {
+
+struct Caps {
+    int points;        // N cap
+    int nodes;         // M cap (all depths)
+    int dnodes;        // D-level node cap
+    int vertices;      // octree vertex records
+    int edges;         // D-level edge records
+    int faces;         // face records
+    int sub_nodes;     // subdivision-space nodes (all groups of one reconstruction)
+    int sub_dnodes;    // D-level subdivision nodes
+    int mesh_vertices; // output vertex cap
+    int mesh_tris;     // output triangle cap
+    int scan_tiles;    // tiles of the largest scan
+};
+
+// mesh-stage scratch
+struct MeshBufs {
+    int* ov_group;             // [8][cap.nodes]: group whose root redirects this child slot
+    int* ov_sub;               // [8][cap.nodes]: root slot inside that group
+    int* groups;               // group records (see mesh.cu)
+    int max_groups;
+    unsigned* edge_of_dnode;   // sub-edge prefix per D-level subdivision node
+    unsigned* tri_of_dnode;    // sub-triangle prefix per D-level subdivision node
+    unsigned* group_cross0;    // per group: crossing prefix at its first sub edge
+    int* parts;                // per output part: vertex start / count, triangle start / count
+    unsigned* kept_prefix;     // per staged vertex: kept vertices before it
+    int* misc;                 // [0] parts, [1] staged vertices, [2] staged triangles
+};
+
+struct Workspace {
+    MeshBufs mb;
+    Caps cap;
+    int depth;
+    Counters* cnt;          // device
+    Counters* cnt_host;     // pinned mirror for the final read-back
+    ScanScratch scan;
+    SortScratch sort;
+    unsigned* scan_total;   // device scratch (points into cnt)
+
+    // input staging (device copies of host inputs, or caller's device pointers)
+    float* in_xyz;
+    float* in_nrm;
+    uint8_t* in_rgb;
+
+    // sort
+    unsigned *code, *sidx;
+
+    // sorted points (SoA)
+    float *px, *py, *pz, *nx, *ny, *nz, *cr, *cg, *cb;
+    int* point2node;        // D-level local index of each sorted point
+    int* puid;              // unique-leaf id of each sorted point
+    unsigned* ucode;        // unique leaf codes
+    int* ufirst;            // first sorted point of each unique leaf (+ sentinel)
+    int* uslot;             // D-level slot of each unique leaf
+    unsigned* uaddr;        // group address of each unique leaf
+
+    // level build staging (levels D, D-1, ..., 0 appended in that order)
+    int *tkey, *tpidx, *tpnum, *tdidx, *tdnum, *tchild;
+    int* tparent_slot;      // per group of 8: slot of its father one level up
+    int *gkey, *gpidx, *gpnum, *gdidx, *gdnum;   // per-group aggregates of the current level
+    unsigned* gaddr;
+
+    // final node arrays
+    int *key, *pidx, *pnum, *parent, *first_child, *didx, *dnum, *ndepth, *enc;
+    float *ctr_x, *ctr_y, *ctr_z;
+    int* neigh;             // [27][cap.nodes]
+    int* node_vtx;          // [8][cap.nodes]
+    int* node_edge;         // [12][cap.nodes]
+    int* node_face;         // [6][cap.nodes]
+
+    // function tables (FP64, res x res) and per-depth stencil coefficients
+    int res;
+    double* dff;            // d/dx F_i . F_j  (index i + res * j)
+    float* stencil;         // [D+1][27] Laplacian coefficients (0 where dropped)
+
+    // field / solve
+    float* vfield;          // 3 x dnodes (SoA: x block, y block, z block)
+    float* divg;            // M
+    float* xsol;            // M
+    float *cg_r, *cg_p, *cg_ap;
+    double* cg_partial;     // per-CTA per-depth partial sums
+    float* point_val;       // N
+    double* iso_partial;
+
+    // mesh geometry
+    unsigned char* vmask;   // per node: owned corner mask (8 bits)
+    unsigned short* emask16;   // per D node: owned edge mask (12 bits)
+    unsigned char* fmask;   // per node: owned face mask (6 bits)
+    float *v_x, *v_y, *v_z; // vertex positions
+    int *v_owner, *v_kind, *v_depth;
+    int *e_owner, *e_kind;
+    int *f_owner, *f_kind, *f_hasparent;
+    float* vvalue;          // implicit value - iso at every vertex
+    unsigned* e_cross;      // per edge: staged vertex index of its crossing (exclusive scan)
+    int* cube_class;        // per D node
+    int* face_hit;          // per face: surface-edge intersection
+
+    // subdivision
+    int* sub_root;          // node index of each root (node order)
+    int* sub_root_depth;
+    int* node_subslot;      // per node: index of the root in its group's array
+    int* node_subgroup;     // per node: group id
+    // subdivision-space nodes of all groups (SoA)
+    int *s_key, *s_parent, *s_first_child, *s_neigh, *s_depth, *s_root;   // s_neigh: [27][cap.sub_nodes]
+    int* s_group;
+    float *s_cx, *s_cy, *s_cz;
+    int *s_vtx, *s_edge;    // [8|12][cap.sub_dnodes] for D-level subdivision nodes
+    unsigned char* s_vmask;
+    unsigned short* s_emask;
+    float *sv_x, *sv_y, *sv_z;
+    int *sv_owner, *sv_kind;
+    float* sv_value;
+    int *se_owner, *se_kind;
+    unsigned* se_cross;
+    int* s_cube_class;
+
+    // output (device)
+    float* mesh_v;          // 3 x mesh_vertices
+    int* mesh_t;            // 3 x mesh_tris
+    float* mesh_c;          // colours
+    float* mesh_n;          // normals
+    double* nacc;           // per output vertex normal accumulator (3 doubles)
+    int* vcount;            // per output vertex triangle count
+    int* cell_start;        // sample grid for the colour search
+
+    // staging for the two-phase insertion of each mesh part
+    float* part_v;          // 3 x cap
+    int* part_t;
+    int part_cap_v, part_cap_t;
+
+    cudaStream_t stream;
+    int num_sms;
+};
+
+// stage entry points (each issues kernels on ws.stream; no host synchronisation)
+cudaError_t octree_build(Workspace& ws, int n_points_host_hint);
+cudaError_t field_build(Workspace& ws);
+cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, int cg_max_iter);
+cudaError_t mesh_build(Workspace& ws);
+cudaError_t transfer_build(Workspace& ws, int with_colour, int with_normals);
+
+}  // namespace psr

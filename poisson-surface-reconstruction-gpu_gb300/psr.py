@@ -1,0 +1,231 @@
+"""Python mirror of the reference's PoissonReconstruction host API over the C ABI.
+
+The reference class (mesh/PoissonReconstruction.h:63-184) owns the pipeline and exposes
+``SolvePoissionReconstructionMesh`` (spelling kept) plus mesh getters
+(mesh/ComputeTriangleIndices.h:331-342).  This module loads the in-tree libpsr.so built
+for sm_103a (include/psr/psr.h) with ctypes.  There is no CPU fallback: if the library
+is missing or no GPU is present the calls raise.
+"""
+import ctypes
+import os
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "libpsr.so"
+
+PSR_OK, PSR_OUT_OF_CAPACITY, PSR_INVALID_INPUT, PSR_NONCONVERGED, PSR_DEVICE_TIMEOUT, PSR_CUDA_ERROR = range(6)
+PSR_HOST, PSR_DEVICE = 0, 1
+
+# every function declared in include/psr/psr.h
+EXPORTED = ["psr_config_default", "psr_create", "psr_destroy", "psr_reconstruct", "psr_get_stats",
+            "psr_debug_array", "psr_status_string", "psr_last_error"]
+
+
+class PsrConfig(ctypes.Structure):
+    _fields_ = [("max_depth", ctypes.c_int), ("max_points", ctypes.c_int), ("max_triangles", ctypes.c_int),
+                ("max_mesh_vertices", ctypes.c_int), ("max_nodes", ctypes.c_int),
+                ("max_subdivision_nodes", ctypes.c_int), ("bbox_scale", ctypes.c_float),
+                ("cg_max_iterations", ctypes.c_int), ("cg_tolerance", ctypes.c_float),
+                ("compute_colors", ctypes.c_int), ("compute_normals", ctypes.c_int), ("device", ctypes.c_int)]
+
+
+class PsrPoints(ctypes.Structure):
+    _fields_ = [("xyz", ctypes.c_void_p), ("normals", ctypes.c_void_p), ("rgb", ctypes.c_void_p),
+                ("count", ctypes.c_int), ("location", ctypes.c_int)]
+
+
+class PsrOptions(ctypes.Structure):
+    _fields_ = [("depth", ctypes.c_int), ("cg_iterations", ctypes.c_int)]
+
+
+class PsrMesh(ctypes.Structure):
+    _fields_ = [("vertices", ctypes.c_void_p), ("triangles", ctypes.c_void_p), ("colors", ctypes.c_void_p),
+                ("normals", ctypes.c_void_p), ("vertex_capacity", ctypes.c_int),
+                ("triangle_capacity", ctypes.c_int), ("location", ctypes.c_int), ("vertex_count", ctypes.c_int),
+                ("triangle_count", ctypes.c_int), ("center", ctypes.c_float * 3), ("scale", ctypes.c_float)]
+
+
+class PsrStats(ctypes.Structure):
+    _fields_ = [("points", ctypes.c_int), ("unique_leaves", ctypes.c_int), ("nodes", ctypes.c_int),
+                ("depth", ctypes.c_int), ("level_count", ctypes.c_int * 10), ("vertices", ctypes.c_int),
+                ("edges", ctypes.c_int), ("faces", ctypes.c_int), ("crossings", ctypes.c_int),
+                ("triangles", ctypes.c_int), ("subdivision_roots", ctypes.c_int),
+                ("subdivision_nodes", ctypes.c_int), ("mesh_vertices", ctypes.c_int),
+                ("mesh_triangles", ctypes.c_int), ("cg_iterations", ctypes.c_int * 10),
+                ("cg_residual", ctypes.c_double * 10), ("iso_value", ctypes.c_float),
+                ("error_bits", ctypes.c_uint), ("stage_ms", ctypes.c_float * 6)]
+
+
+_lib = None
+
+
+def load_library(path=None):
+    """Load libpsr.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"{p} is missing: build it first (python -c 'import __graft_entry__ as g; g.build()')")
+    L = ctypes.CDLL(str(p))
+    L.psr_config_default.argtypes = [ctypes.POINTER(PsrConfig)]
+    L.psr_create.argtypes = [ctypes.POINTER(PsrConfig), ctypes.POINTER(ctypes.c_void_p)]
+    L.psr_destroy.argtypes = [ctypes.c_void_p]
+    L.psr_reconstruct.argtypes = [ctypes.c_void_p, ctypes.POINTER(PsrPoints), ctypes.POINTER(PsrOptions),
+                                  ctypes.POINTER(PsrMesh), ctypes.c_void_p]
+    L.psr_get_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(PsrStats)]
+    L.psr_debug_array.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_size_t,
+                                  ctypes.POINTER(ctypes.c_size_t)]
+    L.psr_status_string.argtypes = [ctypes.c_int]
+    L.psr_status_string.restype = ctypes.c_char_p
+    L.psr_last_error.argtypes = [ctypes.c_void_p]
+    L.psr_last_error.restype = ctypes.c_char_p
+    for fn in EXPORTED:
+        if fn not in ("psr_status_string", "psr_last_error"):
+            getattr(L, fn).restype = ctypes.c_int
+    if path is None:
+        _lib = L
+    return L
+
+
+class PsrError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"{message} (status {status})")
+        self.status = status
+
+
+class Mesh:
+    """Output of one reconstruction (unit-cube vertices, int32 triangles)."""
+
+    def __init__(self, vertices, triangles, colors, normals, center, scale):
+        self.vertices = vertices
+        self.triangles = triangles
+        self.colors = colors
+        self.normals = normals
+        self.center = center
+        self.scale = scale
+
+    def world_vertices(self):
+        return self.center[None, :] + self.vertices * self.scale
+
+
+def default_config():
+    cfg = PsrConfig()
+    load_library().psr_config_default(ctypes.byref(cfg))
+    return cfg
+
+
+class PoissonReconstruction:
+    """Drop-in mirror of SparseSurfelFusion::PoissonReconstruction for the GPU path."""
+
+    def __init__(self, max_depth=7, max_points=300000, max_triangles=1000000, max_mesh_vertices=300000,
+                 compute_colors=False, compute_normals=False, cg_tolerance=1e-5, cg_max_iterations=10000,
+                 max_nodes=0, max_subdivision_nodes=0, device=0):
+        self._lib = load_library()
+        cfg = default_config()
+        cfg.max_depth = max_depth
+        cfg.max_points = max_points
+        cfg.max_triangles = max_triangles
+        cfg.max_mesh_vertices = max_mesh_vertices
+        cfg.compute_colors = int(compute_colors)
+        cfg.compute_normals = int(compute_normals)
+        cfg.cg_tolerance = cg_tolerance
+        cfg.cg_max_iterations = cg_max_iterations
+        cfg.max_nodes = max_nodes
+        cfg.max_subdivision_nodes = max_subdivision_nodes
+        cfg.device = device
+        self.config = cfg
+        h = ctypes.c_void_p()
+        st = self._lib.psr_create(ctypes.byref(cfg), ctypes.byref(h))
+        if st != PSR_OK:
+            raise PsrError(st, "psr_create failed")
+        self._h = h
+        self._mesh = None
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.psr_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _error(self, st, what):
+        msg = self._lib.psr_last_error(self._h).decode()
+        return PsrError(st, f"{what}: {self._lib.psr_status_string(st).decode()}: {msg}")
+
+    def SolvePoissionReconstructionMesh(self, xyz, normals, rgb=None, depth=0, cg_iterations=0):
+        """Reconstruct from host arrays; returns a Mesh (also kept for the getters)."""
+        xyz = np.ascontiguousarray(xyz, np.float32)
+        normals = np.ascontiguousarray(normals, np.float32)
+        if rgb is not None:
+            rgb = np.ascontiguousarray(rgb, np.uint8)
+        n = int(xyz.shape[0])
+        pts = PsrPoints(xyz.ctypes.data, normals.ctypes.data, rgb.ctypes.data if rgb is not None else None, n,
+                        PSR_HOST)
+        opt = PsrOptions(int(depth), int(cg_iterations))
+        vcap = int(self.config.max_mesh_vertices)
+        tcap = int(self.config.max_triangles)
+        v = np.empty((vcap, 3), np.float32)
+        t = np.empty((tcap, 3), np.int32)
+        c = np.empty((vcap, 3), np.float32) if self.config.compute_colors else None
+        nm = np.empty((vcap, 3), np.float32) if self.config.compute_normals else None
+        mesh = PsrMesh(v.ctypes.data, t.ctypes.data, c.ctypes.data if c is not None else None,
+                       nm.ctypes.data if nm is not None else None, vcap, tcap, PSR_HOST, 0, 0)
+        st = self._lib.psr_reconstruct(self._h, ctypes.byref(pts), ctypes.byref(opt), ctypes.byref(mesh), None)
+        if st != PSR_OK:
+            raise self._error(st, "psr_reconstruct")
+        nv, nt = mesh.vertex_count, mesh.triangle_count
+        self._mesh = Mesh(v[:nv].copy(), t[:nt].copy(), None if c is None else c[:nv].copy(),
+                          None if nm is None else nm[:nv].copy(), np.array(mesh.center[:], np.float32),
+                          float(mesh.scale))
+        return self._mesh
+
+    reconstruct = SolvePoissionReconstructionMesh
+
+    def reconstruct_device(self, xyz_ptr, nrm_ptr, rgb_ptr, n, depth=0, cg_iterations=0, stream=None,
+                           out=None):
+        """Reconstruct from device pointers (e.g. torch CUDA tensors' data_ptr())."""
+        pts = PsrPoints(xyz_ptr, nrm_ptr, rgb_ptr, int(n), PSR_DEVICE)
+        opt = PsrOptions(int(depth), int(cg_iterations))
+        mesh = out if out is not None else PsrMesh(None, None, None, None, 0, 0, PSR_HOST, 0, 0)
+        st = self._lib.psr_reconstruct(self._h, ctypes.byref(pts), ctypes.byref(opt), ctypes.byref(mesh), stream)
+        if st != PSR_OK and not (st == PSR_OUT_OF_CAPACITY and out is None):
+            raise self._error(st, "psr_reconstruct")
+        return mesh
+
+    def GetRebuildMeshVertices(self):
+        return None if self._mesh is None else self._mesh.vertices
+
+    def GetRebuildMeshTriangleIndices(self):
+        return None if self._mesh is None else self._mesh.triangles
+
+    def stats(self):
+        s = PsrStats()
+        self._lib.psr_get_stats(self._h, ctypes.byref(s))
+        return s
+
+    def debug(self, name, dtype=np.int32, rows=None):
+        """Copy an internal device array of the last reconstruction to host."""
+        nb = ctypes.c_size_t()
+        st = self._lib.psr_debug_array(self._h, name.encode(), None, 0, ctypes.byref(nb))
+        if st != PSR_OK:
+            raise self._error(st, f"psr_debug_array({name})")
+        buf = np.empty(nb.value // np.dtype(dtype).itemsize, dtype)
+        st = self._lib.psr_debug_array(self._h, name.encode(), buf.ctypes.data, buf.nbytes, ctypes.byref(nb))
+        if st != PSR_OK:
+            raise self._error(st, f"psr_debug_array({name})")
+        if rows:
+            buf = buf.reshape(rows, -1)
+        return buf

@@ -1,0 +1,55 @@
+"""C ABI checks that need no GPU: the library loads and exports every declared entry."""
+import ctypes
+import re
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+HEADER = ROOT / "include" / "psr" / "psr.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    return sorted(set(re.findall(r"^\s*(?:psr_status|const char\*)\s+(psr_\w+)\(", text, re.M)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import psr
+    if not psr.LIB_PATH.exists():
+        import build
+        build.build()
+    return ctypes.CDLL(str(psr.LIB_PATH))
+
+
+def test_library_exports_every_declared_symbol(lib):
+    names = declared_functions()
+    assert len(names) >= 8
+    for n in names:
+        assert hasattr(lib, n), n
+
+
+def test_python_mirror_covers_header():
+    import psr
+    assert sorted(psr.EXPORTED) == declared_functions()
+
+
+def test_config_defaults_without_gpu(lib):
+    import psr
+    cfg = psr.PsrConfig()
+    lib.psr_config_default.argtypes = [ctypes.POINTER(psr.PsrConfig)]
+    assert lib.psr_config_default(ctypes.byref(cfg)) == 0
+    # reference compile-time caps (base/GlobalConfigs.h:7-8,34)
+    assert cfg.max_depth == 7 and cfg.max_points == 300000 and cfg.max_triangles == 1000000
+    assert abs(cfg.bbox_scale - 1.25) < 1e-7 and cfg.cg_max_iterations == 10000
+    lib.psr_status_string.restype = ctypes.c_char_p
+    assert lib.psr_status_string(1) == b"out of capacity"
+
+
+def test_struct_layouts_match_header():
+    import psr
+    # psr_config: 12 x 4-byte fields
+    assert ctypes.sizeof(psr.PsrConfig) == 48
+    assert ctypes.sizeof(psr.PsrPoints) == 32
+    assert ctypes.sizeof(psr.PsrOptions) == 8
