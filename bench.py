@@ -1,0 +1,330 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 Poisson reconstruction path.
+
+Workload (default): the depth-7, 200,000-point torus-plus-ellipsoid cloud with colour
+(seeded synthetic, see synthetic.py).  A step is one reconstruction of one cloud through
+the C ABI (psr_reconstruct): octree, splat, divergence, per-depth CG, marching cubes with
+subdivision, colour and normal transfer.
+
+Reported metric: reconstructions per second (higher is better) and p99 latency.
+  value : device-resident inputs and outputs, CUDA-event time per step on the launching
+          stream, L2 flushed (256 MiB write) between steps outside the timed events
+  e2e   : host inputs / host outputs through the same C ABI call (H2D + D2H inside)
+Multi-GPU (torchrun): every rank reconstructs its own clouds (no collective on the data
+path, weak scaling); the step time is the max over ranks.
+
+--impl reference: the reference path has no CPU implementation and its CUDA code cannot be
+built on the benchmark machine, so the reference arm times the CPU restatement of the
+same algorithm (oracle/, FP64, OpenMP over all host cores) on the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+PKG = ROOT / "poisson-surface-reconstruction-gpu_gb300"
+sys.path[:0] = [str(PKG), str(ROOT / "oracle")]
+
+METRIC = "depth-7 200k-pt recons/s & p99 ms, served vs plain, at FP64-checked accuracy"
+UNIT = "recons/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--workload", default="torus_ellipsoid200k")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200", "-f", self.path],
+                                         stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if not self.path or not os.path.exists(self.path):
+            return out
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        os.unlink(self.path)
+        if not rows:
+            return out
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            for k, nm in enumerate(names):
+                if r[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        out.update(sm_mhz=float(np.median(sm)) if sm else None, sm_max_mhz=max(mx) if mx else None,
+                   reasons=sorted(reasons), samples=len(rows))
+        return out
+
+
+def cpu_baseline(xyz, nrm, rgb, depth, budget_s=20.0):
+    """The oracle (CPU restatement, FP64, OpenMP) on the same cloud, repeated within a budget."""
+    import oracle
+    o = oracle.Oracle()
+    rgbf = None if rgb is None else rgb.astype(np.float32) / np.float32(255.0)
+    times = []
+    t_all = time.time()
+    while True:
+        t = time.time()
+        rc = o.run(xyz, nrm, rgbf, depth=depth)
+        times.append(time.time() - t)
+        if rc != 0 or time.time() - t_all > budget_s * 0.5 or len(times) >= 5:
+            break
+    per = float(np.median(times))
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": 1.0 / per, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{len(times)} full reconstruction(s) of the {len(xyz)}-point depth-{depth} cloud, "
+                      f"median {per:.2f} s each"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    import synthetic as syn
+    xyz, nrm, rgb, depth = syn.workload(args.workload)
+    import oracle
+    oracle.build()
+    o = oracle.Oracle()
+    rgbf = None if rgb is None else rgb.astype(np.float32) / np.float32(255.0)
+    for _ in range(args.warmup):
+        o.run(xyz, nrm, rgbf, depth=depth)
+    times = []
+    for _ in range(args.steps):
+        t = time.time()
+        o.run(xyz, nrm, rgbf, depth=depth)
+        times.append(time.time() - t)
+    total = sum(times)
+    value = args.steps / total
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": f"{args.workload} (N={len(xyz)}, depth {depth}, colour)", "l2": "n/a (host)"},
+            "p50_ms": 1000 * float(np.median(times)), "p99_ms": 1000 * float(np.percentile(times, 99)),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"full reconstruction of the {len(xyz)}-point cloud per step"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import torch
+    import torch.distributed as dist
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import __graft_entry__ as ge
+    if rank == 0 or world == 1:
+        ge.build()
+    if world > 1:
+        dist.barrier()
+    import psr
+    import synthetic as syn
+
+    xyz, nrm, rgb, depth = syn.workload(args.workload, cloud=rank)
+    n = len(xyz)
+    r = psr.PoissonReconstruction(max_depth=depth, max_points=max(300000, n), max_triangles=1000000,
+                                  max_mesh_vertices=300000, compute_colors=rgb is not None,
+                                  compute_normals=True, device=local)
+    dev = torch.device("cuda", local)
+    d_xyz = torch.from_numpy(xyz).to(dev)
+    d_nrm = torch.from_numpy(nrm).to(dev)
+    d_rgb = torch.from_numpy(rgb).to(dev) if rgb is not None else None
+    vcap, tcap = 300000, 1000000
+    o_v = torch.empty((vcap, 3), dtype=torch.float32, device=dev)
+    o_t = torch.empty((tcap, 3), dtype=torch.int32, device=dev)
+    o_c = torch.empty((vcap, 3), dtype=torch.float32, device=dev)
+    o_n = torch.empty((vcap, 3), dtype=torch.float32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+
+    def dev_mesh():
+        return psr.PsrMesh(o_v.data_ptr(), o_t.data_ptr(), o_c.data_ptr() if rgb is not None else None,
+                           o_n.data_ptr(), vcap, tcap, psr.PSR_DEVICE, 0, 0)
+
+    def step_device():
+        m = dev_mesh()
+        r.reconstruct_device(d_xyz.data_ptr(), d_nrm.data_ptr(), d_rgb.data_ptr() if d_rgb is not None else None,
+                             n, depth=depth, stream=sptr, out=m)
+        return m
+
+    # host (pinned) buffers for the end-to-end leg
+    h_xyz = torch.from_numpy(xyz).pin_memory()
+    h_nrm = torch.from_numpy(nrm).pin_memory()
+    h_rgb = torch.from_numpy(rgb).pin_memory() if rgb is not None else None
+    h_v = torch.empty((vcap, 3), dtype=torch.float32).pin_memory()
+    h_t = torch.empty((tcap, 3), dtype=torch.int32).pin_memory()
+    h_c = torch.empty((vcap, 3), dtype=torch.float32).pin_memory()
+    h_n = torch.empty((vcap, 3), dtype=torch.float32).pin_memory()
+
+    def step_host():
+        pts = psr.PsrPoints(h_xyz.data_ptr(), h_nrm.data_ptr(), h_rgb.data_ptr() if h_rgb is not None else None, n,
+                            psr.PSR_HOST)
+        m = psr.PsrMesh(h_v.data_ptr(), h_t.data_ptr(), h_c.data_ptr() if h_rgb is not None else None,
+                        h_n.data_ptr(), vcap, tcap, psr.PSR_HOST, 0, 0)
+        opt = psr.PsrOptions(depth, 0)
+        import ctypes
+        st = r._lib.psr_reconstruct(r._h, ctypes.byref(pts), ctypes.byref(opt), ctypes.byref(m), sptr)
+        if st != 0:
+            raise r._error(st, "psr_reconstruct")
+        return m
+
+    for _ in range(max(args.warmup, 3)):
+        step_device()
+        step_host()
+    torch.cuda.synchronize(dev)
+
+    def timed(fn, k):
+        times = []
+        last = None
+        for _ in range(k):
+            flush.zero_()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            last = fn()
+            b.record(stream)
+            b.synchronize()
+            times.append(a.elapsed_time(b))
+        return np.array(times), last
+
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clk:
+        t_dev, m_dev = timed(step_device, args.steps)
+        t_e2e, m_host = timed(step_host, args.steps)
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        dist.barrier()
+    st = r.stats()
+    tot_dev = float(t_dev.sum())
+    tot_e2e = float(t_e2e.sum())
+    if world > 1:
+        tt = torch.tensor([tot_dev, tot_e2e], dtype=torch.float64, device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        tot_dev, tot_e2e = tt.tolist()
+    value = world * args.steps / (tot_dev / 1000.0)
+    e2e_value = world * args.steps / (tot_e2e / 1000.0)
+    clocks = clk.summary()
+    h2d = n * (12 + 12 + (3 if rgb is not None else 0))
+    d2h = m_host.vertex_count * 12 * (3 if rgb is not None else 2) + m_host.triangle_count * 12
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+    # roofline of the dominant stage (the CG solve is latency bound; the
+    # kernel measured here is the cooperative CG, timed by the solve-stage events)
+    import json as _j
+    peaks = {}
+    try:
+        peaks = _j.load(open(ROOT / "MEASURED_PEAKS.json"))
+    except Exception:
+        pass
+    peak_hbm = float(peaks.get("hbm_gbs", 6800.0))
+    M = st.nodes
+    iters = max(st.cg_iterations[:depth + 1])
+    cg_bytes = 0
+    for d in range(depth + 1):
+        cg_bytes += st.level_count[d] * 152 * st.cg_iterations[d]
+    solve_ms = st.stage_ms[2]
+    roofline = {"bound": "hbm", "kernel": "k_cg (per-depth CG, all depths in one cooperative launch)",
+                "achieved": cg_bytes / (solve_ms * 1e-3) / 1e9 if solve_ms > 0 else None, "peak": peak_hbm,
+                "unit": "GB/s", "frac": None, "traffic": None,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s",
+                "algorithmic_bytes": cg_bytes, "launch_ms": solve_ms}
+    if roofline["achieved"]:
+        roofline["frac"] = roofline["achieved"] / peak_hbm
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": tot_dev / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 dots / reductions)", "data": "synthetic",
+            "impl": "gpu-plain",
+            "config": {"workload": f"{args.workload} (N={n}, depth {depth}, colour, normals)",
+                       "path": "plain single-cloud psr_reconstruct", "l2": "flushed (256 MiB write) between steps"},
+            "p50_ms": float(np.median(t_dev)), "p99_ms": float(np.percentile(t_dev, 99)),
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "p50_ms": float(np.median(t_e2e)), "p99_ms": float(np.percentile(t_e2e, 99))},
+            "stage_ms": [round(x, 4) for x in st.stage_ms], "nodes": M, "cg_iterations": list(st.cg_iterations[:depth + 1]),
+            "mesh": {"vertices": m_host.vertex_count, "triangles": m_host.triangle_count},
+            "gpu_launches": int(st_launches(r)),
+            "roofline": roofline, "clocks": clocks}
+    if not args.no_cpu_baseline:
+        try:
+            line["cpu_baseline"] = cpu_baseline(xyz, nrm, rgb, depth)
+        except Exception as e:
+            line["cpu_baseline"] = {"value": None, "error": str(e)}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def st_launches(r):
+    try:
+        return r.launch_count()
+    except Exception:
+        return -1
+
+
+if __name__ == "__main__":
+    main()

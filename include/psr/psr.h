@@ -93,6 +93,8 @@ typedef struct psr_stats {
     float iso_value;
     unsigned error_bits;
     float stage_ms[6];     /* octree, field, solve, mesh, transfer, total (device time) */
+    int kernel_launches;   /* kernels launched by the call (CUDA-graph kernel nodes) */
+    int graph_replay;      /* 1 when the call replayed a captured CUDA graph */
 } psr_stats;
 
 typedef struct psr_handle psr_handle;

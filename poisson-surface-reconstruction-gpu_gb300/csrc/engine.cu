@@ -32,9 +32,19 @@ struct DebugArray {
     int mult;        // elements per counted item
 };
 
+struct GraphEntry {
+    cudaGraphExec_t exec = nullptr;
+    int kernels = 0;
+};
+
 struct psr_handle {
     psr_config cfg;
     Workspace ws;
+    int* h_params = nullptr;   // pinned: written by the host, copied to ws.d_params per call
+    std::map<long long, GraphEntry> graphs;
+    int use_graphs = 1;
+    int last_kernels = 0;
+    int last_graph = 0;
     void* arena = nullptr;
     size_t arena_bytes = 0;
     cudaStream_t own_stream = nullptr;
@@ -244,6 +254,7 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     A.add(ws.mb.parts, 4 * (size_t)nodes + 8);
     A.add(ws.mb.kept_prefix, (size_t)ws.part_cap_v);
     A.add(ws.mb.misc, 16);
+    A.add(ws.d_params, 16);
 
     e = cudaMalloc(&h->arena, A.bytes);
     if (e != cudaSuccess) { psr_status st = cuda_fail(h, e, "cudaMalloc workspace"); delete h; return st; }
@@ -253,6 +264,7 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     ws.sort.max_tiles = sort_tiles;
     ws.sort.scan = ws.scan;   // sort shares the scan scratch (scans are sequential on one stream)
     e = cudaMallocHost(&ws.cnt_host, sizeof(Counters));
+    if (e == cudaSuccess) e = cudaMallocHost(&h->h_params, 16 * sizeof(int));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
     for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&h->ev[i]);
     // tables
@@ -269,6 +281,12 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
         e = cudaMemcpy(ws.dff, dff.data(), dff.size() * sizeof(double), cudaMemcpyHostToDevice);
         if (e == cudaSuccess) e = cudaMemcpy(ws.stencil, st.data(), st.size() * sizeof(float), cudaMemcpyHostToDevice);
     }
+    if (e == cudaSuccess) {
+        prepare_launch_configs(ws);
+        e = cudaGetLastError();
+    }
+    const char* env = getenv("PSR_NO_GRAPH");
+    if (env && env[0] == '1') h->use_graphs = 0;
     if (e != cudaSuccess) {
         psr_status st = cuda_fail(h, e, "psr_create");
         psr_destroy(h);
@@ -280,8 +298,10 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
 
 psr_status psr_destroy(psr_handle* h) {
     if (!h) return PSR_OK;
+    for (auto& g : h->graphs) if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
     if (h->arena) cudaFree(h->arena);
     if (h->ws.cnt_host) cudaFreeHost(h->ws.cnt_host);
+    if (h->h_params) cudaFreeHost(h->h_params);
     for (int i = 0; i < 6; ++i) if (h->ev[i]) cudaEventDestroy(h->ev[i]);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
@@ -312,21 +332,77 @@ psr_status psr_reconstruct(psr_handle* h, const psr_points* pts, const psr_optio
     const bool has_rgb = pts->rgb != nullptr;
     if (e == cudaSuccess && has_rgb) e = cudaMemcpyAsync(ws.in_rgb, pts->rgb, 3 * (size_t)n, kind, s);
     if (e != cudaSuccess) return cuda_fail(h, e, "input copy");
-    uint8_t* saved_rgb = ws.in_rgb;
-    if (!has_rgb) ws.in_rgb = nullptr;
-    cudaEventRecord(h->ev[0], s);
-    e = octree_build(ws, n);
-    if (e == cudaSuccess) { cudaEventRecord(h->ev[1], s); e = field_build(ws); }
-    if (e == cudaSuccess) {
-        cudaEventRecord(h->ev[2], s);
-        e = solve_build(ws, cg_iters > 0 ? 1 : 0, cg_iters, h->cfg.cg_tolerance, h->cfg.cg_max_iterations);
-    }
-    if (e == cudaSuccess) { cudaEventRecord(h->ev[3], s); e = mesh_build(ws); }
     const int want_colour = h->cfg.compute_colors && mesh->colors;
     const int want_normals = h->cfg.compute_normals && mesh->normals;
-    if (e == cudaSuccess) { cudaEventRecord(h->ev[4], s); e = transfer_build(ws, want_colour, want_normals); }
+    h->h_params[0] = n;
+    e = cudaMemcpyAsync(ws.d_params, h->h_params, sizeof(int), cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return cuda_fail(h, e, "parameter copy");
+    uint8_t* saved_rgb = ws.in_rgb;
+    if (!has_rgb) ws.in_rgb = nullptr;
+    // the whole pipeline: captured once per (depth, options) into a CUDA graph, replayed after
+    auto issue = [&](cudaStream_t qs) -> cudaError_t {
+        ws.stream = qs;
+        cudaError_t q = cudaEventRecordWithFlags(h->ev[0], qs, cudaEventRecordExternal);
+        if (q == cudaSuccess) q = octree_build(ws);
+        if (q == cudaSuccess) q = cudaEventRecordWithFlags(h->ev[1], qs, cudaEventRecordExternal);
+        if (q == cudaSuccess) q = field_build(ws);
+        if (q == cudaSuccess) q = cudaEventRecordWithFlags(h->ev[2], qs, cudaEventRecordExternal);
+        if (q == cudaSuccess)
+            q = solve_build(ws, cg_iters > 0 ? 1 : 0, cg_iters, h->cfg.cg_tolerance, h->cfg.cg_max_iterations);
+        if (q == cudaSuccess) q = cudaEventRecordWithFlags(h->ev[3], qs, cudaEventRecordExternal);
+        if (q == cudaSuccess) q = mesh_build(ws);
+        if (q == cudaSuccess) q = cudaEventRecordWithFlags(h->ev[4], qs, cudaEventRecordExternal);
+        if (q == cudaSuccess) q = transfer_build(ws, want_colour, want_normals);
+        if (q == cudaSuccess) q = cudaEventRecordWithFlags(h->ev[5], qs, cudaEventRecordExternal);
+        return q;
+    };
+    const long long gkey = ((long long)depth << 40) | ((long long)cg_iters << 8) | (want_colour << 2) |
+                           (want_normals << 1) | (has_rgb ? 1 : 0);
+    h->last_graph = 0;
+    if (h->use_graphs) {
+        auto it = h->graphs.find(gkey);
+        if (it == h->graphs.end()) {
+            cudaGraph_t graph = nullptr;
+            GraphEntry ge;
+            cudaError_t q = cudaStreamBeginCapture(h->own_stream, cudaStreamCaptureModeThreadLocal);
+            if (q == cudaSuccess) {
+                cudaError_t qi = issue(h->own_stream);
+                q = cudaStreamEndCapture(h->own_stream, &graph);
+                if (qi != cudaSuccess) q = qi;
+            }
+            if (q == cudaSuccess) q = cudaGraphInstantiate(&ge.exec, graph, 0);
+            if (q == cudaSuccess) {
+                size_t nn = 0;
+                cudaGraphGetNodes(graph, nullptr, &nn);
+                std::vector<cudaGraphNode_t> nodes(nn);
+                cudaGraphGetNodes(graph, nodes.data(), &nn);
+                for (auto nd : nodes) {
+                    cudaGraphNodeType t;
+                    if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ge.kernels++;
+                }
+            }
+            if (graph) cudaGraphDestroy(graph);
+            if (q != cudaSuccess) {
+                (void)cudaGetLastError();
+                h->use_graphs = 0;   // capture not available: run the stages directly from now on
+                if (ge.exec) cudaGraphExecDestroy(ge.exec);
+            } else {
+                it = h->graphs.emplace(gkey, ge).first;
+            }
+        }
+        if (h->use_graphs) {
+            e = cudaGraphLaunch(it->second.exec, s);
+            h->last_kernels = it->second.kernels;
+            h->last_graph = 1;
+        }
+    }
+    if (!h->use_graphs) {
+        e = issue(s);
+        h->last_kernels = -1;
+    }
     ws.in_rgb = saved_rgb;
-    if (e == cudaSuccess) { cudaEventRecord(h->ev[5], s); e = cudaMemcpyAsync(ws.cnt_host, ws.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, s); }
+    ws.stream = s;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ws.cnt_host, ws.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cuda_fail(h, e, "reconstruct");
     Counters& c = *ws.cnt_host;
@@ -343,6 +419,8 @@ psr_status psr_reconstruct(psr_handle* h, const psr_points* pts, const psr_optio
     st.mesh_vertices = c.n_mesh_vertices; st.mesh_triangles = c.n_mesh_triangles;
     st.iso_value = c.iso;
     st.error_bits = c.error;
+    st.kernel_launches = h->last_kernels;
+    st.graph_replay = h->last_graph;
     for (int i = 0; i < 5; ++i) cudaEventElapsedTime(&st.stage_ms[i], h->ev[i], h->ev[i + 1]);
     cudaEventElapsedTime(&st.stage_ms[5], h->ev[0], h->ev[5]);
     if (c.error & kErrInvalid) return fail(h, PSR_INVALID_INPUT, "non-finite input or malformed octree");

@@ -13,8 +13,9 @@ namespace psr {
 // ------------------------------------------------------------------------------------
 // bounding box (mesh/BuildOctree.cu:51-133) and normalisation parameters (:619-631)
 // ------------------------------------------------------------------------------------
-__global__ void k_reset_counters(Counters* c, int n_points) {
+__global__ void k_reset_counters(Counters* c, const int* params) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
+        const int n_points = params[0];
         char* p = (char*)c;
         for (size_t i = 0; i < sizeof(Counters); ++i) p[i] = 0;
         c->n_points = n_points;
@@ -410,14 +411,14 @@ static inline int grid_for(const Workspace& ws, long long work) {
     return (int)(g < 1 ? 1 : g);
 }
 
-cudaError_t octree_build(Workspace& ws, int n_points) {
+cudaError_t octree_build(Workspace& ws) {
     cudaStream_t s = ws.stream;
     const int D = ws.depth;
     Counters* c = ws.cnt;
     unsigned* err = &c->error;
     unsigned* total = (unsigned*)&c->scan_total;
-    const int gp = grid_for(ws, n_points);
-    k_reset_counters<<<1, 1, 0, s>>>(c, n_points);
+    const int gp = grid_for(ws, ws.cap.points);
+    k_reset_counters<<<1, 1, 0, s>>>(c, ws.d_params);
     k_bbox<<<gp, kBlock, 0, s>>>(ws.in_xyz, ws.in_nrm, c);
     k_bbox_finalize<<<1, 1, 0, s>>>(c, 1.25f);
     k_encode<<<gp, kBlock, 0, s>>>(ws.in_xyz, c, D, ws.code, ws.sidx);

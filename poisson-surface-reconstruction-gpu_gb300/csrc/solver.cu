@@ -257,15 +257,20 @@ __global__ void k_iso_finalize(Counters* c, const double* block_sums, int nblock
 
 static int g_cg_grid = 0;
 
-cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, int cg_max_iter) {
-    cudaStream_t s = ws.stream;
+// launch geometry that needs device queries (done once, outside any stream capture)
+void prepare_launch_configs(Workspace& ws) {
     if (g_cg_grid == 0) {
         int per_sm = 0;
-        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg, kCgBlock, 0);
-        if (e != cudaSuccess) return e;
-        if (per_sm < 1) return cudaErrorLaunchOutOfResources;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg, kCgBlock, 0) != cudaSuccess || per_sm < 1)
+            per_sm = 1;
         g_cg_grid = ws.num_sms * (per_sm < 2 ? per_sm : 2);
     }
+    (void)scan_grid(1 << 20);
+}
+
+cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, int cg_max_iter) {
+    cudaStream_t s = ws.stream;
+    if (g_cg_grid == 0) prepare_launch_configs(ws);
     CgArgs a;
     a.c = ws.cnt;
     a.cw = ws.cnt;

@@ -145,12 +145,15 @@ struct Workspace {
     int* part_t;
     int part_cap_v, part_cap_t;
 
+    int* d_params;          // [0] point count of the current call (written before each run)
+
     cudaStream_t stream;
     int num_sms;
 };
 
 // stage entry points (each issues kernels on ws.stream; no host synchronisation)
-cudaError_t octree_build(Workspace& ws, int n_points_host_hint);
+cudaError_t octree_build(Workspace& ws);
+void prepare_launch_configs(Workspace& ws);
 cudaError_t field_build(Workspace& ws);
 cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, int cg_max_iter);
 cudaError_t mesh_build(Workspace& ws);

@@ -55,7 +55,8 @@ class PsrStats(ctypes.Structure):
                 ("subdivision_nodes", ctypes.c_int), ("mesh_vertices", ctypes.c_int),
                 ("mesh_triangles", ctypes.c_int), ("cg_iterations", ctypes.c_int * 10),
                 ("cg_residual", ctypes.c_double * 10), ("iso_value", ctypes.c_float),
-                ("error_bits", ctypes.c_uint), ("stage_ms", ctypes.c_float * 6)]
+                ("error_bits", ctypes.c_uint), ("stage_ms", ctypes.c_float * 6),
+                ("kernel_launches", ctypes.c_int), ("graph_replay", ctypes.c_int)]
 
 
 _lib = None
@@ -215,6 +216,9 @@ class PoissonReconstruction:
         s = PsrStats()
         self._lib.psr_get_stats(self._h, ctypes.byref(s))
         return s
+
+    def launch_count(self):
+        return self.stats().kernel_launches
 
     def debug(self, name, dtype=np.int32, rows=None):
         """Copy an internal device array of the last reconstruction to host."""
