@@ -1,0 +1,121 @@
+// Header-only C++ shim over the C ABI (psr.h) with the reference's class and method names
+// (SparseSurfelFusion::PoissonReconstruction, mesh/PoissonReconstruction.h:63-184), so a
+// caller of the reference's data-parallel path can switch by changing the include and the
+// namespace.  It owns no device memory of its own except the optional surfel staging used
+// by the DepthSurfel overload.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "psr.h"
+
+namespace psr_gb300 {
+
+// Layout of the reference's DepthSurfel (base/CommonTypes.h:113-118): 8-byte pixel
+// coordinate, then position+confidence, normal+radius and colour+time as float4.
+struct DepthSurfel {
+    unsigned int row, col;
+    float4 VertexAndConfidence;
+    float4 NormalAndRadius;
+    float4 ColorAndTime;
+};
+static_assert(sizeof(DepthSurfel) == 64, "DepthSurfel must keep the reference's 64-byte layout");
+
+struct Point3D {
+    float coords[3];
+};
+struct TriangleIndex {
+    int idx[3];
+};
+
+class PoissonReconstruction {
+public:
+    explicit PoissonReconstruction(const psr_config* cfg = nullptr) {
+        psr_config c;
+        if (cfg) c = *cfg;
+        else psr_config_default(&c);
+        cfg_ = c;
+        psr_status s = psr_create(&c, &h_);
+        if (s != PSR_OK) throw std::runtime_error(std::string("psr_create: ") + psr_status_string(s));
+    }
+    ~PoissonReconstruction() {
+        if (h_) psr_destroy(h_);
+        if (staging_) cudaFree(staging_);
+    }
+    PoissonReconstruction(const PoissonReconstruction&) = delete;
+    PoissonReconstruction& operator=(const PoissonReconstruction&) = delete;
+
+    // Same role as the reference's SolvePoissionReconstructionMesh(DeviceArrayView<DepthSurfel>):
+    // device-resident surfels in, mesh kept in the object (read with the getters below).
+    void SolvePoissionReconstructionMesh(const DepthSurfel* device_surfels, int count, cudaStream_t stream = nullptr) {
+        ensure_staging(count);
+        float* xyz = staging_;
+        float* nrm = staging_ + 3 * (size_t)count;
+        // strided 2-D copies gather the AoS fields into the SoA input (no kernel needed)
+        check(cudaMemcpy2DAsync(xyz, 12, (const char*)device_surfels + 16, sizeof(DepthSurfel), 12, count,
+                                cudaMemcpyDeviceToDevice, stream));
+        check(cudaMemcpy2DAsync(nrm, 12, (const char*)device_surfels + 32, sizeof(DepthSurfel), 12, count,
+                                cudaMemcpyDeviceToDevice, stream));
+        Solve(xyz, nrm, nullptr, count, PSR_DEVICE, stream);
+    }
+
+    // Oriented points (host or device), optional 8-bit colour.
+    void Solve(const float* xyz, const float* normals, const uint8_t* rgb, int count, int location,
+               cudaStream_t stream = nullptr, int depth = 0, int cg_iterations = 0) {
+        vertices_.resize((size_t)cfg_.max_mesh_vertices);
+        triangles_.resize((size_t)cfg_.max_triangles);
+        colors_.resize(cfg_.compute_colors ? (size_t)cfg_.max_mesh_vertices : 0);
+        psr_points p{xyz, normals, rgb, count, location};
+        psr_options o{depth, cg_iterations};
+        psr_mesh m{};
+        m.vertices = (float*)vertices_.data();
+        m.triangles = (int32_t*)triangles_.data();
+        m.colors = cfg_.compute_colors ? (float*)colors_.data() : nullptr;
+        m.vertex_capacity = cfg_.max_mesh_vertices;
+        m.triangle_capacity = cfg_.max_triangles;
+        m.location = PSR_HOST;
+        psr_status s = psr_reconstruct(h_, &p, &o, &m, stream);
+        if (s != PSR_OK)
+            throw std::runtime_error(std::string("psr_reconstruct: ") + psr_status_string(s) + ": " + psr_last_error(h_));
+        vertices_.resize((size_t)m.vertex_count);
+        triangles_.resize((size_t)m.triangle_count);
+        if (cfg_.compute_colors) colors_.resize((size_t)m.vertex_count);
+        center_[0] = m.center[0]; center_[1] = m.center[1]; center_[2] = m.center[2];
+        scale_ = m.scale;
+    }
+
+    // mesh/ComputeTriangleIndices.h:331-342 (host copies here)
+    const std::vector<Point3D>& GetRebuildMeshVertices() const { return vertices_; }
+    const std::vector<TriangleIndex>& GetRebuildMeshTriangleIndices() const { return triangles_; }
+    const std::vector<Point3D>& GetRebuildMeshColors() const { return colors_; }
+    const float* BoundingBoxOrigin() const { return center_; }
+    float BoundingBoxEdge() const { return scale_; }
+    psr_handle* handle() const { return h_; }
+
+private:
+    static void check(cudaError_t e) {
+        if (e != cudaSuccess) throw std::runtime_error(cudaGetErrorString(e));
+    }
+    void ensure_staging(int count) {
+        if (count <= staging_count_) return;
+        if (staging_) cudaFree(staging_);
+        staging_ = nullptr;
+        check(cudaMalloc(&staging_, 6 * sizeof(float) * (size_t)count));
+        staging_count_ = count;
+    }
+    psr_config cfg_{};
+    psr_handle* h_ = nullptr;
+    float* staging_ = nullptr;
+    int staging_count_ = 0;
+    std::vector<Point3D> vertices_;
+    std::vector<TriangleIndex> triangles_;
+    std::vector<Point3D> colors_;
+    float center_[3] = {0, 0, 0};
+    float scale_ = 0;
+};
+
+}  // namespace psr_gb300

@@ -53,3 +53,18 @@ def test_struct_layouts_match_header():
     assert ctypes.sizeof(psr.PsrConfig) == 48
     assert ctypes.sizeof(psr.PsrPoints) == 32
     assert ctypes.sizeof(psr.PsrOptions) == 8
+
+
+def test_cpp_shim_compiles(tmp_path):
+    """The header-only C++ shim (reference class and method names) compiles against psr.h."""
+    import shutil
+    import subprocess
+    if not shutil.which("g++"):
+        pytest.skip("no g++")
+    src = tmp_path / "shim.cpp"
+    src.write_text('#include "psr/PoissonReconstruction.hpp"\n'
+                   'int main() { psr_gb300::PoissonReconstruction* p = nullptr; (void)p; return 0; }\n')
+    cuda_inc = "/usr/local/cuda/include"
+    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", str(ROOT / "include"), "-I", cuda_inc, str(src)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
