@@ -122,6 +122,21 @@ psr_status psr_get_stats(const psr_handle* h, psr_stats* out);
  * and inspection).  Returns the byte size in *bytes; dst may be NULL to query it. */
 psr_status psr_debug_array(psr_handle* h, const char* name, void* dst, size_t dst_bytes, size_t* bytes);
 
+/* Point ordering without any device allocation (no counterpart in the reference).
+ * For callers that cannot call cudaMalloc at all (a caller-owned memory pool or arena,
+ * a host process whose allocator must see every byte, a real-time loop that may not
+ * allocate): normalises the cloud exactly like psr_reconstruct, computes each point's
+ * Morton code at `depth` (1..9) and stably sorts by it.  `xyz` (3 * count floats),
+ * `codes` and `order` (count uint32 each: sorted codes, original index of each sorted
+ * point) are device pointers owned by the caller.  All scratch lives in a fixed
+ * file-scope device array (about 9 MB, on every device that loads the library, until
+ * exit), so at most 1,048,576 points per call (PSR_OUT_OF_CAPACITY above that).  Calls
+ * share that array: calls whose GPU work overlaps race.  The first call on a device
+ * looks up the array's address with that device current; make it before any stream
+ * capture.  Returns after the work on `stream` (a cudaStream_t or NULL) has completed. */
+psr_status psr_morton_sort_noalloc(const float* xyz, int count, int depth, float bbox_scale, uint32_t* codes,
+                                   uint32_t* order, void* stream);
+
 const char* psr_status_string(psr_status s);
 const char* psr_last_error(const psr_handle* h);
 

@@ -20,7 +20,7 @@ PSR_HOST, PSR_DEVICE = 0, 1
 
 # every function declared in include/psr/psr.h
 EXPORTED = ["psr_config_default", "psr_create", "psr_destroy", "psr_reconstruct", "psr_get_stats",
-            "psr_debug_array", "psr_status_string", "psr_last_error"]
+            "psr_debug_array", "psr_status_string", "psr_last_error", "psr_morton_sort_noalloc"]
 
 
 class PsrConfig(ctypes.Structure):
@@ -83,6 +83,8 @@ def load_library(path=None):
     L.psr_status_string.restype = ctypes.c_char_p
     L.psr_last_error.argtypes = [ctypes.c_void_p]
     L.psr_last_error.restype = ctypes.c_char_p
+    L.psr_morton_sort_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     for fn in EXPORTED:
         if fn not in ("psr_status_string", "psr_last_error"):
             getattr(L, fn).restype = ctypes.c_int
