@@ -82,30 +82,60 @@ __device__ __forceinline__ double div_terms(int l0, int l1, int step, int ox, in
     return acc;
 }
 
-// one warp per node for depths >= dsplit
+// One warp per node for depths >= dsplit.  The (neighbour, leaf) pairs of the node are
+// flattened over the lanes: lane k < 27 holds neighbour k's leaf range, a warp scan gives
+// the range offsets, and term t belongs to the last neighbour whose offset is <= t.  A
+// depth-D node has at most 27 terms (one leaf per neighbour): one pass, 27 lanes busy.
 __global__ void __launch_bounds__(kBlock) k_div_fine(const Counters* c, int depth, int dsplit, int res,
                                                      const int* enc, const int* didx, const int* dnum,
                                                      const int* neigh, size_t stride, const float* vx,
                                                      const float* vy, const float* vz, const double* dff,
                                                      float* divg) {
+    __shared__ int s_off[kBlock / 32][33];
+    __shared__ int s_base[kBlock / 32][32];
     const int b0 = c->level_base[dsplit];
     const int M = c->n_nodes;
     const int bD = c->level_base[depth];
     const int lane = lane_id();
+    const int wib = threadIdx.x >> 5;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     for (int i = b0 + warp; i < M; i += nwarps) {
         int ox, oy, oz;
         decode3(enc[i], depth, ox, oy, oz);
+        int cnt = 0, base = 0;
+        if (lane < 27) {
+            const int nb = neigh[(size_t)lane * stride + i];
+            if (nb >= 0) { cnt = dnum[nb]; base = didx[nb]; }
+        }
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        s_off[wib][lane] = incl - cnt;   // exclusive offset of neighbour `lane`
+        s_base[wib][lane] = base;
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        __syncwarp();
         double acc = 0.0;
-        for (int k = 0; k < 27; ++k) {
-            const int nb = neigh[(size_t)k * stride + i];
-            if (nb < 0) continue;
-            const int l0 = didx[nb];
-            acc += div_terms(l0 + lane, l0 + dnum[nb], 32, ox, oy, oz, depth, res, bD, enc, vx, vy, vz, dff);
+        int k = 0;
+        for (int t = lane; t < total; t += 32) {
+            while (k < 26 && s_off[wib][k + 1] <= t) ++k;   // terms are visited in increasing order
+            const int l = s_base[wib][k] + (t - s_off[wib][k]);
+            int lx, ly, lz;
+            decode3(enc[bD + l], depth, lx, ly, lz);
+            float ux = (float)dff[(size_t)ox + (size_t)res * lx];
+            float uy = (float)dff[(size_t)oy + (size_t)res * ly];
+            float uz = (float)dff[(size_t)oz + (size_t)res * lz];
+            float tt = vx[l] * ux;
+            tt = fmaf(vy[l], uy, tt);
+            tt = fmaf(vz[l], uz, tt);
+            acc += (double)tt;
         }
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
         if (lane == 0) divg[i] = (float)acc;
+        __syncwarp();
     }
 }
 

@@ -535,55 +535,115 @@ struct RootStore {
     }
 };
 
-// Group table (one thread).  Group record (ints): 0 root depth, 1 first root, 2 root count,
+// Group table.  Group record (ints): 0 root depth, 1 first root, 2 root count,
 // 3 node offset, 4 node count, 5 D-level node offset (in the D-level sub numbering),
-// 6 D-level node count.
+// 6 D-level node count.  Coarse roots (depth < D - 4) are one group each; the finer roots
+// of one depth form one group (mesh/ComputeTriangleIndices.cu:1475-1799, :1801-2194).
 constexpr int kGroupRec = 8;
 
-__global__ void k_build_groups(Counters* c, int depth, const int* sub_root, const int* ndepth, const int* key,
-                               const int* parent, int* sub_root_depth, int* groups, int max_groups, int node_cap,
-                               int dnode_cap, int* node_subgroup, int* node_subslot, int* ov_group, int* ov_sub,
-                               size_t stride) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    const int R = c->n_subroots;
-    const int finer = depth - 4;
-    int ng = 0;
-    long long noff = 0, doff = 0;
-    int r = 0;
-    bool overflow = false;
-    while (r < R) {
+struct GroupFlagLoad {
+    const int* sub_root;
+    const int* ndepth;
+    int finer;
+    __device__ unsigned operator()(int r) const {
         const int rd = ndepth[sub_root[r]];
-        int n = 1;
-        if (rd >= finer) {
-            while (r + n < R && ndepth[sub_root[r + n]] == rd) ++n;
+        if (r == 0 || rd < finer) return 1u;
+        return (ndepth[sub_root[r - 1]] != rd) ? 1u : 0u;
+    }
+};
+struct GroupFlagStore {
+    int* root_group;
+    int* groups;
+    int max_groups;
+    unsigned* err;
+    __device__ void operator()(int r, unsigned pre, unsigned v) const {
+        const int g = (int)(pre + v) - 1;
+        root_group[r] = g;
+        if (v) {
+            if (g >= max_groups) { atomicOr(err, kErrCapacity); return; }
+            groups[(size_t)g * kGroupRec + 1] = r;
         }
+    }
+};
+
+__global__ void k_group_count(Counters* c, const unsigned* total, int max_groups) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        int ng = (int)*total;
+        if (ng > max_groups) { atomicOr(&c->error, kErrCapacity); ng = 0; }
+        c->n_groups = ng;
+    }
+}
+
+// per-group sizes (thread per group)
+__global__ void __launch_bounds__(kBlock) k_group_sizes(const Counters* c, int depth, const int* sub_root,
+                                                        const int* ndepth, int* groups) {
+    const int ng = c->n_groups;
+    const int R = c->n_subroots;
+    PSR_GRID_STRIDE(g, ng) {
+        int* G = groups + (size_t)g * kGroupRec;
+        const int first = G[1];
+        const int next = (g + 1 < ng) ? groups[(size_t)(g + 1) * kGroupRec + 1] : R;
+        const int rd = ndepth[sub_root[first]];
+        const long long n = next - first;
         long long per = 0, dper = 1;
         for (int d = rd; d <= depth; ++d) { per += dper; if (d < depth) dper *= 8; }
-        if (ng >= max_groups || noff + per * n > node_cap || doff + dper * n > dnode_cap) { overflow = true; break; }
-        int* g = groups + (size_t)ng * kGroupRec;
-        g[0] = rd; g[1] = r; g[2] = n; g[3] = (int)noff; g[4] = (int)(per * n); g[5] = (int)doff; g[6] = (int)(dper * n);
-        g[7] = 0;
-        for (int q = 0; q < n; ++q) {
-            const int node = sub_root[r + q];
-            sub_root_depth[r + q] = rd;
-            node_subgroup[node] = ng;
-            node_subslot[node] = q;
-            const int son = (key[node] >> (3 * (depth - rd))) & 7;
-            const int pa = parent[node];
-            if (pa >= 0) {
-                ov_group[(size_t)son * stride + pa] = ng;
-                ov_sub[(size_t)son * stride + pa] = q;
-            }
-        }
-        noff += per * n;
-        doff += dper * n;
-        ++ng;
-        r += n;
+        const long long nodes = per * n, dn = dper * n;
+        G[0] = rd;
+        G[2] = (int)n;
+        G[4] = nodes > 0x3fffffffLL ? 0x3fffffff : (int)nodes;
+        G[6] = dn > 0x3fffffffLL ? 0x3fffffff : (int)dn;
     }
-    if (overflow) atomicOr(&c->error, kErrCapacity);
-    c->n_sub_nodes = overflow ? 0 : (int)noff;
-    c->n_sub_dnodes = overflow ? 0 : (int)doff;
-    c->n_groups = overflow ? 0 : ng;
+}
+
+struct GroupFieldLoad {
+    const int* groups;
+    int field;
+    __device__ unsigned operator()(int g) const { return (unsigned)groups[(size_t)g * kGroupRec + field]; }
+};
+struct GroupFieldStore {
+    int* groups;
+    int field;
+    __device__ void operator()(int g, unsigned pre, unsigned) const { groups[(size_t)g * kGroupRec + field] = (int)pre; }
+};
+
+__global__ void k_group_totals(Counters* c, const unsigned* node_total, const unsigned* dnode_total, int node_cap,
+                               int dnode_cap) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        const unsigned nt = *node_total, dt = *dnode_total;
+        if (nt > (unsigned)node_cap || dt > (unsigned)dnode_cap) {
+            atomicOr(&c->error, kErrCapacity);
+            c->n_groups = 0;
+            c->n_sub_nodes = 0;
+            c->n_sub_dnodes = 0;
+            return;
+        }
+        c->n_sub_nodes = (int)nt;
+        c->n_sub_dnodes = (int)dt;
+    }
+}
+
+// per root: its depth and the redirected child slot of its parent (overlay)
+__global__ void __launch_bounds__(kBlock) k_root_overlay(const Counters* c, int depth, const int* sub_root,
+                                                         const int* ndepth, const int* key, const int* parent,
+                                                         const int* root_group, const int* groups,
+                                                         int* sub_root_depth, int* ov_group, int* ov_sub,
+                                                         size_t stride) {
+    const int R = c->n_subroots;
+    const int ng = c->n_groups;
+    PSR_GRID_STRIDE(r, R) {
+        const int g = root_group[r];
+        if (g < 0 || g >= ng) continue;
+        const int node = sub_root[r];
+        const int rd = ndepth[node];
+        sub_root_depth[r] = rd;
+        const int q = r - groups[(size_t)g * kGroupRec + 1];
+        const int son = (key[node] >> (3 * (depth - rd))) & 7;
+        const int pa = parent[node];
+        if (pa >= 0) {
+            ov_group[(size_t)son * stride + pa] = g;
+            ov_sub[(size_t)son * stride + pa] = q;
+        }
+    }
 }
 
 // subdivision node geometry (singleRebuildArray :599-635 / wholeRebuildArray :1110-1168)
@@ -660,11 +720,13 @@ __global__ void __launch_bounds__(kBlock) k_sub_neighbours(const Counters* c, in
                                                            const int* neigh, size_t stride, const int* first_child,
                                                            const int* ov_group, const int* ov_sub, const int* s_key,
                                                            const int* s_parent, const int* s_first_child,
-                                                           const int* s_depth, const int* s_group, int* s_neigh,
-                                                           size_t sstride, int na) {
+                                                           const int* s_depth, const int* s_group, const int* s_root,
+                                                           int* s_neigh, unsigned char* s_contrib, size_t sstride,
+                                                           int na) {
     const int S = c->n_sub_nodes;
     PSR_GRID_STRIDE(s, S) {
         if (s_depth[s] != d) continue;
+        int contrib = 0;
         const int g = s_group[s];
         const int* G = groups + (size_t)g * kGroupRec;
         const int son = (s_key[s] >> (3 * (depth - d))) & 7;
@@ -689,7 +751,9 @@ __global__ void __launch_bounds__(kBlock) k_sub_neighbours(const Counters* c, in
                 }
             }
             s_neigh[(size_t)k * sstride + s] = v;
+            if (v >= 0 && (v < na || s_root[v - na] >= 0)) contrib = 1;
         }
+        s_contrib[s] = (unsigned char)contrib;
     }
 }
 
@@ -895,7 +959,8 @@ __global__ void __launch_bounds__(kBlock) k_sub_vertex_values(const Counters* c,
                                                               const int* neigh, size_t stride, const int* parent,
                                                               const int* s_neigh, size_t sstride,
                                                               const int* s_parent, const int* s_root,
-                                                              const int* enc, const float* x, float* vvalue, int na) {
+                                                              const unsigned char* s_contrib, const int* enc,
+                                                              const float* x, float* vvalue, int na) {
     const int V = c->n_sub_vertices;
     const float iso = c->iso;
     PSR_GRID_STRIDE(v, V) {
@@ -904,6 +969,8 @@ __global__ void __launch_bounds__(kBlock) k_sub_vertex_values(const Counters* c,
         const float qx = vx[v], qy = vy[v], qz = vz[v];
         if (now > 0) {
             while (now != -1) {
+                // all 27 neighbours zero-valued subdivision nodes: every term is skipped
+                if (now >= na && !s_contrib[now - na]) { now = s_parent[now - na]; continue; }
                 for (int k = 0; k < 27; ++k) {
                     int nb = (now < na) ? neigh[(size_t)k * stride + now] : s_neigh[(size_t)k * sstride + (now - na)];
                     if (nb == -1) continue;
@@ -1200,9 +1267,22 @@ cudaError_t mesh_build_impl(Workspace& ws, const MeshBufs& mb) {
                     RootStore{ws.sub_root, ws.cap.nodes, err}, &c->level_base[D], 0, ws.scan, total, err, s);
     if (e != cudaSuccess) return e;
     k_set_count<<<1, 1, 0, s>>>(&c->n_subroots, total, ws.cap.nodes, err);
-    k_build_groups<<<1, 1, 0, s>>>(c, D, ws.sub_root, ws.ndepth, ws.key, ws.parent, ws.sub_root_depth, mb.groups,
-                                   mb.max_groups, ws.cap.sub_nodes, ws.cap.sub_dnodes, ws.node_subgroup,
-                                   ws.node_subslot, mb.ov_group, mb.ov_sub, stride);
+    // subdivision groups
+    e = launch_scan(GroupFlagLoad{ws.sub_root, ws.ndepth, D - 4},
+                    GroupFlagStore{ws.root_group, mb.groups, mb.max_groups, err}, &c->n_subroots, 0, ws.scan,
+                    total, err, s);
+    if (e != cudaSuccess) return e;
+    k_group_count<<<1, 1, 0, s>>>(c, total, mb.max_groups);
+    k_group_sizes<<<gm, kBlock, 0, s>>>(c, D, ws.sub_root, ws.ndepth, mb.groups);
+    unsigned* total2 = (unsigned*)(mb.misc + 8);
+    e = launch_scan(GroupFieldLoad{mb.groups, 4}, GroupFieldStore{mb.groups, 3}, &c->n_groups, 0, ws.scan, total, err, s);
+    if (e != cudaSuccess) return e;
+    e = launch_scan(GroupFieldLoad{mb.groups, 6}, GroupFieldStore{mb.groups, 5}, &c->n_groups, 0, ws.scan, total2, err,
+                    s);
+    if (e != cudaSuccess) return e;
+    k_group_totals<<<1, 1, 0, s>>>(c, total, total2, ws.cap.sub_nodes, ws.cap.sub_dnodes);
+    k_root_overlay<<<gm, kBlock, 0, s>>>(c, D, ws.sub_root, ws.ndepth, ws.key, ws.parent, ws.root_group, mb.groups,
+                                         ws.sub_root_depth, mb.ov_group, mb.ov_sub, stride);
     return cudaGetLastError();
 }
 
@@ -1226,7 +1306,7 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
     for (int d = 1; d <= D; ++d)
         k_sub_neighbours<<<gs, kBlock, 0, s>>>(c, d, D, mb.groups, ws.neigh, stride, ws.first_child, mb.ov_group,
                                                mb.ov_sub, ws.s_key, ws.s_parent, ws.s_first_child, ws.s_depth,
-                                               ws.s_group, ws.s_neigh, sstride, na);
+                                               ws.s_group, ws.s_root, ws.s_neigh, ws.s_contrib, sstride, na);
     cudaMemsetAsync(ws.s_vtx, 0, sizeof(int) * 8 * dstride, s);
     cudaMemsetAsync(ws.s_edge, 0, sizeof(int) * 12 * dstride, s);
     k_sub_vertex_owner<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.s_key, ws.s_neigh, sstride, ws.s_cx, ws.s_cy, ws.s_cz,
@@ -1256,8 +1336,8 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
                                               ws.s_cx, ws.s_cy, ws.s_cz, ws.s_depth, ws.se_owner, ws.se_kind, ws.s_edge,
                                               dstride, na);
     k_sub_vertex_values<<<gs, kBlock, 0, s>>>(c, D, ws.sv_x, ws.sv_y, ws.sv_z, ws.sv_owner, ws.neigh, stride, ws.parent,
-                                              ws.s_neigh, sstride, ws.s_parent, ws.s_root, ws.enc, ws.xsol,
-                                              ws.sv_value, na);
+                                              ws.s_neigh, sstride, ws.s_parent, ws.s_root, ws.s_contrib, ws.enc,
+                                              ws.xsol, ws.sv_value, na);
     // crossings: staged after the main part's vertices
     e = launch_scan(SubCrossLoad{ws.se_owner, ws.se_kind, ws.s_vtx, dstride, mb.groups, &c->n_groups, D, ws.sv_value, na, err},
                     SubCrossStore{ws.se_owner, ws.se_kind, ws.s_vtx, dstride, mb.groups, &c->n_groups, D, ws.sv_value,

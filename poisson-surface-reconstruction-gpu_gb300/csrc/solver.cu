@@ -7,9 +7,9 @@
 // per depth and the neighbour table.  Right-hand side: the divergence of the depth.
 //
 // CG (mesh/solver/CGAlgorithm.cu:10-80): x0 = 0, r0 = b, stops when r.r <= tol^2 or after
-// max_iter iterations (or after a fixed count).  All depths are independent and are solved
-// together in one cooperative launch: every iteration performs the SpMV of all depths,
-// per-depth FP64 reductions in a fixed order (deterministic), and per-depth updates.
+// max_iter iterations (or after a fixed count).  All depths are independent; they are
+// solved together in one launch of two thread-block clusters (see k_cg_cluster), with
+// per-depth FP64 reductions in a fixed order (deterministic) and per-depth updates.
 //
 // Iso-value (:269-305): mean of the implicit function at the sample points, evaluated in
 // FP32 per point and averaged in FP64.
@@ -23,9 +23,16 @@ namespace cg = cooperative_groups;
 
 namespace psr {
 
-constexpr int kCgBlock = 256;
+// ---- cluster CG -----------------------------------------------------------------------
+// Each thread-block cluster owns whole depths (cluster 0: depth D; cluster 1: depths
+// 0..D-1).  Barriers are cluster barriers (hardware), reductions go through distributed
+// shared memory: every CTA writes its per-depth partial sums to its own shared memory,
+// and after the barrier every CTA sums the partials of all CTAs of the cluster in rank
+// order (identical result in every CTA, deterministic).  Partial buffers alternate
+// between two slots so a slot is only rewritten after a barrier that follows its reads.
+constexpr int kCgcBlock = 1024;
 
-struct CgArgs {
+struct CgcArgs {
     const Counters* c;
     Counters* cw;
     int depth;
@@ -38,64 +45,65 @@ struct CgArgs {
     float* r;
     float* p;
     float* ap;
-    double* partial;   // [gridDim][kMaxDepth + 1]
-    double tol2;       // compared against a float copy of r.r, as the reference does
+    double tol2;
     int max_iter;
 };
 
-// Sum the per-depth values of all threads of the block into smem[depth]; then every
-// block reduces the grid partials of every depth in the same fixed order.
-__device__ __forceinline__ void block_depth_reduce(double (&acc)[kMaxDepth + 1], int nd, double* smem, double* out_row) {
+__device__ __forceinline__ void cgc_cta_partials(const double (&acc)[kMaxDepth + 1], int nd, double* s_warp,
+                                                 double* s_slot) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int d = 0; d <= kMaxDepth; ++d) {
         if (d >= nd) break;
         double v = acc[d];
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0) smem[warp * (kMaxDepth + 1) + d] = v;
+        if (lane == 0) s_warp[warp * (kMaxDepth + 1) + d] = v;
     }
     __syncthreads();
     if (threadIdx.x < nd) {
         double s = 0.0;
-        for (int w = 0; w < kCgBlock / 32; ++w) s += smem[w * (kMaxDepth + 1) + threadIdx.x];
-        out_row[threadIdx.x] = s;
+        for (int w = 0; w < kCgcBlock / 32; ++w) s += s_warp[w * (kMaxDepth + 1) + threadIdx.x];
+        s_slot[threadIdx.x] = s;
     }
-    __syncthreads();
 }
 
-__device__ __forceinline__ void grid_depth_sum(const double* partial, int nblocks, int nd, double* result) {
-    // warp w sums depth w over all blocks (fixed order)
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int d = warp; d < nd; d += kCgBlock / 32) {
+// after cluster.sync: sum slot `buf` of every CTA in rank order
+__device__ __forceinline__ void cgc_cluster_sum(cg::cluster_group& cl, double* s_slot, int nd, double* out) {
+    if (threadIdx.x < nd) {
         double s = 0.0;
-        for (int bi = lane; bi < nblocks; bi += 32) s += partial[(size_t)bi * (kMaxDepth + 1) + d];
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (lane == 0) result[d] = s;
+        const unsigned nb = cl.num_blocks();
+        for (unsigned k = 0; k < nb; ++k) {
+            const double* rem = cl.map_shared_rank(s_slot, k);
+            s += rem[threadIdx.x];
+        }
+        out[threadIdx.x] = s;
     }
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(kCgBlock) k_cg(CgArgs a) {
-    cg::grid_group grid = cg::this_grid();
-    __shared__ double s_red[(kCgBlock / 32) * (kMaxDepth + 1)];
+__global__ void __launch_bounds__(kCgcBlock) k_cg_cluster(CgcArgs a) {
+    cg::cluster_group cl = cg::this_cluster();
+    __shared__ double s_warp[(kCgcBlock / 32) * (kMaxDepth + 1)];
+    __shared__ double s_slot[2][kMaxDepth + 1];
     __shared__ double s_rr[kMaxDepth + 1], s_pap[kMaxDepth + 1], s_new[kMaxDepth + 1];
     __shared__ float s_alpha[kMaxDepth + 1], s_beta[kMaxDepth + 1];
     __shared__ int s_active[kMaxDepth + 1];
     __shared__ float s_st[(kMaxDepth + 1) * 27];
-    const int nd = a.depth + 1;
-    const int M = a.c->n_nodes;
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const int nthr = gridDim.x * blockDim.x;
+    const int D = a.depth;
+    const int nd = D + 1;
+    const int cid = blockIdx.x / cl.num_blocks();
+    // rows owned by this cluster
+    const int bD = a.c->level_base[D];
+    const int row0 = (cid == 0) ? bD : 0;
+    const int row1 = (cid == 0) ? a.c->n_nodes : bD;
+    const int tid = cl.block_rank() * blockDim.x + threadIdx.x;
+    const int nthr = cl.num_blocks() * blockDim.x;
     for (int q = threadIdx.x; q < nd * 27; q += blockDim.x) s_st[q] = a.stencil[q];
-    __syncthreads();
-    double* my_row = a.partial + (size_t)blockIdx.x * (kMaxDepth + 1);
-
-    // r = b, x = 0, p = r, rr = r.r
     double acc[kMaxDepth + 1];
 #pragma unroll
     for (int d = 0; d <= kMaxDepth; ++d) acc[d] = 0.0;
-    for (int i = tid; i < M; i += nthr) {
-        float bi = a.b[i];
+    for (int i = row0 + tid; i < row1; i += nthr) {
+        const float bi = a.b[i];
         a.r[i] = bi;
         a.p[i] = bi;
         a.x[i] = 0.0f;
@@ -103,32 +111,33 @@ __global__ void __launch_bounds__(kCgBlock) k_cg(CgArgs a) {
 #pragma unroll
         for (int q = 0; q <= kMaxDepth; ++q) if (q == d) acc[q] += (double)(bi * bi);
     }
-    block_depth_reduce(acc, nd, s_red, my_row);
-    grid.sync();
-    grid_depth_sum(a.partial, gridDim.x, nd, s_rr);
+    int buf = 0;
+    cgc_cta_partials(acc, nd, s_warp, s_slot[buf]);
+    cl.sync();
+    cgc_cluster_sum(cl, s_slot[buf], nd, s_rr);
+    buf ^= 1;
+    // a depth is active in the cluster that owns it
     if (threadIdx.x < nd) {
         const int d = threadIdx.x;
-        // the reference compares a float copy of r.r (mesh/solver/CGAlgorithm.cu:19,36)
-        s_active[d] = ((double)(float)s_rr[d] > a.tol2) ? 1 : 0;
+        const bool mine = (cid == 0) ? (d == D) : (d < D);
+        s_active[d] = (mine && (double)(float)s_rr[d] > a.tol2) ? 1 : 0;
     }
     __syncthreads();
-    int it = 1;
-    const int maxit = a.max_iter;
     int any = 0;
     for (int d = 0; d < nd; ++d) any |= s_active[d];
-    while (any && it <= maxit) {
-        grid.sync();   // p complete everywhere; partial rows free
-        // Ap and p.Ap
+    int it = 1;
+    while (any && it <= a.max_iter) {
+        // SpMV and p.Ap
 #pragma unroll
         for (int d = 0; d <= kMaxDepth; ++d) acc[d] = 0.0;
-        for (int i = tid; i < M; i += nthr) {
+        for (int i = row0 + tid; i < row1; i += nthr) {
             const int d = a.ndepth[i];
             if (!s_active[d]) continue;
             const float* st = &s_st[d * 27];
             float y = 0.0f;
 #pragma unroll
             for (int k = 0; k < 27; ++k) {
-                int nb = a.neigh[(size_t)k * a.stride + i];
+                const int nb = a.neigh[(size_t)k * a.stride + i];
                 if (nb >= 0) y = fmaf(st[k], a.p[nb], y);
             }
             a.ap[i] = y;
@@ -136,18 +145,19 @@ __global__ void __launch_bounds__(kCgBlock) k_cg(CgArgs a) {
 #pragma unroll
             for (int q = 0; q <= kMaxDepth; ++q) if (q == d) acc[q] += (double)(pi * y);
         }
-        block_depth_reduce(acc, nd, s_red, my_row);
-        grid.sync();
-        grid_depth_sum(a.partial, gridDim.x, nd, s_pap);
+        cgc_cta_partials(acc, nd, s_warp, s_slot[buf]);
+        cl.sync();
+        cgc_cluster_sum(cl, s_slot[buf], nd, s_pap);
+        buf ^= 1;
         if (threadIdx.x < nd) {
             const int d = threadIdx.x;
             s_alpha[d] = (s_active[d] && s_pap[d] != 0.0) ? (float)(s_rr[d] / s_pap[d]) : 0.0f;
         }
         __syncthreads();
-        grid.sync();   // every block has read the p.Ap partials
+        // x, r and r.r
 #pragma unroll
         for (int d = 0; d <= kMaxDepth; ++d) acc[d] = 0.0;
-        for (int i = tid; i < M; i += nthr) {
+        for (int i = row0 + tid; i < row1; i += nthr) {
             const int d = a.ndepth[i];
             if (!s_active[d]) continue;
             const float al = s_alpha[d];
@@ -157,26 +167,27 @@ __global__ void __launch_bounds__(kCgBlock) k_cg(CgArgs a) {
 #pragma unroll
             for (int q = 0; q <= kMaxDepth; ++q) if (q == d) acc[q] += (double)(ri * ri);
         }
-        block_depth_reduce(acc, nd, s_red, my_row);
-        grid.sync();
-        grid_depth_sum(a.partial, gridDim.x, nd, s_new);
+        cgc_cta_partials(acc, nd, s_warp, s_slot[buf]);
+        cl.sync();
+        cgc_cluster_sum(cl, s_slot[buf], nd, s_new);
+        buf ^= 1;
         if (threadIdx.x < nd) {
             const int d = threadIdx.x;
             if (s_active[d]) {
                 s_beta[d] = (s_rr[d] != 0.0) ? (float)(s_new[d] / s_rr[d]) : 0.0f;
                 s_rr[d] = s_new[d];
-                if (blockIdx.x == 0) {
+                if (cl.block_rank() == 0) {
                     a.cw->cg_iters[d] = it;
                     a.cw->cg_rr[d] = s_new[d];
                 }
-                bool go = ((double)(float)s_new[d] > a.tol2) && s_pap[d] != 0.0;
-                s_active[d] = (go && it + 1 <= maxit) ? 1 : 0;
+                const bool go = ((double)(float)s_new[d] > a.tol2) && s_pap[d] != 0.0;
+                s_active[d] = (go && it + 1 <= a.max_iter) ? 1 : 0;
             } else {
                 s_beta[d] = 0.0f;
             }
         }
         __syncthreads();
-        for (int i = tid; i < M; i += nthr) {
+        for (int i = row0 + tid; i < row1; i += nthr) {
             const int d = a.ndepth[i];
             if (!s_active[d]) continue;
             a.p[i] = fmaf(s_beta[d], a.p[i], a.r[i]);
@@ -184,7 +195,9 @@ __global__ void __launch_bounds__(kCgBlock) k_cg(CgArgs a) {
         any = 0;
         for (int d = 0; d < nd; ++d) any |= s_active[d];
         ++it;
+        cl.sync();   // p complete in the whole cluster before the next SpMV
     }
+    cl.sync();   // no CTA exits while others may still read its shared memory
 }
 
 // ---- implicit function at the sample points and the iso-value ----------------------
@@ -255,23 +268,38 @@ __global__ void k_iso_finalize(Counters* c, const double* block_sums, int nblock
     }
 }
 
-static int g_cg_grid = 0;
+static int g_cg_cluster = 0;
 
-// launch geometry that needs device queries (done once, outside any stream capture)
+// launch geometry that needs device queries (done once, outside any stream capture):
+// the largest cluster (16, else 8) the device can schedule for the CG kernel
 void prepare_launch_configs(Workspace& ws) {
-    if (g_cg_grid == 0) {
-        int per_sm = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg, kCgBlock, 0) != cudaSuccess || per_sm < 1)
-            per_sm = 1;
-        g_cg_grid = ws.num_sms * (per_sm < 2 ? per_sm : 2);
+    if (g_cg_cluster == 0) {
+        int size = 8;
+        if (cudaFuncSetAttribute(k_cg_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(16);
+            cfg.blockDim = dim3(kCgcBlock);
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeClusterDimension;
+            attr[0].val.clusterDim.x = 16;
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            int nclusters = 0;
+            if (cudaOccupancyMaxActiveClusters(&nclusters, (void*)k_cg_cluster, &cfg) == cudaSuccess && nclusters >= 2)
+                size = 16;
+        }
+        (void)cudaGetLastError();
+        g_cg_cluster = size;
     }
     (void)scan_grid(1 << 20);
 }
 
 cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, int cg_max_iter) {
     cudaStream_t s = ws.stream;
-    if (g_cg_grid == 0) prepare_launch_configs(ws);
-    CgArgs a;
+    if (g_cg_cluster == 0) prepare_launch_configs(ws);
+    CgcArgs a;
     a.c = ws.cnt;
     a.cw = ws.cnt;
     a.depth = ws.depth;
@@ -284,7 +312,6 @@ cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, 
     a.r = ws.cg_r;
     a.p = ws.cg_p;
     a.ap = ws.cg_ap;
-    a.partial = ws.cg_partial;
     float t2 = cg_tol * cg_tol;
     a.tol2 = (double)t2;
     // a fixed iteration count replaces the reference's max_iter (10000); the tolerance
@@ -292,16 +319,18 @@ cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, 
     a.max_iter = (cg_mode == 1 && cg_iters > 0) ? cg_iters : cg_max_iter;
     void* args[] = {&a};
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(g_cg_grid);
-    cfg.blockDim = dim3(kCgBlock);
+    cfg.gridDim = dim3(2 * g_cg_cluster);
+    cfg.blockDim = dim3(kCgcBlock);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeCooperative;
-    attr[0].val.cooperative = 1;
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = g_cg_cluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cudaError_t e = cudaLaunchKernelExC(&cfg, (const void*)k_cg, args);
+    cudaError_t e = cudaLaunchKernelExC(&cfg, (const void*)k_cg_cluster, args);
     if (e != cudaSuccess) return e;
     // iso-value
     const int nb = ws.num_sms * 4;

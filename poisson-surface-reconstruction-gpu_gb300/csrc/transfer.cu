@@ -29,71 +29,126 @@ __device__ __forceinline__ unsigned point_cell(int i, int depth, int g, int bD, 
 }
 
 // cell_start[m] = first sorted sample whose cell code is >= m, for m in [0, 8^g]
+// (binary search over the Morton-sorted samples; one thread per cell)
 __global__ void __launch_bounds__(kBlock) k_cell_starts(const Counters* c, int depth, int g, const int* key,
                                                         const int* point2node, int* cell_start) {
     const int n = c->n_points;
     const int bD = c->level_base[depth];
     const int ncell = 1 << (3 * g);
-    PSR_GRID_STRIDE(i, n + 1) {
-        const int cur = (i < n) ? (int)point_cell(i, depth, g, bD, key, point2node) : ncell;
-        const int prev = (i > 0) ? (int)point_cell(i - 1, depth, g, bD, key, point2node) : -1;
-        for (int m = prev + 1; m <= cur && m <= ncell; ++m) cell_start[m] = i;
+    PSR_GRID_STRIDE(m, ncell + 1) {
+        int lo = 0, hi = n;   // first i with cell(i) >= m
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if ((int)point_cell(mid, depth, g, bD, key, point2node) < m) lo = mid + 1;
+            else hi = mid;
+        }
+        cell_start[m] = lo;
     }
 }
 
+// (d, i) lexicographic order: smaller squared distance first, then lower sample index
+__device__ __forceinline__ bool knn_less(float da, int ia, float db, int ib) {
+    return da < db || (da == db && ia < ib);
+}
+
+// insert (d, i) into a sorted 4-list held in registers
+__device__ __forceinline__ void knn_insert(float (&bd)[4], int (&bi)[4], float d, int i) {
+    if (!knn_less(d, i, bd[3], bi[3])) return;
+    if (knn_less(d, i, bd[2], bi[2])) {
+        bd[3] = bd[2]; bi[3] = bi[2];
+        if (knn_less(d, i, bd[1], bi[1])) {
+            bd[2] = bd[1]; bi[2] = bi[1];
+            if (knn_less(d, i, bd[0], bi[0])) {
+                bd[1] = bd[0]; bi[1] = bi[0];
+                bd[0] = d; bi[0] = i;
+            } else { bd[1] = d; bi[1] = i; }
+        } else { bd[2] = d; bi[2] = i; }
+    } else { bd[3] = d; bi[3] = i; }
+}
+
+// the 4 smallest of two sorted 4-lists (lists hold disjoint sample sets)
+__device__ __forceinline__ void knn_merge(float (&ad)[4], int (&ai)[4], const float (&bd)[4], const int (&bi)[4]) {
+    float od[4];
+    int oi[4];
+    int p = 0, q = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const bool takeA = (q >= 4) || (p < 4 && knn_less(ad[p], ai[p], bd[q], bi[q]));
+        od[k] = takeA ? ad[p] : bd[q];
+        oi[k] = takeA ? ai[p] : bi[q];
+        p += takeA ? 1 : 0;
+        q += takeA ? 0 : 1;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { ad[k] = od[k]; ai[k] = oi[k]; }
+}
+
+// one warp per mesh vertex: the lanes split the samples of every grid shell, keep private
+// sorted 4-lists and merge them with butterfly shuffles after each shell
 __global__ void __launch_bounds__(kBlock) k_colour(const Counters* c, int g, const float* mv, const float* px,
                                                    const float* py, const float* pz, const float* cr, const float* cg,
                                                    const float* cb, const int* cell_start, float* out) {
     const int V = c->n_mesh_vertices;
     const int G = 1 << g;
-    PSR_GRID_STRIDE(v, V) {
+    const int lane = lane_id();
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int v = warp; v < V; v += nwarps) {
         const float qx = mv[3 * (size_t)v], qy = mv[3 * (size_t)v + 1], qz = mv[3 * (size_t)v + 2];
         float bd[4] = {1e6f, 1e6f, 1e6f, 1e6f};
-        int bi[4] = {0, 0, 0, 0};
+        int bi[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
+        float md[4];
+        int mi[4];
         const int cx = min(max((int)floorf(qx * G), 0), G - 1);
         const int cy = min(max((int)floorf(qy * G), 0), G - 1);
         const int cz = min(max((int)floorf(qz * G), 0), G - 1);
         for (int r = 0; r <= G; ++r) {
-            for (int a = cx - r; a <= cx + r; ++a) {
-                if (a < 0 || a >= G) continue;
-                for (int b = cy - r; b <= cy + r; ++b) {
-                    if (b < 0 || b >= G) continue;
-                    for (int z = cz - r; z <= cz + r; ++z) {
-                        if (z < 0 || z >= G) continue;
-                        if (max(abs(a - cx), max(abs(b - cy), abs(z - cz))) != r) continue;
-                        const unsigned m = morton3(a, b, z, g);
-                        for (int i = cell_start[m]; i < cell_start[m + 1]; ++i) {
-                            const float dx = __fsub_rn(qx, px[i]), dy = __fsub_rn(qy, py[i]), dz = __fsub_rn(qz, pz[i]);
-                            const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-                            if (d2 < bd[3] || (d2 == bd[3] && i < bi[3])) {
-                                int k = 3;
-                                while (k > 0 && (d2 < bd[k - 1] || (d2 == bd[k - 1] && i < bi[k - 1]))) {
-                                    bd[k] = bd[k - 1];
-                                    bi[k] = bi[k - 1];
-                                    --k;
-                                }
-                                bd[k] = d2;
-                                bi[k] = i;
-                            }
-                        }
-                    }
+            const int side = 2 * r + 1;
+            const int ncell = side * side * side;
+            for (int t = 0; t < ncell; ++t) {
+                const int a = cx - r + t / (side * side), b = cy - r + (t / side) % side, z = cz - r + t % side;
+                if (a < 0 || a >= G || b < 0 || b >= G || z < 0 || z >= G) continue;
+                if (max(abs(a - cx), max(abs(b - cy), abs(z - cz))) != r) continue;
+                const unsigned m = morton3(a, b, z, g);
+                const int s0 = cell_start[m], s1 = cell_start[m + 1];
+                for (int i = s0 + lane; i < s1; i += 32) {
+                    const float dx = __fsub_rn(qx, px[i]), dy = __fsub_rn(qy, py[i]), dz = __fsub_rn(qz, pz[i]);
+                    const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                    knn_insert(bd, bi, d2, i);
                 }
             }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) { md[k] = bd[k]; mi[k] = bi[k]; }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                float od[4];
+                int oi[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    od[k] = __shfl_xor_sync(0xffffffffu, md[k], o);
+                    oi[k] = __shfl_xor_sync(0xffffffffu, mi[k], o);
+                }
+                knn_merge(md, mi, od, oi);
+            }
             const float lim = (float)r / (float)G;
-            if (bd[3] < 1e6f && bd[3] < lim * lim) break;
+            if (mi[3] != 0x7fffffff && md[3] < lim * lim) break;
         }
-        const float sum = bd[0] + bd[1] + bd[2] + bd[3];
-        const float inv = (sum > 0.0f) ? 1.0f / sum : 0.0f;
-        float o[3] = {0.f, 0.f, 0.f};
-        for (int k = 0; k < 4; ++k) {
-            const float w = bd[k] * inv;   // weight grows with the squared distance
-            o[0] += cr[bi[k]] * w;
-            o[1] += cg[bi[k]] * w;
-            o[2] += cb[bi[k]] * w;
+        if (lane == 0) {
+            const float sum = md[0] + md[1] + md[2] + md[3];
+            const float inv = (sum > 0.0f) ? 1.0f / sum : 0.0f;
+            float o[3] = {0.f, 0.f, 0.f};
+            for (int k = 0; k < 4; ++k) {
+                // fewer than 4 samples: the reference's unfilled slots (distance 1e6, sample 0)
+                const int idx = (mi[k] == 0x7fffffff) ? 0 : mi[k];
+                const float w = md[k] * inv;   // weight grows with the squared distance
+                o[0] += cr[idx] * w;
+                o[1] += cg[idx] * w;
+                o[2] += cb[idx] * w;
+            }
+            out[3 * (size_t)v] = o[0];
+            out[3 * (size_t)v + 1] = o[1];
+            out[3 * (size_t)v + 2] = o[2];
         }
-        out[3 * (size_t)v] = o[0];
-        out[3 * (size_t)v + 1] = o[1];
-        out[3 * (size_t)v + 2] = o[2];
     }
 }
 

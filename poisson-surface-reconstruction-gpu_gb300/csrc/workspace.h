@@ -115,11 +115,11 @@ struct Workspace {
     // subdivision
     int* sub_root;          // node index of each root (node order)
     int* sub_root_depth;
-    int* node_subslot;      // per node: index of the root in its group's array
-    int* node_subgroup;     // per node: group id
+    int* root_group;        // per subdivision root: its group
     // subdivision-space nodes of all groups (SoA)
     int *s_key, *s_parent, *s_first_child, *s_neigh, *s_depth, *s_root;   // s_neigh: [27][cap.sub_nodes]
     int* s_group;
+    unsigned char* s_contrib;   // 1 when some neighbour of the sub-node carries a solution value
     float *s_cx, *s_cy, *s_cz;
     int *s_vtx, *s_edge;    // [8|12][cap.sub_dnodes] for D-level subdivision nodes
     unsigned char* s_vmask;
