@@ -236,6 +236,8 @@ def main():
         step_host()
     torch.cuda.synchronize(dev)
 
+    cg_samples = []
+
     def timed(fn, k):
         times = []
         last = None
@@ -248,6 +250,8 @@ def main():
             b.record(stream)
             b.synchronize()
             times.append(a.elapsed_time(b))
+            if fn is step_device:
+                cg_samples.append(r.stats().cg_kernel_ms)   # CUDA events around the CG kernel
         return np.array(times), last
 
     if world > 1:
@@ -264,8 +268,8 @@ def main():
     with ClockSampler(local) as clk:
         t_dev, m_dev = timed(step_device, args.steps)
         t_e2e, m_host = timed(step_host, args.steps)
-        s_dev, s_lat = served_leg(slots, args.steps, False, torch, dev)
-        s_e2e, s_lat_e2e = served_leg(slots, args.steps, True, torch, dev)
+        s_dev, s_lat, s_stages = served_leg(slots, args.steps, False, torch, dev)
+        s_e2e, s_lat_e2e, _ = served_leg(slots, args.steps, True, torch, dev)
     torch.cuda.synchronize(dev)
     if world > 1:
         dist.barrier()
@@ -300,16 +304,20 @@ def main():
         pass
     peak_hbm = float(peaks.get("hbm_gbs", 6800.0))
     M = st.nodes
-    iters = max(st.cg_iterations[:depth + 1])
+    # algorithmic bytes of one CG row-iteration: 27 neighbour indices (108 B), the row's
+    # residual and previous direction read (8 B), its new direction and residual written
+    # (8 B); the neighbours' values are the same vectors, counted once per row
+    row_bytes = 124
     cg_bytes = 0
     for d in range(depth + 1):
-        cg_bytes += st.level_count[d] * 152 * st.cg_iterations[d]
-    solve_ms = st.stage_ms[2]
-    roofline = {"bound": "hbm", "kernel": "k_cg_cluster (per-depth CG, thread-block clusters)",
-                "achieved": cg_bytes / (solve_ms * 1e-3) / 1e9 if solve_ms > 0 else None, "peak": peak_hbm,
+        cg_bytes += st.level_count[d] * row_bytes * st.cg_iterations[d]
+    cg_ms = float(np.mean(cg_samples)) if cg_samples else st.cg_kernel_ms
+    roofline = {"bound": "hbm", "kernel": "k_cg_cluster (per-depth CG, one thread-block cluster per depth group)",
+                "achieved": cg_bytes / (cg_ms * 1e-3) / 1e9 if cg_ms > 0 else None, "peak": peak_hbm,
                 "unit": "GB/s", "frac": None, "traffic": None,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s",
-                "algorithmic_bytes": cg_bytes, "launch_ms": solve_ms}
+                "algorithmic_bytes": cg_bytes, "launch_ms": cg_ms,
+                "note": "vectors and neighbour table stay in L2 (DRAM traffic ~10 MB per launch): latency bound"}
     if roofline["achieved"]:
         roofline["frac"] = roofline["achieved"] / peak_hbm
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -328,7 +336,8 @@ def main():
             "served_vs_plain": value / plain_value,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": K * h2d, "d2h_bytes_per_step": K * d2h,
                     "p50_ms": float(np.median(s_lat_e2e)), "p99_ms": float(np.percentile(s_lat_e2e, 99))},
-            "stage_ms": [round(x, 4) for x in st.stage_ms], "nodes": M, "cg_iterations": list(st.cg_iterations[:depth + 1]),
+            "stage_ms": [round(x, 4) for x in st.stage_ms], "served_stage_ms": s_stages,
+            "cg_depth_ms": [round(x, 4) for x in st.cg_depth_ms[:depth + 1]], "nodes": M, "cg_iterations": list(st.cg_iterations[:depth + 1]),
             "mesh": {"vertices": m_host.vertex_count, "triangles": m_host.triangle_count},
             "gpu_launches": int(st_launches(r)) * K,
             "roofline": roofline, "clocks": clocks}
@@ -423,7 +432,8 @@ def served_leg(slots, steps, host, torch, dev):
         torch.cuda.synchronize(dev)
         batch_ms.append(max(start.elapsed_time(e) for e in ends))
         lat.extend(1000.0 * t for t in times)
-    return np.array(batch_ms), np.array(lat)
+    stages = np.mean([list(sl.r.stats().stage_ms) for sl in slots], axis=0)
+    return np.array(batch_ms), np.array(lat), [round(float(x), 4) for x in stages]
 
 
 def st_launches(r):

@@ -95,6 +95,8 @@ typedef struct psr_stats {
     float stage_ms[6];     /* octree, field, solve, mesh, transfer, total (device time) */
     int kernel_launches;   /* kernels launched by the call (CUDA-graph kernel nodes) */
     int graph_replay;      /* 1 when the call replayed a captured CUDA graph */
+    float cg_kernel_ms;    /* device time of the CG kernel alone (part of stage_ms[2]) */
+    float cg_depth_ms[10]; /* device time of each depth's CG (depths solve concurrently) */
 } psr_stats;
 
 typedef struct psr_handle psr_handle;

@@ -48,7 +48,7 @@ struct psr_handle {
     void* arena = nullptr;
     size_t arena_bytes = 0;
     cudaStream_t own_stream = nullptr;
-    cudaEvent_t ev[6] = {};
+    cudaEvent_t ev[7] = {};   // stage boundaries 0..5, end of the CG kernel 6
     Counters host_cnt;
     bool have_result = false;
     std::string last_error;
@@ -206,7 +206,9 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     A.add(ws.vfield, 3 * (size_t)dnodes);
     A.add(ws.divg, (size_t)nodes);
     A.add(ws.xsol, (size_t)nodes);
-    A.add(ws.cg_r, (size_t)nodes); A.add(ws.cg_p, (size_t)nodes); A.add(ws.cg_ap, (size_t)nodes);
+    A.add(ws.cg_r, (size_t)nodes); A.add(ws.cg_p, (size_t)nodes); A.add(ws.cg_q, (size_t)nodes);
+    A.add(ws.cg_ap, (size_t)nodes);
+    A.add(ws.cg_blk, (size_t)nodes * 8 + 64);
     A.add(ws.cg_partial, std::max((size_t)nodes, (size_t)4096 * (kMaxDepth + 1)));
     A.add(ws.point_val, (size_t)N);
     A.add(ws.iso_partial, (size_t)ws.num_sms * 8 + 64);
@@ -266,7 +268,11 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     e = cudaMallocHost(&ws.cnt_host, sizeof(Counters));
     if (e == cudaSuccess) e = cudaMallocHost(&h->h_params, 16 * sizeof(int));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
-    for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&h->ev[i]);
+    for (int i = 0; i < 7 && e == cudaSuccess; ++i) e = cudaEventCreate(&h->ev[i]);
+    h->ws.ev_cg = h->ev[6];
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ws.aux, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ws.ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ws.ev_join, cudaEventDisableTiming);
     // tables
     if (e == cudaSuccess) e = upload_tables_octree();
     if (e == cudaSuccess) e = upload_tables_field();
@@ -302,7 +308,10 @@ psr_status psr_destroy(psr_handle* h) {
     if (h->arena) cudaFree(h->arena);
     if (h->ws.cnt_host) cudaFreeHost(h->ws.cnt_host);
     if (h->h_params) cudaFreeHost(h->h_params);
-    for (int i = 0; i < 6; ++i) if (h->ev[i]) cudaEventDestroy(h->ev[i]);
+    for (int i = 0; i < 7; ++i) if (h->ev[i]) cudaEventDestroy(h->ev[i]);
+    if (h->ws.ev_fork) cudaEventDestroy(h->ws.ev_fork);
+    if (h->ws.ev_join) cudaEventDestroy(h->ws.ev_join);
+    if (h->ws.aux) cudaStreamDestroy(h->ws.aux);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
     return PSR_OK;
@@ -423,6 +432,8 @@ psr_status psr_reconstruct(psr_handle* h, const psr_points* pts, const psr_optio
     st.graph_replay = h->last_graph;
     for (int i = 0; i < 5; ++i) cudaEventElapsedTime(&st.stage_ms[i], h->ev[i], h->ev[i + 1]);
     cudaEventElapsedTime(&st.stage_ms[5], h->ev[0], h->ev[5]);
+    cudaEventElapsedTime(&st.cg_kernel_ms, h->ev[2], h->ev[6]);
+    for (int d = 0; d <= kMaxDepth; ++d) st.cg_depth_ms[d] = (float)(c.cg_depth_ns[d] * 1e-6);
     if (c.error & kErrInvalid) return fail(h, PSR_INVALID_INPUT, "non-finite input or malformed octree");
     if (c.error & kErrCapacity) return fail(h, PSR_OUT_OF_CAPACITY, "a device count exceeded its capacity");
     if (c.error & kErrSpinTimeout) return fail(h, PSR_DEVICE_TIMEOUT, "a bounded device wait gave up");

@@ -222,13 +222,6 @@ __global__ void __launch_bounds__(kBlock) k_div_coarse_reduce(const Counters* c,
     }
 }
 
-static inline int grid_for(const Workspace& ws, long long work) {
-    long long g = (work + kBlock - 1) / kBlock;
-    long long cap = (long long)ws.num_sms * 8;
-    if (g > cap) g = cap;
-    return (int)(g < 1 ? 1 : g);
-}
-
 cudaError_t field_build(Workspace& ws) {
     cudaStream_t s = ws.stream;
     const int D = ws.depth;

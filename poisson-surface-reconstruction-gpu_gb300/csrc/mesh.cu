@@ -1198,13 +1198,6 @@ __global__ void k_count_parts(Counters* c, int* n_parts, int* n_staged_v, int* n
     }
 }
 
-static inline int grid_for(const Workspace& ws, long long work) {
-    long long g = (work + kBlock - 1) / kBlock;
-    long long cap = (long long)ws.num_sms * 8;
-    if (g > cap) g = cap;
-    return (int)(g < 1 ? 1 : g);
-}
-
 cudaError_t mesh_build_impl(Workspace& ws, const MeshBufs& mb) {
     cudaStream_t s = ws.stream;
     const int D = ws.depth;

@@ -14,11 +14,12 @@ namespace psr {
 // bounding box (mesh/BuildOctree.cu:51-133) and normalisation parameters (:619-631)
 // ------------------------------------------------------------------------------------
 __global__ void k_reset_counters(Counters* c, const int* params) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        const int n_points = params[0];
-        char* p = (char*)c;
-        for (size_t i = 0; i < sizeof(Counters); ++i) p[i] = 0;
-        c->n_points = n_points;
+    static_assert(sizeof(Counters) % 4 == 0, "Counters is cleared word by word");
+    unsigned* w = (unsigned*)c;
+    for (int i = threadIdx.x; i < (int)(sizeof(Counters) / 4); i += blockDim.x) w[i] = 0u;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        c->n_points = params[0];
         for (int a = 0; a < 3; ++a) {
             // the reference seeds its reduction with -1e6 / 1e6
             ((int*)c->bbox_max)[a] = float_to_ordered(-1e6f);
@@ -404,13 +405,6 @@ __global__ void k_root_neighbours(int* neigh, size_t stride) {
     if (k < 27) neigh[(size_t)k * stride] = (k == 13) ? 0 : -1;
 }
 
-static inline int grid_for(const Workspace& ws, long long work) {
-    long long g = (work + kBlock - 1) / kBlock;
-    long long cap = (long long)ws.num_sms * 8;
-    if (g > cap) g = cap;
-    return (int)(g < 1 ? 1 : g);
-}
-
 cudaError_t octree_build(Workspace& ws) {
     cudaStream_t s = ws.stream;
     const int D = ws.depth;
@@ -418,7 +412,7 @@ cudaError_t octree_build(Workspace& ws) {
     unsigned* err = &c->error;
     unsigned* total = (unsigned*)&c->scan_total;
     const int gp = grid_for(ws, ws.cap.points);
-    k_reset_counters<<<1, 1, 0, s>>>(c, ws.d_params);
+    k_reset_counters<<<1, 256, 0, s>>>(c, ws.d_params);
     k_bbox<<<gp, kBlock, 0, s>>>(ws.in_xyz, ws.in_nrm, c);
     k_bbox_finalize<<<1, 1, 0, s>>>(c, 1.25f);
     k_encode<<<gp, kBlock, 0, s>>>(ws.in_xyz, c, D, ws.code, ws.sidx);

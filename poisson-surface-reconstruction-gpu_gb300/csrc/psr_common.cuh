@@ -43,6 +43,7 @@ struct Counters {
     float iso;
     int cg_iters[kMaxDepth + 1];
     double cg_rr[kMaxDepth + 1];
+    unsigned long long cg_depth_ns[kMaxDepth + 1];   // device time of each depth's CG
 };
 
 // Look-up tables shared by the kernels (values derived in tables.cpp).
@@ -88,6 +89,59 @@ __device__ __forceinline__ float basis32(int idx, float x) {
     if (a < 0.5f) return __fmul_rn(__fsub_rn(0.75f, __fmul_rn(t, t)), kF43);
     if (a < 1.5f) { float u = __fsub_rn(1.5f, a); return __fmul_rn(__fmul_rn(u, u), kF23); }
     return 0.0f;
+}
+
+// ---- float-float ("double-float") accumulation ---------------------------------------
+// GB300 executes FP64 at a small fraction of its FP32 rate, so sums that need more than
+// FP32 precision are carried as an unevaluated pair hi + lo of floats (|lo| <= ulp(hi)/2):
+// Knuth's TwoSum for the error of an addition, Dekker's FastTwoSum to renormalise, and
+// the fused multiply-add for the exact error of a product (Dekker's TwoProduct).
+// About 44 significant bits; the order of operations is fixed, so sums are deterministic.
+struct FF {
+    float hi, lo;
+};
+
+__device__ __forceinline__ FF ff_zero() { return FF{0.0f, 0.0f}; }
+
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+    const float s = __fadd_rn(a.hi, b.hi);
+    const float bv = __fsub_rn(s, a.hi);
+    const float av = __fsub_rn(s, bv);
+    float e = __fadd_rn(__fsub_rn(a.hi, av), __fsub_rn(b.hi, bv));   // a.hi + b.hi = s + e exactly
+    e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+    const float h = __fadd_rn(s, e);
+    return FF{h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+
+__device__ __forceinline__ FF ff_add_float(FF a, float b) { return ff_add(a, FF{b, 0.0f}); }
+
+// exact product of two floats as a float pair
+__device__ __forceinline__ FF ff_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    return FF{p, fmaf(a, b, -p)};
+}
+
+__device__ __forceinline__ FF ff_shfl_xor(FF v, int o) {
+    return FF{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+}
+
+// warp-wide sum (butterfly; every lane ends with the same value)
+__device__ __forceinline__ FF ff_warp_sum(FF v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = ff_add(v, ff_shfl_xor(v, o));
+    return v;
+}
+
+__device__ __forceinline__ float ff_to_float(FF a) { return __fadd_rn(a.hi, a.lo); }
+
+// a / b rounded to float: float quotient of the leading parts, then one correction step
+// with the remainder a - q b evaluated with fused multiply-adds
+__device__ __forceinline__ float ff_div(FF a, FF b) {
+    const float q = __fdiv_rn(a.hi, b.hi);
+    float r = fmaf(-q, b.hi, a.hi);   // exact: a.hi - q * b.hi
+    r = __fadd_rn(r, a.lo);
+    r = fmaf(-q, b.lo, r);
+    return __fadd_rn(q, __fdiv_rn(r, b.hi));
 }
 
 #endif  // __CUDACC__

@@ -23,182 +23,332 @@ namespace cg = cooperative_groups;
 
 namespace psr {
 
-// ---- cluster CG -----------------------------------------------------------------------
-// Each thread-block cluster owns whole depths (cluster 0: depth D; cluster 1: depths
-// 0..D-1).  Barriers are cluster barriers (hardware), reductions go through distributed
-// shared memory: every CTA writes its per-depth partial sums to its own shared memory,
-// and after the barrier every CTA sums the partials of all CTAs of the cluster in rank
-// order (identical result in every CTA, deterministic).  Partial buffers alternate
-// between two slots so a slot is only rewritten after a barrier that follows its reads.
+// ---- per-depth CG ---------------------------------------------------------------------
+// Every depth is an independent system.  The two finest depths (most rows, most
+// iterations) get one thread-block cluster each (k_cg_cluster: cluster barriers, sums
+// through distributed shared memory); the coarser depths get one CTA each (k_cg_cta,
+// launched concurrently on a second stream).  Both run the same solver body: a cluster
+// of one CTA is a CTA.
+//
+// Reductions: each CTA sums its threads' terms (warp butterflies, then one warp over the
+// warp partials), writes the sum to its shared memory, and after the barrier one warp of
+// every CTA sums the CTAs' values in a fixed order, so every CTA holds the same result.
+// Sums are float pairs (FF: GB300's FP64 rate is far below its FP32 rate) and products
+// enter exactly (fma), so p.Ap and r.r carry about 44 bits.  The partial buffers
+// alternate between two slots, so a slot is only rewritten after a barrier that follows
+// its reads.
+//
+// One iteration costs two barriers: the direction update p = r + beta p is fused into the
+// operator application (a row's neighbours rebuild their p values from r and the
+// previous p), so the FP32 operations per element are the textbook loop's:
+//   p_k = fma(beta, p_{k-1}, r_k)   Ap = sum_k st_k p_k[nb]   alpha = rr / (p.Ap)
+//   x = fma(alpha, p, x)            r = fma(-alpha, Ap, r)    beta = rr_new / rr
+// Missing neighbours contribute fma(st_k, 0, y) = y, the same as skipping them.
+//
+// Resident path (depth >= 1 and at most kCgSmemRows rows per CTA): each CTA owns a
+// contiguous, sibling-group aligned chunk of rows and keeps (r_k, p_{k-1}) in shared
+// memory (two buffers alternating per iteration), plus A p and x.  The operator is
+// applied per sibling group: the 8 children of one parent have all their 27-neighbours
+// inside one 4x4x4 block of same-depth nodes, listed once per group in the block table
+// (k_cg_blocks).  Each lane of a warp (4 groups of 8 siblings) fetches 8 block entries
+// (local shared memory or a remote CTA's through distributed shared memory), the group's
+// 64 p values go to a per-warp shared block, and each lane applies its 27-point stencil
+// from there.  Otherwise (the root, or more rows than fit) the vectors live in global
+// memory and the neighbour table is read row by row.
 constexpr int kCgcBlock = 1024;
+constexpr int kCgWarps = kCgcBlock / 32;
+constexpr int kCgSmemRows = 7168;
+constexpr size_t kCgRowBytes = 2 * sizeof(float2) + 2 * sizeof(float);   // r/p x2, A p, x
+// per-warp shared block of 4 sibling groups: group gi at gi * 80 + {0, 18, 8, 26}[gi]
+// floats, so the 4 groups start in banks 0, 2, 8, 10 and the 32 lanes' stencil reads (at
+// sibling offsets {0,1,4,5,16,17,20,21} + a common neighbour offset) hit 32 distinct banks
+constexpr int kCgWarpBlockFloats = 352;
+constexpr size_t kCgBlockBytes = (size_t)kCgWarps * kCgWarpBlockFloats * sizeof(float);
+constexpr size_t kCgSmemBytes = (size_t)kCgSmemRows * kCgRowBytes + kCgBlockBytes;
+static_assert(kCgSmemRows % 32 == 0, "whole warp slots");
 
 struct CgcArgs {
     const Counters* c;
     Counters* cw;
     int depth;
-    const int* ndepth;
+    int first;          // depth of cluster / CTA 0; unit u solves depth first - u
     const int* neigh;
+    const int* blk;     // block table: 64 entries per sibling group of depth >= 1
     size_t stride;
     const float* stencil;
     const float* b;
     float* x;
     float* r;
-    float* p;
+    float* pa;
+    float* pb;
     float* ap;
-    double tol2;
+    float tol2;
     int max_iter;
 };
 
-__device__ __forceinline__ void cgc_cta_partials(const double (&acc)[kMaxDepth + 1], int nd, double* s_warp,
-                                                 double* s_slot) {
+struct CgcShared {
+    FF warp[kCgWarps];
+    FF slot[2];
+    FF sum;
+    float st[27];
+};
+static_assert(kCgSmemBytes + sizeof(CgcShared) <= 227 * 1024, "shared memory of one CTA");
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Sum of every thread's `v` over the cluster, returned to every thread.  Contains the
+// cluster barrier; identical in every CTA.
+__device__ __forceinline__ FF cgc_allreduce(cg::cluster_group& cl, CgcShared& sh, int& buf, FF v) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int d = 0; d <= kMaxDepth; ++d) {
-        if (d >= nd) break;
-        double v = acc[d];
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0) s_warp[warp * (kMaxDepth + 1) + d] = v;
-    }
+    v = ff_warp_sum(v);
+    if (lane == 0) sh.warp[warp] = v;
     __syncthreads();
-    if (threadIdx.x < nd) {
-        double s = 0.0;
-        for (int w = 0; w < kCgcBlock / 32; ++w) s += s_warp[w * (kMaxDepth + 1) + threadIdx.x];
-        s_slot[threadIdx.x] = s;
+    if (warp == 0) {
+        FF w = ff_warp_sum(sh.warp[lane]);
+        if (lane == 0) sh.slot[buf] = w;
+    }
+    cl.sync();
+    if (warp == 0) {
+        const unsigned nb = cl.num_blocks();
+        FF w = ff_zero();
+        if ((unsigned)lane < nb) w = *cl.map_shared_rank(&sh.slot[buf], (unsigned)lane);
+        w = ff_warp_sum(w);
+        if (lane == 0) sh.sum = w;
+    }
+    buf ^= 1;
+    __syncthreads();
+    return sh.sum;
+}
+
+// position of neighbour k (9 ox + 3 oy + oz) of sibling s (x = 4, y = 2, z = 1) in the
+// group's 4x4x4 block (16 bx + 4 by + bz)
+__host__ __device__ constexpr int cg_kpos(int k) { return 16 * (k / 9) + 4 * ((k / 3) % 3) + (k % 3); }
+__device__ __forceinline__ int cg_spos(int s) { return 16 * ((s >> 2) & 1) + 4 * ((s >> 1) & 1) + (s & 1); }
+
+// Block table of every sibling group (depth >= 1; group G = rows 1 + 8G .. 8 + 8G):
+// block position (bx, by, bz) holds neighbour (ox, oy, oz) of sibling (cx, cy, cz) with
+// b = c + o, taking c = 1 on an axis where b >= 2, else 0.  Stored transposed: table
+// entry j of a group is position (j & 7) * 8 + (j >> 3), so lane s of a group reads its
+// 8 positions s, s + 8, ... as two contiguous int4.
+__global__ void __launch_bounds__(kBlock) k_cg_blocks(const Counters* c, const int* neigh, size_t stride,
+                                                      int* blk) {
+    const int ngroups = (c->n_nodes - 1) >> 3;
+    PSR_GRID_STRIDE(t, ngroups * 64) {
+        const int G = t >> 6, j = t & 63;
+        const int pos = ((j & 7) << 3) | (j >> 3);
+        const int bx = pos >> 4, by = (pos >> 2) & 3, bz = pos & 3;
+        const int cx = bx >= 2, cy = by >= 2, cz = bz >= 2;
+        const int k = 9 * (bx - cx) + 3 * (by - cy) + (bz - cz);
+        const int sib = 4 * cx + 2 * cy + cz;
+        blk[t] = neigh[(size_t)k * stride + 1 + 8 * G + sib];
     }
 }
 
-// after cluster.sync: sum slot `buf` of every CTA in rank order
-__device__ __forceinline__ void cgc_cluster_sum(cg::cluster_group& cl, double* s_slot, int nd, double* out) {
-    if (threadIdx.x < nd) {
-        double s = 0.0;
-        const unsigned nb = cl.num_blocks();
-        for (unsigned k = 0; k < nb; ++k) {
-            const double* rem = cl.map_shared_rank(s_slot, k);
-            s += rem[threadIdx.x];
-        }
-        out[threadIdx.x] = s;
+struct CgUnit {
+    int d, row0, row1;
+};
+
+// Resident path.  CTA k of the cluster owns rows [row0 + k*chunk, row0 + (k+1)*chunk).
+__device__ __forceinline__ void cgc_resident(cg::cluster_group& cl, CgcShared& sh, const CgcArgs& a,
+                                             const CgUnit& u, int chunk, float2* rp0, float2* rp1, float* sap,
+                                             float* sx, float* sblk) {
+    const unsigned me = cl.block_rank();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int m = u.row1 - u.row0;
+    const int mlo = u.row0 + (int)me * chunk;
+    const int nloc = max(0, min(chunk, m - (int)me * chunk));
+    const int nslot = (nloc + 31) >> 5;
+    const int gi = lane >> 3, sib = lane & 7;
+    const int spos = cg_spos(sib);
+    float* myblk = sblk + warp * kCgWarpBlockFloats + gi * 80 + ((0x1a081200 >> (gi * 8)) & 0xff);
+    const int gbase = (mlo - 1) >> 3;   // block-table group of local row 0
+    // r0 = b, p_{-1} = 0, x0 = 0
+    FF acc = ff_zero();
+    for (int l = threadIdx.x; l < nloc; l += kCgcBlock) {
+        const float bi = a.b[mlo + l];
+        rp0[l] = make_float2(bi, 0.0f);
+        sx[l] = 0.0f;
+        acc = ff_add(acc, ff_prod(bi, bi));
     }
+    int buf = 0;
+    FF rr = cgc_allreduce(cl, sh, buf, acc);
+    bool active = ff_to_float(rr) > a.tol2;
+    bool ran = false;
+    float beta = 0.0f;
+    float2* cur = rp0;
+    float2* nxt = rp1;
+    int it = 1;
+    while (active && it <= a.max_iter) {
+        // (A) own p_k, A p_k from the neighbours' (r_k, p_{k-1}), p.Ap
+        acc = ff_zero();
+        for (int sl = warp; sl < nslot; sl += kCgWarps) {
+            const int l = sl * 32 + lane;
+            const bool mine = l < nloc;   // whole groups: a group is all in or all out
+            if (mine) {
+                const int4* bp = reinterpret_cast<const int4*>(a.blk + (size_t)(gbase + (l >> 3)) * 64 + sib * 8);
+                const int4 q0 = __ldg(bp), q1 = __ldg(bp + 1);
+                const int ids[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    const int nb = ids[e];
+                    float val = 0.0f;
+                    const int gl = nb - mlo;
+                    if ((unsigned)gl < (unsigned)nloc) {
+                        const float2 v = cur[gl];
+                        val = fmaf(beta, v.y, v.x);
+                    } else if (nb >= 0) {
+                        const int g = nb - u.row0;
+                        if ((unsigned)g < (unsigned)m) {
+                            const int owner = g / chunk;
+                            const float2 v = *cl.map_shared_rank(cur + (g - owner * chunk), (unsigned)owner);
+                            val = fmaf(beta, v.y, v.x);
+                        }
+                    }
+                    myblk[e * 8 + sib] = val;
+                }
+            }
+            __syncwarp();
+            if (mine) {
+                float y = 0.0f;
+#pragma unroll
+                for (int k = 0; k < 27; ++k) y = fmaf(sh.st[k], myblk[spos + cg_kpos(k)], y);
+                const float2 own = cur[l];
+                const float pi = fmaf(beta, own.y, own.x);
+                nxt[l].y = pi;
+                sap[l] = y;
+                acc = ff_add(acc, ff_prod(pi, y));
+            }
+            __syncwarp();
+        }
+        const FF pap = cgc_allreduce(cl, sh, buf, acc);
+        const float alpha = (pap.hi != 0.0f) ? ff_div(rr, pap) : 0.0f;
+        // (B) x and r, r.r
+        acc = ff_zero();
+        for (int sl = warp; sl < nslot; sl += kCgWarps) {
+            const int l = sl * 32 + lane;
+            if (l < nloc) {
+                const float pi = nxt[l].y;
+                sx[l] = fmaf(alpha, pi, sx[l]);
+                const float ri = fmaf(-alpha, sap[l], cur[l].x);
+                nxt[l].x = ri;
+                acc = ff_add(acc, ff_prod(ri, ri));
+            }
+        }
+        const FF rn = cgc_allreduce(cl, sh, buf, acc);
+        beta = (rr.hi != 0.0f) ? ff_div(rn, rr) : 0.0f;
+        rr = rn;
+        ran = true;
+        if (me == 0 && threadIdx.x == 0) a.cw->cg_iters[u.d] = it;
+        active = (ff_to_float(rn) > a.tol2) && pap.hi != 0.0f && it + 1 <= a.max_iter;
+        float2* t = cur;
+        cur = nxt;
+        nxt = t;
+        ++it;
+    }
+    for (int l = threadIdx.x; l < nloc; l += kCgcBlock) {
+        a.x[mlo + l] = sx[l];
+        a.r[mlo + l] = cur[l].x;
+    }
+    if (ran && me == 0 && threadIdx.x == 0) a.cw->cg_rr[u.d] = (double)rr.hi + (double)rr.lo;
+}
+
+// Global-memory path (any size, any depth).
+__device__ __forceinline__ void cgc_global(cg::cluster_group& cl, CgcShared& sh, const CgcArgs& a,
+                                           const CgUnit& u) {
+    const int tid = cl.block_rank() * blockDim.x + threadIdx.x;
+    const int nthr = cl.num_blocks() * blockDim.x;
+    FF acc = ff_zero();
+    for (int i = u.row0 + tid; i < u.row1; i += nthr) {
+        const float bi = a.b[i];
+        a.r[i] = bi;
+        a.pa[i] = 0.0f;
+        a.x[i] = 0.0f;
+        acc = ff_add(acc, ff_prod(bi, bi));
+    }
+    int buf = 0;
+    FF rr = cgc_allreduce(cl, sh, buf, acc);
+    bool active = ff_to_float(rr) > a.tol2;
+    bool ran = false;
+    float beta = 0.0f;
+    const float* pprev = a.pa;
+    float* pcur = a.pb;
+    int it = 1;
+    while (active && it <= a.max_iter) {
+        acc = ff_zero();
+        for (int i = u.row0 + tid; i < u.row1; i += nthr) {
+            const float pi = fmaf(beta, pprev[i], a.r[i]);
+            float y = 0.0f;
+#pragma unroll 9
+            for (int k = 0; k < 27; ++k) {
+                const int nb = __ldg(&a.neigh[(size_t)k * a.stride + i]);
+                if (nb >= 0) y = fmaf(sh.st[k], fmaf(beta, pprev[nb], a.r[nb]), y);
+            }
+            pcur[i] = pi;
+            a.ap[i] = y;
+            acc = ff_add(acc, ff_prod(pi, y));
+        }
+        const FF pap = cgc_allreduce(cl, sh, buf, acc);
+        const float alpha = (pap.hi != 0.0f) ? ff_div(rr, pap) : 0.0f;
+        acc = ff_zero();
+        for (int i = u.row0 + tid; i < u.row1; i += nthr) {
+            a.x[i] = fmaf(alpha, pcur[i], a.x[i]);
+            const float ri = fmaf(-alpha, a.ap[i], a.r[i]);
+            a.r[i] = ri;
+            acc = ff_add(acc, ff_prod(ri, ri));
+        }
+        const FF rn = cgc_allreduce(cl, sh, buf, acc);
+        beta = (rr.hi != 0.0f) ? ff_div(rn, rr) : 0.0f;
+        rr = rn;
+        ran = true;
+        if (cl.block_rank() == 0 && threadIdx.x == 0) a.cw->cg_iters[u.d] = it;
+        active = (ff_to_float(rn) > a.tol2) && pap.hi != 0.0f && it + 1 <= a.max_iter;
+        float* t = const_cast<float*>(pprev);
+        pprev = pcur;
+        pcur = t;
+        ++it;
+    }
+    if (ran && cl.block_rank() == 0 && threadIdx.x == 0) a.cw->cg_rr[u.d] = (double)rr.hi + (double)rr.lo;
+}
+
+// one depth per cluster (a CTA when the launch has no cluster dimension)
+__device__ __forceinline__ void cg_unit_body(const CgcArgs& a, int unit) {
+    cg::cluster_group cl = cg::this_cluster();
+    __shared__ CgcShared sh;
+    extern __shared__ float4 cg_dyn[];
+    const unsigned long long t_start = global_ns();
+    CgUnit u;
+    u.d = a.first - unit;
+    u.row0 = a.c->level_base[u.d];
+    u.row1 = (u.d < a.depth) ? a.c->level_base[u.d + 1] : a.c->n_nodes;
+    if (threadIdx.x < 27) sh.st[threadIdx.x] = a.stencil[u.d * 27 + threadIdx.x];
     __syncthreads();
+    const int nblk = (int)cl.num_blocks();
+    const int m = u.row1 - u.row0;
+    const int chunk = ((m + nblk - 1) / nblk + 7) & ~7;   // sibling-group aligned
+    if (u.d >= 1 && chunk <= kCgSmemRows) {   // uniform over the cluster
+        float2* rp0 = reinterpret_cast<float2*>(cg_dyn);
+        float2* rp1 = rp0 + kCgSmemRows;
+        float* sap = reinterpret_cast<float*>(rp1 + kCgSmemRows);
+        float* sx = sap + kCgSmemRows;
+        float* sblk = sx + kCgSmemRows;
+        cgc_resident(cl, sh, a, u, chunk, rp0, rp1, sap, sx, sblk);
+    } else {
+        cgc_global(cl, sh, a, u);
+    }
+    cl.sync();   // no CTA exits while others may still read its shared memory
+    if (cl.block_rank() == 0 && threadIdx.x == 0) a.cw->cg_depth_ns[u.d] = global_ns() - t_start;
 }
 
 __global__ void __launch_bounds__(kCgcBlock) k_cg_cluster(CgcArgs a) {
     cg::cluster_group cl = cg::this_cluster();
-    __shared__ double s_warp[(kCgcBlock / 32) * (kMaxDepth + 1)];
-    __shared__ double s_slot[2][kMaxDepth + 1];
-    __shared__ double s_rr[kMaxDepth + 1], s_pap[kMaxDepth + 1], s_new[kMaxDepth + 1];
-    __shared__ float s_alpha[kMaxDepth + 1], s_beta[kMaxDepth + 1];
-    __shared__ int s_active[kMaxDepth + 1];
-    __shared__ float s_st[(kMaxDepth + 1) * 27];
-    const int D = a.depth;
-    const int nd = D + 1;
-    const int cid = blockIdx.x / cl.num_blocks();
-    // rows owned by this cluster
-    const int bD = a.c->level_base[D];
-    const int row0 = (cid == 0) ? bD : 0;
-    const int row1 = (cid == 0) ? a.c->n_nodes : bD;
-    const int tid = cl.block_rank() * blockDim.x + threadIdx.x;
-    const int nthr = cl.num_blocks() * blockDim.x;
-    for (int q = threadIdx.x; q < nd * 27; q += blockDim.x) s_st[q] = a.stencil[q];
-    double acc[kMaxDepth + 1];
-#pragma unroll
-    for (int d = 0; d <= kMaxDepth; ++d) acc[d] = 0.0;
-    for (int i = row0 + tid; i < row1; i += nthr) {
-        const float bi = a.b[i];
-        a.r[i] = bi;
-        a.p[i] = bi;
-        a.x[i] = 0.0f;
-        const int d = a.ndepth[i];
-#pragma unroll
-        for (int q = 0; q <= kMaxDepth; ++q) if (q == d) acc[q] += (double)(bi * bi);
-    }
-    int buf = 0;
-    cgc_cta_partials(acc, nd, s_warp, s_slot[buf]);
-    cl.sync();
-    cgc_cluster_sum(cl, s_slot[buf], nd, s_rr);
-    buf ^= 1;
-    // a depth is active in the cluster that owns it
-    if (threadIdx.x < nd) {
-        const int d = threadIdx.x;
-        const bool mine = (cid == 0) ? (d == D) : (d < D);
-        s_active[d] = (mine && (double)(float)s_rr[d] > a.tol2) ? 1 : 0;
-    }
-    __syncthreads();
-    int any = 0;
-    for (int d = 0; d < nd; ++d) any |= s_active[d];
-    int it = 1;
-    while (any && it <= a.max_iter) {
-        // SpMV and p.Ap
-#pragma unroll
-        for (int d = 0; d <= kMaxDepth; ++d) acc[d] = 0.0;
-        for (int i = row0 + tid; i < row1; i += nthr) {
-            const int d = a.ndepth[i];
-            if (!s_active[d]) continue;
-            const float* st = &s_st[d * 27];
-            float y = 0.0f;
-#pragma unroll
-            for (int k = 0; k < 27; ++k) {
-                const int nb = a.neigh[(size_t)k * a.stride + i];
-                if (nb >= 0) y = fmaf(st[k], a.p[nb], y);
-            }
-            a.ap[i] = y;
-            const float pi = a.p[i];
-#pragma unroll
-            for (int q = 0; q <= kMaxDepth; ++q) if (q == d) acc[q] += (double)(pi * y);
-        }
-        cgc_cta_partials(acc, nd, s_warp, s_slot[buf]);
-        cl.sync();
-        cgc_cluster_sum(cl, s_slot[buf], nd, s_pap);
-        buf ^= 1;
-        if (threadIdx.x < nd) {
-            const int d = threadIdx.x;
-            s_alpha[d] = (s_active[d] && s_pap[d] != 0.0) ? (float)(s_rr[d] / s_pap[d]) : 0.0f;
-        }
-        __syncthreads();
-        // x, r and r.r
-#pragma unroll
-        for (int d = 0; d <= kMaxDepth; ++d) acc[d] = 0.0;
-        for (int i = row0 + tid; i < row1; i += nthr) {
-            const int d = a.ndepth[i];
-            if (!s_active[d]) continue;
-            const float al = s_alpha[d];
-            a.x[i] = fmaf(al, a.p[i], a.x[i]);
-            const float ri = fmaf(-al, a.ap[i], a.r[i]);
-            a.r[i] = ri;
-#pragma unroll
-            for (int q = 0; q <= kMaxDepth; ++q) if (q == d) acc[q] += (double)(ri * ri);
-        }
-        cgc_cta_partials(acc, nd, s_warp, s_slot[buf]);
-        cl.sync();
-        cgc_cluster_sum(cl, s_slot[buf], nd, s_new);
-        buf ^= 1;
-        if (threadIdx.x < nd) {
-            const int d = threadIdx.x;
-            if (s_active[d]) {
-                s_beta[d] = (s_rr[d] != 0.0) ? (float)(s_new[d] / s_rr[d]) : 0.0f;
-                s_rr[d] = s_new[d];
-                if (cl.block_rank() == 0) {
-                    a.cw->cg_iters[d] = it;
-                    a.cw->cg_rr[d] = s_new[d];
-                }
-                const bool go = ((double)(float)s_new[d] > a.tol2) && s_pap[d] != 0.0;
-                s_active[d] = (go && it + 1 <= a.max_iter) ? 1 : 0;
-            } else {
-                s_beta[d] = 0.0f;
-            }
-        }
-        __syncthreads();
-        for (int i = row0 + tid; i < row1; i += nthr) {
-            const int d = a.ndepth[i];
-            if (!s_active[d]) continue;
-            a.p[i] = fmaf(s_beta[d], a.p[i], a.r[i]);
-        }
-        any = 0;
-        for (int d = 0; d < nd; ++d) any |= s_active[d];
-        ++it;
-        cl.sync();   // p complete in the whole cluster before the next SpMV
-    }
-    cl.sync();   // no CTA exits while others may still read its shared memory
+    cg_unit_body(a, (int)(blockIdx.x / cl.num_blocks()));
 }
+
+__global__ void __launch_bounds__(kCgcBlock) k_cg_cta(CgcArgs a) { cg_unit_body(a, (int)blockIdx.x); }
 
 // ---- implicit function at the sample points and the iso-value ----------------------
 __device__ __forceinline__ void decode3s(int e, int depth, int& ix, int& iy, int& iz) {
@@ -275,10 +425,16 @@ static int g_cg_cluster = 0;
 void prepare_launch_configs(Workspace& ws) {
     if (g_cg_cluster == 0) {
         int size = 8;
+        if (cudaFuncSetAttribute(k_cg_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCgSmemBytes) !=
+                cudaSuccess ||
+            cudaFuncSetAttribute(k_cg_cta, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCgSmemBytes) !=
+                cudaSuccess)
+            return;   // left unset: the CG launch reports the error
         if (cudaFuncSetAttribute(k_cg_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
             cudaLaunchConfig_t cfg = {};
             cfg.gridDim = dim3(16);
             cfg.blockDim = dim3(kCgcBlock);
+            cfg.dynamicSmemBytes = kCgSmemBytes;
             cudaLaunchAttribute attr[1];
             attr[0].id = cudaLaunchAttributeClusterDimension;
             attr[0].val.clusterDim.x = 16;
@@ -296,41 +452,71 @@ void prepare_launch_configs(Workspace& ws) {
     (void)scan_grid(1 << 20);
 }
 
+static cudaError_t launch_cg(void (*kernel)(CgcArgs), CgcArgs& a, int grid, int cluster, cudaStream_t s) {
+    void* args[] = {&a};
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kCgcBlock);
+    cfg.dynamicSmemBytes = kCgSmemBytes;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelExC(&cfg, (const void*)kernel, args);
+}
+
 cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, int cg_max_iter) {
     cudaStream_t s = ws.stream;
     if (g_cg_cluster == 0) prepare_launch_configs(ws);
+    const int D = ws.depth;
     CgcArgs a;
     a.c = ws.cnt;
     a.cw = ws.cnt;
-    a.depth = ws.depth;
-    a.ndepth = ws.ndepth;
+    a.depth = D;
     a.neigh = ws.neigh;
+    a.blk = ws.cg_blk;
     a.stride = (size_t)ws.cap.nodes;
     a.stencil = ws.stencil;
     a.b = ws.divg;
     a.x = ws.xsol;
     a.r = ws.cg_r;
-    a.p = ws.cg_p;
+    a.pa = ws.cg_p;
+    a.pb = ws.cg_q;
     a.ap = ws.cg_ap;
-    float t2 = cg_tol * cg_tol;
-    a.tol2 = (double)t2;
+    a.tol2 = cg_tol * cg_tol;
     // a fixed iteration count replaces the reference's max_iter (10000); the tolerance
     // test of the loop is kept (mesh/solver/CGAlgorithm.cu:36)
     a.max_iter = (cg_mode == 1 && cg_iters > 0) ? cg_iters : cg_max_iter;
-    void* args[] = {&a};
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(2 * g_cg_cluster);
-    cfg.blockDim = dim3(kCgcBlock);
-    cfg.dynamicSmemBytes = 0;
-    cfg.stream = s;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = g_cg_cluster;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    cudaError_t e = cudaLaunchKernelExC(&cfg, (const void*)k_cg_cluster, args);
+    k_cg_blocks<<<grid_for(ws, 1 << 20), kBlock, 0, s>>>(ws.cnt, ws.neigh, (size_t)ws.cap.nodes, ws.cg_blk);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    // the finest depths (D, D-1, and D-2 from depth 5 on; never the root) on clusters, the
+    // rest one CTA each, concurrently on the second stream
+    const int ncl = D < 2 ? D : (D >= 5 ? 3 : 2);
+    const int ncta = D - ncl + 1;
+    e = cudaEventRecord(ws.ev_fork, s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ws.aux, ws.ev_fork, 0);
+    if (e == cudaSuccess && ncta > 0) {
+        CgcArgs b = a;
+        b.first = D - ncl;
+        e = launch_cg(k_cg_cta, b, ncta, 1, ws.aux);   // clusters of one CTA
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(ws.ev_join, ws.aux);
+    if (e != cudaSuccess) return e;
+    if (ncl > 0) {
+        a.first = D;
+        e = launch_cg(k_cg_cluster, a, ncl * g_cg_cluster, g_cg_cluster, s);
+        if (e != cudaSuccess) return e;
+    }
+    if (ws.ev_cg) {
+        e = cudaEventRecordWithFlags(ws.ev_cg, s, cudaEventRecordExternal);
+        if (e != cudaSuccess) return e;
+    }
+    e = cudaStreamWaitEvent(s, ws.ev_join, 0);
     if (e != cudaSuccess) return e;
     // iso-value
     const int nb = ws.num_sms * 4;

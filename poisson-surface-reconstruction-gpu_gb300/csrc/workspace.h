@@ -94,7 +94,9 @@ struct Workspace {
     float* vfield;          // 3 x dnodes (SoA: x block, y block, z block)
     float* divg;            // M
     float* xsol;            // M
-    float *cg_r, *cg_p, *cg_ap;
+    cudaEvent_t ev_cg = nullptr;   // recorded right after the CG kernel (stage timing)
+    float *cg_r, *cg_p, *cg_q, *cg_ap;   // residual, two direction buffers, A p
+    int* cg_blk;            // CG block table: 64 same-depth nodes per sibling group
     double* cg_partial;     // per-CTA per-depth partial sums
     float* point_val;       // N
     double* iso_partial;
@@ -148,8 +150,18 @@ struct Workspace {
     int* d_params;          // [0] point count of the current call (written before each run)
 
     cudaStream_t stream;
+    cudaStream_t aux = nullptr;         // second stream for work forked off `stream`
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int num_sms;
 };
+
+// grid of a grid-stride kernel over `work` items: enough blocks, at most 8 per SM
+inline int grid_for(const Workspace& ws, long long work) {
+    long long g = (work + kBlock - 1) / kBlock;
+    long long cap = (long long)ws.num_sms * 8;
+    if (g > cap) g = cap;
+    return (int)(g < 1 ? 1 : g);
+}
 
 // stage entry points (each issues kernels on ws.stream; no host synchronisation)
 cudaError_t octree_build(Workspace& ws);

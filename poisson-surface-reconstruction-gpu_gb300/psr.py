@@ -56,7 +56,8 @@ class PsrStats(ctypes.Structure):
                 ("mesh_triangles", ctypes.c_int), ("cg_iterations", ctypes.c_int * 10),
                 ("cg_residual", ctypes.c_double * 10), ("iso_value", ctypes.c_float),
                 ("error_bits", ctypes.c_uint), ("stage_ms", ctypes.c_float * 6),
-                ("kernel_launches", ctypes.c_int), ("graph_replay", ctypes.c_int)]
+                ("kernel_launches", ctypes.c_int), ("graph_replay", ctypes.c_int),
+                ("cg_kernel_ms", ctypes.c_float), ("cg_depth_ms", ctypes.c_float * 10)]
 
 
 _lib = None
