@@ -56,6 +56,76 @@ __device__ __forceinline__ void edge_center(float cx, float cy, float cz, int e,
     }
 }
 
+// Same-depth cells around a vertex, an edge or a face.  Neighbour slot k of a node is the
+// same-depth cell at offset (k/9 - 1, (k/3)%3 - 1, k%3 - 1).  Node centres, corners and
+// edge / face midpoints are dyadic, so the reference's test "centre within one cell width
+// of the point" is exact, and it holds for precisely these cells: the 8 cells whose offset
+// is 0 or the corner's side on every axis, the 4 around an edge, the 2 across a face.
+// Ownership (smallest key among those cells) and the back-pointers are evaluated on these
+// slots only, with the reference's slot numbering derived from the same offsets.
+__device__ __forceinline__ int nslot(int ax, int ay, int az) { return 9 * (ax + 1) + 3 * (ay + 1) + (az + 1); }
+
+// corner q: + side on x if bit 0, y if bit 1, z if bit 2
+__device__ __forceinline__ void corner_sides(int q, int& mx, int& my, int& mz) {
+    mx = (q & 1) ? 1 : -1;
+    my = (q & 2) ? 1 : -1;
+    mz = (q & 4) ? 1 : -1;
+}
+__device__ __forceinline__ unsigned vertex_cells(int q) {
+    int mx, my, mz;
+    corner_sides(q, mx, my, mz);
+    unsigned m = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) m |= 1u << nslot((j & 1) ? mx : 0, (j & 2) ? my : 0, (j & 4) ? mz : 0);
+    return m;
+}
+// edge e: axis e >> 2; the two other axes (increasing order) at sides 2 (e & 1) - 1 and
+// 2 ((e >> 1) & 1) - 1
+__device__ __forceinline__ void edge_offset(int e, int j, int a[3]) {
+    const int orient = e >> 2;
+    const int m[2] = {2 * (e & 1) - 1, 2 * ((e >> 1) & 1) - 1};
+    int dim = 0;
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        a[ax] = 0;
+        if (ax != orient) { a[ax] = ((j >> dim) & 1) ? m[dim] : 0; dim++; }
+    }
+}
+__device__ __forceinline__ unsigned edge_cells(int e) {
+    unsigned m = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        int a[3];
+        edge_offset(e, j, a);
+        m |= 1u << nslot(a[0], a[1], a[2]);
+    }
+    return m;
+}
+__device__ __forceinline__ unsigned face_cells(int f) {
+    int a[3] = {0, 0, 0};
+    a[f >> 1] = 2 * (f & 1) - 1;
+    return (1u << 13) | (1u << nslot(a[0], a[1], a[2]));
+}
+// vertex_slot() of the cell at offset a for corner sides m (centre minus corner is
+// (2 a - m) half widths on every axis)
+__device__ __forceinline__ int vertex_slot_of(int ax, int ay, int az, int mx, int my, int mz) {
+    int idx = 0;
+    if (2 * ax - mx < 0) idx |= 1;
+    if (2 * az - mz < 0) idx |= 4;
+    if (2 * ay - my < 0) idx += (idx & 1) ? 1 : 3;
+    return idx;
+}
+// edge slot of the cell at offset a around edge e (mesh/BuildMeshGeometry.cu:255-268)
+__device__ __forceinline__ int edge_slot_of(int e, const int a[3]) {
+    const int orient = e >> 2;
+    const int m[2] = {2 * (e & 1) - 1, 2 * ((e >> 1) & 1) - 1};
+    int idx = orient << 2, dim = 0;
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax)
+        if (ax != orient) { if (2 * a[ax] - m[dim] < 0) idx |= 1 << dim; dim++; }
+    return idx;
+}
+
 // ------------------------------------------------------------------------------------
 // octree vertex / edge / face records
 // ------------------------------------------------------------------------------------
@@ -70,34 +140,23 @@ __global__ void __launch_bounds__(kBlock) k_mesh_reset(const Counters* c, int* n
     }
 }
 
-// vertex ownership (initVertexOwner, mesh/BuildMeshGeometry.cu:42-101)
-__global__ void __launch_bounds__(kBlock) k_vertex_owner(const Counters* c, const int* key, const int* ndepth,
-                                                         const float* cx, const float* cy, const float* cz,
-                                                         const int* neigh, size_t stride, unsigned char* vmask) {
+// vertex ownership (initVertexOwner, mesh/BuildMeshGeometry.cu:42-101): a node owns a
+// corner when no other cell around it has a smaller key
+__global__ void __launch_bounds__(kBlock) k_vertex_owner(const Counters* c, const int* key, const int* neigh,
+                                                         size_t stride, unsigned char* vmask) {
     const int M = c->n_nodes;
     PSR_GRID_STRIDE(i, M) {
-        const int d = ndepth[i];
-        const float hw = 1.0f / (float)(1 << (d + 1)), w = 1.0f / (float)(1 << d), w2 = __fmul_rn(w, w);
-        const float ox = cx[i], oy = cy[i], oz = cz[i];
-        int okey[8], oidx[8];
+        const int myk = key[i];
+        unsigned smaller = 0;
 #pragma unroll
-        for (int q = 0; q < 8; ++q) { okey[q] = 0x7fffffff; oidx[q] = -1; }
         for (int k = 0; k < 27; ++k) {
+            if (k == 13) continue;
             const int nb = neigh[(size_t)k * stride + i];
-            if (nb == -1) continue;
-            const float nx = cx[nb], ny = cy[nb], nz = cz[nb];
-            const int nk = key[nb];
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                float vx = __fadd_rn(ox, (float)(2 * (q & 1) - 1) * hw);
-                float vy = __fadd_rn(oy, (float)(2 * ((q >> 1) & 1) - 1) * hw);
-                float vz = __fadd_rn(oz, (float)(2 * ((q >> 2) & 1) - 1) * hw);
-                if (sqdist3(vx, vy, vz, nx, ny, nz) < w2 && okey[q] > nk) { okey[q] = nk; oidx[q] = nb; }
-            }
+            if (nb != -1 && key[nb] < myk) smaller |= 1u << k;
         }
         unsigned m = 0;
 #pragma unroll
-        for (int q = 0; q < 8; ++q) if (oidx[q] == i) m |= 1u << q;
+        for (int q = 0; q < 8; ++q) if (!(smaller & vertex_cells(q))) m |= 1u << q;
         vmask[i] = (unsigned char)m;
     }
 }
@@ -144,53 +203,41 @@ __global__ void k_set_count(int* dst, const unsigned* total, int cap, unsigned* 
 }
 
 // maintainVertexNodePointer (mesh/BuildMeshGeometry.cu:108-147)
-__global__ void __launch_bounds__(kBlock) k_vertex_maintain(const Counters* c, const int* ndepth, const float* cx,
-                                                            const float* cy, const float* cz, const int* neigh,
-                                                            size_t stride, const float* vx, const float* vy,
-                                                            const float* vz, const int* vowner, int* node_vtx) {
+__global__ void __launch_bounds__(kBlock) k_vertex_maintain(const Counters* c, const int* neigh, size_t stride,
+                                                            const int* vowner, const int* vkind, int* node_vtx) {
     const int V = c->n_vertices;
     PSR_GRID_STRIDE(v, V) {
         const int ow = vowner[v];
-        const int d = ndepth[ow];
-        const float w = 1.0f / (float)(1 << d), w2 = __fmul_rn(w, w);
-        const float px = vx[v], py = vy[v], pz = vz[v];
-        for (int k = 0; k < 27; ++k) {
-            const int nb = neigh[(size_t)k * stride + ow];
-            if (nb == -1) continue;
-            const float nx = cx[nb], ny = cy[nb], nz = cz[nb];
-            if (sqdist3(px, py, pz, nx, ny, nz) < w2)
-                node_vtx[(size_t)vertex_slot(nx, ny, nz, px, py, pz) * stride + nb] = v + 1;
+        int mx, my, mz;
+        corner_sides(vkind[v], mx, my, mz);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int ax = (j & 1) ? mx : 0, ay = (j & 2) ? my : 0, az = (j & 4) ? mz : 0;
+            const int nb = neigh[(size_t)nslot(ax, ay, az) * stride + ow];
+            if (nb != -1) node_vtx[(size_t)vertex_slot_of(ax, ay, az, mx, my, mz) * stride + nb] = v + 1;
         }
     }
 }
 
 // edge ownership for D-level nodes (initEdgeArray, mesh/BuildMeshGeometry.cu:149-220)
-__global__ void __launch_bounds__(kBlock) k_edge_owner(const Counters* c, int depth, const int* key, const float* cx,
-                                                       const float* cy, const float* cz, const int* neigh,
+__global__ void __launch_bounds__(kBlock) k_edge_owner(const Counters* c, int depth, const int* key, const int* neigh,
                                                        size_t stride, unsigned short* emask) {
     const int md = c->level_count[depth];
     const int b = c->level_base[depth];
-    const float hw = 1.0f / (float)(1 << (depth + 1)), w = 1.0f / (float)(1 << depth), w2 = __fmul_rn(w, w);
     PSR_GRID_STRIDE(o, md) {
         const int i = b + o;
-        float ec[12][3];
+        const int myk = key[i];
+        unsigned smaller = 0;
 #pragma unroll
-        for (int e = 0; e < 12; ++e) edge_center(cx[i], cy[i], cz[i], e, hw, ec[e]);
-        int okey[12], oidx[12];
-#pragma unroll
-        for (int e = 0; e < 12; ++e) { okey[e] = 0x7fffffff; oidx[e] = -1; }
         for (int k = 0; k < 27; ++k) {
+            if (k == 13 || k == 0 || k == 2 || k == 6 || k == 8 || k == 18 || k == 20 || k == 24 || k == 26)
+                continue;   // corner-diagonal cells touch no edge
             const int nb = neigh[(size_t)k * stride + i];
-            if (nb == -1) continue;
-            const float nx = cx[nb], ny = cy[nb], nz = cz[nb];
-            const int nk = key[nb];
-#pragma unroll
-            for (int e = 0; e < 12; ++e)
-                if (sqdist3(ec[e][0], ec[e][1], ec[e][2], nx, ny, nz) < w2 && okey[e] > nk) { okey[e] = nk; oidx[e] = nb; }
+            if (nb != -1 && key[nb] < myk) smaller |= 1u << k;
         }
         unsigned m = 0;
 #pragma unroll
-        for (int e = 0; e < 12; ++e) if (oidx[e] == i) m |= 1u << e;
+        for (int e = 0; e < 12; ++e) if (!(smaller & edge_cells(e))) m |= 1u << e;
         emask[o] = (unsigned short)m;
     }
 }
@@ -218,59 +265,35 @@ struct EdgeStore {
 };
 
 // maintainEdgeNodePointer (mesh/BuildMeshGeometry.cu:222-280)
-__global__ void __launch_bounds__(kBlock) k_edge_maintain(const Counters* c, int depth, const float* cx, const float* cy,
-                                                          const float* cz, const int* neigh, size_t stride,
+__global__ void __launch_bounds__(kBlock) k_edge_maintain(const Counters* c, const int* neigh, size_t stride,
                                                           const int* eowner, const int* ekind, int* node_edge) {
     const int E = c->n_edges;
-    const float hw = 1.0f / (float)(1 << (depth + 1)), w = 1.0f / (float)(1 << depth), w2 = __fmul_rn(w, w);
     PSR_GRID_STRIDE(ei, E) {
         const int ow = eowner[ei], kind = ekind[ei];
-        float ec[3];
-        edge_center(cx[ow], cy[ow], cz[ow], kind, hw, ec);
-        const int orient = kind >> 2;
-        for (int k = 0; k < 27; ++k) {
-            const int nb = neigh[(size_t)k * stride + ow];
-            if (nb == -1) continue;
-            const float nc[3] = {cx[nb], cy[nb], cz[nb]};
-            if (sqdist3(ec[0], ec[1], ec[2], nc[0], nc[1], nc[2]) < w2) {
-                int idx = orient << 2, dim = 0;
-                for (int a = 0; a < 3; ++a)
-                    if (orient != a) { if (__fsub_rn(nc[a], ec[a]) < 0) idx |= (1 << dim); dim++; }
-                node_edge[(size_t)idx * stride + nb] = ei + 1;
-            }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            int a[3];
+            edge_offset(kind, j, a);
+            const int nb = neigh[(size_t)nslot(a[0], a[1], a[2]) * stride + ow];
+            if (nb != -1) node_edge[(size_t)edge_slot_of(kind, a) * stride + nb] = ei + 1;
         }
     }
 }
 
 // face ownership (initFaceArray, mesh/BuildMeshGeometry.cu:282-354)
-__global__ void __launch_bounds__(kBlock) k_face_owner(const Counters* c, const int* key, const int* ndepth,
-                                                       const float* cx, const float* cy, const float* cz,
-                                                       const int* neigh, size_t stride, unsigned char* fmask) {
+__global__ void __launch_bounds__(kBlock) k_face_owner(const Counters* c, const int* key, const int* neigh,
+                                                       size_t stride, unsigned char* fmask) {
     const int M = c->n_nodes;
     PSR_GRID_STRIDE(i, M) {
-        const int d = ndepth[i];
-        const float hw = 1.0f / (float)(1 << (d + 1)), w = 1.0f / (float)(1 << d), w2 = __fmul_rn(w, w);
-        float fc[6][3];
-#pragma unroll
-        for (int f = 0; f < 6; ++f) {
-            fc[f][0] = cx[i]; fc[f][1] = cy[i]; fc[f][2] = cz[i];
-            fc[f][f >> 1] = __fadd_rn(fc[f][f >> 1], (float)(2 * (f & 1) - 1) * hw);
-        }
-        int okey[6], oidx[6];
-#pragma unroll
-        for (int f = 0; f < 6; ++f) { okey[f] = 0x7fffffff; oidx[f] = -1; }
-        for (int k = 0; k < 27; ++k) {
-            const int nb = neigh[(size_t)k * stride + i];
-            if (nb == -1) continue;
-            const float nx = cx[nb], ny = cy[nb], nz = cz[nb];
-            const int nk = key[nb];
-#pragma unroll
-            for (int f = 0; f < 6; ++f)
-                if (sqdist3(fc[f][0], fc[f][1], fc[f][2], nx, ny, nz) < w2 && okey[f] > nk) { okey[f] = nk; oidx[f] = nb; }
-        }
+        const int myk = key[i];
         unsigned m = 0;
 #pragma unroll
-        for (int f = 0; f < 6; ++f) if (oidx[f] == i) m |= 1u << f;
+        for (int f = 0; f < 6; ++f) {
+            int a[3] = {0, 0, 0};
+            a[f >> 1] = 2 * (f & 1) - 1;
+            const int nb = neigh[(size_t)nslot(a[0], a[1], a[2]) * stride + i];
+            if (!(nb != -1 && key[nb] < myk)) m |= 1u << f;
+        }
         fmask[i] = (unsigned char)m;
     }
 }
@@ -302,27 +325,18 @@ struct FaceStore {
 };
 
 // maintainFaceNodePointer (mesh/BuildMeshGeometry.cu:356-400)
-__global__ void __launch_bounds__(kBlock) k_face_maintain(const Counters* c, const int* ndepth, const float* cx,
-                                                          const float* cy, const float* cz, const int* neigh,
-                                                          size_t stride, const int* fowner, const int* fkind,
-                                                          int* node_face) {
+__global__ void __launch_bounds__(kBlock) k_face_maintain(const Counters* c, const int* neigh, size_t stride,
+                                                          const int* fowner, const int* fkind, int* node_face) {
     const int F = c->n_faces;
     PSR_GRID_STRIDE(fi, F) {
         const int ow = fowner[fi], kind = fkind[fi];
-        const int d = ndepth[ow];
-        const float hw = 1.0f / (float)(1 << (d + 1)), w = 1.0f / (float)(1 << d), w2 = __fmul_rn(w, w);
-        float fc[3] = {cx[ow], cy[ow], cz[ow]};
-        const int orient = kind >> 1;
-        fc[orient] = __fadd_rn(fc[orient], (float)(2 * (kind & 1) - 1) * hw);
-        for (int k = 0; k < 27; ++k) {
-            const int nb = neigh[(size_t)k * stride + ow];
-            if (nb == -1) continue;
-            const float nc[3] = {cx[nb], cy[nb], cz[nb]};
-            if (sqdist3(fc[0], fc[1], fc[2], nc[0], nc[1], nc[2]) < w2) {
-                int idx = orient << 1;
-                if (__fsub_rn(nc[orient], fc[orient]) < 0) idx++;
-                node_face[(size_t)idx * stride + nb] = fi + 1;
-            }
+        const int orient = kind >> 1, m = 2 * (kind & 1) - 1;
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            int a[3] = {0, 0, 0};
+            a[orient] = j ? m : 0;
+            const int nb = neigh[(size_t)nslot(a[0], a[1], a[2]) * stride + ow];
+            if (nb != -1) node_face[(size_t)((orient << 1) + (2 * a[orient] - m < 0 ? 1 : 0)) * stride + nb] = fi + 1;
         }
     }
 }
@@ -774,33 +788,22 @@ __device__ __forceinline__ int sub_dnode_to_node(int o, const int* groups, int n
 // vertex ownership among subdivision nodes only (initSubdivideVertexOwner :698-763)
 __global__ void __launch_bounds__(kBlock) k_sub_vertex_owner(const Counters* c, int depth, const int* groups,
                                                              const int* s_key, const int* s_neigh, size_t sstride,
-                                                             const float* s_cx, const float* s_cy, const float* s_cz,
                                                              unsigned char* s_vmask, int na) {
     const int SD = c->n_sub_dnodes;
     const int ng = c->n_groups;
-    const float hw = 1.0f / (float)(1 << (depth + 1)), w = 1.0f / (float)(1 << depth), w2 = __fmul_rn(w, w);
     PSR_GRID_STRIDE(o, SD) {
         const int s = sub_dnode_to_node(o, groups, ng, depth);
-        const float ox = s_cx[s], oy = s_cy[s], oz = s_cz[s];
-        int okey[8], oidx[8];
+        const int myk = s_key[s];
+        unsigned smaller = 0;
 #pragma unroll
-        for (int q = 0; q < 8; ++q) { okey[q] = 0x7fffffff; oidx[q] = -1; }
         for (int k = 0; k < 27; ++k) {
+            if (k == 13) continue;
             const int nb = s_neigh[(size_t)k * sstride + s];
-            if (nb < na) continue;
-            const float nx = s_cx[nb - na], ny = s_cy[nb - na], nz = s_cz[nb - na];
-            const int nk = s_key[nb - na];
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                float vx = __fadd_rn(ox, (float)(2 * (q & 1) - 1) * hw);
-                float vy = __fadd_rn(oy, (float)(2 * ((q >> 1) & 1) - 1) * hw);
-                float vz = __fadd_rn(oz, (float)(2 * ((q >> 2) & 1) - 1) * hw);
-                if (sqdist3(vx, vy, vz, nx, ny, nz) < w2 && okey[q] > nk) { okey[q] = nk; oidx[q] = nb; }
-            }
+            if (nb >= na && s_key[nb - na] < myk) smaller |= 1u << k;
         }
         unsigned m = 0;
 #pragma unroll
-        for (int q = 0; q < 8; ++q) if (oidx[q] == na + s) m |= 1u << q;
+        for (int q = 0; q < 8; ++q) if (!(smaller & vertex_cells(q))) m |= 1u << q;
         s_vmask[o] = (unsigned char)m;
     }
 }
@@ -844,26 +847,23 @@ __device__ __forceinline__ int sub_node_to_dnode(int s, const int* groups, int n
 
 // maintainSubdivideVertexNodePointer (:765-810): s_vtx indexed by D-level sub node
 __global__ void __launch_bounds__(kBlock) k_sub_vertex_maintain(const Counters* c, int depth, const int* groups,
-                                                                const float* cx, const float* cy, const float* cz,
                                                                 const int* s_neigh, size_t sstride,
-                                                                const float* s_cx, const float* s_cy,
-                                                                const float* s_cz, const int* s_depth,
-                                                                const float* vx, const float* vy, const float* vz,
-                                                                const int* vowner, int* s_vtx, size_t dstride, int na) {
+                                                                const int* s_depth, const int* vowner,
+                                                                const int* vkind, int* s_vtx, size_t dstride,
+                                                                int na) {
     const int V = c->n_sub_vertices;
     const int ng = c->n_groups;
-    const float w = 1.0f / (float)(1 << depth), w2 = __fmul_rn(w, w);
     PSR_GRID_STRIDE(v, V) {
         const int ow = vowner[v] - na;
-        const float px = vx[v], py = vy[v], pz = vz[v];
-        for (int k = 0; k < 27; ++k) {
-            const int nb = s_neigh[(size_t)k * sstride + ow];
-            if (nb == -1) continue;
-            float nx, ny, nz;
-            sub_center(nb, na, cx, cy, cz, s_cx, s_cy, s_cz, nx, ny, nz);
-            if (sqdist3(px, py, pz, nx, ny, nz) < w2 && nb >= na && s_depth[nb - na] == depth) {
+        int mx, my, mz;
+        corner_sides(vkind[v], mx, my, mz);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int ax = (j & 1) ? mx : 0, ay = (j & 2) ? my : 0, az = (j & 4) ? mz : 0;
+            const int nb = s_neigh[(size_t)nslot(ax, ay, az) * sstride + ow];
+            if (nb >= na && s_depth[nb - na] == depth) {
                 const int dn = sub_node_to_dnode(nb - na, groups, ng, depth);
-                s_vtx[(size_t)vertex_slot(nx, ny, nz, px, py, pz) * dstride + dn] = v + 1;
+                s_vtx[(size_t)vertex_slot_of(ax, ay, az, mx, my, mz) * dstride + dn] = v + 1;
             }
         }
     }
@@ -872,31 +872,23 @@ __global__ void __launch_bounds__(kBlock) k_sub_vertex_maintain(const Counters* 
 // edge ownership among subdivision nodes only (initSubdivideEdgeArray :812-886)
 __global__ void __launch_bounds__(kBlock) k_sub_edge_owner(const Counters* c, int depth, const int* groups,
                                                            const int* s_key, const int* s_neigh, size_t sstride,
-                                                           const float* s_cx, const float* s_cy, const float* s_cz,
                                                            unsigned short* s_emask, int na) {
     const int SD = c->n_sub_dnodes;
     const int ng = c->n_groups;
-    const float hw = 1.0f / (float)(1 << (depth + 1)), w = 1.0f / (float)(1 << depth), w2 = __fmul_rn(w, w);
     PSR_GRID_STRIDE(o, SD) {
         const int s = sub_dnode_to_node(o, groups, ng, depth);
-        float ec[12][3];
+        const int myk = s_key[s];
+        unsigned smaller = 0;
 #pragma unroll
-        for (int e = 0; e < 12; ++e) edge_center(s_cx[s], s_cy[s], s_cz[s], e, hw, ec[e]);
-        int okey[12], oidx[12];
-#pragma unroll
-        for (int e = 0; e < 12; ++e) { okey[e] = 0x7fffffff; oidx[e] = -1; }
         for (int k = 0; k < 27; ++k) {
+            if (k == 13 || k == 0 || k == 2 || k == 6 || k == 8 || k == 18 || k == 20 || k == 24 || k == 26)
+                continue;   // corner-diagonal cells touch no edge
             const int nb = s_neigh[(size_t)k * sstride + s];
-            if (nb < na) continue;
-            const float nx = s_cx[nb - na], ny = s_cy[nb - na], nz = s_cz[nb - na];
-            const int nk = s_key[nb - na];
-#pragma unroll
-            for (int e = 0; e < 12; ++e)
-                if (sqdist3(ec[e][0], ec[e][1], ec[e][2], nx, ny, nz) < w2 && okey[e] > nk) { okey[e] = nk; oidx[e] = nb; }
+            if (nb >= na && s_key[nb - na] < myk) smaller |= 1u << k;
         }
         unsigned m = 0;
 #pragma unroll
-        for (int e = 0; e < 12; ++e) if (oidx[e] == na + s) m |= 1u << e;
+        for (int e = 0; e < 12; ++e) if (!(smaller & edge_cells(e))) m |= 1u << e;
         s_emask[o] = (unsigned short)m;
     }
 }
@@ -923,30 +915,21 @@ struct SubEdgeStore {
 
 // maintainSubdivideEdgeNodePointer (:888-949)
 __global__ void __launch_bounds__(kBlock) k_sub_edge_maintain(const Counters* c, int depth, const int* groups,
-                                                              const float* cx, const float* cy, const float* cz,
-                                                              const int* s_neigh, size_t sstride, const float* s_cx,
-                                                              const float* s_cy, const float* s_cz,
-                                                              const int* s_depth, const int* eowner,
-                                                              const int* ekind, int* s_edge, size_t dstride, int na) {
+                                                              const int* s_neigh, size_t sstride, const int* s_depth,
+                                                              const int* eowner, const int* ekind, int* s_edge,
+                                                              size_t dstride, int na) {
     const int E = c->n_sub_edges;
     const int ng = c->n_groups;
-    const float hw = 1.0f / (float)(1 << (depth + 1)), w = 1.0f / (float)(1 << depth), w2 = __fmul_rn(w, w);
     PSR_GRID_STRIDE(ei, E) {
         const int ow = eowner[ei] - na, kind = ekind[ei];
-        float ec[3];
-        edge_center(s_cx[ow], s_cy[ow], s_cz[ow], kind, hw, ec);
-        const int orient = kind >> 2;
-        for (int k = 0; k < 27; ++k) {
-            const int nb = s_neigh[(size_t)k * sstride + ow];
-            if (nb == -1) continue;
-            float nc[3];
-            sub_center(nb, na, cx, cy, cz, s_cx, s_cy, s_cz, nc[0], nc[1], nc[2]);
-            if (sqdist3(ec[0], ec[1], ec[2], nc[0], nc[1], nc[2]) < w2 && nb >= na && s_depth[nb - na] == depth) {
-                int idx = orient << 2, dim = 0;
-                for (int a = 0; a < 3; ++a)
-                    if (orient != a) { if (__fsub_rn(nc[a], ec[a]) < 0) idx |= (1 << dim); dim++; }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            int a[3];
+            edge_offset(kind, j, a);
+            const int nb = s_neigh[(size_t)nslot(a[0], a[1], a[2]) * sstride + ow];
+            if (nb >= na && s_depth[nb - na] == depth) {
                 const int dn = sub_node_to_dnode(nb - na, groups, ng, depth);
-                s_edge[(size_t)idx * dstride + dn] = ei + 1;
+                s_edge[(size_t)edge_slot_of(kind, a) * dstride + dn] = ei + 1;
             }
         }
     }
@@ -1209,34 +1192,31 @@ cudaError_t mesh_build_impl(Workspace& ws, const MeshBufs& mb) {
     cudaError_t e;
     k_mesh_reset<<<gm, kBlock, 0, s>>>(c, ws.node_vtx, ws.node_edge, ws.node_face, mb.ov_group, mb.ov_sub, stride);
     // vertices
-    k_vertex_owner<<<gm, kBlock, 0, s>>>(c, ws.key, ws.ndepth, ws.ctr_x, ws.ctr_y, ws.ctr_z, ws.neigh, stride, ws.vmask);
+    k_vertex_owner<<<gm, kBlock, 0, s>>>(c, ws.key, ws.neigh, stride, ws.vmask);
     e = launch_scan(PopcLoad8{ws.vmask},
                     VertexStore{ws.vmask, ws.ndepth, ws.ctr_x, ws.ctr_y, ws.ctr_z, ws.v_x, ws.v_y, ws.v_z, ws.v_owner,
                                 ws.v_kind, ws.v_depth, ws.cap.vertices, err},
                     &c->n_nodes, 0, ws.scan, total, err, s);
     if (e != cudaSuccess) return e;
     k_set_count<<<1, 1, 0, s>>>(&c->n_vertices, total, ws.cap.vertices, err);
-    k_vertex_maintain<<<gm, kBlock, 0, s>>>(c, ws.ndepth, ws.ctr_x, ws.ctr_y, ws.ctr_z, ws.neigh, stride, ws.v_x, ws.v_y,
-                                            ws.v_z, ws.v_owner, ws.node_vtx);
+    k_vertex_maintain<<<gm, kBlock, 0, s>>>(c, ws.neigh, stride, ws.v_owner, ws.v_kind, ws.node_vtx);
     // edges (D level)
-    k_edge_owner<<<gm, kBlock, 0, s>>>(c, D, ws.key, ws.ctr_x, ws.ctr_y, ws.ctr_z, ws.neigh, stride, ws.emask16);
+    k_edge_owner<<<gm, kBlock, 0, s>>>(c, D, ws.key, ws.neigh, stride, ws.emask16);
     e = launch_scan(PopcLoad16{ws.emask16},
                     EdgeStore{ws.emask16, &c->level_base[D], ws.e_owner, ws.e_kind, ws.cap.edges, err},
                     &c->level_count[D], 0, ws.scan, total, err, s);
     if (e != cudaSuccess) return e;
     k_set_count<<<1, 1, 0, s>>>(&c->n_edges, total, ws.cap.edges, err);
-    k_edge_maintain<<<gm, kBlock, 0, s>>>(c, D, ws.ctr_x, ws.ctr_y, ws.ctr_z, ws.neigh, stride, ws.e_owner, ws.e_kind,
-                                          ws.node_edge);
+    k_edge_maintain<<<gm, kBlock, 0, s>>>(c, ws.neigh, stride, ws.e_owner, ws.e_kind, ws.node_edge);
     // faces
-    k_face_owner<<<gm, kBlock, 0, s>>>(c, ws.key, ws.ndepth, ws.ctr_x, ws.ctr_y, ws.ctr_z, ws.neigh, stride, ws.fmask);
+    k_face_owner<<<gm, kBlock, 0, s>>>(c, ws.key, ws.neigh, stride, ws.fmask);
     e = launch_scan(PopcLoad8{ws.fmask},
                     FaceStore{ws.fmask, ws.key, ws.ndepth, ws.parent, D, ws.f_owner, ws.f_kind, ws.f_hasparent,
                               ws.cap.faces, err},
                     &c->n_nodes, 0, ws.scan, total, err, s);
     if (e != cudaSuccess) return e;
     k_set_count<<<1, 1, 0, s>>>(&c->n_faces, total, ws.cap.faces, err);
-    k_face_maintain<<<gm, kBlock, 0, s>>>(c, ws.ndepth, ws.ctr_x, ws.ctr_y, ws.ctr_z, ws.neigh, stride, ws.f_owner,
-                                          ws.f_kind, ws.node_face);
+    k_face_maintain<<<gm, kBlock, 0, s>>>(c, ws.neigh, stride, ws.f_owner, ws.f_kind, ws.node_face);
     // implicit values
     k_vertex_values<<<gm, kBlock, 0, s>>>(c, D, ws.v_x, ws.v_y, ws.v_z, ws.v_owner, ws.v_kind, ws.v_depth, ws.neigh,
                                           stride, ws.parent, ws.first_child, ws.enc, ws.xsol, ws.vvalue);
@@ -1302,19 +1282,16 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
                                                ws.s_group, ws.s_root, ws.s_neigh, ws.s_contrib, sstride, na);
     cudaMemsetAsync(ws.s_vtx, 0, sizeof(int) * 8 * dstride, s);
     cudaMemsetAsync(ws.s_edge, 0, sizeof(int) * 12 * dstride, s);
-    k_sub_vertex_owner<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.s_key, ws.s_neigh, sstride, ws.s_cx, ws.s_cy, ws.s_cz,
-                                             ws.s_vmask, na);
+    k_sub_vertex_owner<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.s_key, ws.s_neigh, sstride, ws.s_vmask, na);
     e = launch_scan(PopcLoad8{ws.s_vmask},
                     SubVertexStore{ws.s_vmask, mb.groups, &c->n_groups, D, ws.s_cx, ws.s_cy, ws.s_cz, ws.sv_x, ws.sv_y,
                                    ws.sv_z, ws.sv_owner, ws.sv_kind, 8 * ws.cap.sub_dnodes, na, err},
                     &c->n_sub_dnodes, 0, ws.scan, total, err, s);
     if (e != cudaSuccess) return e;
     k_set_count<<<1, 1, 0, s>>>(&c->n_sub_vertices, total, 8 * ws.cap.sub_dnodes, err);
-    k_sub_vertex_maintain<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.ctr_x, ws.ctr_y, ws.ctr_z, ws.s_neigh, sstride,
-                                                ws.s_cx, ws.s_cy, ws.s_cz, ws.s_depth, ws.sv_x, ws.sv_y, ws.sv_z,
-                                                ws.sv_owner, ws.s_vtx, dstride, na);
-    k_sub_edge_owner<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.s_key, ws.s_neigh, sstride, ws.s_cx, ws.s_cy, ws.s_cz,
-                                           ws.s_emask, na);
+    k_sub_vertex_maintain<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.s_neigh, sstride, ws.s_depth, ws.sv_owner,
+                                                ws.sv_kind, ws.s_vtx, dstride, na);
+    k_sub_edge_owner<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.s_key, ws.s_neigh, sstride, ws.s_emask, na);
     e = launch_scan(PopcLoad16{ws.s_emask},
                     SubEdgeStore{ws.s_emask, mb.groups, &c->n_groups, D, ws.se_owner, ws.se_kind,
                                  12 * ws.cap.sub_dnodes, na, err},
@@ -1325,9 +1302,8 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
     e = launch_scan(PopcLoad16{ws.s_emask}, StoreExclusive{mb.edge_of_dnode}, &c->n_sub_dnodes, 0, ws.scan, total,
                     err, s);
     if (e != cudaSuccess) return e;
-    k_sub_edge_maintain<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.ctr_x, ws.ctr_y, ws.ctr_z, ws.s_neigh, sstride,
-                                              ws.s_cx, ws.s_cy, ws.s_cz, ws.s_depth, ws.se_owner, ws.se_kind, ws.s_edge,
-                                              dstride, na);
+    k_sub_edge_maintain<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.s_neigh, sstride, ws.s_depth, ws.se_owner,
+                                              ws.se_kind, ws.s_edge, dstride, na);
     k_sub_vertex_values<<<gs, kBlock, 0, s>>>(c, D, ws.sv_x, ws.sv_y, ws.sv_z, ws.sv_owner, ws.neigh, stride, ws.parent,
                                               ws.s_neigh, sstride, ws.s_parent, ws.s_root, ws.s_contrib, ws.enc,
                                               ws.xsol, ws.sv_value, na);
