@@ -346,17 +346,7 @@ __global__ void __launch_bounds__(kBlock) k_face_maintain(const Counters* c, con
 // ------------------------------------------------------------------------------------
 __device__ __forceinline__ float node_terms(int node, float val, float qx, float qy, float qz, int depth,
                                             const int* neigh, size_t stride, const int* enc, const float* x) {
-    for (int k = 0; k < 27; ++k) {
-        int nb = neigh[(size_t)k * stride + node];
-        if (nb == -1) continue;
-        int ix, iy, iz;
-        decode3m(enc[nb], depth, ix, iy, iz);
-        float t = __fmul_rn(x[nb], basis32(ix, qx));
-        t = __fmul_rn(t, basis32(iy, qy));
-        t = __fmul_rn(t, basis32(iz, qz));
-        val = __fadd_rn(val, t);
-    }
-    return val;
+    return level_terms(node, val, qx, qy, qz, depth, neigh, stride, enc, x);
 }
 
 __global__ void __launch_bounds__(kBlock) k_vertex_values(const Counters* c, int depth, const float* vx,
@@ -745,12 +735,13 @@ __global__ void __launch_bounds__(kBlock) k_sub_neighbours(const Counters* c, in
         const int* G = groups + (size_t)g * kGroupRec;
         const int son = (s_key[s] >> (3 * (depth - d))) & 7;
         const int pa = s_parent[s];
+#pragma unroll
         for (int k = 0; k < 27; ++k) {
-            const int lp = c_tab.lut_parent[son][k];
+            int lp, lc;
+            nb_lut(son, k, lp, lc);
             const int np = (pa < na) ? neigh[(size_t)lp * stride + pa] : s_neigh[(size_t)lp * sstride + (pa - na)];
             int v = -1;
             if (np != -1) {
-                const int lc = c_tab.lut_child[son][k];
                 if (np < na) {
                     if (ov_group[(size_t)lc * stride + np] == g) {
                         // redirected child pointer of this group's root
@@ -954,6 +945,11 @@ __global__ void __launch_bounds__(kBlock) k_sub_vertex_values(const Counters* c,
             while (now != -1) {
                 // all 27 neighbours zero-valued subdivision nodes: every term is skipped
                 if (now >= na && !s_contrib[now - na]) { now = s_parent[now - na]; continue; }
+                if (now < na) {   // octree levels: same-depth neighbours, cached basis values
+                    val = level_terms(now, val, qx, qy, qz, depth, neigh, stride, enc, x);
+                    now = parent[now];
+                    continue;
+                }
                 for (int k = 0; k < 27; ++k) {
                     int nb = (now < na) ? neigh[(size_t)k * stride + now] : s_neigh[(size_t)k * sstride + (now - na)];
                     if (nb == -1) continue;

@@ -387,13 +387,15 @@ __global__ void __launch_bounds__(kBlock) k_neighbours(const Counters* c, int d,
         const int i = b + li;
         const int son = (key[i] >> (3 * (depth - d))) & 7;
         const int pa = parent[i];
-#pragma unroll 3
+#pragma unroll
         for (int k = 0; k < 27; ++k) {
-            int np = neigh[(size_t)c_tab.lut_parent[son][k] * stride + pa];
+            int lp, lc;
+            nb_lut(son, k, lp, lc);
+            int np = neigh[(size_t)lp * stride + pa];
             int v = -1;
             if (np != -1) {
                 int fc = first_child[np];
-                v = (fc == -1) ? -1 : fc + c_tab.lut_child[son][k];
+                v = (fc == -1) ? -1 : fc + lc;
             }
             neigh[(size_t)k * stride + i] = v;
         }

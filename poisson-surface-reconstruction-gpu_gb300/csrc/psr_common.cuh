@@ -83,12 +83,60 @@ __device__ __forceinline__ float basis32(int idx, float x) {
     int d = ilog2_dev(idx + 1);
     int off = idx + 1 - (1 << d);
     float s = (float)(1 << d);
-    float c = __fdiv_rn(__fadd_rn((float)off, 0.5f), s);
+    // (off + 1/2) / 2^d: the quotient by a power of two is exact, so it is the product with 2^-d
+    float c = __fmul_rn(__fadd_rn((float)off, 0.5f), __int_as_float((127 - d) << 23));
     float t = __fmul_rn(__fsub_rn(x, c), s);
     float a = fabsf(t);
     if (a < 0.5f) return __fmul_rn(__fsub_rn(0.75f, __fmul_rn(t, t)), kF43);
     if (a < 1.5f) { float u = __fsub_rn(1.5f, a); return __fmul_rn(__fmul_rn(u, u), kF23); }
     return 0.0f;
+}
+
+// Function index of a node at tree depth `depth` packed as (D+1)-bit fields x | y | z.
+__device__ __forceinline__ void decode_fn_index(int e, int depth, int& ix, int& iy, int& iz) {
+    const int o1 = 1 << (depth + 1);
+    ix = e & (o1 - 1);
+    iy = (e >> (depth + 1)) & (o1 - 1);
+    iz = e >> (2 * (depth + 1));
+}
+
+// Neighbour slot k (9 ox + 3 oy + oz) of child `son` (x = 4, y = 2, z = 1) seen from its
+// parent: the parent's neighbour slot holding that cell's parent (lp) and the cell's child
+// slot there (lc) -- the table of mesh/BuildOctree.cu:20-42 evaluated arithmetically.
+__device__ __forceinline__ void nb_lut(int son, int k, int& lp, int& lc) {
+    const int qx = ((son >> 2) & 1) + k / 9 - 1;
+    const int qy = ((son >> 1) & 1) + (k / 3) % 3 - 1;
+    const int qz = (son & 1) + k % 3 - 1;
+    lp = 9 * ((qx >= 0) + (qx > 1)) + 3 * ((qy >= 0) + (qy > 1)) + ((qz >= 0) + (qz > 1));
+    lc = 4 * ((qx + 2) & 1) + 2 * ((qy + 2) & 1) + ((qz + 2) & 1);
+}
+
+// Terms of one level of an implicit-function chain: the 27 same-depth neighbours nb of
+// `node`, each adding ((x[nb] * Fx) * Fy) * Fz in slot order.  A neighbour's function
+// index is the node's own plus the slot offset, so the 81 basis values come from 9.
+__device__ __forceinline__ float level_terms(int node, float val, float qx, float qy, float qz, int depth,
+                                             const int* neigh, size_t stride, const int* enc, const float* x) {
+    int ox, oy, oz;
+    decode_fn_index(enc[node], depth, ox, oy, oz);
+    float bx[3], by[3], bz[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        bx[j] = basis32(ox - 1 + j, qx);
+        by[j] = basis32(oy - 1 + j, qy);
+        bz[j] = basis32(oz - 1 + j, qz);
+    }
+    int nbs[27];
+#pragma unroll
+    for (int k = 0; k < 27; ++k) nbs[k] = neigh[(size_t)k * stride + node];
+#pragma unroll
+    for (int k = 0; k < 27; ++k) {
+        if (nbs[k] == -1) continue;
+        float t = __fmul_rn(x[nbs[k]], bx[k / 9]);
+        t = __fmul_rn(t, by[(k / 3) % 3]);
+        t = __fmul_rn(t, bz[k % 3]);
+        val = __fadd_rn(val, t);
+    }
+    return val;
 }
 
 // ---- float-float ("double-float") accumulation ---------------------------------------

@@ -364,16 +364,7 @@ __device__ __forceinline__ float chain_value(int node, float qx, float qy, float
                                              size_t stride, const int* parent, const int* enc, const float* x) {
     float val = 0.0f;
     while (node != -1) {
-        for (int k = 0; k < 27; ++k) {
-            int nb = neigh[(size_t)k * stride + node];
-            if (nb == -1) continue;
-            int ix, iy, iz;
-            decode3s(enc[nb], depth, ix, iy, iz);
-            float t = __fmul_rn(x[nb], basis32(ix, qx));
-            t = __fmul_rn(t, basis32(iy, qy));
-            t = __fmul_rn(t, basis32(iz, qz));
-            val = __fadd_rn(val, t);
-        }
+        val = level_terms(node, val, qx, qy, qz, depth, neigh, stride, enc, x);
         node = parent[node];
     }
     return val;

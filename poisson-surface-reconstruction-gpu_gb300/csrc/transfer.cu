@@ -66,25 +66,31 @@ __device__ __forceinline__ void knn_insert(float (&bd)[4], int (&bi)[4], float d
     } else { bd[3] = d; bi[3] = i; }
 }
 
-// the 4 smallest of two sorted 4-lists (lists hold disjoint sample sets)
+// the 4 smallest of two sorted 4-lists (lists hold disjoint sample sets): the pairwise
+// minima of a[k] and b[3-k] are the 4 smallest and form a bitonic sequence, which two
+// half-cleaner stages sort (Batcher's bitonic merge)
+__device__ __forceinline__ void knn_cswap(float& da, int& ia, float& db, int& ib) {
+    if (knn_less(db, ib, da, ia)) {
+        const float td = da; da = db; db = td;
+        const int ti = ia; ia = ib; ib = ti;
+    }
+}
 __device__ __forceinline__ void knn_merge(float (&ad)[4], int (&ai)[4], const float (&bd)[4], const int (&bi)[4]) {
-    float od[4];
-    int oi[4];
-    int p = 0, q = 0;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        const bool takeA = (q >= 4) || (p < 4 && knn_less(ad[p], ai[p], bd[q], bi[q]));
-        od[k] = takeA ? ad[p] : bd[q];
-        oi[k] = takeA ? ai[p] : bi[q];
-        p += takeA ? 1 : 0;
-        q += takeA ? 0 : 1;
+        if (knn_less(bd[3 - k], bi[3 - k], ad[k], ai[k])) { ad[k] = bd[3 - k]; ai[k] = bi[3 - k]; }
     }
-#pragma unroll
-    for (int k = 0; k < 4; ++k) { ad[k] = od[k]; ai[k] = oi[k]; }
+    knn_cswap(ad[0], ai[0], ad[2], ai[2]);
+    knn_cswap(ad[1], ai[1], ad[3], ai[3]);
+    knn_cswap(ad[0], ai[0], ad[1], ai[1]);
+    knn_cswap(ad[2], ai[2], ad[3], ai[3]);
 }
 
-// one warp per mesh vertex: the lanes split the samples of every grid shell, keep private
-// sorted 4-lists and merge them with butterfly shuffles after each shell
+// one warp per mesh vertex: the grid is searched in cubic shells around the vertex's
+// cell (first the 3x3x3 block, then shell r = 2, 3, ...); the lanes take the shell's cells
+// one each, scan their samples into private sorted 4-lists, and the lists are merged with
+// butterfly shuffles after each shell.  The search stops once the 4th distance is below
+// the distance to anything outside the searched block.
 __global__ void __launch_bounds__(kBlock) k_colour(const Counters* c, int g, const float* mv, const float* px,
                                                    const float* py, const float* pz, const float* cr, const float* cg,
                                                    const float* cb, const int* cell_start, float* out) {
@@ -102,16 +108,19 @@ __global__ void __launch_bounds__(kBlock) k_colour(const Counters* c, int g, con
         const int cx = min(max((int)floorf(qx * G), 0), G - 1);
         const int cy = min(max((int)floorf(qy * G), 0), G - 1);
         const int cz = min(max((int)floorf(qz * G), 0), G - 1);
-        for (int r = 0; r <= G; ++r) {
+        for (int r = 1; r <= G; ++r) {
             const int side = 2 * r + 1;
             const int ncell = side * side * side;
-            for (int t = 0; t < ncell; ++t) {
-                const int a = cx - r + t / (side * side), b = cy - r + (t / side) % side, z = cz - r + t % side;
+            for (int t = lane; t < ncell; t += 32) {
+                const int ta = t / (side * side), tr = t - ta * side * side;
+                const int tb = tr / side, tz = tr - tb * side;
+                const int a = cx - r + ta, b = cy - r + tb, z = cz - r + tz;
                 if (a < 0 || a >= G || b < 0 || b >= G || z < 0 || z >= G) continue;
-                if (max(abs(a - cx), max(abs(b - cy), abs(z - cz))) != r) continue;
+                // shell cells only (the first round takes the whole 3x3x3 block)
+                if (r > 1 && max(abs(a - cx), max(abs(b - cy), abs(z - cz))) != r) continue;
                 const unsigned m = morton3(a, b, z, g);
                 const int s0 = cell_start[m], s1 = cell_start[m + 1];
-                for (int i = s0 + lane; i < s1; i += 32) {
+                for (int i = s0; i < s1; ++i) {
                     const float dx = __fsub_rn(qx, px[i]), dy = __fsub_rn(qy, py[i]), dz = __fsub_rn(qz, pz[i]);
                     const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
                     knn_insert(bd, bi, d2, i);
