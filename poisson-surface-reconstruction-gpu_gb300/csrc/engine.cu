@@ -162,14 +162,14 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     long long max_scan = std::max({N + 1, nodes, (long long)cap.edges, (long long)cap.faces, (long long)cap.vertices,
                                    subd * 12, (long long)ws.part_cap_v, (long long)ws.part_cap_t,
                                    256LL * ((N + kSortTile - 1) / kSortTile)});
-    cap.scan_tiles = (int)((max_scan + kScanTile - 1) / kScanTile) + 1;
+    cap.scan_tiles = (int)((max_scan + kScanMinTile - 1) / kScanMinTile) + 1;
     const int sort_tiles = (int)((N + kSortTile - 1) / kSortTile) + 1;
     const int D = cfg.max_depth;
     ws.res = (1 << (D + 1)) - 1;
 
     Arena A;
     A.add(ws.cnt, 1);
-    A.add(ws.scan.words, (size_t)cap.scan_tiles + 1);
+    A.add(ws.scan.words, (size_t)cap.scan_tiles + kScanHeader);
     A.add(ws.sort.hist, (size_t)kRadix * sort_tiles + 16);
     A.add(ws.sort.keys_alt, (size_t)N);
     A.add(ws.sort.vals_alt, (size_t)N);
@@ -243,7 +243,7 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     A.add(ws.mesh_n, 3 * (size_t)cap.mesh_vertices);
     A.add(ws.nacc, 3 * (size_t)cap.mesh_vertices);
     A.add(ws.vcount, (size_t)cap.mesh_vertices);
-    A.add(ws.cell_start, (size_t)(1 << 18) + 16);
+    A.add(ws.cell_start, ((size_t)1 << (3 * kColourGridLevel)) + 16);
     A.add(ws.part_v, 3 * (size_t)ws.part_cap_v);
     A.add(ws.part_t, 3 * (size_t)ws.part_cap_t);
     ws.mb.max_groups = (int)nodes;
@@ -263,6 +263,8 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     h->arena_bytes = A.bytes;
     A.assign((char*)h->arena);
     ws.scan.max_tiles = cap.scan_tiles;
+    // scan counters and epoch start at zero; the scans keep them consistent afterwards
+    e = cudaMemset(ws.scan.words, 0, sizeof(unsigned long long) * ((size_t)cap.scan_tiles + kScanHeader));
     ws.sort.max_tiles = sort_tiles;
     ws.sort.scan = ws.scan;   // sort shares the scan scratch (scans are sequential on one stream)
     e = cudaMallocHost(&ws.cnt_host, sizeof(Counters));

@@ -727,12 +727,33 @@ __global__ void __launch_bounds__(kBlock) k_sub_neighbours(const Counters* c, in
                                                            const int* s_depth, const int* s_group, const int* s_root,
                                                            int* s_neigh, unsigned char* s_contrib, size_t sstride,
                                                            int na) {
-    const int S = c->n_sub_nodes;
-    PSR_GRID_STRIDE(s, S) {
-        if (s_depth[s] != d) continue;
-        int contrib = 0;
-        const int g = s_group[s];
+    // Depth-d nodes only.  Groups are ordered by root depth, so those reaching depth d are
+    // a prefix 0..gd-1, and the depth-d nodes of groups before g number
+    // dnode_prefix(g) / 8^(D-d) (every such group has full subtrees below its roots).
+    const int ng = c->n_groups;
+    int gd = 0;
+    {
+        int lo = 0, hi = ng;   // first group whose root depth exceeds d
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (groups[(size_t)mid * kGroupRec + 0] <= d) lo = mid + 1;
+            else hi = mid;
+        }
+        gd = lo;
+    }
+    const int sh = 3 * (depth - d);
+    const int nd = ((gd < ng) ? groups[(size_t)gd * kGroupRec + 5] : c->n_sub_dnodes) >> sh;
+    PSR_GRID_STRIDE(t, nd) {
+        int lo = 0, hi = gd - 1;   // last group g < gd with offset(g) <= t
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if ((groups[(size_t)mid * kGroupRec + 5] >> sh) <= t) lo = mid;
+            else hi = mid - 1;
+        }
+        const int g = lo;
         const int* G = groups + (size_t)g * kGroupRec;
+        const int s = G[3] + sub_level_off(G[0], G[2], d) + (t - (G[5] >> sh));
+        int contrib = 0;
         const int son = (s_key[s] >> (3 * (depth - d))) & 7;
         const int pa = s_parent[s];
 #pragma unroll
@@ -927,14 +948,19 @@ __global__ void __launch_bounds__(kBlock) k_sub_edge_maintain(const Counters* c,
 }
 
 // implicit values of subdivision vertices (:956-1038): x = 0 inside subdivision space,
-// a root stands for the octree node it replaces
+// a root stands for the octree node it replaces (same depth and position).  Every
+// neighbour of a level is a same-depth cell, so its function index is the level node's
+// own plus the slot offset: 9 basis values per level.  A subdivision node's own index
+// comes from its centre ((off + 1/2) / 2^d exactly).
 __global__ void __launch_bounds__(kBlock) k_sub_vertex_values(const Counters* c, int depth, const float* vx,
                                                               const float* vy, const float* vz, const int* vowner,
                                                               const int* neigh, size_t stride, const int* parent,
                                                               const int* s_neigh, size_t sstride,
                                                               const int* s_parent, const int* s_root,
-                                                              const unsigned char* s_contrib, const int* enc,
-                                                              const float* x, float* vvalue, int na) {
+                                                              const unsigned char* s_contrib, const int* s_depth,
+                                                              const float* s_cx, const float* s_cy,
+                                                              const float* s_cz, const int* enc, const float* x,
+                                                              float* vvalue, int na) {
     const int V = c->n_sub_vertices;
     const float iso = c->iso;
     PSR_GRID_STRIDE(v, V) {
@@ -943,28 +969,41 @@ __global__ void __launch_bounds__(kBlock) k_sub_vertex_values(const Counters* c,
         const float qx = vx[v], qy = vy[v], qz = vz[v];
         if (now > 0) {
             while (now != -1) {
-                // all 27 neighbours zero-valued subdivision nodes: every term is skipped
-                if (now >= na && !s_contrib[now - na]) { now = s_parent[now - na]; continue; }
-                if (now < na) {   // octree levels: same-depth neighbours, cached basis values
+                if (now < na) {   // octree levels
                     val = level_terms(now, val, qx, qy, qz, depth, neigh, stride, enc, x);
                     now = parent[now];
                     continue;
                 }
+                const int sn = now - na;
+                now = s_parent[sn];
+                // all 27 neighbours zero-valued subdivision nodes: every term is skipped
+                if (!s_contrib[sn]) continue;
+                const int d = s_depth[sn];
+                const float sc = (float)(1 << d);
+                const int base = (1 << d) - 1;
+                const int ox = base + (int)__fmul_rn(s_cx[sn], sc);
+                const int oy = base + (int)__fmul_rn(s_cy[sn], sc);
+                const int oz = base + (int)__fmul_rn(s_cz[sn], sc);
+                float bx[3], by[3], bz[3];
+#pragma unroll
+                for (int j = 0; j < 3; ++j) {
+                    bx[j] = basis32(ox - 1 + j, qx);
+                    by[j] = basis32(oy - 1 + j, qy);
+                    bz[j] = basis32(oz - 1 + j, qz);
+                }
+#pragma unroll
                 for (int k = 0; k < 27; ++k) {
-                    int nb = (now < na) ? neigh[(size_t)k * stride + now] : s_neigh[(size_t)k * sstride + (now - na)];
+                    int nb = s_neigh[(size_t)k * sstride + sn];
                     if (nb == -1) continue;
                     if (nb >= na) {
                         nb = s_root[nb - na];
                         if (nb < 0) continue;
                     }
-                    int ix, iy, iz;
-                    decode3m(enc[nb], depth, ix, iy, iz);
-                    float t = __fmul_rn(x[nb], basis32(ix, qx));
-                    t = __fmul_rn(t, basis32(iy, qy));
-                    t = __fmul_rn(t, basis32(iz, qz));
+                    float t = __fmul_rn(x[nb], bx[k / 9]);
+                    t = __fmul_rn(t, by[(k / 3) % 3]);
+                    t = __fmul_rn(t, bz[k % 3]);
                     val = __fadd_rn(val, t);
                 }
-                now = (now < na) ? parent[now] : s_parent[now - na];
             }
         }
         vvalue[v] = __fsub_rn(val, iso);
@@ -1189,7 +1228,7 @@ cudaError_t mesh_build_impl(Workspace& ws, const MeshBufs& mb) {
     k_mesh_reset<<<gm, kBlock, 0, s>>>(c, ws.node_vtx, ws.node_edge, ws.node_face, mb.ov_group, mb.ov_sub, stride);
     // vertices
     k_vertex_owner<<<gm, kBlock, 0, s>>>(c, ws.key, ws.neigh, stride, ws.vmask);
-    e = launch_scan(PopcLoad8{ws.vmask},
+    e = launch_scan<1>(PopcLoad8{ws.vmask},
                     VertexStore{ws.vmask, ws.ndepth, ws.ctr_x, ws.ctr_y, ws.ctr_z, ws.v_x, ws.v_y, ws.v_z, ws.v_owner,
                                 ws.v_kind, ws.v_depth, ws.cap.vertices, err},
                     &c->n_nodes, 0, ws.scan, total, err, s);
@@ -1198,7 +1237,7 @@ cudaError_t mesh_build_impl(Workspace& ws, const MeshBufs& mb) {
     k_vertex_maintain<<<gm, kBlock, 0, s>>>(c, ws.neigh, stride, ws.v_owner, ws.v_kind, ws.node_vtx);
     // edges (D level)
     k_edge_owner<<<gm, kBlock, 0, s>>>(c, D, ws.key, ws.neigh, stride, ws.emask16);
-    e = launch_scan(PopcLoad16{ws.emask16},
+    e = launch_scan<1>(PopcLoad16{ws.emask16},
                     EdgeStore{ws.emask16, &c->level_base[D], ws.e_owner, ws.e_kind, ws.cap.edges, err},
                     &c->level_count[D], 0, ws.scan, total, err, s);
     if (e != cudaSuccess) return e;
@@ -1206,7 +1245,7 @@ cudaError_t mesh_build_impl(Workspace& ws, const MeshBufs& mb) {
     k_edge_maintain<<<gm, kBlock, 0, s>>>(c, ws.neigh, stride, ws.e_owner, ws.e_kind, ws.node_edge);
     // faces
     k_face_owner<<<gm, kBlock, 0, s>>>(c, ws.key, ws.neigh, stride, ws.fmask);
-    e = launch_scan(PopcLoad8{ws.fmask},
+    e = launch_scan<1>(PopcLoad8{ws.fmask},
                     FaceStore{ws.fmask, ws.key, ws.ndepth, ws.parent, D, ws.f_owner, ws.f_kind, ws.f_hasparent,
                               ws.cap.faces, err},
                     &c->n_nodes, 0, ws.scan, total, err, s);
@@ -1217,7 +1256,7 @@ cudaError_t mesh_build_impl(Workspace& ws, const MeshBufs& mb) {
     k_vertex_values<<<gm, kBlock, 0, s>>>(c, D, ws.v_x, ws.v_y, ws.v_z, ws.v_owner, ws.v_kind, ws.v_depth, ws.neigh,
                                           stride, ws.parent, ws.first_child, ws.enc, ws.xsol, ws.vvalue);
     // crossings -> staged vertices of the main part
-    e = launch_scan(CrossLoad{ws.e_owner, ws.e_kind, ws.node_vtx, stride, ws.vvalue, err},
+    e = launch_scan<1>(CrossLoad{ws.e_owner, ws.e_kind, ws.node_vtx, stride, ws.vvalue, err},
                     CrossStore{ws.e_owner, ws.e_kind, ws.node_vtx, stride, ws.vvalue, ws.v_x, ws.v_y, ws.v_z,
                                ws.e_cross, ws.part_v, 0, ws.part_cap_v, err},
                     &c->n_edges, 0, ws.scan, total, err, s);
@@ -1225,14 +1264,14 @@ cudaError_t mesh_build_impl(Workspace& ws, const MeshBufs& mb) {
     k_set_count<<<1, 1, 0, s>>>(&c->n_cross, total, ws.part_cap_v, err);
     // face hits must start cleared
     cudaMemsetAsync(ws.face_hit, 0, sizeof(int) * (size_t)ws.cap.faces, s);
-    e = launch_scan(CubeLoad{ws.node_vtx, stride, &c->level_base[D], ws.vvalue, ws.cube_class, err},
+    e = launch_scan<1>(CubeLoad{ws.node_vtx, stride, &c->level_base[D], ws.vvalue, ws.cube_class, err},
                     CubeStore{ws.cube_class, &c->level_base[D], ws.node_edge, ws.node_face, stride, ws.e_cross,
                               ws.parent, ws.f_hasparent, ws.face_hit, ws.part_t, 0, ws.part_cap_t, err},
                     &c->level_count[D], 0, ws.scan, total, err, s);
     if (e != cudaSuccess) return e;
     k_set_count<<<1, 1, 0, s>>>(&c->n_tri, total, ws.part_cap_t, err);
     // subdivision roots among nodes of depth < D
-    e = launch_scan(RootLoad{ws.node_vtx, ws.node_face, stride, ws.vvalue, ws.face_hit, ws.first_child, err},
+    e = launch_scan<1>(RootLoad{ws.node_vtx, ws.node_face, stride, ws.vvalue, ws.face_hit, ws.first_child, err},
                     RootStore{ws.sub_root, ws.cap.nodes, err}, &c->level_base[D], 0, ws.scan, total, err, s);
     if (e != cudaSuccess) return e;
     k_set_count<<<1, 1, 0, s>>>(&c->n_subroots, total, ws.cap.nodes, err);
@@ -1279,7 +1318,7 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
     cudaMemsetAsync(ws.s_vtx, 0, sizeof(int) * 8 * dstride, s);
     cudaMemsetAsync(ws.s_edge, 0, sizeof(int) * 12 * dstride, s);
     k_sub_vertex_owner<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.s_key, ws.s_neigh, sstride, ws.s_vmask, na);
-    e = launch_scan(PopcLoad8{ws.s_vmask},
+    e = launch_scan<2>(PopcLoad8{ws.s_vmask},
                     SubVertexStore{ws.s_vmask, mb.groups, &c->n_groups, D, ws.s_cx, ws.s_cy, ws.s_cz, ws.sv_x, ws.sv_y,
                                    ws.sv_z, ws.sv_owner, ws.sv_kind, 8 * ws.cap.sub_dnodes, na, err},
                     &c->n_sub_dnodes, 0, ws.scan, total, err, s);
@@ -1288,7 +1327,7 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
     k_sub_vertex_maintain<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.s_neigh, sstride, ws.s_depth, ws.sv_owner,
                                                 ws.sv_kind, ws.s_vtx, dstride, na);
     k_sub_edge_owner<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.s_key, ws.s_neigh, sstride, ws.s_emask, na);
-    e = launch_scan(PopcLoad16{ws.s_emask},
+    e = launch_scan<2>(PopcLoad16{ws.s_emask},
                     SubEdgeStore{ws.s_emask, mb.groups, &c->n_groups, D, ws.se_owner, ws.se_kind,
                                  12 * ws.cap.sub_dnodes, na, err},
                     &c->n_sub_dnodes, 0, ws.scan, total, err, s);
@@ -1301,10 +1340,10 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
     k_sub_edge_maintain<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.s_neigh, sstride, ws.s_depth, ws.se_owner,
                                               ws.se_kind, ws.s_edge, dstride, na);
     k_sub_vertex_values<<<gs, kBlock, 0, s>>>(c, D, ws.sv_x, ws.sv_y, ws.sv_z, ws.sv_owner, ws.neigh, stride, ws.parent,
-                                              ws.s_neigh, sstride, ws.s_parent, ws.s_root, ws.s_contrib, ws.enc,
-                                              ws.xsol, ws.sv_value, na);
+                                              ws.s_neigh, sstride, ws.s_parent, ws.s_root, ws.s_contrib, ws.s_depth,
+                                              ws.s_cx, ws.s_cy, ws.s_cz, ws.enc, ws.xsol, ws.sv_value, na);
     // crossings: staged after the main part's vertices
-    e = launch_scan(SubCrossLoad{ws.se_owner, ws.se_kind, ws.s_vtx, dstride, mb.groups, &c->n_groups, D, ws.sv_value, na, err},
+    e = launch_scan<2>(SubCrossLoad{ws.se_owner, ws.se_kind, ws.s_vtx, dstride, mb.groups, &c->n_groups, D, ws.sv_value, na, err},
                     SubCrossStore{ws.se_owner, ws.se_kind, ws.s_vtx, dstride, mb.groups, &c->n_groups, D, ws.sv_value,
                                   ws.sv_x, ws.sv_y, ws.sv_z, ws.se_cross, ws.part_v, &c->n_cross, ws.part_cap_v, na,
                                   err},
@@ -1312,13 +1351,13 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
     if (e != cudaSuccess) return e;
     k_set_count<<<1, 1, 0, s>>>(&c->n_sub_cross, total, ws.part_cap_v, err);
     // triangle prefix per D-level sub node
-    e = launch_scan(SubCubeLoad{ws.s_vtx, dstride, ws.sv_value, ws.s_cube_class, err}, StoreExclusive{mb.tri_of_dnode},
+    e = launch_scan<2>(SubCubeLoad{ws.s_vtx, dstride, ws.sv_value, ws.s_cube_class, err}, StoreExclusive{mb.tri_of_dnode},
                     &c->n_sub_dnodes, 0, ws.scan, total, err, s);
     if (e != cudaSuccess) return e;
     k_set_count<<<1, 1, 0, s>>>(&c->n_sub_tri, total, ws.part_cap_t, err);
     k_part_table<<<1, 1, 0, s>>>(c, mb.groups, mb.edge_of_dnode, ws.se_cross, mb.tri_of_dnode,
                                  mb.group_cross0, mb.parts);
-    e = launch_scan(SubCubeLoad{ws.s_vtx, dstride, ws.sv_value, ws.s_cube_class, err},
+    e = launch_scan<2>(SubCubeLoad{ws.s_vtx, dstride, ws.sv_value, ws.s_cube_class, err},
                     SubCubeStore{ws.s_cube_class, ws.s_edge, dstride, ws.se_cross, mb.group_cross0, mb.groups,
                                  &c->n_groups, ws.part_t, &c->n_tri, ws.part_cap_t, err},
                     &c->n_sub_dnodes, 0, ws.scan, total, err, s);

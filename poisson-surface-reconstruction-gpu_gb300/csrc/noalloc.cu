@@ -45,7 +45,7 @@ constexpr size_t kNaVals = kNaKeys + 4ull * kNoAllocMaxPoints;
 constexpr size_t kNaHist = kNaVals + 4ull * kNoAllocMaxPoints;
 constexpr size_t kNaHistBytes = ((4ull * ((size_t)kRadix * kNoAllocSortTiles + 16)) + 255) & ~255ull;
 constexpr size_t kNaScan = kNaHist + kNaHistBytes;
-constexpr size_t kNaBytes = kNaScan + 8ull * (kNoAllocScanTiles + 1);
+constexpr size_t kNaBytes = kNaScan + 8ull * (kNoAllocScanTiles + kScanHeader);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
 

@@ -6,18 +6,24 @@
 
 namespace psr {
 
-constexpr int kScanItems = 8;
-constexpr int kScanTile = kBlock * kScanItems;   // 2048 elements per tile
+constexpr int kScanItems = 8;                    // default items per thread
+constexpr int kScanTile = kBlock * kScanItems;   // 2048 elements per default tile
+constexpr int kScanMinTile = kBlock;             // smallest tile (1 item per thread)
 
-// Scratch of one scan call: tile counter + one 64-bit status word per tile
-// (bit 62: aggregate published, bit 63: inclusive prefix published, low 32 bits value).
+// Scratch of the scans: [0] tile counter, [1] blocks finished, [2] epoch, [3 + t] status
+// of tile t.  A status word is value (bits 0-31) | aggregate flag (32) | inclusive flag
+// (33) | epoch (34-63); only statuses of the running launch's epoch count, so nothing is
+// cleared between launches: the last block of a launch resets the counters and advances
+// the epoch (launches on one stream are ordered, so the next launch sees both).
 struct ScanScratch {
-    unsigned long long* words;   // [0] = tile counter, [1 + t] = status of tile t
+    unsigned long long* words;
     int max_tiles;
 };
+constexpr int kScanHeader = 3;
 
-constexpr unsigned long long kFlagAgg = 1ull << 62;
-constexpr unsigned long long kFlagIncl = 1ull << 63;
+constexpr unsigned long long kFlagAgg = 1ull << 32;
+constexpr unsigned long long kFlagIncl = 1ull << 33;
+constexpr int kEpochShift = 34;
 
 __device__ __forceinline__ unsigned long long load_status(const unsigned long long* p) {
     return *((volatile const unsigned long long*)p);
@@ -53,15 +59,18 @@ __device__ __forceinline__ unsigned block_exclusive_scan(unsigned v, unsigned& e
 }
 
 // Generic scan.  Load(i) -> unsigned value of element i; Store(i, prefix, value) gets the
-// exclusive prefix of element i.  *total receives the sum of all n elements.
-template <class Load, class Store>
+// exclusive prefix of element i.  *total receives the sum of all n elements.  kItems
+// elements per thread: 8 for light functors, 1 or 2 where Load / Store do enough work per
+// element that more, smaller tiles (more blocks in flight) pay.
+template <int kItems, class Load, class Store>
 __global__ void __launch_bounds__(kBlock) k_scan(Load load, Store store, const int* count_ptr, int count_add,
                                                  ScanScratch sc, unsigned* total, unsigned* err) {
+    constexpr int kTile = kBlock * kItems;
     __shared__ unsigned s_warp[kBlock / 32 + 1];
     __shared__ int s_tile;
     __shared__ unsigned s_prefix;
     const int n = *count_ptr + count_add;
-    const int ntiles = (n + kScanTile - 1) / kScanTile;
+    const int ntiles = (n + kTile - 1) / kTile;
     if (n <= 0) {
         if (blockIdx.x == 0 && threadIdx.x == 0) *total = 0u;
         return;
@@ -70,17 +79,20 @@ __global__ void __launch_bounds__(kBlock) k_scan(Load load, Store store, const i
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(err, kErrCapacity);
         return;
     }
+    unsigned long long* st = sc.words + kScanHeader;
+    const unsigned long long epoch = load_status(sc.words + 2);
+    const unsigned long long etag = epoch << kEpochShift;
     while (true) {
         if (threadIdx.x == 0) s_tile = (int)atomicAdd(sc.words, 1ull);
         __syncthreads();
         const int t = s_tile;
         __syncthreads();
         if (t >= ntiles) break;
-        const int base = t * kScanTile + threadIdx.x * kScanItems;
-        unsigned v[kScanItems];
+        const int base = t * kTile + threadIdx.x * kItems;
+        unsigned v[kItems];
         unsigned sum = 0;
 #pragma unroll
-        for (int k = 0; k < kScanItems; ++k) {
+        for (int k = 0; k < kItems; ++k) {
             int i = base + k;
             v[k] = (i < n) ? load(i) : 0u;
             sum += v[k];
@@ -90,14 +102,13 @@ __global__ void __launch_bounds__(kBlock) k_scan(Load load, Store store, const i
         // look-back by warp 0
         if (threadIdx.x < 32) {
             const unsigned lane = lane_id();
-            unsigned long long* st = sc.words + 1;
             if (t == 0) {
                 if (lane == 0) {
-                    atomicExch(st, kFlagIncl | (unsigned long long)agg);
+                    atomicExch(st, etag | kFlagIncl | (unsigned long long)agg);
                     s_prefix = 0u;
                 }
             } else {
-                if (lane == 0) atomicExch(st + t, kFlagAgg | (unsigned long long)agg);
+                if (lane == 0) atomicExch(st + t, etag | kFlagAgg | (unsigned long long)agg);
                 unsigned run = 0;
                 int pred = t - 1;
                 bool timeout = false;
@@ -107,7 +118,7 @@ __global__ void __launch_bounds__(kBlock) k_scan(Load load, Store store, const i
                     if (idx >= 0) {
                         int it = 0;
                         s = load_status(st + idx);
-                        while (!(s & (kFlagAgg | kFlagIncl))) {
+                        while ((s >> kEpochShift) != epoch || !(s & (kFlagAgg | kFlagIncl))) {
                             if (++it > kSpinLimit) { timeout = true; s = kFlagIncl; break; }
                             __nanosleep(20);
                             s = load_status(st + idx);
@@ -130,7 +141,7 @@ __global__ void __launch_bounds__(kBlock) k_scan(Load load, Store store, const i
                 }
                 if (__any_sync(0xffffffffu, timeout) && lane == 0) atomicOr(err, kErrSpinTimeout);
                 if (lane == 0) {
-                    atomicExch(st + t, kFlagIncl | (unsigned long long)(run + agg));
+                    atomicExch(st + t, etag | kFlagIncl | (unsigned long long)(run + agg));
                     s_prefix = run;
                 }
             }
@@ -138,7 +149,7 @@ __global__ void __launch_bounds__(kBlock) k_scan(Load load, Store store, const i
         __syncthreads();
         unsigned pre = s_prefix + excl;
 #pragma unroll
-        for (int k = 0; k < kScanItems; ++k) {
+        for (int k = 0; k < kItems; ++k) {
             int i = base + k;
             if (i < n) store(i, pre, v[k]);
             pre += v[k];
@@ -146,18 +157,25 @@ __global__ void __launch_bounds__(kBlock) k_scan(Load load, Store store, const i
         if (t == ntiles - 1 && threadIdx.x == kBlock - 1) *total = s_prefix + agg;
         __syncthreads();
     }
+    // every block ends here after claiming a tile past the end, i.e. after its last tile;
+    // the last one to arrive resets the counters for the next launch
+    if (threadIdx.x == 0) {
+        const unsigned long long done = atomicAdd(sc.words + 1, 1ull);
+        if (done == (unsigned long long)gridDim.x - 1) {
+            atomicExch(sc.words, 0ull);
+            atomicExch(sc.words + 1, 0ull);
+            atomicExch(sc.words + 2, (epoch + 1) & ((1ull << (64 - kEpochShift)) - 1));
+        }
+    }
 }
 
-// host launcher (declared here, defined in primitives.cu)
-struct Device;
 int scan_grid(int max_tiles);
 
-template <class Load, class Store>
+template <int kItems = kScanItems, class Load, class Store>
 inline cudaError_t launch_scan(Load load, Store store, const int* count_ptr, int count_add, ScanScratch sc,
                                unsigned* total, unsigned* err, cudaStream_t stream) {
-    cudaError_t e = cudaMemsetAsync(sc.words, 0, sizeof(unsigned long long) * (size_t)(sc.max_tiles + 1), stream);
-    if (e != cudaSuccess) return e;
-    k_scan<Load, Store><<<scan_grid(sc.max_tiles), kBlock, 0, stream>>>(load, store, count_ptr, count_add, sc, total, err);
+    k_scan<kItems, Load, Store><<<scan_grid(sc.max_tiles), kBlock, 0, stream>>>(load, store, count_ptr, count_add, sc,
+                                                                                total, err);
     return cudaGetLastError();
 }
 

@@ -13,7 +13,6 @@ PSR_DEFINE_CONST_TABLES(upload_tables_transfer)
 
 namespace psr {
 
-constexpr int kGridLevel = 6;   // 64^3 cells
 
 __device__ __forceinline__ unsigned morton3(int x, int y, int z, int g) {
     unsigned m = 0;
@@ -218,7 +217,7 @@ cudaError_t transfer_build(Workspace& ws, int with_colour, int with_normals) {
     const int grid = ws.num_sms * 8;
     const int D = ws.depth;
     if (with_colour) {
-        const int g = D < kGridLevel ? D : kGridLevel;
+        const int g = D < kColourGridLevel ? D : kColourGridLevel;
         int* cell_start = ws.cell_start;   // (1 << 3g) + 1 entries
         k_cell_starts<<<grid, kBlock, 0, s>>>(ws.cnt, D, g, ws.key, ws.point2node, cell_start);
         k_colour<<<grid, kBlock, 0, s>>>(ws.cnt, g, ws.mesh_v, ws.px, ws.py, ws.pz, ws.cr, ws.cg, ws.cb, cell_start,

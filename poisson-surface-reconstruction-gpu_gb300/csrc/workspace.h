@@ -155,6 +155,10 @@ struct Workspace {
     int num_sms;
 };
 
+// sample grid of the colour search: 2^g cells per axis (128^3: a few samples per surface
+// cell at 200k points)
+constexpr int kColourGridLevel = 7;
+
 // grid of a grid-stride kernel over `work` items: enough blocks, at most 8 per SM
 inline int grid_for(const Workspace& ws, long long work) {
     long long g = (work + kBlock - 1) / kBlock;
