@@ -286,7 +286,8 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
         build_dff_table(D, dff);
         std::vector<float> st;
         build_stencil(kMaxDepth, st);
-        e = cudaMemcpy(ws.dff, dff.data(), dff.size() * sizeof(double), cudaMemcpyHostToDevice);
+        std::vector<float> dff32(dff.begin(), dff.end());   // the kernels use float entries
+        e = cudaMemcpy(ws.dff, dff32.data(), dff32.size() * sizeof(float), cudaMemcpyHostToDevice);
         if (e == cudaSuccess) e = cudaMemcpy(ws.stencil, st.data(), st.size() * sizeof(float), cudaMemcpyHostToDevice);
     }
     if (e == cudaSuccess) {

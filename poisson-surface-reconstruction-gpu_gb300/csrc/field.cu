@@ -7,7 +7,9 @@
 // ~1e-4 relative accuracy at depth 7; the value is the same function).
 // Divergence (mesh/ComputeNodesDivergence.cu:25-136): for every node o
 //     div[o] = sum_{27 neighbours nb} sum_{D-level l under nb} V[l] . dff(o, l)
-// with float terms accumulated in FP64, as in the reference's finer-depth kernel.  The
+// with float terms (table entries rounded to float, as the reference's kernel does)
+// accumulated as float pairs (TwoSum, ~44 bits; GB300's FP64 rate is far below FP32), in
+// a fixed order.  The
 // reference's coarse-depth host loop (one node at a time, :159-207) is replaced by one
 // chunked reduction over all coarse nodes.
 #include "workspace.h"
@@ -64,20 +66,20 @@ __device__ __forceinline__ void decode3(int e, int depth, int& ix, int& iy, int&
 }
 
 // contribution of D-level leaves [l0, l1) to node o's divergence
-__device__ __forceinline__ double div_terms(int l0, int l1, int step, int ox, int oy, int oz, int depth, int res,
-                                            int bD, const int* enc, const float* vx, const float* vy, const float* vz,
-                                            const double* dff) {
-    double acc = 0.0;
+__device__ __forceinline__ FF div_terms(int l0, int l1, int step, int ox, int oy, int oz, int depth, int res,
+                                        int bD, const int* enc, const float* vx, const float* vy, const float* vz,
+                                        const float* dff) {
+    FF acc = ff_zero();
     for (int l = l0; l < l1; l += step) {
         int lx, ly, lz;
         decode3(enc[bD + l], depth, lx, ly, lz);
-        float ux = (float)dff[(size_t)ox + (size_t)res * lx];
-        float uy = (float)dff[(size_t)oy + (size_t)res * ly];
-        float uz = (float)dff[(size_t)oz + (size_t)res * lz];
-        float t = vx[l] * ux;
+        const float ux = dff[(size_t)ox + (size_t)res * lx];
+        const float uy = dff[(size_t)oy + (size_t)res * ly];
+        const float uz = dff[(size_t)oz + (size_t)res * lz];
+        float t = __fmul_rn(vx[l], ux);
         t = fmaf(vy[l], uy, t);
         t = fmaf(vz[l], uz, t);
-        acc += (double)t;
+        acc = ff_add_float(acc, t);
     }
     return acc;
 }
@@ -89,7 +91,7 @@ __device__ __forceinline__ double div_terms(int l0, int l1, int step, int ox, in
 __global__ void __launch_bounds__(kBlock) k_div_fine(const Counters* c, int depth, int dsplit, int res,
                                                      const int* enc, const int* didx, const int* dnum,
                                                      const int* neigh, size_t stride, const float* vx,
-                                                     const float* vy, const float* vz, const double* dff,
+                                                     const float* vy, const float* vz, const float* dff,
                                                      float* divg) {
     __shared__ int s_off[kBlock / 32][33];
     __shared__ int s_base[kBlock / 32][32];
@@ -118,23 +120,23 @@ __global__ void __launch_bounds__(kBlock) k_div_fine(const Counters* c, int dept
         s_base[wib][lane] = base;
         const int total = __shfl_sync(0xffffffffu, incl, 31);
         __syncwarp();
-        double acc = 0.0;
+        FF acc = ff_zero();
         int k = 0;
         for (int t = lane; t < total; t += 32) {
             while (k < 26 && s_off[wib][k + 1] <= t) ++k;   // terms are visited in increasing order
             const int l = s_base[wib][k] + (t - s_off[wib][k]);
             int lx, ly, lz;
             decode3(enc[bD + l], depth, lx, ly, lz);
-            float ux = (float)dff[(size_t)ox + (size_t)res * lx];
-            float uy = (float)dff[(size_t)oy + (size_t)res * ly];
-            float uz = (float)dff[(size_t)oz + (size_t)res * lz];
-            float tt = vx[l] * ux;
+            const float ux = dff[(size_t)ox + (size_t)res * lx];
+            const float uy = dff[(size_t)oy + (size_t)res * ly];
+            const float uz = dff[(size_t)oz + (size_t)res * lz];
+            float tt = __fmul_rn(vx[l], ux);
             tt = fmaf(vy[l], uy, tt);
             tt = fmaf(vz[l], uz, tt);
-            acc += (double)tt;
+            acc = ff_add_float(acc, tt);
         }
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (lane == 0) divg[i] = (float)acc;
+        acc = ff_warp_sum(acc);
+        if (lane == 0) divg[i] = ff_to_float(acc);
         __syncwarp();
     }
 }
@@ -169,8 +171,8 @@ __global__ void __launch_bounds__(kBlock) k_div_chunks(const Counters* c, int de
                                                        const int* n_items_ptr, const unsigned* item_start,
                                                        const int* enc, const int* didx, const int* dnum,
                                                        const int* neigh, size_t stride, const float* vx,
-                                                       const float* vy, const float* vz, const double* dff,
-                                                       double* partial) {
+                                                       const float* vy, const float* vz, const float* dff,
+                                                       FF* partial) {
     const int n_nodes = c->level_base[dsplit];
     const int n_items = *n_items_ptr;
     const int bD = c->level_base[depth];
@@ -195,7 +197,7 @@ __global__ void __launch_bounds__(kBlock) k_div_chunks(const Counters* c, int de
             if (rem < nc) { nb = q; ch = rem; break; }
             rem -= nc;
         }
-        double acc = 0.0;
+        FF acc = ff_zero();
         if (nb >= 0) {
             int ox, oy, oz;
             decode3(enc[i], depth, ox, oy, oz);
@@ -203,22 +205,22 @@ __global__ void __launch_bounds__(kBlock) k_div_chunks(const Counters* c, int de
             const int l1 = min(didx[nb] + dnum[nb], l0 + kDivChunk);
             acc = div_terms(l0 + lane, l1, 32, ox, oy, oz, depth, res, bD, enc, vx, vy, vz, dff);
         }
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        acc = ff_warp_sum(acc);
         if (lane == 0) partial[it] = acc;
     }
 }
 
 __global__ void __launch_bounds__(kBlock) k_div_coarse_reduce(const Counters* c, int dsplit, const unsigned* item_start,
-                                                              const int* n_items_ptr, const double* partial,
+                                                              const int* n_items_ptr, const FF* partial,
                                                               float* divg) {
     const int n_nodes = c->level_base[dsplit];
     const int n_items = *n_items_ptr;
     PSR_GRID_STRIDE(i, n_nodes) {
         int a = (int)item_start[i];
         int b = (i + 1 < n_nodes) ? (int)item_start[i + 1] : n_items;
-        double s = 0.0;
-        for (int t = a; t < b; ++t) s += partial[t];
-        divg[i] = (float)s;
+        FF s = ff_zero();
+        for (int t = a; t < b; ++t) s = ff_add(s, partial[t]);
+        divg[i] = ff_to_float(s);
     }
 }
 
@@ -244,11 +246,12 @@ cudaError_t field_build(Workspace& ws) {
         cudaError_t e = launch_scan(DivChunkLoad{ws.neigh, stride, ws.dnum}, StoreExclusive{item_start},
                                     &c->level_base[dsplit], 0, ws.scan, total, &c->error, s);
         if (e != cudaSuccess) return e;
-        const int item_cap = ws.cap.nodes;   // partial buffer holds cap.nodes doubles
+        const int item_cap = ws.cap.nodes;   // partial buffer holds cap.nodes float pairs
         k_div_chunk_count<<<1, 1, 0, s>>>(c, dsplit, total, item_cap, n_items);
+        FF* partial = reinterpret_cast<FF*>(ws.cg_partial);
         k_div_chunks<<<ws.num_sms * 8, kBlock, 0, s>>>(c, D, dsplit, ws.res, n_items, item_start, ws.enc, ws.didx,
-                                                       ws.dnum, ws.neigh, stride, vx, vy, vz, ws.dff, ws.cg_partial);
-        k_div_coarse_reduce<<<grid_for(ws, 1 << 16), kBlock, 0, s>>>(c, dsplit, item_start, n_items, ws.cg_partial,
+                                                       ws.dnum, ws.neigh, stride, vx, vy, vz, ws.dff, partial);
+        k_div_coarse_reduce<<<grid_for(ws, 1 << 16), kBlock, 0, s>>>(c, dsplit, item_start, n_items, partial,
                                                                     ws.divg);
     }
     return cudaGetLastError();

@@ -753,6 +753,7 @@ __global__ void __launch_bounds__(kBlock) k_sub_neighbours(const Counters* c, in
         const int g = lo;
         const int* G = groups + (size_t)g * kGroupRec;
         const int s = G[3] + sub_level_off(G[0], G[2], d) + (t - (G[5] >> sh));
+        const bool at_root_depth = (d == G[0]);
         int contrib = 0;
         const int son = (s_key[s] >> (3 * (depth - d))) & 7;
         const int pa = s_parent[s];
@@ -777,7 +778,9 @@ __global__ void __launch_bounds__(kBlock) k_sub_neighbours(const Counters* c, in
                 }
             }
             s_neigh[(size_t)k * sstride + s] = v;
-            if (v >= 0 && (v < na || s_root[v - na] >= 0)) contrib = 1;
+            // a contributing neighbour is an octree node or a root; the subdivision nodes at a
+            // group's root depth are exactly its roots, and deeper ones are never roots
+            if (v >= 0 && (v < na || at_root_depth)) contrib = 1;
         }
         s_contrib[s] = (unsigned char)contrib;
     }

@@ -85,60 +85,81 @@ __device__ __forceinline__ void knn_merge(float (&ad)[4], int (&ai)[4], const fl
     knn_cswap(ad[2], ai[2], ad[3], ai[3]);
 }
 
-// one warp per mesh vertex: the grid is searched in cubic shells around the vertex's
-// cell (first the 3x3x3 block, then shell r = 2, 3, ...); the lanes take the shell's cells
-// one each, scan their samples into private sorted 4-lists, and the lists are merged with
-// butterfly shuffles after each shell.  The search stops once the 4th distance is below
-// the distance to anything outside the searched block.
-__global__ void __launch_bounds__(kBlock) k_colour(const Counters* c, int g, const float* mv, const float* px,
+// One warp per mesh vertex.  The samples are Morton-sorted, so the samples of a grid cell
+// at any level g <= gmax form one contiguous range, read from the level-gmax table at
+// cell codes shifted by 3 (gmax - g).  Starting at the finest level, the warp gathers the
+// samples of the 3x3x3 block of cells around the vertex's cell (the 27 ranges are
+// flattened over the lanes for balance), keeps the 4 nearest (private sorted lists merged
+// with butterfly shuffles) and stops when the 4th distance is below one cell width: every
+// sample outside the block is at least that far.  Otherwise it restarts one level
+// coarser, where the block covers the finer one.
+__global__ void __launch_bounds__(kBlock) k_colour(const Counters* c, int gmax, const float* mv, const float* px,
                                                    const float* py, const float* pz, const float* cr, const float* cg,
                                                    const float* cb, const int* cell_start, float* out) {
+    __shared__ int s_off[kBlock / 32][28];
+    __shared__ int s_base[kBlock / 32][27];
     const int V = c->n_mesh_vertices;
-    const int G = 1 << g;
     const int lane = lane_id();
+    const int wib = threadIdx.x >> 5;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     for (int v = warp; v < V; v += nwarps) {
         const float qx = mv[3 * (size_t)v], qy = mv[3 * (size_t)v + 1], qz = mv[3 * (size_t)v + 2];
-        float bd[4] = {1e6f, 1e6f, 1e6f, 1e6f};
-        int bi[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
         float md[4];
         int mi[4];
-        const int cx = min(max((int)floorf(qx * G), 0), G - 1);
-        const int cy = min(max((int)floorf(qy * G), 0), G - 1);
-        const int cz = min(max((int)floorf(qz * G), 0), G - 1);
-        for (int r = 1; r <= G; ++r) {
-            const int side = 2 * r + 1;
-            const int ncell = side * side * side;
-            for (int t = lane; t < ncell; t += 32) {
-                const int ta = t / (side * side), tr = t - ta * side * side;
-                const int tb = tr / side, tz = tr - tb * side;
-                const int a = cx - r + ta, b = cy - r + tb, z = cz - r + tz;
-                if (a < 0 || a >= G || b < 0 || b >= G || z < 0 || z >= G) continue;
-                // shell cells only (the first round takes the whole 3x3x3 block)
-                if (r > 1 && max(abs(a - cx), max(abs(b - cy), abs(z - cz))) != r) continue;
-                const unsigned m = morton3(a, b, z, g);
-                const int s0 = cell_start[m], s1 = cell_start[m + 1];
-                for (int i = s0; i < s1; ++i) {
-                    const float dx = __fsub_rn(qx, px[i]), dy = __fsub_rn(qy, py[i]), dz = __fsub_rn(qz, pz[i]);
-                    const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-                    knn_insert(bd, bi, d2, i);
+        for (int g = gmax; g >= 0; --g) {
+            const int G = 1 << g;
+            const int shift = 3 * (gmax - g);
+            const int cx = min(max((int)floorf(qx * G), 0), G - 1);
+            const int cy = min(max((int)floorf(qy * G), 0), G - 1);
+            const int cz = min(max((int)floorf(qz * G), 0), G - 1);
+            int cnt = 0, base = 0;
+            if (lane < 27) {
+                const int a = cx + lane / 9 - 1, b = cy + (lane / 3) % 3 - 1, z = cz + lane % 3 - 1;
+                if (a >= 0 && a < G && b >= 0 && b < G && z >= 0 && z < G) {
+                    const unsigned m = morton3(a, b, z, g);
+                    base = cell_start[(size_t)m << shift];
+                    cnt = cell_start[(size_t)(m + 1) << shift] - base;
                 }
             }
+            int incl = cnt;
 #pragma unroll
-            for (int k = 0; k < 4; ++k) { md[k] = bd[k]; mi[k] = bi[k]; }
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            if (lane < 27) {
+                s_off[wib][lane] = incl - cnt;
+                s_base[wib][lane] = base;
+            }
+            if (lane == 26) s_off[wib][27] = incl;
+            const int total = __shfl_sync(0xffffffffu, incl, 26);
+            __syncwarp();
+            float bd[4] = {1e6f, 1e6f, 1e6f, 1e6f};
+            int bi[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
+            int k = 0;
+            for (int t = lane; t < total; t += 32) {
+                while (s_off[wib][k + 1] <= t) ++k;   // flattened index -> cell (increasing)
+                const int i = s_base[wib][k] + (t - s_off[wib][k]);
+                const float dx = __fsub_rn(qx, px[i]), dy = __fsub_rn(qy, py[i]), dz = __fsub_rn(qz, pz[i]);
+                const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                knn_insert(bd, bi, d2, i);
+            }
+            __syncwarp();
+#pragma unroll
+            for (int q = 0; q < 4; ++q) { md[q] = bd[q]; mi[q] = bi[q]; }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 float od[4];
                 int oi[4];
 #pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    od[k] = __shfl_xor_sync(0xffffffffu, md[k], o);
-                    oi[k] = __shfl_xor_sync(0xffffffffu, mi[k], o);
+                for (int q = 0; q < 4; ++q) {
+                    od[q] = __shfl_xor_sync(0xffffffffu, md[q], o);
+                    oi[q] = __shfl_xor_sync(0xffffffffu, mi[q], o);
                 }
                 knn_merge(md, mi, od, oi);
             }
-            const float lim = (float)r / (float)G;
+            const float lim = 1.0f / (float)G;
             if (mi[3] != 0x7fffffff && md[3] < lim * lim) break;
         }
         if (lane == 0) {

@@ -87,7 +87,7 @@ struct Workspace {
 
     // function tables (FP64, res x res) and per-depth stencil coefficients
     int res;
-    double* dff;            // d/dx F_i . F_j  (index i + res * j)
+    float* dff;             // d/dx F_i . F_j rounded to float (index i + res * j)
     float* stencil;         // [D+1][27] Laplacian coefficients (0 where dropped)
 
     // field / solve
@@ -97,7 +97,7 @@ struct Workspace {
     cudaEvent_t ev_cg = nullptr;   // recorded right after the CG kernel (stage timing)
     float *cg_r, *cg_p, *cg_q, *cg_ap;   // residual, two direction buffers, A p
     int* cg_blk;            // CG block table: 64 same-depth nodes per sibling group
-    double* cg_partial;     // per-CTA per-depth partial sums
+    double* cg_partial;     // scratch: divergence chunk sums (float pairs, 8 bytes each)
     float* point_val;       // N
     double* iso_partial;
 
