@@ -236,6 +236,7 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     A.add(ws.sv_x, 8 * (size_t)subd); A.add(ws.sv_y, 8 * (size_t)subd); A.add(ws.sv_z, 8 * (size_t)subd);
     A.add(ws.sv_owner, 8 * (size_t)subd); A.add(ws.sv_kind, 8 * (size_t)subd); A.add(ws.sv_value, 8 * (size_t)subd);
     A.add(ws.se_owner, 12 * (size_t)subd); A.add(ws.se_kind, 12 * (size_t)subd); A.add(ws.se_cross, 12 * (size_t)subd);
+    A.add(ws.se_dn, 12 * (size_t)subd);
     A.add(ws.s_cube_class, (size_t)subd);
     A.add(ws.mesh_v, 3 * (size_t)cap.mesh_vertices);
     A.add(ws.mesh_t, 3 * (size_t)cap.mesh_tris);

@@ -318,7 +318,7 @@ struct FaceStore {
             if (!((m >> f) & 1)) continue;
             fowner[q] = i;
             fkind[q] = f;
-            fhas[q] = (parent[i] == -1) ? -1 : ((c_tab.parent_face_kind[son][f] != -1) ? 1 : -1);
+            fhas[q] = (parent[i] == -1) ? -1 : ((__ldg(&g_tab.parent_face_kind[son][f]) != -1) ? 1 : -1);
             ++q;
         }
     }
@@ -368,7 +368,7 @@ __global__ void __launch_bounds__(kBlock) k_vertex_values(const Counters* c, int
             }
             node = ow;
             int d = vdepth[v];
-            const int ec = c_tab.children_vertex_kind[vkind[v]];
+            const int ec = __ldg(&g_tab.children_vertex_kind[vkind[v]]);
             while (d < depth) {
                 d++;
                 const int fc = first_child[node];
@@ -402,8 +402,8 @@ struct CrossLoad {
     unsigned* err;
     __device__ unsigned operator()(int e) const {
         const int ow = eowner[e], kind = ekind[e];
-        const float a = ptr_value(vvalue, node_vtx[(size_t)c_tab.edge_vertex[kind][0] * stride + ow], err);
-        const float b = ptr_value(vvalue, node_vtx[(size_t)c_tab.edge_vertex[kind][1] * stride + ow], err);
+        const float a = ptr_value(vvalue, node_vtx[(size_t)__ldg(&g_tab.edge_vertex[kind][0]) * stride + ow], err);
+        const float b = ptr_value(vvalue, node_vtx[(size_t)__ldg(&g_tab.edge_vertex[kind][1]) * stride + ow], err);
         return (__fmul_rn(a, b) <= 0.0f) ? 1u : 0u;
     }
 };
@@ -426,8 +426,8 @@ struct CrossStore {
         const int at = voff + (int)pre;
         if (at >= cap) { atomicOr(err, kErrCapacity); return; }
         const int ow = eowner[e], kind = ekind[e];
-        const int v1 = node_vtx[(size_t)c_tab.edge_vertex[kind][0] * stride + ow] - 1;
-        const int v2 = node_vtx[(size_t)c_tab.edge_vertex[kind][1] * stride + ow] - 1;
+        const int v1 = node_vtx[(size_t)__ldg(&g_tab.edge_vertex[kind][0]) * stride + ow] - 1;
+        const int v2 = node_vtx[(size_t)__ldg(&g_tab.edge_vertex[kind][1]) * stride + ow] - 1;
         if (v1 < 0 || v2 < 0) return;   // only reachable for a malformed tree (flagged in the load)
         interp_point(vx[v1], vy[v1], vz[v1], vx[v2], vy[v2], vz[v2], kind >> 2, vvalue[v1], vvalue[v2],
                      &part_v[3 * (size_t)at]);
@@ -448,7 +448,7 @@ struct CubeLoad {
         for (int q = 0; q < 8; ++q)
             if (ptr_value(vvalue, node_vtx[(size_t)q * stride + i], err) < 0.0f) cls |= 1 << q;
         cube_class[o] = cls;
-        return (unsigned)c_tab.mc_count[cls];
+        return (unsigned)__ldg(&g_tab.mc_count[cls]);
     }
 };
 
@@ -472,7 +472,7 @@ struct CubeStore {
         if (!cnt) return;
         const int i = *base_ptr + o;
         const int cls = cube_class[o];
-        const unsigned long long tri = c_tab.mc_tri[cls];
+        const unsigned long long tri = __ldg(&g_tab.mc_tri[cls]);
         unsigned used = 0;
         for (int t = 0; t < (int)cnt; ++t) {
             const int at = toff + (int)pre + t;
@@ -862,14 +862,17 @@ __device__ __forceinline__ int sub_node_to_dnode(int s, const int* groups, int n
 
 // maintainSubdivideVertexNodePointer (:765-810): s_vtx indexed by D-level sub node
 __global__ void __launch_bounds__(kBlock) k_sub_vertex_maintain(const Counters* c, int depth, const int* groups,
-                                                                const int* s_neigh, size_t sstride,
+                                                                const int* s_group, const int* s_neigh, size_t sstride,
                                                                 const int* s_depth, const int* vowner,
                                                                 const int* vkind, int* s_vtx, size_t dstride,
                                                                 int na) {
     const int V = c->n_sub_vertices;
-    const int ng = c->n_groups;
+    const int SD = c->n_sub_dnodes;
     PSR_GRID_STRIDE(v, V) {
         const int ow = vowner[v] - na;
+        // neighbours of a subdivision node lie in its own group's region
+        const int* G = groups + (size_t)s_group[ow] * kGroupRec;
+        const int dbase = G[3] + sub_level_off(G[0], G[2], depth) - G[5];   // node - dnode
         int mx, my, mz;
         corner_sides(vkind[v], mx, my, mz);
 #pragma unroll
@@ -877,8 +880,8 @@ __global__ void __launch_bounds__(kBlock) k_sub_vertex_maintain(const Counters* 
             const int ax = (j & 1) ? mx : 0, ay = (j & 2) ? my : 0, az = (j & 4) ? mz : 0;
             const int nb = s_neigh[(size_t)nslot(ax, ay, az) * sstride + ow];
             if (nb >= na && s_depth[nb - na] == depth) {
-                const int dn = sub_node_to_dnode(nb - na, groups, ng, depth);
-                s_vtx[(size_t)vertex_slot_of(ax, ay, az, mx, my, mz) * dstride + dn] = v + 1;
+                const int dn = nb - na - dbase;
+                if ((unsigned)dn < (unsigned)SD) s_vtx[(size_t)vertex_slot_of(ax, ay, az, mx, my, mz) * dstride + dn] = v + 1;
             }
         }
     }
@@ -913,7 +916,7 @@ struct SubEdgeStore {
     const int* groups;
     const int* ng_ptr;
     int depth;
-    int *eowner, *ekind;
+    int *eowner, *ekind, *edn;
     int cap;
     int na;
     unsigned* err;
@@ -924,27 +927,31 @@ struct SubEdgeStore {
         const unsigned m = emask[o];
         int q = (int)pre;
         for (int e = 0; e < 12; ++e)
-            if ((m >> e) & 1) { eowner[q] = na + s; ekind[q] = e; ++q; }
+            if ((m >> e) & 1) { eowner[q] = na + s; ekind[q] = e; edn[q] = o; ++q; }
     }
 };
 
 // maintainSubdivideEdgeNodePointer (:888-949)
 __global__ void __launch_bounds__(kBlock) k_sub_edge_maintain(const Counters* c, int depth, const int* groups,
-                                                              const int* s_neigh, size_t sstride, const int* s_depth,
+                                                              const int* s_group, const int* s_neigh, size_t sstride,
+                                                              const int* s_depth,
                                                               const int* eowner, const int* ekind, int* s_edge,
                                                               size_t dstride, int na) {
     const int E = c->n_sub_edges;
-    const int ng = c->n_groups;
+    const int SD = c->n_sub_dnodes;
     PSR_GRID_STRIDE(ei, E) {
         const int ow = eowner[ei] - na, kind = ekind[ei];
+        // neighbours of a subdivision node lie in its own group's region
+        const int* G = groups + (size_t)s_group[ow] * kGroupRec;
+        const int dbase = G[3] + sub_level_off(G[0], G[2], depth) - G[5];   // node - dnode
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             int a[3];
             edge_offset(kind, j, a);
             const int nb = s_neigh[(size_t)nslot(a[0], a[1], a[2]) * sstride + ow];
             if (nb >= na && s_depth[nb - na] == depth) {
-                const int dn = sub_node_to_dnode(nb - na, groups, ng, depth);
-                s_edge[(size_t)edge_slot_of(kind, a) * dstride + dn] = ei + 1;
+                const int dn = nb - na - dbase;
+                if ((unsigned)dn < (unsigned)SD) s_edge[(size_t)edge_slot_of(kind, a) * dstride + dn] = ei + 1;
             }
         }
     }
@@ -1014,49 +1021,41 @@ __global__ void __launch_bounds__(kBlock) k_sub_vertex_values(const Counters* c,
 }
 
 struct SubCrossLoad {
-    const int* eowner;
+    const int* edn;   // D-level subdivision node owning the edge
     const int* ekind;
     const int* s_vtx;
     size_t dstride;
-    const int* groups;
-    const int* ng_ptr;
-    int depth;
     const float* vvalue;
-    int na;
     unsigned* err;
     __device__ unsigned operator()(int e) const {
-        const int dn = sub_node_to_dnode(eowner[e] - na, groups, *ng_ptr, depth);
+        const int dn = edn[e];
         const int kind = ekind[e];
-        const float a = ptr_value(vvalue, s_vtx[(size_t)c_tab.edge_vertex[kind][0] * dstride + dn], err);
-        const float b = ptr_value(vvalue, s_vtx[(size_t)c_tab.edge_vertex[kind][1] * dstride + dn], err);
+        const float a = ptr_value(vvalue, s_vtx[(size_t)__ldg(&g_tab.edge_vertex[kind][0]) * dstride + dn], err);
+        const float b = ptr_value(vvalue, s_vtx[(size_t)__ldg(&g_tab.edge_vertex[kind][1]) * dstride + dn], err);
         return (__fmul_rn(a, b) <= 0.0f) ? 1u : 0u;
     }
 };
 struct SubCrossStore {
-    const int* eowner;
+    const int* edn;
     const int* ekind;
     const int* s_vtx;
     size_t dstride;
-    const int* groups;
-    const int* ng_ptr;
-    int depth;
     const float* vvalue;
     const float *vx, *vy, *vz;
     unsigned* ecross;
     float* part_v;
     const int* voff_ptr;
     int cap;
-    int na;
     unsigned* err;
     __device__ void operator()(int e, unsigned pre, unsigned flag) const {
         ecross[e] = pre;
         if (!flag) return;
         const int at = *voff_ptr + (int)pre;
         if (at >= cap) { atomicOr(err, kErrCapacity); return; }
-        const int dn = sub_node_to_dnode(eowner[e] - na, groups, *ng_ptr, depth);
+        const int dn = edn[e];
         const int kind = ekind[e];
-        const int v1 = s_vtx[(size_t)c_tab.edge_vertex[kind][0] * dstride + dn] - 1;
-        const int v2 = s_vtx[(size_t)c_tab.edge_vertex[kind][1] * dstride + dn] - 1;
+        const int v1 = s_vtx[(size_t)__ldg(&g_tab.edge_vertex[kind][0]) * dstride + dn] - 1;
+        const int v2 = s_vtx[(size_t)__ldg(&g_tab.edge_vertex[kind][1]) * dstride + dn] - 1;
         if (v1 < 0 || v2 < 0) return;
         interp_point(vx[v1], vy[v1], vz[v1], vx[v2], vy[v2], vz[v2], kind >> 2, vvalue[v1], vvalue[v2],
                      &part_v[3 * (size_t)at]);
@@ -1075,7 +1074,7 @@ struct SubCubeLoad {
         for (int q = 0; q < 8; ++q)
             if (ptr_value(vvalue, s_vtx[(size_t)q * dstride + o], err) < 0.0f) cls |= 1 << q;
         cube_class[o] = cls;
-        return (unsigned)c_tab.mc_count[cls];
+        return (unsigned)__ldg(&g_tab.mc_count[cls]);
     }
 };
 
@@ -1097,7 +1096,7 @@ struct SubCubeStore {
         const int g = find_group(groups, *ng_ptr, 5, o);
         const unsigned base = group_cross0[g];
         const int cls = cube_class[o];
-        const unsigned long long tri = c_tab.mc_tri[cls];
+        const unsigned long long tri = __ldg(&g_tab.mc_tri[cls]);
         for (int t = 0; t < (int)cnt; ++t) {
             const int at = *toff_ptr + (int)pre + t;
             if (at >= cap) { atomicOr(err, kErrCapacity); continue; }
@@ -1327,11 +1326,11 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
                     &c->n_sub_dnodes, 0, ws.scan, total, err, s);
     if (e != cudaSuccess) return e;
     k_set_count<<<1, 1, 0, s>>>(&c->n_sub_vertices, total, 8 * ws.cap.sub_dnodes, err);
-    k_sub_vertex_maintain<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.s_neigh, sstride, ws.s_depth, ws.sv_owner,
+    k_sub_vertex_maintain<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.s_group, ws.s_neigh, sstride, ws.s_depth, ws.sv_owner,
                                                 ws.sv_kind, ws.s_vtx, dstride, na);
     k_sub_edge_owner<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.s_key, ws.s_neigh, sstride, ws.s_emask, na);
     e = launch_scan<2>(PopcLoad16{ws.s_emask},
-                    SubEdgeStore{ws.s_emask, mb.groups, &c->n_groups, D, ws.se_owner, ws.se_kind,
+                    SubEdgeStore{ws.s_emask, mb.groups, &c->n_groups, D, ws.se_owner, ws.se_kind, ws.se_dn,
                                  12 * ws.cap.sub_dnodes, na, err},
                     &c->n_sub_dnodes, 0, ws.scan, total, err, s);
     if (e != cudaSuccess) return e;
@@ -1340,16 +1339,15 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
     e = launch_scan(PopcLoad16{ws.s_emask}, StoreExclusive{mb.edge_of_dnode}, &c->n_sub_dnodes, 0, ws.scan, total,
                     err, s);
     if (e != cudaSuccess) return e;
-    k_sub_edge_maintain<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.s_neigh, sstride, ws.s_depth, ws.se_owner,
+    k_sub_edge_maintain<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.s_group, ws.s_neigh, sstride, ws.s_depth, ws.se_owner,
                                               ws.se_kind, ws.s_edge, dstride, na);
     k_sub_vertex_values<<<gs, kBlock, 0, s>>>(c, D, ws.sv_x, ws.sv_y, ws.sv_z, ws.sv_owner, ws.neigh, stride, ws.parent,
                                               ws.s_neigh, sstride, ws.s_parent, ws.s_root, ws.s_contrib, ws.s_depth,
                                               ws.s_cx, ws.s_cy, ws.s_cz, ws.enc, ws.xsol, ws.sv_value, na);
     // crossings: staged after the main part's vertices
-    e = launch_scan<2>(SubCrossLoad{ws.se_owner, ws.se_kind, ws.s_vtx, dstride, mb.groups, &c->n_groups, D, ws.sv_value, na, err},
-                    SubCrossStore{ws.se_owner, ws.se_kind, ws.s_vtx, dstride, mb.groups, &c->n_groups, D, ws.sv_value,
-                                  ws.sv_x, ws.sv_y, ws.sv_z, ws.se_cross, ws.part_v, &c->n_cross, ws.part_cap_v, na,
-                                  err},
+    e = launch_scan<2>(SubCrossLoad{ws.se_dn, ws.se_kind, ws.s_vtx, dstride, ws.sv_value, err},
+                    SubCrossStore{ws.se_dn, ws.se_kind, ws.s_vtx, dstride, ws.sv_value, ws.sv_x, ws.sv_y, ws.sv_z,
+                                  ws.se_cross, ws.part_v, &c->n_cross, ws.part_cap_v, err},
                     &c->n_sub_edges, 0, ws.scan, total, err, s);
     if (e != cudaSuccess) return e;
     k_set_count<<<1, 1, 0, s>>>(&c->n_sub_cross, total, ws.part_cap_v, err);

@@ -85,14 +85,43 @@ __device__ __forceinline__ void knn_merge(float (&ad)[4], int (&ai)[4], const fl
     knn_cswap(ad[2], ai[2], ad[3], ai[3]);
 }
 
+// butterfly merge of the lanes' sorted 4-lists: every lane ends with the warp's 4 nearest
+__device__ __forceinline__ void knn_warp_merge(const float (&bd)[4], const int (&bi)[4], float (&md)[4],
+                                               int (&mi)[4]) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) { md[q] = bd[q]; mi[q] = bi[q]; }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        float od[4];
+        int oi[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            od[q] = __shfl_xor_sync(0xffffffffu, md[q], o);
+            oi[q] = __shfl_xor_sync(0xffffffffu, mi[q], o);
+        }
+        knn_merge(md, mi, od, oi);
+    }
+}
+
+__device__ __forceinline__ void knn_visit(float qx, float qy, float qz, const float* px, const float* py,
+                                          const float* pz, int i, float (&bd)[4], int (&bi)[4]) {
+    const float dx = __fsub_rn(qx, px[i]), dy = __fsub_rn(qy, py[i]), dz = __fsub_rn(qz, pz[i]);
+    const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+    knn_insert(bd, bi, d2, i);
+}
+
+constexpr int kColourMaxShell = 12;   // widest block (2R+1 cells per axis) searched at one level
+
 // One warp per mesh vertex.  The samples are Morton-sorted, so the samples of a grid cell
 // at any level g <= gmax form one contiguous range, read from the level-gmax table at
-// cell codes shifted by 3 (gmax - g).  Starting at the finest level, the warp gathers the
-// samples of the 3x3x3 block of cells around the vertex's cell (the 27 ranges are
-// flattened over the lanes for balance), keeps the 4 nearest (private sorted lists merged
-// with butterfly shuffles) and stops when the 4th distance is below one cell width: every
-// sample outside the block is at least that far.  Otherwise it restarts one level
-// coarser, where the block covers the finer one.
+// cell codes shifted by 3 (gmax - g).  At the finest level the warp gathers the samples
+// of the 3x3x3 block of cells around the vertex's cell (the 27 ranges flattened over the
+// lanes) and keeps the 4 nearest (private sorted lists, butterfly merge).  Every sample
+// outside a block of radius R cells is at least R cell widths away, so:
+//   * 4 found and the 4th distance below 1 width: done;
+//   * 4 found otherwise: the 4th distance bounds the answer; the shell of cells between
+//     radius 2 and the radius R that exceeds it (one lane per cell) completes the search;
+//   * fewer than 4, or R too large: restart one level coarser.
 __global__ void __launch_bounds__(kBlock) k_colour(const Counters* c, int gmax, const float* mv, const float* px,
                                                    const float* py, const float* pz, const float* cr, const float* cg,
                                                    const float* cb, const int* cell_start, float* out) {
@@ -140,27 +169,31 @@ __global__ void __launch_bounds__(kBlock) k_colour(const Counters* c, int gmax, 
             int k = 0;
             for (int t = lane; t < total; t += 32) {
                 while (s_off[wib][k + 1] <= t) ++k;   // flattened index -> cell (increasing)
-                const int i = s_base[wib][k] + (t - s_off[wib][k]);
-                const float dx = __fsub_rn(qx, px[i]), dy = __fsub_rn(qy, py[i]), dz = __fsub_rn(qz, pz[i]);
-                const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-                knn_insert(bd, bi, d2, i);
+                knn_visit(qx, qy, qz, px, py, pz, s_base[wib][k] + (t - s_off[wib][k]), bd, bi);
             }
             __syncwarp();
-#pragma unroll
-            for (int q = 0; q < 4; ++q) { md[q] = bd[q]; mi[q] = bi[q]; }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                float od[4];
-                int oi[4];
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    od[q] = __shfl_xor_sync(0xffffffffu, md[q], o);
-                    oi[q] = __shfl_xor_sync(0xffffffffu, mi[q], o);
-                }
-                knn_merge(md, mi, od, oi);
+            knn_warp_merge(bd, bi, md, mi);
+            if (mi[3] == 0x7fffffff) continue;   // fewer than 4 samples in the block
+            const float w = 1.0f / (float)G;
+            if (md[3] < w * w) break;
+            int R = (int)(sqrtf(md[3]) * (float)G) + 1;
+            while (!(md[3] < __fmul_rn(R * w, R * w))) ++R;
+            if (R > kColourMaxShell && g > 0) continue;
+            // shell of cells with Chebyshev radius 2..R (lane-private lists continue)
+            const int side = 2 * R + 1;
+            const int ncell = side * side * side;
+            for (int t = lane; t < ncell; t += 32) {
+                const int ta = t / (side * side), tr = t - ta * side * side;
+                const int tb = tr / side, tz = tr - tb * side;
+                const int a = cx - R + ta, b = cy - R + tb, z = cz - R + tz;
+                if (a < 0 || a >= G || b < 0 || b >= G || z < 0 || z >= G) continue;
+                if (max(abs(a - cx), max(abs(b - cy), abs(z - cz))) <= 1) continue;
+                const unsigned m = morton3(a, b, z, g);
+                const int s0 = cell_start[(size_t)m << shift], s1 = cell_start[(size_t)(m + 1) << shift];
+                for (int i = s0; i < s1; ++i) knn_visit(qx, qy, qz, px, py, pz, i, bd, bi);
             }
-            const float lim = 1.0f / (float)G;
-            if (mi[3] != 0x7fffffff && md[3] < lim * lim) break;
+            knn_warp_merge(bd, bi, md, mi);
+            break;
         }
         if (lane == 0) {
             const float sum = md[0] + md[1] + md[2] + md[3];

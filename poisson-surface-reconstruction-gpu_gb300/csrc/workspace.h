@@ -130,6 +130,7 @@ struct Workspace {
     int *sv_owner, *sv_kind;
     float* sv_value;
     int *se_owner, *se_kind;
+    int* se_dn;             // D-level subdivision node owning each subdivision edge
     unsigned* se_cross;
     int* s_cube_class;
 
