@@ -28,33 +28,67 @@ __device__ __forceinline__ float bspline32(float t) {
     return 0.0f;
 }
 
+// One warp per D-level node: lane k < 27 holds neighbour k's sample range, a warp scan
+// flattens the (neighbour, sample) pairs over the lanes, every lane accumulates its
+// samples' weighted normals and a butterfly sum combines the lanes (fixed order).
 __global__ void __launch_bounds__(kBlock) k_vector_field(const Counters* c, int depth, const float* px, const float* py,
                                                          const float* pz, const float* nx, const float* ny,
                                                          const float* nz, const int* pidx, const int* pnum,
                                                          const float* cx, const float* cy, const float* cz,
                                                          const int* neigh, size_t stride, float* vx, float* vy,
                                                          float* vz) {
+    __shared__ int s_off[kBlock / 32][28];
+    __shared__ int s_base[kBlock / 32][27];
     const int md = c->level_count[depth];
     const int b = c->level_base[depth];
     const float s = (float)(1 << depth);
-    PSR_GRID_STRIDE(o, md) {
+    const int lane = lane_id();
+    const int wib = threadIdx.x >> 5;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int o = warp; o < md; o += nwarps) {
         const int i = b + o;
         const float ox = cx[i], oy = cy[i], oz = cz[i];
-        float ax = 0.f, ay = 0.f, az = 0.f;
-        for (int k = 0; k < 27; ++k) {
-            const int nb = neigh[(size_t)k * stride + i];
-            if (nb < 0) continue;
-            const int p0 = pidx[nb], pn = pnum[nb];
-            for (int p = p0; p < p0 + pn; ++p) {
-                float w = bspline32((px[p] - ox) * s) * bspline32((py[p] - oy) * s) * bspline32((pz[p] - oz) * s);
-                ax = fmaf(w, nx[p], ax);
-                ay = fmaf(w, ny[p], ay);
-                az = fmaf(w, nz[p], az);
-            }
+        int cnt = 0, base = 0;
+        if (lane < 27) {
+            const int nb = neigh[(size_t)lane * stride + i];
+            if (nb >= 0) { base = pidx[nb]; cnt = pnum[nb]; }
         }
-        vx[o] = ax;
-        vy[o] = ay;
-        vz[o] = az;
+        int incl = cnt;
+#pragma unroll
+        for (int q = 1; q < 32; q <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, q);
+            if (lane >= q) incl += y;
+        }
+        if (lane < 27) {
+            s_off[wib][lane] = incl - cnt;
+            s_base[wib][lane] = base;
+        }
+        if (lane == 26) s_off[wib][27] = incl;
+        const int total = __shfl_sync(0xffffffffu, incl, 26);
+        __syncwarp();
+        float ax = 0.f, ay = 0.f, az = 0.f;
+        int k = 0;
+        for (int t = lane; t < total; t += 32) {
+            while (s_off[wib][k + 1] <= t) ++k;
+            const int p = s_base[wib][k] + (t - s_off[wib][k]);
+            const float w = bspline32((px[p] - ox) * s) * bspline32((py[p] - oy) * s) * bspline32((pz[p] - oz) * s);
+            ax = fmaf(w, nx[p], ax);
+            ay = fmaf(w, ny[p], ay);
+            az = fmaf(w, nz[p], az);
+        }
+#pragma unroll
+        for (int q = 16; q > 0; q >>= 1) {
+            ax += __shfl_xor_sync(0xffffffffu, ax, q);
+            ay += __shfl_xor_sync(0xffffffffu, ay, q);
+            az += __shfl_xor_sync(0xffffffffu, az, q);
+        }
+        if (lane == 0) {
+            vx[o] = ax;
+            vy[o] = ay;
+            vz[o] = az;
+        }
+        __syncwarp();
     }
 }
 
@@ -232,7 +266,7 @@ cudaError_t field_build(Workspace& ws) {
     float* vx = ws.vfield;
     float* vy = ws.vfield + ws.cap.dnodes;
     float* vz = ws.vfield + 2 * (size_t)ws.cap.dnodes;
-    k_vector_field<<<grid_for(ws, ws.cap.dnodes), kBlock, 0, s>>>(c, D, ws.px, ws.py, ws.pz, ws.nx, ws.ny, ws.nz,
+    k_vector_field<<<ws.num_sms * 8, kBlock, 0, s>>>(c, D, ws.px, ws.py, ws.pz, ws.nx, ws.ny, ws.nz,
                                                                     ws.pidx, ws.pnum, ws.ctr_x, ws.ctr_y, ws.ctr_z,
                                                                     ws.neigh, stride, vx, vy, vz);
     const int dsplit = D >= 2 ? D - 2 : 0;

@@ -194,14 +194,6 @@ struct VertexStore {
     }
 };
 
-__global__ void k_set_count(int* dst, const unsigned* total, int cap, unsigned* err) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        int n = (int)*total;
-        if (n > cap) { atomicOr(err, kErrCapacity); n = cap; }
-        *dst = n;
-    }
-}
-
 // maintainVertexNodePointer (mesh/BuildMeshGeometry.cu:108-147)
 __global__ void __launch_bounds__(kBlock) k_vertex_maintain(const Counters* c, const int* neigh, size_t stride,
                                                             const int* vowner, const int* vkind, int* node_vtx) {
@@ -752,13 +744,43 @@ __global__ void __launch_bounds__(kBlock) k_sub_neighbours(const Counters* c, in
         }
         const int g = lo;
         const int* G = groups + (size_t)g * kGroupRec;
-        const int s = G[3] + sub_level_off(G[0], G[2], d) + (t - (G[5] >> sh));
+        const int local = t - (G[5] >> sh);
+        const int s = G[3] + sub_level_off(G[0], G[2], d) + local;
         const bool at_root_depth = (d == G[0]);
         int contrib = 0;
         const int son = (s_key[s] >> (3 * (depth - d))) & 7;
         const int pa = s_parent[s];
+        // Position inside the root's cell: rel = the Morton code of the node's L = d - rd
+        // levels below its root (x = bit 2, y = bit 1, z = bit 0 of every triple).  A
+        // neighbour inside the same root's cell is the node at the shifted code in the same
+        // root's block (dilated-integer +-1 per axis); only neighbours outside the root's
+        // cell need the parent-based look-up.
+        const unsigned lmask = (1u << (3 * (d - G[0]))) - 1u;
+        const unsigned rel = (unsigned)local & lmask;
+        unsigned cmp[3][3];
+        bool ok[3][3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const unsigned M = (0x24924924u >> a) & lmask;   // x, y, z bit positions
+            const unsigned u = 4u >> a;
+            const unsigned cm = rel & M;
+            cmp[a][0] = (cm - u) & M;
+            cmp[a][1] = cm;
+            cmp[a][2] = ((cm | ~M) + u) & M;
+            ok[a][0] = cm != 0u;
+            ok[a][1] = true;
+            ok[a][2] = cm != M;
+        }
 #pragma unroll
         for (int k = 0; k < 27; ++k) {
+            const int ix = k / 9, iy = (k / 3) % 3, iz = k % 3;
+            if (ok[0][ix] && ok[1][iy] && ok[2][iz]) {
+                const unsigned relk = cmp[0][ix] | cmp[1][iy] | cmp[2][iz];
+                const int v = na + s + (int)relk - (int)rel;
+                s_neigh[(size_t)k * sstride + s] = v;
+                if (at_root_depth) contrib = 1;   // the node itself, a root
+                continue;
+            }
             int lp, lc;
             nb_lut(son, k, lp, lc);
             const int np = (pa < na) ? neigh[(size_t)lp * stride + pa] : s_neigh[(size_t)lp * sstride + (pa - na)];
@@ -1233,26 +1255,23 @@ cudaError_t mesh_build_impl(Workspace& ws, const MeshBufs& mb) {
     e = launch_scan<1>(PopcLoad8{ws.vmask},
                     VertexStore{ws.vmask, ws.ndepth, ws.ctr_x, ws.ctr_y, ws.ctr_z, ws.v_x, ws.v_y, ws.v_z, ws.v_owner,
                                 ws.v_kind, ws.v_depth, ws.cap.vertices, err},
-                    &c->n_nodes, 0, ws.scan, total, err, s);
+                    &c->n_nodes, 0, ws.scan, total, err, s, ScanCount{&c->n_vertices, ws.cap.vertices});
     if (e != cudaSuccess) return e;
-    k_set_count<<<1, 1, 0, s>>>(&c->n_vertices, total, ws.cap.vertices, err);
     k_vertex_maintain<<<gm, kBlock, 0, s>>>(c, ws.neigh, stride, ws.v_owner, ws.v_kind, ws.node_vtx);
     // edges (D level)
     k_edge_owner<<<gm, kBlock, 0, s>>>(c, D, ws.key, ws.neigh, stride, ws.emask16);
     e = launch_scan<1>(PopcLoad16{ws.emask16},
                     EdgeStore{ws.emask16, &c->level_base[D], ws.e_owner, ws.e_kind, ws.cap.edges, err},
-                    &c->level_count[D], 0, ws.scan, total, err, s);
+                    &c->level_count[D], 0, ws.scan, total, err, s, ScanCount{&c->n_edges, ws.cap.edges});
     if (e != cudaSuccess) return e;
-    k_set_count<<<1, 1, 0, s>>>(&c->n_edges, total, ws.cap.edges, err);
     k_edge_maintain<<<gm, kBlock, 0, s>>>(c, ws.neigh, stride, ws.e_owner, ws.e_kind, ws.node_edge);
     // faces
     k_face_owner<<<gm, kBlock, 0, s>>>(c, ws.key, ws.neigh, stride, ws.fmask);
     e = launch_scan<1>(PopcLoad8{ws.fmask},
                     FaceStore{ws.fmask, ws.key, ws.ndepth, ws.parent, D, ws.f_owner, ws.f_kind, ws.f_hasparent,
                               ws.cap.faces, err},
-                    &c->n_nodes, 0, ws.scan, total, err, s);
+                    &c->n_nodes, 0, ws.scan, total, err, s, ScanCount{&c->n_faces, ws.cap.faces});
     if (e != cudaSuccess) return e;
-    k_set_count<<<1, 1, 0, s>>>(&c->n_faces, total, ws.cap.faces, err);
     k_face_maintain<<<gm, kBlock, 0, s>>>(c, ws.neigh, stride, ws.f_owner, ws.f_kind, ws.node_face);
     // implicit values
     k_vertex_values<<<gm, kBlock, 0, s>>>(c, D, ws.v_x, ws.v_y, ws.v_z, ws.v_owner, ws.v_kind, ws.v_depth, ws.neigh,
@@ -1261,22 +1280,19 @@ cudaError_t mesh_build_impl(Workspace& ws, const MeshBufs& mb) {
     e = launch_scan<1>(CrossLoad{ws.e_owner, ws.e_kind, ws.node_vtx, stride, ws.vvalue, err},
                     CrossStore{ws.e_owner, ws.e_kind, ws.node_vtx, stride, ws.vvalue, ws.v_x, ws.v_y, ws.v_z,
                                ws.e_cross, ws.part_v, 0, ws.part_cap_v, err},
-                    &c->n_edges, 0, ws.scan, total, err, s);
+                    &c->n_edges, 0, ws.scan, total, err, s, ScanCount{&c->n_cross, ws.part_cap_v});
     if (e != cudaSuccess) return e;
-    k_set_count<<<1, 1, 0, s>>>(&c->n_cross, total, ws.part_cap_v, err);
     // face hits must start cleared
     cudaMemsetAsync(ws.face_hit, 0, sizeof(int) * (size_t)ws.cap.faces, s);
     e = launch_scan<1>(CubeLoad{ws.node_vtx, stride, &c->level_base[D], ws.vvalue, ws.cube_class, err},
                     CubeStore{ws.cube_class, &c->level_base[D], ws.node_edge, ws.node_face, stride, ws.e_cross,
                               ws.parent, ws.f_hasparent, ws.face_hit, ws.part_t, 0, ws.part_cap_t, err},
-                    &c->level_count[D], 0, ws.scan, total, err, s);
+                    &c->level_count[D], 0, ws.scan, total, err, s, ScanCount{&c->n_tri, ws.part_cap_t});
     if (e != cudaSuccess) return e;
-    k_set_count<<<1, 1, 0, s>>>(&c->n_tri, total, ws.part_cap_t, err);
     // subdivision roots among nodes of depth < D
     e = launch_scan<1>(RootLoad{ws.node_vtx, ws.node_face, stride, ws.vvalue, ws.face_hit, ws.first_child, err},
-                    RootStore{ws.sub_root, ws.cap.nodes, err}, &c->level_base[D], 0, ws.scan, total, err, s);
+                    RootStore{ws.sub_root, ws.cap.nodes, err}, &c->level_base[D], 0, ws.scan, total, err, s, ScanCount{&c->n_subroots, ws.cap.nodes});
     if (e != cudaSuccess) return e;
-    k_set_count<<<1, 1, 0, s>>>(&c->n_subroots, total, ws.cap.nodes, err);
     // subdivision groups
     e = launch_scan(GroupFlagLoad{ws.sub_root, ws.ndepth, D - 4},
                     GroupFlagStore{ws.root_group, mb.groups, mb.max_groups, err}, &c->n_subroots, 0, ws.scan,
@@ -1323,18 +1339,16 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
     e = launch_scan<2>(PopcLoad8{ws.s_vmask},
                     SubVertexStore{ws.s_vmask, mb.groups, &c->n_groups, D, ws.s_cx, ws.s_cy, ws.s_cz, ws.sv_x, ws.sv_y,
                                    ws.sv_z, ws.sv_owner, ws.sv_kind, 8 * ws.cap.sub_dnodes, na, err},
-                    &c->n_sub_dnodes, 0, ws.scan, total, err, s);
+                    &c->n_sub_dnodes, 0, ws.scan, total, err, s, ScanCount{&c->n_sub_vertices, 8 * ws.cap.sub_dnodes});
     if (e != cudaSuccess) return e;
-    k_set_count<<<1, 1, 0, s>>>(&c->n_sub_vertices, total, 8 * ws.cap.sub_dnodes, err);
     k_sub_vertex_maintain<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.s_group, ws.s_neigh, sstride, ws.s_depth, ws.sv_owner,
                                                 ws.sv_kind, ws.s_vtx, dstride, na);
     k_sub_edge_owner<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.s_key, ws.s_neigh, sstride, ws.s_emask, na);
     e = launch_scan<2>(PopcLoad16{ws.s_emask},
                     SubEdgeStore{ws.s_emask, mb.groups, &c->n_groups, D, ws.se_owner, ws.se_kind, ws.se_dn,
                                  12 * ws.cap.sub_dnodes, na, err},
-                    &c->n_sub_dnodes, 0, ws.scan, total, err, s);
+                    &c->n_sub_dnodes, 0, ws.scan, total, err, s, ScanCount{&c->n_sub_edges, 12 * ws.cap.sub_dnodes});
     if (e != cudaSuccess) return e;
-    k_set_count<<<1, 1, 0, s>>>(&c->n_sub_edges, total, 12 * ws.cap.sub_dnodes, err);
     // edge prefix per D-level sub node (for the part table): recompute via a scan of popcounts
     e = launch_scan(PopcLoad16{ws.s_emask}, StoreExclusive{mb.edge_of_dnode}, &c->n_sub_dnodes, 0, ws.scan, total,
                     err, s);
@@ -1348,14 +1362,12 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
     e = launch_scan<2>(SubCrossLoad{ws.se_dn, ws.se_kind, ws.s_vtx, dstride, ws.sv_value, err},
                     SubCrossStore{ws.se_dn, ws.se_kind, ws.s_vtx, dstride, ws.sv_value, ws.sv_x, ws.sv_y, ws.sv_z,
                                   ws.se_cross, ws.part_v, &c->n_cross, ws.part_cap_v, err},
-                    &c->n_sub_edges, 0, ws.scan, total, err, s);
+                    &c->n_sub_edges, 0, ws.scan, total, err, s, ScanCount{&c->n_sub_cross, ws.part_cap_v});
     if (e != cudaSuccess) return e;
-    k_set_count<<<1, 1, 0, s>>>(&c->n_sub_cross, total, ws.part_cap_v, err);
     // triangle prefix per D-level sub node
     e = launch_scan<2>(SubCubeLoad{ws.s_vtx, dstride, ws.sv_value, ws.s_cube_class, err}, StoreExclusive{mb.tri_of_dnode},
-                    &c->n_sub_dnodes, 0, ws.scan, total, err, s);
+                    &c->n_sub_dnodes, 0, ws.scan, total, err, s, ScanCount{&c->n_sub_tri, ws.part_cap_t});
     if (e != cudaSuccess) return e;
-    k_set_count<<<1, 1, 0, s>>>(&c->n_sub_tri, total, ws.part_cap_t, err);
     k_part_table<<<1, 1, 0, s>>>(c, mb.groups, mb.edge_of_dnode, ws.se_cross, mb.tri_of_dnode,
                                  mb.group_cross0, mb.parts);
     e = launch_scan<2>(SubCubeLoad{ws.s_vtx, dstride, ws.sv_value, ws.s_cube_class, err},
@@ -1369,15 +1381,13 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
     int* n_staged_t = mb.misc + 2;
     k_count_parts<<<1, 1, 0, s>>>(c, n_parts, n_staged_v, n_staged_t, ws.part_cap_v, ws.part_cap_t);
     e = launch_scan(KeepVertexLoad{ws.part_v}, KeepVertexStore{ws.part_v, ws.mesh_v, mb.kept_prefix, ws.cap.mesh_vertices, err},
-                    n_staged_v, 0, ws.scan, total, err, s);
+                    n_staged_v, 0, ws.scan, total, err, s, ScanCount{&c->n_mesh_vertices, ws.cap.mesh_vertices});
     if (e != cudaSuccess) return e;
-    k_set_count<<<1, 1, 0, s>>>(&c->n_mesh_vertices, total, ws.cap.mesh_vertices, err);
     e = launch_scan(KeepTriLoad{ws.part_t, mb.parts, n_parts},
                     KeepTriStore{ws.part_t, mb.parts, n_parts, mb.kept_prefix, n_staged_v, &c->n_mesh_vertices,
                                  ws.mesh_t, ws.cap.mesh_tris, err},
-                    n_staged_t, 0, ws.scan, total, err, s);
+                    n_staged_t, 0, ws.scan, total, err, s, ScanCount{&c->n_mesh_triangles, ws.cap.mesh_tris});
     if (e != cudaSuccess) return e;
-    k_set_count<<<1, 1, 0, s>>>(&c->n_mesh_triangles, total, ws.cap.mesh_tris, err);
     return cudaGetLastError();
 }
 

@@ -21,6 +21,12 @@ struct ScanScratch {
 };
 constexpr int kScanHeader = 3;
 
+// optional count written by the last tile: min(total, cap) (overflow flags kErrCapacity)
+struct ScanCount {
+    int* dst = nullptr;
+    int cap = 0;
+};
+
 constexpr unsigned long long kFlagAgg = 1ull << 32;
 constexpr unsigned long long kFlagIncl = 1ull << 33;
 constexpr int kEpochShift = 34;
@@ -64,7 +70,7 @@ __device__ __forceinline__ unsigned block_exclusive_scan(unsigned v, unsigned& e
 // element that more, smaller tiles (more blocks in flight) pay.
 template <int kItems, class Load, class Store>
 __global__ void __launch_bounds__(kBlock) k_scan(Load load, Store store, const int* count_ptr, int count_add,
-                                                 ScanScratch sc, unsigned* total, unsigned* err) {
+                                                 ScanScratch sc, unsigned* total, unsigned* err, ScanCount cnt) {
     constexpr int kTile = kBlock * kItems;
     __shared__ unsigned s_warp[kBlock / 32 + 1];
     __shared__ int s_tile;
@@ -72,7 +78,10 @@ __global__ void __launch_bounds__(kBlock) k_scan(Load load, Store store, const i
     const int n = *count_ptr + count_add;
     const int ntiles = (n + kTile - 1) / kTile;
     if (n <= 0) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) *total = 0u;
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            *total = 0u;
+            if (cnt.dst) *cnt.dst = 0;
+        }
         return;
     }
     if (ntiles > sc.max_tiles) {
@@ -154,7 +163,15 @@ __global__ void __launch_bounds__(kBlock) k_scan(Load load, Store store, const i
             if (i < n) store(i, pre, v[k]);
             pre += v[k];
         }
-        if (t == ntiles - 1 && threadIdx.x == kBlock - 1) *total = s_prefix + agg;
+        if (t == ntiles - 1 && threadIdx.x == kBlock - 1) {
+            const unsigned tot = s_prefix + agg;
+            *total = tot;
+            if (cnt.dst) {
+                int c = (int)tot;
+                if (tot > (unsigned)cnt.cap) { atomicOr(err, kErrCapacity); c = cnt.cap; }
+                *cnt.dst = c;
+            }
+        }
         __syncthreads();
     }
     // every block ends here after claiming a tile past the end, i.e. after its last tile;
@@ -173,9 +190,9 @@ int scan_grid(int max_tiles);
 
 template <int kItems = kScanItems, class Load, class Store>
 inline cudaError_t launch_scan(Load load, Store store, const int* count_ptr, int count_add, ScanScratch sc,
-                               unsigned* total, unsigned* err, cudaStream_t stream) {
+                               unsigned* total, unsigned* err, cudaStream_t stream, ScanCount cnt = ScanCount{}) {
     k_scan<kItems, Load, Store><<<scan_grid(sc.max_tiles), kBlock, 0, stream>>>(load, store, count_ptr, count_add, sc,
-                                                                                total, err);
+                                                                                total, err, cnt);
     return cudaGetLastError();
 }
 

@@ -185,13 +185,25 @@ __device__ __forceinline__ void cgc_resident(cg::cluster_group& cl, CgcShared& s
     while (active && it <= a.max_iter) {
         // (A) own p_k, A p_k from the neighbours' (r_k, p_{k-1}), p.Ap
         acc = ff_zero();
+        // the block-table entries of the warp's next slot are loaded while the current
+        // slot is processed (they do not change between iterations)
+        int4 q0 = make_int4(-1, -1, -1, -1), q1 = q0;
+        if (warp < nslot && warp * 32 + lane < nloc) {
+            const int4* bp = reinterpret_cast<const int4*>(a.blk + (size_t)(gbase + ((warp * 32 + lane) >> 3)) * 64 + sib * 8);
+            q0 = __ldg(bp);
+            q1 = __ldg(bp + 1);
+        }
         for (int sl = warp; sl < nslot; sl += kCgWarps) {
             const int l = sl * 32 + lane;
             const bool mine = l < nloc;   // whole groups: a group is all in or all out
+            const int ids[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
+            const int ln = l + kCgWarps * 32;
+            if (ln < nloc) {
+                const int4* bp = reinterpret_cast<const int4*>(a.blk + (size_t)(gbase + (ln >> 3)) * 64 + sib * 8);
+                q0 = __ldg(bp);
+                q1 = __ldg(bp + 1);
+            }
             if (mine) {
-                const int4* bp = reinterpret_cast<const int4*>(a.blk + (size_t)(gbase + (l >> 3)) * 64 + sib * 8);
-                const int4 q0 = __ldg(bp), q1 = __ldg(bp + 1);
-                const int ids[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
 #pragma unroll
                 for (int e = 0; e < 8; ++e) {
                     const int nb = ids[e];
