@@ -257,18 +257,30 @@ def main():
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize(dev)
-    # served slots: distinct seeded clouds of the same workload
-    slots = []
+    # served slots: distinct seeded clouds of the same workload, staged on the device
+    # (value) and in pinned host memory (e2e)
+    from serve import Server
+    dclouds, hclouds = [], []
     for k in range(args.slots):
         cx, cn, cc, _ = syn.workload(args.workload, cloud=rank * args.slots + k) if k else (xyz, nrm, rgb, depth)
-        slots.append(Slot(psr, torch, dev, cx, cn, cc, depth, local))
-    served_leg(slots, 2, False, torch, dev)
-    served_leg(slots, 2, True, torch, dev)
+        dclouds.append((torch.from_numpy(cx).to(dev), torch.from_numpy(cn).to(dev),
+                        torch.from_numpy(cc).to(dev) if cc is not None else None, depth))
+        hclouds.append((torch.from_numpy(cx).pin_memory(), torch.from_numpy(cn).pin_memory(),
+                        torch.from_numpy(cc).pin_memory() if cc is not None else None, depth))
+    caps = dict(max_depth=depth, max_points=max(300000, n), max_triangles=1000000, max_mesh_vertices=300000,
+                compute_colors=rgb is not None, compute_normals=True, device=local)
+    server = Server(slots=args.slots, **caps)
+    server_h = Server(slots=args.slots, host_outputs=True, **caps)
+    served_leg(server, dclouds, 2, torch, dev)
+    served_leg(server_h, hclouds, 2, torch, dev)
     with ClockSampler(local) as clk:
         t_dev, m_dev = timed(step_device, args.steps)
         t_e2e, m_host = timed(step_host, args.steps)
-        s_dev, s_lat, s_stages = served_leg(slots, args.steps, False, torch, dev)
-        s_e2e, s_lat_e2e, _ = served_leg(slots, args.steps, True, torch, dev)
+        s_dev, s_lat, s_stages = served_leg(server, dclouds, args.steps, torch, dev)
+        s_e2e, s_lat_e2e, _ = served_leg(server_h, hclouds, args.steps, torch, dev)
+        # open loop at 70% of the measured served throughput: arrival-to-completion latency
+        rate = 0.7 * args.slots * args.steps / (float(s_dev) / 1000.0)
+        ol_lat = open_loop_leg(server, dclouds, args.slots * args.steps, rate)
     torch.cuda.synchronize(dev)
     if world > 1:
         dist.barrier()
@@ -324,11 +336,14 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 dots / reductions)", "data": "synthetic",
             "impl": "gpu",
             "config": {"workload": f"{args.workload} (N={n}, depth {depth}, colour, normals)",
-                       "path": f"served: {K} concurrent slots (handle + stream + CUDA graph + host thread "
-                               f"each) issuing back-to-back reconstructions; a step = one cloud per slot",
+                       "path": f"served: Server with {K} slots (handle + stream + CUDA graphs each), one host "
+                               f"thread, psr_submit / psr_poll continuous batching; a step = one cloud per slot",
                        "l2": f"working set of {K} concurrent reconstructions exceeds L2; plain leg flushes 256 MiB "
                              f"between steps"},
-            "p50_ms": float(np.median(s_lat)), "p99_ms": float(np.percentile(s_lat, 99)),
+            "p50_ms": float(np.median(ol_lat)), "p99_ms": float(np.percentile(ol_lat, 99)),
+            "latency": {"kind": "open-loop Poisson arrivals at 70% of the served throughput, arrival to completion",
+                        "rate_per_s": round(rate, 1), "requests": int(ol_lat.size),
+                        "service_p50_ms": float(np.median(s_lat)), "service_p99_ms": float(np.percentile(s_lat, 99))},
             "plain": {"value": plain_value, "unit": UNIT, "ms_per_step": tot_dev / args.steps,
                       "p50_ms": float(np.median(t_dev)), "p99_ms": float(np.percentile(t_dev, 99)),
                       "e2e_value": plain_e2e},
@@ -338,7 +353,7 @@ def main():
             "stage_ms": [round(x, 4) for x in st.stage_ms], "served_stage_ms": s_stages,
             "cg_depth_ms": [round(x, 4) for x in st.cg_depth_ms[:depth + 1]], "nodes": M, "cg_iterations": list(st.cg_iterations[:depth + 1]),
             "mesh": {"vertices": m_host.vertex_count, "triangles": m_host.triangle_count},
-            "gpu_launches": int(st_launches(r)) * K,
+            "gpu_launches": (int(st_launches(r)) + 1) * K,   # graph kernels + the output copy kernel
             "roofline": roofline, "clocks": clocks}
     if not args.no_cpu_baseline:
         try:
@@ -350,89 +365,50 @@ def main():
         dist.destroy_process_group()
 
 
-class Slot:
-    """One served slot: its own handle, CUDA stream, device inputs and outputs."""
-
-    def __init__(self, psr, torch, dev, xyz, nrm, rgb, depth, local, vcap=300000, tcap=1000000):
-        import ctypes
-        self.ctypes = ctypes
-        self.psr = psr
-        self.n = len(xyz)
-        self.depth = depth
-        self.r = psr.PoissonReconstruction(max_depth=depth, max_points=max(300000, self.n), compute_colors=rgb is not None,
-                                           compute_normals=True, device=local)
-        self.stream = torch.cuda.Stream(dev)
-        self.sptr = self.stream.cuda_stream
-        self.d_xyz = torch.from_numpy(xyz).to(dev)
-        self.d_nrm = torch.from_numpy(nrm).to(dev)
-        self.d_rgb = torch.from_numpy(rgb).to(dev) if rgb is not None else None
-        self.o = [torch.empty((vcap, 3), dtype=torch.float32, device=dev),
-                  torch.empty((tcap, 3), dtype=torch.int32, device=dev),
-                  torch.empty((vcap, 3), dtype=torch.float32, device=dev),
-                  torch.empty((vcap, 3), dtype=torch.float32, device=dev)]
-        self.h = [torch.from_numpy(xyz).pin_memory(), torch.from_numpy(nrm).pin_memory(),
-                  torch.from_numpy(rgb).pin_memory() if rgb is not None else None,
-                  torch.empty((vcap, 3), dtype=torch.float32).pin_memory(),
-                  torch.empty((tcap, 3), dtype=torch.int32).pin_memory(),
-                  torch.empty((vcap, 3), dtype=torch.float32).pin_memory(),
-                  torch.empty((vcap, 3), dtype=torch.float32).pin_memory()]
-        self.vcap, self.tcap = vcap, tcap
-
-    def run(self, host):
-        psr = self.psr
-        if host:
-            h = self.h
-            pts = psr.PsrPoints(h[0].data_ptr(), h[1].data_ptr(), h[2].data_ptr() if h[2] is not None else None, self.n,
-                                psr.PSR_HOST)
-            m = psr.PsrMesh(h[3].data_ptr(), h[4].data_ptr(), h[5].data_ptr() if h[2] is not None else None,
-                            h[6].data_ptr(), self.vcap, self.tcap, psr.PSR_HOST, 0, 0)
-        else:
-            o = self.o
-            pts = psr.PsrPoints(self.d_xyz.data_ptr(), self.d_nrm.data_ptr(),
-                                self.d_rgb.data_ptr() if self.d_rgb is not None else None, self.n, psr.PSR_DEVICE)
-            m = psr.PsrMesh(o[0].data_ptr(), o[1].data_ptr(), o[2].data_ptr() if self.d_rgb is not None else None,
-                            o[3].data_ptr(), self.vcap, self.tcap, psr.PSR_DEVICE, 0, 0)
-        opt = psr.PsrOptions(self.depth, 0)
-        c = self.ctypes
-        st = self.r._lib.psr_reconstruct(self.r._h, c.byref(pts), c.byref(opt), c.byref(m), self.sptr)
-        if st != 0:
-            raise self.r._error(st, "psr_reconstruct")
-        return m
+def open_loop_leg(server, clouds, n_req, rate, seed=7):
+    """Open-loop serving: n_req requests (cycling over the staged clouds) arriving as a
+    Poisson process at `rate` per second; latency = arrival to completion (queueing
+    included)."""
+    from serve import Request
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_req))
+    K = len(clouds)
+    reqs = [Request(xyz=clouds[i % K][0], normals=clouds[i % K][1], rgb=clouds[i % K][2], depth=clouds[i % K][3])
+            for i in range(n_req)]
+    done = server.run(reqs, arrivals=list(arrivals))
+    errs = [r.error for r in done if r.error]
+    if errs:
+        raise RuntimeError(f"open-loop leg: {errs[0]}")
+    return np.array([r.latency_ms for r in done])
 
 
-def served_leg(slots, steps, host, torch, dev):
-    """Continuous serving: every slot's host thread issues `steps` reconstructions back to
-    back on its own stream, all slots concurrently.  Device time = CUDA events from a common
-    start (the slot streams wait on it) to the last slot's final completion; per-call
-    latency = host wall time of each blocking call."""
-    import threading
-    K = len(slots)
+def served_leg(server, clouds, steps, torch, dev):
+    """Continuous serving through the Server (psr_submit / psr_poll from one host thread):
+    steps x K requests cycling over the K staged clouds, all arriving at once.  Device
+    time = CUDA events from a common start (every slot stream waits on it) to the last
+    slot's final completion; per-request latency = host time from arrival to completion."""
+    from serve import Request, latency_summary
+    K = len(server.slots)
+    reqs = [Request(xyz=c[0], normals=c[1], rgb=c[2], depth=c[3]) for _ in range(steps) for c in clouds[:K]]
     torch.cuda.synchronize(dev)
     start = torch.cuda.Event(enable_timing=True)
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
     start.record(torch.cuda.default_stream(dev))
-    for sl in slots:
+    for sl in server.slots:
         sl.stream.wait_event(start)
-    lat = [[] for _ in range(K)]
-    gate = threading.Barrier(K)
-
-    def work(k):
-        gate.wait()
-        for _ in range(steps):
-            t0 = time.perf_counter()
-            slots[k].run(host)
-            lat[k].append(1000.0 * (time.perf_counter() - t0))
-        ends[k].record(slots[k].stream)
-
-    th = [threading.Thread(target=work, args=(k,)) for k in range(K)]
-    for t in th:
-        t.start()
-    for t in th:
-        t.join()
+    done = server.run(reqs)
+    ends = []
+    for sl in server.slots:
+        e = torch.cuda.Event(enable_timing=True)
+        e.record(sl.stream)
+        ends.append(e)
     torch.cuda.synchronize(dev)
+    errs = [r.error for r in done if r.error]
+    if errs:
+        raise RuntimeError(f"served leg: {errs[0]}")
     total_ms = max(start.elapsed_time(e) for e in ends)
-    stages = np.mean([list(sl.r.stats().stage_ms) for sl in slots], axis=0)
-    return total_ms, np.array([x for l in lat for x in l]), [round(float(x), 4) for x in stages]
+    lat = np.array([1000.0 * (r.finished - r.admitted) for r in done])   # service time (no queueing)
+    stages = np.mean([list(sl.recon.stats().stage_ms) for sl in server.slots], axis=0)
+    return total_ms, lat, [round(float(x), 4) for x in stages]
 
 
 def st_launches(r):

@@ -28,7 +28,8 @@ typedef enum psr_status {
     PSR_INVALID_INPUT = 2,   /* bad argument, empty cloud, non-finite coordinate */
     PSR_NONCONVERGED = 3,    /* CG hit its iteration limit above tolerance (informational) */
     PSR_DEVICE_TIMEOUT = 4,  /* a bounded device-side wait gave up */
-    PSR_CUDA_ERROR = 5       /* CUDA runtime error (message via psr_last_error) */
+    PSR_CUDA_ERROR = 5,      /* CUDA runtime error (message via psr_last_error) */
+    PSR_PENDING = 6          /* psr_poll: the submitted reconstruction is still running */
 } psr_status;
 
 typedef enum psr_location { PSR_HOST = 0, PSR_DEVICE = 1 } psr_location;
@@ -117,6 +118,24 @@ psr_status psr_destroy(psr_handle* h);
  * returns once the mesh counts are known and the mesh has been written. */
 psr_status psr_reconstruct(psr_handle* h, const psr_points* points, const psr_options* options,
                            psr_mesh* mesh, void* stream);
+
+/* Served form (no counterpart in the reference, which blocks): psr_submit enqueues the
+ * same work as psr_reconstruct on `stream` and returns without waiting; one
+ * reconstruction per handle is in flight at a time.  `points` may be released once the
+ * work has run (device inputs are read by the GPU, host inputs are copied from the host
+ * asynchronously: keep them alive and pinned until completion); `mesh` must stay valid
+ * until completion.  Device-resident outputs are written by the GPU; host outputs are
+ * copied when the completion is collected.  psr_poll returns PSR_PENDING while the GPU
+ * is still working, else collects the result (counts, stats, status) exactly like
+ * psr_reconstruct would have; psr_wait blocks until then.  Many handles, each with its
+ * own stream, give concurrent reconstructions driven from one host thread. */
+psr_status psr_submit(psr_handle* h, const psr_points* points, const psr_options* options, psr_mesh* mesh,
+                      void* stream);
+psr_status psr_poll(psr_handle* h);
+psr_status psr_wait(psr_handle* h);
+
+/* Device memory held by the handle (bytes), for admission under a memory budget. */
+psr_status psr_memory_bytes(const psr_handle* h, size_t* bytes);
 
 psr_status psr_get_stats(const psr_handle* h, psr_stats* out);
 

@@ -53,6 +53,12 @@ struct psr_handle {
     bool have_result = false;
     std::string last_error;
     psr_stats stats;
+    // the reconstruction in flight (psr_submit ... psr_poll / psr_wait)
+    cudaEvent_t done = nullptr;
+    bool pending = false;
+    psr_mesh* pend_mesh = nullptr;
+    int pend_depth = 0, pend_colour = 0, pend_normals = 0;
+    cudaStream_t pend_stream = nullptr;
 };
 
 namespace {
@@ -114,6 +120,7 @@ const char* psr_status_string(psr_status s) {
         case PSR_NONCONVERGED: return "not converged";
         case PSR_DEVICE_TIMEOUT: return "device timeout";
         case PSR_CUDA_ERROR: return "cuda error";
+        case PSR_PENDING: return "pending";
     }
     return "unknown";
 }
@@ -276,6 +283,7 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ws.aux, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ws.ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ws.ev_join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->done, cudaEventDisableTiming);
     // tables
     if (e == cudaSuccess) e = upload_tables_octree();
     if (e == cudaSuccess) e = upload_tables_field();
@@ -308,6 +316,7 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
 
 psr_status psr_destroy(psr_handle* h) {
     if (!h) return PSR_OK;
+    if (h->pending && h->done) cudaEventSynchronize(h->done);   // no buffer is freed under running work
     for (auto& g : h->graphs) if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
     if (h->arena) cudaFree(h->arena);
     if (h->ws.cnt_host) cudaFreeHost(h->ws.cnt_host);
@@ -316,14 +325,34 @@ psr_status psr_destroy(psr_handle* h) {
     if (h->ws.ev_fork) cudaEventDestroy(h->ws.ev_fork);
     if (h->ws.ev_join) cudaEventDestroy(h->ws.ev_join);
     if (h->ws.aux) cudaStreamDestroy(h->ws.aux);
+    if (h->done) cudaEventDestroy(h->done);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
     return PSR_OK;
 }
 
-psr_status psr_reconstruct(psr_handle* h, const psr_points* pts, const psr_options* opt, psr_mesh* mesh,
-                           void* stream) {
+// copies the mesh of the last run into device-resident caller buffers (counts read on the
+// device, clamped to the caller's capacities), so a device-output call needs no host wait
+__global__ void __launch_bounds__(kBlock) k_emit_mesh(const Counters* c, const float* v, const int* t,
+                                                      const float* col, const float* nrm, float* ov, int* ot,
+                                                      float* oc, float* on, int vcap, int tcap) {
+    const int nv = 3 * min(max(c->n_mesh_vertices, 0), vcap);
+    const int nt = 3 * min(max(c->n_mesh_triangles, 0), tcap);
+    PSR_GRID_STRIDE(i, max(nv, nt)) {
+        if (i < nv) {
+            if (ov) ov[i] = v[i];
+            if (oc) oc[i] = col[i];
+            if (on) on[i] = nrm[i];
+        }
+        if (i < nt && ot) ot[i] = t[i];
+    }
+}
+
+// Enqueues one reconstruction on `stream` (no host synchronisation).
+static psr_status submit_impl(psr_handle* h, const psr_points* pts, const psr_options* opt, psr_mesh* mesh,
+                              void* stream) {
     if (!h) return PSR_INVALID_INPUT;
+    if (h->pending) return fail(h, PSR_INVALID_INPUT, "a reconstruction is already in flight on this handle");
     h->have_result = false;
     if (!pts || !mesh || !pts->xyz || !pts->normals) return fail(h, PSR_INVALID_INPUT, "null argument");
     const int n = pts->count;
@@ -416,8 +445,34 @@ psr_status psr_reconstruct(psr_handle* h, const psr_points* pts, const psr_optio
     ws.in_rgb = saved_rgb;
     ws.stream = s;
     if (e == cudaSuccess) e = cudaMemcpyAsync(ws.cnt_host, ws.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess && mesh->location == PSR_DEVICE) {
+        k_emit_mesh<<<ws.num_sms * 4, kBlock, 0, s>>>(ws.cnt, ws.mesh_v, ws.mesh_t, ws.mesh_c, ws.mesh_n,
+                                                      mesh->vertices, mesh->triangles,
+                                                      want_colour ? mesh->colors : nullptr,
+                                                      want_normals ? mesh->normals : nullptr, mesh->vertex_capacity,
+                                                      mesh->triangle_capacity);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(h->done, s);
     if (e != cudaSuccess) return cuda_fail(h, e, "reconstruct");
+    h->pending = true;
+    h->pend_mesh = mesh;
+    h->pend_depth = depth;
+    h->pend_colour = want_colour;
+    h->pend_normals = want_normals;
+    h->pend_stream = s;
+    return PSR_OK;
+}
+
+// After the submitted work has completed: statistics, status, mesh counts, host copies.
+static psr_status complete_impl(psr_handle* h) {
+    h->pending = false;
+    Workspace& ws = h->ws;
+    psr_mesh* mesh = h->pend_mesh;
+    const int depth = h->pend_depth;
+    const int want_colour = h->pend_colour, want_normals = h->pend_normals;
+    cudaStream_t s = h->pend_stream;
+    cudaError_t e = cudaSuccess;
     Counters& c = *ws.cnt_host;
     h->host_cnt = c;
     h->have_result = true;
@@ -448,7 +503,8 @@ psr_status psr_reconstruct(psr_handle* h, const psr_points* pts, const psr_optio
     mesh->scale = c.max_edge;
     if (c.n_mesh_vertices > mesh->vertex_capacity || c.n_mesh_triangles > mesh->triangle_capacity)
         return fail(h, PSR_OUT_OF_CAPACITY, "output mesh buffers too small");
-    const cudaMemcpyKind ok = (mesh->location == PSR_DEVICE) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if (mesh->location == PSR_DEVICE) return PSR_OK;   // written by k_emit_mesh
+    const cudaMemcpyKind ok = cudaMemcpyDeviceToHost;
     if (mesh->vertices && c.n_mesh_vertices)
         e = cudaMemcpyAsync(mesh->vertices, ws.mesh_v, 3 * sizeof(float) * (size_t)c.n_mesh_vertices, ok, s);
     if (e == cudaSuccess && mesh->triangles && c.n_mesh_triangles)
@@ -459,6 +515,46 @@ psr_status psr_reconstruct(psr_handle* h, const psr_points* pts, const psr_optio
         e = cudaMemcpyAsync(mesh->normals, ws.mesh_n, 3 * sizeof(float) * (size_t)c.n_mesh_vertices, ok, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cuda_fail(h, e, "output copy");
+    return PSR_OK;
+}
+
+psr_status psr_reconstruct(psr_handle* h, const psr_points* pts, const psr_options* opt, psr_mesh* mesh,
+                           void* stream) {
+    psr_status st = submit_impl(h, pts, opt, mesh, stream);
+    if (st != PSR_OK) return st;
+    return psr_wait(h);
+}
+
+psr_status psr_submit(psr_handle* h, const psr_points* pts, const psr_options* opt, psr_mesh* mesh, void* stream) {
+    return submit_impl(h, pts, opt, mesh, stream);
+}
+
+psr_status psr_poll(psr_handle* h) {
+    if (!h) return PSR_INVALID_INPUT;
+    if (!h->pending) return fail(h, PSR_INVALID_INPUT, "no reconstruction in flight");
+    const cudaError_t q = cudaEventQuery(h->done);
+    if (q == cudaErrorNotReady) return PSR_PENDING;
+    if (q != cudaSuccess) {
+        h->pending = false;
+        return cuda_fail(h, q, "reconstruct");
+    }
+    return complete_impl(h);
+}
+
+psr_status psr_wait(psr_handle* h) {
+    if (!h) return PSR_INVALID_INPUT;
+    if (!h->pending) return fail(h, PSR_INVALID_INPUT, "no reconstruction in flight");
+    const cudaError_t q = cudaEventSynchronize(h->done);
+    if (q != cudaSuccess) {
+        h->pending = false;
+        return cuda_fail(h, q, "reconstruct");
+    }
+    return complete_impl(h);
+}
+
+psr_status psr_memory_bytes(const psr_handle* h, size_t* bytes) {
+    if (!h || !bytes) return PSR_INVALID_INPUT;
+    *bytes = h->arena_bytes;
     return PSR_OK;
 }
 

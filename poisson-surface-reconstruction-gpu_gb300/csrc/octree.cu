@@ -48,11 +48,18 @@ __global__ void __launch_bounds__(kBlock) k_bbox(const float* xyz, const float* 
         }
     }
     if (__any_sync(0xffffffffu, bad) && lane_id() == 0) atomicOr(&c->error, kErrInvalid);
-    if (lane_id() == 0) {
-        for (int a = 0; a < 3; ++a) {
-            atomicMax(&((int*)c->bbox_max)[a], float_to_ordered(mx[a]));
-            atomicMin(&((int*)c->bbox_min)[a], float_to_ordered(mn[a]));
-        }
+    // block reduction, then one set of atomics per block
+    __shared__ float s_mx[3][kBlock / 32], s_mn[3][kBlock / 32];
+    const int w = threadIdx.x >> 5;
+    if (lane_id() == 0)
+        for (int a = 0; a < 3; ++a) { s_mx[a][w] = mx[a]; s_mn[a][w] = mn[a]; }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        const int a = threadIdx.x;
+        float bmx = s_mx[a][0], bmn = s_mn[a][0];
+        for (int q = 1; q < kBlock / 32; ++q) { bmx = fmaxf(bmx, s_mx[a][q]); bmn = fminf(bmn, s_mn[a][q]); }
+        atomicMax(&((int*)c->bbox_max)[a], float_to_ordered(bmx));
+        atomicMin(&((int*)c->bbox_min)[a], float_to_ordered(bmn));
     }
 }
 

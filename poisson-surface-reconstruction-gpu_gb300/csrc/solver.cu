@@ -87,6 +87,7 @@ struct CgcArgs {
 };
 
 struct CgcShared {
+    float2 zero2;   // (r, p) of a missing neighbour
     FF warp[kCgWarps];
     FF slot[2];
     FF sum;
@@ -166,6 +167,9 @@ __device__ __forceinline__ void cgc_resident(cg::cluster_group& cl, CgcShared& s
     const int spos = cg_spos(sib);
     float* myblk = sblk + warp * kCgWarpBlockFloats + gi * 80 + ((0x1a081200 >> (gi * 8)) & 0xff);
     const int gbase = (mlo - 1) >> 3;   // block-table group of local row 0
+    // g / chunk = umulhi(g, ceil(2^32 / chunk)): exact while g * (magic * chunk - 2^32) < 2^32,
+    // true here (g < 2^17 rows, chunk <= kCgSmemRows)
+    const unsigned chunk_magic = chunk > 0 ? (unsigned)((0x100000000ull + (unsigned)chunk - 1) / (unsigned)chunk) : 0u;
     // r0 = b, p_{-1} = 0, x0 = 0
     FF acc = ff_zero();
     for (int l = threadIdx.x; l < nloc; l += kCgcBlock) {
@@ -204,24 +208,28 @@ __device__ __forceinline__ void cgc_resident(cg::cluster_group& cl, CgcShared& s
                 q1 = __ldg(bp + 1);
             }
             if (mine) {
+                // one generic address per entry (own shared memory, a peer's through the
+                // cluster window, or a zero pair for a missing cell), then 8 independent loads
+                const float2* src[8];
 #pragma unroll
                 for (int e = 0; e < 8; ++e) {
                     const int nb = ids[e];
-                    float val = 0.0f;
                     const int gl = nb - mlo;
+                    const int g = nb - u.row0;
                     if ((unsigned)gl < (unsigned)nloc) {
-                        const float2 v = cur[gl];
-                        val = fmaf(beta, v.y, v.x);
-                    } else if (nb >= 0) {
-                        const int g = nb - u.row0;
-                        if ((unsigned)g < (unsigned)m) {
-                            const int owner = g / chunk;
-                            const float2 v = *cl.map_shared_rank(cur + (g - owner * chunk), (unsigned)owner);
-                            val = fmaf(beta, v.y, v.x);
-                        }
+                        src[e] = cur + gl;
+                    } else if (nb >= 0 && (unsigned)g < (unsigned)m) {
+                        const int owner = (int)__umulhi((unsigned)g, chunk_magic);   // g / chunk
+                        src[e] = cl.map_shared_rank(cur + (g - owner * chunk), (unsigned)owner);
+                    } else {
+                        src[e] = &sh.zero2;
                     }
-                    myblk[e * 8 + sib] = val;
                 }
+                float2 vals[8];
+#pragma unroll
+                for (int e = 0; e < 8; ++e) vals[e] = *src[e];
+#pragma unroll
+                for (int e = 0; e < 8; ++e) myblk[e * 8 + sib] = fmaf(beta, vals[e].y, vals[e].x);
             }
             __syncwarp();
             if (mine) {
@@ -337,6 +345,7 @@ __device__ __forceinline__ void cg_unit_body(const CgcArgs& a, int unit) {
     u.row0 = a.c->level_base[u.d];
     u.row1 = (u.d < a.depth) ? a.c->level_base[u.d + 1] : a.c->n_nodes;
     if (threadIdx.x < 27) sh.st[threadIdx.x] = a.stencil[u.d * 27 + threadIdx.x];
+    if (threadIdx.x == 0) sh.zero2 = make_float2(0.0f, 0.0f);
     __syncthreads();
     const int nblk = (int)cl.num_blocks();
     const int m = u.row1 - u.row0;

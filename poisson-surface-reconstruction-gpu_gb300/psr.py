@@ -15,12 +15,14 @@ import numpy as np
 PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "libpsr.so"
 
-PSR_OK, PSR_OUT_OF_CAPACITY, PSR_INVALID_INPUT, PSR_NONCONVERGED, PSR_DEVICE_TIMEOUT, PSR_CUDA_ERROR = range(6)
+(PSR_OK, PSR_OUT_OF_CAPACITY, PSR_INVALID_INPUT, PSR_NONCONVERGED, PSR_DEVICE_TIMEOUT, PSR_CUDA_ERROR,
+ PSR_PENDING) = range(7)
 PSR_HOST, PSR_DEVICE = 0, 1
 
 # every function declared in include/psr/psr.h
-EXPORTED = ["psr_config_default", "psr_create", "psr_destroy", "psr_reconstruct", "psr_get_stats",
-            "psr_debug_array", "psr_status_string", "psr_last_error", "psr_morton_sort_noalloc"]
+EXPORTED = ["psr_config_default", "psr_create", "psr_destroy", "psr_reconstruct", "psr_submit", "psr_poll",
+            "psr_wait", "psr_memory_bytes", "psr_get_stats", "psr_debug_array", "psr_status_string",
+            "psr_last_error", "psr_morton_sort_noalloc"]
 
 
 class PsrConfig(ctypes.Structure):
@@ -77,6 +79,10 @@ def load_library(path=None):
     L.psr_destroy.argtypes = [ctypes.c_void_p]
     L.psr_reconstruct.argtypes = [ctypes.c_void_p, ctypes.POINTER(PsrPoints), ctypes.POINTER(PsrOptions),
                                   ctypes.POINTER(PsrMesh), ctypes.c_void_p]
+    L.psr_submit.argtypes = L.psr_reconstruct.argtypes
+    L.psr_poll.argtypes = [ctypes.c_void_p]
+    L.psr_wait.argtypes = [ctypes.c_void_p]
+    L.psr_memory_bytes.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t)]
     L.psr_get_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(PsrStats)]
     L.psr_debug_array.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_size_t,
                                   ctypes.POINTER(ctypes.c_size_t)]
@@ -208,6 +214,42 @@ class PoissonReconstruction:
         if st != PSR_OK and not (st == PSR_OUT_OF_CAPACITY and out is None):
             raise self._error(st, "psr_reconstruct")
         return mesh
+
+    # ---- served form: submit, then poll / wait (one reconstruction in flight per handle)
+    def submit_device(self, xyz_ptr, nrm_ptr, rgb_ptr, n, out, depth=0, cg_iterations=0, stream=None,
+                      location=PSR_DEVICE):
+        """Enqueue a reconstruction of the points at the given pointers (device memory, or
+        pinned host memory with location=PSR_HOST) into the mesh buffers of ``out`` (a
+        PsrMesh, device- or host-resident); returns immediately."""
+        self._pend = (PsrPoints(xyz_ptr, nrm_ptr, rgb_ptr, int(n), int(location)),
+                      PsrOptions(int(depth), int(cg_iterations)), out)
+        pts, opt, mesh = self._pend
+        st = self._lib.psr_submit(self._h, ctypes.byref(pts), ctypes.byref(opt), ctypes.byref(mesh), stream)
+        if st != PSR_OK:
+            self._pend = None
+            raise self._error(st, "psr_submit")
+
+    def poll(self):
+        """True once the submitted reconstruction has completed (its mesh counts are then
+        set in the PsrMesh given to submit_device); raises on a failed reconstruction."""
+        st = self._lib.psr_poll(self._h)
+        if st == PSR_PENDING:
+            return False
+        self._pend = None
+        if st != PSR_OK:
+            raise self._error(st, "psr_poll")
+        return True
+
+    def wait(self):
+        st = self._lib.psr_wait(self._h)
+        self._pend = None
+        if st != PSR_OK:
+            raise self._error(st, "psr_wait")
+
+    def memory_bytes(self):
+        b = ctypes.c_size_t(0)
+        self._lib.psr_memory_bytes(self._h, ctypes.byref(b))
+        return int(b.value)
 
     def GetRebuildMeshVertices(self):
         return None if self._mesh is None else self._mesh.vertices
