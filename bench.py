@@ -329,6 +329,14 @@ def main():
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s",
                 "algorithmic_bytes": cg_bytes, "launch_ms": cg_ms,
                 "note": "vectors and neighbour table stay in L2 (DRAM traffic ~10 MB per launch): latency bound"}
+    # DRAM traffic of one launch, from the committed ncu summary of the same kernel and workload
+    try:
+        for line in open(ROOT / "profiles" / "cg_cluster_torus200k_d7.md"):
+            if line.startswith("traffic_bytes_per_launch:") and args.workload == "torus_ellipsoid200k":
+                roofline["traffic"] = int(line.split(":")[1])
+                roofline["traffic_source"] = "profiles/cg_cluster_torus200k_d7.md (ncu dram__bytes_read+write)"
+    except OSError:
+        pass
     if roofline["achieved"]:
         roofline["frac"] = roofline["achieved"] / peak_hbm
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -236,7 +236,7 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     A.add(ws.s_key, (size_t)subn); A.add(ws.s_parent, (size_t)subn); A.add(ws.s_first_child, (size_t)subn);
     A.add(ws.s_neigh, 27 * (size_t)subn); A.add(ws.s_depth, (size_t)subn); A.add(ws.s_root, (size_t)subn);
     A.add(ws.s_group, (size_t)subn);
-    A.add(ws.s_contrib, (size_t)subn);
+    A.add(ws.s_jump, (size_t)subn);
     A.add(ws.s_cx, (size_t)subn); A.add(ws.s_cy, (size_t)subn); A.add(ws.s_cz, (size_t)subn);
     A.add(ws.s_vtx, 8 * (size_t)subd); A.add(ws.s_edge, 12 * (size_t)subd);
     A.add(ws.s_vmask, (size_t)subd); A.add(ws.s_emask, (size_t)subd);

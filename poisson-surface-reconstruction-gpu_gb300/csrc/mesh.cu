@@ -717,7 +717,7 @@ __global__ void __launch_bounds__(kBlock) k_sub_neighbours(const Counters* c, in
                                                            const int* ov_group, const int* ov_sub, const int* s_key,
                                                            const int* s_parent, const int* s_first_child,
                                                            const int* s_depth, const int* s_group, const int* s_root,
-                                                           int* s_neigh, unsigned char* s_contrib, size_t sstride,
+                                                           int* s_neigh, int* s_jump, size_t sstride,
                                                            int na) {
     // Depth-d nodes only.  Groups are ordered by root depth, so those reaching depth d are
     // a prefix 0..gd-1, and the depth-d nodes of groups before g number
@@ -804,7 +804,9 @@ __global__ void __launch_bounds__(kBlock) k_sub_neighbours(const Counters* c, in
             // group's root depth are exactly its roots, and deeper ones are never roots
             if (v >= 0 && (v < na || at_root_depth)) contrib = 1;
         }
-        s_contrib[s] = (unsigned char)contrib;
+        // nearest contributing node on the path to the root (itself when it contributes;
+        // roots always do): lets the value chains skip non-contributing levels in one hop
+        s_jump[s] = contrib ? s : ((pa >= na) ? s_jump[pa - na] : s);
     }
 }
 
@@ -989,7 +991,7 @@ __global__ void __launch_bounds__(kBlock) k_sub_vertex_values(const Counters* c,
                                                               const int* neigh, size_t stride, const int* parent,
                                                               const int* s_neigh, size_t sstride,
                                                               const int* s_parent, const int* s_root,
-                                                              const unsigned char* s_contrib, const int* s_depth,
+                                                              const int* s_jump, const int* s_depth,
                                                               const float* s_cx, const float* s_cy,
                                                               const float* s_cz, const int* enc, const float* x,
                                                               float* vvalue, int na) {
@@ -1006,10 +1008,10 @@ __global__ void __launch_bounds__(kBlock) k_sub_vertex_values(const Counters* c,
                     now = parent[now];
                     continue;
                 }
-                const int sn = now - na;
+                // levels whose 27 neighbours are all zero-valued subdivision nodes add nothing:
+                // hop to the nearest contributing node on the way to the root
+                const int sn = s_jump[now - na];
                 now = s_parent[sn];
-                // all 27 neighbours zero-valued subdivision nodes: every term is skipped
-                if (!s_contrib[sn]) continue;
                 const int d = s_depth[sn];
                 const float sc = (float)(1 << d);
                 const int base = (1 << d) - 1;
@@ -1332,7 +1334,7 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
     for (int d = 1; d <= D; ++d)
         k_sub_neighbours<<<gs, kBlock, 0, s>>>(c, d, D, mb.groups, ws.neigh, stride, ws.first_child, mb.ov_group,
                                                mb.ov_sub, ws.s_key, ws.s_parent, ws.s_first_child, ws.s_depth,
-                                               ws.s_group, ws.s_root, ws.s_neigh, ws.s_contrib, sstride, na);
+                                               ws.s_group, ws.s_root, ws.s_neigh, ws.s_jump, sstride, na);
     cudaMemsetAsync(ws.s_vtx, 0, sizeof(int) * 8 * dstride, s);
     cudaMemsetAsync(ws.s_edge, 0, sizeof(int) * 12 * dstride, s);
     k_sub_vertex_owner<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.s_key, ws.s_neigh, sstride, ws.s_vmask, na);
@@ -1356,7 +1358,7 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
     k_sub_edge_maintain<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.s_group, ws.s_neigh, sstride, ws.s_depth, ws.se_owner,
                                               ws.se_kind, ws.s_edge, dstride, na);
     k_sub_vertex_values<<<gs, kBlock, 0, s>>>(c, D, ws.sv_x, ws.sv_y, ws.sv_z, ws.sv_owner, ws.neigh, stride, ws.parent,
-                                              ws.s_neigh, sstride, ws.s_parent, ws.s_root, ws.s_contrib, ws.s_depth,
+                                              ws.s_neigh, sstride, ws.s_parent, ws.s_root, ws.s_jump, ws.s_depth,
                                               ws.s_cx, ws.s_cy, ws.s_cz, ws.enc, ws.xsol, ws.sv_value, na);
     // crossings: staged after the main part's vertices
     e = launch_scan<2>(SubCrossLoad{ws.se_dn, ws.se_kind, ws.s_vtx, dstride, ws.sv_value, err},

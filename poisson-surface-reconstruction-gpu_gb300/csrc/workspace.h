@@ -121,7 +121,7 @@ struct Workspace {
     // subdivision-space nodes of all groups (SoA)
     int *s_key, *s_parent, *s_first_child, *s_neigh, *s_depth, *s_root;   // s_neigh: [27][cap.sub_nodes]
     int* s_group;
-    unsigned char* s_contrib;   // 1 when some neighbour of the sub-node carries a solution value
+    int* s_jump;            // nearest sub-node on the path to the root with a neighbour carrying a value
     float *s_cx, *s_cy, *s_cz;
     int *s_vtx, *s_edge;    // [8|12][cap.sub_dnodes] for D-level subdivision nodes
     unsigned char* s_vmask;
