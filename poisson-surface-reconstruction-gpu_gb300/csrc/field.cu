@@ -278,7 +278,7 @@ cudaError_t field_build(Workspace& ws) {
         int* n_items = (int*)&c->n_groups;
         unsigned* total = (unsigned*)&c->scan_total;
         cudaError_t e = launch_scan(DivChunkLoad{ws.neigh, stride, ws.dnum}, StoreExclusive{item_start},
-                                    &c->level_base[dsplit], 0, ws.scan, total, &c->error, s);
+                                    &c->level_base[dsplit], 0, ws.scan, total, &c->error, s, ScanCount{}, 1);
         if (e != cudaSuccess) return e;
         const int item_cap = ws.cap.nodes;   // partial buffer holds cap.nodes float pairs
         k_div_chunk_count<<<1, 1, 0, s>>>(c, dsplit, total, item_cap, n_items);

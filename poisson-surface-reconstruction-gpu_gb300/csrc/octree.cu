@@ -434,10 +434,11 @@ cudaError_t octree_build(Workspace& ws) {
     k_gather<<<gp, kBlock, 0, s>>>(ws.in_xyz, ws.in_nrm, ws.in_rgb, scode, sidx, c, D, ws.px, ws.py, ws.pz, ws.nx,
                                    ws.ny, ws.nz, ws.cr, ws.cg, ws.cb, head);
     e = launch_scan(LoadArray{head}, HeadStore{scode, ws.puid, ws.ucode, ws.ufirst}, &c->n_points, 0, ws.scan, total,
-                    err, s);
+                    err, s, ScanCount{}, 1);
     if (e != cudaSuccess) return e;
     k_after_unique<<<1, 1, 0, s>>>(c, ws.ufirst, total);
-    e = launch_scan(LeafGroupLoad{ws.ucode}, StoreInclusive{ws.uaddr}, &c->n_unique, 0, ws.scan, total, err, s);
+    e = launch_scan(LeafGroupLoad{ws.ucode}, StoreInclusive{ws.uaddr}, &c->n_unique, 0, ws.scan, total, err, s,
+                    ScanCount{}, 1);
     if (e != cudaSuccess) return e;
     k_after_leaf_groups<<<1, 1, 0, s>>>(c, total, D, ws.cap.dnodes);
     const int gn = grid_for(ws, ws.cap.dnodes);
@@ -450,7 +451,7 @@ cudaError_t octree_build(Workspace& ws) {
         k_group_aggregate<<<gg, kBlock, 0, s>>>(c, d, D, ws.tkey, ws.tpidx, ws.tpnum, ws.tdidx, ws.tdnum, ws.gkey,
                                                 ws.gpidx, ws.gpnum, ws.gdidx, ws.gdnum);
         e = launch_scan(FatherGroupLoad{ws.gkey, 3 * (D - d + 2)}, StoreInclusive{ws.gaddr}, &c->n_groups, 0, ws.scan,
-                        total, err, s);
+                        total, err, s, ScanCount{}, 1);
         if (e != cudaSuccess) return e;
         k_after_father_groups<<<1, 1, 0, s>>>(c, d, total, ws.cap.nodes);
         k_init_level<<<gg, kBlock, 0, s>>>(c, d - 1, D, ws.tkey, ws.tpidx, ws.tpnum, ws.tdidx, ws.tdnum, ws.tchild);

@@ -5,14 +5,14 @@ namespace psr {
 
 static int g_num_sms = 0;
 
-int scan_grid(int max_tiles) {
+int scan_grid(int max_tiles, int blocks_per_sm) {
     if (g_num_sms == 0) {
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
         if (g_num_sms <= 0) g_num_sms = 148;
     }
-    int g = g_num_sms * 4;
+    int g = g_num_sms * blocks_per_sm;
     return g < max_tiles ? g : (max_tiles > 0 ? max_tiles : 1);
 }
 
@@ -143,7 +143,7 @@ cudaError_t radix_sort_pairs(unsigned* keys, unsigned* vals, const int* count_pt
         k_sort_hist<<<grid, kBlock, 0, stream>>>(ki, count_ptr, shift, sc.hist, sc.max_tiles, err);
         k_sort_hist_count<<<1, 1, 0, stream>>>(count_ptr, n_hist);
         cudaError_t e = launch_scan(HistLoad{sc.hist, count_ptr, sc.max_tiles}, HistStore{sc.hist, count_ptr, sc.max_tiles},
-                                    n_hist, 0, sc.scan, total, err, stream);
+                                    n_hist, 0, sc.scan, total, err, stream, ScanCount{}, 1);
         if (e != cudaSuccess) return e;
         k_sort_scatter<<<grid, kBlock, 0, stream>>>(ki, vi, ko, vo, count_ptr, shift, sc.hist, sc.max_tiles);
         unsigned* tk = ki; ki = ko; ko = tk;

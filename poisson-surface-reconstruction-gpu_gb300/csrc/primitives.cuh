@@ -186,13 +186,18 @@ __global__ void __launch_bounds__(kBlock) k_scan(Load load, Store store, const i
     }
 }
 
-int scan_grid(int max_tiles);
+// blocks of a scan launch: blocks_per_sm per SM, at most max_tiles
+int scan_grid(int max_tiles, int blocks_per_sm = 4);
 
+// blocks_per_sm: 4 for scans that can be long (hundreds of tiles or more); small scans
+// (per octree level, per point at a few hundred tiles) take 1 so that idle blocks do not
+// occupy the GPU while other reconstructions run beside them
 template <int kItems = kScanItems, class Load, class Store>
 inline cudaError_t launch_scan(Load load, Store store, const int* count_ptr, int count_add, ScanScratch sc,
-                               unsigned* total, unsigned* err, cudaStream_t stream, ScanCount cnt = ScanCount{}) {
-    k_scan<kItems, Load, Store><<<scan_grid(sc.max_tiles), kBlock, 0, stream>>>(load, store, count_ptr, count_add, sc,
-                                                                                total, err, cnt);
+                               unsigned* total, unsigned* err, cudaStream_t stream, ScanCount cnt = ScanCount{},
+                               int blocks_per_sm = 4) {
+    k_scan<kItems, Load, Store><<<scan_grid(sc.max_tiles, blocks_per_sm), kBlock, 0, stream>>>(
+        load, store, count_ptr, count_add, sc, total, err, cnt);
     return cudaGetLastError();
 }
 
