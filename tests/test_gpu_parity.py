@@ -129,6 +129,24 @@ def full_check(recon, oracle_mod, name, n=None, cg_iters=0, depth=None):
     return mesh, o
 
 
+def full_check_arrays(recon, oracle_mod, p, nr, rgb, D, cg_iters=0):
+    mesh, o = run_both(recon, oracle_mod, p, nr, rgb, D, cg_iters)
+    check_octree(recon, o)
+    x_gpu, iso_gpu = check_field_and_solve(recon, o)
+    check_geometry(recon, o)
+    check_mesh_mirror(recon, o, mesh, x_gpu, iso_gpu)
+    return mesh, o
+
+
+@pytest.mark.parametrize("cloud", [0, 1])
+def test_mix_rotated_scaled_clouds_depth7(recon, oracle_mod, cloud):
+    # the batched / served workloads' clouds: random shape, rotation and scale, with colour
+    p, nr, rgb, _ = syn.workload("mix", cloud=cloud, n=25000, colour=True)
+    mesh, o = full_check_arrays(recon, oracle_mod, p, nr, rgb, 7)
+    assert o.scalars()["ub_events"] == 0
+    assert len(mesh.triangles) > 1000
+
+
 def test_sphere20k_depth6_eight_iterations(recon, oracle_mod):
     full_check(recon, oracle_mod, "sphere20k", cg_iters=8)
 
