@@ -20,7 +20,7 @@
 extern "C" {
 #endif
 
-#define PSR_ABI_VERSION 1
+#define PSR_ABI_VERSION 2
 
 typedef enum psr_status {
     PSR_OK = 0,
@@ -48,6 +48,10 @@ typedef struct psr_config {
     int compute_colors;        /* per-vertex colour transfer (mesh/DrawMesh.cu:179-214) */
     int compute_normals;       /* per-vertex normals (mesh/DrawMesh.cu:102-177) */
     int device;                /* CUDA device ordinal */
+    float laplacian_epsilon;   /* Laplacian entries with |value| <= this are dropped: 1e-6 as in
+                                  mesh/solver/LaplacianSolver.cu:128-204; 0 keeps every entry
+                                  (from depth 9 on the 1e-6 rule drops the stencil's edge and
+                                  corner entries and leaves an indefinite system) */
 } psr_config;
 
 /* Oriented input cloud (the fields of DepthSurfel, base/CommonTypes.h:113-118, as SoA). */

@@ -37,6 +37,7 @@ def lib():
         L = ctypes.CDLL(str(LIB))
         L.oro_create.restype = ctypes.c_void_p
         L.oro_destroy.argtypes = [ctypes.c_void_p]
+        L.oro_set_lap_eps.argtypes = [ctypes.c_void_p, ctypes.c_double]
         L.oro_run.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                               ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
                               ctypes.c_int, ctypes.c_int, ctypes.c_int]
@@ -91,8 +92,10 @@ def mc_tables():
 class Oracle:
     """One oracle run; arrays are copied out on access."""
 
-    def __init__(self):
+    def __init__(self, laplacian_epsilon=None):
         self._h = lib().oro_create()
+        if laplacian_epsilon is not None:   # default: the reference's 1e-6 drop threshold
+            lib().oro_set_lap_eps(self._h, float(laplacian_epsilon))
 
     def __del__(self):
         try:

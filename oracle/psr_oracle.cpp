@@ -213,6 +213,7 @@ struct Options {
     int stop_after = 99;       // 1 octree, 2 field, 3 solve, 4 mesh, 5 colour
     int tri_cap = 1000000;     // MAX_MESH_TRIANGLE_COUNT (base/GlobalConfigs.h:8)
     int vert_cap = 300000;     // MeshTriangleVertex capacity (ComputeTriangleIndices.cpp:32)
+    double lap_eps = (double)1e-6f;   // entries with |L| <= lap_eps are dropped (EPSILON, device::eps)
 };
 
 struct State {
@@ -625,8 +626,6 @@ static void compute_field(State& S) {
 // Per-depth Laplacian and CG (mesh/solver/LaplacianSolver.cu:27-74,120-267,
 // mesh/solver/CGAlgorithm.cu:10-80), FP64.
 // ---------------------------------------------------------------------------------
-static const double kLapEps = (double)1e-6f;   // EPSILON as stored in device::eps
-
 static void solve(State& S) {
     const int D = S.D, res = S.tab.res;
     S.x.assign(S.M, 0.0);
@@ -649,7 +648,7 @@ static void solve(State& S) {
                 decode(S, S.enc[nb], nx, ny, nz);
                 size_t sx = (size_t)ox * res + nx, sy = (size_t)oy * res + ny, sz = (size_t)oz * res + nz;
                 double e = S.tab.ff[sx] * S.tab.ff[sy] * S.tab.ff[sz] * (S.tab.d2[sx] + S.tab.d2[sy] + S.tab.d2[sz]);
-                if (std::fabs(e) > kLapEps) { ci.push_back(nb - b); va.push_back((double)(float)e); }
+                if (std::fabs(e) > S.opt.lap_eps) { ci.push_back(nb - b); va.push_back((double)(float)e); }
             }
             rp[r + 1] = (int)ci.size();
         }
@@ -1529,6 +1528,7 @@ using namespace oracle;
 
 struct OracleHandle {
     State S;
+    double lap_eps = (double)1e-6f;
     std::map<std::string, std::vector<char>> scratch;
 };
 
@@ -1536,6 +1536,10 @@ extern "C" {
 
 void* oro_create(void) { return new OracleHandle(); }
 void oro_destroy(void* h) { delete (OracleHandle*)h; }
+
+// Drop threshold of the Laplacian entries for the following runs (the reference's 1e-6
+// by default; 0 keeps every entry).
+void oro_set_lap_eps(void* h, double eps) { ((OracleHandle*)h)->lap_eps = eps; }
 
 // Runs the pipeline up to `stop_after` (1 octree, 2 field, 3 solve, 4 mesh, 5 colour).
 // cg_iters > 0 selects a fixed iteration count per depth; otherwise CG stops when
@@ -1550,6 +1554,7 @@ int oro_run(void* hp, const float* xyz, const float* nrm, const float* rgb, int 
     S.opt.cg_tol = cg_tol;
     S.opt.cg_max_iter = cg_max_iter;
     S.opt.stop_after = stop_after;
+    S.opt.lap_eps = h->lap_eps;
     if (vert_cap > 0) S.opt.vert_cap = vert_cap;
     if (tri_cap > 0) S.opt.tri_cap = tri_cap;
     if (n <= 0 || depth < 2 || depth > 9) return 2;

@@ -18,7 +18,7 @@ cudaError_t upload_tables_solver();
 cudaError_t upload_tables_mesh();
 cudaError_t upload_tables_transfer();
 void build_dff_table(int depth, std::vector<double>& dff);
-void build_stencil(int depth, std::vector<float>& st);
+void build_stencil(int depth, std::vector<float>& st, double eps);
 }  // namespace psr
 
 using namespace psr;
@@ -106,6 +106,7 @@ psr_status psr_config_default(psr_config* c) {
     c->bbox_scale = 1.25f;
     c->cg_max_iterations = 10000;
     c->cg_tolerance = 1e-5f;
+    c->laplacian_epsilon = 1e-6f;
     c->compute_colors = 0;
     c->compute_normals = 0;
     c->device = 0;
@@ -294,7 +295,7 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
         std::vector<double> dff;
         build_dff_table(D, dff);
         std::vector<float> st;
-        build_stencil(kMaxDepth, st);
+        build_stencil(kMaxDepth, st, (double)cfg.laplacian_epsilon);
         std::vector<float> dff32(dff.begin(), dff.end());   // the kernels use float entries
         e = cudaMemcpy(ws.dff, dff32.data(), dff32.size() * sizeof(float), cudaMemcpyHostToDevice);
         if (e == cudaSuccess) e = cudaMemcpy(ws.stencil, st.data(), st.size() * sizeof(float), cudaMemcpyHostToDevice);

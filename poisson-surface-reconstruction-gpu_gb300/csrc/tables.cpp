@@ -138,9 +138,8 @@ void build_dff_table(int depth, std::vector<double>& dff) {
 // evaluated in FP64 and stored as FP32; entries with |value| <= 1e-6 are dropped.  Same
 // depth pairs only depend on the offset, so one coefficient per (depth, neighbour) is
 // exact.  Returns (D+1) x 27 floats.
-void build_stencil(int depth, std::vector<float>& st) {
+void build_stencil(int depth, std::vector<float>& st, double eps) {
     st.assign((size_t)(depth + 1) * 27, 0.0f);
-    const double eps = (double)1e-6f;
     for (int d = 0; d <= depth; ++d) {
         // representative node well inside the unit interval (or the only node at d = 0)
         int n = 1 << d;

@@ -147,6 +147,23 @@ def test_mix_rotated_scaled_clouds_depth7(recon, oracle_mod, cloud):
     assert len(mesh.triangles) > 1000
 
 
+def test_laplacian_epsilon_is_applied(oracle_mod):
+    # a drop threshold between the depth-6 stencil's edge (2.10e-5) and corner (2.48e-5)
+    # entries: GPU and oracle drop the same entries (8 fixed CG iterations per depth)
+    import psr
+    p, nr, _, D = syn.workload("sphere20k", n=8000)
+    eps = 2.2e-5
+    x = {}
+    for e in (1e-6, eps):
+        with psr.PoissonReconstruction(max_depth=6, max_points=10000, laplacian_epsilon=e) as r:
+            r.SolvePoissionReconstructionMesh(p, nr, None, depth=D, cg_iterations=8)
+            x[e] = r.debug("x", np.float32)
+    o = oracle_mod.Oracle(laplacian_epsilon=eps)
+    assert o.run(p, nr, None, depth=D, cg_iters=8, stop_after=3) == 0
+    assert rel_l2(x[eps], o.get("x")) <= REL_L2
+    assert rel_l2(x[eps], x[1e-6]) > 10 * REL_L2   # the threshold changed the system
+
+
 def test_sphere20k_depth6_eight_iterations(recon, oracle_mod):
     full_check(recon, oracle_mod, "sphere20k", cg_iters=8)
 
