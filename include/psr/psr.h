@@ -52,6 +52,10 @@ typedef struct psr_config {
                                   mesh/solver/LaplacianSolver.cu:128-204; 0 keeps every entry
                                   (from depth 9 on the 1e-6 rule drops the stencil's edge and
                                   corner entries and leaves an indefinite system) */
+    int concurrent_stages;     /* 1: the octree-only mesh records and the colour grid run on a
+                                  second stream beside the solve (lower latency of one call);
+                                  0: one chain (more throughput when many handles share the
+                                  GPU, as in the served form) */
 } psr_config;
 
 /* Oriented input cloud (the fields of DepthSurfel, base/CommonTypes.h:113-118, as SoA). */

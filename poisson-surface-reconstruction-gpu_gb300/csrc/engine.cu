@@ -107,6 +107,7 @@ psr_status psr_config_default(psr_config* c) {
     c->cg_max_iterations = 10000;
     c->cg_tolerance = 1e-5f;
     c->laplacian_epsilon = 1e-6f;
+    c->concurrent_stages = 1;
     c->compute_colors = 0;
     c->compute_normals = 0;
     c->device = 0;
@@ -178,6 +179,7 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     Arena A;
     A.add(ws.cnt, 1);
     A.add(ws.scan.words, (size_t)cap.scan_tiles + kScanHeader);
+    A.add(ws.scan_aux.words, (size_t)cap.scan_tiles + kScanHeader);
     A.add(ws.sort.hist, (size_t)kRadix * sort_tiles + 16);
     A.add(ws.sort.keys_alt, (size_t)N);
     A.add(ws.sort.vals_alt, (size_t)N);
@@ -274,6 +276,9 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     ws.scan.max_tiles = cap.scan_tiles;
     // scan counters and epoch start at zero; the scans keep them consistent afterwards
     e = cudaMemset(ws.scan.words, 0, sizeof(unsigned long long) * ((size_t)cap.scan_tiles + kScanHeader));
+    ws.scan_aux.max_tiles = cap.scan_tiles;
+    if (e == cudaSuccess)
+        e = cudaMemset(ws.scan_aux.words, 0, sizeof(unsigned long long) * ((size_t)cap.scan_tiles + kScanHeader));
     ws.sort.max_tiles = sort_tiles;
     ws.sort.scan = ws.scan;   // sort shares the scan scratch (scans are sequential on one stream)
     e = cudaMallocHost(&ws.cnt_host, sizeof(Counters));
@@ -284,6 +289,9 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ws.aux, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ws.ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ws.ev_join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ws.aux2, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ws.ev_fork2, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ws.ev_join2, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->done, cudaEventDisableTiming);
     // tables
     if (e == cudaSuccess) e = upload_tables_octree();
@@ -325,6 +333,9 @@ psr_status psr_destroy(psr_handle* h) {
     for (int i = 0; i < 7; ++i) if (h->ev[i]) cudaEventDestroy(h->ev[i]);
     if (h->ws.ev_fork) cudaEventDestroy(h->ws.ev_fork);
     if (h->ws.ev_join) cudaEventDestroy(h->ws.ev_join);
+    if (h->ws.ev_fork2) cudaEventDestroy(h->ws.ev_fork2);
+    if (h->ws.ev_join2) cudaEventDestroy(h->ws.ev_join2);
+    if (h->ws.aux2) cudaStreamDestroy(h->ws.aux2);
     if (h->ws.aux) cudaStreamDestroy(h->ws.aux);
     if (h->done) cudaEventDestroy(h->done);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
@@ -388,11 +399,32 @@ static psr_status submit_impl(psr_handle* h, const psr_points* pts, const psr_op
         cudaError_t q = cudaEventRecordWithFlags(h->ev[0], qs, cudaEventRecordExternal);
         if (q == cudaSuccess) q = octree_build(ws);
         if (q == cudaSuccess) q = cudaEventRecordWithFlags(h->ev[1], qs, cudaEventRecordExternal);
+        // octree-only work on a third stream, beside the divergence and the solve: the
+        // vertex / edge / face records and the colour search grid (own scan scratch)
+        const bool overlap = h->cfg.concurrent_stages != 0;
+        if (overlap) {
+            if (q == cudaSuccess) q = cudaEventRecord(ws.ev_fork2, qs);
+            if (q == cudaSuccess) q = cudaStreamWaitEvent(ws.aux2, ws.ev_fork2, 0);
+            if (q == cudaSuccess) {
+                const ScanScratch main_scan = ws.scan;
+                ws.stream = ws.aux2;
+                ws.scan = ws.scan_aux;
+                q = mesh_geometry(ws);
+                if (q == cudaSuccess) q = transfer_prepare(ws, want_colour);
+                ws.stream = qs;
+                ws.scan = main_scan;
+            }
+            if (q == cudaSuccess) q = cudaEventRecord(ws.ev_join2, ws.aux2);
+        } else {
+            if (q == cudaSuccess) q = mesh_geometry(ws);
+            if (q == cudaSuccess) q = transfer_prepare(ws, want_colour);
+        }
         if (q == cudaSuccess) q = field_build(ws);
         if (q == cudaSuccess) q = cudaEventRecordWithFlags(h->ev[2], qs, cudaEventRecordExternal);
         if (q == cudaSuccess)
             q = solve_build(ws, cg_iters > 0 ? 1 : 0, cg_iters, h->cfg.cg_tolerance, h->cfg.cg_max_iterations);
         if (q == cudaSuccess) q = cudaEventRecordWithFlags(h->ev[3], qs, cudaEventRecordExternal);
+        if (q == cudaSuccess && overlap) q = cudaStreamWaitEvent(qs, ws.ev_join2, 0);
         if (q == cudaSuccess) q = mesh_build(ws);
         if (q == cudaSuccess) q = cudaEventRecordWithFlags(h->ev[4], qs, cudaEventRecordExternal);
         if (q == cudaSuccess) q = transfer_build(ws, want_colour, want_normals);

@@ -1242,12 +1242,14 @@ __global__ void k_count_parts(Counters* c, int* n_parts, int* n_staged_v, int* n
     }
 }
 
-cudaError_t mesh_build_impl(Workspace& ws, const MeshBufs& mb) {
+// Vertex, edge and face records of the octree: they need only the octree, so they are
+// issued on their own stream beside the divergence and the solve (ws.stream, ws.scan and
+// the scan total are the caller's for that stream).
+cudaError_t mesh_geometry_impl(Workspace& ws, const MeshBufs& mb, unsigned* total) {
     cudaStream_t s = ws.stream;
     const int D = ws.depth;
     Counters* c = ws.cnt;
     unsigned* err = &c->error;
-    unsigned* total = (unsigned*)&c->scan_total;
     const size_t stride = (size_t)ws.cap.nodes;
     const int gm = grid_for(ws, ws.cap.nodes);
     cudaError_t e;
@@ -1275,6 +1277,18 @@ cudaError_t mesh_build_impl(Workspace& ws, const MeshBufs& mb) {
                     &c->n_nodes, 0, ws.scan, total, err, s, ScanCount{&c->n_faces, ws.cap.faces});
     if (e != cudaSuccess) return e;
     k_face_maintain<<<gm, kBlock, 0, s>>>(c, ws.neigh, stride, ws.f_owner, ws.f_kind, ws.node_face);
+    return cudaGetLastError();
+}
+
+cudaError_t mesh_build_impl(Workspace& ws, const MeshBufs& mb) {
+    cudaStream_t s = ws.stream;
+    const int D = ws.depth;
+    Counters* c = ws.cnt;
+    unsigned* err = &c->error;
+    unsigned* total = (unsigned*)&c->scan_total;
+    const size_t stride = (size_t)ws.cap.nodes;
+    const int gm = grid_for(ws, ws.cap.nodes);
+    cudaError_t e;
     // implicit values
     k_vertex_values<<<gm, kBlock, 0, s>>>(c, D, ws.v_x, ws.v_y, ws.v_z, ws.v_owner, ws.v_kind, ws.v_depth, ws.neigh,
                                           stride, ws.parent, ws.first_child, ws.enc, ws.xsol, ws.vvalue);
@@ -1396,6 +1410,10 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
 }  // namespace psr
 
 namespace psr {
+cudaError_t mesh_geometry(Workspace& ws) {
+    return mesh_geometry_impl(ws, ws.mb, (unsigned*)&ws.cnt->scan_total_aux);
+}
+
 cudaError_t mesh_build(Workspace& ws) {
     cudaError_t e = mesh_build_impl(ws, ws.mb);
     if (e != cudaSuccess) return e;

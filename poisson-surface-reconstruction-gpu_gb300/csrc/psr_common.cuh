@@ -35,6 +35,7 @@ struct Counters {
     int n_sub_vertices, n_sub_edges, n_sub_cross, n_sub_tri;
     int n_mesh_vertices, n_mesh_triangles;
     int scan_total;               // scratch total written by scans
+    int scan_total_aux;           // the same for scans issued on the geometry stream
     unsigned error;
     float bbox_min[3], bbox_max[3];
     float center[3];

@@ -266,14 +266,22 @@ __global__ void __launch_bounds__(kBlock) k_vertex_normals(const Counters* c, co
     }
 }
 
+// sample grid of the colour search: needs only the sorted samples, so it runs beside the solve
+cudaError_t transfer_prepare(Workspace& ws, int with_colour) {
+    if (!with_colour) return cudaSuccess;
+    const int D = ws.depth;
+    const int g = D < kColourGridLevel ? D : kColourGridLevel;
+    k_cell_starts<<<ws.num_sms * 8, kBlock, 0, ws.stream>>>(ws.cnt, D, g, ws.key, ws.point2node, ws.cell_start);
+    return cudaGetLastError();
+}
+
 cudaError_t transfer_build(Workspace& ws, int with_colour, int with_normals) {
     cudaStream_t s = ws.stream;
     const int grid = ws.num_sms * 8;
     const int D = ws.depth;
     if (with_colour) {
         const int g = D < kColourGridLevel ? D : kColourGridLevel;
-        int* cell_start = ws.cell_start;   // (1 << 3g) + 1 entries
-        k_cell_starts<<<grid, kBlock, 0, s>>>(ws.cnt, D, g, ws.key, ws.point2node, cell_start);
+        int* cell_start = ws.cell_start;   // (1 << 3g) + 1 entries, from transfer_prepare
         k_colour<<<grid, kBlock, 0, s>>>(ws.cnt, g, ws.mesh_v, ws.px, ws.py, ws.pz, ws.cr, ws.cg, ws.cb, cell_start,
                                          ws.mesh_c);
     }

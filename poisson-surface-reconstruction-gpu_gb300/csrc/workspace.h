@@ -51,6 +51,7 @@ struct Workspace {
     Counters* cnt;          // device
     Counters* cnt_host;     // pinned mirror for the final read-back
     ScanScratch scan;
+    ScanScratch scan_aux;   // scans issued on the geometry stream (aux2) while `scan` is in use
     SortScratch sort;
     unsigned* scan_total;   // device scratch (points into cnt)
 
@@ -153,6 +154,8 @@ struct Workspace {
     cudaStream_t stream;
     cudaStream_t aux = nullptr;         // second stream for work forked off `stream`
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaStream_t aux2 = nullptr;        // third stream: octree-only mesh records beside the solve
+    cudaEvent_t ev_fork2 = nullptr, ev_join2 = nullptr;
     int num_sms;
 };
 
@@ -173,7 +176,9 @@ cudaError_t octree_build(Workspace& ws);
 void prepare_launch_configs(Workspace& ws);
 cudaError_t field_build(Workspace& ws);
 cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, int cg_max_iter);
-cudaError_t mesh_build(Workspace& ws);
+cudaError_t mesh_geometry(Workspace& ws);   // vertex / edge / face records (octree only)
+cudaError_t mesh_build(Workspace& ws);      // values, marching cubes, subdivision, compaction
+cudaError_t transfer_prepare(Workspace& ws, int with_colour);   // sample grid (points only)
 cudaError_t transfer_build(Workspace& ws, int with_colour, int with_normals);
 
 }  // namespace psr

@@ -6,6 +6,8 @@ one CUDA stream and one device-resident output mesh each -- and one host thread 
 them through the non-blocking C ABI (psr_submit / psr_poll): a request that arrives while
 others are on the GPU is admitted as soon as a slot is free, and the slots' work overlaps
 on the device.  K is bounded by a device-memory budget (the handles' workspace sizes).
+Each slot's pipeline is one chain (concurrent_stages off): with K reconstructions
+already overlapping, a second stream per slot only adds contention.
 Results are the same as psr_reconstruct alone (the pipeline is deterministic per handle).
 
 Device buffers for the slots' outputs come from PyTorch (plumbing only).
@@ -70,7 +72,8 @@ class Server:
         for k in range(slots):
             r = psr.PoissonReconstruction(max_depth=max_depth, max_points=max_points, max_triangles=max_triangles,
                                           max_mesh_vertices=max_mesh_vertices, compute_colors=compute_colors,
-                                          compute_normals=compute_normals, device=device, **caps)
+                                          compute_normals=compute_normals, device=device,
+                                          **{"concurrent_stages": False, **caps})
             if memory_budget is not None and k > 0 and (k + 1) * r.memory_bytes() > memory_budget:
                 r.close()
                 break

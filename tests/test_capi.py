@@ -43,15 +43,15 @@ def test_config_defaults_without_gpu(lib):
     # reference compile-time caps (base/GlobalConfigs.h:7-8,34)
     assert cfg.max_depth == 7 and cfg.max_points == 300000 and cfg.max_triangles == 1000000
     assert abs(cfg.bbox_scale - 1.25) < 1e-7 and cfg.cg_max_iterations == 10000
-    assert cfg.laplacian_epsilon == ctypes.c_float(1e-6).value
+    assert cfg.laplacian_epsilon == ctypes.c_float(1e-6).value and cfg.concurrent_stages == 1
     lib.psr_status_string.restype = ctypes.c_char_p
     assert lib.psr_status_string(1) == b"out of capacity"
 
 
 def test_struct_layouts_match_header():
     import psr
-    # psr_config: 13 x 4-byte fields
-    assert ctypes.sizeof(psr.PsrConfig) == 52
+    # psr_config: 14 x 4-byte fields
+    assert ctypes.sizeof(psr.PsrConfig) == 56
     assert ctypes.sizeof(psr.PsrPoints) == 32
     assert ctypes.sizeof(psr.PsrOptions) == 8
 
