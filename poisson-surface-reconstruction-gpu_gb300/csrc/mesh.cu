@@ -1137,15 +1137,16 @@ struct SubCubeStore {
 // parts: [0] main, [1 + g] group g.  part record: vstart, vcount, tstart, tcount
 __global__ void k_part_table(Counters* c, const int* groups, const unsigned* edge_of_dnode, const unsigned* ecross_sub, const unsigned* tri_of_dnode,
                              unsigned* group_cross0, int* parts) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const int ng = c->n_groups;
     const int nE = c->n_sub_edges;
     const int nSD = c->n_sub_dnodes;
-    parts[0] = 0;
-    parts[1] = c->n_cross;
-    parts[2] = 0;
-    parts[3] = c->n_tri;
-    for (int g = 0; g < ng; ++g) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        parts[0] = 0;
+        parts[1] = c->n_cross;
+        parts[2] = 0;
+        parts[3] = c->n_tri;
+    }
+    PSR_GRID_STRIDE(g, ng) {   // one thread per group (independent entries)
         const int* G = groups + (size_t)g * kGroupRec;
         const int d0 = G[5], d1 = G[5] + G[6];
         // first sub edge of the group = edge prefix at its first D-level sub node
@@ -1384,7 +1385,7 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
     e = launch_scan<2>(SubCubeLoad{ws.s_vtx, dstride, ws.sv_value, ws.s_cube_class, err}, StoreExclusive{mb.tri_of_dnode},
                     &c->n_sub_dnodes, 0, ws.scan, total, err, s, ScanCount{&c->n_sub_tri, ws.part_cap_t});
     if (e != cudaSuccess) return e;
-    k_part_table<<<1, 1, 0, s>>>(c, mb.groups, mb.edge_of_dnode, ws.se_cross, mb.tri_of_dnode,
+    k_part_table<<<grid_for(ws, 1 << 16), kBlock, 0, s>>>(c, mb.groups, mb.edge_of_dnode, ws.se_cross, mb.tri_of_dnode,
                                  mb.group_cross0, mb.parts);
     e = launch_scan<2>(SubCubeLoad{ws.s_vtx, dstride, ws.sv_value, ws.s_cube_class, err},
                     SubCubeStore{ws.s_cube_class, ws.s_edge, dstride, ws.se_cross, mb.group_cross0, mb.groups,

@@ -299,6 +299,154 @@ __global__ void __launch_bounds__(kBlock) k_place_fathers(const Counters* c, int
     }
 }
 
+// ---- coarse levels in one CTA --------------------------------------------------------
+// The levels near the root hold few nodes, so their per-level passes (group aggregate,
+// father-group scan, level set-up, father placement) run inside one 1024-thread CTA with
+// block barriers between steps instead of five launches per level.  Same arithmetic as
+// the per-level kernels above.
+constexpr int kLevelBlock = 1024;
+
+// inclusive block scan of one value per thread (1024 threads); returns the block total
+__device__ __forceinline__ unsigned block_inclusive_scan_1024(unsigned v, unsigned* s_warp) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += y;
+    }
+    if (lane == 31) s_warp[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned w = s_warp[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        s_warp[lane] = w;   // inclusive warp totals
+    }
+    __syncthreads();
+    const unsigned r = v + (warp > 0 ? s_warp[warp - 1] : 0u);
+    const unsigned total = s_warp[31];
+    __syncthreads();
+    s_warp[32] = total;
+    return r;
+}
+
+__global__ void __launch_bounds__(kLevelBlock) k_levels_block(Counters* c, int dtop, int depth, int* tkey, int* tpidx,
+                                                              int* tpnum, int* tdidx, int* tdnum, int* tchild,
+                                                              int* tparent_slot, int* gkey, int* gpidx, int* gpnum,
+                                                              int* gdidx, int* gdnum, unsigned* gaddr, int node_cap) {
+    __shared__ unsigned s_warp[33];
+    const int t = threadIdx.x;
+    for (int d = dtop; d >= 1; --d) {
+        const int m = c->level_count[d];
+        const int off = c->level_tmp_off[d];
+        const int G = m / 8;
+        const int sh = 3 * (depth - d);
+        // (1) sibling groups of level d -> father candidates
+        for (int g = t; g < G; g += kLevelBlock) {
+            int fk = 0, pn = 0, pi = 0x7fffffff, dn = 0, di = 0x7fffffff;
+            for (int j = 0; j < 8; ++j) {
+                const int q = off + 8 * g + j;
+                const int pnum = tpnum[q], dnum = tdnum[q], didx = tdidx[q];
+                if (pnum == 0) {
+                    if (dnum != 0) { dn += dnum; di = min(di, didx); }
+                } else {
+                    fk = tkey[q] & ~(7 << sh);
+                    pn += pnum;
+                    pi = min(pi, tpidx[q]);
+                    dn += dnum;
+                    di = min(di, didx);
+                }
+            }
+            gkey[g] = fk;
+            gpidx[g] = pi;
+            gpnum[g] = pn;
+            gdidx[g] = di;
+            gdnum[g] = dn;
+        }
+        __syncthreads();
+        // (2) inclusive scan of "new father group" flags (8 per new group of level d-1)
+        const int sh2 = 3 * (depth - d + 2);
+        unsigned carry = 0;
+        for (int b = 0; b < G; b += kLevelBlock) {
+            const int g = b + t;
+            const unsigned f = (g < G && g > 0) ? (((gkey[g - 1] >> sh2) != (gkey[g] >> sh2)) ? 8u : 0u) : 0u;
+            const unsigned incl = block_inclusive_scan_1024(f, s_warp);
+            if (g < G) gaddr[g] = carry + incl;
+            carry += s_warp[32];
+            __syncthreads();
+        }
+        // (3) size and offset of level d-1
+        int m1 = (d > 1) ? (int)carry + 8 : 1;
+        const int off1 = off + m;
+        if (off1 + m1 > node_cap) {
+            if (t == 0) atomicOr(&c->error, kErrCapacity);
+            m1 = 0;
+        }
+        if (t == 0) {
+            c->level_count[d - 1] = m1;
+            c->level_tmp_off[d - 1] = off1;
+            c->n_groups = G;
+        }
+        for (int i = t; i < m1; i += kLevelBlock) {
+            tkey[off1 + i] = 0;
+            tpidx[off1 + i] = 0;
+            tpnum[off1 + i] = 0;
+            tdidx[off1 + i] = 0;
+            tdnum[off1 + i] = 0;
+            tchild[off1 + i] = -1;
+        }
+        __syncthreads();
+        // (4) fathers into their slots of level d-1
+        const int off_group = off / 8;
+        const int sh3 = 3 * (depth - d + 1);
+        for (int g = t; g < G; g += kLevelBlock) {
+            const int sl = (int)gaddr[g] + ((gkey[g] >> sh3) & 7);
+            if (sl >= m1) continue;   // capacity overflow (flagged)
+            const int q = off1 + sl;
+            tkey[q] = gkey[g];
+            tpidx[q] = gpidx[g];
+            tpnum[q] = gpnum[g];
+            tdidx[q] = gdidx[g];
+            tdnum[q] = gdnum[g];
+            tchild[q] = 8 * g;
+            tparent_slot[off_group + g] = sl;
+        }
+        __syncthreads();
+    }
+}
+
+// 27-neighbour tables of levels 1..dmax in one CTA (levels in order: a level reads its
+// parents' table)
+__global__ void __launch_bounds__(kLevelBlock) k_neighbours_block(const Counters* c, int dmax, int depth,
+                                                                  const int* key, const int* parent,
+                                                                  const int* first_child, int* neigh, size_t stride) {
+    for (int d = 1; d <= dmax; ++d) {
+        const int m = c->level_count[d];
+        const int b = c->level_base[d];
+        for (int li = threadIdx.x; li < m; li += kLevelBlock) {
+            const int i = b + li;
+            const int son = (key[i] >> (3 * (depth - d))) & 7;
+            const int pa = parent[i];
+#pragma unroll
+            for (int k = 0; k < 27; ++k) {
+                int lp, lc;
+                nb_lut(son, k, lp, lc);
+                const int np = neigh[(size_t)lp * stride + pa];
+                int v = -1;
+                if (np != -1) {
+                    const int fc = first_child[np];
+                    v = (fc == -1) ? -1 : fc + lc;
+                }
+                neigh[(size_t)k * stride + i] = v;
+            }
+        }
+        __syncthreads();
+    }
+}
+
 __global__ void k_levels_done(Counters* c, int depth) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         int b = 0;
@@ -445,8 +593,10 @@ cudaError_t octree_build(Workspace& ws) {
     k_init_level<<<gn, kBlock, 0, s>>>(c, D, D, ws.tkey, ws.tpidx, ws.tpnum, ws.tdidx, ws.tdnum, ws.tchild);
     k_place_leaves<<<gp, kBlock, 0, s>>>(c, ws.ucode, ws.ufirst, ws.uaddr, ws.uslot, ws.tkey, ws.tpidx, ws.tpnum);
     k_point2node<<<gp, kBlock, 0, s>>>(c, ws.puid, ws.uslot, ws.point2node);
-    // levels D .. 1
-    for (int d = D; d >= 1; --d) {
+    // levels D .. dfuse+1 level by level across the GPU, the small levels near the root in
+    // one CTA
+    const int dfuse = D >= 9 ? D - 3 : D - 2;
+    for (int d = D; d >= 1 && d > dfuse; --d) {
         const int gg = grid_for(ws, ws.cap.dnodes / 8 + 1);
         k_group_aggregate<<<gg, kBlock, 0, s>>>(c, d, D, ws.tkey, ws.tpidx, ws.tpnum, ws.tdidx, ws.tdnum, ws.gkey,
                                                 ws.gpidx, ws.gpnum, ws.gdidx, ws.gdnum);
@@ -459,6 +609,10 @@ cudaError_t octree_build(Workspace& ws) {
                                               ws.tkey, ws.tpidx, ws.tpnum, ws.tdidx, ws.tdnum, ws.tchild,
                                               ws.tparent_slot);
     }
+    if (dfuse >= 1)
+        k_levels_block<<<1, kLevelBlock, 0, s>>>(c, dfuse, D, ws.tkey, ws.tpidx, ws.tpnum, ws.tdidx, ws.tdnum, ws.tchild,
+                                                 ws.tparent_slot, ws.gkey, ws.gpidx, ws.gpnum, ws.gdidx, ws.gdnum,
+                                                 ws.gaddr, ws.cap.nodes);
     k_levels_done<<<1, 1, 0, s>>>(c, D);
     const int gm = grid_for(ws, ws.cap.nodes);
     k_finalize_nodes<<<gm, kBlock, 0, s>>>(c, D, ws.tkey, ws.tpidx, ws.tpnum, ws.tdidx, ws.tdnum, ws.tchild,
@@ -466,7 +620,9 @@ cudaError_t octree_build(Workspace& ws) {
                                            ws.didx, ws.dnum, ws.ndepth, ws.enc, ws.ctr_x, ws.ctr_y, ws.ctr_z);
     const size_t stride = (size_t)ws.cap.nodes;
     k_root_neighbours<<<1, 32, 0, s>>>(ws.neigh, stride);
-    for (int d = 1; d <= D; ++d)
+    if (dfuse >= 1)
+        k_neighbours_block<<<1, kLevelBlock, 0, s>>>(c, dfuse, D, ws.key, ws.parent, ws.first_child, ws.neigh, stride);
+    for (int d = (dfuse >= 1 ? dfuse + 1 : 1); d <= D; ++d)
         k_neighbours<<<gm, kBlock, 0, s>>>(c, d, D, ws.key, ws.parent, ws.first_child, ws.neigh, stride);
     return cudaGetLastError();
 }
