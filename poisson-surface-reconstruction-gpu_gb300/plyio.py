@@ -1,0 +1,149 @@
+"""Point-cloud input and mesh output files (host side, numpy).
+
+The reference reads its inputs through PCL (mesh/PoissonReconstruction.cpp:63-188:
+`.pcd`, `.ply`, `.txt`) and only draws its mesh.  These readers cover the oriented
+point formats of its `PointCloudData/` fixtures without PCL:
+
+* PLY (ascii, binary_little_endian, binary_big_endian) with vertex properties x, y, z,
+  nx, ny, nz and optionally red, green, blue (any numeric types);
+* whitespace-separated text, one point per line: x y z nx ny nz [r g b].
+
+`write_mesh_ply` writes a reconstructed mesh (binary little endian; optional per-vertex
+normals and colours), in world coordinates when given the call's center / scale.
+"""
+import numpy as np
+
+_PLY_TYPES = {"char": "i1", "int8": "i1", "uchar": "u1", "uint8": "u1", "short": "i2", "int16": "i2",
+              "ushort": "u2", "uint16": "u2", "int": "i4", "int32": "i4", "uint": "u4", "uint32": "u4",
+              "float": "f4", "float32": "f4", "double": "f8", "float64": "f8"}
+
+
+def _read_header(f):
+    if f.readline().strip() != b"ply":
+        raise ValueError("not a PLY file")
+    fmt, elements = None, []
+    while True:
+        line = f.readline()
+        if not line:
+            raise ValueError("PLY header without end_header")
+        w = line.decode("ascii", "replace").split()
+        if not w or w[0] in ("comment", "obj_info"):
+            continue
+        if w[0] == "format":
+            fmt = w[1]
+        elif w[0] == "element":
+            elements.append([w[1], int(w[2]), []])
+        elif w[0] == "property":
+            if w[1] == "list":
+                elements[-1][2].append((w[4], ("list", w[2], w[3])))
+            else:
+                elements[-1][2].append((w[2], w[1]))
+        elif w[0] == "end_header":
+            return fmt, elements
+
+
+def read_ply_points(path):
+    """Returns (xyz float32 N x 3, normals float32 N x 3, rgb uint8 N x 3 or None)."""
+    with open(path, "rb") as f:
+        fmt, elements = _read_header(f)
+        if fmt not in ("ascii", "binary_little_endian", "binary_big_endian"):
+            raise ValueError(f"PLY format {fmt!r} not supported")
+        end = "<" if fmt == "binary_little_endian" else ">"
+        vertex = None
+        for name, count, props in elements:
+            if any(isinstance(t, tuple) for _, t in props):
+                if name == "vertex":
+                    raise ValueError("list properties in the vertex element are not supported")
+                if vertex is None:
+                    raise ValueError("elements with lists before the vertex element are not supported")
+                break
+            if fmt == "ascii":
+                data = np.loadtxt(f, max_rows=count, ndmin=2) if count else np.zeros((0, len(props)))
+                cols = {p: data[:, i] for i, (p, _) in enumerate(props)}
+            else:
+                dt = np.dtype([(p, end + _PLY_TYPES[t]) for p, t in props])
+                arr = np.frombuffer(f.read(dt.itemsize * count), dtype=dt, count=count)
+                cols = {p: arr[p] for p, _ in props}
+            if name == "vertex":
+                vertex = cols
+                break
+        if vertex is None:
+            raise ValueError("PLY file without a vertex element")
+    for k in ("x", "y", "z", "nx", "ny", "nz"):
+        if k not in vertex:
+            raise ValueError(f"PLY vertex element lacks '{k}' (oriented points are required)")
+    xyz = np.stack([vertex["x"], vertex["y"], vertex["z"]], 1).astype(np.float32)
+    nrm = np.stack([vertex["nx"], vertex["ny"], vertex["nz"]], 1).astype(np.float32)
+    rgb = None
+    if all(k in vertex for k in ("red", "green", "blue")):
+        rgb = np.clip(np.stack([vertex["red"], vertex["green"], vertex["blue"]], 1), 0, 255).astype(np.uint8)
+    return xyz, nrm, rgb
+
+
+def read_txt_points(path):
+    """x y z nx ny nz [r g b] per line (r g b in 0..255)."""
+    data = np.loadtxt(path, ndmin=2)
+    if data.shape[1] < 6:
+        raise ValueError("text points need at least 6 columns: x y z nx ny nz")
+    rgb = np.clip(data[:, 6:9], 0, 255).astype(np.uint8) if data.shape[1] >= 9 else None
+    return data[:, :3].astype(np.float32), data[:, 3:6].astype(np.float32), rgb
+
+
+def read_points(path):
+    p = str(path).lower()
+    if p.endswith(".ply"):
+        return read_ply_points(path)
+    if p.endswith((".txt", ".xyz", ".xyzn")):
+        return read_txt_points(path)
+    raise ValueError(f"unsupported point file {path}")
+
+
+def write_mesh_ply(path, vertices, triangles, colors=None, normals=None, center=None, scale=None):
+    """Binary little-endian PLY.  vertices in the unit cube of the reconstruction are mapped
+    to world coordinates (center + v * scale) when center and scale are given; colours are
+    floats in [0, 1] (written as uchar)."""
+    v = np.asarray(vertices, np.float32).reshape(-1, 3)
+    if center is not None and scale is not None:
+        v = (np.asarray(center, np.float32) + v * np.float32(scale)).astype(np.float32)
+    t = np.asarray(triangles, np.int32).reshape(-1, 3)
+    fields = [("x", "<f4"), ("y", "<f4"), ("z", "<f4")]
+    if normals is not None:
+        fields += [("nx", "<f4"), ("ny", "<f4"), ("nz", "<f4")]
+    if colors is not None:
+        fields += [("red", "u1"), ("green", "u1"), ("blue", "u1")]
+    rec = np.zeros(v.shape[0], dtype=np.dtype(fields))
+    rec["x"], rec["y"], rec["z"] = v[:, 0], v[:, 1], v[:, 2]
+    if normals is not None:
+        n = np.asarray(normals, np.float32).reshape(-1, 3)
+        rec["nx"], rec["ny"], rec["nz"] = n[:, 0], n[:, 1], n[:, 2]
+    if colors is not None:
+        c = np.clip(np.rint(np.asarray(colors, np.float32).reshape(-1, 3) * 255.0), 0, 255).astype(np.uint8)
+        rec["red"], rec["green"], rec["blue"] = c[:, 0], c[:, 1], c[:, 2]
+    faces = np.zeros(t.shape[0], dtype=np.dtype([("n", "u1"), ("i", "<i4", (3,))]))
+    faces["n"] = 3
+    faces["i"] = t
+    head = ["ply", "format binary_little_endian 1.0", f"element vertex {v.shape[0]}"]
+    head += [f"property float {k}" for k in ("x", "y", "z")]
+    if normals is not None:
+        head += [f"property float {k}" for k in ("nx", "ny", "nz")]
+    if colors is not None:
+        head += [f"property uchar {k}" for k in ("red", "green", "blue")]
+    head += [f"element face {t.shape[0]}", "property list uchar int vertex_indices", "end_header"]
+    with open(path, "wb") as f:
+        f.write(("\n".join(head) + "\n").encode("ascii"))
+        f.write(rec.tobytes())
+        f.write(faces.tobytes())
+
+
+def read_mesh_ply(path):
+    """Reads back a triangle mesh written by write_mesh_ply (binary little endian)."""
+    with open(path, "rb") as f:
+        fmt, elements = _read_header(f)
+        if fmt != "binary_little_endian":
+            raise ValueError("only binary_little_endian meshes are read back")
+        (vn, vc, vp), (fn, fc, fp) = elements[0], elements[1]
+        dt = np.dtype([(p, "<" + _PLY_TYPES[t]) for p, t in vp])
+        v = np.frombuffer(f.read(dt.itemsize * vc), dtype=dt, count=vc)
+        faces = np.frombuffer(f.read(13 * fc), dtype=np.dtype([("n", "u1"), ("i", "<i4", (3,))]), count=fc)
+    xyz = np.stack([v["x"], v["y"], v["z"]], 1)
+    return xyz, faces["i"].copy(), v
