@@ -55,12 +55,11 @@ public:
         ensure_staging(count);
         float* xyz = staging_;
         float* nrm = staging_ + 3 * (size_t)count;
-        // strided 2-D copies gather the AoS fields into the SoA input (no kernel needed)
-        check(cudaMemcpy2DAsync(xyz, 12, (const char*)device_surfels + 16, sizeof(DepthSurfel), 12, count,
-                                cudaMemcpyDeviceToDevice, stream));
-        check(cudaMemcpy2DAsync(nrm, 12, (const char*)device_surfels + 32, sizeof(DepthSurfel), 12, count,
-                                cudaMemcpyDeviceToDevice, stream));
-        Solve(xyz, nrm, nullptr, count, PSR_DEVICE, stream);
+        // colour from ColorAndTime.xyz when the handle transfers colours
+        uint8_t* rgb = cfg_.compute_colors ? (uint8_t*)(staging_ + 6 * (size_t)count) : nullptr;
+        psr_status s = psr_surfels_to_points(device_surfels, count, xyz, nrm, rgb, stream);
+        if (s != PSR_OK) throw std::runtime_error(std::string("psr_surfels_to_points: ") + psr_status_string(s));
+        Solve(xyz, nrm, rgb, count, PSR_DEVICE, stream);
     }
 
     // Oriented points (host or device), optional 8-bit colour.
@@ -104,7 +103,7 @@ private:
         if (count <= staging_count_) return;
         if (staging_) cudaFree(staging_);
         staging_ = nullptr;
-        check(cudaMalloc(&staging_, 6 * sizeof(float) * (size_t)count));
+        check(cudaMalloc(&staging_, 6 * sizeof(float) * (size_t)count + 3 * (size_t)count));
         staging_count_ = count;
     }
     psr_config cfg_{};

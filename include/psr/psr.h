@@ -142,6 +142,14 @@ psr_status psr_submit(psr_handle* h, const psr_points* points, const psr_options
 psr_status psr_poll(psr_handle* h);
 psr_status psr_wait(psr_handle* h);
 
+/* Input adaptor: device array of `count` DepthSurfel records (base/CommonTypes.h:113-118,
+ * 64 bytes each) -> device SoA arrays for psr_points: xyz and normals (3 * count floats),
+ * and rgb (3 * count bytes, round(255 * ColorAndTime.xyz) clamped) unless rgb is NULL.
+ * Replaces getCoordinateAndNormalKernel (mesh/BuildOctree.cu:135-143); enqueued on
+ * `stream` (a cudaStream_t or NULL), no host wait. */
+psr_status psr_surfels_to_points(const void* surfels, int count, float* xyz, float* normals, uint8_t* rgb,
+                                 void* stream);
+
 /* Device memory held by the handle (bytes), for admission under a memory budget. */
 psr_status psr_memory_bytes(const psr_handle* h, size_t* bytes);
 

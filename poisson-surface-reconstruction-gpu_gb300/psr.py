@@ -22,7 +22,7 @@ PSR_HOST, PSR_DEVICE = 0, 1
 # every function declared in include/psr/psr.h
 EXPORTED = ["psr_config_default", "psr_create", "psr_destroy", "psr_reconstruct", "psr_submit", "psr_poll",
             "psr_wait", "psr_memory_bytes", "psr_get_stats", "psr_debug_array", "psr_status_string",
-            "psr_last_error", "psr_morton_sort_noalloc"]
+            "psr_last_error", "psr_surfels_to_points", "psr_morton_sort_noalloc"]
 
 
 class PsrConfig(ctypes.Structure):
@@ -84,6 +84,8 @@ def load_library(path=None):
     L.psr_poll.argtypes = [ctypes.c_void_p]
     L.psr_wait.argtypes = [ctypes.c_void_p]
     L.psr_memory_bytes.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t)]
+    L.psr_surfels_to_points.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_void_p, ctypes.c_void_p]
     L.psr_get_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(PsrStats)]
     L.psr_debug_array.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_size_t,
                                   ctypes.POINTER(ctypes.c_size_t)]
