@@ -240,9 +240,10 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     A.add(ws.s_neigh, 27 * (size_t)subn); A.add(ws.s_depth, (size_t)subn); A.add(ws.s_root, (size_t)subn);
     A.add(ws.s_group, (size_t)subn);
     A.add(ws.s_jump, (size_t)subn);
+    A.add(ws.s_sign, (size_t)subn);
     A.add(ws.s_cx, (size_t)subn); A.add(ws.s_cy, (size_t)subn); A.add(ws.s_cz, (size_t)subn);
     A.add(ws.s_vtx, 8 * (size_t)subd); A.add(ws.s_edge, 12 * (size_t)subd);
-    A.add(ws.s_vmask, (size_t)subd); A.add(ws.s_emask, (size_t)subd);
+    A.add(ws.s_vmask, (size_t)subd); A.add(ws.s_emask, (size_t)subd); A.add(ws.s_live, (size_t)subd);
     A.add(ws.sv_x, 8 * (size_t)subd); A.add(ws.sv_y, 8 * (size_t)subd); A.add(ws.sv_z, 8 * (size_t)subd);
     A.add(ws.sv_owner, 8 * (size_t)subd); A.add(ws.sv_kind, 8 * (size_t)subd); A.add(ws.sv_value, 8 * (size_t)subd);
     A.add(ws.se_owner, 12 * (size_t)subd); A.add(ws.se_kind, 12 * (size_t)subd); A.add(ws.se_cross, 12 * (size_t)subd);
@@ -655,6 +656,13 @@ psr_status psr_debug_array(psr_handle* h, const char* name, void* dst, size_t ds
     else if (nm == "mesh_t") one(ws.mesh_t, 12 * (size_t)c.n_mesh_triangles);
     else if (nm == "mesh_c") one(ws.mesh_c, 12 * (size_t)c.n_mesh_vertices);
     else if (nm == "mesh_n") one(ws.mesh_n, 12 * (size_t)c.n_mesh_vertices);
+    else if (nm == "s_key") one(ws.s_key, 4 * (size_t)c.n_sub_nodes);
+    else if (nm == "s_depth") one(ws.s_depth, 4 * (size_t)c.n_sub_nodes);
+    else if (nm == "s_sign") one(ws.s_sign, (size_t)c.n_sub_nodes);
+    else if (nm == "sv_value") one(ws.sv_value, 4 * (size_t)c.n_sub_vertices);
+    else if (nm == "sv_owner") one(ws.sv_owner, 4 * (size_t)c.n_sub_vertices);
+    else if (nm == "s_cube_class") one(ws.s_cube_class, 4 * (size_t)c.n_sub_dnodes);
+    else if (nm == "s_vtx") rows(ws.s_vtx, 8, 4 * (size_t)c.n_sub_dnodes, 4 * (size_t)ws.cap.sub_dnodes);
     else if (nm == "counters") { if (bytes) *bytes = sizeof(Counters); if (dst && dst_bytes >= sizeof(Counters)) memcpy(dst, &c, sizeof(Counters)); return PSR_OK; }
     else return fail(h, PSR_INVALID_INPUT, "unknown array name");
     size_t total = 0;

@@ -711,14 +711,155 @@ __global__ void __launch_bounds__(kBlock) k_sub_build(const Counters* c, int dep
     }
 }
 
-// computeRebuildNeighbor (:669-696) for all subdivision nodes at depth d
+// ---- certain-sign cells -------------------------------------------------------------
+// Subdivision replaces a coarse leaf that carries surface by all of its depth-D cells, but
+// the surface crosses few of them.  A cell where F - iso provably keeps one sign has no
+// crossing edge and no triangle, so it needs no vertex, edge or cube record; its subtree
+// inherits the sign.  The test below is conservative, so the mesh is unchanged.
+//
+// On the closed cell (centre c, half width h = 2^-(d+1)) of a sub node s at depth d, F is
+// the sum over the levels l <= d of the 27 neighbour terms y_k B_k of s's ancestor at l
+// (y = 0 for absent nodes and for sub nodes that are not roots), provided no octree node
+// deeper than d reaches the cell: that holds when none of s's 27 neighbours is an octree
+// node with children.  B_k = b(x) b(y) b(z) with b(t) = 4/3 (3/4 - t^2) for |t| < 1/2,
+// 2/3 (3/2 - |t|)^2 for |t| < 3/2 (t in level widths): b <= 1, |b'| <= 4/3, |b''| <= 8/3.
+// The translates of one level sum to (4/3)^3 on the ancestor's cell, so every derivative of
+// F_l there is sum_k (y_k - m) dB_k for any constant m; take m = the mid-range of the y_k
+// and S_l = sum_k |y_k - m|.  For |p - c|_inf <= h:
+//   level d (first order):   |F_d(p) - F_d(c)| <= 3 h (4/3) 2^d S_d = 2 S_d
+//   levels l < d (Taylor):   |F_l(p) - F_l(c) - grad F_l(c) . (p - c)|
+//                              <= h^2 / 2 (3 (8/3) + 6 (4/3)^2) 4^l S_l = 7/3 4^(l-d) S_l
+// so |F(p) - F(c)| <= h |G|_1 + 2 S_d + sum_{l<d} 7/3 4^(l-d) S_l, G = sum_{l<d} grad F_l(c).
+// Float vertex values are sums of the same nonzero terms (at most 27 (D+1)), within
+// ~1.7e-5 sum |y| of the exact value, as are the float F(c) and h G here; the test keeps a
+// margin of 1e-4 (sum |y| + |iso|) beyond the bound.
+struct SignAcc {
+    float val = 0.0f, gx = 0.0f, gy = 0.0f, gz = 0.0f, rem = 0.0f, mag = 0.0f;
+};
+
+// b and h db/dx of the translate `idx` at x (hs = h 2^l, the half width in level widths)
+__device__ __forceinline__ void basis_grad(int idx, float x, float hs, float& b, float& g) {
+    const int l = ilog2_dev(idx + 1);
+    const int off = idx + 1 - (1 << l);
+    const float c = __fmul_rn(__fadd_rn((float)off, 0.5f), __int_as_float((127 - l) << 23));
+    const float t = __fmul_rn(__fsub_rn(x, c), (float)(1 << l));
+    const float a = fabsf(t);
+    if (a < 0.5f) {
+        b = (0.75f - t * t) * (4.0f / 3.0f);
+        g = -(8.0f / 3.0f) * t * hs;
+    } else if (a < 1.5f) {
+        const float u = 1.5f - a;
+        b = u * u * (2.0f / 3.0f);
+        g = copysignf((4.0f / 3.0f) * u * hs, -t);
+    } else {
+        b = 0.0f;
+        g = 0.0f;
+    }
+}
+
+// one level: the ancestor's function indices (ox, oy, oz), its 27 values y; l == d takes
+// the first-order bound, coarser levels the Taylor one (hs = h 2^l)
+__device__ __forceinline__ void sign_level(const float (&y)[27], int ox, int oy, int oz, float qx, float qy,
+                                           float qz, int l, int d, SignAcc& A) {
+    const float hs = __int_as_float((127 + l - d - 1) << 23);   // h 2^l = 2^(l-d-1)
+    float bx[3], by[3], bz[3], dx[3], dy[3], dz[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        basis_grad(ox - 1 + j, qx, hs, bx[j], dx[j]);
+        basis_grad(oy - 1 + j, qy, hs, by[j], dy[j]);
+        basis_grad(oz - 1 + j, qz, hs, bz[j], dz[j]);
+    }
+    float lo = y[0], hi = y[0];
+#pragma unroll
+    for (int k = 1; k < 27; ++k) { lo = fminf(lo, y[k]); hi = fmaxf(hi, y[k]); }
+    const float m = 0.5f * (lo + hi);
+    float dev = 0.0f, ab = 0.0f, gx = 0.0f, gy = 0.0f, gz = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 27; ++k) {
+        const int i = k / 9, j = (k / 3) % 3, kk = k % 3;
+        const float yk = y[k];
+        A.val = fmaf(yk, bx[i] * by[j] * bz[kk], A.val);
+        gx = fmaf(yk, dx[i] * by[j] * bz[kk], gx);
+        gy = fmaf(yk, bx[i] * dy[j] * bz[kk], gy);
+        gz = fmaf(yk, bx[i] * by[j] * dz[kk], gz);
+        dev += fabsf(yk - m);
+        ab += fabsf(yk);
+    }
+    A.mag += ab;
+    if (l >= d) {
+        A.rem = fmaf(2.0f, dev, A.rem);
+    } else {
+        A.gx += gx;
+        A.gy += gy;
+        A.gz += gz;
+        A.rem = fmaf((7.0f / 3.0f) * 4.0f * hs * hs, dev, A.rem);   // 7/3 4^(l-d) = 28/3 hs^2
+    }
+}
+
+// sign of F - iso on the closed cell of sub node s at depth d; sn = s_jump[s], the nearest
+// node at or above s with a contributing neighbour
+__device__ __forceinline__ int sub_cell_sign(int s, int d, int sn, int depth, const int* neigh, size_t stride,
+                                             const int* parent, const int* s_neigh, size_t sstride,
+                                             const int* s_parent, const int* s_root, const int* s_jump,
+                                             const int* s_depth, const float* s_cx, const float* s_cy,
+                                             const float* s_cz, const int* enc, const float* x, float iso,
+                                             int na) {
+    const float qx = s_cx[s], qy = s_cy[s], qz = s_cz[s];
+    SignAcc A;
+    float y[27];
+    int now;
+    // subdivision levels that carry a value (s_jump hops over the others)
+    while (true) {
+        const int l = s_depth[sn];
+        const float sc = (float)(1 << l);
+        const int base = (1 << l) - 1;
+        const int ox = base + (int)__fmul_rn(s_cx[sn], sc);
+        const int oy = base + (int)__fmul_rn(s_cy[sn], sc);
+        const int oz = base + (int)__fmul_rn(s_cz[sn], sc);
+#pragma unroll
+        for (int k = 0; k < 27; ++k) {
+            int v = s_neigh[(size_t)k * sstride + sn];
+            if (v >= na) v = s_root[v - na];
+            y[k] = (v >= 0) ? x[v] : 0.0f;
+        }
+        sign_level(y, ox, oy, oz, qx, qy, qz, l, d, A);
+        now = s_parent[sn];
+        if (now < na) break;
+        sn = s_jump[now - na];
+    }
+    // octree levels above the root
+    while (now >= 0) {
+        int ox, oy, oz;
+        decode_fn_index(enc[now], depth, ox, oy, oz);
+        const int l = ilog2_dev(ox + 1);
+#pragma unroll
+        for (int k = 0; k < 27; ++k) {
+            const int v = neigh[(size_t)k * stride + now];
+            y[k] = (v >= 0) ? x[v] : 0.0f;
+        }
+        sign_level(y, ox, oy, oz, qx, qy, qz, l, d, A);
+        now = parent[now];
+    }
+    const float var = fabsf(A.gx) + fabsf(A.gy) + fabsf(A.gz) + A.rem;
+    const float bound = var * 1.001f + 1e-4f * (A.mag + fabsf(iso));
+    const float f = A.val - iso;
+    if (f > bound) return 1;
+    if (f < -bound) return -1;
+    return 0;
+}
+
+// computeRebuildNeighbor (:669-696) for all subdivision nodes at depth d, and the certain
+// sign of each node's cell (inherited from a parent with a certain sign, whose subtree needs
+// no neighbours; else tested above once the node lies below its root)
 __global__ void __launch_bounds__(kBlock) k_sub_neighbours(const Counters* c, int d, int depth, const int* groups,
                                                            const int* neigh, size_t stride, const int* first_child,
                                                            const int* ov_group, const int* ov_sub, const int* s_key,
                                                            const int* s_parent, const int* s_first_child,
                                                            const int* s_depth, const int* s_group, const int* s_root,
-                                                           int* s_neigh, int* s_jump, size_t sstride,
-                                                           int na) {
+                                                           int* s_neigh, int* s_jump, signed char* s_sign,
+                                                           size_t sstride, const int* parent, const float* s_cx,
+                                                           const float* s_cy, const float* s_cz, const int* enc,
+                                                           const float* x, int na) {
     // Depth-d nodes only.  Groups are ordered by root depth, so those reaching depth d are
     // a prefix 0..gd-1, and the depth-d nodes of groups before g number
     // dnode_prefix(g) / 8^(D-d) (every such group has full subtrees below its roots).
@@ -746,10 +887,15 @@ __global__ void __launch_bounds__(kBlock) k_sub_neighbours(const Counters* c, in
         const int* G = groups + (size_t)g * kGroupRec;
         const int local = t - (G[5] >> sh);
         const int s = G[3] + sub_level_off(G[0], G[2], d) + local;
+        const int pa = s_parent[s];
+        if (pa >= na) {
+            const int ps = s_sign[pa - na];
+            if (ps != 0) { s_sign[s] = (signed char)ps; continue; }
+        }
         const bool at_root_depth = (d == G[0]);
         int contrib = 0;
+        bool deeper = false;   // an octree neighbour with children reaches below depth d
         const int son = (s_key[s] >> (3 * (depth - d))) & 7;
-        const int pa = s_parent[s];
         // Position inside the root's cell: rel = the Morton code of the node's L = d - rd
         // levels below its root (x = bit 2, y = bit 1, z = bit 0 of every triple).  A
         // neighbour inside the same root's cell is the node at the shifted code in the same
@@ -771,13 +917,14 @@ __global__ void __launch_bounds__(kBlock) k_sub_neighbours(const Counters* c, in
             ok[a][1] = true;
             ok[a][2] = cm != M;
         }
+        int nb[27];
 #pragma unroll
         for (int k = 0; k < 27; ++k) {
             const int ix = k / 9, iy = (k / 3) % 3, iz = k % 3;
             if (ok[0][ix] && ok[1][iy] && ok[2][iz]) {
                 const unsigned relk = cmp[0][ix] | cmp[1][iy] | cmp[2][iz];
                 const int v = na + s + (int)relk - (int)rel;
-                s_neigh[(size_t)k * sstride + s] = v;
+                nb[k] = v;
                 if (at_root_depth) contrib = 1;   // the node itself, a root
                 continue;
             }
@@ -793,20 +940,29 @@ __global__ void __launch_bounds__(kBlock) k_sub_neighbours(const Counters* c, in
                     } else {
                         const int fc = first_child[np];
                         v = (fc == -1) ? -1 : fc + lc;
+                        if (v >= 0 && d < depth && first_child[v] != -1) deeper = true;
                     }
                 } else {
                     const int fc = s_first_child[np - na];
                     v = (fc == -1) ? -1 : fc + lc;
                 }
             }
-            s_neigh[(size_t)k * sstride + s] = v;
+            nb[k] = v;
             // a contributing neighbour is an octree node or a root; the subdivision nodes at a
             // group's root depth are exactly its roots, and deeper ones are never roots
             if (v >= 0 && (v < na || at_root_depth)) contrib = 1;
         }
+#pragma unroll
+        for (int k = 0; k < 27; ++k) s_neigh[(size_t)k * sstride + s] = nb[k];
         // nearest contributing node on the path to the root (itself when it contributes;
         // roots always do): lets the value chains skip non-contributing levels in one hop
-        s_jump[s] = contrib ? s : ((pa >= na) ? s_jump[pa - na] : s);
+        const int jump = contrib ? s : ((pa >= na) ? s_jump[pa - na] : s);
+        s_jump[s] = jump;
+        int sg = 0;
+        if (!at_root_depth && !deeper)
+            sg = sub_cell_sign(s, d, jump, depth, neigh, stride, parent, s_neigh, sstride, s_parent, s_root, s_jump,
+                               s_depth, s_cx, s_cy, s_cz, enc, x, c->iso, na);
+        s_sign[s] = (signed char)sg;
     }
 }
 
@@ -824,21 +980,29 @@ __device__ __forceinline__ int sub_dnode_to_node(int o, const int* groups, int n
     return G[3] + sub_level_off(G[0], G[2], depth) + (o - G[5]);
 }
 
-// vertex ownership among subdivision nodes only (initSubdivideVertexOwner :698-763)
+// vertex ownership among subdivision nodes only (initSubdivideVertexOwner :698-763).  Cells
+// with a certain sign take no part: a corner is owned by the smallest-key cell around it
+// without one.  Every corner of such a cell still gets exactly one record, the records of
+// crossing edges keep their owners (every cell around a crossing edge has a sign change),
+// and a vertex value does not depend on the cell that evaluates it (the same nonzero terms
+// in the same order), so the mesh is unchanged.
 __global__ void __launch_bounds__(kBlock) k_sub_vertex_owner(const Counters* c, int depth, const int* groups,
                                                              const int* s_key, const int* s_neigh, size_t sstride,
-                                                             unsigned char* s_vmask, int na) {
+                                                             const signed char* s_sign, unsigned char* s_vmask,
+                                                             unsigned char* s_live, int na) {
     const int SD = c->n_sub_dnodes;
     const int ng = c->n_groups;
     PSR_GRID_STRIDE(o, SD) {
         const int s = sub_dnode_to_node(o, groups, ng, depth);
+        if (s_sign[s] != 0) { s_vmask[o] = 0; s_live[o] = 0; continue; }
+        s_live[o] = 1;
         const int myk = s_key[s];
         unsigned smaller = 0;
 #pragma unroll
         for (int k = 0; k < 27; ++k) {
             if (k == 13) continue;
             const int nb = s_neigh[(size_t)k * sstride + s];
-            if (nb >= na && s_key[nb - na] < myk) smaller |= 1u << k;
+            if (nb >= na && s_sign[nb - na] == 0 && s_key[nb - na] < myk) smaller |= 1u << k;
         }
         unsigned m = 0;
 #pragma unroll
@@ -911,13 +1075,16 @@ __global__ void __launch_bounds__(kBlock) k_sub_vertex_maintain(const Counters* 
     }
 }
 
-// edge ownership among subdivision nodes only (initSubdivideEdgeArray :812-886)
+// edge ownership among subdivision nodes only (initSubdivideEdgeArray :812-886), among the
+// cells without a certain sign as for the vertices
 __global__ void __launch_bounds__(kBlock) k_sub_edge_owner(const Counters* c, int depth, const int* groups,
                                                            const int* s_key, const int* s_neigh, size_t sstride,
+                                                           const unsigned char* s_live, const signed char* s_sign,
                                                            unsigned short* s_emask, int na) {
     const int SD = c->n_sub_dnodes;
     const int ng = c->n_groups;
     PSR_GRID_STRIDE(o, SD) {
+        if (!s_live[o]) { s_emask[o] = 0; continue; }
         const int s = sub_dnode_to_node(o, groups, ng, depth);
         const int myk = s_key[s];
         unsigned smaller = 0;
@@ -926,7 +1093,7 @@ __global__ void __launch_bounds__(kBlock) k_sub_edge_owner(const Counters* c, in
             if (k == 13 || k == 0 || k == 2 || k == 6 || k == 8 || k == 18 || k == 20 || k == 24 || k == 26)
                 continue;   // corner-diagonal cells touch no edge
             const int nb = s_neigh[(size_t)k * sstride + s];
-            if (nb >= na && s_key[nb - na] < myk) smaller |= 1u << k;
+            if (nb >= na && s_sign[nb - na] == 0 && s_key[nb - na] < myk) smaller |= 1u << k;
         }
         unsigned m = 0;
 #pragma unroll
@@ -1090,9 +1257,11 @@ struct SubCubeLoad {
     const int* s_vtx;
     size_t dstride;
     const float* vvalue;
+    const unsigned char* live;
     int* cube_class;
     unsigned* err;
     __device__ unsigned operator()(int o) const {
+        if (!live[o]) { cube_class[o] = 0; return 0u; }   // certain sign: no triangle
         int cls = 0;
 #pragma unroll
         for (int q = 0; q < 8; ++q)
@@ -1349,10 +1518,12 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
     for (int d = 1; d <= D; ++d)
         k_sub_neighbours<<<gs, kBlock, 0, s>>>(c, d, D, mb.groups, ws.neigh, stride, ws.first_child, mb.ov_group,
                                                mb.ov_sub, ws.s_key, ws.s_parent, ws.s_first_child, ws.s_depth,
-                                               ws.s_group, ws.s_root, ws.s_neigh, ws.s_jump, sstride, na);
-    cudaMemsetAsync(ws.s_vtx, 0, sizeof(int) * 8 * dstride, s);
-    cudaMemsetAsync(ws.s_edge, 0, sizeof(int) * 12 * dstride, s);
-    k_sub_vertex_owner<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.s_key, ws.s_neigh, sstride, ws.s_vmask, na);
+                                               ws.s_group, ws.s_root, ws.s_neigh, ws.s_jump, ws.s_sign, sstride,
+                                               ws.parent, ws.s_cx, ws.s_cy, ws.s_cz, ws.enc, ws.xsol, na);
+    // s_vtx / s_edge need no clearing: every slot of a cell without a certain sign is written
+    // by the owner of that vertex / edge, and no other cell's slots are read
+    k_sub_vertex_owner<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.s_key, ws.s_neigh, sstride, ws.s_sign, ws.s_vmask,
+                                             ws.s_live, na);
     e = launch_scan<2>(PopcLoad8{ws.s_vmask},
                     SubVertexStore{ws.s_vmask, mb.groups, &c->n_groups, D, ws.s_cx, ws.s_cy, ws.s_cz, ws.sv_x, ws.sv_y,
                                    ws.sv_z, ws.sv_owner, ws.sv_kind, 8 * ws.cap.sub_dnodes, na, err},
@@ -1360,7 +1531,8 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
     if (e != cudaSuccess) return e;
     k_sub_vertex_maintain<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.s_group, ws.s_neigh, sstride, ws.s_depth, ws.sv_owner,
                                                 ws.sv_kind, ws.s_vtx, dstride, na);
-    k_sub_edge_owner<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.s_key, ws.s_neigh, sstride, ws.s_emask, na);
+    k_sub_edge_owner<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.s_key, ws.s_neigh, sstride, ws.s_live, ws.s_sign,
+                                           ws.s_emask, na);
     e = launch_scan<2>(PopcLoad16{ws.s_emask},
                     SubEdgeStore{ws.s_emask, mb.groups, &c->n_groups, D, ws.se_owner, ws.se_kind, ws.se_dn,
                                  12 * ws.cap.sub_dnodes, na, err},
@@ -1382,12 +1554,12 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
                     &c->n_sub_edges, 0, ws.scan, total, err, s, ScanCount{&c->n_sub_cross, ws.part_cap_v});
     if (e != cudaSuccess) return e;
     // triangle prefix per D-level sub node
-    e = launch_scan<2>(SubCubeLoad{ws.s_vtx, dstride, ws.sv_value, ws.s_cube_class, err}, StoreExclusive{mb.tri_of_dnode},
+    e = launch_scan<2>(SubCubeLoad{ws.s_vtx, dstride, ws.sv_value, ws.s_live, ws.s_cube_class, err}, StoreExclusive{mb.tri_of_dnode},
                     &c->n_sub_dnodes, 0, ws.scan, total, err, s, ScanCount{&c->n_sub_tri, ws.part_cap_t});
     if (e != cudaSuccess) return e;
     k_part_table<<<grid_for(ws, 1 << 16), kBlock, 0, s>>>(c, mb.groups, mb.edge_of_dnode, ws.se_cross, mb.tri_of_dnode,
                                  mb.group_cross0, mb.parts);
-    e = launch_scan<2>(SubCubeLoad{ws.s_vtx, dstride, ws.sv_value, ws.s_cube_class, err},
+    e = launch_scan<2>(SubCubeLoad{ws.s_vtx, dstride, ws.sv_value, ws.s_live, ws.s_cube_class, err},
                     SubCubeStore{ws.s_cube_class, ws.s_edge, dstride, ws.se_cross, mb.group_cross0, mb.groups,
                                  &c->n_groups, ws.part_t, &c->n_tri, ws.part_cap_t, err},
                     &c->n_sub_dnodes, 0, ws.scan, total, err, s);

@@ -123,9 +123,11 @@ struct Workspace {
     int *s_key, *s_parent, *s_first_child, *s_neigh, *s_depth, *s_root;   // s_neigh: [27][cap.sub_nodes]
     int* s_group;
     int* s_jump;            // nearest sub-node on the path to the root with a neighbour carrying a value
+    signed char* s_sign;    // +1 / -1: F - iso keeps that sign on the whole closed cell; 0: not known
     float *s_cx, *s_cy, *s_cz;
     int *s_vtx, *s_edge;    // [8|12][cap.sub_dnodes] for D-level subdivision nodes
     unsigned char* s_vmask;
+    unsigned char* s_live;  // per D-level sub node: 1 unless its cell has a certain sign
     unsigned short* s_emask;
     float *sv_x, *sv_y, *sv_z;
     int *sv_owner, *sv_kind;
