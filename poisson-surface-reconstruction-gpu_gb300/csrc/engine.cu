@@ -659,6 +659,14 @@ psr_status psr_debug_array(psr_handle* h, const char* name, void* dst, size_t ds
     else if (nm == "s_key") one(ws.s_key, 4 * (size_t)c.n_sub_nodes);
     else if (nm == "s_depth") one(ws.s_depth, 4 * (size_t)c.n_sub_nodes);
     else if (nm == "s_sign") one(ws.s_sign, (size_t)c.n_sub_nodes);
+    else if (nm == "s_parent") one(ws.s_parent, 4 * (size_t)c.n_sub_nodes);
+    else if (nm == "s_root") one(ws.s_root, 4 * (size_t)c.n_sub_nodes);
+    else if (nm == "s_jump") one(ws.s_jump, 4 * (size_t)c.n_sub_nodes);
+    else if (nm == "s_cx") one(ws.s_cx, 4 * (size_t)c.n_sub_nodes);
+    else if (nm == "s_cy") one(ws.s_cy, 4 * (size_t)c.n_sub_nodes);
+    else if (nm == "s_cz") one(ws.s_cz, 4 * (size_t)c.n_sub_nodes);
+    else if (nm == "s_neigh") rows(ws.s_neigh, 27, 4 * (size_t)c.n_sub_nodes, 4 * (size_t)ws.cap.sub_nodes);
+    else if (nm == "s_live") one(ws.s_live, (size_t)c.n_sub_dnodes);
     else if (nm == "sv_value") one(ws.sv_value, 4 * (size_t)c.n_sub_vertices);
     else if (nm == "sv_owner") one(ws.sv_owner, 4 * (size_t)c.n_sub_vertices);
     else if (nm == "s_cube_class") one(ws.s_cube_class, 4 * (size_t)c.n_sub_dnodes);

@@ -717,83 +717,88 @@ __global__ void __launch_bounds__(kBlock) k_sub_build(const Counters* c, int dep
 // crossing edge and no triangle, so it needs no vertex, edge or cube record; its subtree
 // inherits the sign.  The test below is conservative, so the mesh is unchanged.
 //
-// On the closed cell (centre c, half width h = 2^-(d+1)) of a sub node s at depth d, F is
-// the sum over the levels l <= d of the 27 neighbour terms y_k B_k of s's ancestor at l
-// (y = 0 for absent nodes and for sub nodes that are not roots), provided no octree node
-// deeper than d reaches the cell: that holds when none of s's 27 neighbours is an octree
-// node with children.  B_k = b(x) b(y) b(z) with b(t) = 4/3 (3/4 - t^2) for |t| < 1/2,
-// 2/3 (3/2 - |t|)^2 for |t| < 3/2 (t in level widths): b <= 1, |b'| <= 4/3, |b''| <= 8/3.
-// The translates of one level sum to (4/3)^3 on the ancestor's cell, so every derivative of
-// F_l there is sum_k (y_k - m) dB_k for any constant m; take m = the mid-range of the y_k
-// and S_l = sum_k |y_k - m|.  For |p - c|_inf <= h:
-//   level d (first order):   |F_d(p) - F_d(c)| <= 3 h (4/3) 2^d S_d = 2 S_d
-//   levels l < d (Taylor):   |F_l(p) - F_l(c) - grad F_l(c) . (p - c)|
-//                              <= h^2 / 2 (3 (8/3) + 6 (4/3)^2) 4^l S_l = 7/3 4^(l-d) S_l
-// so |F(p) - F(c)| <= h |G|_1 + 2 S_d + sum_{l<d} 7/3 4^(l-d) S_l, G = sum_{l<d} grad F_l(c).
+// On the closed cell of a sub node s at depth d, F is the sum over the levels l <= d of the
+// 27 neighbour terms y_k B_k of s's ancestor at l (y = 0 for absent nodes and for sub nodes
+// that are not roots), provided no octree node deeper than d reaches the cell: that holds
+// when none of s's 27 neighbours is an octree node with children.  B_k = b(x) b(y) b(z) with
+// b(t) = 4/3 (3/4 - t^2) for |t| < 1/2 and 2/3 (3/2 - |t|)^2 for |t| < 3/2 (t in level
+// widths from the translate's centre).  The knots of a level-l translate lie on level-l cell
+// boundaries and the cell of s lies inside one level-l cell, so on it every translate is a
+// single quadratic and F is a tensor-product quadratic.  Written in the Bernstein basis of
+// the cell, F's 27 coefficients bound its values there (convex hull), so all coefficients
+// above iso (below iso) make the sign certain.  With s in [-1, 1] across the cell, a
+// translate is q(s) = b + g s + k/2 s^2 (b, g = h b', k = h^2 b'' at the centre, h the half
+// width), whose Bernstein coefficients are b - g + k/2, b - k/2, b + g + k/2.
 // Float vertex values are sums of the same nonzero terms (at most 27 (D+1)), within
-// ~1.7e-5 sum |y| of the exact value, as are the float F(c) and h G here; the test keeps a
-// margin of 1e-4 (sum |y| + |iso|) beyond the bound.
-struct SignAcc {
-    float val = 0.0f, gx = 0.0f, gy = 0.0f, gz = 0.0f, rem = 0.0f, mag = 0.0f;
-};
+// ~1.7e-5 sum |y| of the exact value; the float coefficients here are as close; the test
+// keeps a margin of 1e-4 (sum |y| + |iso|).
 
-// b and h db/dx of the translate `idx` at x (hs = h 2^l, the half width in level widths)
-__device__ __forceinline__ void basis_grad(int idx, float x, float hs, float& b, float& g) {
+// Bernstein coefficients on the cell of the translate `idx` (hs = h 2^l: half width in
+// level widths; x the cell centre)
+__device__ __forceinline__ void basis_bernstein(int idx, float x, float hs, float (&q)[3]) {
     const int l = ilog2_dev(idx + 1);
     const int off = idx + 1 - (1 << l);
     const float c = __fmul_rn(__fadd_rn((float)off, 0.5f), __int_as_float((127 - l) << 23));
     const float t = __fmul_rn(__fsub_rn(x, c), (float)(1 << l));
     const float a = fabsf(t);
+    float b, g, k2;
     if (a < 0.5f) {
         b = (0.75f - t * t) * (4.0f / 3.0f);
         g = -(8.0f / 3.0f) * t * hs;
+        k2 = -(4.0f / 3.0f) * hs * hs;
     } else if (a < 1.5f) {
         const float u = 1.5f - a;
         b = u * u * (2.0f / 3.0f);
         g = copysignf((4.0f / 3.0f) * u * hs, -t);
+        k2 = (2.0f / 3.0f) * hs * hs;
     } else {
         b = 0.0f;
         g = 0.0f;
+        k2 = 0.0f;
     }
+    q[0] = b - g + k2;
+    q[1] = b - k2;
+    q[2] = b + g + k2;
 }
 
-// one level: the ancestor's function indices (ox, oy, oz), its 27 values y; l == d takes
-// the first-order bound, coarser levels the Taylor one (hs = h 2^l)
+// adds one level (ancestor function indices ox, oy, oz; its 27 values y) to the cell's
+// Bernstein coefficients C[alpha][beta][gamma] (x, y, z), separably
 __device__ __forceinline__ void sign_level(const float (&y)[27], int ox, int oy, int oz, float qx, float qy,
-                                           float qz, int l, int d, SignAcc& A) {
-    const float hs = __int_as_float((127 + l - d - 1) << 23);   // h 2^l = 2^(l-d-1)
-    float bx[3], by[3], bz[3], dx[3], dy[3], dz[3];
+                                           float qz, float hs, float (&C)[27], float& mag) {
+    float X[3][3], Y[3][3], Z[3][3];
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
-        basis_grad(ox - 1 + j, qx, hs, bx[j], dx[j]);
-        basis_grad(oy - 1 + j, qy, hs, by[j], dy[j]);
-        basis_grad(oz - 1 + j, qz, hs, bz[j], dz[j]);
+        basis_bernstein(ox - 1 + j, qx, hs, X[j]);
+        basis_bernstein(oy - 1 + j, qy, hs, Y[j]);
+        basis_bernstein(oz - 1 + j, qz, hs, Z[j]);
     }
-    float lo = y[0], hi = y[0];
+    float ab = 0.0f;
 #pragma unroll
-    for (int k = 1; k < 27; ++k) { lo = fminf(lo, y[k]); hi = fmaxf(hi, y[k]); }
-    const float m = 0.5f * (lo + hi);
-    float dev = 0.0f, ab = 0.0f, gx = 0.0f, gy = 0.0f, gz = 0.0f;
+    for (int k = 0; k < 27; ++k) ab += fabsf(y[k]);
+    mag += ab;
+    // T1[a][j][k] = sum_i X[i][a] y[i][j][k]
+    float T1[27];
 #pragma unroll
-    for (int k = 0; k < 27; ++k) {
-        const int i = k / 9, j = (k / 3) % 3, kk = k % 3;
-        const float yk = y[k];
-        A.val = fmaf(yk, bx[i] * by[j] * bz[kk], A.val);
-        gx = fmaf(yk, dx[i] * by[j] * bz[kk], gx);
-        gy = fmaf(yk, bx[i] * dy[j] * bz[kk], gy);
-        gz = fmaf(yk, bx[i] * by[j] * dz[kk], gz);
-        dev += fabsf(yk - m);
-        ab += fabsf(yk);
-    }
-    A.mag += ab;
-    if (l >= d) {
-        A.rem = fmaf(2.0f, dev, A.rem);
-    } else {
-        A.gx += gx;
-        A.gy += gy;
-        A.gz += gz;
-        A.rem = fmaf((7.0f / 3.0f) * 4.0f * hs * hs, dev, A.rem);   // 7/3 4^(l-d) = 28/3 hs^2
-    }
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int jk = 0; jk < 9; ++jk)
+            T1[a * 9 + jk] = fmaf(X[0][a], y[jk], fmaf(X[1][a], y[9 + jk], X[2][a] * y[18 + jk]));
+    // T2[a][b][k] = sum_j Y[j][b] T1[a][j][k]
+    float T2[27];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int bb = 0; bb < 3; ++bb)
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                T2[a * 9 + bb * 3 + k] = fmaf(Y[0][bb], T1[a * 9 + k],
+                                              fmaf(Y[1][bb], T1[a * 9 + 3 + k], Y[2][bb] * T1[a * 9 + 6 + k]));
+    // C[a][b][g] += sum_k Z[k][g] T2[a][b][k]
+#pragma unroll
+    for (int ab3 = 0; ab3 < 9; ++ab3)
+#pragma unroll
+        for (int gg = 0; gg < 3; ++gg)
+            C[ab3 * 3 + gg] += fmaf(Z[0][gg], T2[ab3 * 3], fmaf(Z[1][gg], T2[ab3 * 3 + 1], Z[2][gg] * T2[ab3 * 3 + 2]));
 }
 
 // sign of F - iso on the closed cell of sub node s at depth d; sn = s_jump[s], the nearest
@@ -805,7 +810,10 @@ __device__ __forceinline__ int sub_cell_sign(int s, int d, int sn, int depth, co
                                              const float* s_cz, const int* enc, const float* x, float iso,
                                              int na) {
     const float qx = s_cx[s], qy = s_cy[s], qz = s_cz[s];
-    SignAcc A;
+    float C[27];
+#pragma unroll
+    for (int k = 0; k < 27; ++k) C[k] = 0.0f;
+    float mag = 0.0f;
     float y[27];
     int now;
     // subdivision levels that carry a value (s_jump hops over the others)
@@ -822,7 +830,7 @@ __device__ __forceinline__ int sub_cell_sign(int s, int d, int sn, int depth, co
             if (v >= na) v = s_root[v - na];
             y[k] = (v >= 0) ? x[v] : 0.0f;
         }
-        sign_level(y, ox, oy, oz, qx, qy, qz, l, d, A);
+        sign_level(y, ox, oy, oz, qx, qy, qz, __int_as_float((126 + l - d) << 23), C, mag);
         now = s_parent[sn];
         if (now < na) break;
         sn = s_jump[now - na];
@@ -837,14 +845,15 @@ __device__ __forceinline__ int sub_cell_sign(int s, int d, int sn, int depth, co
             const int v = neigh[(size_t)k * stride + now];
             y[k] = (v >= 0) ? x[v] : 0.0f;
         }
-        sign_level(y, ox, oy, oz, qx, qy, qz, l, d, A);
+        sign_level(y, ox, oy, oz, qx, qy, qz, __int_as_float((126 + l - d) << 23), C, mag);
         now = parent[now];
     }
-    const float var = fabsf(A.gx) + fabsf(A.gy) + fabsf(A.gz) + A.rem;
-    const float bound = var * 1.001f + 1e-4f * (A.mag + fabsf(iso));
-    const float f = A.val - iso;
-    if (f > bound) return 1;
-    if (f < -bound) return -1;
+    float lo = C[0], hi = C[0];
+#pragma unroll
+    for (int k = 1; k < 27; ++k) { lo = fminf(lo, C[k]); hi = fmaxf(hi, C[k]); }
+    const float margin = 1e-4f * (mag + fabsf(iso));
+    if (lo - iso > margin) return 1;
+    if (hi - iso < -margin) return -1;
     return 0;
 }
 
