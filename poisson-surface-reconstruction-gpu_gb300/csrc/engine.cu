@@ -236,18 +236,19 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     A.add(ws.sub_root, (size_t)nodes);
     A.add(ws.sub_root_depth, (size_t)nodes);
     A.add(ws.root_group, (size_t)nodes);
-    A.add(ws.s_key, (size_t)subn); A.add(ws.s_parent, (size_t)subn); A.add(ws.s_first_child, (size_t)subn);
-    A.add(ws.s_neigh, 27 * (size_t)subn); A.add(ws.s_depth, (size_t)subn); A.add(ws.s_root, (size_t)subn);
-    A.add(ws.s_group, (size_t)subn);
-    A.add(ws.s_jump, (size_t)subn);
-    A.add(ws.s_sign, (size_t)subn);
-    A.add(ws.s_cx, (size_t)subn); A.add(ws.s_cy, (size_t)subn); A.add(ws.s_cz, (size_t)subn);
+    A.add(ws.root_self, (size_t)nodes);
+    A.add(ws.c_vnode, (size_t)subn); A.add(ws.c_key, (size_t)subn); A.add(ws.c_group, (size_t)subn);
+    A.add(ws.c_parent, (size_t)subn); A.add(ws.c_jump, (size_t)subn); A.add(ws.c_depth, (size_t)subn);
+    A.add(ws.c_cx, (size_t)subn); A.add(ws.c_cy, (size_t)subn); A.add(ws.c_cz, (size_t)subn);
+    A.add(ws.c_neigh, 27 * (size_t)subn);
+    A.add(ws.c_live, (size_t)subn);
+    A.add(ws.lv_vnode, (size_t)subd);
+    A.add(ws.lv_nb, 27 * (size_t)subd);
     A.add(ws.s_vtx, 8 * (size_t)subd); A.add(ws.s_edge, 12 * (size_t)subd);
-    A.add(ws.s_vmask, (size_t)subd); A.add(ws.s_emask, (size_t)subd); A.add(ws.s_live, (size_t)subd);
+    A.add(ws.s_vmask, (size_t)subd); A.add(ws.s_emask, (size_t)subd);
     A.add(ws.sv_x, 8 * (size_t)subd); A.add(ws.sv_y, 8 * (size_t)subd); A.add(ws.sv_z, 8 * (size_t)subd);
     A.add(ws.sv_owner, 8 * (size_t)subd); A.add(ws.sv_kind, 8 * (size_t)subd); A.add(ws.sv_value, 8 * (size_t)subd);
     A.add(ws.se_owner, 12 * (size_t)subd); A.add(ws.se_kind, 12 * (size_t)subd); A.add(ws.se_cross, 12 * (size_t)subd);
-    A.add(ws.se_dn, 12 * (size_t)subd);
     A.add(ws.s_cube_class, (size_t)subd);
     A.add(ws.mesh_v, 3 * (size_t)cap.mesh_vertices);
     A.add(ws.mesh_t, 3 * (size_t)cap.mesh_tris);
@@ -656,21 +657,9 @@ psr_status psr_debug_array(psr_handle* h, const char* name, void* dst, size_t ds
     else if (nm == "mesh_t") one(ws.mesh_t, 12 * (size_t)c.n_mesh_triangles);
     else if (nm == "mesh_c") one(ws.mesh_c, 12 * (size_t)c.n_mesh_vertices);
     else if (nm == "mesh_n") one(ws.mesh_n, 12 * (size_t)c.n_mesh_vertices);
-    else if (nm == "s_key") one(ws.s_key, 4 * (size_t)c.n_sub_nodes);
-    else if (nm == "s_depth") one(ws.s_depth, 4 * (size_t)c.n_sub_nodes);
-    else if (nm == "s_sign") one(ws.s_sign, (size_t)c.n_sub_nodes);
-    else if (nm == "s_parent") one(ws.s_parent, 4 * (size_t)c.n_sub_nodes);
-    else if (nm == "s_root") one(ws.s_root, 4 * (size_t)c.n_sub_nodes);
-    else if (nm == "s_jump") one(ws.s_jump, 4 * (size_t)c.n_sub_nodes);
-    else if (nm == "s_cx") one(ws.s_cx, 4 * (size_t)c.n_sub_nodes);
-    else if (nm == "s_cy") one(ws.s_cy, 4 * (size_t)c.n_sub_nodes);
-    else if (nm == "s_cz") one(ws.s_cz, 4 * (size_t)c.n_sub_nodes);
-    else if (nm == "s_neigh") rows(ws.s_neigh, 27, 4 * (size_t)c.n_sub_nodes, 4 * (size_t)ws.cap.sub_nodes);
-    else if (nm == "s_live") one(ws.s_live, (size_t)c.n_sub_dnodes);
     else if (nm == "sv_value") one(ws.sv_value, 4 * (size_t)c.n_sub_vertices);
-    else if (nm == "sv_owner") one(ws.sv_owner, 4 * (size_t)c.n_sub_vertices);
     else if (nm == "s_cube_class") one(ws.s_cube_class, 4 * (size_t)c.n_sub_dnodes);
-    else if (nm == "s_vtx") rows(ws.s_vtx, 8, 4 * (size_t)c.n_sub_dnodes, 4 * (size_t)ws.cap.sub_dnodes);
+    else if (nm == "sub_live_vnode") one(ws.lv_vnode, 4 * (size_t)c.n_sub_dnodes);
     else if (nm == "counters") { if (bytes) *bytes = sizeof(Counters); if (dst && dst_bytes >= sizeof(Counters)) memcpy(dst, &c, sizeof(Counters)); return PSR_OK; }
     else return fail(h, PSR_INVALID_INPUT, "unknown array name");
     size_t total = 0;

@@ -532,8 +532,7 @@ struct RootStore {
 };
 
 // Group table.  Group record (ints): 0 root depth, 1 first root, 2 root count,
-// 3 node offset, 4 node count, 5 D-level node offset (in the D-level sub numbering),
-// 6 D-level node count.  Coarse roots (depth < D - 4) are one group each; the finer roots
+// 3 virtual node offset, 4 virtual node count.  Coarse roots (depth < D - 4) are one group each; the finer roots
 // of one depth form one group (mesh/ComputeTriangleIndices.cu:1475-1799, :1801-2194).
 constexpr int kGroupRec = 8;
 
@@ -571,7 +570,7 @@ __global__ void k_group_count(Counters* c, const unsigned* total, int max_groups
 }
 
 // per-group sizes (thread per group)
-__global__ void __launch_bounds__(kBlock) k_group_sizes(const Counters* c, int depth, const int* sub_root,
+__global__ void __launch_bounds__(kBlock) k_group_sizes(Counters* c, int depth, const int* sub_root,
                                                         const int* ndepth, int* groups) {
     const int ng = c->n_groups;
     const int R = c->n_subroots;
@@ -583,11 +582,11 @@ __global__ void __launch_bounds__(kBlock) k_group_sizes(const Counters* c, int d
         const long long n = next - first;
         long long per = 0, dper = 1;
         for (int d = rd; d <= depth; ++d) { per += dper; if (d < depth) dper *= 8; }
-        const long long nodes = per * n, dn = dper * n;
+        const long long nodes = per * n;
         G[0] = rd;
         G[2] = (int)n;
+        if (nodes > 0x3fffffffLL) atomicOr(&c->error, kErrCapacity);
         G[4] = nodes > 0x3fffffffLL ? 0x3fffffff : (int)nodes;
-        G[6] = dn > 0x3fffffffLL ? 0x3fffffff : (int)dn;
     }
 }
 
@@ -602,36 +601,34 @@ struct GroupFieldStore {
     __device__ void operator()(int g, unsigned pre, unsigned) const { groups[(size_t)g * kGroupRec + field] = (int)pre; }
 };
 
-__global__ void k_group_totals(Counters* c, const unsigned* node_total, const unsigned* dnode_total, int node_cap,
-                               int dnode_cap) {
+// the virtual numbering of all groups must fit beside the octree indices (na + index)
+__global__ void k_group_totals(Counters* c, const unsigned* node_total, int na) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
-        const unsigned nt = *node_total, dt = *dnode_total;
-        if (nt > (unsigned)node_cap || dt > (unsigned)dnode_cap) {
+        const unsigned nt = *node_total;
+        if (nt > 0x7fffffffu - (unsigned)na) {
             atomicOr(&c->error, kErrCapacity);
             c->n_groups = 0;
-            c->n_sub_nodes = 0;
-            c->n_sub_dnodes = 0;
-            return;
         }
-        c->n_sub_nodes = (int)nt;
-        c->n_sub_dnodes = (int)dt;
     }
 }
 
-// per root: its depth and the redirected child slot of its parent (overlay)
+// per root: its depth, the octree node it stands for, and the redirected child slot of
+// its parent (overlay)
 __global__ void __launch_bounds__(kBlock) k_root_overlay(const Counters* c, int depth, const int* sub_root,
                                                          const int* ndepth, const int* key, const int* parent,
-                                                         const int* root_group, const int* groups,
-                                                         int* sub_root_depth, int* ov_group, int* ov_sub,
-                                                         size_t stride) {
+                                                         const int* neigh, const int* root_group, const int* groups,
+                                                         int* sub_root_depth, int* root_self, int* ov_group,
+                                                         int* ov_sub, size_t stride) {
     const int R = c->n_subroots;
     const int ng = c->n_groups;
     PSR_GRID_STRIDE(r, R) {
-        const int g = root_group[r];
-        if (g < 0 || g >= ng) continue;
         const int node = sub_root[r];
         const int rd = ndepth[node];
         sub_root_depth[r] = rd;
+        const int self = neigh[(size_t)13 * stride + node];   // its neighs[13] in the reference
+        root_self[r] = (self == -1) ? node : self;
+        const int g = root_group[r];
+        if (g < 0 || g >= ng) continue;
         const int q = r - groups[(size_t)g * kGroupRec + 1];
         const int son = (key[node] >> (3 * (depth - rd))) & 7;
         const int pa = parent[node];
@@ -642,80 +639,62 @@ __global__ void __launch_bounds__(kBlock) k_root_overlay(const Counters* c, int 
     }
 }
 
-// subdivision node geometry (singleRebuildArray :599-635 / wholeRebuildArray :1110-1168)
-__device__ __forceinline__ int find_group(const int* groups, int ng, int field, int v) {
-    int lo = 0, hi = ng - 1;
-    while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (groups[(size_t)mid * kGroupRec + field] <= v) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
-
-// local index inside a group -> (depth, root slot q, rel)
-__device__ __forceinline__ void sub_locate(int local, int rd, int n, int depth, int& d, int& q, int& rel) {
-    int off = 0, cnt = n;
-    d = rd;
-    while (d < depth && local >= off + cnt) { off += cnt; cnt *= 8; ++d; }
-    const int per = cnt / n;
-    q = (local - off) / per;
-    rel = (local - off) - q * per;
-}
+// ---- subdivision, breadth-first over live nodes ----------------------------------------
+// Virtual numbering (singleRebuildArray :599-635 / wholeRebuildArray :1110-1168): group g
+// owns the virtual sub nodes G[3] .. G[3] + G[4] - 1, level by level from its root depth rd
+// (its n roots) to D; node (q, rel) of level d sits at G[3] + off_d + q 8^(d-rd) + rel (rel:
+// the Morton code below root q).  Neighbour tables hold octree nodes (< na), na + virtual
+// index for sub nodes, or -1.  Only candidates are stored, in compact slots: at depth d the
+// 8 children of every live node of depth d-1, in order, then the roots of depth d.  Both
+// parts are in virtual order (groups are ordered by root depth), so the live depth-D cells,
+// which carry all records from here on, come out in the reference's order.
 __device__ __forceinline__ int sub_level_off(int rd, int n, int d) {
     int off = 0, cnt = n;
     for (int e = rd; e < d; ++e) { off += cnt; cnt *= 8; }
     return off;
 }
 
-__global__ void __launch_bounds__(kBlock) k_sub_build(const Counters* c, int depth, const int* groups,
-                                                      const int* sub_root, const int* key, const int* parent,
-                                                      const int* neigh, size_t stride, int* s_key, int* s_parent,
-                                                      int* s_first_child, int* s_depth, int* s_group, int* s_root,
-                                                      float* s_cx, float* s_cy, float* s_cz, int na) {
-    const int S = c->n_sub_nodes;
-    const int ng = c->n_groups;
-    PSR_GRID_STRIDE(s, S) {
-        const int g = find_group(groups, ng, 3, s);
-        const int* G = groups + (size_t)g * kGroupRec;
-        const int rd = G[0], n = G[2], goff = G[3];
-        const int local = s - goff;
-        int d, q, rel;
-        sub_locate(local, rd, n, depth, d, q, rel);
-        const int root_node = sub_root[G[1] + q];
-        const int k = key[root_node] | (rel << (3 * (depth - d)));
-        s_key[s] = k;
-        s_depth[s] = d;
-        s_group[s] = g;
-        // root: the octree node it replaces (its neighs[13] in the reference)
-        int self = neigh[(size_t)13 * stride + root_node];
-        if (self == -1) self = root_node;
-        s_root[s] = (d == rd) ? self : -1;
-        if (d == rd) s_parent[s] = parent[root_node];
-        else s_parent[s] = na + goff + sub_level_off(rd, n, d - 1) + q * (1 << (3 * (d - 1 - rd))) + (rel >> 3);
-        s_first_child[s] = (d < depth) ? na + goff + sub_level_off(rd, n, d + 1) + q * (1 << (3 * (d + 1 - rd))) + (rel << 3)
-                                       : -1;
-        float cc[3] = {0.5f, 0.5f, 0.5f};
-        float w = 0.25f;
-        for (int l = depth - 1; l >= depth - d; --l) {
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                if ((k >> (3 * l + 2 - a)) & 1) cc[a] = __fadd_rn(cc[a], w);
-                else cc[a] = __fsub_rn(cc[a], w);
-            }
-            w = __fdiv_rn(w, 2.0f);
+// per-depth candidate bookkeeping (Counters::sub_*): [d] for depth d
+__global__ void k_sub_setup(Counters* c, int depth, const int* sub_root_depth, int cap_nodes) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int R = c->n_subroots;
+    int start = 0;
+    for (int d = 0; d <= depth + 1; ++d) {
+        int lo = start, hi = R;   // first root deeper than d (roots are in depth order)
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (sub_root_depth[mid] <= d) lo = mid + 1;
+            else hi = mid;
         }
-        s_cx[s] = cc[0];
-        s_cy[s] = cc[1];
-        s_cz[s] = cc[2];
+        c->sub_rstart[d] = start;
+        c->sub_nroots[d] = (c->n_groups > 0) ? lo - start : 0;
+        start = lo;
+        c->sub_cand[d] = 0;
+        c->sub_cbase[d] = 0;
+        c->sub_lbase[d] = 0;
+        c->sub_nlive[d] = 0;
     }
+    if (c->sub_nroots[1] > cap_nodes) atomicOr(&c->error, kErrCapacity);
+    else c->sub_cand[1] = c->sub_nroots[1];
+    c->n_sub_nodes = 0;
+    c->n_sub_dnodes = 0;
 }
+
+struct SubArrays {
+    int *vnode, *key, *group, *parent, *jump, *depth;   // parent: slot, or -2 - octree parent
+    float *cx, *cy, *cz;
+    int* neigh;   // [27][cap]
+    size_t cstride;
+    int* live;    // live slots, depth after depth
+    int* lv_vnode;   // virtual index of each live depth-D cell
+    int cap_nodes, cap_live_d;
+};
 
 // ---- certain-sign cells -------------------------------------------------------------
 // Subdivision replaces a coarse leaf that carries surface by all of its depth-D cells, but
 // the surface crosses few of them.  A cell where F - iso provably keeps one sign has no
-// crossing edge and no triangle, so it needs no vertex, edge or cube record; its subtree
-// inherits the sign.  The test below is conservative, so the mesh is unchanged.
+// crossing edge and no triangle, so it needs no vertex, edge or cube record, and its
+// subtree is never built.  The test below is conservative, so the mesh is unchanged.
 //
 // On the closed cell of a sub node s at depth d, F is the sum over the levels l <= d of the
 // 27 neighbour terms y_k B_k of s's ancestor at l (y = 0 for absent nodes and for sub nodes
@@ -801,39 +780,43 @@ __device__ __forceinline__ void sign_level(const float (&y)[27], int ox, int oy,
             C[ab3 * 3 + gg] += fmaf(Z[0][gg], T2[ab3 * 3], fmaf(Z[1][gg], T2[ab3 * 3 + 1], Z[2][gg] * T2[ab3 * 3 + 2]));
 }
 
-// sign of F - iso on the closed cell of sub node s at depth d; sn = s_jump[s], the nearest
-// node at or above s with a contributing neighbour
-__device__ __forceinline__ int sub_cell_sign(int s, int d, int sn, int depth, const int* neigh, size_t stride,
-                                             const int* parent, const int* s_neigh, size_t sstride,
-                                             const int* s_parent, const int* s_root, const int* s_jump,
-                                             const int* s_depth, const float* s_cx, const float* s_cy,
-                                             const float* s_cz, const int* enc, const float* x, float iso,
-                                             int na) {
-    const float qx = s_cx[s], qy = s_cy[s], qz = s_cz[s];
+// value carried by a sub-node neighbour (na + virtual index) of group G: its root's octree
+// node for a root (it stands for that node), else nothing (x = 0 in subdivision space)
+__device__ __forceinline__ int sub_value_node(int v, int na, const int* G, const int* root_self) {
+    const int local = v - na - G[3];
+    return ((unsigned)local < (unsigned)G[2]) ? root_self[G[1] + local] : -1;
+}
+
+// sign of F - iso on the closed cell (centre q) of a node at depth d; sn = the slot of the
+// nearest node at or above it with a contributing neighbour
+__device__ __forceinline__ int sub_cell_sign(float qx, float qy, float qz, int d, int sn, const int* G,
+                                             int depth, const int* neigh, size_t stride, const int* parent,
+                                             const int* enc, const float* x, const int* root_self, float iso,
+                                             const SubArrays& A, int na) {
     float C[27];
 #pragma unroll
     for (int k = 0; k < 27; ++k) C[k] = 0.0f;
     float mag = 0.0f;
     float y[27];
     int now;
-    // subdivision levels that carry a value (s_jump hops over the others)
+    // subdivision levels that carry a value (jump hops over the others)
     while (true) {
-        const int l = s_depth[sn];
+        const int l = A.depth[sn];
         const float sc = (float)(1 << l);
         const int base = (1 << l) - 1;
-        const int ox = base + (int)__fmul_rn(s_cx[sn], sc);
-        const int oy = base + (int)__fmul_rn(s_cy[sn], sc);
-        const int oz = base + (int)__fmul_rn(s_cz[sn], sc);
+        const int ox = base + (int)__fmul_rn(A.cx[sn], sc);
+        const int oy = base + (int)__fmul_rn(A.cy[sn], sc);
+        const int oz = base + (int)__fmul_rn(A.cz[sn], sc);
 #pragma unroll
         for (int k = 0; k < 27; ++k) {
-            int v = s_neigh[(size_t)k * sstride + sn];
-            if (v >= na) v = s_root[v - na];
+            int v = A.neigh[(size_t)k * A.cstride + sn];
+            if (v >= na) v = sub_value_node(v, na, G, root_self);
             y[k] = (v >= 0) ? x[v] : 0.0f;
         }
         sign_level(y, ox, oy, oz, qx, qy, qz, __int_as_float((126 + l - d) << 23), C, mag);
-        now = s_parent[sn];
-        if (now < na) break;
-        sn = s_jump[now - na];
+        const int p = A.parent[sn];
+        if (p < 0) { now = -2 - p; break; }
+        sn = A.jump[p];
     }
     // octree levels above the root
     while (now >= 0) {
@@ -857,54 +840,71 @@ __device__ __forceinline__ int sub_cell_sign(int s, int d, int sn, int depth, co
     return 0;
 }
 
-// computeRebuildNeighbor (:669-696) for all subdivision nodes at depth d, and the certain
-// sign of each node's cell (inherited from a parent with a certain sign, whose subtree needs
-// no neighbours; else tested above once the node lies below its root)
-__global__ void __launch_bounds__(kBlock) k_sub_neighbours(const Counters* c, int d, int depth, const int* groups,
-                                                           const int* neigh, size_t stride, const int* first_child,
-                                                           const int* ov_group, const int* ov_sub, const int* s_key,
-                                                           const int* s_parent, const int* s_first_child,
-                                                           const int* s_depth, const int* s_group, const int* s_root,
-                                                           int* s_neigh, int* s_jump, signed char* s_sign,
-                                                           size_t sstride, const int* parent, const float* s_cx,
-                                                           const float* s_cy, const float* s_cz, const int* enc,
-                                                           const float* x, int na) {
-    // Depth-d nodes only.  Groups are ordered by root depth, so those reaching depth d are
-    // a prefix 0..gd-1, and the depth-d nodes of groups before g number
-    // dnode_prefix(g) / 8^(D-d) (every such group has full subtrees below its roots).
-    const int ng = c->n_groups;
-    int gd = 0;
-    {
-        int lo = 0, hi = ng;   // first group whose root depth exceeds d
-        while (lo < hi) {
-            const int mid = (lo + hi) >> 1;
-            if (groups[(size_t)mid * kGroupRec + 0] <= d) lo = mid + 1;
-            else hi = mid;
+// One candidate of depth d (computeRebuildNeighbor :669-696 for its neighbours): its record,
+// its neighbours and its sign test; returns 1 when it stays live.
+struct SubLevelLoad {
+    const Counters* c;
+    int d, depth, na;
+    const int* groups;
+    const int* sub_root;
+    const int* root_group;
+    const int* root_self;
+    const int* key;
+    const int* neigh;
+    size_t stride;
+    const int* first_child;
+    const int* parent;
+    const int* ov_group;
+    const int* ov_sub;
+    const int* enc;
+    const float* x;
+    SubArrays A;
+    __device__ unsigned operator()(int i) const {
+        const int nl_prev = c->sub_nlive[d - 1];
+        const int slot = c->sub_cbase[d] + i;
+        int g, vnode, k, pslot, pa;   // pa: parent as a neighbour-table entry
+        float cc[3];
+        if (i < 8 * nl_prev) {
+            pslot = A.live[c->sub_lbase[d - 1] + (i >> 3)];
+            const int ch = i & 7;
+            g = A.group[pslot];
+            const int* G = groups + (size_t)g * kGroupRec;
+            const int pl = A.vnode[pslot] - G[3] - sub_level_off(G[0], G[2], d - 1);
+            vnode = G[3] + sub_level_off(G[0], G[2], d) + 8 * pl + ch;
+            k = A.key[pslot] | (ch << (3 * (depth - d)));
+            const float w = __int_as_float((126 - d) << 23);   // 2^-(d+1)
+            cc[0] = (ch & 4) ? __fadd_rn(A.cx[pslot], w) : __fsub_rn(A.cx[pslot], w);
+            cc[1] = (ch & 2) ? __fadd_rn(A.cy[pslot], w) : __fsub_rn(A.cy[pslot], w);
+            cc[2] = (ch & 1) ? __fadd_rn(A.cz[pslot], w) : __fsub_rn(A.cz[pslot], w);
+            pa = na + A.vnode[pslot];
+        } else {
+            const int r = c->sub_rstart[d] + (i - 8 * nl_prev);
+            g = root_group[r];
+            const int* G = groups + (size_t)g * kGroupRec;
+            vnode = G[3] + (r - G[1]);
+            const int root_node = sub_root[r];
+            k = key[root_node];
+            cc[0] = cc[1] = cc[2] = 0.5f;
+            float w = 0.25f;
+            for (int l = depth - 1; l >= depth - d; --l) {
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    if ((k >> (3 * l + 2 - a)) & 1) cc[a] = __fadd_rn(cc[a], w);
+                    else cc[a] = __fsub_rn(cc[a], w);
+                }
+                w = __fdiv_rn(w, 2.0f);
+            }
+            pslot = -1;
+            pa = parent[root_node];
         }
-        gd = lo;
-    }
-    const int sh = 3 * (depth - d);
-    const int nd = ((gd < ng) ? groups[(size_t)gd * kGroupRec + 5] : c->n_sub_dnodes) >> sh;
-    PSR_GRID_STRIDE(t, nd) {
-        int lo = 0, hi = gd - 1;   // last group g < gd with offset(g) <= t
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if ((groups[(size_t)mid * kGroupRec + 5] >> sh) <= t) lo = mid;
-            else hi = mid - 1;
-        }
-        const int g = lo;
         const int* G = groups + (size_t)g * kGroupRec;
-        const int local = t - (G[5] >> sh);
-        const int s = G[3] + sub_level_off(G[0], G[2], d) + local;
-        const int pa = s_parent[s];
-        if (pa >= na) {
-            const int ps = s_sign[pa - na];
-            if (ps != 0) { s_sign[s] = (signed char)ps; continue; }
-        }
         const bool at_root_depth = (d == G[0]);
+        const int local = vnode - G[3] - sub_level_off(G[0], G[2], d);
+        const int off_prev = (d > G[0]) ? sub_level_off(G[0], G[2], d - 1) : 0;
+        const int off_cur = sub_level_off(G[0], G[2], d);
         int contrib = 0;
         bool deeper = false;   // an octree neighbour with children reaches below depth d
-        const int son = (s_key[s] >> (3 * (depth - d))) & 7;
+        const int son = (k >> (3 * (depth - d))) & 7;
         // Position inside the root's cell: rel = the Morton code of the node's L = d - rd
         // levels below its root (x = bit 2, y = bit 1, z = bit 0 of every triple).  A
         // neighbour inside the same root's cell is the node at the shifted code in the same
@@ -926,233 +926,254 @@ __global__ void __launch_bounds__(kBlock) k_sub_neighbours(const Counters* c, in
             ok[a][1] = true;
             ok[a][2] = cm != M;
         }
-        int nb[27];
 #pragma unroll
-        for (int k = 0; k < 27; ++k) {
-            const int ix = k / 9, iy = (k / 3) % 3, iz = k % 3;
+        for (int kk = 0; kk < 27; ++kk) {
+            const int ix = kk / 9, iy = (kk / 3) % 3, iz = kk % 3;
+            int v;
             if (ok[0][ix] && ok[1][iy] && ok[2][iz]) {
                 const unsigned relk = cmp[0][ix] | cmp[1][iy] | cmp[2][iz];
-                const int v = na + s + (int)relk - (int)rel;
-                nb[k] = v;
+                v = na + vnode + (int)relk - (int)rel;
                 if (at_root_depth) contrib = 1;   // the node itself, a root
-                continue;
-            }
-            int lp, lc;
-            nb_lut(son, k, lp, lc);
-            const int np = (pa < na) ? neigh[(size_t)lp * stride + pa] : s_neigh[(size_t)lp * sstride + (pa - na)];
-            int v = -1;
-            if (np != -1) {
-                if (np < na) {
-                    if (ov_group[(size_t)lc * stride + np] == g) {
-                        // redirected child pointer of this group's root
-                        v = na + G[3] + ov_sub[(size_t)lc * stride + np];
+            } else {
+                int lp, lc;
+                nb_lut(son, kk, lp, lc);
+                const int np = (pslot < 0) ? ((pa >= 0) ? neigh[(size_t)lp * stride + pa] : -1)
+                                           : A.neigh[(size_t)lp * A.cstride + pslot];
+                v = -1;
+                if (np != -1) {
+                    if (np < na) {
+                        if (ov_group[(size_t)lc * stride + np] == g) {
+                            // redirected child pointer of this group's root
+                            v = na + G[3] + ov_sub[(size_t)lc * stride + np];
+                        } else {
+                            const int fc = first_child[np];
+                            v = (fc == -1) ? -1 : fc + lc;
+                            if (v >= 0 && d < depth && first_child[v] != -1) deeper = true;
+                        }
                     } else {
-                        const int fc = first_child[np];
-                        v = (fc == -1) ? -1 : fc + lc;
-                        if (v >= 0 && d < depth && first_child[v] != -1) deeper = true;
+                        // a sub node of depth d - 1 in this group: its children are at 8 x its
+                        // index in level d
+                        v = na + G[3] + off_cur + 8 * (np - na - G[3] - off_prev) + lc;
                     }
-                } else {
-                    const int fc = s_first_child[np - na];
-                    v = (fc == -1) ? -1 : fc + lc;
                 }
+                // a contributing neighbour is an octree node or a root; the subdivision nodes at
+                // a group's root depth are exactly its roots, and deeper ones are never roots
+                if (v >= 0 && (v < na || at_root_depth)) contrib = 1;
             }
-            nb[k] = v;
-            // a contributing neighbour is an octree node or a root; the subdivision nodes at a
-            // group's root depth are exactly its roots, and deeper ones are never roots
-            if (v >= 0 && (v < na || at_root_depth)) contrib = 1;
+            A.neigh[(size_t)kk * A.cstride + slot] = v;
         }
-#pragma unroll
-        for (int k = 0; k < 27; ++k) s_neigh[(size_t)k * sstride + s] = nb[k];
         // nearest contributing node on the path to the root (itself when it contributes;
         // roots always do): lets the value chains skip non-contributing levels in one hop
-        const int jump = contrib ? s : ((pa >= na) ? s_jump[pa - na] : s);
-        s_jump[s] = jump;
-        int sg = 0;
-        if (!at_root_depth && !deeper)
-            sg = sub_cell_sign(s, d, jump, depth, neigh, stride, parent, s_neigh, sstride, s_parent, s_root, s_jump,
-                               s_depth, s_cx, s_cy, s_cz, enc, x, c->iso, na);
-        s_sign[s] = (signed char)sg;
+        const int jump = contrib ? slot : ((pslot >= 0) ? A.jump[pslot] : slot);
+        A.vnode[slot] = vnode;
+        A.key[slot] = k;
+        A.group[slot] = g;
+        A.parent[slot] = (pslot >= 0) ? pslot : -2 - pa;
+        A.jump[slot] = jump;
+        A.depth[slot] = d;
+        A.cx[slot] = cc[0];
+        A.cy[slot] = cc[1];
+        A.cz[slot] = cc[2];
+        if (at_root_depth || deeper) return 1u;
+        const int sg = sub_cell_sign(cc[0], cc[1], cc[2], d, jump, G, depth, neigh, stride, parent, enc, x,
+                                     root_self, c->iso, A, na);
+        return (sg == 0) ? 1u : 0u;
+    }
+};
+struct SubLevelStore {
+    Counters* c;
+    int d, depth;
+    SubArrays A;
+    unsigned* err;
+    __device__ void operator()(int i, unsigned pre, unsigned live) const {
+        if (!live) return;
+        const int at = c->sub_lbase[d] + (int)pre;
+        if (at >= A.cap_nodes) { atomicOr(err, kErrCapacity); return; }
+        const int slot = c->sub_cbase[d] + i;
+        A.live[at] = slot;
+        if (d == depth) {
+            if ((int)pre >= A.cap_live_d) { atomicOr(err, kErrCapacity); return; }
+            A.lv_vnode[pre] = A.vnode[slot];
+        }
+    }
+    // chains the counts: candidates of depth d + 1 = 8 x live of depth d + roots of d + 1
+    __device__ void done(unsigned total) const {
+        const int nl = (int)total;
+        c->sub_nlive[d] = nl;
+        const int cend = c->sub_cbase[d] + c->sub_cand[d];
+        if (d < depth) {
+            const long long nc = 8LL * nl + c->sub_nroots[d + 1];
+            c->sub_cbase[d + 1] = cend;
+            c->sub_lbase[d + 1] = c->sub_lbase[d] + nl;
+            if (cend + nc > (long long)A.cap_nodes || c->sub_lbase[d] + nl > A.cap_nodes) {
+                atomicOr(err, kErrCapacity);
+                c->sub_cand[d + 1] = 0;
+            } else {
+                c->sub_cand[d + 1] = (int)nc;
+            }
+        } else {
+            // live cells beyond either capacity were not stored (and flagged)
+            int n = nl;
+            if (n > A.cap_live_d) n = A.cap_live_d;
+            if (n > A.cap_nodes - c->sub_lbase[d]) n = A.cap_nodes - c->sub_lbase[d];
+            c->n_sub_nodes = cend;
+            c->n_sub_dnodes = n;
+        }
+    }
+};
+
+// index of virtual node v among the live depth-D cells (sorted), or -1
+__device__ __forceinline__ int live_index(const int* lv_vnode, int n, int v) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (lv_vnode[mid] < v) lo = mid + 1;
+        else hi = mid;
+    }
+    return (lo < n && lv_vnode[lo] == v) ? lo : -1;
+}
+
+// per live depth-D cell: the live index of each same-depth sub neighbour (-1: none, an
+// octree node, or a cell with a certain sign)
+__global__ void __launch_bounds__(kBlock) k_sub_live_neigh(const Counters* c, int depth, SubArrays A,
+                                                           int* lv_nb, size_t dstride, int na) {
+    const int nl = c->n_sub_dnodes;
+    const int lb = c->sub_lbase[depth];
+    PSR_GRID_STRIDE(L, nl) {
+        const int slot = A.live[lb + L];
+#pragma unroll 1
+        for (int k = 0; k < 27; ++k) {
+            const int v = A.neigh[(size_t)k * A.cstride + slot];
+            lv_nb[(size_t)k * dstride + L] = (k == 13) ? L : ((v >= na) ? live_index(A.lv_vnode, nl, v - na) : -1);
+        }
     }
 }
 
-__device__ __forceinline__ void sub_center(int nb, int na, const float* cx, const float* cy, const float* cz,
-                                           const float* s_cx, const float* s_cy, const float* s_cz, float& x, float& y,
-                                           float& z) {
-    if (nb < na) { x = cx[nb]; y = cy[nb]; z = cz[nb]; }
-    else { x = s_cx[nb - na]; y = s_cy[nb - na]; z = s_cz[nb - na]; }
-}
-
-// D-level subdivision node o (0..n_sub_dnodes) -> subdivision node index
-__device__ __forceinline__ int sub_dnode_to_node(int o, const int* groups, int ng, int depth) {
-    const int g = find_group(groups, ng, 5, o);
-    const int* G = groups + (size_t)g * kGroupRec;
-    return G[3] + sub_level_off(G[0], G[2], depth) + (o - G[5]);
-}
-
-// vertex ownership among subdivision nodes only (initSubdivideVertexOwner :698-763).  Cells
-// with a certain sign take no part: a corner is owned by the smallest-key cell around it
-// without one.  Every corner of such a cell still gets exactly one record, the records of
-// crossing edges keep their owners (every cell around a crossing edge has a sign change),
-// and a vertex value does not depend on the cell that evaluates it (the same nonzero terms
-// in the same order), so the mesh is unchanged.
-__global__ void __launch_bounds__(kBlock) k_sub_vertex_owner(const Counters* c, int depth, const int* groups,
-                                                             const int* s_key, const int* s_neigh, size_t sstride,
-                                                             const signed char* s_sign, unsigned char* s_vmask,
-                                                             unsigned char* s_live, int na) {
-    const int SD = c->n_sub_dnodes;
-    const int ng = c->n_groups;
-    PSR_GRID_STRIDE(o, SD) {
-        const int s = sub_dnode_to_node(o, groups, ng, depth);
-        if (s_sign[s] != 0) { s_vmask[o] = 0; s_live[o] = 0; continue; }
-        s_live[o] = 1;
-        const int myk = s_key[s];
+// vertex ownership among the live depth-D cells (initSubdivideVertexOwner :698-763): a corner
+// is owned by the smallest-key live cell around it.  Cells with a certain sign take no part:
+// every corner of a live cell still gets exactly one record, the records of crossing edges
+// keep their owners (every cell around a crossing edge has a sign change, so is live), and a
+// vertex value does not depend on the cell that evaluates it (the same nonzero terms in the
+// same order), so the mesh is unchanged.
+__global__ void __launch_bounds__(kBlock) k_sub_vertex_owner(const Counters* c, int depth, SubArrays A,
+                                                             const int* lv_nb, size_t dstride,
+                                                             unsigned char* s_vmask) {
+    const int nl = c->n_sub_dnodes;
+    const int lb = c->sub_lbase[depth];
+    PSR_GRID_STRIDE(L, nl) {
+        const int myk = A.key[A.live[lb + L]];
         unsigned smaller = 0;
 #pragma unroll
         for (int k = 0; k < 27; ++k) {
             if (k == 13) continue;
-            const int nb = s_neigh[(size_t)k * sstride + s];
-            if (nb >= na && s_sign[nb - na] == 0 && s_key[nb - na] < myk) smaller |= 1u << k;
+            const int nb = lv_nb[(size_t)k * dstride + L];
+            if (nb >= 0 && A.key[A.live[lb + nb]] < myk) smaller |= 1u << k;
         }
         unsigned m = 0;
 #pragma unroll
         for (int q = 0; q < 8; ++q) if (!(smaller & vertex_cells(q))) m |= 1u << q;
-        s_vmask[o] = (unsigned char)m;
+        s_vmask[L] = (unsigned char)m;
     }
 }
 
 struct SubVertexStore {
     const unsigned char* vmask;
-    const int* groups;
-    const int* ng_ptr;
+    const Counters* c;
     int depth;
-    const float *s_cx, *s_cy, *s_cz;
+    SubArrays A;
     float *vx, *vy, *vz;
     int *vowner, *vkind;
     int cap;
-    int na;
     unsigned* err;
-    __device__ void operator()(int o, unsigned pre, unsigned cnt) const {
+    __device__ void operator()(int L, unsigned pre, unsigned cnt) const {
         if (!cnt) return;
         if ((int)(pre + cnt) > cap) { atomicOr(err, kErrCapacity); return; }
-        const int s = sub_dnode_to_node(o, groups, *ng_ptr, depth);
-        const unsigned m = vmask[o];
+        const int s = A.live[c->sub_lbase[depth] + L];
+        const unsigned m = vmask[L];
         const float hw = 1.0f / (float)(1 << (depth + 1));
         int q = (int)pre;
         for (int k = 0; k < 8; ++k) {
             if (!((m >> k) & 1)) continue;
-            vx[q] = __fadd_rn(s_cx[s], (float)(2 * (k & 1) - 1) * hw);
-            vy[q] = __fadd_rn(s_cy[s], (float)(2 * ((k >> 1) & 1) - 1) * hw);
-            vz[q] = __fadd_rn(s_cz[s], (float)(2 * ((k >> 2) & 1) - 1) * hw);
-            vowner[q] = na + s;
+            vx[q] = __fadd_rn(A.cx[s], (float)(2 * (k & 1) - 1) * hw);
+            vy[q] = __fadd_rn(A.cy[s], (float)(2 * ((k >> 1) & 1) - 1) * hw);
+            vz[q] = __fadd_rn(A.cz[s], (float)(2 * ((k >> 2) & 1) - 1) * hw);
+            vowner[q] = L;
             vkind[q] = k;
             ++q;
         }
     }
 };
 
-// D-level subdivision node index of subdivision node s (s must be at depth D)
-__device__ __forceinline__ int sub_node_to_dnode(int s, const int* groups, int ng, int depth) {
-    const int g = find_group(groups, ng, 3, s);
-    const int* G = groups + (size_t)g * kGroupRec;
-    return G[5] + (s - G[3] - sub_level_off(G[0], G[2], depth));
-}
-
-// maintainSubdivideVertexNodePointer (:765-810): s_vtx indexed by D-level sub node
-__global__ void __launch_bounds__(kBlock) k_sub_vertex_maintain(const Counters* c, int depth, const int* groups,
-                                                                const int* s_group, const int* s_neigh, size_t sstride,
-                                                                const int* s_depth, const int* vowner,
-                                                                const int* vkind, int* s_vtx, size_t dstride,
-                                                                int na) {
+// maintainSubdivideVertexNodePointer (:765-810): s_vtx indexed by live cell
+__global__ void __launch_bounds__(kBlock) k_sub_vertex_maintain(const Counters* c, const int* lv_nb,
+                                                                size_t dstride, const int* vowner, const int* vkind,
+                                                                int* s_vtx) {
     const int V = c->n_sub_vertices;
-    const int SD = c->n_sub_dnodes;
     PSR_GRID_STRIDE(v, V) {
-        const int ow = vowner[v] - na;
-        // neighbours of a subdivision node lie in its own group's region
-        const int* G = groups + (size_t)s_group[ow] * kGroupRec;
-        const int dbase = G[3] + sub_level_off(G[0], G[2], depth) - G[5];   // node - dnode
+        const int ow = vowner[v];
         int mx, my, mz;
         corner_sides(vkind[v], mx, my, mz);
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
             const int ax = (j & 1) ? mx : 0, ay = (j & 2) ? my : 0, az = (j & 4) ? mz : 0;
-            const int nb = s_neigh[(size_t)nslot(ax, ay, az) * sstride + ow];
-            if (nb >= na && s_depth[nb - na] == depth) {
-                const int dn = nb - na - dbase;
-                if ((unsigned)dn < (unsigned)SD) s_vtx[(size_t)vertex_slot_of(ax, ay, az, mx, my, mz) * dstride + dn] = v + 1;
-            }
+            const int nb = lv_nb[(size_t)nslot(ax, ay, az) * dstride + ow];
+            if (nb >= 0) s_vtx[(size_t)vertex_slot_of(ax, ay, az, mx, my, mz) * dstride + nb] = v + 1;
         }
     }
 }
 
-// edge ownership among subdivision nodes only (initSubdivideEdgeArray :812-886), among the
-// cells without a certain sign as for the vertices
-__global__ void __launch_bounds__(kBlock) k_sub_edge_owner(const Counters* c, int depth, const int* groups,
-                                                           const int* s_key, const int* s_neigh, size_t sstride,
-                                                           const unsigned char* s_live, const signed char* s_sign,
-                                                           unsigned short* s_emask, int na) {
-    const int SD = c->n_sub_dnodes;
-    const int ng = c->n_groups;
-    PSR_GRID_STRIDE(o, SD) {
-        if (!s_live[o]) { s_emask[o] = 0; continue; }
-        const int s = sub_dnode_to_node(o, groups, ng, depth);
-        const int myk = s_key[s];
+// edge ownership among the live depth-D cells (initSubdivideEdgeArray :812-886)
+__global__ void __launch_bounds__(kBlock) k_sub_edge_owner(const Counters* c, int depth, SubArrays A,
+                                                           const int* lv_nb, size_t dstride,
+                                                           unsigned short* s_emask) {
+    const int nl = c->n_sub_dnodes;
+    const int lb = c->sub_lbase[depth];
+    PSR_GRID_STRIDE(L, nl) {
+        const int myk = A.key[A.live[lb + L]];
         unsigned smaller = 0;
 #pragma unroll
         for (int k = 0; k < 27; ++k) {
             if (k == 13 || k == 0 || k == 2 || k == 6 || k == 8 || k == 18 || k == 20 || k == 24 || k == 26)
                 continue;   // corner-diagonal cells touch no edge
-            const int nb = s_neigh[(size_t)k * sstride + s];
-            if (nb >= na && s_sign[nb - na] == 0 && s_key[nb - na] < myk) smaller |= 1u << k;
+            const int nb = lv_nb[(size_t)k * dstride + L];
+            if (nb >= 0 && A.key[A.live[lb + nb]] < myk) smaller |= 1u << k;
         }
         unsigned m = 0;
 #pragma unroll
         for (int e = 0; e < 12; ++e) if (!(smaller & edge_cells(e))) m |= 1u << e;
-        s_emask[o] = (unsigned short)m;
+        s_emask[L] = (unsigned short)m;
     }
 }
 
 struct SubEdgeStore {
     const unsigned short* emask;
-    const int* groups;
-    const int* ng_ptr;
-    int depth;
-    int *eowner, *ekind, *edn;
+    int *eowner, *ekind;
+    unsigned* edge_of_live;   // sub-edge prefix per live cell (for the part table)
     int cap;
-    int na;
     unsigned* err;
-    __device__ void operator()(int o, unsigned pre, unsigned cnt) const {
+    __device__ void operator()(int L, unsigned pre, unsigned cnt) const {
+        edge_of_live[L] = pre;
         if (!cnt) return;
         if ((int)(pre + cnt) > cap) { atomicOr(err, kErrCapacity); return; }
-        const int s = sub_dnode_to_node(o, groups, *ng_ptr, depth);
-        const unsigned m = emask[o];
+        const unsigned m = emask[L];
         int q = (int)pre;
         for (int e = 0; e < 12; ++e)
-            if ((m >> e) & 1) { eowner[q] = na + s; ekind[q] = e; edn[q] = o; ++q; }
+            if ((m >> e) & 1) { eowner[q] = L; ekind[q] = e; ++q; }
     }
 };
 
 // maintainSubdivideEdgeNodePointer (:888-949)
-__global__ void __launch_bounds__(kBlock) k_sub_edge_maintain(const Counters* c, int depth, const int* groups,
-                                                              const int* s_group, const int* s_neigh, size_t sstride,
-                                                              const int* s_depth,
-                                                              const int* eowner, const int* ekind, int* s_edge,
-                                                              size_t dstride, int na) {
+__global__ void __launch_bounds__(kBlock) k_sub_edge_maintain(const Counters* c, const int* lv_nb, size_t dstride,
+                                                              const int* eowner, const int* ekind, int* s_edge) {
     const int E = c->n_sub_edges;
-    const int SD = c->n_sub_dnodes;
     PSR_GRID_STRIDE(ei, E) {
-        const int ow = eowner[ei] - na, kind = ekind[ei];
-        // neighbours of a subdivision node lie in its own group's region
-        const int* G = groups + (size_t)s_group[ow] * kGroupRec;
-        const int dbase = G[3] + sub_level_off(G[0], G[2], depth) - G[5];   // node - dnode
+        const int ow = eowner[ei], kind = ekind[ei];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             int a[3];
             edge_offset(kind, j, a);
-            const int nb = s_neigh[(size_t)nslot(a[0], a[1], a[2]) * sstride + ow];
-            if (nb >= na && s_depth[nb - na] == depth) {
-                const int dn = nb - na - dbase;
-                if ((unsigned)dn < (unsigned)SD) s_edge[(size_t)edge_slot_of(kind, a) * dstride + dn] = ei + 1;
-            }
+            const int nb = lv_nb[(size_t)nslot(a[0], a[1], a[2]) * dstride + ow];
+            if (nb >= 0) s_edge[(size_t)edge_slot_of(kind, a) * dstride + nb] = ei + 1;
         }
     }
 }
@@ -1165,70 +1186,68 @@ __global__ void __launch_bounds__(kBlock) k_sub_edge_maintain(const Counters* c,
 __global__ void __launch_bounds__(kBlock) k_sub_vertex_values(const Counters* c, int depth, const float* vx,
                                                               const float* vy, const float* vz, const int* vowner,
                                                               const int* neigh, size_t stride, const int* parent,
-                                                              const int* s_neigh, size_t sstride,
-                                                              const int* s_parent, const int* s_root,
-                                                              const int* s_jump, const int* s_depth,
-                                                              const float* s_cx, const float* s_cy,
-                                                              const float* s_cz, const int* enc, const float* x,
-                                                              float* vvalue, int na) {
+                                                              const int* groups, const int* root_self, SubArrays A,
+                                                              const int* enc, const float* x, float* vvalue, int na) {
     const int V = c->n_sub_vertices;
     const float iso = c->iso;
+    const int lb = c->sub_lbase[depth];
     PSR_GRID_STRIDE(v, V) {
         float val = 0.0f;
-        int now = vowner[v];
         const float qx = vx[v], qy = vy[v], qz = vz[v];
-        if (now > 0) {
-            while (now != -1) {
-                if (now < na) {   // octree levels
-                    val = level_terms(now, val, qx, qy, qz, depth, neigh, stride, enc, x);
-                    now = parent[now];
-                    continue;
-                }
-                // levels whose 27 neighbours are all zero-valued subdivision nodes add nothing:
-                // hop to the nearest contributing node on the way to the root
-                const int sn = s_jump[now - na];
-                now = s_parent[sn];
-                const int d = s_depth[sn];
-                const float sc = (float)(1 << d);
-                const int base = (1 << d) - 1;
-                const int ox = base + (int)__fmul_rn(s_cx[sn], sc);
-                const int oy = base + (int)__fmul_rn(s_cy[sn], sc);
-                const int oz = base + (int)__fmul_rn(s_cz[sn], sc);
-                float bx[3], by[3], bz[3];
+        const int own = A.live[lb + vowner[v]];
+        const int* G = groups + (size_t)A.group[own] * kGroupRec;
+        // levels whose 27 neighbours are all zero-valued subdivision nodes add nothing: hop
+        // to the nearest contributing node on the way to the root
+        int sn = A.jump[own];
+        int now;
+        while (true) {
+            const int d = A.depth[sn];
+            const float sc = (float)(1 << d);
+            const int base = (1 << d) - 1;
+            const int ox = base + (int)__fmul_rn(A.cx[sn], sc);
+            const int oy = base + (int)__fmul_rn(A.cy[sn], sc);
+            const int oz = base + (int)__fmul_rn(A.cz[sn], sc);
+            float bx[3], by[3], bz[3];
 #pragma unroll
-                for (int j = 0; j < 3; ++j) {
-                    bx[j] = basis32(ox - 1 + j, qx);
-                    by[j] = basis32(oy - 1 + j, qy);
-                    bz[j] = basis32(oz - 1 + j, qz);
-                }
-#pragma unroll
-                for (int k = 0; k < 27; ++k) {
-                    int nb = s_neigh[(size_t)k * sstride + sn];
-                    if (nb == -1) continue;
-                    if (nb >= na) {
-                        nb = s_root[nb - na];
-                        if (nb < 0) continue;
-                    }
-                    float t = __fmul_rn(x[nb], bx[k / 9]);
-                    t = __fmul_rn(t, by[(k / 3) % 3]);
-                    t = __fmul_rn(t, bz[k % 3]);
-                    val = __fadd_rn(val, t);
-                }
+            for (int j = 0; j < 3; ++j) {
+                bx[j] = basis32(ox - 1 + j, qx);
+                by[j] = basis32(oy - 1 + j, qy);
+                bz[j] = basis32(oz - 1 + j, qz);
             }
+#pragma unroll
+            for (int k = 0; k < 27; ++k) {
+                int nb = A.neigh[(size_t)k * A.cstride + sn];
+                if (nb == -1) continue;
+                if (nb >= na) {
+                    nb = sub_value_node(nb, na, G, root_self);
+                    if (nb < 0) continue;
+                }
+                float t = __fmul_rn(x[nb], bx[k / 9]);
+                t = __fmul_rn(t, by[(k / 3) % 3]);
+                t = __fmul_rn(t, bz[k % 3]);
+                val = __fadd_rn(val, t);
+            }
+            const int p = A.parent[sn];
+            if (p < 0) { now = -2 - p; break; }
+            sn = A.jump[p];
+        }
+        while (now != -1) {   // octree levels
+            val = level_terms(now, val, qx, qy, qz, depth, neigh, stride, enc, x);
+            now = parent[now];
         }
         vvalue[v] = __fsub_rn(val, iso);
     }
 }
 
 struct SubCrossLoad {
-    const int* edn;   // D-level subdivision node owning the edge
+    const int* eowner;   // live cell owning the edge
     const int* ekind;
     const int* s_vtx;
     size_t dstride;
     const float* vvalue;
     unsigned* err;
     __device__ unsigned operator()(int e) const {
-        const int dn = edn[e];
+        const int dn = eowner[e];
         const int kind = ekind[e];
         const float a = ptr_value(vvalue, s_vtx[(size_t)__ldg(&g_tab.edge_vertex[kind][0]) * dstride + dn], err);
         const float b = ptr_value(vvalue, s_vtx[(size_t)__ldg(&g_tab.edge_vertex[kind][1]) * dstride + dn], err);
@@ -1236,7 +1255,7 @@ struct SubCrossLoad {
     }
 };
 struct SubCrossStore {
-    const int* edn;
+    const int* eowner;
     const int* ekind;
     const int* s_vtx;
     size_t dstride;
@@ -1252,7 +1271,7 @@ struct SubCrossStore {
         if (!flag) return;
         const int at = *voff_ptr + (int)pre;
         if (at >= cap) { atomicOr(err, kErrCapacity); return; }
-        const int dn = edn[e];
+        const int dn = eowner[e];
         const int kind = ekind[e];
         const int v1 = s_vtx[(size_t)__ldg(&g_tab.edge_vertex[kind][0]) * dstride + dn] - 1;
         const int v2 = s_vtx[(size_t)__ldg(&g_tab.edge_vertex[kind][1]) * dstride + dn] - 1;
@@ -1266,58 +1285,69 @@ struct SubCubeLoad {
     const int* s_vtx;
     size_t dstride;
     const float* vvalue;
-    const unsigned char* live;
     int* cube_class;
     unsigned* err;
-    __device__ unsigned operator()(int o) const {
-        if (!live[o]) { cube_class[o] = 0; return 0u; }   // certain sign: no triangle
+    __device__ unsigned operator()(int L) const {
         int cls = 0;
 #pragma unroll
         for (int q = 0; q < 8; ++q)
-            if (ptr_value(vvalue, s_vtx[(size_t)q * dstride + o], err) < 0.0f) cls |= 1 << q;
-        cube_class[o] = cls;
+            if (ptr_value(vvalue, s_vtx[(size_t)q * dstride + L], err) < 0.0f) cls |= 1 << q;
+        cube_class[L] = cls;
         return (unsigned)__ldg(&g_tab.mc_count[cls]);
     }
 };
 
-// group-local first crossing index of group g: ecross of the group's first sub edge
+// triangles of a live cell; indices relative to its group's first crossing
 struct SubCubeStore {
     const int* cube_class;
     const int* s_edge;
     size_t dstride;
     const unsigned* ecross;
     const unsigned* group_cross0;   // per group: crossing prefix at its first edge
-    const int* groups;
-    const int* ng_ptr;
+    const Counters* c;
+    int depth;
+    SubArrays A;
     int* part_t;
     const int* toff_ptr;
     int cap;
     unsigned* err;
-    __device__ void operator()(int o, unsigned pre, unsigned cnt) const {
+    __device__ void operator()(int L, unsigned pre, unsigned cnt) const {
         if (!cnt) return;
-        const int g = find_group(groups, *ng_ptr, 5, o);
+        const int g = A.group[A.live[c->sub_lbase[depth] + L]];
         const unsigned base = group_cross0[g];
-        const int cls = cube_class[o];
+        const int cls = cube_class[L];
         const unsigned long long tri = __ldg(&g_tab.mc_tri[cls]);
         for (int t = 0; t < (int)cnt; ++t) {
             const int at = *toff_ptr + (int)pre + t;
             if (at >= cap) { atomicOr(err, kErrCapacity); continue; }
             for (int a = 0; a < 3; ++a) {
                 const int e = (int)((tri >> (4 * (3 * t + a))) & 0xF);
-                const int ei = s_edge[(size_t)e * dstride + o] - 1;
+                const int ei = s_edge[(size_t)e * dstride + L] - 1;
                 part_t[3 * (size_t)at + a] = (ei >= 0) ? (int)(ecross[ei] - base) : -1;
             }
         }
     }
 };
 
+// first live index at or after virtual node v
+__device__ __forceinline__ int live_lower_bound(const int* lv_vnode, int n, int v) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (lv_vnode[mid] < v) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
 // per-group first sub edge / first crossing / first triangle -> part table
 // parts: [0] main, [1 + g] group g.  part record: vstart, vcount, tstart, tcount
-__global__ void k_part_table(Counters* c, const int* groups, const unsigned* edge_of_dnode, const unsigned* ecross_sub, const unsigned* tri_of_dnode,
+__global__ void k_part_table(Counters* c, int depth, const int* groups, const int* lv_vnode,
+                             const unsigned* edge_of_live, const unsigned* ecross_sub, const unsigned* tri_of_live,
                              unsigned* group_cross0, int* parts) {
     const int ng = c->n_groups;
     const int nE = c->n_sub_edges;
-    const int nSD = c->n_sub_dnodes;
+    const int nl = c->n_sub_dnodes;
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         parts[0] = 0;
         parts[1] = c->n_cross;
@@ -1326,14 +1356,17 @@ __global__ void k_part_table(Counters* c, const int* groups, const unsigned* edg
     }
     PSR_GRID_STRIDE(g, ng) {   // one thread per group (independent entries)
         const int* G = groups + (size_t)g * kGroupRec;
-        const int d0 = G[5], d1 = G[5] + G[6];
-        // first sub edge of the group = edge prefix at its first D-level sub node
-        const int e0 = (d0 < nSD) ? (int)edge_of_dnode[d0] : nE;
-        const int e1 = (d1 < nSD) ? (int)edge_of_dnode[d1] : nE;
+        const int v0 = G[3] + sub_level_off(G[0], G[2], depth);
+        const int v1 = G[3] + G[4];
+        // first sub edge of the group = edge prefix at its first live cell
+        const int L0 = live_lower_bound(lv_vnode, nl, v0);
+        const int L1 = live_lower_bound(lv_vnode, nl, v1);
+        const int e0 = (L0 < nl) ? (int)edge_of_live[L0] : nE;
+        const int e1 = (L1 < nl) ? (int)edge_of_live[L1] : nE;
         const unsigned x0 = (e0 < nE) ? ecross_sub[e0] : (unsigned)c->n_sub_cross;
         const unsigned x1 = (e1 < nE) ? ecross_sub[e1] : (unsigned)c->n_sub_cross;
-        const unsigned t0 = (d0 < nSD) ? tri_of_dnode[d0] : (unsigned)c->n_sub_tri;
-        const unsigned t1 = (d1 < nSD) ? tri_of_dnode[d1] : (unsigned)c->n_sub_tri;
+        const unsigned t0 = (L0 < nl) ? tri_of_live[L0] : (unsigned)c->n_sub_tri;
+        const unsigned t1 = (L1 < nl) ? tri_of_live[L1] : (unsigned)c->n_sub_tri;
         group_cross0[g] = x0;
         int* P = parts + 4 * (size_t)(g + 1);
         P[0] = c->n_cross + (int)x0;
@@ -1495,20 +1528,16 @@ cudaError_t mesh_build_impl(Workspace& ws, const MeshBufs& mb) {
     if (e != cudaSuccess) return e;
     k_group_count<<<1, 1, 0, s>>>(c, total, mb.max_groups);
     k_group_sizes<<<gm, kBlock, 0, s>>>(c, D, ws.sub_root, ws.ndepth, mb.groups);
-    unsigned* total2 = (unsigned*)(mb.misc + 8);
     e = launch_scan(GroupFieldLoad{mb.groups, 4}, GroupFieldStore{mb.groups, 3}, &c->n_groups, 0, ws.scan, total, err, s);
     if (e != cudaSuccess) return e;
-    e = launch_scan(GroupFieldLoad{mb.groups, 6}, GroupFieldStore{mb.groups, 5}, &c->n_groups, 0, ws.scan, total2, err,
-                    s);
-    if (e != cudaSuccess) return e;
-    k_group_totals<<<1, 1, 0, s>>>(c, total, total2, ws.cap.sub_nodes, ws.cap.sub_dnodes);
-    k_root_overlay<<<gm, kBlock, 0, s>>>(c, D, ws.sub_root, ws.ndepth, ws.key, ws.parent, ws.root_group, mb.groups,
-                                         ws.sub_root_depth, mb.ov_group, mb.ov_sub, stride);
+    k_group_totals<<<1, 1, 0, s>>>(c, total, ws.cap.nodes);
+    k_root_overlay<<<gm, kBlock, 0, s>>>(c, D, ws.sub_root, ws.ndepth, ws.key, ws.parent, ws.neigh, ws.root_group,
+                                         mb.groups, ws.sub_root_depth, ws.root_self, mb.ov_group, mb.ov_sub, stride);
     return cudaGetLastError();
 }
 
-// Subdivision-space nodes are numbered cap.nodes + local index: every such number is
-// larger than any octree index, which is all the kernels compare against.
+// Subdivision nodes appear in neighbour tables as cap.nodes + virtual index: every such
+// number is larger than any octree index, which is all the kernels compare against.
 cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
     cudaStream_t s = ws.stream;
     const int D = ws.depth;
@@ -1516,62 +1545,59 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
     unsigned* err = &c->error;
     unsigned* total = (unsigned*)&c->scan_total;
     const size_t stride = (size_t)ws.cap.nodes;
-    const size_t sstride = (size_t)ws.cap.sub_nodes;
     const size_t dstride = (size_t)ws.cap.sub_dnodes;
     const int na = ws.cap.nodes;
-    const int gs = grid_for(ws, ws.cap.sub_nodes);
+    const int gl = grid_for(ws, ws.cap.sub_dnodes);
     cudaError_t e;
-    k_sub_build<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.sub_root, ws.key, ws.parent, ws.neigh, stride, ws.s_key,
-                                      ws.s_parent, ws.s_first_child, ws.s_depth, ws.s_group, ws.s_root, ws.s_cx,
-                                      ws.s_cy, ws.s_cz, na);
-    for (int d = 1; d <= D; ++d)
-        k_sub_neighbours<<<gs, kBlock, 0, s>>>(c, d, D, mb.groups, ws.neigh, stride, ws.first_child, mb.ov_group,
-                                               mb.ov_sub, ws.s_key, ws.s_parent, ws.s_first_child, ws.s_depth,
-                                               ws.s_group, ws.s_root, ws.s_neigh, ws.s_jump, ws.s_sign, sstride,
-                                               ws.parent, ws.s_cx, ws.s_cy, ws.s_cz, ws.enc, ws.xsol, na);
-    // s_vtx / s_edge need no clearing: every slot of a cell without a certain sign is written
-    // by the owner of that vertex / edge, and no other cell's slots are read
-    k_sub_vertex_owner<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.s_key, ws.s_neigh, sstride, ws.s_sign, ws.s_vmask,
-                                             ws.s_live, na);
+    SubArrays A{ws.c_vnode, ws.c_key, ws.c_group, ws.c_parent, ws.c_jump, ws.c_depth, ws.c_cx, ws.c_cy, ws.c_cz,
+                ws.c_neigh, (size_t)ws.cap.sub_nodes, ws.c_live, ws.lv_vnode, ws.cap.sub_nodes, ws.cap.sub_dnodes};
+    k_sub_setup<<<1, 32, 0, s>>>(c, D, ws.sub_root_depth, ws.cap.sub_nodes);
+    // depth after depth: candidates (children of the live nodes above, then the roots of this
+    // depth), their neighbours and sign tests; the live ones are compacted in order
+    for (int d = 1; d <= D; ++d) {
+        e = launch_scan<1>(SubLevelLoad{c, d, D, na, mb.groups, ws.sub_root, ws.root_group, ws.root_self, ws.key,
+                                        ws.neigh, stride, ws.first_child, ws.parent, mb.ov_group, mb.ov_sub, ws.enc,
+                                        ws.xsol, A},
+                           SubLevelStore{c, d, D, A, err}, &c->sub_cand[d], 0, ws.scan, total, err, s, ScanCount{},
+                           1);
+        if (e != cudaSuccess) return e;
+    }
+    // the live depth-D cells carry every record from here on, indexed by their live index
+    k_sub_live_neigh<<<gl, kBlock, 0, s>>>(c, D, A, ws.lv_nb, dstride, na);
+    // s_vtx / s_edge need no clearing: every slot of a live cell is written by the owner of
+    // that vertex / edge
+    k_sub_vertex_owner<<<gl, kBlock, 0, s>>>(c, D, A, ws.lv_nb, dstride, ws.s_vmask);
     e = launch_scan<2>(PopcLoad8{ws.s_vmask},
-                    SubVertexStore{ws.s_vmask, mb.groups, &c->n_groups, D, ws.s_cx, ws.s_cy, ws.s_cz, ws.sv_x, ws.sv_y,
-                                   ws.sv_z, ws.sv_owner, ws.sv_kind, 8 * ws.cap.sub_dnodes, na, err},
-                    &c->n_sub_dnodes, 0, ws.scan, total, err, s, ScanCount{&c->n_sub_vertices, 8 * ws.cap.sub_dnodes});
+                       SubVertexStore{ws.s_vmask, c, D, A, ws.sv_x, ws.sv_y, ws.sv_z, ws.sv_owner, ws.sv_kind,
+                                      8 * ws.cap.sub_dnodes, err},
+                       &c->n_sub_dnodes, 0, ws.scan, total, err, s, ScanCount{&c->n_sub_vertices, 8 * ws.cap.sub_dnodes});
     if (e != cudaSuccess) return e;
-    k_sub_vertex_maintain<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.s_group, ws.s_neigh, sstride, ws.s_depth, ws.sv_owner,
-                                                ws.sv_kind, ws.s_vtx, dstride, na);
-    k_sub_edge_owner<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.s_key, ws.s_neigh, sstride, ws.s_live, ws.s_sign,
-                                           ws.s_emask, na);
+    k_sub_vertex_maintain<<<gl, kBlock, 0, s>>>(c, ws.lv_nb, dstride, ws.sv_owner, ws.sv_kind, ws.s_vtx);
+    k_sub_edge_owner<<<gl, kBlock, 0, s>>>(c, D, A, ws.lv_nb, dstride, ws.s_emask);
     e = launch_scan<2>(PopcLoad16{ws.s_emask},
-                    SubEdgeStore{ws.s_emask, mb.groups, &c->n_groups, D, ws.se_owner, ws.se_kind, ws.se_dn,
-                                 12 * ws.cap.sub_dnodes, na, err},
-                    &c->n_sub_dnodes, 0, ws.scan, total, err, s, ScanCount{&c->n_sub_edges, 12 * ws.cap.sub_dnodes});
+                       SubEdgeStore{ws.s_emask, ws.se_owner, ws.se_kind, mb.edge_of_dnode, 12 * ws.cap.sub_dnodes, err},
+                       &c->n_sub_dnodes, 0, ws.scan, total, err, s, ScanCount{&c->n_sub_edges, 12 * ws.cap.sub_dnodes});
     if (e != cudaSuccess) return e;
-    // edge prefix per D-level sub node (for the part table): recompute via a scan of popcounts
-    e = launch_scan(PopcLoad16{ws.s_emask}, StoreExclusive{mb.edge_of_dnode}, &c->n_sub_dnodes, 0, ws.scan, total,
-                    err, s);
-    if (e != cudaSuccess) return e;
-    k_sub_edge_maintain<<<gs, kBlock, 0, s>>>(c, D, mb.groups, ws.s_group, ws.s_neigh, sstride, ws.s_depth, ws.se_owner,
-                                              ws.se_kind, ws.s_edge, dstride, na);
-    k_sub_vertex_values<<<gs, kBlock, 0, s>>>(c, D, ws.sv_x, ws.sv_y, ws.sv_z, ws.sv_owner, ws.neigh, stride, ws.parent,
-                                              ws.s_neigh, sstride, ws.s_parent, ws.s_root, ws.s_jump, ws.s_depth,
-                                              ws.s_cx, ws.s_cy, ws.s_cz, ws.enc, ws.xsol, ws.sv_value, na);
+    k_sub_edge_maintain<<<gl, kBlock, 0, s>>>(c, ws.lv_nb, dstride, ws.se_owner, ws.se_kind, ws.s_edge);
+    k_sub_vertex_values<<<gl, kBlock, 0, s>>>(c, D, ws.sv_x, ws.sv_y, ws.sv_z, ws.sv_owner, ws.neigh, stride,
+                                              ws.parent, mb.groups, ws.root_self, A, ws.enc, ws.xsol, ws.sv_value, na);
     // crossings: staged after the main part's vertices
-    e = launch_scan<2>(SubCrossLoad{ws.se_dn, ws.se_kind, ws.s_vtx, dstride, ws.sv_value, err},
-                    SubCrossStore{ws.se_dn, ws.se_kind, ws.s_vtx, dstride, ws.sv_value, ws.sv_x, ws.sv_y, ws.sv_z,
-                                  ws.se_cross, ws.part_v, &c->n_cross, ws.part_cap_v, err},
-                    &c->n_sub_edges, 0, ws.scan, total, err, s, ScanCount{&c->n_sub_cross, ws.part_cap_v});
+    e = launch_scan<2>(SubCrossLoad{ws.se_owner, ws.se_kind, ws.s_vtx, dstride, ws.sv_value, err},
+                       SubCrossStore{ws.se_owner, ws.se_kind, ws.s_vtx, dstride, ws.sv_value, ws.sv_x, ws.sv_y,
+                                     ws.sv_z, ws.se_cross, ws.part_v, &c->n_cross, ws.part_cap_v, err},
+                       &c->n_sub_edges, 0, ws.scan, total, err, s, ScanCount{&c->n_sub_cross, ws.part_cap_v});
     if (e != cudaSuccess) return e;
-    // triangle prefix per D-level sub node
-    e = launch_scan<2>(SubCubeLoad{ws.s_vtx, dstride, ws.sv_value, ws.s_live, ws.s_cube_class, err}, StoreExclusive{mb.tri_of_dnode},
-                    &c->n_sub_dnodes, 0, ws.scan, total, err, s, ScanCount{&c->n_sub_tri, ws.part_cap_t});
+    // triangle prefix per live cell
+    e = launch_scan<2>(SubCubeLoad{ws.s_vtx, dstride, ws.sv_value, ws.s_cube_class, err},
+                       StoreExclusive{mb.tri_of_dnode}, &c->n_sub_dnodes, 0, ws.scan, total, err, s,
+                       ScanCount{&c->n_sub_tri, ws.part_cap_t});
     if (e != cudaSuccess) return e;
-    k_part_table<<<grid_for(ws, 1 << 16), kBlock, 0, s>>>(c, mb.groups, mb.edge_of_dnode, ws.se_cross, mb.tri_of_dnode,
-                                 mb.group_cross0, mb.parts);
-    e = launch_scan<2>(SubCubeLoad{ws.s_vtx, dstride, ws.sv_value, ws.s_live, ws.s_cube_class, err},
-                    SubCubeStore{ws.s_cube_class, ws.s_edge, dstride, ws.se_cross, mb.group_cross0, mb.groups,
-                                 &c->n_groups, ws.part_t, &c->n_tri, ws.part_cap_t, err},
-                    &c->n_sub_dnodes, 0, ws.scan, total, err, s);
+    k_part_table<<<grid_for(ws, 1 << 16), kBlock, 0, s>>>(c, D, mb.groups, ws.lv_vnode, mb.edge_of_dnode, ws.se_cross,
+                                                          mb.tri_of_dnode, mb.group_cross0, mb.parts);
+    e = launch_scan<2>(SubCubeLoad{ws.s_vtx, dstride, ws.sv_value, ws.s_cube_class, err},
+                       SubCubeStore{ws.s_cube_class, ws.s_edge, dstride, ws.se_cross, mb.group_cross0, c, D, A,
+                                    ws.part_t, &c->n_tri, ws.part_cap_t, err},
+                       &c->n_sub_dnodes, 0, ws.scan, total, err, s);
     if (e != cudaSuccess) return e;
     // insertion of all parts
     int* n_parts = mb.misc;

@@ -27,6 +27,15 @@ struct ScanCount {
     int cap = 0;
 };
 
+// Store functors may define `void done(unsigned total) const`: the scan calls it once, after
+// the last element (or at once for an empty scan), to chain counts into the next launch.
+template <class S>
+__device__ __forceinline__ auto scan_done(const S& s, unsigned tot, int) -> decltype(s.done(tot), void()) {
+    s.done(tot);
+}
+template <class S>
+__device__ __forceinline__ void scan_done(const S&, unsigned, long) {}
+
 constexpr unsigned long long kFlagAgg = 1ull << 32;
 constexpr unsigned long long kFlagIncl = 1ull << 33;
 constexpr int kEpochShift = 34;
@@ -81,6 +90,7 @@ __global__ void __launch_bounds__(kBlock) k_scan(Load load, Store store, const i
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             *total = 0u;
             if (cnt.dst) *cnt.dst = 0;
+            scan_done(store, 0u, 0);
         }
         return;
     }
@@ -171,6 +181,7 @@ __global__ void __launch_bounds__(kBlock) k_scan(Load load, Store store, const i
                 if (tot > (unsigned)cnt.cap) { atomicOr(err, kErrCapacity); c = cnt.cap; }
                 *cnt.dst = c;
             }
+            scan_done(store, tot, 0);
         }
         __syncthreads();
     }

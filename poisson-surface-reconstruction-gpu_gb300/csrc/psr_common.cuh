@@ -28,10 +28,12 @@ struct Counters {
     int n_vertices, n_edges, n_faces;
     int n_cross, n_tri;
     int n_subroots;
-    int sub_depth_count[kMaxDepth + 1];
-    int sub_depth_start[kMaxDepth + 1];
-    int n_sub_nodes;              // all subdivision-space nodes over all groups
-    int n_sub_dnodes;             // D-level subdivision nodes
+    // subdivision, per depth d: candidates, their first compact slot, the first entry of
+    // the depth's live list, live nodes, first root index and roots of depth d
+    int sub_cand[kMaxDepth + 2], sub_cbase[kMaxDepth + 2], sub_lbase[kMaxDepth + 2];
+    int sub_nlive[kMaxDepth + 2], sub_rstart[kMaxDepth + 2], sub_nroots[kMaxDepth + 2];
+    int n_sub_nodes;              // subdivision nodes built (candidates of all depths)
+    int n_sub_dnodes;             // live depth-D subdivision cells
     int n_sub_vertices, n_sub_edges, n_sub_cross, n_sub_tri;
     int n_mesh_vertices, n_mesh_triangles;
     int scan_total;               // scratch total written by scans

@@ -36,8 +36,8 @@ struct MeshBufs {
     int* ov_sub;               // [8][cap.nodes]: root slot inside that group
     int* groups;               // group records (see mesh.cu)
     int max_groups;
-    unsigned* edge_of_dnode;   // sub-edge prefix per D-level subdivision node
-    unsigned* tri_of_dnode;    // sub-triangle prefix per D-level subdivision node
+    unsigned* edge_of_dnode;   // sub-edge prefix per live depth-D cell
+    unsigned* tri_of_dnode;    // sub-triangle prefix per live depth-D cell
     unsigned* group_cross0;    // per group: crossing prefix at its first sub edge
     int* parts;                // per output part: vertex start / count, triangle start / count
     unsigned* kept_prefix;     // per staged vertex: kept vertices before it
@@ -119,21 +119,22 @@ struct Workspace {
     int* sub_root;          // node index of each root (node order)
     int* sub_root_depth;
     int* root_group;        // per subdivision root: its group
-    // subdivision-space nodes of all groups (SoA)
-    int *s_key, *s_parent, *s_first_child, *s_neigh, *s_depth, *s_root;   // s_neigh: [27][cap.sub_nodes]
-    int* s_group;
-    int* s_jump;            // nearest sub-node on the path to the root with a neighbour carrying a value
-    signed char* s_sign;    // +1 / -1: F - iso keeps that sign on the whole closed cell; 0: not known
-    float *s_cx, *s_cy, *s_cz;
-    int *s_vtx, *s_edge;    // [8|12][cap.sub_dnodes] for D-level subdivision nodes
+    int* root_self;         // per root: the octree node it stands for
+    // subdivision candidates in compact slots (SoA, capacity cap.sub_nodes)
+    int *c_vnode, *c_key, *c_group, *c_parent, *c_jump, *c_depth;
+    float *c_cx, *c_cy, *c_cz;
+    int* c_neigh;           // [27][cap.sub_nodes]
+    int* c_live;            // live slots, depth after depth
+    // live depth-D cells (capacity cap.sub_dnodes)
+    int* lv_vnode;          // virtual index, ascending
+    int* lv_nb;             // [27][cap.sub_dnodes]: live index of each same-depth neighbour
+    int *s_vtx, *s_edge;    // [8|12][cap.sub_dnodes]
     unsigned char* s_vmask;
-    unsigned char* s_live;  // per D-level sub node: 1 unless its cell has a certain sign
     unsigned short* s_emask;
     float *sv_x, *sv_y, *sv_z;
     int *sv_owner, *sv_kind;
     float* sv_value;
     int *se_owner, *se_kind;
-    int* se_dn;             // D-level subdivision node owning each subdivision edge
     unsigned* se_cross;
     int* s_cube_class;
 
