@@ -237,6 +237,8 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     A.add(ws.sub_root_depth, (size_t)nodes);
     A.add(ws.root_group, (size_t)nodes);
     A.add(ws.root_self, (size_t)nodes);
+    ws.cap_poly = (int)std::max<long long>(65536, nodes / 16);
+    A.add(ws.root_poly, 28 * (size_t)ws.cap_poly);
     A.add(ws.c_vnode, (size_t)subn); A.add(ws.c_key, (size_t)subn); A.add(ws.c_group, (size_t)subn);
     A.add(ws.c_parent, (size_t)subn); A.add(ws.c_jump, (size_t)subn); A.add(ws.c_depth, (size_t)subn);
     A.add(ws.c_cx, (size_t)subn); A.add(ws.c_cy, (size_t)subn); A.add(ws.c_cz, (size_t)subn);

@@ -654,30 +654,37 @@ __device__ __forceinline__ int sub_level_off(int rd, int n, int d) {
     return off;
 }
 
-// per-depth candidate bookkeeping (Counters::sub_*): [d] for depth d
+// per-depth candidate bookkeeping (Counters::sub_*): [d] for depth d; one lane per depth
 __global__ void k_sub_setup(Counters* c, int depth, const int* sub_root_depth, int cap_nodes) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int d = threadIdx.x;
     const int R = c->n_subroots;
-    int start = 0;
-    for (int d = 0; d <= depth + 1; ++d) {
-        int lo = start, hi = R;   // first root deeper than d (roots are in depth order)
+    __shared__ int s_end[kMaxDepth + 2];
+    if (d <= depth + 1) {
+        int lo = 0, hi = R;   // first root deeper than d (roots are in depth order)
         while (lo < hi) {
             const int mid = (lo + hi) >> 1;
             if (sub_root_depth[mid] <= d) lo = mid + 1;
             else hi = mid;
         }
+        s_end[d] = lo;
+    }
+    __syncthreads();
+    if (d <= depth + 1) {
+        const int start = (d > 0) ? s_end[d - 1] : 0;
         c->sub_rstart[d] = start;
-        c->sub_nroots[d] = (c->n_groups > 0) ? lo - start : 0;
-        start = lo;
+        c->sub_nroots[d] = (c->n_groups > 0) ? s_end[d] - start : 0;
         c->sub_cand[d] = 0;
         c->sub_cbase[d] = 0;
         c->sub_lbase[d] = 0;
         c->sub_nlive[d] = 0;
     }
-    if (c->sub_nroots[1] > cap_nodes) atomicOr(&c->error, kErrCapacity);
-    else c->sub_cand[1] = c->sub_nroots[1];
-    c->n_sub_nodes = 0;
-    c->n_sub_dnodes = 0;
+    __syncthreads();
+    if (d == 0) {
+        if (c->sub_nroots[1] > cap_nodes) atomicOr(&c->error, kErrCapacity);
+        else c->sub_cand[1] = c->sub_nroots[1];
+        c->n_sub_nodes = 0;
+        c->n_sub_dnodes = 0;
+    }
 }
 
 struct SubArrays {
@@ -787,21 +794,106 @@ __device__ __forceinline__ int sub_value_node(int v, int na, const int* G, const
     return ((unsigned)local < (unsigned)G[2]) ? root_self[G[1] + local] : -1;
 }
 
-// sign of F - iso on the closed cell (centre q) of a node at depth d; sn = the slot of the
-// nearest node at or above it with a contributing neighbour
-__device__ __forceinline__ int sub_cell_sign(float qx, float qy, float qz, int d, int sn, const int* G,
-                                             int depth, const int* neigh, size_t stride, const int* parent,
-                                             const int* enc, const float* x, const int* root_self, float iso,
-                                             const SubArrays& A, int na) {
+// Levels up to a root's depth are the same for every cell below that root: their sum is one
+// tensor-product quadratic on the root's cell, kept as its 27 Bernstein coefficients
+// (root_poly[k][r], k < 27; [27][r]: sum |y| of those levels).  A cell inside it takes
+// them by Bernstein subdivision: with the cell at [a, b] of the root's unit interval, the
+// new coefficients are the blossom values P(a, a), P(a, b), P(b, b) -- convex weights, exact
+// for these dyadic a, b.
+__global__ void __launch_bounds__(kBlock) k_root_poly(const Counters* c, int depth, const int* sub_root,
+                                                      const int* ndepth, const float* ctr_x, const float* ctr_y,
+                                                      const float* ctr_z, const int* neigh, size_t stride,
+                                                      const int* parent, const int* enc, const float* x,
+                                                      float* root_poly, int cap_poly) {
+    const int R = c->n_subroots < cap_poly ? c->n_subroots : cap_poly;
+    PSR_GRID_STRIDE(r, R) {
+        const int node = sub_root[r];
+        const int rd = ndepth[node];
+        const float qx = ctr_x[node], qy = ctr_y[node], qz = ctr_z[node];
+        float C[27];
+#pragma unroll
+        for (int k = 0; k < 27; ++k) C[k] = 0.0f;
+        float mag = 0.0f, y[27];
+        for (int now = node; now >= 0; now = parent[now]) {
+            int ox, oy, oz;
+            decode_fn_index(enc[now], depth, ox, oy, oz);
+            const int l = ilog2_dev(ox + 1);
+#pragma unroll
+            for (int k = 0; k < 27; ++k) {
+                const int v = neigh[(size_t)k * stride + now];
+                y[k] = (v >= 0) ? x[v] : 0.0f;
+            }
+            sign_level(y, ox, oy, oz, qx, qy, qz, __int_as_float((126 + l - rd) << 23), C, mag);
+        }
+#pragma unroll
+        for (int k = 0; k < 27; ++k) root_poly[(size_t)k * cap_poly + r] = C[k];
+        root_poly[(size_t)27 * cap_poly + r] = mag;
+    }
+}
+
+// blossom matrix of [a, b] (rows: new coefficients, columns: old)
+__device__ __forceinline__ void blossom3(float a, float b, float (&M)[3][3]) {
+    const float a1 = 1.0f - a, b1 = 1.0f - b;
+    M[0][0] = a1 * a1; M[0][1] = 2.0f * a * a1;     M[0][2] = a * a;
+    M[1][0] = a1 * b1; M[1][1] = a1 * b + a * b1;   M[1][2] = a * b;
+    M[2][0] = b1 * b1; M[2][1] = 2.0f * b * b1;     M[2][2] = b * b;
+}
+
+// C += the root polynomial P subdivided to the cell at Morton code rel (m levels below it)
+__device__ __forceinline__ void add_subdivided(const float* P, size_t pstride, unsigned rel, int m, float (&C)[27]) {
+    int i3[3] = {0, 0, 0};
+    for (int j = 0; j < m; ++j)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) i3[a] |= (int)((rel >> (3 * j + 2 - a)) & 1u) << j;
+    const float inv = __int_as_float((127 - m) << 23);   // 2^-m
+    float Mx[3][3], My[3][3], Mz[3][3];
+    blossom3((float)i3[0] * inv, (float)(i3[0] + 1) * inv, Mx);
+    blossom3((float)i3[1] * inv, (float)(i3[1] + 1) * inv, My);
+    blossom3((float)i3[2] * inv, (float)(i3[2] + 1) * inv, Mz);
+    float p[27];
+#pragma unroll
+    for (int k = 0; k < 27; ++k) p[k] = P[(size_t)k * pstride];
+    float T1[27], T2[27];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int jk = 0; jk < 9; ++jk)
+            T1[a * 9 + jk] = fmaf(Mx[a][0], p[jk], fmaf(Mx[a][1], p[9 + jk], Mx[a][2] * p[18 + jk]));
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int bb = 0; bb < 3; ++bb)
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                T2[a * 9 + bb * 3 + k] = fmaf(My[bb][0], T1[a * 9 + k],
+                                              fmaf(My[bb][1], T1[a * 9 + 3 + k], My[bb][2] * T1[a * 9 + 6 + k]));
+#pragma unroll
+    for (int ab3 = 0; ab3 < 9; ++ab3)
+#pragma unroll
+        for (int gg = 0; gg < 3; ++gg)
+            C[ab3 * 3 + gg] += fmaf(Mz[gg][0], T2[ab3 * 3], fmaf(Mz[gg][1], T2[ab3 * 3 + 1], Mz[gg][2] * T2[ab3 * 3 + 2]));
+}
+
+// sign of F - iso on the closed cell (centre q) of a node at depth d below its root (rd < d;
+// root index r, Morton code rel below it); sn = the slot of the nearest node at or above it
+// with a contributing neighbour
+__device__ __forceinline__ int sub_cell_sign(float qx, float qy, float qz, int d, int rd, int r, unsigned rel,
+                                             int sn, const int* G, int depth, const int* neigh, size_t stride,
+                                             const int* parent, const int* enc, const float* x,
+                                             const int* root_self, const float* root_poly, int cap_poly,
+                                             float iso, const SubArrays& A, int na) {
     float C[27];
 #pragma unroll
     for (int k = 0; k < 27; ++k) C[k] = 0.0f;
     float mag = 0.0f;
     float y[27];
-    int now;
-    // subdivision levels that carry a value (jump hops over the others)
+    const bool poly = r < cap_poly;
+    int now = -1;
+    // subdivision levels that carry a value (jump hops over the others); with the root's
+    // polynomial at hand, the root's own level is in it
     while (true) {
         const int l = A.depth[sn];
+        if (poly && l == rd) break;
         const float sc = (float)(1 << l);
         const int base = (1 << l) - 1;
         const int ox = base + (int)__fmul_rn(A.cx[sn], sc);
@@ -818,18 +910,23 @@ __device__ __forceinline__ int sub_cell_sign(float qx, float qy, float qz, int d
         if (p < 0) { now = -2 - p; break; }
         sn = A.jump[p];
     }
-    // octree levels above the root
-    while (now >= 0) {
-        int ox, oy, oz;
-        decode_fn_index(enc[now], depth, ox, oy, oz);
-        const int l = ilog2_dev(ox + 1);
+    if (poly) {
+        add_subdivided(root_poly + r, (size_t)cap_poly, rel, d - rd, C);
+        mag += root_poly[(size_t)27 * cap_poly + r];
+    } else {
+        // octree levels above the root
+        while (now >= 0) {
+            int ox, oy, oz;
+            decode_fn_index(enc[now], depth, ox, oy, oz);
+            const int l = ilog2_dev(ox + 1);
 #pragma unroll
-        for (int k = 0; k < 27; ++k) {
-            const int v = neigh[(size_t)k * stride + now];
-            y[k] = (v >= 0) ? x[v] : 0.0f;
+            for (int k = 0; k < 27; ++k) {
+                const int v = neigh[(size_t)k * stride + now];
+                y[k] = (v >= 0) ? x[v] : 0.0f;
+            }
+            sign_level(y, ox, oy, oz, qx, qy, qz, __int_as_float((126 + l - d) << 23), C, mag);
+            now = parent[now];
         }
-        sign_level(y, ox, oy, oz, qx, qy, qz, __int_as_float((126 + l - d) << 23), C, mag);
-        now = parent[now];
     }
     float lo = C[0], hi = C[0];
 #pragma unroll
@@ -858,6 +955,8 @@ struct SubLevelLoad {
     const int* ov_sub;
     const int* enc;
     const float* x;
+    const float* root_poly;
+    int cap_poly;
     SubArrays A;
     __device__ unsigned operator()(int i) const {
         const int nl_prev = c->sub_nlive[d - 1];
@@ -975,8 +1074,9 @@ struct SubLevelLoad {
         A.cy[slot] = cc[1];
         A.cz[slot] = cc[2];
         if (at_root_depth || deeper) return 1u;
-        const int sg = sub_cell_sign(cc[0], cc[1], cc[2], d, jump, G, depth, neigh, stride, parent, enc, x,
-                                     root_self, c->iso, A, na);
+        const int r = G[1] + (int)((unsigned)local >> (3 * (d - G[0])));
+        const int sg = sub_cell_sign(cc[0], cc[1], cc[2], d, G[0], r, rel, jump, G, depth, neigh, stride, parent,
+                                     enc, x, root_self, root_poly, cap_poly, c->iso, A, na);
         return (sg == 0) ? 1u : 0u;
     }
 };
@@ -1034,18 +1134,16 @@ __device__ __forceinline__ int live_index(const int* lv_vnode, int n, int v) {
 }
 
 // per live depth-D cell: the live index of each same-depth sub neighbour (-1: none, an
-// octree node, or a cell with a certain sign)
+// octree node, or a cell with a certain sign); one thread per (cell, slot)
 __global__ void __launch_bounds__(kBlock) k_sub_live_neigh(const Counters* c, int depth, SubArrays A,
                                                            int* lv_nb, size_t dstride, int na) {
     const int nl = c->n_sub_dnodes;
     const int lb = c->sub_lbase[depth];
-    PSR_GRID_STRIDE(L, nl) {
-        const int slot = A.live[lb + L];
-#pragma unroll 1
-        for (int k = 0; k < 27; ++k) {
-            const int v = A.neigh[(size_t)k * A.cstride + slot];
-            lv_nb[(size_t)k * dstride + L] = (k == 13) ? L : ((v >= na) ? live_index(A.lv_vnode, nl, v - na) : -1);
-        }
+    const long long n = 27LL * nl;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const int L = (int)(t / 27), k = (int)(t - 27LL * L);
+        const int v = A.neigh[(size_t)k * A.cstride + A.live[lb + L]];
+        lv_nb[(size_t)k * dstride + L] = (k == 13) ? L : ((v >= na) ? live_index(A.lv_vnode, nl, v - na) : -1);
     }
 }
 
@@ -1551,19 +1649,22 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
     cudaError_t e;
     SubArrays A{ws.c_vnode, ws.c_key, ws.c_group, ws.c_parent, ws.c_jump, ws.c_depth, ws.c_cx, ws.c_cy, ws.c_cz,
                 ws.c_neigh, (size_t)ws.cap.sub_nodes, ws.c_live, ws.lv_vnode, ws.cap.sub_nodes, ws.cap.sub_dnodes};
-    k_sub_setup<<<1, 32, 0, s>>>(c, D, ws.sub_root_depth, ws.cap.sub_nodes);
+    k_sub_setup<<<1, 32, 0, s>>>(c, D, ws.sub_root_depth, ws.cap.sub_nodes);   // kMaxDepth + 2 <= 32 lanes
+    k_root_poly<<<grid_for(ws, ws.cap_poly), kBlock, 0, s>>>(c, D, ws.sub_root, ws.ndepth, ws.ctr_x, ws.ctr_y,
+                                                             ws.ctr_z, ws.neigh, stride, ws.parent, ws.enc, ws.xsol,
+                                                             ws.root_poly, ws.cap_poly);
     // depth after depth: candidates (children of the live nodes above, then the roots of this
     // depth), their neighbours and sign tests; the live ones are compacted in order
     for (int d = 1; d <= D; ++d) {
         e = launch_scan<1>(SubLevelLoad{c, d, D, na, mb.groups, ws.sub_root, ws.root_group, ws.root_self, ws.key,
                                         ws.neigh, stride, ws.first_child, ws.parent, mb.ov_group, mb.ov_sub, ws.enc,
-                                        ws.xsol, A},
+                                        ws.xsol, ws.root_poly, ws.cap_poly, A},
                            SubLevelStore{c, d, D, A, err}, &c->sub_cand[d], 0, ws.scan, total, err, s, ScanCount{},
                            1);
         if (e != cudaSuccess) return e;
     }
     // the live depth-D cells carry every record from here on, indexed by their live index
-    k_sub_live_neigh<<<gl, kBlock, 0, s>>>(c, D, A, ws.lv_nb, dstride, na);
+    k_sub_live_neigh<<<grid_for(ws, 27LL * ws.cap.sub_dnodes), kBlock, 0, s>>>(c, D, A, ws.lv_nb, dstride, na);
     // s_vtx / s_edge need no clearing: every slot of a live cell is written by the owner of
     // that vertex / edge
     k_sub_vertex_owner<<<gl, kBlock, 0, s>>>(c, D, A, ws.lv_nb, dstride, ws.s_vmask);

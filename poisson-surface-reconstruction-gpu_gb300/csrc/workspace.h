@@ -120,6 +120,8 @@ struct Workspace {
     int* sub_root_depth;
     int* root_group;        // per subdivision root: its group
     int* root_self;         // per root: the octree node it stands for
+    float* root_poly;       // [28][cap_poly]: per root, Bernstein coefficients of the levels up to it
+    int cap_poly;
     // subdivision candidates in compact slots (SoA, capacity cap.sub_nodes)
     int *c_vnode, *c_key, *c_group, *c_parent, *c_jump, *c_depth;
     float *c_cx, *c_cy, *c_cz;
