@@ -880,8 +880,8 @@ __device__ __forceinline__ void add_subdivided(const float* P, size_t pstride, u
 __device__ __forceinline__ int sub_cell_sign(float qx, float qy, float qz, int d, int rd, int r, unsigned rel,
                                              int sn, const int* G, int depth, const int* neigh, size_t stride,
                                              const int* parent, const int* enc, const float* x,
-                                             const int* root_self, const float* root_poly, int cap_poly,
-                                             float iso, const SubArrays& A, int na) {
+                                             const int* root_self, const float* root_poly, int cap_poly, float iso,
+                                             const SubArrays& A, int na) {
     float C[27];
 #pragma unroll
     for (int k = 0; k < 27; ++k) C[k] = 0.0f;
@@ -1025,59 +1025,84 @@ struct SubLevelLoad {
             ok[a][1] = true;
             ok[a][2] = cm != M;
         }
+        const int r = G[1] + (int)((unsigned)local >> (3 * (d - G[0])));
+        // An interior node (below its root, all 27 neighbours inside the root's cell) has only
+        // zero-valued sub nodes around it and nothing deeper: it is tested before anything is
+        // built.  Other nodes are built first (the test may read their own level).  Only live
+        // nodes are referred to later (children, value chains), so a node dropped here needs
+        // nothing else.
+        const bool interior = ok[0][0] && ok[0][2] && ok[1][0] && ok[1][2] && ok[2][0] && ok[2][2];
+        if (!interior) {
 #pragma unroll
-        for (int kk = 0; kk < 27; ++kk) {
-            const int ix = kk / 9, iy = (kk / 3) % 3, iz = kk % 3;
-            int v;
-            if (ok[0][ix] && ok[1][iy] && ok[2][iz]) {
-                const unsigned relk = cmp[0][ix] | cmp[1][iy] | cmp[2][iz];
-                v = na + vnode + (int)relk - (int)rel;
-                if (at_root_depth) contrib = 1;   // the node itself, a root
-            } else {
-                int lp, lc;
-                nb_lut(son, kk, lp, lc);
-                const int np = (pslot < 0) ? ((pa >= 0) ? neigh[(size_t)lp * stride + pa] : -1)
-                                           : A.neigh[(size_t)lp * A.cstride + pslot];
-                v = -1;
-                if (np != -1) {
-                    if (np < na) {
-                        if (ov_group[(size_t)lc * stride + np] == g) {
-                            // redirected child pointer of this group's root
-                            v = na + G[3] + ov_sub[(size_t)lc * stride + np];
+            for (int kk = 0; kk < 27; ++kk) {
+                const int ix = kk / 9, iy = (kk / 3) % 3, iz = kk % 3;
+                int v;
+                if (ok[0][ix] && ok[1][iy] && ok[2][iz]) {
+                    const unsigned relk = cmp[0][ix] | cmp[1][iy] | cmp[2][iz];
+                    v = na + vnode + (int)relk - (int)rel;
+                    if (at_root_depth) contrib = 1;   // the node itself, a root
+                } else {
+                    int lp, lc;
+                    nb_lut(son, kk, lp, lc);
+                    const int np = (pslot < 0) ? ((pa >= 0) ? neigh[(size_t)lp * stride + pa] : -1)
+                                               : A.neigh[(size_t)lp * A.cstride + pslot];
+                    v = -1;
+                    if (np != -1) {
+                        if (np < na) {
+                            if (ov_group[(size_t)lc * stride + np] == g) {
+                                // redirected child pointer of this group's root
+                                v = na + G[3] + ov_sub[(size_t)lc * stride + np];
+                            } else {
+                                const int fc = first_child[np];
+                                v = (fc == -1) ? -1 : fc + lc;
+                                if (v >= 0 && d < depth && first_child[v] != -1) deeper = true;
+                            }
                         } else {
-                            const int fc = first_child[np];
-                            v = (fc == -1) ? -1 : fc + lc;
-                            if (v >= 0 && d < depth && first_child[v] != -1) deeper = true;
+                            // a sub node of depth d - 1 in this group: its children are at 8 x
+                            // its index in level d
+                            v = na + G[3] + off_cur + 8 * (np - na - G[3] - off_prev) + lc;
                         }
-                    } else {
-                        // a sub node of depth d - 1 in this group: its children are at 8 x its
-                        // index in level d
-                        v = na + G[3] + off_cur + 8 * (np - na - G[3] - off_prev) + lc;
                     }
+                    // a contributing neighbour is an octree node or a root; the subdivision nodes
+                    // at a group's root depth are exactly its roots, and deeper ones are never roots
+                    if (v >= 0 && (v < na || at_root_depth)) contrib = 1;
                 }
-                // a contributing neighbour is an octree node or a root; the subdivision nodes at
-                // a group's root depth are exactly its roots, and deeper ones are never roots
-                if (v >= 0 && (v < na || at_root_depth)) contrib = 1;
+                A.neigh[(size_t)kk * A.cstride + slot] = v;
             }
-            A.neigh[(size_t)kk * A.cstride + slot] = v;
+        }
+        const int prec = (pslot >= 0) ? pslot : -2 - pa;
+        if (!interior) {   // what the test reads of the node's own level
+            A.depth[slot] = d;
+            A.cx[slot] = cc[0];
+            A.cy[slot] = cc[1];
+            A.cz[slot] = cc[2];
+            A.parent[slot] = prec;
         }
         // nearest contributing node on the path to the root (itself when it contributes;
         // roots always do): lets the value chains skip non-contributing levels in one hop
         const int jump = contrib ? slot : ((pslot >= 0) ? A.jump[pslot] : slot);
+        if (!at_root_depth && !deeper &&
+            sub_cell_sign(cc[0], cc[1], cc[2], d, G[0], r, rel, jump, G, depth, neigh, stride, parent, enc, x,
+                          root_self, root_poly, cap_poly, c->iso, A, na) != 0)
+            return 0u;
+        if (interior) {
+#pragma unroll
+            for (int kk = 0; kk < 27; ++kk) {
+                const int ix = kk / 9, iy = (kk / 3) % 3, iz = kk % 3;
+                const unsigned relk = cmp[0][ix] | cmp[1][iy] | cmp[2][iz];
+                A.neigh[(size_t)kk * A.cstride + slot] = na + vnode + (int)relk - (int)rel;
+            }
+            A.depth[slot] = d;
+            A.cx[slot] = cc[0];
+            A.cy[slot] = cc[1];
+            A.cz[slot] = cc[2];
+            A.parent[slot] = prec;
+        }
+        A.jump[slot] = jump;
         A.vnode[slot] = vnode;
         A.key[slot] = k;
         A.group[slot] = g;
-        A.parent[slot] = (pslot >= 0) ? pslot : -2 - pa;
-        A.jump[slot] = jump;
-        A.depth[slot] = d;
-        A.cx[slot] = cc[0];
-        A.cy[slot] = cc[1];
-        A.cz[slot] = cc[2];
-        if (at_root_depth || deeper) return 1u;
-        const int r = G[1] + (int)((unsigned)local >> (3 * (d - G[0])));
-        const int sg = sub_cell_sign(cc[0], cc[1], cc[2], d, G[0], r, rel, jump, G, depth, neigh, stride, parent,
-                                     enc, x, root_self, root_poly, cap_poly, c->iso, A, na);
-        return (sg == 0) ? 1u : 0u;
+        return 1u;
     }
 };
 struct SubLevelStore {
