@@ -361,7 +361,10 @@ def main():
             "stage_ms": [round(x, 4) for x in st.stage_ms], "served_stage_ms": s_stages,
             "cg_depth_ms": [round(x, 4) for x in st.cg_depth_ms[:depth + 1]], "nodes": M, "cg_iterations": list(st.cg_iterations[:depth + 1]),
             "mesh": {"vertices": m_host.vertex_count, "triangles": m_host.triangle_count},
-            "gpu_launches": (int(st_launches(r)) + 1) * K,   # graph kernels + the output copy kernel
+            # kernels launched in the timed served leg: per reconstruction the graph's kernel
+            # nodes + the output copy kernel, K reconstructions per step
+            "gpu_launches": (int(st_launches(server.slots[0].recon)) + 1) * K * args.steps,
+            "gpu_launches_per_recon": int(st_launches(server.slots[0].recon)) + 1,
             "roofline": roofline, "clocks": clocks}
     if not args.no_cpu_baseline:
         try:

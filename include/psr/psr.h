@@ -41,7 +41,8 @@ typedef struct psr_config {
     int max_triangles;         /* MAX_MESH_TRIANGLE_COUNT (:8) */
     int max_mesh_vertices;     /* MeshTriangleVertex capacity (mesh/ComputeTriangleIndices.cpp:32) */
     int max_nodes;             /* 0: 10 x max_points (TOTAL_NODEARRAY_MAX_COUNT, :42) */
-    int max_subdivision_nodes; /* 0: 16 x max_points */
+    int max_subdivision_nodes; /* subdivision nodes built (0: 8 x max_points); a quarter of
+                                  it bounds the nodes kept live */
     float bbox_scale;          /* 1.25 (mesh/BuildOctree.cpp:91) */
     int cg_max_iterations;     /* 10000 (mesh/solver/CGAlgorithm.cu:15) */
     float cg_tolerance;        /* 1e-5, absolute on ||r|| (mesh/solver/CGAlgorithm.cu:298) */

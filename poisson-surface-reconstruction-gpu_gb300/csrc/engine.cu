@@ -153,8 +153,10 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     const long long N = cfg.max_points;
     const long long nodes = cfg.max_nodes > 0 ? cfg.max_nodes : 10 * N;
     const long long dnodes = std::min(nodes, 8 * N);
-    const long long subn = cfg.max_subdivision_nodes > 0 ? cfg.max_subdivision_nodes : 16 * N;
-    const long long subd = subn;   // D-level subdivision nodes are a subset
+    const long long subn = cfg.max_subdivision_nodes > 0 ? cfg.max_subdivision_nodes : 8 * N;
+    // live subdivision nodes (all depths) and live depth-D cells: the nodes whose sign is
+    // not certain, a small part of the subdivision nodes built
+    const long long subd = std::max(65536LL, subn / 4);
     Caps& cap = ws.cap;
     cap.points = (int)N;
     cap.nodes = (int)nodes;
@@ -164,6 +166,7 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     cap.faces = (int)std::min(4 * nodes, (long long)1 << 30);
     cap.sub_nodes = (int)subn;
     cap.sub_dnodes = (int)subd;
+    cap.sub_live = (int)subd;
     cap.mesh_vertices = cfg.max_mesh_vertices;
     cap.mesh_tris = cfg.max_triangles;
     ws.part_cap_v = 2 * cfg.max_mesh_vertices + 4096;
@@ -243,7 +246,8 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     A.add(ws.c_parent, (size_t)subn); A.add(ws.c_jump, (size_t)subn); A.add(ws.c_depth, (size_t)subn);
     A.add(ws.c_cx, (size_t)subn); A.add(ws.c_cy, (size_t)subn); A.add(ws.c_cz, (size_t)subn);
     A.add(ws.c_neigh, 27 * (size_t)subn);
-    A.add(ws.c_live, (size_t)subn);
+    A.add(ws.c_live, (size_t)subd);
+    A.add(ws.c_poly, 28 * (size_t)subd);
     A.add(ws.lv_vnode, (size_t)subd);
     A.add(ws.lv_nb, 27 * (size_t)subd);
     A.add(ws.s_vtx, 8 * (size_t)subd); A.add(ws.s_edge, 12 * (size_t)subd);

@@ -693,8 +693,9 @@ struct SubArrays {
     int* neigh;   // [27][cap]
     size_t cstride;
     int* live;    // live slots, depth after depth
+    float* poly;  // [28][cap_live]: per live entry, Bernstein coefficients of its levels, sum |y|
     int* lv_vnode;   // virtual index of each live depth-D cell
-    int cap_nodes, cap_live_d;
+    int cap_nodes, cap_live, cap_live_d;
 };
 
 // ---- certain-sign cells -------------------------------------------------------------
@@ -874,67 +875,42 @@ __device__ __forceinline__ void add_subdivided(const float* P, size_t pstride, u
             C[ab3 * 3 + gg] += fmaf(Mz[gg][0], T2[ab3 * 3], fmaf(Mz[gg][1], T2[ab3 * 3 + 1], Mz[gg][2] * T2[ab3 * 3 + 2]));
 }
 
-// sign of F - iso on the closed cell (centre q) of a node at depth d below its root (rd < d;
-// root index r, Morton code rel below it); sn = the slot of the nearest node at or above it
-// with a contributing neighbour
-__device__ __forceinline__ int sub_cell_sign(float qx, float qy, float qz, int d, int rd, int r, unsigned rel,
-                                             int sn, const int* G, int depth, const int* neigh, size_t stride,
-                                             const int* parent, const int* enc, const float* x,
-                                             const int* root_self, const float* root_poly, int cap_poly, float iso,
-                                             const SubArrays& A, int na) {
-    float C[27];
+// Coefficients of a live node are kept (per live entry): a child's levels above its own are
+// its parent's polynomial restricted to the child's octant (Bernstein subdivision, convex
+// weights: the float error grows by a few ulp of the coefficients per level, inside the
+// margin), so a candidate adds at most its own level.  A root starts from root_poly, or,
+// beyond its capacity, from the walk over its octree chain.
+__device__ __forceinline__ void root_coefficients(int r, int root_node, int rd, float qx, float qy, float qz,
+                                                  int depth, const int* neigh, size_t stride, const int* parent,
+                                                  const int* enc, const float* x, const float* root_poly,
+                                                  int cap_poly, float (&C)[27], float& mag) {
+    if (r < cap_poly) {
+#pragma unroll
+        for (int k = 0; k < 27; ++k) C[k] = root_poly[(size_t)k * cap_poly + r];
+        mag = root_poly[(size_t)27 * cap_poly + r];
+        return;
+    }
 #pragma unroll
     for (int k = 0; k < 27; ++k) C[k] = 0.0f;
-    float mag = 0.0f;
+    mag = 0.0f;
     float y[27];
-    const bool poly = r < cap_poly;
-    int now = -1;
-    // subdivision levels that carry a value (jump hops over the others); with the root's
-    // polynomial at hand, the root's own level is in it
-    while (true) {
-        const int l = A.depth[sn];
-        if (poly && l == rd) break;
-        const float sc = (float)(1 << l);
-        const int base = (1 << l) - 1;
-        const int ox = base + (int)__fmul_rn(A.cx[sn], sc);
-        const int oy = base + (int)__fmul_rn(A.cy[sn], sc);
-        const int oz = base + (int)__fmul_rn(A.cz[sn], sc);
+    for (int now = root_node; now >= 0; now = parent[now]) {
+        int ox, oy, oz;
+        decode_fn_index(enc[now], depth, ox, oy, oz);
+        const int l = ilog2_dev(ox + 1);
 #pragma unroll
         for (int k = 0; k < 27; ++k) {
-            int v = A.neigh[(size_t)k * A.cstride + sn];
-            if (v >= na) v = sub_value_node(v, na, G, root_self);
+            const int v = neigh[(size_t)k * stride + now];
             y[k] = (v >= 0) ? x[v] : 0.0f;
         }
-        sign_level(y, ox, oy, oz, qx, qy, qz, __int_as_float((126 + l - d) << 23), C, mag);
-        const int p = A.parent[sn];
-        if (p < 0) { now = -2 - p; break; }
-        sn = A.jump[p];
+        sign_level(y, ox, oy, oz, qx, qy, qz, __int_as_float((126 + l - rd) << 23), C, mag);
     }
-    if (poly) {
-        add_subdivided(root_poly + r, (size_t)cap_poly, rel, d - rd, C);
-        mag += root_poly[(size_t)27 * cap_poly + r];
-    } else {
-        // octree levels above the root
-        while (now >= 0) {
-            int ox, oy, oz;
-            decode_fn_index(enc[now], depth, ox, oy, oz);
-            const int l = ilog2_dev(ox + 1);
-#pragma unroll
-            for (int k = 0; k < 27; ++k) {
-                const int v = neigh[(size_t)k * stride + now];
-                y[k] = (v >= 0) ? x[v] : 0.0f;
-            }
-            sign_level(y, ox, oy, oz, qx, qy, qz, __int_as_float((126 + l - d) << 23), C, mag);
-            now = parent[now];
-        }
-    }
-    float lo = C[0], hi = C[0];
-#pragma unroll
-    for (int k = 1; k < 27; ++k) { lo = fminf(lo, C[k]); hi = fmaxf(hi, C[k]); }
-    const float margin = 1e-4f * (mag + fabsf(iso));
-    if (lo - iso > margin) return 1;
-    if (hi - iso < -margin) return -1;
-    return 0;
+}
+
+// per-thread hand-over of a candidate's coefficients from the scan's load to its store
+__device__ __forceinline__ float* sub_poly_stash() {
+    __shared__ float s_stash[28 * kBlock];
+    return s_stash;
 }
 
 // One candidate of depth d (computeRebuildNeighbor :669-696 for its neighbours): its record,
@@ -1071,20 +1047,46 @@ struct SubLevelLoad {
             }
         }
         const int prec = (pslot >= 0) ? pslot : -2 - pa;
-        if (!interior) {   // what the test reads of the node's own level
-            A.depth[slot] = d;
-            A.cx[slot] = cc[0];
-            A.cy[slot] = cc[1];
-            A.cz[slot] = cc[2];
-            A.parent[slot] = prec;
-        }
         // nearest contributing node on the path to the root (itself when it contributes;
         // roots always do): lets the value chains skip non-contributing levels in one hop
         const int jump = contrib ? slot : ((pslot >= 0) ? A.jump[pslot] : slot);
-        if (!at_root_depth && !deeper &&
-            sub_cell_sign(cc[0], cc[1], cc[2], d, G[0], r, rel, jump, G, depth, neigh, stride, parent, enc, x,
-                          root_self, root_poly, cap_poly, c->iso, A, na) != 0)
-            return 0u;
+        // Bernstein coefficients of the levels up to d on the node's cell
+        float C[27], mag;
+        if (at_root_depth) {
+            root_coefficients(r, sub_root[r], d, cc[0], cc[1], cc[2], depth, neigh, stride, parent, enc, x,
+                              root_poly, cap_poly, C, mag);
+        } else {
+            const int pl = c->sub_lbase[d - 1] + (i >> 3);   // the parent's live entry
+#pragma unroll
+            for (int kk = 0; kk < 27; ++kk) C[kk] = 0.0f;
+            add_subdivided(A.poly + pl, (size_t)A.cap_live, (unsigned)(i & 7), 1, C);
+            mag = A.poly[(size_t)27 * A.cap_live + pl];
+            if (contrib) {   // its own level (octree neighbours; never for an interior node)
+                float y[27];
+#pragma unroll
+                for (int kk = 0; kk < 27; ++kk) {
+                    int v = A.neigh[(size_t)kk * A.cstride + slot];
+                    if (v >= na) v = sub_value_node(v, na, G, root_self);
+                    y[kk] = (v >= 0) ? x[v] : 0.0f;
+                }
+                const float sc = (float)(1 << d);
+                const int base = (1 << d) - 1;
+                sign_level(y, base + (int)__fmul_rn(cc[0], sc), base + (int)__fmul_rn(cc[1], sc),
+                           base + (int)__fmul_rn(cc[2], sc), cc[0], cc[1], cc[2], 0.5f, C, mag);
+            }
+            if (!deeper) {
+                float lo = C[0], hi = C[0];
+#pragma unroll
+                for (int kk = 1; kk < 27; ++kk) { lo = fminf(lo, C[kk]); hi = fmaxf(hi, C[kk]); }
+                const float iso = c->iso;
+                const float margin = 1e-4f * (mag + fabsf(iso));
+                if (lo - iso > margin || hi - iso < -margin) return 0u;   // certain sign
+            }
+        }
+        float* stash = sub_poly_stash();
+#pragma unroll
+        for (int kk = 0; kk < 27; ++kk) stash[kk * kBlock + threadIdx.x] = C[kk];
+        stash[27 * kBlock + threadIdx.x] = mag;
         if (interior) {
 #pragma unroll
             for (int kk = 0; kk < 27; ++kk) {
@@ -1092,12 +1094,12 @@ struct SubLevelLoad {
                 const unsigned relk = cmp[0][ix] | cmp[1][iy] | cmp[2][iz];
                 A.neigh[(size_t)kk * A.cstride + slot] = na + vnode + (int)relk - (int)rel;
             }
-            A.depth[slot] = d;
-            A.cx[slot] = cc[0];
-            A.cy[slot] = cc[1];
-            A.cz[slot] = cc[2];
-            A.parent[slot] = prec;
         }
+        A.depth[slot] = d;
+        A.cx[slot] = cc[0];
+        A.cy[slot] = cc[1];
+        A.cz[slot] = cc[2];
+        A.parent[slot] = prec;
         A.jump[slot] = jump;
         A.vnode[slot] = vnode;
         A.key[slot] = k;
@@ -1113,9 +1115,12 @@ struct SubLevelStore {
     __device__ void operator()(int i, unsigned pre, unsigned live) const {
         if (!live) return;
         const int at = c->sub_lbase[d] + (int)pre;
-        if (at >= A.cap_nodes) { atomicOr(err, kErrCapacity); return; }
+        if (at >= A.cap_live) { atomicOr(err, kErrCapacity); return; }
         const int slot = c->sub_cbase[d] + i;
         A.live[at] = slot;
+        const float* stash = sub_poly_stash();
+#pragma unroll
+        for (int k = 0; k < 28; ++k) A.poly[(size_t)k * A.cap_live + at] = stash[k * kBlock + threadIdx.x];
         if (d == depth) {
             if ((int)pre >= A.cap_live_d) { atomicOr(err, kErrCapacity); return; }
             A.lv_vnode[pre] = A.vnode[slot];
@@ -1130,7 +1135,7 @@ struct SubLevelStore {
             const long long nc = 8LL * nl + c->sub_nroots[d + 1];
             c->sub_cbase[d + 1] = cend;
             c->sub_lbase[d + 1] = c->sub_lbase[d] + nl;
-            if (cend + nc > (long long)A.cap_nodes || c->sub_lbase[d] + nl > A.cap_nodes) {
+            if (cend + nc > (long long)A.cap_nodes || c->sub_lbase[d] + nl > A.cap_live) {
                 atomicOr(err, kErrCapacity);
                 c->sub_cand[d + 1] = 0;
             } else {
@@ -1140,7 +1145,7 @@ struct SubLevelStore {
             // live cells beyond either capacity were not stored (and flagged)
             int n = nl;
             if (n > A.cap_live_d) n = A.cap_live_d;
-            if (n > A.cap_nodes - c->sub_lbase[d]) n = A.cap_nodes - c->sub_lbase[d];
+            if (n > A.cap_live - c->sub_lbase[d]) n = A.cap_live - c->sub_lbase[d];
             c->n_sub_nodes = cend;
             c->n_sub_dnodes = n;
         }
@@ -1673,7 +1678,8 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
     const int gl = grid_for(ws, ws.cap.sub_dnodes);
     cudaError_t e;
     SubArrays A{ws.c_vnode, ws.c_key, ws.c_group, ws.c_parent, ws.c_jump, ws.c_depth, ws.c_cx, ws.c_cy, ws.c_cz,
-                ws.c_neigh, (size_t)ws.cap.sub_nodes, ws.c_live, ws.lv_vnode, ws.cap.sub_nodes, ws.cap.sub_dnodes};
+                ws.c_neigh, (size_t)ws.cap.sub_nodes, ws.c_live, ws.c_poly, ws.lv_vnode, ws.cap.sub_nodes,
+                ws.cap.sub_live, ws.cap.sub_dnodes};
     k_sub_setup<<<1, 32, 0, s>>>(c, D, ws.sub_root_depth, ws.cap.sub_nodes);   // kMaxDepth + 2 <= 32 lanes
     k_root_poly<<<grid_for(ws, ws.cap_poly), kBlock, 0, s>>>(c, D, ws.sub_root, ws.ndepth, ws.ctr_x, ws.ctr_y,
                                                              ws.ctr_z, ws.neigh, stride, ws.parent, ws.enc, ws.xsol,

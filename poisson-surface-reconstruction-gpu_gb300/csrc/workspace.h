@@ -24,7 +24,8 @@ struct Caps {
     int edges;         // D-level edge records
     int faces;         // face records
     int sub_nodes;     // subdivision-space nodes (all groups of one reconstruction)
-    int sub_dnodes;    // D-level subdivision nodes
+    int sub_dnodes;    // live D-level subdivision cells
+    int sub_live;      // live subdivision nodes of all depths
     int mesh_vertices; // output vertex cap
     int mesh_tris;     // output triangle cap
     int scan_tiles;    // tiles of the largest scan
@@ -126,7 +127,8 @@ struct Workspace {
     int *c_vnode, *c_key, *c_group, *c_parent, *c_jump, *c_depth;
     float *c_cx, *c_cy, *c_cz;
     int* c_neigh;           // [27][cap.sub_nodes]
-    int* c_live;            // live slots, depth after depth
+    int* c_live;            // live slots, depth after depth (capacity cap.sub_live)
+    float* c_poly;          // [28][cap.sub_live]: per live entry, its Bernstein coefficients, sum |y|
     // live depth-D cells (capacity cap.sub_dnodes)
     int* lv_vnode;          // virtual index, ascending
     int* lv_nb;             // [27][cap.sub_dnodes]: live index of each same-depth neighbour

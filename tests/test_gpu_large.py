@@ -8,8 +8,8 @@ bit-identical), and the iso-value equal to the mean implicit value at the sample
 With the reference's Laplacian drop threshold (1e-6) the depth-9 stencil loses its edge
 and corner entries and the system is indefinite, so CG runs to its iteration cap there;
 the run below keeps every entry (laplacian_epsilon = 0), which leaves depths 0-8 unchanged.
-The cloud needs about 92M subdivision nodes (114k coarse leaves carry surface), hence the
-capacities.
+114k coarse leaves carry surface; with the cells of certain sign left out, subdivision
+builds about 4.9M nodes (the full subtrees would be 92M), hence the capacities.
 """
 import numpy as np
 import pytest
@@ -24,10 +24,12 @@ def test_superquadric_2m_depth9_properties():
     p, nr, _, D = syn.workload("superquadric2m")
     assert D == 9 and p.shape[0] == 2000000
     with psr.PoissonReconstruction(max_depth=9, max_points=2000000, max_triangles=12000000,
-                                   max_mesh_vertices=6000000, max_subdivision_nodes=100000000,
+                                   max_mesh_vertices=6000000, max_subdivision_nodes=8000000,
                                    compute_normals=True, laplacian_epsilon=0.0) as r:
         a = r.SolvePoissionReconstructionMesh(p, nr, depth=D)
         st = r.stats()
+        assert st.error_bits == 0
+        assert 0 < st.subdivision_nodes <= 8000000
         # octree: every level below the root is made of whole sibling groups
         lc = np.array(st.level_count[:D + 1])
         assert lc[0] == 1 and np.all(lc[1:] % 8 == 0)
