@@ -1691,7 +1691,7 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
                                         ws.neigh, stride, ws.first_child, ws.parent, mb.ov_group, mb.ov_sub, ws.enc,
                                         ws.xsol, ws.root_poly, ws.cap_poly, A},
                            SubLevelStore{c, d, D, A, err}, &c->sub_cand[d], 0, ws.scan, total, err, s, ScanCount{},
-                           1);
+                           2);
         if (e != cudaSuccess) return e;
     }
     // the live depth-D cells carry every record from here on, indexed by their live index
@@ -1739,7 +1739,7 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
     e = launch_scan(KeepVertexLoad{ws.part_v}, KeepVertexStore{ws.part_v, ws.mesh_v, mb.kept_prefix, ws.cap.mesh_vertices, err},
                     n_staged_v, 0, ws.scan, total, err, s, ScanCount{&c->n_mesh_vertices, ws.cap.mesh_vertices});
     if (e != cudaSuccess) return e;
-    e = launch_scan(KeepTriLoad{ws.part_t, mb.parts, n_parts},
+    e = launch_scan<1>(KeepTriLoad{ws.part_t, mb.parts, n_parts},
                     KeepTriStore{ws.part_t, mb.parts, n_parts, mb.kept_prefix, n_staged_v, &c->n_mesh_vertices,
                                  ws.mesh_t, ws.cap.mesh_tris, err},
                     n_staged_t, 0, ws.scan, total, err, s, ScanCount{&c->n_mesh_triangles, ws.cap.mesh_tris});
