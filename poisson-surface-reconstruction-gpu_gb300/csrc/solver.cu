@@ -87,7 +87,6 @@ struct CgcArgs {
 };
 
 struct CgcShared {
-    float2 zero2;   // (r, p) of a missing neighbour
     FF warp[kCgWarps];
     FF slot[2];
     FF sum;
@@ -153,6 +152,18 @@ struct CgUnit {
     int d, row0, row1;
 };
 
+// (r, p) pair at byte offset `off` of the `cur` buffer of cluster CTA `rank`: the shared
+// address of this CTA's buffer mapped into that CTA's window (mapa), then one
+// distributed-shared-memory load
+__device__ __forceinline__ float2 cg_ld_pair(unsigned cur_sa, unsigned desc) {
+    unsigned ra;
+    float2 v;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(cur_sa + (desc & 0xffffffu)), "r"(desc >> 24));
+    asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(ra));
+    return v;
+}
+constexpr int kCgZeroRow = kCgSmemRows - 1;   // kept (0, 0) in both buffers: absent neighbours
+
 // Resident path.  CTA k of the cluster owns rows [row0 + k*chunk, row0 + (k+1)*chunk).
 __device__ __forceinline__ void cgc_resident(cg::cluster_group& cl, CgcShared& sh, const CgcArgs& a,
                                              const CgUnit& u, int chunk, float2* rp0, float2* rp1, float* sap,
@@ -170,6 +181,29 @@ __device__ __forceinline__ void cgc_resident(cg::cluster_group& cl, CgcShared& s
     // g / chunk = umulhi(g, ceil(2^32 / chunk)): exact while g * (magic * chunk - 2^32) < 2^32,
     // true here (g < 2^17 rows, chunk <= kCgSmemRows)
     const unsigned chunk_magic = chunk > 0 ? (unsigned)((0x100000000ull + (unsigned)chunk - 1) / (unsigned)chunk) : 0u;
+    // The block table of this CTA's groups becomes descriptors, once: (CTA rank << 24) |
+    // byte offset of the row inside that CTA's buffer (the zero row for an absent cell), so
+    // an iteration reads a neighbour with one mapped load instead of locating its owner.
+    // Only this CTA reads these groups' entries; the barrier below publishes them.
+    int* blkw = const_cast<int*>(a.blk);
+    for (int t = threadIdx.x; t < nloc * 8; t += kCgcBlock) {
+        const size_t at = (size_t)gbase * 64 + t;
+        const int nb = blkw[at];
+        const int gl = nb - mlo;
+        const int g = nb - u.row0;
+        unsigned desc = (me << 24) | (unsigned)(kCgZeroRow * 8);
+        if ((unsigned)gl < (unsigned)nloc) {
+            desc = (me << 24) | (unsigned)(gl * 8);
+        } else if (nb >= 0 && (unsigned)g < (unsigned)m) {
+            const int owner = (int)__umulhi((unsigned)g, chunk_magic);   // g / chunk
+            desc = ((unsigned)owner << 24) | (unsigned)((g - owner * chunk) * 8);
+        }
+        blkw[at] = (int)desc;
+    }
+    if (threadIdx.x == 0) {
+        rp0[kCgZeroRow] = make_float2(0.0f, 0.0f);
+        rp1[kCgZeroRow] = make_float2(0.0f, 0.0f);
+    }
     // r0 = b, p_{-1} = 0, x0 = 0
     FF acc = ff_zero();
     for (int l = threadIdx.x; l < nloc; l += kCgcBlock) {
@@ -194,9 +228,10 @@ __device__ __forceinline__ void cgc_resident(cg::cluster_group& cl, CgcShared& s
         int4 q0 = make_int4(-1, -1, -1, -1), q1 = q0;
         if (warp < nslot && warp * 32 + lane < nloc) {
             const int4* bp = reinterpret_cast<const int4*>(a.blk + (size_t)(gbase + ((warp * 32 + lane) >> 3)) * 64 + sib * 8);
-            q0 = __ldg(bp);
-            q1 = __ldg(bp + 1);
+            q0 = bp[0];
+            q1 = bp[1];
         }
+        const unsigned cur_sa = (unsigned)__cvta_generic_to_shared(cur);
         for (int sl = warp; sl < nslot; sl += kCgWarps) {
             const int l = sl * 32 + lane;
             const bool mine = l < nloc;   // whole groups: a group is all in or all out
@@ -204,30 +239,14 @@ __device__ __forceinline__ void cgc_resident(cg::cluster_group& cl, CgcShared& s
             const int ln = l + kCgWarps * 32;
             if (ln < nloc) {
                 const int4* bp = reinterpret_cast<const int4*>(a.blk + (size_t)(gbase + (ln >> 3)) * 64 + sib * 8);
-                q0 = __ldg(bp);
-                q1 = __ldg(bp + 1);
+                q0 = bp[0];
+                q1 = bp[1];
             }
             if (mine) {
-                // one generic address per entry (own shared memory, a peer's through the
-                // cluster window, or a zero pair for a missing cell), then 8 independent loads
-                const float2* src[8];
-#pragma unroll
-                for (int e = 0; e < 8; ++e) {
-                    const int nb = ids[e];
-                    const int gl = nb - mlo;
-                    const int g = nb - u.row0;
-                    if ((unsigned)gl < (unsigned)nloc) {
-                        src[e] = cur + gl;
-                    } else if (nb >= 0 && (unsigned)g < (unsigned)m) {
-                        const int owner = (int)__umulhi((unsigned)g, chunk_magic);   // g / chunk
-                        src[e] = cl.map_shared_rank(cur + (g - owner * chunk), (unsigned)owner);
-                    } else {
-                        src[e] = &sh.zero2;
-                    }
-                }
+                // 8 independent mapped loads (own buffer, a peer's, or the zero row)
                 float2 vals[8];
 #pragma unroll
-                for (int e = 0; e < 8; ++e) vals[e] = *src[e];
+                for (int e = 0; e < 8; ++e) vals[e] = cg_ld_pair(cur_sa, (unsigned)ids[e]);
 #pragma unroll
                 for (int e = 0; e < 8; ++e) myblk[e * 8 + sib] = fmaf(beta, vals[e].y, vals[e].x);
             }
@@ -345,12 +364,11 @@ __device__ __forceinline__ void cg_unit_body(const CgcArgs& a, int unit) {
     u.row0 = a.c->level_base[u.d];
     u.row1 = (u.d < a.depth) ? a.c->level_base[u.d + 1] : a.c->n_nodes;
     if (threadIdx.x < 27) sh.st[threadIdx.x] = a.stencil[u.d * 27 + threadIdx.x];
-    if (threadIdx.x == 0) sh.zero2 = make_float2(0.0f, 0.0f);
     __syncthreads();
     const int nblk = (int)cl.num_blocks();
     const int m = u.row1 - u.row0;
     const int chunk = ((m + nblk - 1) / nblk + 7) & ~7;   // sibling-group aligned
-    if (u.d >= 1 && chunk <= kCgSmemRows) {   // uniform over the cluster
+    if (u.d >= 1 && chunk < kCgSmemRows) {   // uniform over the cluster; the last row is the zero row
         float2* rp0 = reinterpret_cast<float2*>(cg_dyn);
         float2* rp1 = rp0 + kCgSmemRows;
         float* sap = reinterpret_cast<float*>(rp1 + kCgSmemRows);
