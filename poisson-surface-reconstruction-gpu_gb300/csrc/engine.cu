@@ -315,6 +315,7 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
         std::vector<float> dff32(dff.begin(), dff.end());   // the kernels use float entries
         e = cudaMemcpy(ws.dff, dff32.data(), dff32.size() * sizeof(float), cudaMemcpyHostToDevice);
         if (e == cudaSuccess) e = cudaMemcpy(ws.stencil, st.data(), st.size() * sizeof(float), cudaMemcpyHostToDevice);
+        std::copy(st.begin(), st.end(), ws.stencil_host);   // the CG launch passes some as parameters
     }
     if (e == cudaSuccess) {
         prepare_launch_configs(ws);

@@ -84,6 +84,7 @@ struct CgcArgs {
     float* ap;
     float tol2;
     int max_iter;
+    float stp[3][27];   // stencils of units 0..2 of k_cg_cluster (depth first - u)
 };
 
 struct CgcShared {
@@ -165,6 +166,9 @@ __device__ __forceinline__ float2 cg_ld_pair(unsigned cur_sa, unsigned desc) {
 constexpr int kCgZeroRow = kCgSmemRows - 1;   // kept (0, 0) in both buffers: absent neighbours
 
 // Resident path.  CTA k of the cluster owns rows [row0 + k*chunk, row0 + (k+1)*chunk).
+// U >= 0: the cluster unit whose stencil is a launch parameter (a.stp[U]), read as a
+// constant operand of the FMAs; U < 0: the stencil staged in shared memory.
+template <int U>
 __device__ __forceinline__ void cgc_resident(cg::cluster_group& cl, CgcShared& sh, const CgcArgs& a,
                                              const CgUnit& u, int chunk, float2* rp0, float2* rp1, float* sap,
                                              float* sx, float* sblk) {
@@ -254,7 +258,7 @@ __device__ __forceinline__ void cgc_resident(cg::cluster_group& cl, CgcShared& s
             if (mine) {
                 float y = 0.0f;
 #pragma unroll
-                for (int k = 0; k < 27; ++k) y = fmaf(sh.st[k], myblk[spos + cg_kpos(k)], y);
+                for (int k = 0; k < 27; ++k) y = fmaf(U >= 0 ? a.stp[U < 0 ? 0 : U][k] : sh.st[k], myblk[spos + cg_kpos(k)], y);
                 const float2 own = cur[l];
                 const float pi = fmaf(beta, own.y, own.x);
                 nxt[l].y = pi;
@@ -353,7 +357,9 @@ __device__ __forceinline__ void cgc_global(cg::cluster_group& cl, CgcShared& sh,
     if (ran && cl.block_rank() == 0 && threadIdx.x == 0) a.cw->cg_rr[u.d] = (double)rr.hi + (double)rr.lo;
 }
 
-// one depth per cluster (a CTA when the launch has no cluster dimension)
+// one depth per cluster (a CTA when the launch has no cluster dimension); kClusterUnits:
+// the unit's stencil is a launch parameter
+template <bool kClusterUnits>
 __device__ __forceinline__ void cg_unit_body(const CgcArgs& a, int unit) {
     cg::cluster_group cl = cg::this_cluster();
     __shared__ CgcShared sh;
@@ -374,7 +380,10 @@ __device__ __forceinline__ void cg_unit_body(const CgcArgs& a, int unit) {
         float* sap = reinterpret_cast<float*>(rp1 + kCgSmemRows);
         float* sx = sap + kCgSmemRows;
         float* sblk = sx + kCgSmemRows;
-        cgc_resident(cl, sh, a, u, chunk, rp0, rp1, sap, sx, sblk);
+        if (kClusterUnits && unit == 0) cgc_resident<0>(cl, sh, a, u, chunk, rp0, rp1, sap, sx, sblk);
+        else if (kClusterUnits && unit == 1) cgc_resident<1>(cl, sh, a, u, chunk, rp0, rp1, sap, sx, sblk);
+        else if (kClusterUnits && unit == 2) cgc_resident<2>(cl, sh, a, u, chunk, rp0, rp1, sap, sx, sblk);
+        else cgc_resident<-1>(cl, sh, a, u, chunk, rp0, rp1, sap, sx, sblk);
     } else {
         cgc_global(cl, sh, a, u);
     }
@@ -384,10 +393,10 @@ __device__ __forceinline__ void cg_unit_body(const CgcArgs& a, int unit) {
 
 __global__ void __launch_bounds__(kCgcBlock) k_cg_cluster(CgcArgs a) {
     cg::cluster_group cl = cg::this_cluster();
-    cg_unit_body(a, (int)(blockIdx.x / cl.num_blocks()));
+    cg_unit_body<true>(a, (int)(blockIdx.x / cl.num_blocks()));
 }
 
-__global__ void __launch_bounds__(kCgcBlock) k_cg_cta(CgcArgs a) { cg_unit_body(a, (int)blockIdx.x); }
+__global__ void __launch_bounds__(kCgcBlock) k_cg_cta(CgcArgs a) { cg_unit_body<false>(a, (int)blockIdx.x); }
 
 // ---- implicit function at the sample points and the iso-value ----------------------
 __device__ __forceinline__ void decode3s(int e, int depth, int& ix, int& iy, int& iz) {
@@ -539,6 +548,8 @@ cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, 
     if (e != cudaSuccess) return e;
     if (ncl > 0) {
         a.first = D;
+        for (int u = 0; u < 3; ++u)
+            for (int k = 0; k < 27; ++k) a.stp[u][k] = (D - u >= 0) ? ws.stencil_host[(D - u) * 27 + k] : 0.0f;
         e = launch_cg(k_cg_cluster, a, ncl * g_cg_cluster, g_cg_cluster, s);
         if (e != cudaSuccess) return e;
     }

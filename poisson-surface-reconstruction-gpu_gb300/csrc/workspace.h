@@ -91,6 +91,7 @@ struct Workspace {
     int res;
     float* dff;             // d/dx F_i . F_j rounded to float (index i + res * j)
     float* stencil;         // [D+1][27] Laplacian coefficients (0 where dropped)
+    float stencil_host[(kMaxDepth + 1) * 27];   // the same on the host
 
     // field / solve
     float* vfield;          // 3 x dnodes (SoA: x block, y block, z block)
