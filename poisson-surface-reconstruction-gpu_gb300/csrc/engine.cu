@@ -300,6 +300,8 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ws.aux2, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ws.ev_fork2, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ws.ev_join2, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ws.aux3, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ws.ev_join3, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->done, cudaEventDisableTiming);
     // tables
     if (e == cudaSuccess) e = upload_tables_octree();
@@ -344,6 +346,8 @@ psr_status psr_destroy(psr_handle* h) {
     if (h->ws.ev_join) cudaEventDestroy(h->ws.ev_join);
     if (h->ws.ev_fork2) cudaEventDestroy(h->ws.ev_fork2);
     if (h->ws.ev_join2) cudaEventDestroy(h->ws.ev_join2);
+    if (h->ws.ev_join3) cudaEventDestroy(h->ws.ev_join3);
+    if (h->ws.aux3) cudaStreamDestroy(h->ws.aux3);
     if (h->ws.aux2) cudaStreamDestroy(h->ws.aux2);
     if (h->ws.aux) cudaStreamDestroy(h->ws.aux);
     if (h->done) cudaEventDestroy(h->done);

@@ -533,12 +533,15 @@ cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, 
     k_cg_blocks<<<grid_for(ws, 1 << 20), kBlock, 0, s>>>(ws.cnt, ws.neigh, (size_t)ws.cap.nodes, ws.cg_blk);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    // the finest depths (D, D-1, and D-2 from depth 5 on; never the root) on clusters, the
-    // rest one CTA each, concurrently on the second stream
+    // The finest depths (D, D-1, and D-2 from depth 5 on; never the root) on clusters: depth
+    // D on the widest cluster, D-1 and D-2 (fewer rows, done well before depth D) on clusters
+    // of at most 8 CTAs, on a third stream, so that they hold fewer SMs; the rest one CTA
+    // each, on the second stream.  All three run concurrently.
     const int ncl = D < 2 ? D : (D >= 5 ? 3 : 2);
     const int ncta = D - ncl + 1;
     e = cudaEventRecord(ws.ev_fork, s);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(ws.aux, ws.ev_fork, 0);
+    if (e == cudaSuccess && ncl > 1) e = cudaStreamWaitEvent(ws.aux3, ws.ev_fork, 0);
     if (e == cudaSuccess && ncta > 0) {
         CgcArgs b = a;
         b.first = D - ncl;
@@ -546,11 +549,24 @@ cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, 
     }
     if (e == cudaSuccess) e = cudaEventRecord(ws.ev_join, ws.aux);
     if (e != cudaSuccess) return e;
+    auto set_stencils = [&](CgcArgs& q) {
+        for (int u = 0; u < 3; ++u)
+            for (int k = 0; k < 27; ++k)
+                q.stp[u][k] = (q.first - u >= 0) ? ws.stencil_host[(q.first - u) * 27 + k] : 0.0f;
+    };
+    if (ncl > 1) {
+        CgcArgs b = a;
+        b.first = D - 1;
+        set_stencils(b);
+        const int cl2 = g_cg_cluster < 8 ? g_cg_cluster : 8;
+        e = launch_cg(k_cg_cluster, b, (ncl - 1) * cl2, cl2, ws.aux3);
+        if (e == cudaSuccess) e = cudaEventRecord(ws.ev_join3, ws.aux3);
+        if (e != cudaSuccess) return e;
+    }
     if (ncl > 0) {
         a.first = D;
-        for (int u = 0; u < 3; ++u)
-            for (int k = 0; k < 27; ++k) a.stp[u][k] = (D - u >= 0) ? ws.stencil_host[(D - u) * 27 + k] : 0.0f;
-        e = launch_cg(k_cg_cluster, a, ncl * g_cg_cluster, g_cg_cluster, s);
+        set_stencils(a);
+        e = launch_cg(k_cg_cluster, a, g_cg_cluster, g_cg_cluster, s);
         if (e != cudaSuccess) return e;
     }
     if (ws.ev_cg) {
@@ -558,6 +574,7 @@ cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, 
         if (e != cudaSuccess) return e;
     }
     e = cudaStreamWaitEvent(s, ws.ev_join, 0);
+    if (e == cudaSuccess && ncl > 1) e = cudaStreamWaitEvent(s, ws.ev_join3, 0);
     if (e != cudaSuccess) return e;
     // iso-value
     const int nb = ws.num_sms * 4;

@@ -164,6 +164,8 @@ struct Workspace {
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaStream_t aux2 = nullptr;        // third stream: octree-only mesh records beside the solve
     cudaEvent_t ev_fork2 = nullptr, ev_join2 = nullptr;
+    cudaStream_t aux3 = nullptr;        // fourth stream: the CG of depths D-1 and D-2
+    cudaEvent_t ev_join3 = nullptr;
     int num_sms;
 };
 
