@@ -323,12 +323,14 @@ def main():
     for d in range(depth + 1):
         cg_bytes += st.level_count[d] * row_bytes * st.cg_iterations[d]
     cg_ms = float(np.mean(cg_samples)) if cg_samples else st.cg_kernel_ms
-    roofline = {"bound": "hbm", "kernel": "k_cg_cluster (per-depth CG, one thread-block cluster per depth group)",
+    roofline = {"bound": "hbm", "kernel": "CG of all depths: k_cg_cluster (depth D on 16 CTAs; D-1, D-2 on 8-CTA "
+                                          "clusters) and k_cg_cta (coarser depths), concurrent, timed together",
                 "achieved": cg_bytes / (cg_ms * 1e-3) / 1e9 if cg_ms > 0 else None, "peak": peak_hbm,
                 "unit": "GB/s", "frac": None, "traffic": None,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s",
                 "algorithmic_bytes": cg_bytes, "launch_ms": cg_ms,
-                "note": "vectors and neighbour table stay in L2 (DRAM traffic ~10 MB per launch): latency bound"}
+                "note": "vectors resident in shared memory, descriptor table in L2 (DRAM traffic ~3 MB per "
+                        "reconstruction): latency bound"}
     # DRAM traffic of one launch, from the committed ncu summary of the same kernel and workload
     try:
         for line in open(ROOT / "profiles" / "cg_cluster_torus200k_d7.md"):
