@@ -1309,61 +1309,91 @@ __global__ void __launch_bounds__(kBlock) k_sub_edge_maintain(const Counters* c,
 // implicit values of subdivision vertices (:956-1038): x = 0 inside subdivision space,
 // a root stands for the octree node it replaces (same depth and position).  Every
 // neighbour of a level is a same-depth cell, so its function index is the level node's
-// own plus the slot offset: 9 basis values per level.  A subdivision node's own index
-// comes from its centre ((off + 1/2) / 2^d exactly).
+// own plus the slot offset.  A subdivision node's own index comes from its centre
+// ((off + 1/2) / 2^d exactly).  The value is the sum, level after level from the owner's
+// nearest contributing node up to the root and then 27 neighbour terms in slot order, of
+// ((x Fx) Fy) Fz.  One warp per vertex: lane 0 finds the levels (subdivision nodes through
+// the jump links, then the octree ancestors), the lanes gather the coefficients and form
+// the terms in parallel, and lane 0 adds them in that order (absent neighbours as +0, which
+// leaves such a sum unchanged): the chain's dependent loads are paid once per level instead
+// of once per term.
+constexpr int kSvWarps = kBlock / 32;
+constexpr int kSvMaxLevels = kMaxDepth + 1;
 __global__ void __launch_bounds__(kBlock) k_sub_vertex_values(const Counters* c, int depth, const float* vx,
                                                               const float* vy, const float* vz, const int* vowner,
                                                               const int* neigh, size_t stride, const int* parent,
                                                               const int* groups, const int* root_self, SubArrays A,
                                                               const int* enc, const float* x, float* vvalue, int na) {
+    __shared__ int s_node[kSvWarps][kSvMaxLevels];   // slot (subdivision) or octree node
+    __shared__ int s_o[kSvWarps][kSvMaxLevels][3];   // function index of the level's node
+    __shared__ float s_t[kSvWarps][kSvMaxLevels * 27];
     const int V = c->n_sub_vertices;
     const float iso = c->iso;
     const int lb = c->sub_lbase[depth];
-    PSR_GRID_STRIDE(v, V) {
-        float val = 0.0f;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int v = blockIdx.x * kSvWarps + w; v < V; v += gridDim.x * kSvWarps) {
         const float qx = vx[v], qy = vy[v], qz = vz[v];
         const int own = A.live[lb + vowner[v]];
         const int* G = groups + (size_t)A.group[own] * kGroupRec;
-        // levels whose 27 neighbours are all zero-valued subdivision nodes add nothing: hop
-        // to the nearest contributing node on the way to the root
-        int sn = A.jump[own];
-        int now;
-        while (true) {
-            const int d = A.depth[sn];
-            const float sc = (float)(1 << d);
-            const int base = (1 << d) - 1;
-            const int ox = base + (int)__fmul_rn(A.cx[sn], sc);
-            const int oy = base + (int)__fmul_rn(A.cy[sn], sc);
-            const int oz = base + (int)__fmul_rn(A.cz[sn], sc);
-            float bx[3], by[3], bz[3];
-#pragma unroll
-            for (int j = 0; j < 3; ++j) {
-                bx[j] = basis32(ox - 1 + j, qx);
-                by[j] = basis32(oy - 1 + j, qy);
-                bz[j] = basis32(oz - 1 + j, qz);
+        int nsub = 0, nlev = 0;
+        if (lane == 0) {
+            // levels whose 27 neighbours are all zero-valued subdivision nodes add nothing:
+            // the jump links skip them
+            int sn = A.jump[own], now = -1;
+            while (nsub < kSvMaxLevels) {
+                s_node[w][nsub++] = sn;
+                const int p = A.parent[sn];
+                if (p < 0) { now = -2 - p; break; }
+                sn = A.jump[p];
             }
-#pragma unroll
-            for (int k = 0; k < 27; ++k) {
-                int nb = A.neigh[(size_t)k * A.cstride + sn];
-                if (nb == -1) continue;
-                if (nb >= na) {
-                    nb = sub_value_node(nb, na, G, root_self);
-                    if (nb < 0) continue;
-                }
-                float t = __fmul_rn(x[nb], bx[k / 9]);
-                t = __fmul_rn(t, by[(k / 3) % 3]);
-                t = __fmul_rn(t, bz[k % 3]);
-                val = __fadd_rn(val, t);
+            nlev = nsub;
+            for (; now != -1 && nlev < kSvMaxLevels; now = parent[now]) s_node[w][nlev++] = now;
+        }
+        nsub = __shfl_sync(0xffffffffu, nsub, 0);
+        nlev = __shfl_sync(0xffffffffu, nlev, 0);
+        __syncwarp();
+        if (lane < nlev) {
+            const int nd = s_node[w][lane];
+            int ox, oy, oz;
+            if (lane < nsub) {
+                const int d = A.depth[nd];
+                const float sc = (float)(1 << d);
+                const int base = (1 << d) - 1;
+                ox = base + (int)__fmul_rn(A.cx[nd], sc);
+                oy = base + (int)__fmul_rn(A.cy[nd], sc);
+                oz = base + (int)__fmul_rn(A.cz[nd], sc);
+            } else {
+                decode_fn_index(enc[nd], depth, ox, oy, oz);
             }
-            const int p = A.parent[sn];
-            if (p < 0) { now = -2 - p; break; }
-            sn = A.jump[p];
+            s_o[w][lane][0] = ox;
+            s_o[w][lane][1] = oy;
+            s_o[w][lane][2] = oz;
         }
-        while (now != -1) {   // octree levels
-            val = level_terms(now, val, qx, qy, qz, depth, neigh, stride, enc, x);
-            now = parent[now];
+        __syncwarp();
+        for (int t = lane; t < nlev * 27; t += 32) {
+            const int l = t / 27, k = t - 27 * l;
+            const int nd = s_node[w][l];
+            int nb = (l < nsub) ? A.neigh[(size_t)k * A.cstride + nd] : neigh[(size_t)k * stride + nd];
+            if (nb >= na) nb = sub_value_node(nb, na, G, root_self);
+            float term = 0.0f;
+            if (nb >= 0) {
+                const float bxk = basis32(s_o[w][l][0] - 1 + k / 9, qx);
+                const float byk = basis32(s_o[w][l][1] - 1 + (k / 3) % 3, qy);
+                const float bzk = basis32(s_o[w][l][2] - 1 + k % 3, qz);
+                term = __fmul_rn(__fmul_rn(__fmul_rn(x[nb], bxk), byk), bzk);
+            }
+            s_t[w][t] = term;
         }
-        vvalue[v] = __fsub_rn(val, iso);
+        __syncwarp();
+        if (lane == 0) {
+            float val = 0.0f;
+            for (int l = 0; l < nlev; ++l) {
+#pragma unroll
+                for (int k = 0; k < 27; ++k) val = __fadd_rn(val, s_t[w][l * 27 + k]);
+            }
+            vvalue[v] = __fsub_rn(val, iso);
+        }
+        __syncwarp();
     }
 }
 
@@ -1711,7 +1741,7 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
                        &c->n_sub_dnodes, 0, ws.scan, total, err, s, ScanCount{&c->n_sub_edges, 12 * ws.cap.sub_dnodes});
     if (e != cudaSuccess) return e;
     k_sub_edge_maintain<<<gl, kBlock, 0, s>>>(c, ws.lv_nb, dstride, ws.se_owner, ws.se_kind, ws.s_edge);
-    k_sub_vertex_values<<<gl, kBlock, 0, s>>>(c, D, ws.sv_x, ws.sv_y, ws.sv_z, ws.sv_owner, ws.neigh, stride,
+    k_sub_vertex_values<<<grid_for(ws, 32LL * 8 * ws.cap.sub_dnodes), kBlock, 0, s>>>(c, D, ws.sv_x, ws.sv_y, ws.sv_z, ws.sv_owner, ws.neigh, stride,
                                               ws.parent, mb.groups, ws.root_self, A, ws.enc, ws.xsol, ws.sv_value, na);
     // crossings: staged after the main part's vertices
     e = launch_scan<2>(SubCrossLoad{ws.se_owner, ws.se_kind, ws.s_vtx, dstride, ws.sv_value, err},
