@@ -65,41 +65,31 @@ __device__ __forceinline__ void knn_insert(float (&bd)[4], int (&bi)[4], float d
     } else { bd[3] = d; bi[3] = i; }
 }
 
-// the 4 smallest of two sorted 4-lists (lists hold disjoint sample sets): the pairwise
-// minima of a[k] and b[3-k] are the 4 smallest and form a bitonic sequence, which two
-// half-cleaner stages sort (Batcher's bitonic merge)
-__device__ __forceinline__ void knn_cswap(float& da, int& ia, float& db, int& ib) {
-    if (knn_less(db, ib, da, ia)) {
-        const float td = da; da = db; db = td;
-        const int ti = ia; ia = ib; ib = ti;
-    }
-}
-__device__ __forceinline__ void knn_merge(float (&ad)[4], int (&ai)[4], const float (&bd)[4], const int (&bi)[4]) {
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        if (knn_less(bd[3 - k], bi[3 - k], ad[k], ai[k])) { ad[k] = bd[3 - k]; ai[k] = bi[3 - k]; }
-    }
-    knn_cswap(ad[0], ai[0], ad[2], ai[2]);
-    knn_cswap(ad[1], ai[1], ad[3], ai[3]);
-    knn_cswap(ad[0], ai[0], ad[1], ai[1]);
-    knn_cswap(ad[2], ai[2], ad[3], ai[3]);
-}
-
-// butterfly merge of the lanes' sorted 4-lists: every lane ends with the warp's 4 nearest
+// the warp's 4 nearest from the lanes' sorted 4-lists (sample sets disjoint between lanes):
+// four rounds of a warp-wide minimum of the lanes' heads under the (d, i) order, the lane
+// holding the minimum popping its head; every lane ends with the same 4
 __device__ __forceinline__ void knn_warp_merge(const float (&bd)[4], const int (&bi)[4], float (&md)[4],
                                                int (&mi)[4]) {
+    float hd[4] = {bd[0], bd[1], bd[2], bd[3]};
+    int hi[4] = {bi[0], bi[1], bi[2], bi[3]};
 #pragma unroll
-    for (int q = 0; q < 4; ++q) { md[q] = bd[q]; mi[q] = bi[q]; }
+    for (int r = 0; r < 4; ++r) {
+        float d = hd[0];
+        int i = hi[0];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        float od[4];
-        int oi[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            od[q] = __shfl_xor_sync(0xffffffffu, md[q], o);
-            oi[q] = __shfl_xor_sync(0xffffffffu, mi[q], o);
+        for (int o = 16; o > 0; o >>= 1) {
+            const float od = __shfl_xor_sync(0xffffffffu, d, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, i, o);
+            if (knn_less(od, oi, d, i)) { d = od; i = oi; }
         }
-        knn_merge(md, mi, od, oi);
+        md[r] = d;
+        mi[r] = i;
+        if (hd[0] == d && hi[0] == i) {   // this lane's head was taken
+            hd[0] = hd[1]; hi[0] = hi[1];
+            hd[1] = hd[2]; hi[1] = hi[2];
+            hd[2] = hd[3]; hi[2] = hi[3];
+            hd[3] = 1e6f; hi[3] = 0x7fffffff;
+        }
     }
 }
 
