@@ -263,6 +263,7 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     A.add(ws.nacc, 3 * (size_t)cap.mesh_vertices);
     A.add(ws.vcount, (size_t)cap.mesh_vertices);
     A.add(ws.cell_start, ((size_t)1 << (3 * kColourGridLevel)) + 16);
+    A.add(ws.colour_far, (size_t)cap.mesh_vertices);
     A.add(ws.part_v, 3 * (size_t)ws.part_cap_v);
     A.add(ws.part_t, 3 * (size_t)ws.part_cap_t);
     ws.mb.max_groups = (int)nodes;

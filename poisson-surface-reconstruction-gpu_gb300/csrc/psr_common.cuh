@@ -36,6 +36,7 @@ struct Counters {
     int n_sub_dnodes;             // live depth-D subdivision cells
     int n_sub_vertices, n_sub_edges, n_sub_cross, n_sub_tri;
     int n_mesh_vertices, n_mesh_triangles;
+    int n_colour_far;             // mesh vertices whose 4 nearest samples need the wide search
     int scan_total;               // scratch total written by scans
     int scan_total_aux;           // the same for scans issued on the geometry stream
     unsigned error;

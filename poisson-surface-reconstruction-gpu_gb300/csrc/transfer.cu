@@ -100,13 +100,135 @@ __device__ __forceinline__ void knn_visit(float qx, float qy, float qz, const fl
     knn_insert(bd, bi, d2, i);
 }
 
+// colour of a vertex from its 4 nearest (fewer than 4 samples: the reference's unfilled
+// slots, distance 1e6 and sample 0); weights grow with the squared distance
+__device__ __forceinline__ void colour_blend(const float (&md)[4], const int (&mi)[4], const float* cr,
+                                             const float* cg, const float* cb, float* out) {
+    const float sum = md[0] + md[1] + md[2] + md[3];
+    const float inv = (sum > 0.0f) ? 1.0f / sum : 0.0f;
+    float o[3] = {0.f, 0.f, 0.f};
+    for (int k = 0; k < 4; ++k) {
+        const int idx = (mi[k] == 0x7fffffff) ? 0 : mi[k];
+        const float w = md[k] * inv;
+        o[0] += cr[idx] * w;
+        o[1] += cg[idx] * w;
+        o[2] += cb[idx] * w;
+    }
+    out[0] = o[0];
+    out[1] = o[1];
+    out[2] = o[2];
+}
+
+// bits of v (< 1024) to every third bit
+__device__ __forceinline__ unsigned spread3(unsigned v) {
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000ffu;
+    v = (v | (v << 8)) & 0x0300f00fu;
+    v = (v | (v << 4)) & 0x030c30c3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+// Near pass, 8 lanes per mesh vertex: the samples of the 3x3x3 block of finest-level
+// cells around the vertex's cell (every sample outside it is at least one cell width
+// away), spread over the group's lanes (flattened over the 27 cell ranges), each lane
+// keeping a sorted 4-list, merged by warp-minimum rounds within the group.  When 4 were
+// found and the 4th is closer than one width they are the exact 4 nearest and the colour
+// is written; otherwise the vertex goes to the far list for the wide search (k_colour).
+constexpr int kNearLanes = 8;
+constexpr int kNearGroups = kBlock / kNearLanes;
+__global__ void __launch_bounds__(kBlock) k_colour_near(Counters* c, int g, const float* mv, const float* px,
+                                                        const float* py, const float* pz, const float* cr,
+                                                        const float* cg, const float* cb, const int* cell_start,
+                                                        int* far, float* out) {
+    __shared__ int s_off[kNearGroups][28];
+    __shared__ int s_base[kNearGroups][27];
+    const int V = c->n_mesh_vertices;
+    const int G = 1 << g;
+    const float w = 1.0f / (float)G;
+    const int lane = threadIdx.x & (kNearLanes - 1);
+    const int gib = threadIdx.x / kNearLanes;
+    const unsigned gmask = 0xffu << (threadIdx.x & 24);   // the group's lanes in its warp
+    const int group = (blockIdx.x * blockDim.x + threadIdx.x) / kNearLanes;
+    const int ngroups = (gridDim.x * blockDim.x) / kNearLanes;
+    for (int v = group; v < V; v += ngroups) {
+        const float qx = mv[3 * (size_t)v], qy = mv[3 * (size_t)v + 1], qz = mv[3 * (size_t)v + 2];
+        const int cx = min(max((int)floorf(qx * G), 0), G - 1);
+        const int cy = min(max((int)floorf(qy * G), 0), G - 1);
+        const int cz = min(max((int)floorf(qz * G), 0), G - 1);
+        // cells k = lane + 8 r, offsets in k order
+        int running = 0;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int k = lane + kNearLanes * r;
+            int cnt = 0, base = 0;
+            if (k < 27) {
+                const int a = cx + k / 9 - 1, b = cy + (k / 3) % 3 - 1, z = cz + k % 3 - 1;
+                if (a >= 0 && a < G && b >= 0 && b < G && z >= 0 && z < G) {
+                    const unsigned m = (spread3((unsigned)a) << 2) | (spread3((unsigned)b) << 1) | spread3((unsigned)z);
+                    base = cell_start[m];
+                    cnt = cell_start[m + 1] - base;
+                }
+            }
+            int incl = cnt;
+#pragma unroll
+            for (int o = 1; o < kNearLanes; o <<= 1) {
+                const int y = __shfl_up_sync(gmask, incl, o, kNearLanes);
+                if (lane >= o) incl += y;
+            }
+            if (k < 27) {
+                s_off[gib][k] = running + incl - cnt;
+                s_base[gib][k] = base;
+            }
+            running += __shfl_sync(gmask, incl, kNearLanes - 1, kNearLanes);
+        }
+        if (lane == 0) s_off[gib][27] = running;
+        __syncwarp(gmask);
+        float bd[4] = {1e6f, 1e6f, 1e6f, 1e6f};
+        int bi[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
+        int k = 0;
+        for (int t = lane; t < running; t += kNearLanes) {
+            while (s_off[gib][k + 1] <= t) ++k;   // flattened index -> cell (increasing)
+            knn_visit(qx, qy, qz, px, py, pz, s_base[gib][k] + (t - s_off[gib][k]), bd, bi);
+        }
+        __syncwarp(gmask);
+        // the group's 4 nearest: four rounds of the minimum head, its lane popping it
+        float md[4];
+        int mi[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            float d = bd[0];
+            int i = bi[0];
+#pragma unroll
+            for (int o = kNearLanes / 2; o > 0; o >>= 1) {
+                const float od = __shfl_xor_sync(gmask, d, o);
+                const int oi = __shfl_xor_sync(gmask, i, o);
+                if (knn_less(od, oi, d, i)) { d = od; i = oi; }
+            }
+            md[r] = d;
+            mi[r] = i;
+            if (bd[0] == d && bi[0] == i) {
+                bd[0] = bd[1]; bi[0] = bi[1];
+                bd[1] = bd[2]; bi[1] = bi[2];
+                bd[2] = bd[3]; bi[2] = bi[3];
+                bd[3] = 1e6f; bi[3] = 0x7fffffff;
+            }
+        }
+        if (lane == 0) {
+            if (mi[3] != 0x7fffffff && md[3] < w * w) colour_blend(md, mi, cr, cg, cb, &out[3 * (size_t)v]);
+            else far[atomicAdd(&c->n_colour_far, 1)] = v;
+        }
+    }
+}
+
 constexpr int kColourMaxShell = 12;   // widest block (2R+1 cells per axis) searched at one level
 
-// One warp per mesh vertex.  The samples are Morton-sorted, so the samples of a grid cell
-// at any level g <= gmax form one contiguous range, read from the level-gmax table at
-// cell codes shifted by 3 (gmax - g).  At the finest level the warp gathers the samples
-// of the 3x3x3 block of cells around the vertex's cell (the 27 ranges flattened over the
-// lanes) and keeps the 4 nearest (private sorted lists, butterfly merge).  Every sample
+// Far pass, one warp per vertex of the far list.  The samples are Morton-sorted, so the
+// samples of a grid cell at any level g <= gmax form one contiguous range, read from the
+// level-gmax table at cell codes shifted by 3 (gmax - g).  At the finest level the warp
+// gathers the samples of the 3x3x3 block of cells around the vertex's cell (the 27 ranges
+// flattened over the lanes) and keeps the 4 nearest (private sorted lists, merged by
+// warp-minimum rounds).  Every sample
 // outside a block of radius R cells is at least R cell widths away, so:
 //   * 4 found and the 4th distance below 1 width: done;
 //   * 4 found otherwise: the 4th distance bounds the answer; the shell of cells between
@@ -114,15 +236,17 @@ constexpr int kColourMaxShell = 12;   // widest block (2R+1 cells per axis) sear
 //   * fewer than 4, or R too large: restart one level coarser.
 __global__ void __launch_bounds__(kBlock) k_colour(const Counters* c, int gmax, const float* mv, const float* px,
                                                    const float* py, const float* pz, const float* cr, const float* cg,
-                                                   const float* cb, const int* cell_start, float* out) {
+                                                   const float* cb, const int* cell_start, const int* far,
+                                                   float* out) {
     __shared__ int s_off[kBlock / 32][28];
     __shared__ int s_base[kBlock / 32][27];
-    const int V = c->n_mesh_vertices;
+    const int nfar = c->n_colour_far;
     const int lane = lane_id();
     const int wib = threadIdx.x >> 5;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int v = warp; v < V; v += nwarps) {
+    for (int t = warp; t < nfar; t += nwarps) {
+        const int v = far[t];
         const float qx = mv[3 * (size_t)v], qy = mv[3 * (size_t)v + 1], qz = mv[3 * (size_t)v + 2];
         float md[4];
         int mi[4];
@@ -185,22 +309,7 @@ __global__ void __launch_bounds__(kBlock) k_colour(const Counters* c, int gmax, 
             knn_warp_merge(bd, bi, md, mi);
             break;
         }
-        if (lane == 0) {
-            const float sum = md[0] + md[1] + md[2] + md[3];
-            const float inv = (sum > 0.0f) ? 1.0f / sum : 0.0f;
-            float o[3] = {0.f, 0.f, 0.f};
-            for (int k = 0; k < 4; ++k) {
-                // fewer than 4 samples: the reference's unfilled slots (distance 1e6, sample 0)
-                const int idx = (mi[k] == 0x7fffffff) ? 0 : mi[k];
-                const float w = md[k] * inv;   // weight grows with the squared distance
-                o[0] += cr[idx] * w;
-                o[1] += cg[idx] * w;
-                o[2] += cb[idx] * w;
-            }
-            out[3 * (size_t)v] = o[0];
-            out[3 * (size_t)v + 1] = o[1];
-            out[3 * (size_t)v + 2] = o[2];
-        }
+        if (lane == 0) colour_blend(md, mi, cr, cg, cb, &out[3 * (size_t)v]);
     }
 }
 
@@ -272,8 +381,10 @@ cudaError_t transfer_build(Workspace& ws, int with_colour, int with_normals) {
     if (with_colour) {
         const int g = D < kColourGridLevel ? D : kColourGridLevel;
         int* cell_start = ws.cell_start;   // (1 << 3g) + 1 entries, from transfer_prepare
-        k_colour<<<grid, kBlock, 0, s>>>(ws.cnt, g, ws.mesh_v, ws.px, ws.py, ws.pz, ws.cr, ws.cg, ws.cb, cell_start,
-                                         ws.mesh_c);
+        k_colour_near<<<grid, kBlock, 0, s>>>(ws.cnt, g, ws.mesh_v, ws.px, ws.py, ws.pz, ws.cr, ws.cg, ws.cb,
+                                              cell_start, ws.colour_far, ws.mesh_c);
+        k_colour<<<ws.num_sms, kBlock, 0, s>>>(ws.cnt, g, ws.mesh_v, ws.px, ws.py, ws.pz, ws.cr, ws.cg, ws.cb,
+                                               cell_start, ws.colour_far, ws.mesh_c);
     }
     if (with_normals) {
         double* acc = ws.nacc;

@@ -151,6 +151,7 @@ struct Workspace {
     double* nacc;           // per output vertex normal accumulator (3 doubles)
     int* vcount;            // per output vertex triangle count
     int* cell_start;        // sample grid for the colour search
+    int* colour_far;        // mesh vertices left to the wide colour search
 
     // staging for the two-phase insertion of each mesh part
     float* part_v;          // 3 x cap
