@@ -223,29 +223,68 @@ __global__ void __launch_bounds__(kBlock) k_colour_near(Counters* c, int g, cons
 
 constexpr int kColourMaxShell = 12;   // widest block (2R+1 cells per axis) searched at one level
 
-// Far pass, one warp per vertex of the far list.  The samples are Morton-sorted, so the
-// samples of a grid cell at any level g <= gmax form one contiguous range, read from the
-// level-gmax table at cell codes shifted by 3 (gmax - g).  At the finest level the warp
-// gathers the samples of the 3x3x3 block of cells around the vertex's cell (the 27 ranges
-// flattened over the lanes) and keeps the 4 nearest (private sorted lists, merged by
-// warp-minimum rounds).  Every sample
+// Far pass, one block of 256 threads per vertex of the far list.  The samples are
+// Morton-sorted, so the samples of a grid cell at any level g <= gmax form one contiguous
+// range, read from the level-gmax table at cell codes shifted by 3 (gmax - g).  At the
+// finest level the block gathers the samples of the 3x3x3 block of cells around the
+// vertex's cell (the 27 ranges flattened over the threads) and keeps the 4 nearest
+// (private sorted lists, merged by warp-minimum rounds).  Every sample
 // outside a block of radius R cells is at least R cell widths away, so:
 //   * 4 found and the 4th distance below 1 width: done;
 //   * 4 found otherwise: the 4th distance bounds the answer; the shell of cells between
-//     radius 2 and the radius R that exceeds it (one lane per cell) completes the search;
+//     radius 2 and the radius R that exceeds it (one thread per cell) completes the search;
 //   * fewer than 4, or R too large: restart one level coarser.
-__global__ void __launch_bounds__(kBlock) k_colour(const Counters* c, int gmax, const float* mv, const float* px,
-                                                   const float* py, const float* pz, const float* cr, const float* cg,
-                                                   const float* cb, const int* cell_start, const int* far,
-                                                   float* out) {
-    __shared__ int s_off[kBlock / 32][28];
-    __shared__ int s_base[kBlock / 32][27];
+// the block's 4 nearest from its threads' sorted 4-lists: each warp merges its lanes, then
+// warp 0 merges the warps' 4 (one candidate per lane); every thread gets the result
+constexpr int kFarThreads = kBlock;
+static_assert(kFarThreads / 32 * 4 == 32, "one warp holds the candidates of all warps");
+__device__ __forceinline__ void knn_block_merge(const float (&bd)[4], const int (&bi)[4], float (&md)[4],
+                                                int (&mi)[4], float* s_cd, int* s_ci) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float wd[4];
+    int wi[4];
+    knn_warp_merge(bd, bi, wd, wi);
+    if (lane == 0) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            s_cd[warp * 4 + q] = wd[q];
+            s_ci[warp * 4 + q] = wi[q];
+        }
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const float cd[4] = {s_cd[lane], 1e6f, 1e6f, 1e6f};
+        const int ci[4] = {s_ci[lane], 0x7fffffff, 0x7fffffff, 0x7fffffff};
+        knn_warp_merge(cd, ci, wd, wi);
+    }
+    __syncthreads();   // every warp has read its candidates before they are replaced
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            s_cd[q] = wd[q];
+            s_ci[q] = wi[q];
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        md[q] = s_cd[q];
+        mi[q] = s_ci[q];
+    }
+    __syncthreads();   // read before the next merge writes
+}
+
+__global__ void __launch_bounds__(kFarThreads) k_colour(const Counters* c, int gmax, const float* mv,
+                                                       const float* px, const float* py, const float* pz,
+                                                       const float* cr, const float* cg, const float* cb,
+                                                       const int* cell_start, const int* far, float* out) {
+    __shared__ int s_off[28];
+    __shared__ int s_base[27];
+    __shared__ float s_cd[32];
+    __shared__ int s_ci[32];
     const int nfar = c->n_colour_far;
-    const int lane = lane_id();
-    const int wib = threadIdx.x >> 5;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int t = warp; t < nfar; t += nwarps) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int t = blockIdx.x; t < nfar; t += gridDim.x) {
         const int v = far[t];
         const float qx = mv[3 * (size_t)v], qy = mv[3 * (size_t)v + 1], qz = mv[3 * (size_t)v + 2];
         float md[4];
@@ -256,60 +295,61 @@ __global__ void __launch_bounds__(kBlock) k_colour(const Counters* c, int gmax, 
             const int cx = min(max((int)floorf(qx * G), 0), G - 1);
             const int cy = min(max((int)floorf(qy * G), 0), G - 1);
             const int cz = min(max((int)floorf(qz * G), 0), G - 1);
-            int cnt = 0, base = 0;
-            if (lane < 27) {
-                const int a = cx + lane / 9 - 1, b = cy + (lane / 3) % 3 - 1, z = cz + lane % 3 - 1;
-                if (a >= 0 && a < G && b >= 0 && b < G && z >= 0 && z < G) {
-                    const unsigned m = morton3(a, b, z, g);
-                    base = cell_start[(size_t)m << shift];
-                    cnt = cell_start[(size_t)(m + 1) << shift] - base;
+            if (warp == 0) {
+                int cnt = 0, base = 0;
+                if (lane < 27) {
+                    const int a = cx + lane / 9 - 1, b = cy + (lane / 3) % 3 - 1, z = cz + lane % 3 - 1;
+                    if (a >= 0 && a < G && b >= 0 && b < G && z >= 0 && z < G) {
+                        const unsigned m = morton3(a, b, z, g);
+                        base = cell_start[(size_t)m << shift];
+                        cnt = cell_start[(size_t)(m + 1) << shift] - base;
+                    }
                 }
-            }
-            int incl = cnt;
+                int incl = cnt;
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int y = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o) incl += y;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += y;
+                }
+                if (lane < 27) {
+                    s_off[lane] = incl - cnt;
+                    s_base[lane] = base;
+                }
+                if (lane == 26) s_off[27] = incl;
             }
-            if (lane < 27) {
-                s_off[wib][lane] = incl - cnt;
-                s_base[wib][lane] = base;
-            }
-            if (lane == 26) s_off[wib][27] = incl;
-            const int total = __shfl_sync(0xffffffffu, incl, 26);
-            __syncwarp();
+            __syncthreads();
+            const int total = s_off[27];
             float bd[4] = {1e6f, 1e6f, 1e6f, 1e6f};
             int bi[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
             int k = 0;
-            for (int t = lane; t < total; t += 32) {
-                while (s_off[wib][k + 1] <= t) ++k;   // flattened index -> cell (increasing)
-                knn_visit(qx, qy, qz, px, py, pz, s_base[wib][k] + (t - s_off[wib][k]), bd, bi);
+            for (int i = tid; i < total; i += kFarThreads) {
+                while (s_off[k + 1] <= i) ++k;   // flattened index -> cell (increasing)
+                knn_visit(qx, qy, qz, px, py, pz, s_base[k] + (i - s_off[k]), bd, bi);
             }
-            __syncwarp();
-            knn_warp_merge(bd, bi, md, mi);
+            knn_block_merge(bd, bi, md, mi, s_cd, s_ci);
             if (mi[3] == 0x7fffffff) continue;   // fewer than 4 samples in the block
             const float w = 1.0f / (float)G;
             if (md[3] < w * w) break;
             int R = (int)(sqrtf(md[3]) * (float)G) + 1;
             while (!(md[3] < __fmul_rn(R * w, R * w))) ++R;
             if (R > kColourMaxShell && g > 0) continue;
-            // shell of cells with Chebyshev radius 2..R (lane-private lists continue)
+            // shell of cells with Chebyshev radius 2..R (thread-private lists continue)
             const int side = 2 * R + 1;
             const int ncell = side * side * side;
-            for (int t = lane; t < ncell; t += 32) {
-                const int ta = t / (side * side), tr = t - ta * side * side;
+            for (int i = tid; i < ncell; i += kFarThreads) {
+                const int ta = i / (side * side), tr = i - ta * side * side;
                 const int tb = tr / side, tz = tr - tb * side;
                 const int a = cx - R + ta, b = cy - R + tb, z = cz - R + tz;
                 if (a < 0 || a >= G || b < 0 || b >= G || z < 0 || z >= G) continue;
                 if (max(abs(a - cx), max(abs(b - cy), abs(z - cz))) <= 1) continue;
                 const unsigned m = morton3(a, b, z, g);
                 const int s0 = cell_start[(size_t)m << shift], s1 = cell_start[(size_t)(m + 1) << shift];
-                for (int i = s0; i < s1; ++i) knn_visit(qx, qy, qz, px, py, pz, i, bd, bi);
+                for (int j = s0; j < s1; ++j) knn_visit(qx, qy, qz, px, py, pz, j, bd, bi);
             }
-            knn_warp_merge(bd, bi, md, mi);
+            knn_block_merge(bd, bi, md, mi, s_cd, s_ci);
             break;
         }
-        if (lane == 0) colour_blend(md, mi, cr, cg, cb, &out[3 * (size_t)v]);
+        if (tid == 0) colour_blend(md, mi, cr, cg, cb, &out[3 * (size_t)v]);
     }
 }
 
@@ -383,8 +423,8 @@ cudaError_t transfer_build(Workspace& ws, int with_colour, int with_normals) {
         int* cell_start = ws.cell_start;   // (1 << 3g) + 1 entries, from transfer_prepare
         k_colour_near<<<grid, kBlock, 0, s>>>(ws.cnt, g, ws.mesh_v, ws.px, ws.py, ws.pz, ws.cr, ws.cg, ws.cb,
                                               cell_start, ws.colour_far, ws.mesh_c);
-        k_colour<<<ws.num_sms, kBlock, 0, s>>>(ws.cnt, g, ws.mesh_v, ws.px, ws.py, ws.pz, ws.cr, ws.cg, ws.cb,
-                                               cell_start, ws.colour_far, ws.mesh_c);
+        k_colour<<<2 * ws.num_sms, kFarThreads, 0, s>>>(ws.cnt, g, ws.mesh_v, ws.px, ws.py, ws.pz, ws.cr, ws.cg,
+                                                        ws.cb, cell_start, ws.colour_far, ws.mesh_c);
     }
     if (with_normals) {
         double* acc = ws.nacc;
