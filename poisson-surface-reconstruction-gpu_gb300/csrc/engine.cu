@@ -248,6 +248,7 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     A.add(ws.c_neigh, 27 * (size_t)subn);
     A.add(ws.c_live, (size_t)subd);
     A.add(ws.c_poly, 28 * (size_t)subd);
+    A.add(ws.c_touch, (size_t)subd);
     A.add(ws.lv_vnode, (size_t)subd);
     A.add(ws.lv_nb, 27 * (size_t)subd);
     A.add(ws.s_vtx, 8 * (size_t)subd); A.add(ws.s_edge, 12 * (size_t)subd);

@@ -694,6 +694,7 @@ struct SubArrays {
     size_t cstride;
     int* live;    // live slots, depth after depth
     float* poly;  // [28][cap_live]: per live entry, Bernstein coefficients of its levels, sum |y|
+    unsigned char* touch;   // per live entry: faces of its root's cell it lies on (bits x-, x+, y-, y+, z-, z+)
     int* lv_vnode;   // virtual index of each live depth-D cell
     int cap_nodes, cap_live, cap_live_d;
 };
@@ -907,10 +908,18 @@ __device__ __forceinline__ void root_coefficients(int r, int root_node, int rd, 
     }
 }
 
-// per-thread hand-over of a candidate's coefficients from the scan's load to its store
+// per-thread hand-over of a candidate's coefficients (28) and face bits (1) from the
+// scan's load to its store
 __device__ __forceinline__ float* sub_poly_stash() {
-    __shared__ float s_stash[28 * kBlock];
+    __shared__ float s_stash[29 * kBlock];
     return s_stash;
+}
+
+// faces of the root's cell that child `ch` (x = 4, y = 2, z = 1) of a cell with face bits
+// pt lies on: a face its parent lies on, on the child's side
+__device__ __forceinline__ unsigned child_touch(unsigned pt, int ch) {
+    const unsigned side = ((ch & 4) ? 2u : 1u) | ((ch & 2) ? 8u : 4u) | ((ch & 1) ? 32u : 16u);
+    return pt & side;
 }
 
 // One candidate of depth d (computeRebuildNeighbor :669-696 for its neighbours): its record,
@@ -936,6 +945,25 @@ struct SubLevelLoad {
     SubArrays A;
     __device__ unsigned operator()(int i) const {
         const int nl_prev = c->sub_nlive[d - 1];
+        if (i < 8 * nl_prev) {
+            // A child on no face of its root's cell is interior: its levels are its parent's,
+            // restricted to its octant, with nothing of its own or deeper; test that first
+            // (the same test as below, without touching any record)
+            const int pl = c->sub_lbase[d - 1] + (i >> 3);
+            if (child_touch(A.touch[pl], i & 7) == 0u) {
+                float C[27];
+#pragma unroll
+                for (int kk = 0; kk < 27; ++kk) C[kk] = 0.0f;
+                add_subdivided(A.poly + pl, (size_t)A.cap_live, (unsigned)(i & 7), 1, C);
+                const float mag = A.poly[(size_t)27 * A.cap_live + pl];
+                float lo = C[0], hi = C[0];
+#pragma unroll
+                for (int kk = 1; kk < 27; ++kk) { lo = fminf(lo, C[kk]); hi = fmaxf(hi, C[kk]); }
+                const float iso = c->iso;
+                const float margin = 1e-4f * (mag + fabsf(iso));
+                if (lo - iso > margin || hi - iso < -margin) return 0u;   // certain sign
+            }
+        }
         const int slot = c->sub_cbase[d] + i;
         int g, vnode, k, pslot, pa;   // pa: parent as a neighbour-table entry
         float cc[3];
@@ -1087,6 +1115,9 @@ struct SubLevelLoad {
 #pragma unroll
         for (int kk = 0; kk < 27; ++kk) stash[kk * kBlock + threadIdx.x] = C[kk];
         stash[27 * kBlock + threadIdx.x] = mag;
+        const unsigned touch = at_root_depth ? 0x3fu
+                                             : child_touch(A.touch[c->sub_lbase[d - 1] + (i >> 3)], i & 7);
+        stash[28 * kBlock + threadIdx.x] = __uint_as_float(touch);
         if (interior) {
 #pragma unroll
             for (int kk = 0; kk < 27; ++kk) {
@@ -1121,6 +1152,7 @@ struct SubLevelStore {
         const float* stash = sub_poly_stash();
 #pragma unroll
         for (int k = 0; k < 28; ++k) A.poly[(size_t)k * A.cap_live + at] = stash[k * kBlock + threadIdx.x];
+        A.touch[at] = (unsigned char)__float_as_uint(stash[28 * kBlock + threadIdx.x]);
         if (d == depth) {
             if ((int)pre >= A.cap_live_d) { atomicOr(err, kErrCapacity); return; }
             A.lv_vnode[pre] = A.vnode[slot];
@@ -1708,8 +1740,8 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
     const int gl = grid_for(ws, ws.cap.sub_dnodes);
     cudaError_t e;
     SubArrays A{ws.c_vnode, ws.c_key, ws.c_group, ws.c_parent, ws.c_jump, ws.c_depth, ws.c_cx, ws.c_cy, ws.c_cz,
-                ws.c_neigh, (size_t)ws.cap.sub_nodes, ws.c_live, ws.c_poly, ws.lv_vnode, ws.cap.sub_nodes,
-                ws.cap.sub_live, ws.cap.sub_dnodes};
+                ws.c_neigh, (size_t)ws.cap.sub_nodes, ws.c_live, ws.c_poly, ws.c_touch, ws.lv_vnode,
+                ws.cap.sub_nodes, ws.cap.sub_live, ws.cap.sub_dnodes};
     k_sub_setup<<<1, 32, 0, s>>>(c, D, ws.sub_root_depth, ws.cap.sub_nodes);   // kMaxDepth + 2 <= 32 lanes
     k_root_poly<<<grid_for(ws, ws.cap_poly), kBlock, 0, s>>>(c, D, ws.sub_root, ws.ndepth, ws.ctr_x, ws.ctr_y,
                                                              ws.ctr_z, ws.neigh, stride, ws.parent, ws.enc, ws.xsol,

@@ -130,6 +130,7 @@ struct Workspace {
     int* c_neigh;           // [27][cap.sub_nodes]
     int* c_live;            // live slots, depth after depth (capacity cap.sub_live)
     float* c_poly;          // [28][cap.sub_live]: per live entry, its Bernstein coefficients, sum |y|
+    unsigned char* c_touch; // per live entry: faces of its root's cell its cell lies on
     // live depth-D cells (capacity cap.sub_dnodes)
     int* lv_vnode;          // virtual index, ascending
     int* lv_nb;             // [27][cap.sub_dnodes]: live index of each same-depth neighbour
