@@ -908,10 +908,10 @@ __device__ __forceinline__ void root_coefficients(int r, int root_node, int rd, 
     }
 }
 
-// per-thread hand-over of a candidate's coefficients (28) and face bits (1) from the
-// scan's load to its store
+// per-thread hand-over of a candidate's coefficients (28), face bits and virtual index
+// from the scan's load to its store
 __device__ __forceinline__ float* sub_poly_stash() {
-    __shared__ float s_stash[29 * kBlock];
+    __shared__ float s_stash[30 * kBlock];
     return s_stash;
 }
 
@@ -1036,6 +1036,11 @@ struct SubLevelLoad {
         // nodes are referred to later (children, value chains), so a node dropped here needs
         // nothing else.
         const bool interior = ok[0][0] && ok[0][2] && ok[1][0] && ok[1][2] && ok[2][0] && ok[2][2];
+        // values of the own level's neighbours, read as each neighbour is found: below its
+        // root only octree neighbours carry one (deeper subdivision nodes are never roots)
+        float y[27];
+#pragma unroll
+        for (int kk = 0; kk < 27; ++kk) y[kk] = 0.0f;
         if (!interior) {
 #pragma unroll
             for (int kk = 0; kk < 27; ++kk) {
@@ -1072,6 +1077,7 @@ struct SubLevelLoad {
                     if (v >= 0 && (v < na || at_root_depth)) contrib = 1;
                 }
                 A.neigh[(size_t)kk * A.cstride + slot] = v;
+                if (v >= 0 && v < na && !at_root_depth) y[kk] = x[v];
             }
         }
         const int prec = (pslot >= 0) ? pslot : -2 - pa;
@@ -1090,13 +1096,6 @@ struct SubLevelLoad {
             add_subdivided(A.poly + pl, (size_t)A.cap_live, (unsigned)(i & 7), 1, C);
             mag = A.poly[(size_t)27 * A.cap_live + pl];
             if (contrib) {   // its own level (octree neighbours; never for an interior node)
-                float y[27];
-#pragma unroll
-                for (int kk = 0; kk < 27; ++kk) {
-                    int v = A.neigh[(size_t)kk * A.cstride + slot];
-                    if (v >= na) v = sub_value_node(v, na, G, root_self);
-                    y[kk] = (v >= 0) ? x[v] : 0.0f;
-                }
                 const float sc = (float)(1 << d);
                 const int base = (1 << d) - 1;
                 sign_level(y, base + (int)__fmul_rn(cc[0], sc), base + (int)__fmul_rn(cc[1], sc),
@@ -1118,6 +1117,7 @@ struct SubLevelLoad {
         const unsigned touch = at_root_depth ? 0x3fu
                                              : child_touch(A.touch[c->sub_lbase[d - 1] + (i >> 3)], i & 7);
         stash[28 * kBlock + threadIdx.x] = __uint_as_float(touch);
+        stash[29 * kBlock + threadIdx.x] = __int_as_float(vnode);
         if (interior) {
 #pragma unroll
             for (int kk = 0; kk < 27; ++kk) {
@@ -1155,7 +1155,7 @@ struct SubLevelStore {
         A.touch[at] = (unsigned char)__float_as_uint(stash[28 * kBlock + threadIdx.x]);
         if (d == depth) {
             if ((int)pre >= A.cap_live_d) { atomicOr(err, kErrCapacity); return; }
-            A.lv_vnode[pre] = A.vnode[slot];
+            A.lv_vnode[pre] = __float_as_int(stash[29 * kBlock + threadIdx.x]);
         }
     }
     // chains the counts: candidates of depth d + 1 = 8 x live of depth d + roots of d + 1
