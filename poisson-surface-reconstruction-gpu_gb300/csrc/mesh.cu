@@ -1764,47 +1764,51 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
     e = launch_scan<2>(PopcLoad8{ws.s_vmask},
                        SubVertexStore{ws.s_vmask, c, D, A, ws.sv_x, ws.sv_y, ws.sv_z, ws.sv_owner, ws.sv_kind,
                                       8 * ws.cap.sub_dnodes, err},
-                       &c->n_sub_dnodes, 0, ws.scan, total, err, s, ScanCount{&c->n_sub_vertices, 8 * ws.cap.sub_dnodes});
+                       &c->n_sub_dnodes, 0, ws.scan, total, err, s, ScanCount{&c->n_sub_vertices, 8 * ws.cap.sub_dnodes},
+                       1);
     if (e != cudaSuccess) return e;
     k_sub_vertex_maintain<<<gl, kBlock, 0, s>>>(c, ws.lv_nb, dstride, ws.sv_owner, ws.sv_kind, ws.s_vtx);
     k_sub_edge_owner<<<gl, kBlock, 0, s>>>(c, D, A, ws.lv_nb, dstride, ws.s_emask);
     e = launch_scan<2>(PopcLoad16{ws.s_emask},
                        SubEdgeStore{ws.s_emask, ws.se_owner, ws.se_kind, mb.edge_of_dnode, 12 * ws.cap.sub_dnodes, err},
-                       &c->n_sub_dnodes, 0, ws.scan, total, err, s, ScanCount{&c->n_sub_edges, 12 * ws.cap.sub_dnodes});
+                       &c->n_sub_dnodes, 0, ws.scan, total, err, s, ScanCount{&c->n_sub_edges, 12 * ws.cap.sub_dnodes},
+                       1);
     if (e != cudaSuccess) return e;
     k_sub_edge_maintain<<<gl, kBlock, 0, s>>>(c, ws.lv_nb, dstride, ws.se_owner, ws.se_kind, ws.s_edge);
-    k_sub_vertex_values<<<grid_for(ws, 32LL * 8 * ws.cap.sub_dnodes), kBlock, 0, s>>>(c, D, ws.sv_x, ws.sv_y, ws.sv_z, ws.sv_owner, ws.neigh, stride,
-                                              ws.parent, mb.groups, ws.root_self, A, ws.enc, ws.xsol, ws.sv_value, na);
+    k_sub_vertex_values<<<grid_for(ws, 32LL * 8 * ws.cap.sub_dnodes), kBlock, 0, s>>>(
+        c, D, ws.sv_x, ws.sv_y, ws.sv_z, ws.sv_owner, ws.neigh, stride, ws.parent, mb.groups, ws.root_self, A, ws.enc,
+        ws.xsol, ws.sv_value, na);
     // crossings: staged after the main part's vertices
     e = launch_scan<2>(SubCrossLoad{ws.se_owner, ws.se_kind, ws.s_vtx, dstride, ws.sv_value, err},
                        SubCrossStore{ws.se_owner, ws.se_kind, ws.s_vtx, dstride, ws.sv_value, ws.sv_x, ws.sv_y,
                                      ws.sv_z, ws.se_cross, ws.part_v, &c->n_cross, ws.part_cap_v, err},
-                       &c->n_sub_edges, 0, ws.scan, total, err, s, ScanCount{&c->n_sub_cross, ws.part_cap_v});
+                       &c->n_sub_edges, 0, ws.scan, total, err, s, ScanCount{&c->n_sub_cross, ws.part_cap_v}, 1);
     if (e != cudaSuccess) return e;
     // triangle prefix per live cell
     e = launch_scan<2>(SubCubeLoad{ws.s_vtx, dstride, ws.sv_value, ws.s_cube_class, err},
                        StoreExclusive{mb.tri_of_dnode}, &c->n_sub_dnodes, 0, ws.scan, total, err, s,
-                       ScanCount{&c->n_sub_tri, ws.part_cap_t});
+                       ScanCount{&c->n_sub_tri, ws.part_cap_t}, 1);
     if (e != cudaSuccess) return e;
     k_part_table<<<grid_for(ws, 1 << 16), kBlock, 0, s>>>(c, D, mb.groups, ws.lv_vnode, mb.edge_of_dnode, ws.se_cross,
                                                           mb.tri_of_dnode, mb.group_cross0, mb.parts);
     e = launch_scan<2>(SubCubeLoad{ws.s_vtx, dstride, ws.sv_value, ws.s_cube_class, err},
                        SubCubeStore{ws.s_cube_class, ws.s_edge, dstride, ws.se_cross, mb.group_cross0, c, D, A,
                                     ws.part_t, &c->n_tri, ws.part_cap_t, err},
-                       &c->n_sub_dnodes, 0, ws.scan, total, err, s);
+                       &c->n_sub_dnodes, 0, ws.scan, total, err, s, ScanCount{}, 1);
     if (e != cudaSuccess) return e;
     // insertion of all parts
     int* n_parts = mb.misc;
     int* n_staged_v = mb.misc + 1;
     int* n_staged_t = mb.misc + 2;
     k_count_parts<<<1, 1, 0, s>>>(c, n_parts, n_staged_v, n_staged_t, ws.part_cap_v, ws.part_cap_t);
-    e = launch_scan(KeepVertexLoad{ws.part_v}, KeepVertexStore{ws.part_v, ws.mesh_v, mb.kept_prefix, ws.cap.mesh_vertices, err},
-                    n_staged_v, 0, ws.scan, total, err, s, ScanCount{&c->n_mesh_vertices, ws.cap.mesh_vertices});
+    e = launch_scan(KeepVertexLoad{ws.part_v},
+                    KeepVertexStore{ws.part_v, ws.mesh_v, mb.kept_prefix, ws.cap.mesh_vertices, err}, n_staged_v, 0,
+                    ws.scan, total, err, s, ScanCount{&c->n_mesh_vertices, ws.cap.mesh_vertices}, 1);
     if (e != cudaSuccess) return e;
     e = launch_scan<1>(KeepTriLoad{ws.part_t, mb.parts, n_parts},
                     KeepTriStore{ws.part_t, mb.parts, n_parts, mb.kept_prefix, n_staged_v, &c->n_mesh_vertices,
                                  ws.mesh_t, ws.cap.mesh_tris, err},
-                    n_staged_t, 0, ws.scan, total, err, s, ScanCount{&c->n_mesh_triangles, ws.cap.mesh_tris});
+                    n_staged_t, 0, ws.scan, total, err, s, ScanCount{&c->n_mesh_triangles, ws.cap.mesh_tris}, 1);
     if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }
