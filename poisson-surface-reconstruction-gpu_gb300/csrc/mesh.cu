@@ -1714,11 +1714,12 @@ cudaError_t mesh_build_impl(Workspace& ws, const MeshBufs& mb) {
     // subdivision groups
     e = launch_scan(GroupFlagLoad{ws.sub_root, ws.ndepth, D - 4},
                     GroupFlagStore{ws.root_group, mb.groups, mb.max_groups, err}, &c->n_subroots, 0, ws.scan,
-                    total, err, s);
+                    total, err, s, ScanCount{}, 1);
     if (e != cudaSuccess) return e;
     k_group_count<<<1, 1, 0, s>>>(c, total, mb.max_groups);
     k_group_sizes<<<gm, kBlock, 0, s>>>(c, D, ws.sub_root, ws.ndepth, mb.groups);
-    e = launch_scan(GroupFieldLoad{mb.groups, 4}, GroupFieldStore{mb.groups, 3}, &c->n_groups, 0, ws.scan, total, err, s);
+    e = launch_scan(GroupFieldLoad{mb.groups, 4}, GroupFieldStore{mb.groups, 3}, &c->n_groups, 0, ws.scan, total, err,
+                    s, ScanCount{}, 1);
     if (e != cudaSuccess) return e;
     k_group_totals<<<1, 1, 0, s>>>(c, total, ws.cap.nodes);
     k_root_overlay<<<gm, kBlock, 0, s>>>(c, D, ws.sub_root, ws.ndepth, ws.key, ws.parent, ws.neigh, ws.root_group,
@@ -1737,7 +1738,8 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
     const size_t stride = (size_t)ws.cap.nodes;
     const size_t dstride = (size_t)ws.cap.sub_dnodes;
     const int na = ws.cap.nodes;
-    const int gl = grid_for(ws, ws.cap.sub_dnodes);
+    // kernels over live depth-D cells (few: one block per SM, grid-stride beyond)
+    const int gl = ws.num_sms;
     cudaError_t e;
     SubArrays A{ws.c_vnode, ws.c_key, ws.c_group, ws.c_parent, ws.c_jump, ws.c_depth, ws.c_cx, ws.c_cy, ws.c_cz,
                 ws.c_neigh, (size_t)ws.cap.sub_nodes, ws.c_live, ws.c_poly, ws.c_touch, ws.lv_vnode,
@@ -1757,7 +1759,7 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
         if (e != cudaSuccess) return e;
     }
     // the live depth-D cells carry every record from here on, indexed by their live index
-    k_sub_live_neigh<<<grid_for(ws, 27LL * ws.cap.sub_dnodes), kBlock, 0, s>>>(c, D, A, ws.lv_nb, dstride, na);
+    k_sub_live_neigh<<<2 * ws.num_sms, kBlock, 0, s>>>(c, D, A, ws.lv_nb, dstride, na);
     // s_vtx / s_edge need no clearing: every slot of a live cell is written by the owner of
     // that vertex / edge
     k_sub_vertex_owner<<<gl, kBlock, 0, s>>>(c, D, A, ws.lv_nb, dstride, ws.s_vmask);
@@ -1775,7 +1777,7 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
                        1);
     if (e != cudaSuccess) return e;
     k_sub_edge_maintain<<<gl, kBlock, 0, s>>>(c, ws.lv_nb, dstride, ws.se_owner, ws.se_kind, ws.s_edge);
-    k_sub_vertex_values<<<grid_for(ws, 32LL * 8 * ws.cap.sub_dnodes), kBlock, 0, s>>>(
+    k_sub_vertex_values<<<4 * ws.num_sms, kBlock, 0, s>>>(
         c, D, ws.sv_x, ws.sv_y, ws.sv_z, ws.sv_owner, ws.neigh, stride, ws.parent, mb.groups, ws.root_self, A, ws.enc,
         ws.xsol, ws.sv_value, na);
     // crossings: staged after the main part's vertices
