@@ -406,29 +406,37 @@ __device__ __forceinline__ void decode3s(int e, int depth, int& ix, int& iy, int
     iz = e >> (2 * (depth + 1));
 }
 
-// chain value: every ancestor of `node` (itself first), 27 neighbours each, terms
-// ((x * Fx) * Fy) * Fz accumulated in order (mirrored by the oracle's float mode)
-__device__ __forceinline__ float chain_value(int node, float qx, float qy, float qz, int depth, const int* neigh,
-                                             size_t stride, const int* parent, const int* enc, const float* x) {
-    float val = 0.0f;
-    while (node != -1) {
-        val = level_terms(node, val, qx, qy, qz, depth, neigh, stride, enc, x);
-        node = parent[node];
+// Implicit value at a sample point: the 27 neighbour terms ((x * Fx) * Fy) * Fz of every
+// level of its chain (its depth-D node and that node's ancestors).  The coarser levels are
+// summed first, as soon as their systems are solved (k_point_values_coarse, beside the
+// depth-D CG; the partial sum is kept in `out`), then the depth-D terms are added
+// (k_point_values).  The iso-value is the FP64 mean of these float values.
+__global__ void __launch_bounds__(kBlock) k_point_values_coarse(const Counters* c, int depth, const float* px,
+                                                                const float* py, const float* pz,
+                                                                const int* point2node, const int* neigh,
+                                                                size_t stride, const int* parent, const int* enc,
+                                                                const float* x, float* out) {
+    const int n = c->n_points;
+    const int bD = c->level_base[depth];
+    PSR_GRID_STRIDE(i, n) {
+        const float qx = px[i], qy = py[i], qz = pz[i];
+        float val = 0.0f;
+        for (int node = parent[bD + point2node[i]]; node != -1; node = parent[node])
+            val = level_terms(node, val, qx, qy, qz, depth, neigh, stride, enc, x);
+        out[i] = val;
     }
-    return val;
 }
 
 __global__ void __launch_bounds__(kBlock) k_point_values(const Counters* c, int depth, const float* px,
                                                          const float* py, const float* pz, const int* point2node,
-                                                         const int* neigh, size_t stride, const int* parent,
-                                                         const int* enc, const float* x, float* out,
-                                                         double* block_sums) {
+                                                         const int* neigh, size_t stride, const int* enc,
+                                                         const float* x, float* out, double* block_sums) {
     __shared__ double s_w[kBlock / 32];
     const int n = c->n_points;
     const int bD = c->level_base[depth];
     double acc = 0.0;
     PSR_GRID_STRIDE(i, n) {
-        float v = chain_value(bD + point2node[i], px[i], py[i], pz[i], depth, neigh, stride, parent, enc, x);
+        const float v = level_terms(bD + point2node[i], out[i], px[i], py[i], pz[i], depth, neigh, stride, enc, x);
         out[i] = v;
         acc += (double)v;
     }
@@ -436,9 +444,9 @@ __global__ void __launch_bounds__(kBlock) k_point_values(const Counters* c, int 
     if (lane_id() == 0) s_w[threadIdx.x >> 5] = acc;
     __syncthreads();
     if (threadIdx.x == 0) {
-        double s = 0.0;
-        for (int w = 0; w < kBlock / 32; ++w) s += s_w[w];
-        block_sums[blockIdx.x] = s;
+        double sum = 0.0;
+        for (int w = 0; w < kBlock / 32; ++w) sum += s_w[w];
+        block_sums[blockIdx.x] = sum;
     }
 }
 
@@ -547,7 +555,6 @@ cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, 
         b.first = D - ncl;
         e = launch_cg(k_cg_cta, b, ncta, 1, ws.aux);   // clusters of one CTA
     }
-    if (e == cudaSuccess) e = cudaEventRecord(ws.ev_join, ws.aux);
     if (e != cudaSuccess) return e;
     auto set_stencils = [&](CgcArgs& q) {
         for (int u = 0; u < 3; ++u)
@@ -563,6 +570,16 @@ cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, 
         if (e == cudaSuccess) e = cudaEventRecord(ws.ev_join3, ws.aux3);
         if (e != cudaSuccess) return e;
     }
+    // the coarser levels' part of the sample values, as soon as every depth below D is
+    // solved, beside the depth-D CG
+    if (ncl > 1) e = cudaStreamWaitEvent(ws.aux, ws.ev_join3, 0);
+    if (e == cudaSuccess) {
+        k_point_values_coarse<<<ws.num_sms * 4, kBlock, 0, ws.aux>>>(ws.cnt, ws.depth, ws.px, ws.py, ws.pz,
+                                                                     ws.point2node, ws.neigh, (size_t)ws.cap.nodes,
+                                                                     ws.parent, ws.enc, ws.xsol, ws.point_val);
+        e = cudaEventRecord(ws.ev_join, ws.aux);
+    }
+    if (e != cudaSuccess) return e;
     if (ncl > 0) {
         a.first = D;
         set_stencils(a);
@@ -574,13 +591,11 @@ cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, 
         if (e != cudaSuccess) return e;
     }
     e = cudaStreamWaitEvent(s, ws.ev_join, 0);
-    if (e == cudaSuccess && ncl > 1) e = cudaStreamWaitEvent(s, ws.ev_join3, 0);
     if (e != cudaSuccess) return e;
-    // iso-value
+    // iso-value: the depth-D terms complete the sample values
     const int nb = ws.num_sms * 4;
     k_point_values<<<nb, kBlock, 0, s>>>(ws.cnt, ws.depth, ws.px, ws.py, ws.pz, ws.point2node, ws.neigh,
-                                         (size_t)ws.cap.nodes, ws.parent, ws.enc, ws.xsol, ws.point_val,
-                                         ws.iso_partial);
+                                         (size_t)ws.cap.nodes, ws.enc, ws.xsol, ws.point_val, ws.iso_partial);
     k_iso_finalize<<<1, 256, 0, s>>>(ws.cnt, ws.iso_partial, nb);
     return cudaGetLastError();
 }
