@@ -270,23 +270,36 @@ cudaError_t field_build(Workspace& ws) {
                                                                     ws.pidx, ws.pnum, ws.ctr_x, ws.ctr_y, ws.ctr_z,
                                                                     ws.neigh, stride, vx, vy, vz);
     const int dsplit = D >= 2 ? D - 2 : 0;
-    k_div_fine<<<ws.num_sms * 8, kBlock, 0, s>>>(c, D, dsplit, ws.res, ws.enc, ws.didx, ws.dnum, ws.neigh, stride, vx,
-                                                 vy, vz, ws.dff, ws.divg);
+    cudaError_t e = cudaSuccess;
     if (dsplit > 0) {
-        // item_start / n_items / partial live in the (otherwise idle) CG scratch
+        // The coarse depths' chunked divergence runs on the second stream beside k_div_fine
+        // (both only read the vector field); it issues the only scan meanwhile.
+        // item_start / n_items / partial live in the (otherwise idle) CG scratch.
+        cudaStream_t a2 = ws.aux;
+        e = cudaEventRecord(ws.ev_fork, s);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(a2, ws.ev_fork, 0);
+        if (e != cudaSuccess) return e;
         unsigned* item_start = (unsigned*)ws.cg_r;
         int* n_items = (int*)&c->n_groups;
         unsigned* total = (unsigned*)&c->scan_total;
-        cudaError_t e = launch_scan(DivChunkLoad{ws.neigh, stride, ws.dnum}, StoreExclusive{item_start},
-                                    &c->level_base[dsplit], 0, ws.scan, total, &c->error, s, ScanCount{}, 1);
+        e = launch_scan(DivChunkLoad{ws.neigh, stride, ws.dnum}, StoreExclusive{item_start}, &c->level_base[dsplit],
+                        0, ws.scan, total, &c->error, a2, ScanCount{}, 1);
         if (e != cudaSuccess) return e;
         const int item_cap = ws.cap.nodes;   // partial buffer holds cap.nodes float pairs
-        k_div_chunk_count<<<1, 1, 0, s>>>(c, dsplit, total, item_cap, n_items);
+        k_div_chunk_count<<<1, 1, 0, a2>>>(c, dsplit, total, item_cap, n_items);
         FF* partial = reinterpret_cast<FF*>(ws.cg_partial);
-        k_div_chunks<<<ws.num_sms * 8, kBlock, 0, s>>>(c, D, dsplit, ws.res, n_items, item_start, ws.enc, ws.didx,
-                                                       ws.dnum, ws.neigh, stride, vx, vy, vz, ws.dff, partial);
-        k_div_coarse_reduce<<<grid_for(ws, 1 << 16), kBlock, 0, s>>>(c, dsplit, item_start, n_items, partial,
-                                                                    ws.divg);
+        k_div_chunks<<<ws.num_sms * 8, kBlock, 0, a2>>>(c, D, dsplit, ws.res, n_items, item_start, ws.enc, ws.didx,
+                                                        ws.dnum, ws.neigh, stride, vx, vy, vz, ws.dff, partial);
+        k_div_coarse_reduce<<<grid_for(ws, 1 << 16), kBlock, 0, a2>>>(c, dsplit, item_start, n_items, partial,
+                                                                     ws.divg);
+        e = cudaEventRecord(ws.ev_join, a2);
+        if (e != cudaSuccess) return e;
+    }
+    k_div_fine<<<ws.num_sms * 8, kBlock, 0, s>>>(c, D, dsplit, ws.res, ws.enc, ws.didx, ws.dnum, ws.neigh, stride, vx,
+                                                 vy, vz, ws.dff, ws.divg);
+    if (dsplit > 0) {
+        e = cudaStreamWaitEvent(s, ws.ev_join, 0);
+        if (e != cudaSuccess) return e;
     }
     return cudaGetLastError();
 }
