@@ -224,6 +224,7 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     A.add(ws.cg_blk, (size_t)nodes * 8 + 64);
     A.add(ws.cg_partial, std::max((size_t)nodes, (size_t)4096 * (kMaxDepth + 1)));
     A.add(ws.point_val, (size_t)N);
+    A.add(ws.pv_coef, 27 * ((size_t)dnodes / 8 + 64));
     A.add(ws.iso_partial, (size_t)ws.num_sms * 8 + 64);
     A.add(ws.vmask, (size_t)nodes);
     A.add(ws.emask16, (size_t)dnodes);

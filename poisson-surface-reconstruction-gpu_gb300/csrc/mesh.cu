@@ -721,74 +721,6 @@ struct SubArrays {
 // ~1.7e-5 sum |y| of the exact value; the float coefficients here are as close; the test
 // keeps a margin of 1e-4 (sum |y| + |iso|).
 
-// Bernstein coefficients on the cell of the translate `idx` (hs = h 2^l: half width in
-// level widths; x the cell centre)
-__device__ __forceinline__ void basis_bernstein(int idx, float x, float hs, float (&q)[3]) {
-    const int l = ilog2_dev(idx + 1);
-    const int off = idx + 1 - (1 << l);
-    const float c = __fmul_rn(__fadd_rn((float)off, 0.5f), __int_as_float((127 - l) << 23));
-    const float t = __fmul_rn(__fsub_rn(x, c), (float)(1 << l));
-    const float a = fabsf(t);
-    float b, g, k2;
-    if (a < 0.5f) {
-        b = (0.75f - t * t) * (4.0f / 3.0f);
-        g = -(8.0f / 3.0f) * t * hs;
-        k2 = -(4.0f / 3.0f) * hs * hs;
-    } else if (a < 1.5f) {
-        const float u = 1.5f - a;
-        b = u * u * (2.0f / 3.0f);
-        g = copysignf((4.0f / 3.0f) * u * hs, -t);
-        k2 = (2.0f / 3.0f) * hs * hs;
-    } else {
-        b = 0.0f;
-        g = 0.0f;
-        k2 = 0.0f;
-    }
-    q[0] = b - g + k2;
-    q[1] = b - k2;
-    q[2] = b + g + k2;
-}
-
-// adds one level (ancestor function indices ox, oy, oz; its 27 values y) to the cell's
-// Bernstein coefficients C[alpha][beta][gamma] (x, y, z), separably
-__device__ __forceinline__ void sign_level(const float (&y)[27], int ox, int oy, int oz, float qx, float qy,
-                                           float qz, float hs, float (&C)[27], float& mag) {
-    float X[3][3], Y[3][3], Z[3][3];
-#pragma unroll
-    for (int j = 0; j < 3; ++j) {
-        basis_bernstein(ox - 1 + j, qx, hs, X[j]);
-        basis_bernstein(oy - 1 + j, qy, hs, Y[j]);
-        basis_bernstein(oz - 1 + j, qz, hs, Z[j]);
-    }
-    float ab = 0.0f;
-#pragma unroll
-    for (int k = 0; k < 27; ++k) ab += fabsf(y[k]);
-    mag += ab;
-    // T1[a][j][k] = sum_i X[i][a] y[i][j][k]
-    float T1[27];
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-        for (int jk = 0; jk < 9; ++jk)
-            T1[a * 9 + jk] = fmaf(X[0][a], y[jk], fmaf(X[1][a], y[9 + jk], X[2][a] * y[18 + jk]));
-    // T2[a][b][k] = sum_j Y[j][b] T1[a][j][k]
-    float T2[27];
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-        for (int bb = 0; bb < 3; ++bb)
-#pragma unroll
-            for (int k = 0; k < 3; ++k)
-                T2[a * 9 + bb * 3 + k] = fmaf(Y[0][bb], T1[a * 9 + k],
-                                              fmaf(Y[1][bb], T1[a * 9 + 3 + k], Y[2][bb] * T1[a * 9 + 6 + k]));
-    // C[a][b][g] += sum_k Z[k][g] T2[a][b][k]
-#pragma unroll
-    for (int ab3 = 0; ab3 < 9; ++ab3)
-#pragma unroll
-        for (int gg = 0; gg < 3; ++gg)
-            C[ab3 * 3 + gg] += fmaf(Z[0][gg], T2[ab3 * 3], fmaf(Z[1][gg], T2[ab3 * 3 + 1], Z[2][gg] * T2[ab3 * 3 + 2]));
-}
-
 // value carried by a sub-node neighbour (na + virtual index) of group G: its root's octree
 // node for a root (it stands for that node), else nothing (x = 0 in subdivision space)
 __device__ __forceinline__ int sub_value_node(int v, int na, const int* G, const int* root_self) {

@@ -407,22 +407,67 @@ __device__ __forceinline__ void decode3s(int e, int depth, int& ix, int& iy, int
 }
 
 // Implicit value at a sample point: the 27 neighbour terms ((x * Fx) * Fy) * Fz of every
-// level of its chain (its depth-D node and that node's ancestors).  The coarser levels are
-// summed first, as soon as their systems are solved (k_point_values_coarse, beside the
-// depth-D CG; the partial sum is kept in `out`), then the depth-D terms are added
-// (k_point_values).  The iso-value is the FP64 mean of these float values.
+// level of its chain (its depth-D node and that node's ancestors).  The levels up to D-1
+// are summed first, as soon as their systems are solved, beside the depth-D CG: on the cell
+// of a depth-(D-1) node they form one tensor-product quadratic (k_point_poly: its 27
+// Bernstein coefficients, one thread per node), evaluated at each sample of the cell
+// (k_point_values_coarse; the partial sum is kept in `out`).  The depth-D terms are added
+// after the depth-D CG (k_point_values).  The iso-value is the FP64 mean of these float
+// values.
+__global__ void __launch_bounds__(kBlock) k_point_poly(const Counters* c, int depth, const float* ctr_x,
+                                                       const float* ctr_y, const float* ctr_z, const int* neigh,
+                                                       size_t stride, const int* parent, const int* enc,
+                                                       const float* x, float* coef, size_t cstride) {
+    const int d1 = depth - 1;
+    const int n = c->level_count[d1];
+    const int b = c->level_base[d1];
+    PSR_GRID_STRIDE(a, n) {
+        const int node = b + a;
+        const float qx = ctr_x[node], qy = ctr_y[node], qz = ctr_z[node];
+        float C[27], y[27], mag = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 27; ++k) C[k] = 0.0f;
+        for (int now = node; now >= 0; now = parent[now]) {
+            int ox, oy, oz;
+            decode3s(enc[now], depth, ox, oy, oz);
+            const int l = ilog2_dev(ox + 1);
+#pragma unroll
+            for (int k = 0; k < 27; ++k) {
+                const int v = neigh[(size_t)k * stride + now];
+                y[k] = (v >= 0) ? x[v] : 0.0f;
+            }
+            sign_level(y, ox, oy, oz, qx, qy, qz, __int_as_float((127 + l - depth) << 23), C, mag);   // h 2^l
+        }
+#pragma unroll
+        for (int k = 0; k < 27; ++k) coef[(size_t)k * cstride + a] = C[k];
+    }
+}
+
 __global__ void __launch_bounds__(kBlock) k_point_values_coarse(const Counters* c, int depth, const float* px,
                                                                 const float* py, const float* pz,
-                                                                const int* point2node, const int* neigh,
-                                                                size_t stride, const int* parent, const int* enc,
-                                                                const float* x, float* out) {
+                                                                const int* point2node, const int* parent,
+                                                                const float* ctr_x, const float* ctr_y,
+                                                                const float* ctr_z, const float* coef,
+                                                                size_t cstride, float* out) {
     const int n = c->n_points;
     const int bD = c->level_base[depth];
+    const int b1 = c->level_base[depth - 1];
+    const float inv2h = (float)(1 << (depth - 1));   // 1 / (2 h) of a depth-(D-1) cell
     PSR_GRID_STRIDE(i, n) {
-        const float qx = px[i], qy = py[i], qz = pz[i];
+        const int node = parent[bD + point2node[i]];
+        const int a = node - b1;
+        // position in the cell, u in [0, 1] per axis (cell from centre - h to centre + h)
+        const float hh = 0.5f / inv2h;
+        const float ux = (px[i] - (ctr_x[node] - hh)) * inv2h;
+        const float uy = (py[i] - (ctr_y[node] - hh)) * inv2h;
+        const float uz = (pz[i] - (ctr_z[node] - hh)) * inv2h;
+        const float wx[3] = {(1.0f - ux) * (1.0f - ux), 2.0f * ux * (1.0f - ux), ux * ux};
+        const float wy[3] = {(1.0f - uy) * (1.0f - uy), 2.0f * uy * (1.0f - uy), uy * uy};
+        const float wz[3] = {(1.0f - uz) * (1.0f - uz), 2.0f * uz * (1.0f - uz), uz * uz};
         float val = 0.0f;
-        for (int node = parent[bD + point2node[i]]; node != -1; node = parent[node])
-            val = level_terms(node, val, qx, qy, qz, depth, neigh, stride, enc, x);
+#pragma unroll
+        for (int k = 0; k < 27; ++k)
+            val = fmaf(wx[k / 9] * wy[(k / 3) % 3] * wz[k % 3], coef[(size_t)k * cstride + a], val);
         out[i] = val;
     }
 }
@@ -574,9 +619,13 @@ cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, 
     // solved, beside the depth-D CG
     if (ncl > 1) e = cudaStreamWaitEvent(ws.aux, ws.ev_join3, 0);
     if (e == cudaSuccess) {
-        k_point_values_coarse<<<ws.num_sms * 4, kBlock, 0, ws.aux>>>(ws.cnt, ws.depth, ws.px, ws.py, ws.pz,
-                                                                     ws.point2node, ws.neigh, (size_t)ws.cap.nodes,
-                                                                     ws.parent, ws.enc, ws.xsol, ws.point_val);
+        const size_t cstride = (size_t)ws.cap.dnodes / 8 + 64;
+        k_point_poly<<<ws.num_sms * 4, kBlock, 0, ws.aux>>>(ws.cnt, D, ws.ctr_x, ws.ctr_y, ws.ctr_z, ws.neigh,
+                                                            (size_t)ws.cap.nodes, ws.parent, ws.enc, ws.xsol,
+                                                            ws.pv_coef, cstride);
+        k_point_values_coarse<<<ws.num_sms * 4, kBlock, 0, ws.aux>>>(ws.cnt, D, ws.px, ws.py, ws.pz, ws.point2node,
+                                                                     ws.parent, ws.ctr_x, ws.ctr_y, ws.ctr_z,
+                                                                     ws.pv_coef, cstride, ws.point_val);
         e = cudaEventRecord(ws.ev_join, ws.aux);
     }
     if (e != cudaSuccess) return e;

@@ -102,6 +102,7 @@ struct Workspace {
     int* cg_blk;            // CG block table: 64 same-depth nodes per sibling group
     double* cg_partial;     // scratch: divergence chunk sums (float pairs, 8 bytes each)
     float* point_val;       // N
+    float* pv_coef;         // [27][cap.dnodes / 8 + 64]: per depth-(D-1) node, Bernstein coefficients
     double* iso_partial;
 
     // mesh geometry
