@@ -28,67 +28,76 @@ __device__ __forceinline__ float bspline32(float t) {
     return 0.0f;
 }
 
-// One warp per D-level node: lane k < 27 holds neighbour k's sample range, a warp scan
-// flattens the (neighbour, sample) pairs over the lanes, every lane accumulates its
-// samples' weighted normals and a butterfly sum combines the lanes (fixed order).
+// 8 lanes per D-level node (4 nodes per warp): the 27 neighbours' sample ranges are
+// flattened over the group's lanes (a group scan gives the range offsets), every lane
+// accumulates its samples' weighted normals and a butterfly over the group combines the
+// lanes (fixed order).
+constexpr int kVfLanes = 8;
+constexpr int kVfGroups = kBlock / kVfLanes;
 __global__ void __launch_bounds__(kBlock) k_vector_field(const Counters* c, int depth, const float* px, const float* py,
                                                          const float* pz, const float* nx, const float* ny,
                                                          const float* nz, const int* pidx, const int* pnum,
                                                          const float* cx, const float* cy, const float* cz,
                                                          const int* neigh, size_t stride, float* vx, float* vy,
                                                          float* vz) {
-    __shared__ int s_off[kBlock / 32][28];
-    __shared__ int s_base[kBlock / 32][27];
+    __shared__ int s_off[kVfGroups][28];
+    __shared__ int s_base[kVfGroups][27];
     const int md = c->level_count[depth];
     const int b = c->level_base[depth];
     const float s = (float)(1 << depth);
-    const int lane = lane_id();
-    const int wib = threadIdx.x >> 5;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int o = warp; o < md; o += nwarps) {
+    const int lane = threadIdx.x & (kVfLanes - 1);
+    const int gib = threadIdx.x / kVfLanes;
+    const unsigned gmask = 0xffu << (threadIdx.x & 24);   // the group's lanes in its warp
+    const int group = (blockIdx.x * blockDim.x + threadIdx.x) / kVfLanes;
+    const int ngroups = (gridDim.x * blockDim.x) / kVfLanes;
+    for (int o = group; o < md; o += ngroups) {
         const int i = b + o;
         const float ox = cx[i], oy = cy[i], oz = cz[i];
-        int cnt = 0, base = 0;
-        if (lane < 27) {
-            const int nb = neigh[(size_t)lane * stride + i];
-            if (nb >= 0) { base = pidx[nb]; cnt = pnum[nb]; }
-        }
-        int incl = cnt;
+        int running = 0;
 #pragma unroll
-        for (int q = 1; q < 32; q <<= 1) {
-            const int y = __shfl_up_sync(0xffffffffu, incl, q);
-            if (lane >= q) incl += y;
+        for (int r = 0; r < 4; ++r) {
+            const int k = lane + kVfLanes * r;
+            int cnt = 0, base = 0;
+            if (k < 27) {
+                const int nb = neigh[(size_t)k * stride + i];
+                if (nb >= 0) { base = pidx[nb]; cnt = pnum[nb]; }
+            }
+            int incl = cnt;
+#pragma unroll
+            for (int q = 1; q < kVfLanes; q <<= 1) {
+                const int y = __shfl_up_sync(gmask, incl, q, kVfLanes);
+                if (lane >= q) incl += y;
+            }
+            if (k < 27) {
+                s_off[gib][k] = running + incl - cnt;
+                s_base[gib][k] = base;
+            }
+            running += __shfl_sync(gmask, incl, kVfLanes - 1, kVfLanes);
         }
-        if (lane < 27) {
-            s_off[wib][lane] = incl - cnt;
-            s_base[wib][lane] = base;
-        }
-        if (lane == 26) s_off[wib][27] = incl;
-        const int total = __shfl_sync(0xffffffffu, incl, 26);
-        __syncwarp();
+        if (lane == 0) s_off[gib][27] = running;
+        __syncwarp(gmask);
         float ax = 0.f, ay = 0.f, az = 0.f;
         int k = 0;
-        for (int t = lane; t < total; t += 32) {
-            while (s_off[wib][k + 1] <= t) ++k;
-            const int p = s_base[wib][k] + (t - s_off[wib][k]);
+        for (int t = lane; t < running; t += kVfLanes) {
+            while (s_off[gib][k + 1] <= t) ++k;
+            const int p = s_base[gib][k] + (t - s_off[gib][k]);
             const float w = bspline32((px[p] - ox) * s) * bspline32((py[p] - oy) * s) * bspline32((pz[p] - oz) * s);
             ax = fmaf(w, nx[p], ax);
             ay = fmaf(w, ny[p], ay);
             az = fmaf(w, nz[p], az);
         }
 #pragma unroll
-        for (int q = 16; q > 0; q >>= 1) {
-            ax += __shfl_xor_sync(0xffffffffu, ax, q);
-            ay += __shfl_xor_sync(0xffffffffu, ay, q);
-            az += __shfl_xor_sync(0xffffffffu, az, q);
+        for (int q = kVfLanes / 2; q > 0; q >>= 1) {
+            ax += __shfl_xor_sync(gmask, ax, q);
+            ay += __shfl_xor_sync(gmask, ay, q);
+            az += __shfl_xor_sync(gmask, az, q);
         }
         if (lane == 0) {
             vx[o] = ax;
             vy[o] = ay;
             vz[o] = az;
         }
-        __syncwarp();
+        __syncwarp(gmask);
     }
 }
 
@@ -118,7 +127,39 @@ __device__ __forceinline__ FF div_terms(int l0, int l1, int step, int ox, int oy
     return acc;
 }
 
-// One warp per node for depths >= dsplit.  The (neighbour, leaf) pairs of the node are
+// Depth-D nodes: every neighbour holds exactly one depth-D leaf (itself), so a node's
+// divergence has at most 27 terms; one thread per node sums them in slot order.
+__global__ void __launch_bounds__(kBlock) k_div_leaf(const Counters* c, int depth, int res, const int* enc,
+                                                     const int* neigh, size_t stride, const float* vx,
+                                                     const float* vy, const float* vz, const float* dff,
+                                                     float* divg) {
+    const int bD = c->level_base[depth];
+    const int MD = c->level_count[depth];
+    PSR_GRID_STRIDE(o, MD) {
+        const int i = bD + o;
+        int ox, oy, oz;
+        decode3(enc[i], depth, ox, oy, oz);
+        FF acc = ff_zero();
+#pragma unroll 9
+        for (int k = 0; k < 27; ++k) {
+            const int nb = neigh[(size_t)k * stride + i];
+            if (nb < 0) continue;
+            int lx, ly, lz;
+            decode3(enc[nb], depth, lx, ly, lz);
+            const int l = nb - bD;
+            const float ux = dff[(size_t)ox + (size_t)res * lx];
+            const float uy = dff[(size_t)oy + (size_t)res * ly];
+            const float uz = dff[(size_t)oz + (size_t)res * lz];
+            float t = __fmul_rn(vx[l], ux);
+            t = fmaf(vy[l], uy, t);
+            t = fmaf(vz[l], uz, t);
+            acc = ff_add_float(acc, t);
+        }
+        divg[i] = ff_to_float(acc);
+    }
+}
+
+// One warp per node for depths dsplit .. D-1.  The (neighbour, leaf) pairs of the node are
 // flattened over the lanes: lane k < 27 holds neighbour k's leaf range, a warp scan gives
 // the range offsets, and term t belongs to the last neighbour whose offset is <= t.  A
 // depth-D node has at most 27 terms (one leaf per neighbour): one pass, 27 lanes busy.
@@ -130,8 +171,8 @@ __global__ void __launch_bounds__(kBlock) k_div_fine(const Counters* c, int dept
     __shared__ int s_off[kBlock / 32][33];
     __shared__ int s_base[kBlock / 32][32];
     const int b0 = c->level_base[dsplit];
-    const int M = c->n_nodes;
     const int bD = c->level_base[depth];
+    const int M = bD;   // depth-D nodes: k_div_leaf
     const int lane = lane_id();
     const int wib = threadIdx.x >> 5;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -297,6 +338,7 @@ cudaError_t field_build(Workspace& ws) {
     }
     k_div_fine<<<ws.num_sms * 8, kBlock, 0, s>>>(c, D, dsplit, ws.res, ws.enc, ws.didx, ws.dnum, ws.neigh, stride, vx,
                                                  vy, vz, ws.dff, ws.divg);
+    k_div_leaf<<<ws.num_sms * 8, kBlock, 0, s>>>(c, D, ws.res, ws.enc, ws.neigh, stride, vx, vy, vz, ws.dff, ws.divg);
     if (dsplit > 0) {
         e = cudaStreamWaitEvent(s, ws.ev_join, 0);
         if (e != cudaSuccess) return e;
