@@ -173,7 +173,8 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     ws.part_cap_t = 2 * cfg.max_triangles + 4096;
     long long max_scan = std::max({N + 1, nodes, (long long)cap.edges, (long long)cap.faces, (long long)cap.vertices,
                                    subd * 12, (long long)ws.part_cap_v, (long long)ws.part_cap_t,
-                                   256LL * ((N + kSortTile - 1) / kSortTile)});
+                                   256LL * ((N + kSortTile - 1) / kSortTile),
+                                   (1LL << (3 * kColourGridLevel)) + 1});   // colour cell table
     cap.scan_tiles = (int)((max_scan + kScanMinTile - 1) / kScanMinTile) + 1;
     const int sort_tiles = (int)((N + kSortTile - 1) / kSortTile) + 1;
     const int D = cfg.max_depth;

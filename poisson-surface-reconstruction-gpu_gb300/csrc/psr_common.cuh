@@ -37,6 +37,7 @@ struct Counters {
     int n_sub_vertices, n_sub_edges, n_sub_cross, n_sub_tri;
     int n_mesh_vertices, n_mesh_triangles;
     int n_colour_far;             // mesh vertices whose 4 nearest samples need the wide search
+    int n_colour_cells;           // entries of the colour cell table
     int scan_total;               // scratch total written by scans
     int scan_total_aux;           // the same for scans issued on the geometry stream
     unsigned error;

@@ -27,21 +27,25 @@ __device__ __forceinline__ unsigned point_cell(int i, int depth, int g, int bD, 
     return (unsigned)key[bD + point2node[i]] >> (3 * (depth - g));
 }
 
-// cell_start[m] = first sorted sample whose cell code is >= m, for m in [0, 8^g]
-// (binary search over the Morton-sorted samples; one thread per cell)
-__global__ void __launch_bounds__(kBlock) k_cell_starts(const Counters* c, int depth, int g, const int* key,
-                                                        const int* point2node, int* cell_start) {
+// cell_start[m] = first sorted sample whose cell code is >= m, for m in [0, 8^g]: the
+// exclusive prefix sum of the samples per cell.  k_cell_count counts them (the table
+// starts zeroed; the samples are Morton-sorted, so the last sample of a cell's run adds
+// the run's length), then one scan turns the counts into starts in place.
+__global__ void __launch_bounds__(kBlock) k_cell_count(Counters* c, int depth, int g, const int* key,
+                                                       const int* point2node, int* count) {
     const int n = c->n_points;
     const int bD = c->level_base[depth];
-    const int ncell = 1 << (3 * g);
-    PSR_GRID_STRIDE(m, ncell + 1) {
-        int lo = 0, hi = n;   // first i with cell(i) >= m
+    if (blockIdx.x == 0 && threadIdx.x == 0) c->n_colour_cells = (1 << (3 * g)) + 1;
+    PSR_GRID_STRIDE(i, n) {
+        const unsigned m = point_cell(i, depth, g, bD, key, point2node);
+        if (i + 1 < n && point_cell(i + 1, depth, g, bD, key, point2node) == m) continue;
+        int lo = 0, hi = i;   // first sample of the run ending at i
         while (lo < hi) {
             const int mid = (lo + hi) >> 1;
-            if ((int)point_cell(mid, depth, g, bD, key, point2node) < m) lo = mid + 1;
+            if (point_cell(mid, depth, g, bD, key, point2node) < m) lo = mid + 1;
             else hi = mid;
         }
-        cell_start[m] = lo;
+        count[m] = i + 1 - lo;
     }
 }
 
@@ -410,8 +414,13 @@ cudaError_t transfer_prepare(Workspace& ws, int with_colour) {
     if (!with_colour) return cudaSuccess;
     const int D = ws.depth;
     const int g = D < kColourGridLevel ? D : kColourGridLevel;
-    k_cell_starts<<<ws.num_sms * 8, kBlock, 0, ws.stream>>>(ws.cnt, D, g, ws.key, ws.point2node, ws.cell_start);
-    return cudaGetLastError();
+    cudaError_t e = cudaMemsetAsync(ws.cell_start, 0, sizeof(int) * (((size_t)1 << (3 * g)) + 1), ws.stream);
+    if (e != cudaSuccess) return e;
+    k_cell_count<<<ws.num_sms * 4, kBlock, 0, ws.stream>>>(ws.cnt, D, g, ws.key, ws.point2node, ws.cell_start);
+    unsigned* table = reinterpret_cast<unsigned*>(ws.cell_start);
+    Counters* c = ws.cnt;
+    return launch_scan(LoadArray{table}, StoreExclusive{table}, &c->n_colour_cells, 0, ws.scan,
+                       (unsigned*)&c->scan_total_aux, &c->error, ws.stream, ScanCount{}, 2);
 }
 
 cudaError_t transfer_build(Workspace& ws, int with_colour, int with_normals) {
