@@ -346,6 +346,13 @@ __global__ void __launch_bounds__(kFarThreads) k_colour(const Counters* c, int g
                 const int a = cx - R + ta, b = cy - R + tb, z = cz - R + tz;
                 if (a < 0 || a >= G || b < 0 || b >= G || z < 0 || z >= G) continue;
                 if (max(abs(a - cx), max(abs(b - cy), abs(z - cz))) <= 1) continue;
+                // a cell whose box is farther than the 4th nearest holds no closer sample
+                // (rounding is monotone: a sample's float distance is at least the box's)
+                const float gx = fmaxf(fmaxf(__fsub_rn(a * w, qx), __fsub_rn(qx, (a + 1) * w)), 0.0f);
+                const float gy = fmaxf(fmaxf(__fsub_rn(b * w, qy), __fsub_rn(qy, (b + 1) * w)), 0.0f);
+                const float gz = fmaxf(fmaxf(__fsub_rn(z * w, qz), __fsub_rn(qz, (z + 1) * w)), 0.0f);
+                const float mind2 = __fadd_rn(__fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy)), __fmul_rn(gz, gz));
+                if (mind2 > md[3] * 1.0001f) continue;
                 const unsigned m = morton3(a, b, z, g);
                 const int s0 = cell_start[(size_t)m << shift], s1 = cell_start[(size_t)(m + 1) << shift];
                 for (int j = s0; j < s1; ++j) knn_visit(qx, qy, qz, px, py, pz, j, bd, bi);
