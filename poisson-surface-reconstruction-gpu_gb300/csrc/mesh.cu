@@ -1687,7 +1687,7 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
                                         ws.neigh, stride, ws.first_child, ws.parent, mb.ov_group, mb.ov_sub, ws.enc,
                                         ws.xsol, ws.root_poly, ws.cap_poly, A},
                            SubLevelStore{c, d, D, A, err}, &c->sub_cand[d], 0, ws.scan, total, err, s, ScanCount{},
-                           2);
+                           1);
         if (e != cudaSuccess) return e;
     }
     // the live depth-D cells carry every record from here on, indexed by their live index

@@ -595,7 +595,7 @@ cudaError_t octree_build(Workspace& ws) {
     k_point2node<<<gp, kBlock, 0, s>>>(c, ws.puid, ws.uslot, ws.point2node);
     // levels D .. dfuse+1 level by level across the GPU, the small levels near the root in
     // one CTA
-    const int dfuse = D >= 9 ? D - 3 : D - 2;
+    const int dfuse = D - 3;
     for (int d = D; d >= 1 && d > dfuse; --d) {
         const int gg = grid_for(ws, ws.cap.dnodes / 8 + 1);
         k_group_aggregate<<<gg, kBlock, 0, s>>>(c, d, D, ws.tkey, ws.tpidx, ws.tpnum, ws.tdidx, ws.tdnum, ws.gkey,
