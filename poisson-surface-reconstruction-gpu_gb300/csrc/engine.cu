@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <new>
@@ -242,7 +243,13 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     A.add(ws.sub_root_depth, (size_t)nodes);
     A.add(ws.root_group, (size_t)nodes);
     A.add(ws.root_self, (size_t)nodes);
+    // roots beyond this capacity take the walk over their octree chain in the subdivision
+    // scan itself; PSR_ROOT_POLY_CAPACITY lowers it (that path gives the same mesh)
     ws.cap_poly = (int)std::max<long long>(65536, nodes / 16);
+    if (const char* ev = getenv("PSR_ROOT_POLY_CAPACITY")) {
+        const long long v = atoll(ev);
+        if (v > 0 && v < ws.cap_poly) ws.cap_poly = (int)v;
+    }
     A.add(ws.root_poly, 28 * (size_t)ws.cap_poly);
     A.add(ws.c_vnode, (size_t)subn); A.add(ws.c_key, (size_t)subn); A.add(ws.c_group, (size_t)subn);
     A.add(ws.c_parent, (size_t)subn); A.add(ws.c_jump, (size_t)subn); A.add(ws.c_depth, (size_t)subn);

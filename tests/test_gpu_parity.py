@@ -232,3 +232,21 @@ def test_deterministic(recon):
     b = recon.SolvePoissionReconstructionMesh(p, nr, rgb, depth=D)
     np.testing.assert_array_equal(a.vertices, b.vertices)
     np.testing.assert_array_equal(a.triangles, b.triangles)
+
+
+def test_root_polynomial_fallback_same_mesh(monkeypatch):
+    # subdivision roots beyond the root-polynomial capacity sum their octree chain in the
+    # level scan itself: with a capacity of one root that path runs for nearly every root
+    import psr
+    p, nr, rgb, D = syn.workload("mix", cloud=0, n=25000, colour=True)
+    caps = dict(max_depth=7, max_points=30000, compute_colors=True, compute_normals=True)
+    with psr.PoissonReconstruction(**caps) as r:
+        a = r.SolvePoissionReconstructionMesh(p, nr, rgb, depth=7)
+        roots = r.stats().subdivision_roots
+    monkeypatch.setenv("PSR_ROOT_POLY_CAPACITY", "1")
+    with psr.PoissonReconstruction(**caps) as r:
+        b = r.SolvePoissionReconstructionMesh(p, nr, rgb, depth=7)
+    assert roots > 1
+    np.testing.assert_array_equal(a.vertices, b.vertices)
+    np.testing.assert_array_equal(a.triangles, b.triangles)
+    np.testing.assert_array_equal(a.colors, b.colors)
