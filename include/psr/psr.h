@@ -148,6 +148,17 @@ psr_status psr_wait(psr_handle* h);
  * and rgb (3 * count bytes, round(255 * ColorAndTime.xyz) clamped) unless rgb is NULL.
  * Replaces getCoordinateAndNormalKernel (mesh/BuildOctree.cu:135-143); enqueued on
  * `stream` (a cudaStream_t or NULL), no host wait. */
+/* Normals of an unoriented cloud (replaces the PCL step the reference runs before the path,
+ * CalculatePointCloudNormal, mesh/PoissonReconstruction.cpp:137-161: NormalEstimationOMP,
+ * k = 10 nearest neighbours, viewpoint (0, 0, 0)): for every point the eigenvector of the
+ * smallest eigenvalue of its 10 nearest samples' covariance (itself included), flipped
+ * towards `viewpoint` (NULL: the origin); NaN when the cloud has fewer than 3 points.
+ * xyz and normals are count x 3 floats, both on the device or both on the host
+ * (`location`); count <= max_points.  Blocks until the normals are written; uses the
+ * handle's scratch (no reconstruction in flight on the handle). */
+psr_status psr_estimate_normals(psr_handle* h, const float* xyz, int count, psr_location location, float* normals,
+                                const float* viewpoint, void* stream);
+
 psr_status psr_surfels_to_points(const void* surfels, int count, float* xyz, float* normals, uint8_t* rgb,
                                  void* stream);
 

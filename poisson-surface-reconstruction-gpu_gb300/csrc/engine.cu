@@ -18,6 +18,7 @@ cudaError_t upload_tables_field();
 cudaError_t upload_tables_solver();
 cudaError_t upload_tables_mesh();
 cudaError_t upload_tables_transfer();
+cudaError_t normals_build(Workspace& ws, const float* xyz, int n, float* out, float vpx, float vpy, float vpz);
 void build_dff_table(int depth, std::vector<double>& dff);
 void build_stencil(int depth, std::vector<float>& st, double eps);
 }  // namespace psr
@@ -607,6 +608,43 @@ psr_status psr_wait(psr_handle* h) {
         return cuda_fail(h, q, "reconstruct");
     }
     return complete_impl(h);
+}
+
+psr_status psr_estimate_normals(psr_handle* h, const float* xyz, int count, psr_location location, float* normals,
+                                const float* viewpoint, void* stream) {
+    if (!h) return PSR_INVALID_INPUT;
+    if (count < 0 || (count > 0 && (!xyz || !normals))) return fail(h, PSR_INVALID_INPUT, "bad arguments");
+    if (h->pending) return fail(h, PSR_INVALID_INPUT, "a reconstruction is in flight on this handle");
+    if (count > h->ws.cap.points) return fail(h, PSR_OUT_OF_CAPACITY, "more points than max_points");
+    // the 10 neighbours of every point are kept in the node neighbour table's storage
+    if ((size_t)27 * h->ws.cap.nodes < (size_t)10 * count)
+        return fail(h, PSR_OUT_OF_CAPACITY, "max_nodes too small for the neighbour lists");
+    if (count == 0) return PSR_OK;
+    Workspace& ws = h->ws;
+    cudaStream_t s = stream ? (cudaStream_t)stream : h->own_stream;
+    ws.stream = s;
+    h->have_result = false;   // the stage reuses the reconstruction's scratch
+    const float vp[3] = {viewpoint ? viewpoint[0] : 0.0f, viewpoint ? viewpoint[1] : 0.0f,
+                         viewpoint ? viewpoint[2] : 0.0f};
+    const size_t bytes = 3 * sizeof(float) * (size_t)count;
+    const float* in = xyz;
+    float* out = normals;
+    cudaError_t e = cudaSuccess;
+    if (location == PSR_HOST) {
+        e = cudaMemcpyAsync(ws.in_xyz, xyz, bytes, cudaMemcpyHostToDevice, s);
+        in = ws.in_xyz;
+        out = ws.in_nrm;
+    }
+    if (e == cudaSuccess) e = normals_build(ws, in, count, out, vp[0], vp[1], vp[2]);
+    if (e == cudaSuccess && location == PSR_HOST) e = cudaMemcpyAsync(normals, out, bytes, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ws.cnt_host, ws.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(h, e, "normal estimation");
+    const unsigned err = ws.cnt_host->error;
+    if (err & kErrInvalid) return fail(h, PSR_INVALID_INPUT, "non-finite input coordinates");
+    if (err & kErrCapacity) return fail(h, PSR_OUT_OF_CAPACITY, "a device count exceeded its capacity");
+    if (err & kErrSpinTimeout) return fail(h, PSR_DEVICE_TIMEOUT, "a bounded device wait gave up");
+    return PSR_OK;
 }
 
 psr_status psr_memory_bytes(const psr_handle* h, size_t* bytes) {

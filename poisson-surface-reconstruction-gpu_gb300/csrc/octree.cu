@@ -562,6 +562,25 @@ __global__ void k_root_neighbours(int* neigh, size_t stride) {
     if (k < 27) neigh[(size_t)k * stride] = (k == 13) ? 0 : -1;
 }
 
+// points -> Morton codes of the reference's normalised coordinates at `depth`, sorted with
+// their input indices (the octree's first steps; the normal estimation stage uses them on
+// their own).  n_points and the bounding-box seeds must be set.
+cudaError_t encode_sort_points(Workspace& ws, const float* xyz, int depth, const unsigned** scode,
+                               const unsigned** sidx) {
+    cudaStream_t s = ws.stream;
+    Counters* c = ws.cnt;
+    const int gp = grid_for(ws, ws.cap.points);
+    k_bbox<<<gp, kBlock, 0, s>>>(xyz, xyz, c);
+    k_bbox_finalize<<<1, 1, 0, s>>>(c, 1.25f);
+    k_encode<<<gp, kBlock, 0, s>>>(xyz, c, depth, ws.code, ws.sidx);
+    bool alt = false;
+    cudaError_t e = radix_sort_pairs(ws.code, ws.sidx, &c->n_points, 3 * depth, ws.sort, &c->error, s, &alt);
+    if (e != cudaSuccess) return e;
+    *scode = alt ? ws.sort.keys_alt : ws.code;
+    *sidx = alt ? ws.sort.vals_alt : ws.sidx;
+    return cudaGetLastError();
+}
+
 cudaError_t octree_build(Workspace& ws) {
     cudaStream_t s = ws.stream;
     const int D = ws.depth;

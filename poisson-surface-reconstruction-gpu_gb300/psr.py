@@ -22,7 +22,7 @@ PSR_HOST, PSR_DEVICE = 0, 1
 # every function declared in include/psr/psr.h
 EXPORTED = ["psr_config_default", "psr_create", "psr_destroy", "psr_reconstruct", "psr_submit", "psr_poll",
             "psr_wait", "psr_memory_bytes", "psr_get_stats", "psr_debug_array", "psr_status_string",
-            "psr_last_error", "psr_surfels_to_points", "psr_morton_sort_noalloc"]
+            "psr_last_error", "psr_surfels_to_points", "psr_morton_sort_noalloc", "psr_estimate_normals"]
 
 
 class PsrConfig(ctypes.Structure):
@@ -86,6 +86,8 @@ def load_library(path=None):
     L.psr_memory_bytes.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t)]
     L.psr_surfels_to_points.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_void_p]
+    L.psr_estimate_normals.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                       ctypes.c_void_p, ctypes.c_void_p]
     L.psr_get_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(PsrStats)]
     L.psr_debug_array.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_size_t,
                                   ctypes.POINTER(ctypes.c_size_t)]
@@ -250,6 +252,26 @@ class PoissonReconstruction:
         self._pend = None
         if st != PSR_OK:
             raise self._error(st, "psr_wait")
+
+    def CalculatePointCloudNormal(self, xyz, viewpoint=(0.0, 0.0, 0.0)):
+        """Normals of an unoriented cloud (float32 N x 3, host): the smallest-eigenvalue
+        eigenvector of each point's 10 nearest neighbours' covariance, flipped towards
+        `viewpoint` (mesh/PoissonReconstruction.cpp:137-161).  Returns float32 N x 3."""
+        xyz = np.ascontiguousarray(xyz, np.float32).reshape(-1, 3)
+        out = np.empty_like(xyz)
+        vp = np.asarray(viewpoint, np.float32)
+        st = self._lib.psr_estimate_normals(self._h, xyz.ctypes.data, xyz.shape[0], PSR_HOST, out.ctypes.data,
+                                            vp.ctypes.data, None)
+        if st != PSR_OK:
+            raise self._error(st, "psr_estimate_normals")
+        return out
+
+    def estimate_normals_device(self, xyz_ptr, n, out_ptr, viewpoint=(0.0, 0.0, 0.0), stream=None):
+        """The same on device buffers (n x 3 floats each); blocks until written."""
+        vp = np.asarray(viewpoint, np.float32)
+        st = self._lib.psr_estimate_normals(self._h, xyz_ptr, int(n), PSR_DEVICE, out_ptr, vp.ctypes.data, stream)
+        if st != PSR_OK:
+            raise self._error(st, "psr_estimate_normals")
 
     def memory_bytes(self):
         b = ctypes.c_size_t(0)
