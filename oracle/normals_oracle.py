@@ -4,7 +4,8 @@ product path imports it).
 The reference estimates normals of unoriented clouds with PCL before the path
 (mesh/PoissonReconstruction.cpp:137-161, CalculatePointCloudNormal):
 pcl::NormalEstimationOMP with a kd-tree, setKSearch(10), the default viewpoint (0, 0, 0).
-PCL is a third-party dependency absent from the reference tree; its published algorithm
+PCL (1.12.1 in the reference's build notes, README.md:23) is a third-party dependency
+absent from the reference tree; its published algorithm
 (pcl::computePointNormal / flipNormalTowardsViewpoint) is restated here in FP64:
 
 * the k nearest samples of a point, the point itself included;
