@@ -57,6 +57,13 @@ typedef struct psr_config {
                                   second stream beside the solve (lower latency of one call);
                                   0: one chain (more throughput when many handles share the
                                   GPU, as in the served form) */
+    int weld_vertices;         /* 1: vertices with bit-identical coordinates become one (the
+                                  reference emits the vertices on the boundary of every
+                                  subdivided region once per region,
+                                  mesh/ComputeTriangleIndices.cu:1247-1282); representatives
+                                  keep their order, triangles are renumbered, colours and
+                                  normals come from the welded mesh.  0 (default): as the
+                                  reference */
 } psr_config;
 
 /* Oriented input cloud (the fields of DepthSurfel, base/CommonTypes.h:113-118, as SoA). */

@@ -17,7 +17,7 @@ CSRC = PKG / "csrc"
 OUT = PKG / "_build"
 LIB = PKG / "libpsr.so"
 
-CUDA_SOURCES = ["primitives.cu", "octree.cu", "field.cu", "solver.cu", "mesh.cu", "transfer.cu", "engine.cu", "surfel.cu", "noalloc.cu", "normals.cu"]
+CUDA_SOURCES = ["primitives.cu", "octree.cu", "field.cu", "solver.cu", "mesh.cu", "transfer.cu", "engine.cu", "surfel.cu", "noalloc.cu", "normals.cu", "weld.cu"]
 CXX_SOURCES = ["tables.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

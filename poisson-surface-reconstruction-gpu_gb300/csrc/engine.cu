@@ -19,6 +19,7 @@ cudaError_t upload_tables_solver();
 cudaError_t upload_tables_mesh();
 cudaError_t upload_tables_transfer();
 cudaError_t normals_build(Workspace& ws, const float* xyz, int n, float* out, float vpx, float vpy, float vpz);
+cudaError_t weld_build(Workspace& ws);
 void build_dff_table(int depth, std::vector<double>& dff);
 void build_stencil(int depth, std::vector<float>& st, double eps);
 }  // namespace psr
@@ -112,6 +113,7 @@ psr_status psr_config_default(psr_config* c) {
     c->concurrent_stages = 1;
     c->compute_colors = 0;
     c->compute_normals = 0;
+    c->weld_vertices = 0;
     c->device = 0;
     return PSR_OK;
 }
@@ -275,6 +277,15 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     A.add(ws.vcount, (size_t)cap.mesh_vertices);
     A.add(ws.cell_start, ((size_t)1 << (3 * kColourGridLevel)) + 16);
     A.add(ws.colour_far, (size_t)cap.mesh_vertices);
+    if (cfg.weld_vertices) {
+        size_t slots = 1;
+        while (slots < 2 * (size_t)cap.mesh_vertices) slots <<= 1;
+        ws.weld_mask = (unsigned)(slots - 1);
+        A.add(ws.weld_table, slots);
+        A.add(ws.weld_slot, (size_t)cap.mesh_vertices);
+        A.add(ws.weld_newid, (size_t)cap.mesh_vertices);
+        A.add(ws.weld_v, 3 * (size_t)cap.mesh_vertices);
+    }
     A.add(ws.part_v, 3 * (size_t)ws.part_cap_v);
     A.add(ws.part_t, 3 * (size_t)ws.part_cap_t);
     ws.mb.max_groups = (int)nodes;
@@ -451,6 +462,7 @@ static psr_status submit_impl(psr_handle* h, const psr_points* pts, const psr_op
         if (q == cudaSuccess) q = cudaEventRecordWithFlags(h->ev[3], qs, cudaEventRecordExternal);
         if (q == cudaSuccess && overlap) q = cudaStreamWaitEvent(qs, ws.ev_join2, 0);
         if (q == cudaSuccess) q = mesh_build(ws);
+        if (q == cudaSuccess) q = weld_build(ws);
         if (q == cudaSuccess) q = cudaEventRecordWithFlags(h->ev[4], qs, cudaEventRecordExternal);
         if (q == cudaSuccess) q = transfer_build(ws, want_colour, want_normals);
         if (q == cudaSuccess) q = cudaEventRecordWithFlags(h->ev[5], qs, cudaEventRecordExternal);

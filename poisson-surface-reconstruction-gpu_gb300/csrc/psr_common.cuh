@@ -38,6 +38,7 @@ struct Counters {
     int n_mesh_vertices, n_mesh_triangles;
     int n_colour_far;             // mesh vertices whose 4 nearest samples need the wide search
     int n_colour_cells;           // entries of the colour cell table
+    int n_weld;                   // mesh vertices left by welding
     int scan_total;               // scratch total written by scans
     int scan_total_aux;           // the same for scans issued on the geometry stream
     unsigned error;

@@ -154,6 +154,12 @@ struct Workspace {
     int* vcount;            // per output vertex triangle count
     int* cell_start;        // sample grid for the colour search
     int* colour_far;        // mesh vertices left to the wide colour search
+    // vertex welding (allocated only when the handle welds)
+    int* weld_table = nullptr;   // hash slots: a vertex of the class, then its smallest index
+    unsigned weld_mask = 0;      // slots - 1 (a power of two >= 2 x mesh vertex capacity)
+    int* weld_slot = nullptr;    // slot of every vertex's class
+    int* weld_newid = nullptr;   // welded number of every representative
+    float* weld_v = nullptr;     // compacted positions
 
     // staging for the two-phase insertion of each mesh part
     float* part_v;          // 3 x cap

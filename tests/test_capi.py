@@ -48,12 +48,34 @@ def test_config_defaults_without_gpu(lib):
     assert lib.psr_status_string(1) == b"out of capacity"
 
 
-def test_struct_layouts_match_header():
+def test_struct_layouts_match_header(tmp_path):
+    """Every ctypes mirror has the size and field offsets the C compiler gives the header."""
+    import shutil
+    import subprocess
     import psr
-    # psr_config: 14 x 4-byte fields
-    assert ctypes.sizeof(psr.PsrConfig) == 56
+    assert ctypes.sizeof(psr.PsrConfig) == 15 * 4
     assert ctypes.sizeof(psr.PsrPoints) == 32
     assert ctypes.sizeof(psr.PsrOptions) == 8
+    if not shutil.which("gcc"):
+        pytest.skip("no gcc")
+    mirrors = {"psr_config": psr.PsrConfig, "psr_points": psr.PsrPoints, "psr_options": psr.PsrOptions,
+               "psr_mesh": psr.PsrMesh, "psr_stats": psr.PsrStats}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "psr/psr.h"', "int main(void) {"]
+    for cname, py in mirrors.items():
+        lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
+        for f in py._fields_:
+            lines.append(f'printf("{cname}.{f[0]} %zu\\n", offsetof({cname}, {f[0]}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    r = subprocess.run(["gcc", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = dict(l.split() for l in subprocess.run([str(exe)], capture_output=True, text=True).stdout.splitlines())
+    for cname, py in mirrors.items():
+        assert int(got[cname]) == ctypes.sizeof(py), cname
+        for f in py._fields_:
+            assert int(got[f"{cname}.{f[0]}"]) == getattr(py, f[0]).offset, (cname, f[0])
 
 
 def test_cpp_shim_compiles(tmp_path):
