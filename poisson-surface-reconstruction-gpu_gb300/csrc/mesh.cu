@@ -786,7 +786,7 @@ __device__ __forceinline__ void add_subdivided(const float* P, size_t pstride, u
     blossom3((float)i3[2] * inv, (float)(i3[2] + 1) * inv, Mz);
     float p[27];
 #pragma unroll
-    for (int k = 0; k < 27; ++k) p[k] = P[(size_t)k * pstride];
+    for (int k = 0; k < 27; ++k) p[k] = __ldg(P + (size_t)k * pstride);   // written by an earlier launch
     float T1[27], T2[27];
 #pragma unroll
     for (int a = 0; a < 3; ++a)
@@ -969,7 +969,9 @@ struct SubLevelLoad {
         // nothing else.
         const bool interior = ok[0][0] && ok[0][2] && ok[1][0] && ok[1][2] && ok[2][0] && ok[2][2];
         // values of the own level's neighbours, read as each neighbour is found: below its
-        // root only octree neighbours carry one (deeper subdivision nodes are never roots)
+        // root only octree neighbours carry one (deeper subdivision nodes are never roots).
+        // Every array read in the loop is written by earlier launches only: read-only loads
+        // let the 27 look-up chains overlap instead of waiting behind each A.neigh store
         float y[27];
 #pragma unroll
         for (int kk = 0; kk < 27; ++kk) y[kk] = 0.0f;
@@ -985,18 +987,18 @@ struct SubLevelLoad {
                 } else {
                     int lp, lc;
                     nb_lut(son, kk, lp, lc);
-                    const int np = (pslot < 0) ? ((pa >= 0) ? neigh[(size_t)lp * stride + pa] : -1)
-                                               : A.neigh[(size_t)lp * A.cstride + pslot];
+                    const int np = (pslot < 0) ? ((pa >= 0) ? __ldg(neigh + (size_t)lp * stride + pa) : -1)
+                                               : __ldg(A.neigh + (size_t)lp * A.cstride + pslot);
                     v = -1;
                     if (np != -1) {
                         if (np < na) {
-                            if (ov_group[(size_t)lc * stride + np] == g) {
+                            if (__ldg(ov_group + (size_t)lc * stride + np) == g) {
                                 // redirected child pointer of this group's root
-                                v = na + G[3] + ov_sub[(size_t)lc * stride + np];
+                                v = na + G[3] + __ldg(ov_sub + (size_t)lc * stride + np);
                             } else {
-                                const int fc = first_child[np];
+                                const int fc = __ldg(first_child + np);
                                 v = (fc == -1) ? -1 : fc + lc;
-                                if (v >= 0 && d < depth && first_child[v] != -1) deeper = true;
+                                if (v >= 0 && d < depth && __ldg(first_child + v) != -1) deeper = true;
                             }
                         } else {
                             // a sub node of depth d - 1 in this group: its children are at 8 x
@@ -1009,13 +1011,13 @@ struct SubLevelLoad {
                     if (v >= 0 && (v < na || at_root_depth)) contrib = 1;
                 }
                 A.neigh[(size_t)kk * A.cstride + slot] = v;
-                if (v >= 0 && v < na && !at_root_depth) y[kk] = x[v];
+                if (v >= 0 && v < na && !at_root_depth) y[kk] = __ldg(x + v);
             }
         }
         const int prec = (pslot >= 0) ? pslot : -2 - pa;
         // nearest contributing node on the path to the root (itself when it contributes;
         // roots always do): lets the value chains skip non-contributing levels in one hop
-        const int jump = contrib ? slot : ((pslot >= 0) ? A.jump[pslot] : slot);
+        const int jump = contrib ? slot : ((pslot >= 0) ? __ldg(A.jump + pslot) : slot);
         // Bernstein coefficients of the levels up to d on the node's cell
         float C[27], mag;
         if (at_root_depth) {
@@ -1026,7 +1028,7 @@ struct SubLevelLoad {
 #pragma unroll
             for (int kk = 0; kk < 27; ++kk) C[kk] = 0.0f;
             add_subdivided(A.poly + pl, (size_t)A.cap_live, (unsigned)(i & 7), 1, C);
-            mag = A.poly[(size_t)27 * A.cap_live + pl];
+            mag = __ldg(A.poly + (size_t)27 * A.cap_live + pl);
             if (contrib) {   // its own level (octree neighbours; never for an interior node)
                 const float sc = (float)(1 << d);
                 const int base = (1 << d) - 1;
@@ -1047,7 +1049,7 @@ struct SubLevelLoad {
         for (int kk = 0; kk < 27; ++kk) stash[kk * kBlock + threadIdx.x] = C[kk];
         stash[27 * kBlock + threadIdx.x] = mag;
         const unsigned touch = at_root_depth ? 0x3fu
-                                             : child_touch(A.touch[c->sub_lbase[d - 1] + (i >> 3)], i & 7);
+                                             : child_touch(__ldg(A.touch + c->sub_lbase[d - 1] + (i >> 3)), i & 7);
         stash[28 * kBlock + threadIdx.x] = __uint_as_float(touch);
         stash[29 * kBlock + threadIdx.x] = __int_as_float(vnode);
         if (interior) {

@@ -430,18 +430,12 @@ __global__ void __launch_bounds__(kLevelBlock) k_neighbours_block(const Counters
             const int i = b + li;
             const int son = (key[i] >> (3 * (depth - d))) & 7;
             const int pa = parent[i];
+            // every read before the first store: the look-ups overlap
+            int v[27];
+            child_neighbours(son, [&](int j) { return neigh[(size_t)j * stride + pa]; },
+                             [&](int n) { return first_child[n]; }, v);
 #pragma unroll
-            for (int k = 0; k < 27; ++k) {
-                int lp, lc;
-                nb_lut(son, k, lp, lc);
-                const int np = neigh[(size_t)lp * stride + pa];
-                int v = -1;
-                if (np != -1) {
-                    const int fc = first_child[np];
-                    v = (fc == -1) ? -1 : fc + lc;
-                }
-                neigh[(size_t)k * stride + i] = v;
-            }
+            for (int k = 0; k < 27; ++k) neigh[(size_t)k * stride + i] = v[k];
         }
         __syncthreads();
     }
@@ -542,18 +536,11 @@ __global__ void __launch_bounds__(kBlock) k_neighbours(const Counters* c, int d,
         const int i = b + li;
         const int son = (key[i] >> (3 * (depth - d))) & 7;
         const int pa = parent[i];
+        int v[27];
+        child_neighbours(son, [&](int j) { return neigh[(size_t)j * stride + pa]; },
+                         [&](int n) { return first_child[n]; }, v);
 #pragma unroll
-        for (int k = 0; k < 27; ++k) {
-            int lp, lc;
-            nb_lut(son, k, lp, lc);
-            int np = neigh[(size_t)lp * stride + pa];
-            int v = -1;
-            if (np != -1) {
-                int fc = first_child[np];
-                v = (fc == -1) ? -1 : fc + lc;
-            }
-            neigh[(size_t)k * stride + i] = v;
-        }
+        for (int k = 0; k < 27; ++k) neigh[(size_t)k * stride + i] = v[k];
     }
 }
 

@@ -117,6 +117,56 @@ __device__ __forceinline__ void nb_lut(int son, int k, int& lp, int& lc) {
     lc = 4 * ((qx + 2) & 1) + 2 * ((qy + 2) & 1) + ((qz + 2) & 1);
 }
 
+// The 27 same-depth neighbours of child `son` (x = bit 2) of a node, the child of the same
+// slot order as nb_lut: per axis they lie in two of the parent's neighbours (the parent's -1
+// and 0 for a lower child, 0 and +1 for an upper one), so 8 parent-row reads and 8
+// first-child reads, all independent, give the 27 (children of a missing neighbour, or of a
+// childless one, are -1).  `row(j)` reads entry j (0..26) of the parent's neighbour row;
+// `first(n)` reads first_child[n].  The picks below use compile-time indices only.
+template <class Row, class First>
+__device__ __forceinline__ void child_neighbours(int son, Row row, First first, int (&v)[27]) {
+    const int sx = (son >> 2) & 1, sy = (son >> 1) & 1, sz = son & 1;
+    int F[2][2][2];
+#pragma unroll
+    for (int jx = 0; jx < 2; ++jx)
+#pragma unroll
+        for (int jy = 0; jy < 2; ++jy)
+#pragma unroll
+            for (int jz = 0; jz < 2; ++jz) F[jx][jy][jz] = row(9 * (sx + jx) + 3 * (sy + jy) + (sz + jz));
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        int& f = F[j >> 2][(j >> 1) & 1][j & 1];
+        f = (f == -1) ? -1 : first(f);
+    }
+    // offset d per axis (0, 1, 2 for -1, 0, +1): parent column 0, 1 - s, 1
+    int Gx[3][2][2];
+#pragma unroll
+    for (int jy = 0; jy < 2; ++jy)
+#pragma unroll
+        for (int jz = 0; jz < 2; ++jz) {
+            Gx[0][jy][jz] = F[0][jy][jz];
+            Gx[1][jy][jz] = sx ? F[0][jy][jz] : F[1][jy][jz];
+            Gx[2][jy][jz] = F[1][jy][jz];
+        }
+    int Gy[3][3][2];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int jz = 0; jz < 2; ++jz) {
+            Gy[a][0][jz] = Gx[a][0][jz];
+            Gy[a][1][jz] = sy ? Gx[a][0][jz] : Gx[a][1][jz];
+            Gy[a][2][jz] = Gx[a][1][jz];
+        }
+#pragma unroll
+    for (int k = 0; k < 27; ++k) {
+        const int a = k / 9, b = (k / 3) % 3, cz = k % 3;
+        const int g = (cz == 0) ? Gy[a][b][0] : (cz == 2) ? Gy[a][b][1] : (sz ? Gy[a][b][0] : Gy[a][b][1]);
+        // child bit per axis: (s + d - 1) & 1
+        const int lc = 4 * ((sx + a + 1) & 1) + 2 * ((sy + b + 1) & 1) + ((sz + cz + 1) & 1);
+        v[k] = (g == -1) ? -1 : g + lc;
+    }
+}
+
 // Terms of one level of an implicit-function chain: the 27 same-depth neighbours nb of
 // `node`, each adding ((x[nb] * Fx) * Fy) * Fz in slot order.  A neighbour's function
 // index is the node's own plus the slot offset, so the 81 basis values come from 9.
