@@ -976,42 +976,85 @@ struct SubLevelLoad {
 #pragma unroll
         for (int kk = 0; kk < 27; ++kk) y[kk] = 0.0f;
         if (!interior) {
+            // Three slabs of 9 neighbours, each in three rounds of independent loads (all
+            // addresses clamped to valid entries, results selected afterwards): the parent's
+            // neighbour row; the redirect, child and first-child entries of those neighbours;
+            // the values and grandchildren of the neighbours found
+            const bool has_row = pslot >= 0 || pa >= 0;
+            const int* rowp = (pslot >= 0) ? A.neigh + pslot : neigh + (pa >= 0 ? pa : 0);
+            const size_t rstride = (pslot >= 0) ? A.cstride : stride;
 #pragma unroll
-            for (int kk = 0; kk < 27; ++kk) {
-                const int ix = kk / 9, iy = (kk / 3) % 3, iz = kk % 3;
-                int v;
-                if (ok[0][ix] && ok[1][iy] && ok[2][iz]) {
-                    const unsigned relk = cmp[0][ix] | cmp[1][iy] | cmp[2][iz];
-                    v = na + vnode + (int)relk - (int)rel;
-                    if (at_root_depth) contrib = 1;   // the node itself, a root
-                } else {
+            for (int ix = 0; ix < 3; ++ix) {
+                int np[9];
+#pragma unroll
+                for (int q = 0; q < 9; ++q) {
+                    const int kk = 9 * ix + q;
                     int lp, lc;
                     nb_lut(son, kk, lp, lc);
-                    const int np = (pslot < 0) ? ((pa >= 0) ? __ldg(neigh + (size_t)lp * stride + pa) : -1)
-                                               : __ldg(A.neigh + (size_t)lp * A.cstride + pslot);
-                    v = -1;
-                    if (np != -1) {
-                        if (np < na) {
-                            if (__ldg(ov_group + (size_t)lc * stride + np) == g) {
-                                // redirected child pointer of this group's root
-                                v = na + G[3] + __ldg(ov_sub + (size_t)lc * stride + np);
-                            } else {
-                                const int fc = __ldg(first_child + np);
-                                v = (fc == -1) ? -1 : fc + lc;
-                                if (v >= 0 && d < depth && __ldg(first_child + v) != -1) deeper = true;
-                            }
-                        } else {
-                            // a sub node of depth d - 1 in this group: its children are at 8 x
-                            // its index in level d
-                            v = na + G[3] + off_cur + 8 * (np - na - G[3] - off_prev) + lc;
-                        }
-                    }
-                    // a contributing neighbour is an octree node or a root; the subdivision nodes
-                    // at a group's root depth are exactly its roots, and deeper ones are never roots
-                    if (v >= 0 && (v < na || at_root_depth)) contrib = 1;
+                    const int t = __ldg(rowp + (size_t)lp * rstride);
+                    np[q] = has_row ? t : -1;
                 }
-                A.neigh[(size_t)kk * A.cstride + slot] = v;
-                if (v >= 0 && v < na && !at_root_depth) y[kk] = __ldg(x + v);
+                int og[9], fc[9], os[9];
+#pragma unroll
+                for (int q = 0; q < 9; ++q) {
+                    const int kk = 9 * ix + q;
+                    int lp, lc;
+                    nb_lut(son, kk, lp, lc);
+                    const int n0 = (np[q] >= 0 && np[q] < na) ? np[q] : 0;
+                    og[q] = __ldg(ov_group + (size_t)lc * stride + n0);
+                    os[q] = __ldg(ov_sub + (size_t)lc * stride + n0);
+                    fc[q] = __ldg(first_child + n0);
+                }
+                int vv[9];
+                bool plain_oct[9];
+#pragma unroll
+                for (int q = 0; q < 9; ++q) {
+                    const int kk = 9 * ix + q;
+                    const int iy = (kk / 3) % 3, iz = kk % 3;
+                    int lp, lc;
+                    nb_lut(son, kk, lp, lc);
+                    int v = -1;
+                    plain_oct[q] = false;
+                    if (ok[0][ix] && ok[1][iy] && ok[2][iz]) {
+                        const unsigned relk = cmp[0][ix] | cmp[1][iy] | cmp[2][iz];
+                        v = na + vnode + (int)relk - (int)rel;
+                        if (at_root_depth) contrib = 1;   // the node itself, a root
+                    } else {
+                        const int n = np[q];
+                        if (n != -1) {
+                            if (n < na) {
+                                if (og[q] == g) {
+                                    // redirected child pointer of this group's root
+                                    v = na + G[3] + os[q];
+                                } else {
+                                    v = (fc[q] == -1) ? -1 : fc[q] + lc;
+                                    plain_oct[q] = true;
+                                }
+                            } else {
+                                // a sub node of depth d - 1 in this group: its children are
+                                // at 8 x its index in level d
+                                v = na + G[3] + off_cur + 8 * (n - na - G[3] - off_prev) + lc;
+                            }
+                        }
+                        // a contributing neighbour is an octree node or a root; the subdivision
+                        // nodes at a group's root depth are exactly its roots, and deeper ones
+                        // are never roots
+                        if (v >= 0 && (v < na || at_root_depth)) contrib = 1;
+                    }
+                    vv[q] = v;
+                }
+#pragma unroll
+                for (int q = 0; q < 9; ++q) {
+                    const int v = vv[q];
+                    const bool oct = v >= 0 && v < na;
+                    const int v0 = oct ? v : 0;
+                    const float xv = __ldg(x + v0);
+                    const int gc = __ldg(first_child + v0);
+                    if (plain_oct[q] && v >= 0 && d < depth && gc != -1) deeper = true;
+                    if (oct && !at_root_depth) y[9 * ix + q] = xv;
+                }
+#pragma unroll
+                for (int q = 0; q < 9; ++q) A.neigh[(size_t)(9 * ix + q) * A.cstride + slot] = vv[q];
             }
         }
         const int prec = (pslot >= 0) ? pslot : -2 - pa;
