@@ -20,11 +20,17 @@ __device__ __forceinline__ float sqdist3(float ax, float ay, float az, float bx,
     return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
 }
 
-// value behind a 1-based back-pointer; a missing pointer (0) flags the tree as malformed
-// and reads as +1 instead of touching memory outside the array
-__device__ __forceinline__ float ptr_value(const float* vals, int ptr1, unsigned* err) {
-    if (ptr1 <= 0) { atomicOr(err, kErrInvalid); return 1.0f; }
-    return vals[ptr1 - 1];
+// values behind N 1-based vertex pointers, every load issued before any check (a pointer
+// <= 0 is a broken record: it reads entry 0, yields 1.0f and flags the error)
+template <int N>
+__device__ __forceinline__ void ptr_values(const float* vals, const int (&p)[N], float (&v)[N], unsigned* err) {
+#pragma unroll
+    for (int q = 0; q < N; ++q) v[q] = vals[p[q] > 0 ? p[q] - 1 : 0];
+    bool bad = false;
+#pragma unroll
+    for (int q = 0; q < N; ++q)
+        if (p[q] <= 0) { v[q] = 1.0f; bad = true; }
+    if (bad) atomicOr(err, kErrInvalid);
 }
 
 __device__ __forceinline__ void decode3m(int e, int depth, int& ix, int& iy, int& iz) {
@@ -352,21 +358,47 @@ __global__ void __launch_bounds__(kBlock) k_vertex_values(const Counters* c, int
         float val = 0.0f;
         const int ow = vowner[v];
         if (ow > 0) {
+            // The chain: the owner, its ancestors up to the root, then the owner's
+            // descendants of child kind ec down to depth D.  Software-pipelined: the next
+            // node's neighbour row, code, parent and first child are read while the current
+            // node's values are in flight; terms are added in chain order as before.
             const float qx = vx[v], qy = vy[v], qz = vz[v];
-            int node = ow;
-            while (node != -1) {
-                val = node_terms(node, val, qx, qy, qz, depth, neigh, stride, enc, x);
-                node = parent[node];
-            }
-            node = ow;
-            int d = vdepth[v];
             const int ec = __ldg(&g_tab.children_vertex_kind[vkind[v]]);
-            while (d < depth) {
-                d++;
-                const int fc = first_child[node];
-                node = (fc == -1) ? -1 : fc + ec;
-                if (node == -1) break;
-                val = node_terms(node, val, qx, qy, qz, depth, neigh, stride, enc, x);
+            int d = vdepth[v];
+            const int fc_ow = first_child[ow];
+            bool up = true;
+            int nbs[27];
+#pragma unroll
+            for (int k = 0; k < 27; ++k) nbs[k] = neigh[(size_t)k * stride + ow];
+            int e = enc[ow], par = parent[ow], fcn = fc_ow;
+            while (true) {
+                float xv[27];
+#pragma unroll
+                for (int k = 0; k < 27; ++k) xv[k] = x[nbs[k] >= 0 ? nbs[k] : 0];
+                int nx;
+                if (up && par != -1) {
+                    nx = par;
+                } else {
+                    const int f = up ? fc_ow : fcn;
+                    up = false;
+                    nx = (d < depth && f != -1) ? f + ec : -1;
+                    if (nx != -1) ++d;
+                }
+                int nb2[27];
+                int e2 = 0, par2 = -1, fc2 = -1;
+                const int n0 = (nx != -1) ? nx : 0;
+#pragma unroll
+                for (int k = 0; k < 27; ++k) nb2[k] = neigh[(size_t)k * stride + n0];
+                e2 = enc[n0];
+                par2 = parent[n0];
+                fc2 = first_child[n0];
+                val = terms_from(e, nbs, xv, val, qx, qy, qz, depth);
+                if (nx == -1) break;
+#pragma unroll
+                for (int k = 0; k < 27; ++k) nbs[k] = nb2[k];
+                e = e2;
+                par = par2;
+                fcn = fc2;
             }
         }
         vvalue[v] = __fsub_rn(val, iso);
@@ -379,10 +411,11 @@ __global__ void __launch_bounds__(kBlock) k_vertex_values(const Counters* c, int
 __device__ __forceinline__ void interp_point(float p1x, float p1y, float p1z, float p2x, float p2y, float p2z, int dim,
                                              float v1, float v2, float* out) {
     out[0] = p1x; out[1] = p1y; out[2] = p1z;
-    const float p1[3] = {p1x, p1y, p1z}, p2[3] = {p2x, p2y, p2z};
+    const float a1 = (dim == 0) ? p1x : (dim == 1) ? p1y : p1z;   // selects: no local array
+    const float a2 = (dim == 0) ? p2x : (dim == 1) ? p2y : p2z;
     float pivot = __fdiv_rn(v1, __fsub_rn(v1, v2));
     float other = __fsub_rn(1.0f, pivot);
-    out[dim] = __fadd_rn(__fmul_rn(p2[dim], pivot), __fmul_rn(p1[dim], other));
+    out[dim] = __fadd_rn(__fmul_rn(a2, pivot), __fmul_rn(a1, other));
 }
 
 struct CrossLoad {
@@ -394,8 +427,11 @@ struct CrossLoad {
     unsigned* err;
     __device__ unsigned operator()(int e) const {
         const int ow = eowner[e], kind = ekind[e];
-        const float a = ptr_value(vvalue, node_vtx[(size_t)__ldg(&g_tab.edge_vertex[kind][0]) * stride + ow], err);
-        const float b = ptr_value(vvalue, node_vtx[(size_t)__ldg(&g_tab.edge_vertex[kind][1]) * stride + ow], err);
+        const int p[2] = {node_vtx[(size_t)__ldg(&g_tab.edge_vertex[kind][0]) * stride + ow],
+                          node_vtx[(size_t)__ldg(&g_tab.edge_vertex[kind][1]) * stride + ow]};
+        float ab[2];
+        ptr_values(vvalue, p, ab, err);
+        const float a = ab[0], b = ab[1];
         return (__fmul_rn(a, b) <= 0.0f) ? 1u : 0u;
     }
 };
@@ -435,10 +471,15 @@ struct CubeLoad {
     unsigned* err;
     __device__ unsigned operator()(int o) const {
         const int i = *base_ptr + o;
+        int p[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) p[q] = node_vtx[(size_t)q * stride + i];
+        float vq[8];
+        ptr_values(vvalue, p, vq, err);
         int cls = 0;
 #pragma unroll
         for (int q = 0; q < 8; ++q)
-            if (ptr_value(vvalue, node_vtx[(size_t)q * stride + i], err) < 0.0f) cls |= 1 << q;
+            if (vq[q] < 0.0f) cls |= 1 << q;
         cube_class[o] = cls;
         return (unsigned)__ldg(&g_tab.mc_count[cls]);
     }
@@ -507,17 +548,29 @@ struct RootLoad {
     const int* first_child;
     unsigned* err;
     __device__ unsigned operator()(int i) const {
-        const float v0 = ptr_value(vvalue, node_vtx[i], err);
-        const float s = (v0 < 0.0f) ? -1.0f : 1.0f;
+        // all reads first (the cell's 8 corner values, 6 faces and their flags), then the tests
+        int p[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) p[q] = node_vtx[(size_t)q * stride + i];
+        int fp[6];
+#pragma unroll
+        for (int f = 0; f < 6; ++f) fp[f] = node_face[(size_t)f * stride + i] - 1;
+        int fh[6];
+#pragma unroll
+        for (int f = 0; f < 6; ++f) fh[f] = face_hit[fp[f] >= 0 ? fp[f] : 0];
+        const int fc = first_child[i];
+        float vq[8];
+        ptr_values(vvalue, p, vq, err);
+        const float s = (vq[0] < 0.0f) ? -1.0f : 1.0f;
         int ht = 0;
+#pragma unroll
         for (int q = 1; q < 8; ++q)
-            if (__fmul_rn(s, ptr_value(vvalue, node_vtx[(size_t)q * stride + i], err)) < 0.0f) { ht = 1; break; }
+            if (__fmul_rn(s, vq[q]) < 0.0f) ht = 1;
         int hi = 0;
-        for (int f = 0; f < 6; ++f) {
-            const int fp = node_face[(size_t)f * stride + i] - 1;
-            if (fp >= 0 && face_hit[fp]) { hi = 1; break; }
-        }
-        return (first_child[i] == -1 && (ht || hi)) ? 1u : 0u;
+#pragma unroll
+        for (int f = 0; f < 6; ++f)
+            if (fp[f] >= 0 && fh[f]) hi = 1;
+        return (fc == -1 && (ht || hi)) ? 1u : 0u;
     }
 };
 struct RootStore {
@@ -1416,8 +1469,11 @@ struct SubCrossLoad {
     __device__ unsigned operator()(int e) const {
         const int dn = eowner[e];
         const int kind = ekind[e];
-        const float a = ptr_value(vvalue, s_vtx[(size_t)__ldg(&g_tab.edge_vertex[kind][0]) * dstride + dn], err);
-        const float b = ptr_value(vvalue, s_vtx[(size_t)__ldg(&g_tab.edge_vertex[kind][1]) * dstride + dn], err);
+        const int p[2] = {s_vtx[(size_t)__ldg(&g_tab.edge_vertex[kind][0]) * dstride + dn],
+                          s_vtx[(size_t)__ldg(&g_tab.edge_vertex[kind][1]) * dstride + dn]};
+        float ab[2];
+        ptr_values(vvalue, p, ab, err);
+        const float a = ab[0], b = ab[1];
         return (__fmul_rn(a, b) <= 0.0f) ? 1u : 0u;
     }
 };
@@ -1455,10 +1511,15 @@ struct SubCubeLoad {
     int* cube_class;
     unsigned* err;
     __device__ unsigned operator()(int L) const {
+        int p[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) p[q] = s_vtx[(size_t)q * dstride + L];
+        float vq[8];
+        ptr_values(vvalue, p, vq, err);
         int cls = 0;
 #pragma unroll
         for (int q = 0; q < 8; ++q)
-            if (ptr_value(vvalue, s_vtx[(size_t)q * dstride + L], err) < 0.0f) cls |= 1 << q;
+            if (vq[q] < 0.0f) cls |= 1 << q;
         cube_class[L] = cls;
         return (unsigned)__ldg(&g_tab.mc_count[cls]);
     }

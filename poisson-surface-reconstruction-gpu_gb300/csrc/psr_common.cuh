@@ -170,10 +170,10 @@ __device__ __forceinline__ void child_neighbours(int son, Row row, First first, 
 // Terms of one level of an implicit-function chain: the 27 same-depth neighbours nb of
 // `node`, each adding ((x[nb] * Fx) * Fy) * Fz in slot order.  A neighbour's function
 // index is the node's own plus the slot offset, so the 81 basis values come from 9.
-__device__ __forceinline__ float level_terms(int node, float val, float qx, float qy, float qz, int depth,
-                                             const int* neigh, size_t stride, const int* enc, const float* x) {
+__device__ __forceinline__ float terms_from(int encv, const int (&nbs)[27], const float (&xv)[27], float val,
+                                            float qx, float qy, float qz, int depth) {
     int ox, oy, oz;
-    decode_fn_index(enc[node], depth, ox, oy, oz);
+    decode_fn_index(encv, depth, ox, oy, oz);
     float bx[3], by[3], bz[3];
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
@@ -181,18 +181,28 @@ __device__ __forceinline__ float level_terms(int node, float val, float qx, floa
         by[j] = basis32(oy - 1 + j, qy);
         bz[j] = basis32(oz - 1 + j, qz);
     }
-    int nbs[27];
-#pragma unroll
-    for (int k = 0; k < 27; ++k) nbs[k] = neigh[(size_t)k * stride + node];
 #pragma unroll
     for (int k = 0; k < 27; ++k) {
         if (nbs[k] == -1) continue;
-        float t = __fmul_rn(x[nbs[k]], bx[k / 9]);
+        float t = __fmul_rn(xv[k], bx[k / 9]);
         t = __fmul_rn(t, by[(k / 3) % 3]);
         t = __fmul_rn(t, bz[k % 3]);
         val = __fadd_rn(val, t);
     }
     return val;
+}
+
+__device__ __forceinline__ float level_terms(int node, float val, float qx, float qy, float qz, int depth,
+                                             const int* neigh, size_t stride, const int* enc, const float* x) {
+    const int e = enc[node];
+    int nbs[27];
+#pragma unroll
+    for (int k = 0; k < 27; ++k) nbs[k] = neigh[(size_t)k * stride + node];
+    // every value read at once (a missing neighbour reads entry 0 and adds nothing)
+    float xv[27];
+#pragma unroll
+    for (int k = 0; k < 27; ++k) xv[k] = x[nbs[k] >= 0 ? nbs[k] : 0];
+    return terms_from(e, nbs, xv, val, qx, qy, qz, depth);
 }
 
 // ---- Bernstein form of the implicit function on a cell --------------------------------
