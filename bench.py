@@ -55,6 +55,29 @@ def dist_env():
     return rank, world, local
 
 
+def rank_clouds(rank, slots):
+    """Cloud seeds a rank reconstructs: slot k of the served leg takes rank * slots + k, and
+    the plain and host legs take the rank's slot-0 cloud.  Ranks hold disjoint clouds (the
+    shards of the job); rank 0 of a 1-GPU run uses clouds 0 .. slots - 1."""
+    return [rank * slots + k for k in range(slots)]
+
+
+def job_rates(world, steps, slots, totals_ms, reduce_max=None):
+    """Whole-job reconstructions/s from each rank's timed totals (ms): the plain, plain-e2e,
+    served and served-e2e legs.  The job's time is the slowest rank's (`reduce_max` takes
+    the element-wise maximum over ranks, e.g. an all_reduce MAX); every rank processed
+    `steps` clouds in the plain legs and `slots * steps` in the served legs."""
+    t = list(totals_ms)
+    if world > 1 and reduce_max is not None:
+        t = reduce_max(t)
+    t_dev, t_e2e, t_sdev, t_se2e = t
+    return {"plain": world * steps / (t_dev / 1000.0),
+            "plain_e2e": world * steps / (t_e2e / 1000.0),
+            "served": world * slots * steps / (t_sdev / 1000.0),
+            "served_e2e": world * slots * steps / (t_se2e / 1000.0),
+            "max_totals_ms": t}
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
 
@@ -182,7 +205,8 @@ def main():
     import psr
     import synthetic as syn
 
-    xyz, nrm, rgb, depth = syn.workload(args.workload, cloud=rank)
+    seeds = rank_clouds(rank, args.slots)
+    xyz, nrm, rgb, depth = syn.workload(args.workload, cloud=seeds[0])
     n = len(xyz)
     r = psr.PoissonReconstruction(max_depth=depth, max_points=max(300000, n), max_triangles=1000000,
                                   max_mesh_vertices=300000, compute_colors=rgb is not None,
@@ -262,7 +286,7 @@ def main():
     from serve import Server
     dclouds, hclouds = [], []
     for k in range(args.slots):
-        cx, cn, cc, _ = syn.workload(args.workload, cloud=rank * args.slots + k) if k else (xyz, nrm, rgb, depth)
+        cx, cn, cc, _ = syn.workload(args.workload, cloud=seeds[k]) if k else (xyz, nrm, rgb, depth)
         dclouds.append((torch.from_numpy(cx).to(dev), torch.from_numpy(cn).to(dev),
                         torch.from_numpy(cc).to(dev) if cc is not None else None, depth))
         hclouds.append((torch.from_numpy(cx).pin_memory(), torch.from_numpy(cn).pin_memory(),
@@ -285,19 +309,17 @@ def main():
     if world > 1:
         dist.barrier()
     st = r.stats()
-    tot_dev = float(t_dev.sum())
-    tot_e2e = float(t_e2e.sum())
-    tot_sdev = float(s_dev)
-    tot_se2e = float(s_e2e)
-    if world > 1:
-        tt = torch.tensor([tot_dev, tot_e2e, tot_sdev, tot_se2e], dtype=torch.float64, device=dev)
+    def all_max(vals):
+        tt = torch.tensor(vals, dtype=torch.float64, device=dev)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        tot_dev, tot_e2e, tot_sdev, tot_se2e = tt.tolist()
+        return tt.tolist()
+
     K = args.slots
-    plain_value = world * args.steps / (tot_dev / 1000.0)
-    plain_e2e = world * args.steps / (tot_e2e / 1000.0)
-    value = world * K * args.steps / (tot_sdev / 1000.0)
-    e2e_value = world * K * args.steps / (tot_se2e / 1000.0)
+    rates = job_rates(world, args.steps, K, [float(t_dev.sum()), float(t_e2e.sum()), float(s_dev), float(s_e2e)],
+                      all_max)
+    tot_dev, tot_e2e, tot_sdev, tot_se2e = rates["max_totals_ms"]
+    plain_value, plain_e2e = rates["plain"], rates["plain_e2e"]
+    value, e2e_value = rates["served"], rates["served_e2e"]
     clocks = clk.summary()
     h2d = n * (12 + 12 + (3 if rgb is not None else 0))
     d2h = m_host.vertex_count * 12 * (3 if rgb is not None else 2) + m_host.triangle_count * 12
