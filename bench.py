@@ -390,6 +390,7 @@ def main():
             "gpu_launches": (int(st_launches(server.slots[0].recon)) + 1) * K * args.steps,
             "gpu_launches_per_recon": int(st_launches(server.slots[0].recon)) + 1,
             "roofline": roofline, "clocks": clocks}
+    line.update(side_legs(psr, r, caps, d_xyz, d_nrm, d_rgb, n, depth, dev_mesh, stream, torch, st))
     if not args.no_cpu_baseline:
         try:
             line["cpu_baseline"] = cpu_baseline(xyz, nrm, rgb, depth)
@@ -398,6 +399,40 @@ def main():
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def side_legs(psr, r, caps, d_xyz, d_nrm, d_rgb, n, depth, dev_mesh, stream, torch, st, reps=10):
+    """Stages beside the reconstruction, timed after the headline legs with CUDA events on
+    the launching stream (device-resident arrays, median of `reps` after 3 warm-ups):
+    normal estimation of the cloud as if unoriented (psr_estimate_normals, k = 10), and the
+    plain leg on a handle that welds the vertices repeated by subdivided regions."""
+    def median_ms(fn):
+        for _ in range(3):
+            fn()
+        ts = []
+        for _ in range(reps):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            b.synchronize()
+            ts.append(a.elapsed_time(b))
+        return float(np.median(ts))
+    out = {}
+    d_out = torch.empty_like(d_xyz)
+    ms = median_ms(lambda: r.estimate_normals_device(d_xyz.data_ptr(), n, d_out.data_ptr(),
+                                                     stream=stream.cuda_stream))
+    out["normal_estimation"] = {"points": n, "k": 10, "ms": ms, "points_per_s": n / (ms * 1e-3)}
+    with psr.PoissonReconstruction(weld_vertices=True, **caps) as rw:
+        def weld_step():
+            rw.reconstruct_device(d_xyz.data_ptr(), d_nrm.data_ptr(),
+                                  d_rgb.data_ptr() if d_rgb is not None else None, n, depth=depth,
+                                  stream=stream.cuda_stream, out=dev_mesh())
+        ms = median_ms(weld_step)
+        out["weld"] = {"plain_ms": ms, "vertices_before": st.mesh_vertices,
+                       "vertices_after": rw.stats().mesh_vertices}
+    return out
 
 
 def open_loop_leg(server, clouds, n_req, rate, seed=7):
