@@ -6,7 +6,13 @@ point formats of its `PointCloudData/` fixtures without PCL:
 
 * PLY (ascii, binary_little_endian, binary_big_endian) with vertex properties x, y, z,
   nx, ny, nz and optionally red, green, blue (any numeric types);
-* whitespace-separated text, one point per line: x y z nx ny nz [r g b].
+* whitespace-separated text, one point per line: x y z [nx ny nz [r g b]];
+* PCD v0.7 (`DATA ascii` or `binary`) with fields x, y, z, optionally normal_x,
+  normal_y, normal_z and a packed rgb, other fields (intensity, padding `_`) skipped.
+
+Files without normals (the reference's `.txt` and `.pcd` fixtures) return normals None;
+the caller estimates them on the GPU (`PoissonReconstruction.CalculatePointCloudNormal`,
+the reference's PCL step of readPCDFile, mesh/PoissonReconstruction.cpp:80-101).
 
 `write_mesh_ply` writes a reconstructed mesh (binary little endian; optional per-vertex
 normals and colours), in world coordinates when given the call's center / scale.
@@ -81,18 +87,96 @@ def read_ply_points(path):
 
 
 def read_txt_points(path):
-    """x y z nx ny nz [r g b] per line (r g b in 0..255)."""
+    """x y z [nx ny nz [r g b]] per line (r g b in 0..255); normals None for 3 columns
+    (the reference's readTXTFile, mesh/PoissonReconstruction.cpp:63-78, reads positions)."""
     data = np.loadtxt(path, ndmin=2)
-    if data.shape[1] < 6:
-        raise ValueError("text points need at least 6 columns: x y z nx ny nz")
+    if data.shape[1] < 3 or 3 < data.shape[1] < 6:
+        raise ValueError("text points need 3 columns (x y z) or at least 6 (x y z nx ny nz)")
+    nrm = data[:, 3:6].astype(np.float32) if data.shape[1] >= 6 else None
     rgb = np.clip(data[:, 6:9], 0, 255).astype(np.uint8) if data.shape[1] >= 9 else None
-    return data[:, :3].astype(np.float32), data[:, 3:6].astype(np.float32), rgb
+    return data[:, :3].astype(np.float32), nrm, rgb
+
+
+_PCD_TYPES = {("F", 4): "f4", ("F", 8): "f8", ("U", 1): "u1", ("U", 2): "u2", ("U", 4): "u4", ("U", 8): "u8",
+              ("I", 1): "i1", ("I", 2): "i2", ("I", 4): "i4", ("I", 8): "i8"}
+
+
+def read_pcd_points(path):
+    """PCD v0.7 (the reference's readPCDFile input, pcl::io::loadPCDFile): returns (xyz
+    float32 N x 3, normals float32 N x 3 or None, rgb uint8 N x 3 or None)."""
+    with open(path, "rb") as f:
+        hdr = {}
+        while True:
+            line = f.readline()
+            if not line:
+                raise ValueError("PCD header without DATA")
+            w = line.decode("ascii", "replace").split()
+            if not w or w[0].startswith("#"):
+                continue
+            hdr[w[0].upper()] = w[1:]
+            if w[0].upper() == "DATA":
+                break
+        fields = hdr.get("FIELDS")
+        if not fields:
+            raise ValueError("PCD header without FIELDS")
+        nf = len(fields)
+        sizes = [int(x) for x in hdr.get("SIZE", ["4"] * nf)]
+        types = hdr.get("TYPE", ["F"] * nf)
+        counts = [int(x) for x in hdr.get("COUNT", ["1"] * nf)]
+        if not (len(sizes) == len(types) == len(counts) == nf):
+            raise ValueError("PCD FIELDS / SIZE / TYPE / COUNT lengths differ")
+        n = int(hdr["POINTS"][0]) if "POINTS" in hdr else int(hdr["WIDTH"][0]) * int(hdr.get("HEIGHT", ["1"])[0])
+        data_kind = hdr["DATA"][0].lower()
+        cols = {}
+        if data_kind == "ascii":
+            arr = np.loadtxt(f, max_rows=n, ndmin=2) if n else np.zeros((0, sum(counts)))
+            if arr.shape[0] != n:
+                raise ValueError(f"PCD declares {n} points, holds {arr.shape[0]}")
+            at = 0
+            for name, t, sz, c in zip(fields, types, sizes, counts):
+                col = arr[:, at]
+                if (t.upper(), sz) in (("U", 4), ("F", 4)) and name == "rgb":
+                    col = col.astype(np.float32 if t.upper() == "F" else np.uint32)
+                cols[name] = col
+                at += c
+        elif data_kind == "binary":
+            dt = []
+            for k, (name, t, sz, c) in enumerate(zip(fields, types, sizes, counts)):
+                key = (t.upper(), sz)
+                if key not in _PCD_TYPES:
+                    raise ValueError(f"PCD field {name!r}: type {t} size {sz} not supported")
+                dt.append((f"{name}#{k}", "<" + _PCD_TYPES[key], (c,) if c > 1 else ()))
+            dt = np.dtype(dt)
+            buf = f.read(dt.itemsize * n)
+            if len(buf) != dt.itemsize * n:
+                raise ValueError("PCD binary data shorter than declared")
+            arr = np.frombuffer(buf, dtype=dt, count=n)
+            for k, name in enumerate(fields):
+                cols.setdefault(name, arr[f"{name}#{k}"])
+        else:
+            raise ValueError(f"PCD DATA {data_kind!r} not supported (ascii or binary)")
+    for k in ("x", "y", "z"):
+        if k not in cols:
+            raise ValueError(f"PCD file lacks field '{k}'")
+    xyz = np.stack([cols["x"], cols["y"], cols["z"]], 1).astype(np.float32)
+    nrm = None
+    if all(k in cols for k in ("normal_x", "normal_y", "normal_z")):
+        nrm = np.stack([cols["normal_x"], cols["normal_y"], cols["normal_z"]], 1).astype(np.float32)
+    rgb = None
+    if "rgb" in cols or "rgba" in cols:
+        packed = np.asarray(cols.get("rgb", cols.get("rgba")))
+        packed = packed.view(np.uint32) if packed.dtype == np.float32 else packed.astype(np.uint32)
+        rgb = np.stack([(packed >> 16) & 255, (packed >> 8) & 255, packed & 255], 1).astype(np.uint8)
+    return xyz, nrm, rgb
 
 
 def read_points(path):
+    """(xyz, normals or None, rgb or None) of a .ply, .pcd or text point file."""
     p = str(path).lower()
     if p.endswith(".ply"):
         return read_ply_points(path)
+    if p.endswith(".pcd"):
+        return read_pcd_points(path)
     if p.endswith((".txt", ".xyz", ".xyzn")):
         return read_txt_points(path)
     raise ValueError(f"unsupported point file {path}")

@@ -255,6 +255,35 @@ class PoissonReconstruction:
         if st != PSR_OK:
             raise self._error(st, "psr_wait")
 
+    # ---- file inputs: the reference's readTXTFile / readPCDFile / readPLYFile and
+    # getDenseSurfel (mesh/PoissonReconstruction.cpp:63-135, :176-179)
+    def readPointFile(self, path, viewpoint=(0.0, 0.0, 0.0)):
+        """Reads a .ply / .pcd / .txt cloud (plyio.read_points); a file without normals gets
+        them estimated on the GPU as the reference's readPCDFile does through PCL (k = 10,
+        viewpoint at the origin).  Returns (xyz, normals, rgb or None), also kept for
+        getDenseSurfel()."""
+        import plyio
+        xyz, nrm, rgb = plyio.read_points(path)
+        if nrm is None:
+            nrm = self.CalculatePointCloudNormal(xyz, viewpoint)
+        self._surfel = (xyz, nrm, rgb)
+        return self._surfel
+
+    def readTXTFile(self, path):
+        return self.readPointFile(path)
+
+    def readPCDFile(self, path):
+        return self.readPointFile(path)
+
+    def readPLYFile(self, path):
+        """Oriented points of a PLY file (the reference only displays the file in a PCL viewer)."""
+        return self.readPointFile(path)
+
+    def getDenseSurfel(self):
+        """The points of the last file read: (xyz, normals, rgb or None), the arguments of
+        SolvePoissionReconstructionMesh."""
+        return getattr(self, "_surfel", None)
+
     def CalculatePointCloudNormal(self, xyz, viewpoint=(0.0, 0.0, 0.0)):
         """Normals of an unoriented cloud (float32 N x 3, host): the smallest-eigenvalue
         eigenvector of each point's 10 nearest neighbours' covariance, flipped towards

@@ -54,3 +54,32 @@ def test_surfels_to_points_and_reconstruction():
         np.testing.assert_array_equal(out[2][:m.vertex_count].cpu().numpy(), a.colors)
     # invalid arguments are rejected before any launch
     assert lib.psr_surfels_to_points(None, 5, xyz.data_ptr(), nrm.data_ptr(), None, None) == psr.PSR_INVALID_INPUT
+
+
+def test_unoriented_pcd_and_txt_files_reconstruct(tmp_path):
+    """The reference's unoriented inputs (readPCDFile, readTXTFile): positions only, normals
+    estimated on the GPU, then the reconstruction.  The normals point towards the viewpoint
+    at the centre (inwards), which negates the indicator function and its iso value: the
+    surface still lies on the sphere."""
+    import psr
+    p, _, _, D = syn.workload("sphere20k")
+    pcd = tmp_path / "sphere.pcd"
+    head = ("VERSION 0.7\nFIELDS x y z _\nSIZE 4 4 4 1\nTYPE F F F U\nCOUNT 1 1 1 4\n"
+            f"WIDTH {len(p)}\nHEIGHT 1\nVIEWPOINT 0 0 0 1 0 0 0\nPOINTS {len(p)}\nDATA binary\n")
+    rec = np.zeros(len(p), dtype=[("xyz", "<f4", (3,)), ("pad", "u1", (4,))])
+    rec["xyz"] = p
+    pcd.write_bytes(head.encode() + rec.tobytes())
+    txt = tmp_path / "sphere.txt"
+    np.savetxt(txt, p, fmt="%.9g", delimiter="\t")
+    with psr.PoissonReconstruction(max_depth=D, max_points=30000) as r:
+        for path, read in ((pcd, r.readPCDFile), (txt, r.readTXTFile)):
+            xyz, nrm, rgb = read(str(path))
+            assert rgb is None and np.all(np.isfinite(nrm))
+            radial = (nrm.astype(np.float64) * p).sum(axis=1) / np.linalg.norm(p, axis=1)
+            assert np.median(radial) < -0.99                       # inwards, towards the origin
+            mesh = r.SolvePoissionReconstructionMesh(*r.getDenseSurfel(), depth=D)
+            w = mesh.world_vertices().astype(np.float64)
+            rad = np.linalg.norm(w, axis=1)
+            cell = mesh.scale / (1 << D)
+            assert len(w) > 1000
+            assert abs(np.median(rad) - 1.0) < 0.5 * cell
