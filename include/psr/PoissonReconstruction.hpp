@@ -87,6 +87,26 @@ public:
         scale_ = m.scale;
     }
 
+    // Normals of an unoriented cloud (the reference's PCL step, CalculatePointCloudNormal,
+    // mesh/PoissonReconstruction.cpp:137-161: k = 10, viewpoint at the origin by default);
+    // xyz and normals are 3 * count floats in `location` memory.  NaN for clouds of fewer
+    // than 3 points.
+    void CalculatePointCloudNormal(const float* xyz, int count, float* normals, int location = PSR_HOST,
+                                   const float* viewpoint = nullptr, cudaStream_t stream = nullptr) {
+        psr_status s = psr_estimate_normals(h_, xyz, count, (psr_location)location, normals, viewpoint, stream);
+        if (s != PSR_OK)
+            throw std::runtime_error(std::string("psr_estimate_normals: ") + psr_status_string(s) + ": " +
+                                     psr_last_error(h_));
+    }
+
+    // Unoriented host points: normals estimated on the GPU, then the reconstruction (the
+    // reference's readPCDFile followed by SolvePoissionReconstructionMesh)
+    void SolveUnoriented(const float* xyz, int count, const uint8_t* rgb = nullptr) {
+        std::vector<float> nrm(3 * (size_t)count);
+        CalculatePointCloudNormal(xyz, count, nrm.data(), PSR_HOST);
+        Solve(xyz, nrm.data(), rgb, count, PSR_HOST);
+    }
+
     // mesh/ComputeTriangleIndices.h:331-342 (host copies here)
     const std::vector<Point3D>& GetRebuildMeshVertices() const { return vertices_; }
     const std::vector<TriangleIndex>& GetRebuildMeshTriangleIndices() const { return triangles_; }
