@@ -24,3 +24,24 @@ def test_plane_normals():
 def test_fewer_than_three_points_have_no_normal():
     nrm, _ = normals_oracle.estimate_normals(np.zeros((2, 3)))
     assert np.all(np.isnan(nrm))
+
+
+def test_oracle_matches_brute_force_neighbours():
+    """The kd-tree query equals a brute-force search of the 10 nearest (the point itself
+    included) wherever the 10th and 11th distances are not tied, and the normal equals the
+    smallest eigenvector of those neighbours' covariance computed directly."""
+    rng = np.random.default_rng(11)
+    p = rng.standard_normal((400, 3)).astype(np.float32)
+    p[:, 2] *= 0.05                                    # a noisy slab: well-defined normals
+    o, cond = normals_oracle.estimate_normals(p)
+    d2 = ((p[:, None, :].astype(np.float64) - p[None, :, :]) ** 2).sum(-1)
+    order = np.argsort(d2, axis=1, kind="stable")[:, :10]
+    for i in range(0, 400, 7):
+        if cond["tie"][i]:
+            continue
+        nb = p[order[i]].astype(np.float64)
+        c = np.cov(nb.T, bias=True)
+        w, v = np.linalg.eigh(c)
+        n = v[:, 0] if np.dot(-p[i], v[:, 0]) >= 0 else -v[:, 0]
+        assert abs(abs(np.dot(n, o[i])) - 1.0) < 1e-9
+        assert np.allclose(n, o[i], atol=1e-6) or cond["cos"][i] < 1e-6
