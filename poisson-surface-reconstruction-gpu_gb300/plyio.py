@@ -170,16 +170,29 @@ def read_pcd_points(path):
     return xyz, nrm, rgb
 
 
-def read_points(path):
-    """(xyz, normals or None, rgb or None) of a .ply, .pcd or text point file."""
+def read_points(path, finite_only=True):
+    """(xyz, normals or None, rgb or None) of a .ply, .pcd or text point file.  With
+    finite_only, points whose position (or normal, when present) is not finite are
+    dropped, order kept: organised PCD clouds mark invalid pixels with NaN, and the
+    reconstruction rejects non-finite input."""
     p = str(path).lower()
     if p.endswith(".ply"):
-        return read_ply_points(path)
-    if p.endswith(".pcd"):
-        return read_pcd_points(path)
-    if p.endswith((".txt", ".xyz", ".xyzn")):
-        return read_txt_points(path)
-    raise ValueError(f"unsupported point file {path}")
+        xyz, nrm, rgb = read_ply_points(path)
+    elif p.endswith(".pcd"):
+        xyz, nrm, rgb = read_pcd_points(path)
+    elif p.endswith((".txt", ".xyz", ".xyzn")):
+        xyz, nrm, rgb = read_txt_points(path)
+    else:
+        raise ValueError(f"unsupported point file {path}")
+    if finite_only:
+        keep = np.isfinite(xyz).all(axis=1)
+        if nrm is not None:
+            keep &= np.isfinite(nrm).all(axis=1)
+        if not keep.all():
+            xyz = xyz[keep]
+            nrm = None if nrm is None else nrm[keep]
+            rgb = None if rgb is None else rgb[keep]
+    return xyz, nrm, rgb
 
 
 def write_mesh_ply(path, vertices, triangles, colors=None, normals=None, center=None, scale=None):

@@ -158,3 +158,20 @@ def test_txt_positions_only(tmp_path):
     x, n, c = plyio.read_points(path)
     np.testing.assert_array_equal(x, p)
     assert n is None and c is None
+
+
+def test_organised_pcd_with_invalid_pixels(tmp_path):
+    """An organised cloud (HEIGHT > 1) with NaN pixels: dropped by default, kept on request."""
+    p, _, _, _ = syn.workload("sphere20k", n=64)
+    q = p.copy()
+    q[[3, 10, 40]] = np.nan
+    path = tmp_path / "org.pcd"
+    head = ("VERSION 0.7\nFIELDS x y z\nSIZE 4 4 4\nTYPE F F F\nCOUNT 1 1 1\nWIDTH 8\nHEIGHT 8\n"
+            "VIEWPOINT 0 0 0 1 0 0 0\nPOINTS 64\nDATA binary\n")
+    path.write_bytes(head.encode() + q.astype("<f4").tobytes())
+    x, n, c = plyio.read_points(path)
+    keep = np.ones(64, bool)
+    keep[[3, 10, 40]] = False
+    np.testing.assert_array_equal(x, p[keep])
+    x2, _, _ = plyio.read_points(path, finite_only=False)
+    assert x2.shape == (64, 3) and np.isnan(x2[3]).all()
