@@ -7,6 +7,7 @@
 
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -104,6 +105,10 @@ public:
     void SolveUnoriented(const float* xyz, int count, const uint8_t* rgb = nullptr) {
         std::vector<float> nrm(3 * (size_t)count);
         CalculatePointCloudNormal(xyz, count, nrm.data(), PSR_HOST);
+        // no normal (NaN: degenerate neighbourhood) -> zero, which adds nothing to the field
+        for (size_t i = 0; i < nrm.size(); i += 3)
+            if (!(std::isfinite(nrm[i]) && std::isfinite(nrm[i + 1]) && std::isfinite(nrm[i + 2])))
+                nrm[i] = nrm[i + 1] = nrm[i + 2] = 0.0f;
         Solve(xyz, nrm.data(), rgb, count, PSR_HOST);
     }
 

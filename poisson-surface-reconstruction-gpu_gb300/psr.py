@@ -266,6 +266,10 @@ class PoissonReconstruction:
         xyz, nrm, rgb = plyio.read_points(path)
         if nrm is None:
             nrm = self.CalculatePointCloudNormal(xyz, viewpoint)
+            # no normal (fewer than 3 samples, or all neighbours at one position): a zero
+            # normal, which adds nothing to the vector field, instead of a NaN that the
+            # reconstruction rejects
+            nrm[~np.isfinite(nrm).all(axis=1)] = 0.0
         self._surfel = (xyz, nrm, rgb)
         return self._surfel
 
