@@ -1,4 +1,4 @@
-// Driver for pinning the oracle's B-spline tables against the reference's own host code.
+// Host program pinning the oracle's B-spline tables against the reference's own host code.
 // Compiled by oracle/build_ref.sh against the reference headers (mesh/FunctionData.h,
 // math/PPolynomial.h, math/Polynomial.h, mesh/BinaryNode.h); never shipped.
 // Prints, for a given max depth, the piecewise polynomial of the normalised base function
