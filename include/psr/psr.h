@@ -64,6 +64,13 @@ typedef struct psr_config {
                                   keep their order, triangles are renumbered, colours and
                                   normals come from the welded mesh.  0 (default): as the
                                   reference */
+    int disable_graphs;        /* 0 (default): each (depth, options) pipeline is captured once
+                                  into a CUDA graph and replayed; 1: kernels are issued one by
+                                  one on every call (same results; for inspection) */
+    int root_poly_capacity;    /* 0 (default): max(65536, nodes / 16).  Subdivision roots beyond
+                                  this many evaluate the levels above them by walking their
+                                  octree chain instead of from one cached polynomial per root
+                                  (same mesh, slower) */
 } psr_config;
 
 /* Oriented input cloud (the fields of DepthSurfel, base/CommonTypes.h:113-118, as SoA). */
@@ -150,11 +157,6 @@ psr_status psr_submit(psr_handle* h, const psr_points* points, const psr_options
 psr_status psr_poll(psr_handle* h);
 psr_status psr_wait(psr_handle* h);
 
-/* Input adaptor: device array of `count` DepthSurfel records (base/CommonTypes.h:113-118,
- * 64 bytes each) -> device SoA arrays for psr_points: xyz and normals (3 * count floats),
- * and rgb (3 * count bytes, round(255 * ColorAndTime.xyz) clamped) unless rgb is NULL.
- * Replaces getCoordinateAndNormalKernel (mesh/BuildOctree.cu:135-143); enqueued on
- * `stream` (a cudaStream_t or NULL), no host wait. */
 /* Normals of an unoriented cloud (replaces the PCL step the reference runs before the path,
  * CalculatePointCloudNormal, mesh/PoissonReconstruction.cpp:137-161: NormalEstimationOMP,
  * k = 10 nearest neighbours, viewpoint (0, 0, 0)): for every point the eigenvector of the
@@ -166,6 +168,11 @@ psr_status psr_wait(psr_handle* h);
 psr_status psr_estimate_normals(psr_handle* h, const float* xyz, int count, psr_location location, float* normals,
                                 const float* viewpoint, void* stream);
 
+/* Input adaptor: device array of `count` DepthSurfel records (base/CommonTypes.h:113-118,
+ * 64 bytes each) -> device SoA arrays for psr_points: xyz and normals (3 * count floats),
+ * and rgb (3 * count bytes, round(255 * ColorAndTime.xyz) clamped) unless rgb is NULL.
+ * Replaces getCoordinateAndNormalKernel (mesh/BuildOctree.cu:135-143); enqueued on
+ * `stream` (a cudaStream_t or NULL), no host wait. */
 psr_status psr_surfels_to_points(const void* surfels, int count, float* xyz, float* normals, uint8_t* rgb,
                                  void* stream);
 
@@ -188,8 +195,9 @@ psr_status psr_debug_array(psr_handle* h, const char* name, void* dst, size_t ds
  * file-scope device array (about 9 MB, on every device that loads the library, until
  * exit), so at most 1,048,576 points per call (PSR_OUT_OF_CAPACITY above that).  Calls
  * share that array: calls whose GPU work overlaps race.  The first call on a device
- * looks up the array's address with that device current; make it before any stream
- * capture.  Returns after the work on `stream` (a cudaStream_t or NULL) has completed. */
+ * looks up the array's address with that device current.  Every call synchronises
+ * `stream` (a cudaStream_t or NULL) and returns after its work there has completed, so
+ * it must not be called while any stream of the device is being captured. */
 psr_status psr_morton_sort_noalloc(const float* xyz, int count, int depth, float bbox_scale, uint32_t* codes,
                                    uint32_t* order, void* stream);
 

@@ -15,7 +15,7 @@ reference source (mesh/ComputeTriangleIndices.cu:41-315, the `trianglesCount[256
 The output is committed (poisson-surface-reconstruction-gpu_gb300/csrc/mc_tables.inc);
 re-running this script against the reference must reproduce it byte for byte.
 
-Usage:  python3 oracle/gen_tables.py [reference_root] [output_path]
+Usage:  python3 oracle/gen_tables.py REFERENCE_ROOT [output_path]   (or $PSR_REFERENCE_ROOT)
 """
 import re
 import subprocess
@@ -53,7 +53,11 @@ def _int_block(text: str, name: str, count: int):
 
 
 def main():
-    ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    import os
+    arg = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PSR_REFERENCE_ROOT")
+    if not arg:
+        raise SystemExit("usage: gen_tables.py REFERENCE_ROOT [out] (or set PSR_REFERENCE_ROOT)")
+    ref = Path(arg)
     out = Path(sys.argv[2] if len(sys.argv) > 2 else
                Path(__file__).resolve().parent.parent /
                "poisson-surface-reconstruction-gpu_gb300" / "csrc" / "mc_tables.inc")

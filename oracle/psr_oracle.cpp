@@ -25,6 +25,7 @@
 // build script).  Plain C ABI at the bottom for ctypes.
 
 #include <algorithm>
+#include <cfloat>
 #include <climits>
 #include <cmath>
 #include <cstdint>
@@ -264,8 +265,11 @@ static int build_octree(State& S, const float* xyz, const float* nrm, const floa
     const int D = S.opt.depth;
     S.D = D;
     S.N = n;
-    // bounding box (mesh/BuildOctree.cu:51-133, host finish :121-133)
-    float mx[3] = {-1e6f, -1e6f, -1e6f}, mn[3] = {1e6f, 1e6f, 1e6f};
+    // bounding box (mesh/BuildOctree.cu:51-133, host finish :121-133).  The reference seeds
+    // with -1e6 / 1e6 (mesh/BuildOctree.cpp:87-88, BuildOctree.cu:66-73); -FLT_MAX / FLT_MAX
+    // gives the same box unless every coordinate of an axis lies beyond 1e6 in magnitude,
+    // where the reference's box is wrong and this one is the true box.
+    float mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX}, mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX};
     for (int i = 0; i < n; ++i)
         for (int a = 0; a < 3; ++a) {
             float v = xyz[3 * i + a];

@@ -247,12 +247,9 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     A.add(ws.root_group, (size_t)nodes);
     A.add(ws.root_self, (size_t)nodes);
     // roots beyond this capacity take the walk over their octree chain in the subdivision
-    // scan itself; PSR_ROOT_POLY_CAPACITY lowers it (that path gives the same mesh)
+    // scan itself; psr_config.root_poly_capacity sets it (that path gives the same mesh)
     ws.cap_poly = (int)std::max<long long>(65536, nodes / 16);
-    if (const char* ev = getenv("PSR_ROOT_POLY_CAPACITY")) {
-        const long long v = atoll(ev);
-        if (v > 0 && v < ws.cap_poly) ws.cap_poly = (int)v;
-    }
+    if (cfg.root_poly_capacity > 0) ws.cap_poly = cfg.root_poly_capacity;
     A.add(ws.root_poly, 28 * (size_t)ws.cap_poly);
     A.add(ws.c_vnode, (size_t)subn); A.add(ws.c_key, (size_t)subn); A.add(ws.c_group, (size_t)subn);
     A.add(ws.c_parent, (size_t)subn); A.add(ws.c_jump, (size_t)subn); A.add(ws.c_depth, (size_t)subn);
@@ -346,8 +343,7 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
         prepare_launch_configs(ws);
         e = cudaGetLastError();
     }
-    const char* env = getenv("PSR_NO_GRAPH");
-    if (env && env[0] == '1') h->use_graphs = 0;
+    if (cfg.disable_graphs) h->use_graphs = 0;
     if (e != cudaSuccess) {
         psr_status st = cuda_fail(h, e, "psr_create");
         psr_destroy(h);

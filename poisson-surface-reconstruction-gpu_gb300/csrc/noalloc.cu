@@ -17,8 +17,10 @@
 //     contents (everything that must start at zero is cleared by each call), and calls
 //     whose GPU work overlaps in time race on it;
 //   * the first call on a device looks up the array's device address
-//     (cudaGetSymbolAddress) with that device current; make that first call before any
-//     stream capture.
+//     (cudaGetSymbolAddress) with that device current;
+//   * every call waits for its own work on `stream` (it reads the device error word back
+//     and synchronises that stream), so it must not be called while any stream of the
+//     device is being captured into a CUDA graph.
 #include <mutex>
 
 #include "../../include/psr/psr.h"
@@ -54,15 +56,17 @@ __global__ void k_na_init(NoAllocState* st, int n) {
         st->n = n;
         st->error = 0;
         for (int a = 0; a < 3; ++a) {
-            st->bmax[a] = float_to_ordered(-1e6f);
-            st->bmin[a] = float_to_ordered(1e6f);
+            // seeded like the pipeline's reduction (-FLT_MAX / FLT_MAX), so the two agree
+            // for coordinates of any magnitude
+            st->bmax[a] = float_to_ordered(-FLT_MAX);
+            st->bmin[a] = float_to_ordered(FLT_MAX);
         }
     }
 }
 
 __global__ void __launch_bounds__(kBlock) k_na_bbox(const float* xyz, NoAllocState* st) {
     const int n = st->n;
-    float mx[3] = {-1e6f, -1e6f, -1e6f}, mn[3] = {1e6f, 1e6f, 1e6f};
+    float mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX}, mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX};
     bool bad = false;
     PSR_GRID_STRIDE(i, n) {
         for (int a = 0; a < 3; ++a) {
@@ -176,9 +180,11 @@ extern "C" psr_status psr_morton_sort_noalloc(const float* xyz, int count, int d
         e = cudaMemcpyAsync(codes, sc.keys_alt, 4 * (size_t)count, cudaMemcpyDeviceToDevice, s);
         if (e == cudaSuccess) e = cudaMemcpyAsync(order, sc.vals_alt, 4 * (size_t)count, cudaMemcpyDeviceToDevice, s);
     }
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    // the error word is read on the caller's stream only: no other stream of the device
+    // is waited on
     unsigned err = 0;
-    if (e == cudaSuccess) e = cudaMemcpy(&err, &st->error, sizeof(unsigned), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&err, &st->error, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return PSR_CUDA_ERROR;
     if (err & kErrInvalid) return PSR_INVALID_INPUT;
     if (err & kErrCapacity) return PSR_OUT_OF_CAPACITY;

@@ -92,8 +92,8 @@ __global__ void k_nrm_reset(Counters* c, int n) {
     c->error = 0u;
     c->n_colour_far = 0;
     for (int a = 0; a < 3; ++a) {
-        ((int*)c->bbox_max)[a] = float_to_ordered(-1e6f);
-        ((int*)c->bbox_min)[a] = float_to_ordered(1e6f);
+        ((int*)c->bbox_max)[a] = float_to_ordered(-FLT_MAX);
+        ((int*)c->bbox_min)[a] = float_to_ordered(FLT_MAX);
     }
 }
 

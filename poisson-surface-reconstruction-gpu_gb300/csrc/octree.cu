@@ -21,16 +21,20 @@ __global__ void k_reset_counters(Counters* c, const int* params) {
     if (threadIdx.x == 0) {
         c->n_points = params[0];
         for (int a = 0; a < 3; ++a) {
-            // the reference seeds its reduction with -1e6 / 1e6
-            ((int*)c->bbox_max)[a] = float_to_ordered(-1e6f);
-            ((int*)c->bbox_min)[a] = float_to_ordered(1e6f);
+            // The reference seeds its reduction (padding threads, mesh/BuildOctree.cu:66-73)
+            // and its host finish (mesh/BuildOctree.cpp:87-88) with -1e6 / 1e6, which gives a
+            // wrong box when every coordinate of an axis lies beyond 1e6 in magnitude (a
+            // georeferenced scan).  Seeding with -FLT_MAX / FLT_MAX gives the reference's box
+            // for every other input and the true box for those.
+            ((int*)c->bbox_max)[a] = float_to_ordered(-FLT_MAX);
+            ((int*)c->bbox_min)[a] = float_to_ordered(FLT_MAX);
         }
     }
 }
 
 __global__ void __launch_bounds__(kBlock) k_bbox(const float* xyz, const float* nrm, Counters* c) {
     const int n = c->n_points;
-    float mx[3] = {-1e6f, -1e6f, -1e6f}, mn[3] = {1e6f, 1e6f, 1e6f};
+    float mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX}, mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX};
     bool bad = false;
     PSR_GRID_STRIDE(i, n) {
         for (int a = 0; a < 3; ++a) {

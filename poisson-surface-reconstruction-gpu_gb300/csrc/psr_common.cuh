@@ -1,6 +1,7 @@
 // Common device definitions for the Poisson reconstruction kernels (sm_103a).
 #pragma once
 #include <cuda_runtime.h>
+#include <cfloat>
 #include <cstdint>
 
 namespace psr {

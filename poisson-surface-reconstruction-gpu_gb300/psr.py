@@ -32,7 +32,8 @@ class PsrConfig(ctypes.Structure):
                 ("cg_max_iterations", ctypes.c_int), ("cg_tolerance", ctypes.c_float),
                 ("compute_colors", ctypes.c_int), ("compute_normals", ctypes.c_int), ("device", ctypes.c_int),
                 ("laplacian_epsilon", ctypes.c_float), ("concurrent_stages", ctypes.c_int),
-                ("weld_vertices", ctypes.c_int)]
+                ("weld_vertices", ctypes.c_int), ("disable_graphs", ctypes.c_int),
+                ("root_poly_capacity", ctypes.c_int)]
 
 
 class PsrPoints(ctypes.Structure):
@@ -138,7 +139,8 @@ class PoissonReconstruction:
 
     def __init__(self, max_depth=7, max_points=300000, max_triangles=1000000, max_mesh_vertices=300000,
                  compute_colors=False, compute_normals=False, cg_tolerance=1e-5, cg_max_iterations=10000,
-                 max_nodes=0, max_subdivision_nodes=0, device=0, laplacian_epsilon=1e-6, concurrent_stages=True, weld_vertices=False):
+                 max_nodes=0, max_subdivision_nodes=0, device=0, laplacian_epsilon=1e-6, concurrent_stages=True, weld_vertices=False,
+                 disable_graphs=False, root_poly_capacity=0):
         self._lib = load_library()
         cfg = default_config()
         cfg.max_depth = max_depth
@@ -155,6 +157,8 @@ class PoissonReconstruction:
         cfg.laplacian_epsilon = laplacian_epsilon
         cfg.concurrent_stages = int(concurrent_stages)
         cfg.weld_vertices = int(weld_vertices)
+        cfg.disable_graphs = int(disable_graphs)
+        cfg.root_poly_capacity = int(root_poly_capacity)
         self.config = cfg
         h = ctypes.c_void_p()
         st = self._lib.psr_create(ctypes.byref(cfg), ctypes.byref(h))

@@ -74,8 +74,11 @@ class Server:
                                           max_mesh_vertices=max_mesh_vertices, compute_colors=compute_colors,
                                           compute_normals=compute_normals, device=device,
                                           **{"concurrent_stages": False, **caps})
-            if memory_budget is not None and k > 0 and (k + 1) * r.memory_bytes() > memory_budget:
+            if memory_budget is not None and (k + 1) * self.slot_bytes(r) > memory_budget:
                 r.close()
+                if k == 0:
+                    raise ValueError(f"memory_budget {memory_budget} B is below one slot "
+                                     f"({self.slot_bytes(r)} B: workspace and output buffers)")
                 break
             def buf(shape, dtype):
                 if host_outputs:
@@ -87,6 +90,16 @@ class Server:
             self.slots.append(_Slot(r, torch.cuda.Stream(self.dev), out))
         self.queue = []
         self.done = []
+
+    def slot_bytes(self, recon):
+        """Device bytes of one slot: the handle's workspace plus its output mesh buffers
+        (vertices, triangles, and colours / normals when computed; none on the device when
+        outputs go to pinned host memory)."""
+        out = 0
+        if not self.host_outputs:
+            per_vertex = 12 * (1 + int(self.compute_colors) + int(self.compute_normals))
+            out = per_vertex * self.vcap + 12 * self.tcap
+        return recon.memory_bytes() + out
 
     def close(self):
         for sl in self.slots:

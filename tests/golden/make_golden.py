@@ -11,7 +11,9 @@
    mesh/ComputeTriangleIndices.cu:31-38,317-322, mesh/BuildMeshGeometry.cu:19-26), parsed
    from the source text -> ref_luts.json.
 
-Usage: python3 tests/golden/make_golden.py [reference_root]
+   It also holds the marching-cubes case table (mesh/ComputeTriangleIndices.cu:41-315).
+
+Usage: python3 tests/golden/make_golden.py REFERENCE_ROOT (or with $PSR_REFERENCE_ROOT set)
 """
 import json
 import re
@@ -28,7 +30,7 @@ ROOT = HERE.parent.parent
 def tables(depth):
     exe = ROOT / "oracle" / "_ref" / "ref_tables"
     if not exe.exists():
-        subprocess.run(["sh", str(ROOT / "oracle" / "build_ref.sh")], check=True)
+        subprocess.run(["sh", str(ROOT / "oracle" / "build_ref.sh"), str(reference_root())], check=True)
     out = subprocess.run([str(exe), str(depth)], check=True, capture_output=True, text=True).stdout
     pieces, rows = [], []
     res = None
@@ -76,12 +78,25 @@ def luts(ref):
         "face_edges": _array(tri_src, "faceEdges[6][4]", 24),
         "children_vertex_kind": _array(tri_src, "childrenVertexKind[8]", 8),
         "parent_face_kind": _array(geo_src, "parentFaceKind[8][6]", 48),
+        # marching-cubes case table (mesh/ComputeTriangleIndices.cu:41-315): triangle count
+        # and the 16-entry edge list (-1 terminated) of every cube class
+        "mc_count": _array(tri_src, "trianglesCount[256]", 256),
+        "mc_triangles": _array(tri_src, "triangles[256][16]", 256 * 16),
     }
     (HERE / "ref_luts.json").write_text(json.dumps(out))
 
 
+def reference_root():
+    """The reference tree: first argument, else $PSR_REFERENCE_ROOT."""
+    import os
+    arg = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PSR_REFERENCE_ROOT")
+    if not arg:
+        raise SystemExit("usage: make_golden.py REFERENCE_ROOT (or set PSR_REFERENCE_ROOT)")
+    return Path(arg)
+
+
 if __name__ == "__main__":
-    ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = reference_root()
     tables(3)
     tables(6)
     luts(ref)

@@ -234,7 +234,7 @@ def test_deterministic(recon):
     np.testing.assert_array_equal(a.triangles, b.triangles)
 
 
-def test_root_polynomial_fallback_same_mesh(monkeypatch):
+def test_root_polynomial_fallback_same_mesh():
     # subdivision roots beyond the root-polynomial capacity sum their octree chain in the
     # level scan itself: with a capacity of one root that path runs for nearly every root
     import psr
@@ -243,8 +243,7 @@ def test_root_polynomial_fallback_same_mesh(monkeypatch):
     with psr.PoissonReconstruction(**caps) as r:
         a = r.SolvePoissionReconstructionMesh(p, nr, rgb, depth=7)
         roots = r.stats().subdivision_roots
-    monkeypatch.setenv("PSR_ROOT_POLY_CAPACITY", "1")
-    with psr.PoissonReconstruction(**caps) as r:
+    with psr.PoissonReconstruction(root_poly_capacity=1, **caps) as r:
         b = r.SolvePoissionReconstructionMesh(p, nr, rgb, depth=7)
     assert roots > 1
     np.testing.assert_array_equal(a.vertices, b.vertices)

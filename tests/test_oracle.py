@@ -52,7 +52,25 @@ def test_luts_match_reference_constants(oracle_mod):
     ref = json.loads((GOLDEN / "ref_luts.json").read_text())
     mine = oracle_mod.luts()
     for k, v in ref.items():
+        if k.startswith("mc_"):
+            continue   # the case table: test_mc_table_matches_reference_case_table
         assert mine[k] == v, k
+
+
+def test_mc_table_matches_reference_case_table(oracle_mod):
+    """The case table the kernels and the oracle decode (csrc/mc_tables.inc) equals the
+    reference's trianglesCount[256] / triangles[256][16] (mesh/ComputeTriangleIndices.cu:
+    41-315), parsed from the reference source: same triangle count, same edges, same order
+    and so the same winding, for every cube class."""
+    ref = json.loads((GOLDEN / "ref_luts.json").read_text())
+    counts, edges = oracle_mod.mc_tables()
+    tri = np.array(ref["mc_triangles"]).reshape(256, 16)
+    assert counts == ref["mc_count"]
+    for c in range(256):
+        row = list(tri[c])
+        want = row[:row.index(-1)] if -1 in row else row
+        assert len(want) == 3 * ref["mc_count"][c], c
+        assert edges[c] == want, c
 
 
 def test_mc_table_uses_exactly_the_crossing_edges(oracle_mod):

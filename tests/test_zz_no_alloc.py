@@ -18,10 +18,13 @@ pytestmark = pytest.mark.gpu
 
 
 def _reference_order(xyz, nrm, depth):
-    """Sorted normalised positions and per-point codes from the full pipeline."""
+    """Sorted normalised positions and per-point codes from the full pipeline (a few CG
+    iterations and every Laplacian entry kept: only the octree is compared)."""
     import psr
-    with psr.PoissonReconstruction(max_depth=depth, max_points=max(len(xyz), 300000)) as r:
-        mesh = r.SolvePoissionReconstructionMesh(xyz, nrm, depth=depth)
+    with psr.PoissonReconstruction(max_depth=depth, max_points=max(len(xyz), 300000),
+                                   laplacian_epsilon=0.0, max_triangles=4000000,
+                                   max_mesh_vertices=2000000) as r:
+        mesh = r.SolvePoissionReconstructionMesh(xyz, nrm, depth=depth, cg_iterations=4)
         st = r.stats()
         px, py, pz = (r.debug(n, np.float32) for n in ("px", "py", "pz"))
         key = r.debug("key")
@@ -46,10 +49,25 @@ def _noalloc(xyz, depth):
     return d_codes.cpu().numpy().view(np.uint32), d_order.cpu().numpy()
 
 
-@pytest.mark.parametrize("calls", [[("torus_ellipsoid200k", None, 7), ("sphere20k", 5000, 6)]])
+def _far_cloud(n):
+    """A sphere of radius 1e5 centred near (1e7, -2e7, 3e7): every coordinate of every
+    axis lies beyond 1e6 in magnitude (a georeferenced scan)."""
+    xyz, nrm, _, _ = syn.workload("sphere20k", n=n)
+    far = xyz.astype(np.float64) * 1e5 + np.array([1e7, -2e7, 3e7])
+    return far.astype(np.float32), nrm
+
+
+# depths 7 and 6 take three radix passes (the result lands in the scratch and is copied
+# back), depths 5 and 9 an even number (sorted in place)
+@pytest.mark.parametrize("calls", [[("torus_ellipsoid200k", None, 7), ("sphere20k", 5000, 6)],
+                                   [("sphere20k", 20000, 5), ("sphere20k", 20000, 9)],
+                                   [("far", 20000, 6), ("far", 20000, 6)]])
 def test_noalloc_sort_matches_pipeline_twice(calls):
     for name, n, depth in calls:
-        xyz, nrm, _, _ = syn.workload(name, n=n)
+        if name == "far":
+            xyz, nrm = _far_cloud(n)
+        else:
+            xyz, nrm, _, _ = syn.workload(name, n=n)
         sorted_pos, codes_ref, center, scale = _reference_order(xyz, nrm, depth)
         codes, order = _noalloc(xyz, depth)
         np.testing.assert_array_equal(codes, codes_ref)
