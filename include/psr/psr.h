@@ -71,6 +71,13 @@ typedef struct psr_config {
                                   this many evaluate the levels above them by walking their
                                   octree chain instead of from one cached polynomial per root
                                   (same mesh, slower) */
+    int cg_residual_period;    /* CG iterative refinement: the true residual b - A x (exact
+                                  products, double-float sums, FP64 norm) is evaluated every
+                                  this many iterations and when the recursive residual reaches
+                                  the tolerance; the CG restarts from it when it is above the
+                                  tolerance and the floor of an FP32 solution (2^-20 ||b||).
+                                  0 (default): every 32 iterations; -1: never (the reference's
+                                  recursive residual only, mesh/solver/CGAlgorithm.cu:36-75) */
 } psr_config;
 
 /* Oriented input cloud (the fields of DepthSurfel, base/CommonTypes.h:113-118, as SoA). */
@@ -113,7 +120,8 @@ typedef struct psr_stats {
     int subdivision_roots, subdivision_nodes;
     int mesh_vertices, mesh_triangles;
     int cg_iterations[10];
-    double cg_residual[10];
+    double cg_residual[10]; /* ||r|| of the recursive residual at the end of each depth's CG
+                               (the reference's stopping quantity) */
     float iso_value;
     unsigned error_bits;
     float stage_ms[6];     /* octree, field, solve, mesh, transfer, total (device time) */
@@ -121,6 +129,10 @@ typedef struct psr_stats {
     int graph_replay;      /* 1 when the call replayed a captured CUDA graph */
     float cg_kernel_ms;    /* device time of the CG kernel alone (part of stage_ms[2]) */
     float cg_depth_ms[10]; /* device time of each depth's CG (depths solve concurrently) */
+    double cg_true_residual[10]; /* ||b - A x|| of each depth at its last true-residual
+                                    evaluation (exact products, FP64 norm); -1: none */
+    int cg_residual_checks[10];  /* true-residual evaluations of each depth's CG */
+    int cg_restarts[10];         /* refinement restarts from the true residual */
 } psr_stats;
 
 typedef struct psr_handle psr_handle;

@@ -38,6 +38,7 @@ def lib():
         L.oro_create.restype = ctypes.c_void_p
         L.oro_destroy.argtypes = [ctypes.c_void_p]
         L.oro_set_lap_eps.argtypes = [ctypes.c_void_p, ctypes.c_double]
+        L.oro_set_tables.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 5
         L.oro_run.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                               ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
                               ctypes.c_int, ctypes.c_int, ctypes.c_int]
@@ -96,6 +97,15 @@ class Oracle:
         self._h = lib().oro_create()
         if laplacian_epsilon is not None:   # default: the reference's 1e-6 drop threshold
             lib().oro_set_lap_eps(self._h, float(laplacian_epsilon))
+
+    def set_tables(self, res, i, j, ff, dff, d2):
+        """Solve the following runs (of the depth with this res) on the given table entries
+        instead of the exact integrals; res = 0 goes back to the exact tables."""
+        arrs = [np.ascontiguousarray(i, np.int32), np.ascontiguousarray(j, np.int32),
+                np.ascontiguousarray(ff, np.float64), np.ascontiguousarray(dff, np.float64),
+                np.ascontiguousarray(d2, np.float64)]
+        self._keept = arrs
+        lib().oro_set_tables(self._h, int(res), int(arrs[0].shape[0]), *[_ptr(a) for a in arrs])
 
     def __del__(self):
         try:

@@ -1534,6 +1534,7 @@ struct OracleHandle {
     State S;
     double lap_eps = (double)1e-6f;
     std::map<std::string, std::vector<char>> scratch;
+    Tables given;            // tables supplied by the caller (res 0: none)
 };
 
 extern "C" {
@@ -1544,6 +1545,26 @@ void oro_destroy(void* h) { delete (OracleHandle*)h; }
 // Drop threshold of the Laplacian entries for the following runs (the reference's 1e-6
 // by default; 0 keeps every entry).
 void oro_set_lap_eps(void* h, double eps) { ((OracleHandle*)h)->lap_eps = eps; }
+
+// Tables for the following runs instead of the exact integrals: `count` entries (i, j) of
+// <F,F>, <F',F>, <F',F'> (every other entry zero) for runs whose depth gives this `res`
+// (2^(depth+1) - 1).  Used to solve on the reference's own tables (mesh/FunctionData.h
+// setDotTables, float polynomial arithmetic).  res = 0 goes back to the exact tables.
+void oro_set_tables(void* hp, int res, int count, const int* i, const int* j, const double* ff, const double* dff,
+                    const double* d2) {
+    OracleHandle* h = (OracleHandle*)hp;
+    Tables& t = h->given;
+    t.res = res;
+    t.ff.assign((size_t)res * res, 0.0);
+    t.dff.assign((size_t)res * res, 0.0);
+    t.d2.assign((size_t)res * res, 0.0);
+    for (int k = 0; k < count; ++k) {
+        const size_t at = (size_t)i[k] + (size_t)res * j[k];
+        t.ff[at] = ff[k];
+        t.dff[at] = dff[k];
+        t.d2[at] = d2[k];
+    }
+}
 
 // Runs the pipeline up to `stop_after` (1 octree, 2 field, 3 solve, 4 mesh, 5 colour).
 // cg_iters > 0 selects a fixed iteration count per depth; otherwise CG stops when
@@ -1564,7 +1585,8 @@ int oro_run(void* hp, const float* xyz, const float* nrm, const float* rgb, int 
     if (n <= 0 || depth < 2 || depth > 9) return 2;
     build_octree(S, xyz, nrm, rgb, n);
     if (stop_after <= 1) return 0;
-    S.tab.build(depth);
+    if (h->given.res == (1 << (depth + 1)) - 1) S.tab = h->given;
+    else S.tab.build(depth);
     compute_field(S);
     if (stop_after <= 2) return 0;
     solve(S);

@@ -26,6 +26,9 @@ void build_stencil(int depth, std::vector<float>& st, double eps);
 
 using namespace psr;
 
+// CG iterations between true-residual evaluations (psr_config.cg_residual_period = 0)
+constexpr int kDefaultResidualPeriod = 32;
+
 struct DebugArray {
     const void* ptr;
     int elem;        // bytes per element
@@ -454,7 +457,9 @@ static psr_status submit_impl(psr_handle* h, const psr_points* pts, const psr_op
         if (q == cudaSuccess) q = field_build(ws);
         if (q == cudaSuccess) q = cudaEventRecordWithFlags(h->ev[2], qs, cudaEventRecordExternal);
         if (q == cudaSuccess)
-            q = solve_build(ws, cg_iters > 0 ? 1 : 0, cg_iters, h->cfg.cg_tolerance, h->cfg.cg_max_iterations);
+            q = solve_build(ws, cg_iters > 0 ? 1 : 0, cg_iters, h->cfg.cg_tolerance, h->cfg.cg_max_iterations,
+                            h->cfg.cg_residual_period == 0 ? kDefaultResidualPeriod
+                                                           : (h->cfg.cg_residual_period < 0 ? -1 : h->cfg.cg_residual_period));
         if (q == cudaSuccess) q = cudaEventRecordWithFlags(h->ev[3], qs, cudaEventRecordExternal);
         if (q == cudaSuccess && overlap) q = cudaStreamWaitEvent(qs, ws.ev_join2, 0);
         if (q == cudaSuccess) q = mesh_build(ws);
@@ -546,7 +551,9 @@ static psr_status complete_impl(psr_handle* h) {
     psr_stats& st = h->stats;
     memset(&st, 0, sizeof(st));
     st.points = c.n_points; st.unique_leaves = c.n_unique; st.nodes = c.n_nodes; st.depth = depth;
-    for (int d = 0; d <= kMaxDepth; ++d) { st.level_count[d] = c.level_count[d]; st.cg_iterations[d] = c.cg_iters[d]; st.cg_residual[d] = c.cg_rr[d] > 0 ? sqrt(c.cg_rr[d]) : 0.0; }
+    for (int d = 0; d <= kMaxDepth; ++d) { st.level_count[d] = c.level_count[d]; st.cg_iterations[d] = c.cg_iters[d]; st.cg_residual[d] = c.cg_rr[d] > 0 ? sqrt(c.cg_rr[d]) : 0.0;
+        st.cg_true_residual[d] = c.cg_rr_true[d] >= 0 ? sqrt(c.cg_rr_true[d]) : -1.0;
+        st.cg_residual_checks[d] = c.cg_checks[d]; st.cg_restarts[d] = c.cg_restarts[d]; }
     st.vertices = c.n_vertices; st.edges = c.n_edges; st.faces = c.n_faces;
     st.crossings = c.n_cross; st.triangles = c.n_tri;
     st.subdivision_roots = c.n_subroots; st.subdivision_nodes = c.n_sub_nodes;
@@ -728,6 +735,12 @@ psr_status psr_debug_array(psr_handle* h, const char* name, void* dst, size_t ds
     else if (nm == "sv_value") one(ws.sv_value, 4 * (size_t)c.n_sub_vertices);
     else if (nm == "s_cube_class") one(ws.s_cube_class, 4 * (size_t)c.n_sub_dnodes);
     else if (nm == "sub_live_vnode") one(ws.lv_vnode, 4 * (size_t)c.n_sub_dnodes);
+    else if (nm == "bbox") {   // the normalisation of the last run: center[3], max edge (4 floats)
+        const float v[4] = {c.center[0], c.center[1], c.center[2], c.max_edge};
+        if (bytes) *bytes = sizeof(v);
+        if (dst && dst_bytes >= sizeof(v)) memcpy(dst, v, sizeof(v));
+        return PSR_OK;
+    }
     else if (nm == "counters") { if (bytes) *bytes = sizeof(Counters); if (dst && dst_bytes >= sizeof(Counters)) memcpy(dst, &c, sizeof(Counters)); return PSR_OK; }
     else return fail(h, PSR_INVALID_INPUT, "unknown array name");
     size_t total = 0;

@@ -49,7 +49,10 @@ struct Counters {
     double iso_sum;
     float iso;
     int cg_iters[kMaxDepth + 1];
-    double cg_rr[kMaxDepth + 1];
+    double cg_rr[kMaxDepth + 1];      // recursive r.r at the end of each depth's CG (FP64)
+    double cg_rr_true[kMaxDepth + 1]; // r.r of the last true residual b - A x (-1: none)
+    int cg_checks[kMaxDepth + 1];     // true-residual evaluations of each depth's CG
+    int cg_restarts[kMaxDepth + 1];   // refinement restarts from the true residual
     unsigned long long cg_depth_ns[kMaxDepth + 1];   // device time of each depth's CG
 };
 
@@ -322,6 +325,17 @@ __device__ __forceinline__ FF ff_warp_sum(FF v) {
 }
 
 __device__ __forceinline__ float ff_to_float(FF a) { return __fadd_rn(a.hi, a.lo); }
+
+// the pair as one FP64 value (hi and lo are floats, so each converts exactly)
+__device__ __forceinline__ double ff_to_double(FF a) { return (double)a.hi + (double)a.lo; }
+
+// FP64 warp-wide sum (butterfly; IEEE addition is commutative, so every lane ends with the
+// same value, in a fixed order)
+__device__ __forceinline__ double dbl_warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
 
 // a / b rounded to float: float quotient of the leading parts, then one correction step
 // with the remainder a - q b evaluated with fused multiply-adds

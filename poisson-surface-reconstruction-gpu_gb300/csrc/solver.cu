@@ -8,8 +8,14 @@
 //
 // CG (mesh/solver/CGAlgorithm.cu:10-80): x0 = 0, r0 = b, stops when r.r <= tol^2 or after
 // max_iter iterations (or after a fixed count).  All depths are independent; they are
-// solved together in one launch of two thread-block clusters (see k_cg_cluster), with
-// per-depth FP64 reductions in a fixed order (deterministic) and per-depth updates.
+// solved together in concurrent launches of thread-block clusters (see k_cg_cluster).
+// Precision: the operator, the vectors and the updates are FP32; the dot products and
+// residual norms are FP64 quantities (exact products, double-float sums within a warp, FP64
+// sums across warps and CTAs, in a fixed order).  Every res_period iterations and when the
+// recursive residual reaches the tolerance, the true residual b - A x of the current x is
+// evaluated (exact products, double-float sums, FP64 norm); it drives iterative refinement:
+// the CG restarts from it when it is above both the tolerance and the floor an FP32
+// solution can reach (2^-20 ||b||) and the recursive residual has converged or drifted.
 //
 // Iso-value (:269-305): mean of the implicit function at the sample points, evaluated in
 // FP32 per point and averaged in FP64.
@@ -30,13 +36,32 @@ namespace psr {
 // launched concurrently on a second stream).  Both run the same solver body: a cluster
 // of one CTA is a CTA.
 //
-// Reductions: each CTA sums its threads' terms (warp butterflies, then one warp over the
-// warp partials), writes the sum to its shared memory, and after the barrier one warp of
-// every CTA sums the CTAs' values in a fixed order, so every CTA holds the same result.
-// Sums are float pairs (FF: GB300's FP64 rate is far below its FP32 rate) and products
-// enter exactly (fma), so p.Ap and r.r carry about 44 bits.  The partial buffers
-// alternate between two slots, so a slot is only rewritten after a barrier that follows
-// its reads.
+// Reductions: every product enters exactly (fma: TwoProduct) into a per-thread float pair,
+// warp butterflies sum the pairs (FF arithmetic on the FP32 pipes), one warp per CTA sums
+// the 32 warp partials in FP64 and writes the CTA's sum to its shared memory, and after
+// the barrier one warp of every CTA sums the CTAs' values in FP64 in a fixed order, so
+// every CTA holds the same result.  GB300 executes FP64 at a small fraction of its FP32
+// rate (an FP64 add per element cost 2.4 us per reduction against 0.3 us for the
+// cluster barrier), so FP64 arithmetic is kept to the 32 + 16 values of the cross-warp
+// and cross-CTA steps; the in-warp pairs carry about 44 bits, more than the reference's
+// float-rounded products summed in double (mesh/solver/CGAlgorithm.cu:106-133).  The
+// scalars of an iteration (alpha, beta, the continue flag) are computed once, by the
+// thread that finishes the sum, and read by every thread from shared memory.  The
+// partial buffers alternate between two slots, so a slot is only rewritten after a
+// barrier that follows its reads.
+//
+// True residual (iterative refinement): every res_period iterations, and when the
+// recursive r.r reaches tol^2, each row's b - sum_k st_k x[nb_k] is evaluated with exact
+// products and float-pair sums (staged in the A p buffer) and its FP64 norm is taken.  With
+// the reference's absolute tolerance (1e-5) and right-hand sides of norm ~1e7, the FP32
+// recursion ends with a true residual near 1e-7 ||b||, below what an FP32 x can resolve
+// (2^-20 ||b||, 16 ulps of b); refinement restarts the CG from the true residual only
+// above that floor (and the tolerance), when the recursive residual has converged or has
+// drifted below the true one by more than 2x in norm, at most kCgMaxRefine times and while
+// each restart cuts the true r.r fourfold.  Replacing r periodically while keeping the
+// direction was tried and fails at this scale: beta = r_true.r_true / r_old.r_old mixes a
+// true residual at the FP32 floor with a recursive one far below it and the iteration
+// stalls (it ran to the 10,000-iteration cap on the depth-3 system of the superquadric).
 //
 // One iteration costs two barriers: the direction update p = r + beta p is fused into the
 // operator application (a row's neighbours rebuild their p values from r and the
@@ -67,6 +92,8 @@ constexpr size_t kCgBlockBytes = (size_t)kCgWarps * kCgWarpBlockFloats * sizeof(
 constexpr size_t kCgSmemBytes = (size_t)kCgSmemRows * kCgRowBytes + kCgBlockBytes;
 static_assert(kCgSmemRows % 32 == 0, "whole warp slots");
 
+constexpr int kCgMaxRefine = 4;
+
 struct CgcArgs {
     const Counters* c;
     Counters* cw;
@@ -84,15 +111,28 @@ struct CgcArgs {
     float* ap;
     float tol2;
     int max_iter;
+    int res_period;     // > 0: true residual every res_period iterations; 0: only at
+                        // convergence; < 0: never (the recursive residual alone)
     float stp[3][27];   // stencils of units 0..2 of k_cg_cluster (depth first - u)
 };
 
 struct CgcShared {
     FF warp[kCgWarps];
-    FF slot[2];
-    FF sum;
+    double slot[2];
+    double rr;          // r.r of the recursive residual (FP64)
+    double rr_prev;     // the same one iteration earlier
+    double pap;
+    double floor2;      // (2^-20 ||b||)^2: what the true residual of an FP32 solution can reach
+    double rr_true;     // r.r of the last true residual (-1: none yet)
+    float alpha, beta;
+    int go;             // the iteration continues
+    int check;          // the true residual is due
+    int replace;        // the true residual replaces r (a refinement restart)
+    int checks;         // true-residual evaluations
+    int restarts;       // refinement restarts
     float st[27];
 };
+static_assert(kCgWarps == 32, "one FP64 lane per warp partial");
 static_assert(kCgSmemBytes + sizeof(CgcShared) <= 227 * 1024, "shared memory of one CTA");
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -101,28 +141,83 @@ __device__ __forceinline__ unsigned long long global_ns() {
     return t;
 }
 
-// Sum of every thread's `v` over the cluster, returned to every thread.  Contains the
-// cluster barrier; identical in every CTA.
-__device__ __forceinline__ FF cgc_allreduce(cg::cluster_group& cl, CgcShared& sh, int& buf, FF v) {
+// Sum of every thread's `v` over the cluster (FP64).  Thread 0 hands the sum to `post`,
+// which sets the shared scalars the next step reads; every thread sees them when this
+// returns.  Contains the cluster barrier; identical in every CTA.
+template <class Post>
+__device__ __forceinline__ void cgc_allreduce(cg::cluster_group& cl, CgcShared& sh, int& buf, FF v, Post post) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     v = ff_warp_sum(v);
     if (lane == 0) sh.warp[warp] = v;
     __syncthreads();
     if (warp == 0) {
-        FF w = ff_warp_sum(sh.warp[lane]);
+        const double w = dbl_warp_sum(ff_to_double(sh.warp[lane]));
         if (lane == 0) sh.slot[buf] = w;
     }
     cl.sync();
     if (warp == 0) {
         const unsigned nb = cl.num_blocks();
-        FF w = ff_zero();
+        double w = 0.0;
         if ((unsigned)lane < nb) w = *cl.map_shared_rank(&sh.slot[buf], (unsigned)lane);
-        w = ff_warp_sum(w);
-        if (lane == 0) sh.sum = w;
+        w = dbl_warp_sum(w);
+        if (lane == 0) post(w);
     }
     buf ^= 1;
     __syncthreads();
-    return sh.sum;
+}
+
+// After the r.r reduction of an iteration (thread 0): beta, the continue flag and whether
+// the true residual is due.  `it` is the iteration just completed.
+__device__ __forceinline__ void cg_after_rr(CgcShared& sh, const CgcArgs& a, double w, int it) {
+    sh.beta = (sh.rr != 0.0) ? (float)(w / sh.rr) : 0.0f;
+    sh.rr_prev = sh.rr;
+    sh.rr = w;
+    const bool conv = !((float)w > a.tol2);   // the reference compares a float r.r (CGAlgorithm.cu:36)
+    const bool more = sh.pap != 0.0 && it + 1 <= a.max_iter;
+    sh.go = !conv && more;
+    sh.check = a.res_period >= 0 && sh.pap != 0.0 &&
+               (conv || (a.res_period > 0 && it % a.res_period == 0 && more));
+}
+
+// After the true-residual reduction (thread 0).  The CG restarts from the true residual
+// (beta = 0: one cycle of iterative refinement) when that residual is above both the
+// tolerance and the floor an FP32 solution can reach, and either the recursive residual
+// has converged or has drifted more than 2x (in norm) below the true one; at most
+// kCgMaxRefine restarts, each one reducing the true r.r at least fourfold.  `it` is the
+// next iteration's number.
+__device__ __forceinline__ void cg_after_true(CgcShared& sh, const CgcArgs& a, double w, int it) {
+    ++sh.checks;
+    const double target = fmax((double)a.tol2, sh.floor2);
+    const bool drift = w > 4.0 * fmax(sh.rr, sh.floor2);
+    const bool falling = sh.rr_true < 0.0 || w < 0.25 * sh.rr_true;
+    sh.replace = w > target && (!sh.go || drift) && sh.restarts < kCgMaxRefine && it <= a.max_iter && falling;
+    if (sh.replace) {
+        ++sh.restarts;
+        sh.beta = 0.0f;
+        sh.go = 1;
+        sh.rr = w;
+    }
+    sh.rr_true = w;
+}
+
+// Start of a solve (thread 0): r0 = b, so r.r is also ||b||^2.
+__device__ __forceinline__ void cg_start(CgcShared& sh, const CgcArgs& a, double w) {
+    sh.rr = w;
+    sh.beta = 0.0f;
+    sh.go = ((float)w > a.tol2) && a.max_iter >= 1;
+    sh.floor2 = w * 0x1p-40;
+    sh.rr_true = -1.0;
+    sh.checks = 0;
+    sh.restarts = 0;
+    sh.replace = 0;
+}
+
+// Per-depth results of a finished solve (thread 0 of cluster CTA 0).
+__device__ __forceinline__ void cg_report(const CgcArgs& a, int d, const CgcShared& sh) {
+    a.cw->cg_rr[d] = sh.rr;
+    a.cw->cg_rr_true[d] = sh.rr_true;
+    a.cw->cg_checks[d] = sh.checks;
+    a.cw->cg_restarts[d] = sh.restarts;
 }
 
 // position of neighbour k (9 ox + 3 oy + oz) of sibling s (x = 4, y = 2, z = 1) in the
@@ -164,6 +259,16 @@ __device__ __forceinline__ float2 cg_ld_pair(unsigned cur_sa, unsigned desc) {
     return v;
 }
 constexpr int kCgZeroRow = kCgSmemRows - 1;   // kept (0, 0) in both buffers: absent neighbours
+
+// x of the row whose (r, p) pair a descriptor addresses: the x array holds one float per
+// row, so the row's byte offset in the pair buffer halves
+__device__ __forceinline__ float cg_ld_x(unsigned x_sa, unsigned desc) {
+    unsigned ra;
+    float v;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(x_sa + ((desc & 0xffffffu) >> 1)), "r"(desc >> 24));
+    asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(ra));
+    return v;
+}
 
 // Resident path.  CTA k of the cluster owns rows [row0 + k*chunk, row0 + (k+1)*chunk).
 // U >= 0: the cluster unit whose stencil is a launch parameter (a.stp[U]), read as a
@@ -207,6 +312,7 @@ __device__ __forceinline__ void cgc_resident(cg::cluster_group& cl, CgcShared& s
     if (threadIdx.x == 0) {
         rp0[kCgZeroRow] = make_float2(0.0f, 0.0f);
         rp1[kCgZeroRow] = make_float2(0.0f, 0.0f);
+        sx[kCgZeroRow] = 0.0f;
     }
     // r0 = b, p_{-1} = 0, x0 = 0
     FF acc = ff_zero();
@@ -217,14 +323,13 @@ __device__ __forceinline__ void cgc_resident(cg::cluster_group& cl, CgcShared& s
         acc = ff_add(acc, ff_prod(bi, bi));
     }
     int buf = 0;
-    FF rr = cgc_allreduce(cl, sh, buf, acc);
-    bool active = ff_to_float(rr) > a.tol2;
+    cgc_allreduce(cl, sh, buf, acc, [&](double w) { cg_start(sh, a, w); });
     bool ran = false;
-    float beta = 0.0f;
     float2* cur = rp0;
     float2* nxt = rp1;
     int it = 1;
-    while (active && it <= a.max_iter) {
+    while (sh.go) {
+        const float beta = sh.beta;
         // (A) own p_k, A p_k from the neighbours' (r_k, p_{k-1}), p.Ap
         acc = ff_zero();
         // the block-table entries of the warp's next slot are loaded while the current
@@ -267,8 +372,11 @@ __device__ __forceinline__ void cgc_resident(cg::cluster_group& cl, CgcShared& s
             }
             __syncwarp();
         }
-        const FF pap = cgc_allreduce(cl, sh, buf, acc);
-        const float alpha = (pap.hi != 0.0f) ? ff_div(rr, pap) : 0.0f;
+        cgc_allreduce(cl, sh, buf, acc, [&](double w) {
+            sh.pap = w;
+            sh.alpha = (w != 0.0) ? (float)(sh.rr / w) : 0.0f;
+        });
+        const float alpha = sh.alpha;
         // (B) x and r, r.r
         acc = ff_zero();
         for (int sl = warp; sl < nslot; sl += kCgWarps) {
@@ -281,22 +389,56 @@ __device__ __forceinline__ void cgc_resident(cg::cluster_group& cl, CgcShared& s
                 acc = ff_add(acc, ff_prod(ri, ri));
             }
         }
-        const FF rn = cgc_allreduce(cl, sh, buf, acc);
-        beta = (rr.hi != 0.0f) ? ff_div(rn, rr) : 0.0f;
-        rr = rn;
+        cgc_allreduce(cl, sh, buf, acc, [&](double w) { cg_after_rr(sh, a, w, it); });
         ran = true;
         if (me == 0 && threadIdx.x == 0) a.cw->cg_iters[u.d] = it;
-        active = (ff_to_float(rn) > a.tol2) && pap.hi != 0.0f && it + 1 <= a.max_iter;
         float2* t = cur;
         cur = nxt;
         nxt = t;
         ++it;
+        if (sh.check) {
+            // (C) true residual b - A x of the current x from the neighbours' x (the barrier
+            // of the last reduction published every CTA's x), with exact products and
+            // float-pair sums; staged in the A p buffer, which holds nothing live here
+            acc = ff_zero();
+            const unsigned x_sa = (unsigned)__cvta_generic_to_shared(sx);
+            for (int sl = warp; sl < nslot; sl += kCgWarps) {
+                const int l = sl * 32 + lane;
+                const bool mine = l < nloc;
+                if (mine) {
+                    const int4* bp = reinterpret_cast<const int4*>(a.blk + (size_t)(gbase + (l >> 3)) * 64 + sib * 8);
+                    const int4 d0 = bp[0], d1 = bp[1];
+                    const int ids[8] = {d0.x, d0.y, d0.z, d0.w, d1.x, d1.y, d1.z, d1.w};
+                    float vals[8];
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) vals[e] = cg_ld_x(x_sa, (unsigned)ids[e]);
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) myblk[e * 8 + sib] = vals[e];
+                }
+                __syncwarp();
+                if (mine) {
+                    FF y = ff_zero();
+#pragma unroll
+                    for (int k = 0; k < 27; ++k)
+                        y = ff_add(y, ff_prod(U >= 0 ? a.stp[U < 0 ? 0 : U][k] : sh.st[k], myblk[spos + cg_kpos(k)]));
+                    const float ri = ff_to_float(ff_add(FF{a.b[mlo + l], 0.0f}, FF{-y.hi, -y.lo}));
+                    sap[l] = ri;
+                    acc = ff_add(acc, ff_prod(ri, ri));
+                }
+                __syncwarp();
+            }
+            cgc_allreduce(cl, sh, buf, acc, [&](double w) { cg_after_true(sh, a, w, it); });
+            if (sh.replace) {   // refinement restart: CG continues from the true residual
+                for (int l = threadIdx.x; l < nloc; l += kCgcBlock) cur[l].x = sap[l];
+                cl.sync();      // before any CTA reads a neighbour's new r
+            }
+        }
     }
     for (int l = threadIdx.x; l < nloc; l += kCgcBlock) {
         a.x[mlo + l] = sx[l];
         a.r[mlo + l] = cur[l].x;
     }
-    if (ran && me == 0 && threadIdx.x == 0) a.cw->cg_rr[u.d] = (double)rr.hi + (double)rr.lo;
+    if (ran && me == 0 && threadIdx.x == 0) cg_report(a, u.d, sh);
 }
 
 // Global-memory path (any size, any depth).
@@ -313,14 +455,13 @@ __device__ __forceinline__ void cgc_global(cg::cluster_group& cl, CgcShared& sh,
         acc = ff_add(acc, ff_prod(bi, bi));
     }
     int buf = 0;
-    FF rr = cgc_allreduce(cl, sh, buf, acc);
-    bool active = ff_to_float(rr) > a.tol2;
+    cgc_allreduce(cl, sh, buf, acc, [&](double w) { cg_start(sh, a, w); });
     bool ran = false;
-    float beta = 0.0f;
     const float* pprev = a.pa;
     float* pcur = a.pb;
     int it = 1;
-    while (active && it <= a.max_iter) {
+    while (sh.go) {
+        const float beta = sh.beta;
         acc = ff_zero();
         for (int i = u.row0 + tid; i < u.row1; i += nthr) {
             const float pi = fmaf(beta, pprev[i], a.r[i]);
@@ -334,8 +475,11 @@ __device__ __forceinline__ void cgc_global(cg::cluster_group& cl, CgcShared& sh,
             a.ap[i] = y;
             acc = ff_add(acc, ff_prod(pi, y));
         }
-        const FF pap = cgc_allreduce(cl, sh, buf, acc);
-        const float alpha = (pap.hi != 0.0f) ? ff_div(rr, pap) : 0.0f;
+        cgc_allreduce(cl, sh, buf, acc, [&](double w) {
+            sh.pap = w;
+            sh.alpha = (w != 0.0) ? (float)(sh.rr / w) : 0.0f;
+        });
+        const float alpha = sh.alpha;
         acc = ff_zero();
         for (int i = u.row0 + tid; i < u.row1; i += nthr) {
             a.x[i] = fmaf(alpha, pcur[i], a.x[i]);
@@ -343,18 +487,34 @@ __device__ __forceinline__ void cgc_global(cg::cluster_group& cl, CgcShared& sh,
             a.r[i] = ri;
             acc = ff_add(acc, ff_prod(ri, ri));
         }
-        const FF rn = cgc_allreduce(cl, sh, buf, acc);
-        beta = (rr.hi != 0.0f) ? ff_div(rn, rr) : 0.0f;
-        rr = rn;
+        cgc_allreduce(cl, sh, buf, acc, [&](double w) { cg_after_rr(sh, a, w, it); });
         ran = true;
         if (cl.block_rank() == 0 && threadIdx.x == 0) a.cw->cg_iters[u.d] = it;
-        active = (ff_to_float(rn) > a.tol2) && pap.hi != 0.0f && it + 1 <= a.max_iter;
         float* t = const_cast<float*>(pprev);
         pprev = pcur;
         pcur = t;
         ++it;
+        if (sh.check) {
+            // true residual r = b - A x (the barrier of the last reduction published x)
+            acc = ff_zero();
+            for (int i = u.row0 + tid; i < u.row1; i += nthr) {
+                FF y = ff_zero();
+                for (int k = 0; k < 27; ++k) {
+                    const int nb = __ldg(&a.neigh[(size_t)k * a.stride + i]);
+                    if (nb >= 0) y = ff_add(y, ff_prod(sh.st[k], a.x[nb]));
+                }
+                const float ri = ff_to_float(ff_add(FF{a.b[i], 0.0f}, FF{-y.hi, -y.lo}));
+                a.ap[i] = ri;   // staged; A p holds nothing live here
+                acc = ff_add(acc, ff_prod(ri, ri));
+            }
+            cgc_allreduce(cl, sh, buf, acc, [&](double w) { cg_after_true(sh, a, w, it); });
+            if (sh.replace) {   // refinement restart: CG continues from the true residual
+                for (int i = u.row0 + tid; i < u.row1; i += nthr) a.r[i] = a.ap[i];
+                cl.sync();
+            }
+        }
     }
-    if (ran && cl.block_rank() == 0 && threadIdx.x == 0) a.cw->cg_rr[u.d] = (double)rr.hi + (double)rr.lo;
+    if (ran && cl.block_rank() == 0 && threadIdx.x == 0) cg_report(a, u.d, sh);
 }
 
 // one depth per cluster (a CTA when the launch has no cluster dimension); kClusterUnits:
@@ -561,7 +721,7 @@ static cudaError_t launch_cg(void (*kernel)(CgcArgs), CgcArgs& a, int grid, int 
     return cudaLaunchKernelExC(&cfg, (const void*)kernel, args);
 }
 
-cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, int cg_max_iter) {
+cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, int cg_max_iter, int res_period) {
     cudaStream_t s = ws.stream;
     if (g_cg_cluster == 0) prepare_launch_configs(ws);
     const int D = ws.depth;
@@ -583,6 +743,7 @@ cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, 
     // a fixed iteration count replaces the reference's max_iter (10000); the tolerance
     // test of the loop is kept (mesh/solver/CGAlgorithm.cu:36)
     a.max_iter = (cg_mode == 1 && cg_iters > 0) ? cg_iters : cg_max_iter;
+    a.res_period = res_period;
     k_cg_blocks<<<grid_for(ws, 1 << 20), kBlock, 0, s>>>(ws.cnt, ws.neigh, (size_t)ws.cap.nodes, ws.cg_blk);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;

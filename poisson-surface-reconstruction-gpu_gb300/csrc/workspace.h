@@ -194,7 +194,9 @@ inline int grid_for(const Workspace& ws, long long work) {
 cudaError_t octree_build(Workspace& ws);
 void prepare_launch_configs(Workspace& ws);
 cudaError_t field_build(Workspace& ws);
-cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, int cg_max_iter);
+// res_period: true residual every res_period CG iterations and at convergence (0: only at
+// convergence, < 0: never)
+cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, int cg_max_iter, int res_period);
 cudaError_t mesh_geometry(Workspace& ws);   // vertex / edge / face records (octree only)
 cudaError_t mesh_build(Workspace& ws);      // values, marching cubes, subdivision, compaction
 cudaError_t transfer_prepare(Workspace& ws, int with_colour);   // sample grid (points only)

@@ -33,7 +33,7 @@ class PsrConfig(ctypes.Structure):
                 ("compute_colors", ctypes.c_int), ("compute_normals", ctypes.c_int), ("device", ctypes.c_int),
                 ("laplacian_epsilon", ctypes.c_float), ("concurrent_stages", ctypes.c_int),
                 ("weld_vertices", ctypes.c_int), ("disable_graphs", ctypes.c_int),
-                ("root_poly_capacity", ctypes.c_int)]
+                ("root_poly_capacity", ctypes.c_int), ("cg_residual_period", ctypes.c_int)]
 
 
 class PsrPoints(ctypes.Structure):
@@ -62,7 +62,9 @@ class PsrStats(ctypes.Structure):
                 ("cg_residual", ctypes.c_double * 10), ("iso_value", ctypes.c_float),
                 ("error_bits", ctypes.c_uint), ("stage_ms", ctypes.c_float * 6),
                 ("kernel_launches", ctypes.c_int), ("graph_replay", ctypes.c_int),
-                ("cg_kernel_ms", ctypes.c_float), ("cg_depth_ms", ctypes.c_float * 10)]
+                ("cg_kernel_ms", ctypes.c_float), ("cg_depth_ms", ctypes.c_float * 10),
+                ("cg_true_residual", ctypes.c_double * 10), ("cg_residual_checks", ctypes.c_int * 10),
+                ("cg_restarts", ctypes.c_int * 10)]
 
 
 _lib = None
@@ -140,7 +142,7 @@ class PoissonReconstruction:
     def __init__(self, max_depth=7, max_points=300000, max_triangles=1000000, max_mesh_vertices=300000,
                  compute_colors=False, compute_normals=False, cg_tolerance=1e-5, cg_max_iterations=10000,
                  max_nodes=0, max_subdivision_nodes=0, device=0, laplacian_epsilon=1e-6, concurrent_stages=True, weld_vertices=False,
-                 disable_graphs=False, root_poly_capacity=0):
+                 disable_graphs=False, root_poly_capacity=0, cg_residual_period=0):
         self._lib = load_library()
         cfg = default_config()
         cfg.max_depth = max_depth
@@ -159,6 +161,7 @@ class PoissonReconstruction:
         cfg.weld_vertices = int(weld_vertices)
         cfg.disable_graphs = int(disable_graphs)
         cfg.root_poly_capacity = int(root_poly_capacity)
+        cfg.cg_residual_period = int(cg_residual_period)
         self.config = cfg
         h = ctypes.c_void_p()
         st = self._lib.psr_create(ctypes.byref(cfg), ctypes.byref(h))

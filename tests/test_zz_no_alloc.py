@@ -18,20 +18,26 @@ pytestmark = pytest.mark.gpu
 
 
 def _reference_order(xyz, nrm, depth):
-    """Sorted normalised positions and per-point codes from the full pipeline (a few CG
-    iterations and every Laplacian entry kept: only the octree is compared)."""
+    """Sorted normalised positions and per-point codes from psr_reconstruct.  Only its
+    octree is compared, so a few CG iterations do; a sparse cloud at depth 9 can then
+    overflow a mesh capacity, which leaves the octree arrays (built before the mesh)
+    intact."""
     import psr
     with psr.PoissonReconstruction(max_depth=depth, max_points=max(len(xyz), 300000),
-                                   laplacian_epsilon=0.0, max_triangles=4000000,
-                                   max_mesh_vertices=2000000) as r:
-        mesh = r.SolvePoissionReconstructionMesh(xyz, nrm, depth=depth, cg_iterations=4)
+                                   laplacian_epsilon=0.0) as r:
+        try:
+            r.SolvePoissionReconstructionMesh(xyz, nrm, depth=depth, cg_iterations=4)
+        except psr.PsrError as e:
+            if e.status != psr.PSR_OUT_OF_CAPACITY:
+                raise
         st = r.stats()
+        bbox = r.debug("bbox", np.float32)
         px, py, pz = (r.debug(n, np.float32) for n in ("px", "py", "pz"))
         key = r.debug("key")
         p2n = r.debug("point2node")
         bD = sum(st.level_count[d] for d in range(depth))
         codes = key[bD + p2n].astype(np.uint32)
-    return np.stack([px, py, pz], 1), codes, mesh.center, mesh.scale
+    return np.stack([px, py, pz], 1), codes, bbox[:3], float(bbox[3])
 
 
 def _noalloc(xyz, depth):
