@@ -78,6 +78,12 @@ typedef struct psr_config {
                                   tolerance and the floor of an FP32 solution (2^-20 ||b||).
                                   0 (default): every 32 iterations; -1: never (the reference's
                                   recursive residual only, mesh/solver/CGAlgorithm.cu:36-75) */
+    int batch_clouds;          /* 0 or 1: one cloud per call.  K (2..64): the handle holds K
+                                  complete workspaces and psr_submit_batch reconstructs up to K
+                                  clouds of one depth with one launch of each kernel for all of
+                                  them (the clouds' data never mix; each result equals the
+                                  one-cloud call's).  Device memory: K x psr_memory_bytes of a
+                                  one-cloud handle */
 } psr_config;
 
 /* Oriented input cloud (the fields of DepthSurfel, base/CommonTypes.h:113-118, as SoA). */
@@ -180,6 +186,23 @@ psr_status psr_wait(psr_handle* h);
 psr_status psr_estimate_normals(psr_handle* h, const float* xyz, int count, psr_location location, float* normals,
                                 const float* viewpoint, void* stream);
 
+/* Multi-cloud form (no counterpart in the reference, which reconstructs one cloud per
+ * blocking call, mesh/PoissonReconstruction.cpp:195-245): enqueues the reconstruction of
+ * `count` clouds (1 <= count <= batch_clouds) on `stream` and returns without waiting.
+ * Every kernel of the pipeline is launched once for all of them, cloud i in workspace slot
+ * i; options (depth, iterations) are shared, and the clouds must agree on having colours
+ * (points[i].rgb) and on the outputs asked for (meshes[i].colors / normals).  Completion is
+ * collected with psr_poll / psr_wait, which fill meshes[i] like psr_reconstruct does and
+ * return PSR_OK when every cloud succeeded; psr_get_batch_result gives each cloud's status
+ * and statistics.  psr_reconstruct_batch submits and waits. */
+psr_status psr_submit_batch(psr_handle* h, const psr_points* points, int count, const psr_options* options,
+                            psr_mesh* meshes, void* stream);
+psr_status psr_reconstruct_batch(psr_handle* h, const psr_points* points, int count, const psr_options* options,
+                                 psr_mesh* meshes, void* stream);
+/* Status and statistics of cloud `index` of the last completed call (index 0 for a one-cloud
+ * call); `out` may be NULL. */
+psr_status psr_get_batch_result(const psr_handle* h, int index, psr_stats* out);
+
 /* Input adaptor: device array of `count` DepthSurfel records (base/CommonTypes.h:113-118,
  * 64 bytes each) -> device SoA arrays for psr_points: xyz and normals (3 * count floats),
  * and rgb (3 * count bytes, round(255 * ColorAndTime.xyz) clamped) unless rgb is NULL.
@@ -194,7 +217,8 @@ psr_status psr_memory_bytes(const psr_handle* h, size_t* bytes);
 psr_status psr_get_stats(const psr_handle* h, psr_stats* out);
 
 /* Copies an internal device array of the last reconstruction to host memory (testing
- * and inspection).  Returns the byte size in *bytes; dst may be NULL to query it. */
+ * and inspection); "name@k" names cloud k's array after a multi-cloud call.  Returns the
+ * byte size in *bytes; dst may be NULL to query it. */
 psr_status psr_debug_array(psr_handle* h, const char* name, void* dst, size_t dst_bytes, size_t* bytes);
 
 /* Point ordering without any device allocation (no counterpart in the reference).

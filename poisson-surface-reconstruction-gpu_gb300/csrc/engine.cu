@@ -1,4 +1,5 @@
 // Handle, workspace allocation and the C ABI (include/psr/psr.h).
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cstdio>
@@ -59,12 +60,22 @@ struct psr_handle {
     bool have_result = false;
     std::string last_error;
     psr_stats stats;
-    // the reconstruction in flight (psr_submit ... psr_poll / psr_wait)
+    // the reconstruction in flight (psr_submit / psr_submit_batch ... psr_poll / psr_wait)
     cudaEvent_t done = nullptr;
     bool pending = false;
-    psr_mesh* pend_mesh = nullptr;
+    bool pend_batch = false;
+    std::vector<psr_mesh> pend_meshes;        // copies of the callers' mesh descriptors
+    psr_mesh* pend_user_mesh = nullptr;       // single call: the caller's descriptor
+    psr_mesh* pend_user_meshes = nullptr;     // batch call: the callers' descriptors
     int pend_depth = 0, pend_colour = 0, pend_normals = 0;
     cudaStream_t pend_stream = nullptr;
+    // cloud slots: 1, or batch_clouds workspaces mapped kCloudStride apart
+    int clouds = 1;
+    unsigned long long va_base = 0;           // reserved address range of a batch handle
+    size_t va_slot = 0;                       // bytes mapped per slot
+    Counters* cnt_host_all = nullptr;         // pinned count read-back, one per slot
+    std::vector<psr_stats> batch_stats;       // per cloud of the last completed call
+    std::vector<psr_status> batch_status;
 };
 
 namespace {
@@ -94,6 +105,106 @@ psr_status fail(psr_handle* h, psr_status s, const char* msg) {
 psr_status cuda_fail(psr_handle* h, cudaError_t e, const char* where) {
     if (h) h->last_error = std::string(where) + ": " + cudaGetErrorString(e);
     return PSR_CUDA_ERROR;
+}
+
+// Cloud k's copy of a workspace buffer of a batch handle.
+template <class T>
+T* slot_ptr(T* p, int k) {
+    return p ? (T*)((char*)p + (unsigned long long)k * kCloudStride) : p;
+}
+
+// ---- cloud slots of a batch handle ---------------------------------------------------
+// One address range of batch_clouds * kCloudStride bytes, aligned to kMaxBatchClouds *
+// kCloudStride, is reserved and every slot's workspace is backed by its own physical
+// allocation mapped at the slot's start, so slot k's buffers sit exactly k * kCloudStride
+// bytes after slot 0's (the kernels' PSR_CLOUD rebasing).  The driver's virtual-memory
+// calls are reached through the runtime's driver entry points (no link-time dependency
+// on the driver library).
+typedef CUresult (*PfnGranularity)(size_t*, const CUmemAllocationProp*, CUmemAllocationGranularity_flags);
+typedef CUresult (*PfnReserve)(CUdeviceptr*, size_t, size_t, CUdeviceptr, unsigned long long);
+typedef CUresult (*PfnAddressFree)(CUdeviceptr, size_t);
+typedef CUresult (*PfnCreate)(CUmemGenericAllocationHandle*, size_t, const CUmemAllocationProp*, unsigned long long);
+typedef CUresult (*PfnRelease)(CUmemGenericAllocationHandle);
+typedef CUresult (*PfnMap)(CUdeviceptr, size_t, size_t, CUmemGenericAllocationHandle, unsigned long long);
+typedef CUresult (*PfnUnmap)(CUdeviceptr, size_t);
+typedef CUresult (*PfnSetAccess)(CUdeviceptr, size_t, const CUmemAccessDesc*, size_t);
+
+struct VmmApi {
+    PfnGranularity granularity = nullptr;
+    PfnReserve reserve = nullptr;
+    PfnAddressFree address_free = nullptr;
+    PfnCreate create = nullptr;
+    PfnRelease release = nullptr;
+    PfnMap map = nullptr;
+    PfnUnmap unmap = nullptr;
+    PfnSetAccess set_access = nullptr;
+    bool ok = false;
+};
+
+const VmmApi& vmm() {
+    static VmmApi api = [] {
+        VmmApi a;
+        auto get = [](const char* name, void** fn) {
+            cudaDriverEntryPointQueryResult q;
+            return cudaGetDriverEntryPointByVersion(name, fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+                   q == cudaDriverEntryPointSuccess && *fn;
+        };
+        a.ok = get("cuMemGetAllocationGranularity", (void**)&a.granularity) &&
+               get("cuMemAddressReserve", (void**)&a.reserve) && get("cuMemAddressFree", (void**)&a.address_free) &&
+               get("cuMemCreate", (void**)&a.create) && get("cuMemRelease", (void**)&a.release) &&
+               get("cuMemMap", (void**)&a.map) && get("cuMemUnmap", (void**)&a.unmap) &&
+               get("cuMemSetAccess", (void**)&a.set_access);
+        return a;
+    }();
+    return api;
+}
+
+// Unmaps the first `mapped` slots and frees the reserved range.
+void release_cloud_slots(psr_handle* h, int mapped) {
+    const VmmApi& v = vmm();
+    for (int k = 0; k < mapped; ++k) v.unmap((CUdeviceptr)(h->va_base + (unsigned long long)k * kCloudStride), h->va_slot);
+    v.address_free((CUdeviceptr)h->va_base, (size_t)h->clouds * kCloudStride);
+    h->va_base = 0;
+    h->va_slot = 0;
+}
+
+psr_status map_cloud_slots(psr_handle* h, size_t bytes) {
+    const VmmApi& v = vmm();
+    if (!v.ok) return fail(h, PSR_CUDA_ERROR, "virtual memory management calls unavailable");
+    CUmemAllocationProp prop = {};
+    prop.type = CU_MEM_ALLOCATION_TYPE_PINNED;
+    prop.location.type = CU_MEM_LOCATION_TYPE_DEVICE;
+    prop.location.id = h->cfg.device;
+    size_t gran = 0;
+    if (v.granularity(&gran, &prop, CU_MEM_ALLOC_GRANULARITY_RECOMMENDED) != CUDA_SUCCESS || gran == 0)
+        return fail(h, PSR_CUDA_ERROR, "cuMemGetAllocationGranularity");
+    const size_t slot = (bytes + gran - 1) / gran * gran;
+    if (slot > kCloudStride) return fail(h, PSR_OUT_OF_CAPACITY, "one cloud's workspace exceeds the slot stride");
+    CUdeviceptr base = 0;
+    if (v.reserve(&base, (size_t)h->clouds * kCloudStride, (size_t)kMaxBatchClouds * kCloudStride, 0, 0) !=
+            CUDA_SUCCESS ||
+        (((unsigned long long)base >> 35) & (kMaxBatchClouds - 1)) != 0)
+        return fail(h, PSR_CUDA_ERROR, "cuMemAddressReserve");
+    h->va_base = (unsigned long long)base;
+    h->va_slot = slot;
+    CUmemAccessDesc acc = {};
+    acc.location = prop.location;
+    acc.flags = CU_MEM_ACCESS_FLAGS_PROT_READWRITE;
+    for (int k = 0; k < h->clouds; ++k) {
+        const CUdeviceptr at = base + (CUdeviceptr)((unsigned long long)k * kCloudStride);
+        CUmemGenericAllocationHandle mh;
+        if (v.create(&mh, slot, &prop, 0) != CUDA_SUCCESS) {
+            release_cloud_slots(h, k);
+            return fail(h, PSR_OUT_OF_CAPACITY, "cuMemCreate: not enough device memory for the cloud slots");
+        }
+        const bool mapped = v.map(at, slot, 0, mh, 0) == CUDA_SUCCESS;
+        v.release(mh);   // the mapping keeps the memory until it is unmapped
+        if (!mapped || v.set_access(at, slot, &acc, 1) != CUDA_SUCCESS) {
+            release_cloud_slots(h, k + (mapped ? 1 : 0));
+            return fail(h, PSR_CUDA_ERROR, "cuMemMap / cuMemSetAccess");
+        }
+    }
+    return PSR_OK;
 }
 
 }  // namespace
@@ -233,7 +344,7 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     A.add(ws.cg_partial, std::max((size_t)nodes, (size_t)4096 * (kMaxDepth + 1)));
     A.add(ws.point_val, (size_t)N);
     A.add(ws.pv_coef, 27 * ((size_t)dnodes / 8 + 64));
-    A.add(ws.iso_partial, (size_t)ws.num_sms * 8 + 64);
+    A.add(ws.iso_partial, (size_t)N / kBlock + 2);   // one sum per chunk of kBlock sample points
     A.add(ws.vmask, (size_t)nodes);
     A.add(ws.emask16, (size_t)dnodes);
     A.add(ws.fmask, (size_t)nodes);
@@ -300,10 +411,19 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     A.add(ws.mb.misc, 16);
     A.add(ws.d_params, 16);
 
-    e = cudaMalloc(&h->arena, A.bytes);
-    if (e != cudaSuccess) { psr_status st = cuda_fail(h, e, "cudaMalloc workspace"); delete h; return st; }
+    if (cfg.batch_clouds > kMaxBatchClouds) { delete h; return PSR_INVALID_INPUT; }
+    h->clouds = cfg.batch_clouds > 1 ? cfg.batch_clouds : 1;
+    if (h->clouds == 1) {
+        e = cudaMalloc(&h->arena, A.bytes);
+        if (e != cudaSuccess) { psr_status st = cuda_fail(h, e, "cudaMalloc workspace"); delete h; return st; }
+    } else {
+        const psr_status st = map_cloud_slots(h, A.bytes);
+        if (st != PSR_OK) { delete h; return st; }
+        h->arena = (void*)h->va_base;
+    }
     h->arena_bytes = A.bytes;
     A.assign((char*)h->arena);
+    set_batch(ws, 1);
     ws.scan.max_tiles = cap.scan_tiles;
     // scan counters and epoch start at zero; the scans keep them consistent afterwards
     e = cudaMemset(ws.scan.words, 0, sizeof(unsigned long long) * ((size_t)cap.scan_tiles + kScanHeader));
@@ -312,8 +432,9 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
         e = cudaMemset(ws.scan_aux.words, 0, sizeof(unsigned long long) * ((size_t)cap.scan_tiles + kScanHeader));
     ws.sort.max_tiles = sort_tiles;
     ws.sort.scan = ws.scan;   // sort shares the scan scratch (scans are sequential on one stream)
-    e = cudaMallocHost(&ws.cnt_host, sizeof(Counters));
-    if (e == cudaSuccess) e = cudaMallocHost(&h->h_params, 16 * sizeof(int));
+    e = cudaMallocHost(&h->cnt_host_all, sizeof(Counters) * (size_t)h->clouds);
+    ws.cnt_host = h->cnt_host_all;
+    if (e == cudaSuccess) e = cudaMallocHost(&h->h_params, 16 * sizeof(int) * (size_t)h->clouds);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
     for (int i = 0; i < 7 && e == cudaSuccess; ++i) e = cudaEventCreate(&h->ev[i]);
     h->ws.ev_cg = h->ev[6];
@@ -342,6 +463,13 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
         if (e == cudaSuccess) e = cudaMemcpy(ws.stencil, st.data(), st.size() * sizeof(float), cudaMemcpyHostToDevice);
         std::copy(st.begin(), st.end(), ws.stencil_host);   // the CG launch passes some as parameters
     }
+    // the other cloud slots start as copies of slot 0 (tables, zeroed scan counters)
+    for (int k = 1; k < h->clouds && e == cudaSuccess; ++k)
+        e = cudaMemcpy(slot_ptr((char*)h->arena, k), h->arena, A.bytes, cudaMemcpyDeviceToDevice);
+    // device-to-device copies and memsets return before they complete, and the handle's
+    // streams do not wait for the legacy default stream: finish the set-up here, so no
+    // later copy into a slot can be overwritten by it
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e == cudaSuccess) {
         prepare_launch_configs(ws);
         e = cudaGetLastError();
@@ -359,9 +487,13 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
 psr_status psr_destroy(psr_handle* h) {
     if (!h) return PSR_OK;
     if (h->pending && h->done) cudaEventSynchronize(h->done);   // no buffer is freed under running work
+    // work a failed call left queued may still run: unmapping a batch handle's slots (unlike
+    // cudaFree) does not wait for it
+    if (h->va_base) cudaDeviceSynchronize();
     for (auto& g : h->graphs) if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
-    if (h->arena) cudaFree(h->arena);
-    if (h->ws.cnt_host) cudaFreeHost(h->ws.cnt_host);
+    if (h->arena && h->clouds == 1) cudaFree(h->arena);
+    if (h->va_base) release_cloud_slots(h, h->clouds);
+    if (h->cnt_host_all) cudaFreeHost(h->cnt_host_all);
     if (h->h_params) cudaFreeHost(h->h_params);
     for (int i = 0; i < 7; ++i) if (h->ev[i]) cudaEventDestroy(h->ev[i]);
     if (h->ws.ev_fork) cudaEventDestroy(h->ws.ev_fork);
@@ -395,82 +527,75 @@ __global__ void __launch_bounds__(kBlock) k_emit_mesh(const Counters* c, const f
     }
 }
 
-// Enqueues one reconstruction on `stream` (no host synchronisation).
-static psr_status submit_impl(psr_handle* h, const psr_points* pts, const psr_options* opt, psr_mesh* mesh,
-                              void* stream) {
-    if (!h) return PSR_INVALID_INPUT;
-    if (h->pending) return fail(h, PSR_INVALID_INPUT, "a reconstruction is already in flight on this handle");
-    h->have_result = false;
-    if (!pts || !mesh || !pts->xyz || !pts->normals) return fail(h, PSR_INVALID_INPUT, "null argument");
-    const int n = pts->count;
-    if (n <= 0) return fail(h, PSR_INVALID_INPUT, "empty point cloud");
-    if (n > h->ws.cap.points) return fail(h, PSR_OUT_OF_CAPACITY, "more points than max_points");
-    int depth = (opt && opt->depth > 0) ? opt->depth : h->cfg.max_depth;
-    if (depth < 2 || depth > h->cfg.max_depth) return fail(h, PSR_INVALID_INPUT, "depth outside [2, max_depth]");
-    const int cg_iters = (opt && opt->cg_iterations > 0) ? opt->cg_iterations : 0;
+// The whole pipeline for the clouds set by set_batch, issued on `qs` (captured into a graph
+// or run directly).
+#ifdef PSR_CLOUD_CHECK
+#define PSR_TRACE(q, what) do { if ((q) != cudaSuccess) fprintf(stderr, "issue_pipeline: %s: %s\n", what, cudaGetErrorString(q)); } while (0)
+#else
+#define PSR_TRACE(q, what) do { } while (0)
+#endif
+
+static cudaError_t issue_pipeline(psr_handle* h, cudaStream_t qs, int cg_iters, int want_colour, int want_normals) {
+    Workspace& ws = h->ws;
+    ws.stream = qs;
+    // stage-boundary events: external event nodes when captured into a graph (so a replay
+    // records them), plain records when the stages are issued directly (the external flag
+    // is refused outside a capture)
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(qs, &cap);
+    ws.ev_flags = (cap == cudaStreamCaptureStatusActive) ? cudaEventRecordExternal : cudaEventRecordDefault;
+    cudaError_t q = cudaEventRecordWithFlags(h->ev[0], qs, ws.ev_flags);
+    PSR_TRACE(q, "event 0");
+    if (q == cudaSuccess) q = octree_build(ws); PSR_TRACE(q, "octree_build");
+    if (q == cudaSuccess) q = cudaEventRecordWithFlags(h->ev[1], qs, ws.ev_flags);
+    // octree-only work on a third stream, beside the divergence and the solve: the
+    // vertex / edge / face records and the colour search grid (own scan scratch)
+    const bool overlap = h->cfg.concurrent_stages != 0;
+    if (overlap) {
+        if (q == cudaSuccess) q = cudaEventRecord(ws.ev_fork2, qs);
+        if (q == cudaSuccess) q = cudaStreamWaitEvent(ws.aux2, ws.ev_fork2, 0);
+        if (q == cudaSuccess) {
+            const ScanScratch main_scan = ws.scan;
+            ws.stream = ws.aux2;
+            ws.scan = ws.scan_aux;
+            q = mesh_geometry(ws);
+            if (q == cudaSuccess) q = transfer_prepare(ws, want_colour); PSR_TRACE(q, "mesh_geometry/transfer_prepare");
+            ws.stream = qs;
+            ws.scan = main_scan;
+        }
+        if (q == cudaSuccess) q = cudaEventRecord(ws.ev_join2, ws.aux2);
+    } else {
+        if (q == cudaSuccess) q = mesh_geometry(ws);
+        if (q == cudaSuccess) q = transfer_prepare(ws, want_colour);
+    }
+    if (q == cudaSuccess) q = field_build(ws); PSR_TRACE(q, "field_build");
+    if (q == cudaSuccess) q = cudaEventRecordWithFlags(h->ev[2], qs, ws.ev_flags);
+    if (q == cudaSuccess)
+        q = solve_build(ws, cg_iters > 0 ? 1 : 0, cg_iters, h->cfg.cg_tolerance, h->cfg.cg_max_iterations,
+                        h->cfg.cg_residual_period == 0 ? kDefaultResidualPeriod
+                                                       : (h->cfg.cg_residual_period < 0 ? -1 : h->cfg.cg_residual_period)); PSR_TRACE(q, "solve_build");
+    if (q == cudaSuccess) q = cudaEventRecordWithFlags(h->ev[3], qs, ws.ev_flags);
+    if (q == cudaSuccess && overlap) q = cudaStreamWaitEvent(qs, ws.ev_join2, 0);
+    if (q == cudaSuccess) q = mesh_build(ws); PSR_TRACE(q, "mesh_build");
+    if (q == cudaSuccess) q = weld_build(ws); PSR_TRACE(q, "weld_build");
+    if (q == cudaSuccess) q = cudaEventRecordWithFlags(h->ev[4], qs, ws.ev_flags);
+    if (q == cudaSuccess) q = transfer_build(ws, want_colour, want_normals); PSR_TRACE(q, "transfer_build");
+    if (q == cudaSuccess) q = cudaEventRecordWithFlags(h->ev[5], qs, ws.ev_flags);
+    return q;
+}
+
+// Launches the pipeline for `clouds` clouds (slots 0 .. clouds - 1) on `s`: captured once
+// per (clouds, depth, options) into a CUDA graph, replayed afterwards.
+static cudaError_t launch_pipeline(psr_handle* h, int depth, int cg_iters, int want_colour, int want_normals,
+                                   bool has_rgb, int clouds, cudaStream_t s) {
     Workspace& ws = h->ws;
     ws.depth = depth;
-    cudaStream_t s = stream ? (cudaStream_t)stream : h->own_stream;
-    ws.stream = s;
-    cudaError_t e = cudaSetDevice(h->cfg.device);
-    if (e != cudaSuccess) return cuda_fail(h, e, "cudaSetDevice");
-    // inputs
-    const cudaMemcpyKind kind = (pts->location == PSR_DEVICE) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-    e = cudaMemcpyAsync(ws.in_xyz, pts->xyz, 3 * sizeof(float) * (size_t)n, kind, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(ws.in_nrm, pts->normals, 3 * sizeof(float) * (size_t)n, kind, s);
-    const bool has_rgb = pts->rgb != nullptr;
-    if (e == cudaSuccess && has_rgb) e = cudaMemcpyAsync(ws.in_rgb, pts->rgb, 3 * (size_t)n, kind, s);
-    if (e != cudaSuccess) return cuda_fail(h, e, "input copy");
-    const int want_colour = h->cfg.compute_colors && mesh->colors;
-    const int want_normals = h->cfg.compute_normals && mesh->normals;
-    h->h_params[0] = n;
-    e = cudaMemcpyAsync(ws.d_params, h->h_params, sizeof(int), cudaMemcpyHostToDevice, s);
-    if (e != cudaSuccess) return cuda_fail(h, e, "parameter copy");
     uint8_t* saved_rgb = ws.in_rgb;
     if (!has_rgb) ws.in_rgb = nullptr;
-    // the whole pipeline: captured once per (depth, options) into a CUDA graph, replayed after
-    auto issue = [&](cudaStream_t qs) -> cudaError_t {
-        ws.stream = qs;
-        cudaError_t q = cudaEventRecordWithFlags(h->ev[0], qs, cudaEventRecordExternal);
-        if (q == cudaSuccess) q = octree_build(ws);
-        if (q == cudaSuccess) q = cudaEventRecordWithFlags(h->ev[1], qs, cudaEventRecordExternal);
-        // octree-only work on a third stream, beside the divergence and the solve: the
-        // vertex / edge / face records and the colour search grid (own scan scratch)
-        const bool overlap = h->cfg.concurrent_stages != 0;
-        if (overlap) {
-            if (q == cudaSuccess) q = cudaEventRecord(ws.ev_fork2, qs);
-            if (q == cudaSuccess) q = cudaStreamWaitEvent(ws.aux2, ws.ev_fork2, 0);
-            if (q == cudaSuccess) {
-                const ScanScratch main_scan = ws.scan;
-                ws.stream = ws.aux2;
-                ws.scan = ws.scan_aux;
-                q = mesh_geometry(ws);
-                if (q == cudaSuccess) q = transfer_prepare(ws, want_colour);
-                ws.stream = qs;
-                ws.scan = main_scan;
-            }
-            if (q == cudaSuccess) q = cudaEventRecord(ws.ev_join2, ws.aux2);
-        } else {
-            if (q == cudaSuccess) q = mesh_geometry(ws);
-            if (q == cudaSuccess) q = transfer_prepare(ws, want_colour);
-        }
-        if (q == cudaSuccess) q = field_build(ws);
-        if (q == cudaSuccess) q = cudaEventRecordWithFlags(h->ev[2], qs, cudaEventRecordExternal);
-        if (q == cudaSuccess)
-            q = solve_build(ws, cg_iters > 0 ? 1 : 0, cg_iters, h->cfg.cg_tolerance, h->cfg.cg_max_iterations,
-                            h->cfg.cg_residual_period == 0 ? kDefaultResidualPeriod
-                                                           : (h->cfg.cg_residual_period < 0 ? -1 : h->cfg.cg_residual_period));
-        if (q == cudaSuccess) q = cudaEventRecordWithFlags(h->ev[3], qs, cudaEventRecordExternal);
-        if (q == cudaSuccess && overlap) q = cudaStreamWaitEvent(qs, ws.ev_join2, 0);
-        if (q == cudaSuccess) q = mesh_build(ws);
-        if (q == cudaSuccess) q = weld_build(ws);
-        if (q == cudaSuccess) q = cudaEventRecordWithFlags(h->ev[4], qs, cudaEventRecordExternal);
-        if (q == cudaSuccess) q = transfer_build(ws, want_colour, want_normals);
-        if (q == cudaSuccess) q = cudaEventRecordWithFlags(h->ev[5], qs, cudaEventRecordExternal);
-        return q;
-    };
-    const long long gkey = ((long long)depth << 40) | ((long long)cg_iters << 8) | (want_colour << 2) |
-                           (want_normals << 1) | (has_rgb ? 1 : 0);
+    set_batch(ws, clouds);
+    cudaError_t e = cudaSuccess;
+    const long long gkey = ((long long)clouds << 44) | ((long long)depth << 40) | ((long long)cg_iters << 8) |
+                           (want_colour << 2) | (want_normals << 1) | (has_rgb ? 1 : 0);
     h->last_graph = 0;
     if (h->use_graphs) {
         auto it = h->graphs.find(gkey);
@@ -479,7 +604,7 @@ static psr_status submit_impl(psr_handle* h, const psr_points* pts, const psr_op
             GraphEntry ge;
             cudaError_t q = cudaStreamBeginCapture(h->own_stream, cudaStreamCaptureModeThreadLocal);
             if (q == cudaSuccess) {
-                cudaError_t qi = issue(h->own_stream);
+                cudaError_t qi = issue_pipeline(h, h->own_stream, cg_iters, want_colour, want_normals);
                 q = cudaStreamEndCapture(h->own_stream, &graph);
                 if (qi != cudaSuccess) q = qi;
             }
@@ -510,24 +635,93 @@ static psr_status submit_impl(psr_handle* h, const psr_points* pts, const psr_op
         }
     }
     if (!h->use_graphs) {
-        e = issue(s);
+        e = issue_pipeline(h, s, cg_iters, want_colour, want_normals);
         h->last_kernels = -1;
     }
+    set_batch(ws, 1);
     ws.in_rgb = saved_rgb;
     ws.stream = s;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(ws.cnt_host, ws.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, s);
+    return e;
+}
+
+// Copies the inputs of one cloud into slot k and enqueues its point count.
+static cudaError_t stage_inputs(psr_handle* h, const psr_points* pts, int k, cudaStream_t s) {
+    Workspace& ws = h->ws;
+    const int n = pts->count;
+    const cudaMemcpyKind kind = (pts->location == PSR_DEVICE) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    cudaError_t e = cudaMemcpyAsync(slot_ptr(ws.in_xyz, k), pts->xyz, 3 * sizeof(float) * (size_t)n, kind, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(slot_ptr(ws.in_nrm, k), pts->normals, 3 * sizeof(float) * (size_t)n, kind, s);
+    if (e == cudaSuccess && pts->rgb) e = cudaMemcpyAsync(slot_ptr(ws.in_rgb, k), pts->rgb, 3 * (size_t)n, kind, s);
+    if (e == cudaSuccess) {
+        int* hp = h->h_params + 16 * k;
+        hp[0] = n;
+        e = cudaMemcpyAsync(slot_ptr(ws.d_params, k), hp, sizeof(int), cudaMemcpyHostToDevice, s);
+    }
+    return e;
+}
+
+// Enqueues the count read-back of slot k and, for device-resident outputs, the copy of its
+// mesh into the caller's buffers (counts read on the device: no host wait).
+static cudaError_t stage_outputs(psr_handle* h, psr_mesh* mesh, int k, int want_colour, int want_normals,
+                                 cudaStream_t s) {
+    Workspace& ws = h->ws;
+    cudaError_t e =
+        cudaMemcpyAsync(h->cnt_host_all + k, slot_ptr(ws.cnt, k), sizeof(Counters), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess && mesh->location == PSR_DEVICE) {
-        k_emit_mesh<<<ws.num_sms * 4, kBlock, 0, s>>>(ws.cnt, ws.mesh_v, ws.mesh_t, ws.mesh_c, ws.mesh_n,
-                                                      mesh->vertices, mesh->triangles,
+        k_emit_mesh<<<ws.num_sms * 4, kBlock, 0, s>>>(slot_ptr(ws.cnt, k), slot_ptr(ws.mesh_v, k),
+                                                      slot_ptr(ws.mesh_t, k), slot_ptr(ws.mesh_c, k),
+                                                      slot_ptr(ws.mesh_n, k), mesh->vertices, mesh->triangles,
                                                       want_colour ? mesh->colors : nullptr,
                                                       want_normals ? mesh->normals : nullptr, mesh->vertex_capacity,
                                                       mesh->triangle_capacity);
         e = cudaGetLastError();
     }
+    return e;
+}
+
+static psr_status check_points(psr_handle* h, const psr_points* pts, const psr_mesh* mesh) {
+    if (!pts || !mesh || !pts->xyz || !pts->normals) return fail(h, PSR_INVALID_INPUT, "null argument");
+    if (pts->count <= 0) return fail(h, PSR_INVALID_INPUT, "empty point cloud");
+    if (pts->count > h->ws.cap.points) return fail(h, PSR_OUT_OF_CAPACITY, "more points than max_points");
+    return PSR_OK;
+}
+
+// Enqueues the reconstruction of `count` clouds (one launch per kernel for all of them) on
+// `stream`, without a host synchronisation.  psr_submit is the one-cloud case.
+static psr_status submit_clouds(psr_handle* h, const psr_points* pts, int count, const psr_options* opt,
+                                psr_mesh* meshes, void* stream, bool batch_call) {
+    if (h->pending) return fail(h, PSR_INVALID_INPUT, "a reconstruction is already in flight on this handle");
+    h->have_result = false;
+    h->batch_stats.clear();
+    h->batch_status.clear();
+    if (!pts || !meshes || count < 1) return fail(h, PSR_INVALID_INPUT, "null argument or no cloud");
+    if (count > h->clouds) return fail(h, PSR_OUT_OF_CAPACITY, "more clouds than the handle's batch_clouds");
+    for (int k = 0; k < count; ++k) {
+        const psr_status st = check_points(h, pts + k, meshes + k);
+        if (st != PSR_OK) return st;
+    }
+    const bool has_rgb = pts[0].rgb != nullptr;
+    const int want_colour = h->cfg.compute_colors && meshes[0].colors;
+    const int want_normals = h->cfg.compute_normals && meshes[0].normals;
+    for (int k = 1; k < count; ++k)
+        if ((pts[k].rgb != nullptr) != has_rgb || (h->cfg.compute_colors && meshes[k].colors) != want_colour ||
+            (h->cfg.compute_normals && meshes[k].normals) != want_normals)
+            return fail(h, PSR_INVALID_INPUT, "the clouds of a batch differ in colour or normal outputs");
+    const int depth = (opt && opt->depth > 0) ? opt->depth : h->cfg.max_depth;
+    if (depth < 2 || depth > h->cfg.max_depth) return fail(h, PSR_INVALID_INPUT, "depth outside [2, max_depth]");
+    const int cg_iters = (opt && opt->cg_iterations > 0) ? opt->cg_iterations : 0;
+    cudaStream_t s = stream ? (cudaStream_t)stream : h->own_stream;
+    cudaError_t e = cudaSetDevice(h->cfg.device);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaSetDevice");
+    for (int k = 0; k < count && e == cudaSuccess; ++k) e = stage_inputs(h, pts + k, k, s);
+    if (e != cudaSuccess) return cuda_fail(h, e, "input copy");
+    e = launch_pipeline(h, depth, cg_iters, want_colour, want_normals, has_rgb, count, s);
+    for (int k = 0; k < count && e == cudaSuccess; ++k) e = stage_outputs(h, meshes + k, k, want_colour, want_normals, s);
     if (e == cudaSuccess) e = cudaEventRecord(h->done, s);
     if (e != cudaSuccess) return cuda_fail(h, e, "reconstruct");
     h->pending = true;
-    h->pend_mesh = mesh;
+    h->pend_meshes.assign(meshes, meshes + count);
+    h->pend_batch = batch_call;
     h->pend_depth = depth;
     h->pend_colour = want_colour;
     h->pend_normals = want_normals;
@@ -535,25 +729,34 @@ static psr_status submit_impl(psr_handle* h, const psr_points* pts, const psr_op
     return PSR_OK;
 }
 
-// After the submitted work has completed: statistics, status, mesh counts, host copies.
-static psr_status complete_impl(psr_handle* h) {
-    h->pending = false;
-    Workspace& ws = h->ws;
-    psr_mesh* mesh = h->pend_mesh;
-    const int depth = h->pend_depth;
-    const int want_colour = h->pend_colour, want_normals = h->pend_normals;
-    cudaStream_t s = h->pend_stream;
-    cudaError_t e = cudaSuccess;
-    Counters& c = *ws.cnt_host;
-    h->host_cnt = c;
-    h->have_result = true;
-    // stats
-    psr_stats& st = h->stats;
+static psr_status status_of(const Counters& c) {
+    if (c.error & kErrInvalid) return PSR_INVALID_INPUT;
+    if (c.error & kErrCapacity) return PSR_OUT_OF_CAPACITY;
+    if (c.error & kErrSpinTimeout) return PSR_DEVICE_TIMEOUT;
+    return PSR_OK;
+}
+
+static const char* status_message(psr_status st) {
+    switch (st) {
+        case PSR_INVALID_INPUT: return "non-finite input or malformed octree";
+        case PSR_OUT_OF_CAPACITY: return "a device count exceeded its capacity";
+        case PSR_DEVICE_TIMEOUT: return "a bounded device wait gave up";
+        default: return "";
+    }
+}
+
+static void fill_stats(const psr_handle* h, const Counters& c, int depth, psr_stats& st) {
     memset(&st, 0, sizeof(st));
     st.points = c.n_points; st.unique_leaves = c.n_unique; st.nodes = c.n_nodes; st.depth = depth;
-    for (int d = 0; d <= kMaxDepth; ++d) { st.level_count[d] = c.level_count[d]; st.cg_iterations[d] = c.cg_iters[d]; st.cg_residual[d] = c.cg_rr[d] > 0 ? sqrt(c.cg_rr[d]) : 0.0;
+    for (int d = 0; d <= kMaxDepth; ++d) {
+        st.level_count[d] = c.level_count[d];
+        st.cg_iterations[d] = c.cg_iters[d];
+        st.cg_residual[d] = c.cg_rr[d] > 0 ? sqrt(c.cg_rr[d]) : 0.0;
         st.cg_true_residual[d] = c.cg_rr_true[d] >= 0 ? sqrt(c.cg_rr_true[d]) : -1.0;
-        st.cg_residual_checks[d] = c.cg_checks[d]; st.cg_restarts[d] = c.cg_restarts[d]; }
+        st.cg_residual_checks[d] = c.cg_checks[d];
+        st.cg_restarts[d] = c.cg_restarts[d];
+        st.cg_depth_ms[d] = (float)(c.cg_depth_ns[d] * 1e-6);
+    }
     st.vertices = c.n_vertices; st.edges = c.n_edges; st.faces = c.n_faces;
     st.crossings = c.n_cross; st.triangles = c.n_tri;
     st.subdivision_roots = c.n_subroots; st.subdivision_nodes = c.n_sub_nodes;
@@ -565,41 +768,101 @@ static psr_status complete_impl(psr_handle* h) {
     for (int i = 0; i < 5; ++i) cudaEventElapsedTime(&st.stage_ms[i], h->ev[i], h->ev[i + 1]);
     cudaEventElapsedTime(&st.stage_ms[5], h->ev[0], h->ev[5]);
     cudaEventElapsedTime(&st.cg_kernel_ms, h->ev[2], h->ev[6]);
-    for (int d = 0; d <= kMaxDepth; ++d) st.cg_depth_ms[d] = (float)(c.cg_depth_ns[d] * 1e-6);
-    if (c.error & kErrInvalid) return fail(h, PSR_INVALID_INPUT, "non-finite input or malformed octree");
-    if (c.error & kErrCapacity) return fail(h, PSR_OUT_OF_CAPACITY, "a device count exceeded its capacity");
-    if (c.error & kErrSpinTimeout) return fail(h, PSR_DEVICE_TIMEOUT, "a bounded device wait gave up");
-    // outputs
+}
+
+// Mesh counts and, for host outputs, the copies of cloud k (after its work completed).
+static psr_status finish_cloud(psr_handle* h, int k, const Counters& c, psr_status st) {
+    Workspace& ws = h->ws;
+    psr_mesh* mesh = &h->pend_meshes[k];
+    cudaStream_t s = h->pend_stream;
+    if (st != PSR_OK) return st;
     mesh->vertex_count = c.n_mesh_vertices;
     mesh->triangle_count = c.n_mesh_triangles;
     for (int a = 0; a < 3; ++a) mesh->center[a] = c.center[a];
     mesh->scale = c.max_edge;
-    if (c.n_mesh_vertices > mesh->vertex_capacity || c.n_mesh_triangles > mesh->triangle_capacity)
-        return fail(h, PSR_OUT_OF_CAPACITY, "output mesh buffers too small");
+    if (c.n_mesh_vertices > mesh->vertex_capacity || c.n_mesh_triangles > mesh->triangle_capacity) {
+        h->last_error = "output mesh buffers too small";
+        return PSR_OUT_OF_CAPACITY;
+    }
     if (mesh->location == PSR_DEVICE) return PSR_OK;   // written by k_emit_mesh
     const cudaMemcpyKind ok = cudaMemcpyDeviceToHost;
+    cudaError_t e = cudaSuccess;
     if (mesh->vertices && c.n_mesh_vertices)
-        e = cudaMemcpyAsync(mesh->vertices, ws.mesh_v, 3 * sizeof(float) * (size_t)c.n_mesh_vertices, ok, s);
+        e = cudaMemcpyAsync(mesh->vertices, slot_ptr(ws.mesh_v, k), 3 * sizeof(float) * (size_t)c.n_mesh_vertices, ok, s);
     if (e == cudaSuccess && mesh->triangles && c.n_mesh_triangles)
-        e = cudaMemcpyAsync(mesh->triangles, ws.mesh_t, 3 * sizeof(int) * (size_t)c.n_mesh_triangles, ok, s);
-    if (e == cudaSuccess && want_colour && c.n_mesh_vertices)
-        e = cudaMemcpyAsync(mesh->colors, ws.mesh_c, 3 * sizeof(float) * (size_t)c.n_mesh_vertices, ok, s);
-    if (e == cudaSuccess && want_normals && c.n_mesh_vertices)
-        e = cudaMemcpyAsync(mesh->normals, ws.mesh_n, 3 * sizeof(float) * (size_t)c.n_mesh_vertices, ok, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        e = cudaMemcpyAsync(mesh->triangles, slot_ptr(ws.mesh_t, k), 3 * sizeof(int) * (size_t)c.n_mesh_triangles, ok, s);
+    if (e == cudaSuccess && h->pend_colour && c.n_mesh_vertices)
+        e = cudaMemcpyAsync(mesh->colors, slot_ptr(ws.mesh_c, k), 3 * sizeof(float) * (size_t)c.n_mesh_vertices, ok, s);
+    if (e == cudaSuccess && h->pend_normals && c.n_mesh_vertices)
+        e = cudaMemcpyAsync(mesh->normals, slot_ptr(ws.mesh_n, k), 3 * sizeof(float) * (size_t)c.n_mesh_vertices, ok, s);
+    return e == cudaSuccess ? PSR_OK : PSR_CUDA_ERROR;
+}
+
+// After the submitted work has completed: statistics, status, mesh counts, host copies.
+static psr_status complete_impl(psr_handle* h) {
+    h->pending = false;
+    const int count = (int)h->pend_meshes.size();
+    h->batch_stats.assign(count, psr_stats{});
+    h->batch_status.assign(count, PSR_OK);
+    psr_status first = PSR_OK;
+    for (int k = 0; k < count; ++k) {
+        const Counters& c = h->cnt_host_all[k];
+        fill_stats(h, c, h->pend_depth, h->batch_stats[k]);
+        const psr_status st = finish_cloud(h, k, c, status_of(c));
+        h->batch_status[k] = st;
+        if (st != PSR_OK && first == PSR_OK) first = st;
+    }
+    const cudaError_t e = cudaStreamSynchronize(h->pend_stream);   // the host copies
+    if (h->pend_batch) {
+        for (int k = 0; k < count; ++k) h->pend_user_meshes[k] = h->pend_meshes[k];
+    } else {
+        // one-cloud call: its results are the handle's (stats, debug arrays)
+        h->host_cnt = h->cnt_host_all[0];
+        h->stats = h->batch_stats[0];
+        h->have_result = true;
+        *h->pend_user_mesh = h->pend_meshes[0];
+    }
     if (e != cudaSuccess) return cuda_fail(h, e, "output copy");
-    return PSR_OK;
+    if (first == PSR_OK) return PSR_OK;
+    if (h->pend_batch) return fail(h, first, "a cloud of the batch failed (see psr_get_batch_result)");
+    if (status_of(h->cnt_host_all[0]) != PSR_OK) return fail(h, first, status_message(first));
+    return first;   // the output buffers were too small (message set by finish_cloud)
 }
 
 psr_status psr_reconstruct(psr_handle* h, const psr_points* pts, const psr_options* opt, psr_mesh* mesh,
                            void* stream) {
-    psr_status st = submit_impl(h, pts, opt, mesh, stream);
+    psr_status st = psr_submit(h, pts, opt, mesh, stream);
     if (st != PSR_OK) return st;
     return psr_wait(h);
 }
 
 psr_status psr_submit(psr_handle* h, const psr_points* pts, const psr_options* opt, psr_mesh* mesh, void* stream) {
-    return submit_impl(h, pts, opt, mesh, stream);
+    if (!h) return PSR_INVALID_INPUT;
+    if (!mesh) return fail(h, PSR_INVALID_INPUT, "null argument");
+    const psr_status st = submit_clouds(h, pts, 1, opt, mesh, stream, false);
+    if (st == PSR_OK) h->pend_user_mesh = mesh;
+    return st;
+}
+
+psr_status psr_submit_batch(psr_handle* h, const psr_points* points, int count, const psr_options* options,
+                            psr_mesh* meshes, void* stream) {
+    if (!h) return PSR_INVALID_INPUT;
+    const psr_status st = submit_clouds(h, points, count, options, meshes, stream, true);
+    if (st == PSR_OK) h->pend_user_meshes = meshes;
+    return st;
+}
+
+psr_status psr_reconstruct_batch(psr_handle* h, const psr_points* points, int count, const psr_options* options,
+                                 psr_mesh* meshes, void* stream) {
+    psr_status st = psr_submit_batch(h, points, count, options, meshes, stream);
+    if (st != PSR_OK) return st;
+    return psr_wait(h);
+}
+
+psr_status psr_get_batch_result(const psr_handle* h, int index, psr_stats* out) {
+    if (!h || index < 0 || index >= (int)h->batch_status.size()) return PSR_INVALID_INPUT;
+    if (out) *out = h->batch_stats[index];
+    return h->batch_status[index];
 }
 
 psr_status psr_poll(psr_handle* h) {
@@ -664,7 +927,7 @@ psr_status psr_estimate_normals(psr_handle* h, const float* xyz, int count, psr_
 
 psr_status psr_memory_bytes(const psr_handle* h, size_t* bytes) {
     if (!h || !bytes) return PSR_INVALID_INPUT;
-    *bytes = h->arena_bytes;
+    *bytes = h->arena_bytes * (size_t)h->clouds;
     return PSR_OK;
 }
 
@@ -676,13 +939,23 @@ psr_status psr_get_stats(const psr_handle* h, psr_stats* out) {
 
 psr_status psr_debug_array(psr_handle* h, const char* name, void* dst, size_t dst_bytes, size_t* bytes) {
     if (!h || !name) return PSR_INVALID_INPUT;
-    if (!h->have_result) return fail(h, PSR_INVALID_INPUT, "no reconstruction yet");
+    // "name@k": the array of cloud k of the last multi-cloud call
+    std::string nm(name);
+    int slot = -1;
+    const size_t at = nm.find('@');
+    if (at != std::string::npos) {
+        slot = atoi(nm.c_str() + at + 1);
+        nm = nm.substr(0, at);
+        if (slot < 0 || slot >= (int)h->batch_stats.size() || slot >= h->clouds || h->pending)
+            return fail(h, PSR_INVALID_INPUT, "no such cloud in the last call");
+    } else if (!h->have_result) {
+        return fail(h, PSR_INVALID_INPUT, "no reconstruction yet");
+    }
     const Workspace& ws = h->ws;
-    const Counters& c = h->host_cnt;
+    const Counters& c = slot >= 0 ? h->cnt_host_all[slot] : h->host_cnt;
     const int D = ws.depth;
     const size_t M = (size_t)c.n_nodes, N = (size_t)c.n_points, MD = (size_t)c.level_count[D];
     struct Item { const void* p; size_t bytes; size_t stride_bytes; int rows; };
-    std::string nm(name);
     std::vector<Item> items;
     auto one = [&](const void* p, size_t b) { items.push_back({p, b, 0, 1}); };
     auto rows = [&](const void* p, int r, size_t row_bytes, size_t stride_bytes) { items.push_back({p, row_bytes, stride_bytes, r}); };
@@ -752,7 +1025,8 @@ psr_status psr_debug_array(psr_handle* h, const char* name, void* dst, size_t ds
     cudaError_t e = cudaSuccess;
     for (auto& it : items)
         for (int r = 0; r < it.rows && e == cudaSuccess; ++r) {
-            e = cudaMemcpy(d, (const char*)it.p + r * it.stride_bytes, it.bytes, cudaMemcpyDeviceToHost);
+            e = cudaMemcpy(d, slot_ptr((const char*)it.p, slot < 0 ? 0 : slot) + r * it.stride_bytes, it.bytes,
+                           cudaMemcpyDeviceToHost);
             d += it.bytes;
         }
     if (e != cudaSuccess) return cuda_fail(h, e, "debug copy");

@@ -40,6 +40,7 @@ __global__ void __launch_bounds__(kBlock) k_vector_field(const Counters* c, int 
                                                          const float* cx, const float* cy, const float* cz,
                                                          const int* neigh, size_t stride, float* vx, float* vy,
                                                          float* vz) {
+    PSR_CLOUD(c, px, py, pz, nx, ny, nz, pidx, pnum, cx, cy, cz, neigh, vx, vy, vz);
     __shared__ int s_off[kVfGroups][28];
     __shared__ int s_base[kVfGroups][27];
     const int md = c->level_count[depth];
@@ -133,6 +134,7 @@ __global__ void __launch_bounds__(kBlock) k_div_leaf(const Counters* c, int dept
                                                      const int* neigh, size_t stride, const float* vx,
                                                      const float* vy, const float* vz, const float* dff,
                                                      float* divg) {
+    PSR_CLOUD(c, enc, neigh, vx, vy, vz, dff, divg);
     const int bD = c->level_base[depth];
     const int MD = c->level_count[depth];
     PSR_GRID_STRIDE(o, MD) {
@@ -168,6 +170,7 @@ __global__ void __launch_bounds__(kBlock) k_div_fine(const Counters* c, int dept
                                                      const int* neigh, size_t stride, const float* vx,
                                                      const float* vy, const float* vz, const float* dff,
                                                      float* divg) {
+    PSR_CLOUD(c, enc, didx, dnum, neigh, vx, vy, vz, dff, divg);
     __shared__ int s_off[kBlock / 32][33];
     __shared__ int s_base[kBlock / 32][32];
     const int b0 = c->level_base[dsplit];
@@ -231,9 +234,11 @@ struct DivChunkLoad {
         }
         return n;
     }
+    __device__ void rebase() { PSR_CLOUD(neigh, dnum); }   // to cloud blockIdx.y
 };
 
 __global__ void k_div_chunk_count(Counters* c, int dsplit, const unsigned* total, int cap, int* n_items) {
+    PSR_CLOUD(c, total, n_items);
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         int n = (int)*total;
         if (n > cap) { atomicOr(&c->error, kErrCapacity); n = 0; }
@@ -248,6 +253,7 @@ __global__ void __launch_bounds__(kBlock) k_div_chunks(const Counters* c, int de
                                                        const int* neigh, size_t stride, const float* vx,
                                                        const float* vy, const float* vz, const float* dff,
                                                        FF* partial) {
+    PSR_CLOUD(c, n_items_ptr, item_start, enc, didx, dnum, neigh, vx, vy, vz, dff, partial);
     const int n_nodes = c->level_base[dsplit];
     const int n_items = *n_items_ptr;
     const int bD = c->level_base[depth];
@@ -288,6 +294,7 @@ __global__ void __launch_bounds__(kBlock) k_div_chunks(const Counters* c, int de
 __global__ void __launch_bounds__(kBlock) k_div_coarse_reduce(const Counters* c, int dsplit, const unsigned* item_start,
                                                               const int* n_items_ptr, const FF* partial,
                                                               float* divg) {
+    PSR_CLOUD(c, item_start, n_items_ptr, partial, divg);
     const int n_nodes = c->level_base[dsplit];
     const int n_items = *n_items_ptr;
     PSR_GRID_STRIDE(i, n_nodes) {
@@ -307,7 +314,7 @@ cudaError_t field_build(Workspace& ws) {
     float* vx = ws.vfield;
     float* vy = ws.vfield + ws.cap.dnodes;
     float* vz = ws.vfield + 2 * (size_t)ws.cap.dnodes;
-    k_vector_field<<<ws.num_sms * 8, kBlock, 0, s>>>(c, D, ws.px, ws.py, ws.pz, ws.nx, ws.ny, ws.nz,
+    k_vector_field<<<PSR_GRID(ws, ws.num_sms * 8), kBlock, 0, s>>>(c, D, ws.px, ws.py, ws.pz, ws.nx, ws.ny, ws.nz,
                                                                     ws.pidx, ws.pnum, ws.ctr_x, ws.ctr_y, ws.ctr_z,
                                                                     ws.neigh, stride, vx, vy, vz);
     const int dsplit = D >= 2 ? D - 2 : 0;
@@ -327,18 +334,18 @@ cudaError_t field_build(Workspace& ws) {
                         0, ws.scan, total, &c->error, a2, ScanCount{}, 1);
         if (e != cudaSuccess) return e;
         const int item_cap = ws.cap.nodes;   // partial buffer holds cap.nodes float pairs
-        k_div_chunk_count<<<1, 1, 0, a2>>>(c, dsplit, total, item_cap, n_items);
+        k_div_chunk_count<<<PSR_GRID(ws, 1), 1, 0, a2>>>(c, dsplit, total, item_cap, n_items);
         FF* partial = reinterpret_cast<FF*>(ws.cg_partial);
-        k_div_chunks<<<ws.num_sms * 8, kBlock, 0, a2>>>(c, D, dsplit, ws.res, n_items, item_start, ws.enc, ws.didx,
+        k_div_chunks<<<PSR_GRID(ws, ws.num_sms * 8), kBlock, 0, a2>>>(c, D, dsplit, ws.res, n_items, item_start, ws.enc, ws.didx,
                                                         ws.dnum, ws.neigh, stride, vx, vy, vz, ws.dff, partial);
-        k_div_coarse_reduce<<<grid_for(ws, 1 << 16), kBlock, 0, a2>>>(c, dsplit, item_start, n_items, partial,
+        k_div_coarse_reduce<<<PSR_GRID(ws, grid_for(ws, 1 << 16)), kBlock, 0, a2>>>(c, dsplit, item_start, n_items, partial,
                                                                      ws.divg);
         e = cudaEventRecord(ws.ev_join, a2);
         if (e != cudaSuccess) return e;
     }
-    k_div_fine<<<ws.num_sms * 8, kBlock, 0, s>>>(c, D, dsplit, ws.res, ws.enc, ws.didx, ws.dnum, ws.neigh, stride, vx,
+    k_div_fine<<<PSR_GRID(ws, ws.num_sms * 8), kBlock, 0, s>>>(c, D, dsplit, ws.res, ws.enc, ws.didx, ws.dnum, ws.neigh, stride, vx,
                                                  vy, vz, ws.dff, ws.divg);
-    k_div_leaf<<<ws.num_sms * 8, kBlock, 0, s>>>(c, D, ws.res, ws.enc, ws.neigh, stride, vx, vy, vz, ws.dff, ws.divg);
+    k_div_leaf<<<PSR_GRID(ws, ws.num_sms * 8), kBlock, 0, s>>>(c, D, ws.res, ws.enc, ws.neigh, stride, vx, vy, vz, ws.dff, ws.divg);
     if (dsplit > 0) {
         e = cudaStreamWaitEvent(s, ws.ev_join, 0);
         if (e != cudaSuccess) return e;

@@ -137,6 +137,7 @@ __device__ __forceinline__ int edge_slot_of(int e, const int a[3]) {
 // ------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(kBlock) k_mesh_reset(const Counters* c, int* node_vtx, int* node_edge,
                                                        int* node_face, int* ov_group, int* ov_sub, size_t stride) {
+    PSR_CLOUD(c, node_vtx, node_edge, node_face, ov_group, ov_sub);
     const int M = c->n_nodes;
     PSR_GRID_STRIDE(i, M) {
         for (int k = 0; k < 8; ++k) node_vtx[(size_t)k * stride + i] = 0;
@@ -150,6 +151,7 @@ __global__ void __launch_bounds__(kBlock) k_mesh_reset(const Counters* c, int* n
 // corner when no other cell around it has a smaller key
 __global__ void __launch_bounds__(kBlock) k_vertex_owner(const Counters* c, const int* key, const int* neigh,
                                                          size_t stride, unsigned char* vmask) {
+    PSR_CLOUD(c, key, neigh, vmask);
     const int M = c->n_nodes;
     PSR_GRID_STRIDE(i, M) {
         const int myk = key[i];
@@ -170,6 +172,7 @@ __global__ void __launch_bounds__(kBlock) k_vertex_owner(const Counters* c, cons
 struct PopcLoad8 {
     const unsigned char* m;
     __device__ unsigned operator()(int i) const { return __popc((unsigned)m[i]); }
+    __device__ void rebase() { PSR_CLOUD(m); }   // to cloud blockIdx.y
 };
 
 struct VertexStore {
@@ -198,11 +201,13 @@ struct VertexStore {
             ++o;
         }
     }
+    __device__ void rebase() { PSR_CLOUD(vmask, ndepth, cx, cy, cz, vx, vy, vz, vowner, vkind, vdepth, err); }   // to cloud blockIdx.y
 };
 
 // maintainVertexNodePointer (mesh/BuildMeshGeometry.cu:108-147)
 __global__ void __launch_bounds__(kBlock) k_vertex_maintain(const Counters* c, const int* neigh, size_t stride,
                                                             const int* vowner, const int* vkind, int* node_vtx) {
+    PSR_CLOUD(c, neigh, vowner, vkind, node_vtx);
     const int V = c->n_vertices;
     PSR_GRID_STRIDE(v, V) {
         const int ow = vowner[v];
@@ -220,6 +225,7 @@ __global__ void __launch_bounds__(kBlock) k_vertex_maintain(const Counters* c, c
 // edge ownership for D-level nodes (initEdgeArray, mesh/BuildMeshGeometry.cu:149-220)
 __global__ void __launch_bounds__(kBlock) k_edge_owner(const Counters* c, int depth, const int* key, const int* neigh,
                                                        size_t stride, unsigned short* emask) {
+    PSR_CLOUD(c, key, neigh, emask);
     const int md = c->level_count[depth];
     const int b = c->level_base[depth];
     PSR_GRID_STRIDE(o, md) {
@@ -243,6 +249,7 @@ __global__ void __launch_bounds__(kBlock) k_edge_owner(const Counters* c, int de
 struct PopcLoad16 {
     const unsigned short* m;
     __device__ unsigned operator()(int i) const { return __popc((unsigned)m[i]); }
+    __device__ void rebase() { PSR_CLOUD(m); }   // to cloud blockIdx.y
 };
 
 struct EdgeStore {
@@ -260,11 +267,13 @@ struct EdgeStore {
         for (int e = 0; e < 12; ++e)
             if ((m >> e) & 1) { eowner[q] = i; ekind[q] = e; ++q; }
     }
+    __device__ void rebase() { PSR_CLOUD(emask, base_ptr, eowner, ekind, err); }   // to cloud blockIdx.y
 };
 
 // maintainEdgeNodePointer (mesh/BuildMeshGeometry.cu:222-280)
 __global__ void __launch_bounds__(kBlock) k_edge_maintain(const Counters* c, const int* neigh, size_t stride,
                                                           const int* eowner, const int* ekind, int* node_edge) {
+    PSR_CLOUD(c, neigh, eowner, ekind, node_edge);
     const int E = c->n_edges;
     PSR_GRID_STRIDE(ei, E) {
         const int ow = eowner[ei], kind = ekind[ei];
@@ -281,6 +290,7 @@ __global__ void __launch_bounds__(kBlock) k_edge_maintain(const Counters* c, con
 // face ownership (initFaceArray, mesh/BuildMeshGeometry.cu:282-354)
 __global__ void __launch_bounds__(kBlock) k_face_owner(const Counters* c, const int* key, const int* neigh,
                                                        size_t stride, unsigned char* fmask) {
+    PSR_CLOUD(c, key, neigh, fmask);
     const int M = c->n_nodes;
     PSR_GRID_STRIDE(i, M) {
         const int myk = key[i];
@@ -320,11 +330,13 @@ struct FaceStore {
             ++q;
         }
     }
+    __device__ void rebase() { PSR_CLOUD(fmask, key, ndepth, parent, fowner, fkind, fhas, err); }   // to cloud blockIdx.y
 };
 
 // maintainFaceNodePointer (mesh/BuildMeshGeometry.cu:356-400)
 __global__ void __launch_bounds__(kBlock) k_face_maintain(const Counters* c, const int* neigh, size_t stride,
                                                           const int* fowner, const int* fkind, int* node_face) {
+    PSR_CLOUD(c, neigh, fowner, fkind, node_face);
     const int F = c->n_faces;
     PSR_GRID_STRIDE(fi, F) {
         const int ow = fowner[fi], kind = fkind[fi];
@@ -352,6 +364,7 @@ __global__ void __launch_bounds__(kBlock) k_vertex_values(const Counters* c, int
                                                           const int* vkind, const int* vdepth, const int* neigh,
                                                           size_t stride, const int* parent, const int* first_child,
                                                           const int* enc, const float* x, float* vvalue) {
+    PSR_CLOUD(c, vx, vy, vz, vowner, vkind, vdepth, neigh, parent, first_child, enc, x, vvalue);
     const int V = c->n_vertices;
     const float iso = c->iso;
     PSR_GRID_STRIDE(v, V) {
@@ -434,6 +447,7 @@ struct CrossLoad {
         const float a = ab[0], b = ab[1];
         return (__fmul_rn(a, b) <= 0.0f) ? 1u : 0u;
     }
+    __device__ void rebase() { PSR_CLOUD(eowner, ekind, node_vtx, vvalue, err); }   // to cloud blockIdx.y
 };
 
 struct CrossStore {
@@ -460,6 +474,7 @@ struct CrossStore {
         interp_point(vx[v1], vy[v1], vz[v1], vx[v2], vy[v2], vz[v2], kind >> 2, vvalue[v1], vvalue[v2],
                      &part_v[3 * (size_t)at]);
     }
+    __device__ void rebase() { PSR_CLOUD(eowner, ekind, node_vtx, vvalue, vx, vy, vz, ecross, part_v, err); }   // to cloud blockIdx.y
 };
 
 struct CubeLoad {
@@ -483,6 +498,7 @@ struct CubeLoad {
         cube_class[o] = cls;
         return (unsigned)__ldg(&g_tab.mc_count[cls]);
     }
+    __device__ void rebase() { PSR_CLOUD(node_vtx, base_ptr, vvalue, cube_class, err); }   // to cloud blockIdx.y
 };
 
 // emits the triangles of a D-level cube and marks surface-edge intersections on faces,
@@ -534,6 +550,7 @@ struct CubeStore {
             }
         }
     }
+    __device__ void rebase() { PSR_CLOUD(cube_class, base_ptr, node_edge, node_face, ecross, parent, fhas, face_hit, part_t, err); }   // to cloud blockIdx.y
 };
 
 // ------------------------------------------------------------------------------------
@@ -572,6 +589,7 @@ struct RootLoad {
             if (fp[f] >= 0 && fh[f]) hi = 1;
         return (fc == -1 && (ht || hi)) ? 1u : 0u;
     }
+    __device__ void rebase() { PSR_CLOUD(node_vtx, node_face, vvalue, face_hit, first_child, err); }   // to cloud blockIdx.y
 };
 struct RootStore {
     int* sub_root;
@@ -582,6 +600,7 @@ struct RootStore {
         if ((int)pre >= cap) { atomicOr(err, kErrCapacity); return; }
         sub_root[pre] = i;
     }
+    __device__ void rebase() { PSR_CLOUD(sub_root, err); }   // to cloud blockIdx.y
 };
 
 // Group table.  Group record (ints): 0 root depth, 1 first root, 2 root count,
@@ -598,6 +617,7 @@ struct GroupFlagLoad {
         if (r == 0 || rd < finer) return 1u;
         return (ndepth[sub_root[r - 1]] != rd) ? 1u : 0u;
     }
+    __device__ void rebase() { PSR_CLOUD(sub_root, ndepth); }   // to cloud blockIdx.y
 };
 struct GroupFlagStore {
     int* root_group;
@@ -612,9 +632,11 @@ struct GroupFlagStore {
             groups[(size_t)g * kGroupRec + 1] = r;
         }
     }
+    __device__ void rebase() { PSR_CLOUD(root_group, groups, err); }   // to cloud blockIdx.y
 };
 
 __global__ void k_group_count(Counters* c, const unsigned* total, int max_groups) {
+    PSR_CLOUD(c, total);
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         int ng = (int)*total;
         if (ng > max_groups) { atomicOr(&c->error, kErrCapacity); ng = 0; }
@@ -625,6 +647,7 @@ __global__ void k_group_count(Counters* c, const unsigned* total, int max_groups
 // per-group sizes (thread per group)
 __global__ void __launch_bounds__(kBlock) k_group_sizes(Counters* c, int depth, const int* sub_root,
                                                         const int* ndepth, int* groups) {
+    PSR_CLOUD(c, sub_root, ndepth, groups);
     const int ng = c->n_groups;
     const int R = c->n_subroots;
     PSR_GRID_STRIDE(g, ng) {
@@ -647,15 +670,18 @@ struct GroupFieldLoad {
     const int* groups;
     int field;
     __device__ unsigned operator()(int g) const { return (unsigned)groups[(size_t)g * kGroupRec + field]; }
+    __device__ void rebase() { PSR_CLOUD(groups); }   // to cloud blockIdx.y
 };
 struct GroupFieldStore {
     int* groups;
     int field;
     __device__ void operator()(int g, unsigned pre, unsigned) const { groups[(size_t)g * kGroupRec + field] = (int)pre; }
+    __device__ void rebase() { PSR_CLOUD(groups); }   // to cloud blockIdx.y
 };
 
 // the virtual numbering of all groups must fit beside the octree indices (na + index)
 __global__ void k_group_totals(Counters* c, const unsigned* node_total, int na) {
+    PSR_CLOUD(c, node_total);
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         const unsigned nt = *node_total;
         if (nt > 0x7fffffffu - (unsigned)na) {
@@ -672,6 +698,7 @@ __global__ void __launch_bounds__(kBlock) k_root_overlay(const Counters* c, int 
                                                          const int* neigh, const int* root_group, const int* groups,
                                                          int* sub_root_depth, int* root_self, int* ov_group,
                                                          int* ov_sub, size_t stride) {
+    PSR_CLOUD(c, sub_root, ndepth, key, parent, neigh, root_group, groups, sub_root_depth, root_self, ov_group, ov_sub);
     const int R = c->n_subroots;
     const int ng = c->n_groups;
     PSR_GRID_STRIDE(r, R) {
@@ -709,6 +736,7 @@ __device__ __forceinline__ int sub_level_off(int rd, int n, int d) {
 
 // per-depth candidate bookkeeping (Counters::sub_*): [d] for depth d; one lane per depth
 __global__ void k_sub_setup(Counters* c, int depth, const int* sub_root_depth, int cap_nodes) {
+    PSR_CLOUD(c, sub_root_depth);
     const int d = threadIdx.x;
     const int R = c->n_subroots;
     __shared__ int s_end[kMaxDepth + 2];
@@ -750,6 +778,7 @@ struct SubArrays {
     unsigned char* touch;   // per live entry: faces of its root's cell it lies on (bits x-, x+, y-, y+, z-, z+)
     int* lv_vnode;   // virtual index of each live depth-D cell
     int cap_nodes, cap_live, cap_live_d;
+    __device__ void rebase() { PSR_CLOUD(vnode, key, group, parent, jump, depth, cx, cy, cz, neigh, live, poly, touch, lv_vnode); }   // to cloud blockIdx.y
 };
 
 // ---- certain-sign cells -------------------------------------------------------------
@@ -792,6 +821,7 @@ __global__ void __launch_bounds__(kBlock) k_root_poly(const Counters* c, int dep
                                                       const float* ctr_z, const int* neigh, size_t stride,
                                                       const int* parent, const int* enc, const float* x,
                                                       float* root_poly, int cap_poly) {
+    PSR_CLOUD(c, sub_root, ndepth, ctr_x, ctr_y, ctr_z, neigh, parent, enc, x, root_poly);
     const int R = c->n_subroots < cap_poly ? c->n_subroots : cap_poly;
     PSR_GRID_STRIDE(r, R) {
         const int node = sub_root[r];
@@ -1167,6 +1197,7 @@ struct SubLevelLoad {
         A.group[slot] = g;
         return 1u;
     }
+    __device__ void rebase() { PSR_CLOUD(c, groups, sub_root, root_group, root_self, key, neigh, first_child, parent, ov_group, ov_sub, enc, x, root_poly, A); }   // to cloud blockIdx.y
 };
 struct SubLevelStore {
     Counters* c;
@@ -1212,6 +1243,7 @@ struct SubLevelStore {
             c->n_sub_dnodes = n;
         }
     }
+    __device__ void rebase() { PSR_CLOUD(c, A, err); }   // to cloud blockIdx.y
 };
 
 // index of virtual node v among the live depth-D cells (sorted), or -1
@@ -1229,6 +1261,7 @@ __device__ __forceinline__ int live_index(const int* lv_vnode, int n, int v) {
 // octree node, or a cell with a certain sign); one thread per (cell, slot)
 __global__ void __launch_bounds__(kBlock) k_sub_live_neigh(const Counters* c, int depth, SubArrays A,
                                                            int* lv_nb, size_t dstride, int na) {
+    PSR_CLOUD(c, A, lv_nb);
     const int nl = c->n_sub_dnodes;
     const int lb = c->sub_lbase[depth];
     const long long n = 27LL * nl;
@@ -1248,6 +1281,7 @@ __global__ void __launch_bounds__(kBlock) k_sub_live_neigh(const Counters* c, in
 __global__ void __launch_bounds__(kBlock) k_sub_vertex_owner(const Counters* c, int depth, SubArrays A,
                                                              const int* lv_nb, size_t dstride,
                                                              unsigned char* s_vmask) {
+    PSR_CLOUD(c, A, lv_nb, s_vmask);
     const int nl = c->n_sub_dnodes;
     const int lb = c->sub_lbase[depth];
     PSR_GRID_STRIDE(L, nl) {
@@ -1292,12 +1326,14 @@ struct SubVertexStore {
             ++q;
         }
     }
+    __device__ void rebase() { PSR_CLOUD(vmask, c, A, vx, vy, vz, vowner, vkind, err); }   // to cloud blockIdx.y
 };
 
 // maintainSubdivideVertexNodePointer (:765-810): s_vtx indexed by live cell
 __global__ void __launch_bounds__(kBlock) k_sub_vertex_maintain(const Counters* c, const int* lv_nb,
                                                                 size_t dstride, const int* vowner, const int* vkind,
                                                                 int* s_vtx) {
+    PSR_CLOUD(c, lv_nb, vowner, vkind, s_vtx);
     const int V = c->n_sub_vertices;
     PSR_GRID_STRIDE(v, V) {
         const int ow = vowner[v];
@@ -1316,6 +1352,7 @@ __global__ void __launch_bounds__(kBlock) k_sub_vertex_maintain(const Counters* 
 __global__ void __launch_bounds__(kBlock) k_sub_edge_owner(const Counters* c, int depth, SubArrays A,
                                                            const int* lv_nb, size_t dstride,
                                                            unsigned short* s_emask) {
+    PSR_CLOUD(c, A, lv_nb, s_emask);
     const int nl = c->n_sub_dnodes;
     const int lb = c->sub_lbase[depth];
     PSR_GRID_STRIDE(L, nl) {
@@ -1350,11 +1387,13 @@ struct SubEdgeStore {
         for (int e = 0; e < 12; ++e)
             if ((m >> e) & 1) { eowner[q] = L; ekind[q] = e; ++q; }
     }
+    __device__ void rebase() { PSR_CLOUD(emask, eowner, ekind, edge_of_live, err); }   // to cloud blockIdx.y
 };
 
 // maintainSubdivideEdgeNodePointer (:888-949)
 __global__ void __launch_bounds__(kBlock) k_sub_edge_maintain(const Counters* c, const int* lv_nb, size_t dstride,
                                                               const int* eowner, const int* ekind, int* s_edge) {
+    PSR_CLOUD(c, lv_nb, eowner, ekind, s_edge);
     const int E = c->n_sub_edges;
     PSR_GRID_STRIDE(ei, E) {
         const int ow = eowner[ei], kind = ekind[ei];
@@ -1386,6 +1425,7 @@ __global__ void __launch_bounds__(kBlock) k_sub_vertex_values(const Counters* c,
                                                               const int* neigh, size_t stride, const int* parent,
                                                               const int* groups, const int* root_self, SubArrays A,
                                                               const int* enc, const float* x, float* vvalue, int na) {
+    PSR_CLOUD(c, vx, vy, vz, vowner, neigh, parent, groups, root_self, A, enc, x, vvalue);
     __shared__ int s_node[kSvWarps][kSvMaxLevels];   // slot (subdivision) or octree node
     __shared__ int s_o[kSvWarps][kSvMaxLevels][3];   // function index of the level's node
     __shared__ float s_t[kSvWarps][kSvMaxLevels * 27];
@@ -1476,6 +1516,7 @@ struct SubCrossLoad {
         const float a = ab[0], b = ab[1];
         return (__fmul_rn(a, b) <= 0.0f) ? 1u : 0u;
     }
+    __device__ void rebase() { PSR_CLOUD(eowner, ekind, s_vtx, vvalue, err); }   // to cloud blockIdx.y
 };
 struct SubCrossStore {
     const int* eowner;
@@ -1502,6 +1543,7 @@ struct SubCrossStore {
         interp_point(vx[v1], vy[v1], vz[v1], vx[v2], vy[v2], vz[v2], kind >> 2, vvalue[v1], vvalue[v2],
                      &part_v[3 * (size_t)at]);
     }
+    __device__ void rebase() { PSR_CLOUD(eowner, ekind, s_vtx, vvalue, vx, vy, vz, ecross, part_v, voff_ptr, err); }   // to cloud blockIdx.y
 };
 
 struct SubCubeLoad {
@@ -1523,6 +1565,7 @@ struct SubCubeLoad {
         cube_class[L] = cls;
         return (unsigned)__ldg(&g_tab.mc_count[cls]);
     }
+    __device__ void rebase() { PSR_CLOUD(s_vtx, vvalue, cube_class, err); }   // to cloud blockIdx.y
 };
 
 // triangles of a live cell; indices relative to its group's first crossing
@@ -1555,6 +1598,7 @@ struct SubCubeStore {
             }
         }
     }
+    __device__ void rebase() { PSR_CLOUD(cube_class, s_edge, ecross, group_cross0, c, A, part_t, toff_ptr, err); }   // to cloud blockIdx.y
 };
 
 // first live index at or after virtual node v
@@ -1573,6 +1617,7 @@ __device__ __forceinline__ int live_lower_bound(const int* lv_vnode, int n, int 
 __global__ void k_part_table(Counters* c, int depth, const int* groups, const int* lv_vnode,
                              const unsigned* edge_of_live, const unsigned* ecross_sub, const unsigned* tri_of_live,
                              unsigned* group_cross0, int* parts) {
+    PSR_CLOUD(c, groups, lv_vnode, edge_of_live, ecross_sub, tri_of_live, group_cross0, parts);
     const int ng = c->n_groups;
     const int nE = c->n_sub_edges;
     const int nl = c->n_sub_dnodes;
@@ -1611,6 +1656,7 @@ __global__ void k_part_table(Counters* c, int depth, const int* groups, const in
 struct KeepVertexLoad {
     const float* part_v;
     __device__ unsigned operator()(int v) const { return (fabsf(part_v[3 * (size_t)v]) < 1e-6f) ? 0u : 1u; }
+    __device__ void rebase() { PSR_CLOUD(part_v); }   // to cloud blockIdx.y
 };
 struct KeepVertexStore {
     const float* part_v;
@@ -1626,6 +1672,7 @@ struct KeepVertexStore {
         mesh_v[3 * (size_t)pre + 1] = part_v[3 * (size_t)v + 1];
         mesh_v[3 * (size_t)pre + 2] = part_v[3 * (size_t)v + 2];
     }
+    __device__ void rebase() { PSR_CLOUD(part_v, mesh_v, kept_prefix, err); }   // to cloud blockIdx.y
 };
 
 __device__ __forceinline__ int find_part(const int* parts, int np, int t) {
@@ -1651,6 +1698,7 @@ struct KeepTriLoad {
         }
         return 1u;
     }
+    __device__ void rebase() { PSR_CLOUD(part_t, parts, np_ptr); }   // to cloud blockIdx.y
 };
 struct KeepTriStore {
     const int* part_t;
@@ -1670,9 +1718,11 @@ struct KeepTriStore {
         const int prev = (vs < *n_staged_v) ? (int)kept_prefix[vs] : *n_kept_v;
         for (int a = 0; a < 3; ++a) mesh_t[3 * (size_t)pre + a] = part_t[3 * (size_t)t + a] + prev;
     }
+    __device__ void rebase() { PSR_CLOUD(part_t, parts, np_ptr, kept_prefix, n_staged_v, n_kept_v, mesh_t, err); }   // to cloud blockIdx.y
 };
 
 __global__ void k_count_parts(Counters* c, int* n_parts, int* n_staged_v, int* n_staged_t, int cap_v, int cap_t) {
+    PSR_CLOUD(c, n_parts, n_staged_v, n_staged_t);
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         *n_parts = 1 + c->n_groups;
         int nv = c->n_cross + c->n_sub_cross, nt = c->n_tri + c->n_sub_tri;
@@ -1693,30 +1743,30 @@ cudaError_t mesh_geometry_impl(Workspace& ws, const MeshBufs& mb, unsigned* tota
     const size_t stride = (size_t)ws.cap.nodes;
     const int gm = grid_for(ws, ws.cap.nodes);
     cudaError_t e;
-    k_mesh_reset<<<gm, kBlock, 0, s>>>(c, ws.node_vtx, ws.node_edge, ws.node_face, mb.ov_group, mb.ov_sub, stride);
+    k_mesh_reset<<<PSR_GRID(ws, gm), kBlock, 0, s>>>(c, ws.node_vtx, ws.node_edge, ws.node_face, mb.ov_group, mb.ov_sub, stride);
     // vertices
-    k_vertex_owner<<<gm, kBlock, 0, s>>>(c, ws.key, ws.neigh, stride, ws.vmask);
+    k_vertex_owner<<<PSR_GRID(ws, gm), kBlock, 0, s>>>(c, ws.key, ws.neigh, stride, ws.vmask);
     e = launch_scan<1>(PopcLoad8{ws.vmask},
                     VertexStore{ws.vmask, ws.ndepth, ws.ctr_x, ws.ctr_y, ws.ctr_z, ws.v_x, ws.v_y, ws.v_z, ws.v_owner,
                                 ws.v_kind, ws.v_depth, ws.cap.vertices, err},
                     &c->n_nodes, 0, ws.scan, total, err, s, ScanCount{&c->n_vertices, ws.cap.vertices});
     if (e != cudaSuccess) return e;
-    k_vertex_maintain<<<gm, kBlock, 0, s>>>(c, ws.neigh, stride, ws.v_owner, ws.v_kind, ws.node_vtx);
+    k_vertex_maintain<<<PSR_GRID(ws, gm), kBlock, 0, s>>>(c, ws.neigh, stride, ws.v_owner, ws.v_kind, ws.node_vtx);
     // edges (D level)
-    k_edge_owner<<<gm, kBlock, 0, s>>>(c, D, ws.key, ws.neigh, stride, ws.emask16);
+    k_edge_owner<<<PSR_GRID(ws, gm), kBlock, 0, s>>>(c, D, ws.key, ws.neigh, stride, ws.emask16);
     e = launch_scan<1>(PopcLoad16{ws.emask16},
                     EdgeStore{ws.emask16, &c->level_base[D], ws.e_owner, ws.e_kind, ws.cap.edges, err},
                     &c->level_count[D], 0, ws.scan, total, err, s, ScanCount{&c->n_edges, ws.cap.edges});
     if (e != cudaSuccess) return e;
-    k_edge_maintain<<<gm, kBlock, 0, s>>>(c, ws.neigh, stride, ws.e_owner, ws.e_kind, ws.node_edge);
+    k_edge_maintain<<<PSR_GRID(ws, gm), kBlock, 0, s>>>(c, ws.neigh, stride, ws.e_owner, ws.e_kind, ws.node_edge);
     // faces
-    k_face_owner<<<gm, kBlock, 0, s>>>(c, ws.key, ws.neigh, stride, ws.fmask);
+    k_face_owner<<<PSR_GRID(ws, gm), kBlock, 0, s>>>(c, ws.key, ws.neigh, stride, ws.fmask);
     e = launch_scan<1>(PopcLoad8{ws.fmask},
                     FaceStore{ws.fmask, ws.key, ws.ndepth, ws.parent, D, ws.f_owner, ws.f_kind, ws.f_hasparent,
                               ws.cap.faces, err},
                     &c->n_nodes, 0, ws.scan, total, err, s, ScanCount{&c->n_faces, ws.cap.faces});
     if (e != cudaSuccess) return e;
-    k_face_maintain<<<gm, kBlock, 0, s>>>(c, ws.neigh, stride, ws.f_owner, ws.f_kind, ws.node_face);
+    k_face_maintain<<<PSR_GRID(ws, gm), kBlock, 0, s>>>(c, ws.neigh, stride, ws.f_owner, ws.f_kind, ws.node_face);
     return cudaGetLastError();
 }
 
@@ -1730,7 +1780,7 @@ cudaError_t mesh_build_impl(Workspace& ws, const MeshBufs& mb) {
     const int gm = grid_for(ws, ws.cap.nodes);
     cudaError_t e;
     // implicit values
-    k_vertex_values<<<gm, kBlock, 0, s>>>(c, D, ws.v_x, ws.v_y, ws.v_z, ws.v_owner, ws.v_kind, ws.v_depth, ws.neigh,
+    k_vertex_values<<<PSR_GRID(ws, gm), kBlock, 0, s>>>(c, D, ws.v_x, ws.v_y, ws.v_z, ws.v_owner, ws.v_kind, ws.v_depth, ws.neigh,
                                           stride, ws.parent, ws.first_child, ws.enc, ws.xsol, ws.vvalue);
     // crossings -> staged vertices of the main part
     e = launch_scan<1>(CrossLoad{ws.e_owner, ws.e_kind, ws.node_vtx, stride, ws.vvalue, err},
@@ -1739,7 +1789,7 @@ cudaError_t mesh_build_impl(Workspace& ws, const MeshBufs& mb) {
                     &c->n_edges, 0, ws.scan, total, err, s, ScanCount{&c->n_cross, ws.part_cap_v});
     if (e != cudaSuccess) return e;
     // face hits must start cleared
-    cudaMemsetAsync(ws.face_hit, 0, sizeof(int) * (size_t)ws.cap.faces, s);
+    fill_words((unsigned*)ws.face_hit, 0u, ws.cap.faces, ws.batch, s);
     e = launch_scan<1>(CubeLoad{ws.node_vtx, stride, &c->level_base[D], ws.vvalue, ws.cube_class, err},
                     CubeStore{ws.cube_class, &c->level_base[D], ws.node_edge, ws.node_face, stride, ws.e_cross,
                               ws.parent, ws.f_hasparent, ws.face_hit, ws.part_t, 0, ws.part_cap_t, err},
@@ -1754,13 +1804,13 @@ cudaError_t mesh_build_impl(Workspace& ws, const MeshBufs& mb) {
                     GroupFlagStore{ws.root_group, mb.groups, mb.max_groups, err}, &c->n_subroots, 0, ws.scan,
                     total, err, s, ScanCount{}, 1);
     if (e != cudaSuccess) return e;
-    k_group_count<<<1, 1, 0, s>>>(c, total, mb.max_groups);
-    k_group_sizes<<<gm, kBlock, 0, s>>>(c, D, ws.sub_root, ws.ndepth, mb.groups);
+    k_group_count<<<PSR_GRID(ws, 1), 1, 0, s>>>(c, total, mb.max_groups);
+    k_group_sizes<<<PSR_GRID(ws, gm), kBlock, 0, s>>>(c, D, ws.sub_root, ws.ndepth, mb.groups);
     e = launch_scan(GroupFieldLoad{mb.groups, 4}, GroupFieldStore{mb.groups, 3}, &c->n_groups, 0, ws.scan, total, err,
                     s, ScanCount{}, 1);
     if (e != cudaSuccess) return e;
-    k_group_totals<<<1, 1, 0, s>>>(c, total, ws.cap.nodes);
-    k_root_overlay<<<gm, kBlock, 0, s>>>(c, D, ws.sub_root, ws.ndepth, ws.key, ws.parent, ws.neigh, ws.root_group,
+    k_group_totals<<<PSR_GRID(ws, 1), 1, 0, s>>>(c, total, ws.cap.nodes);
+    k_root_overlay<<<PSR_GRID(ws, gm), kBlock, 0, s>>>(c, D, ws.sub_root, ws.ndepth, ws.key, ws.parent, ws.neigh, ws.root_group,
                                          mb.groups, ws.sub_root_depth, ws.root_self, mb.ov_group, mb.ov_sub, stride);
     return cudaGetLastError();
 }
@@ -1782,8 +1832,8 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
     SubArrays A{ws.c_vnode, ws.c_key, ws.c_group, ws.c_parent, ws.c_jump, ws.c_depth, ws.c_cx, ws.c_cy, ws.c_cz,
                 ws.c_neigh, (size_t)ws.cap.sub_nodes, ws.c_live, ws.c_poly, ws.c_touch, ws.lv_vnode,
                 ws.cap.sub_nodes, ws.cap.sub_live, ws.cap.sub_dnodes};
-    k_sub_setup<<<1, 32, 0, s>>>(c, D, ws.sub_root_depth, ws.cap.sub_nodes);   // kMaxDepth + 2 <= 32 lanes
-    k_root_poly<<<grid_for(ws, ws.cap_poly), kBlock, 0, s>>>(c, D, ws.sub_root, ws.ndepth, ws.ctr_x, ws.ctr_y,
+    k_sub_setup<<<PSR_GRID(ws, 1), 32, 0, s>>>(c, D, ws.sub_root_depth, ws.cap.sub_nodes);   // kMaxDepth + 2 <= 32 lanes
+    k_root_poly<<<PSR_GRID(ws, grid_for(ws, ws.cap_poly)), kBlock, 0, s>>>(c, D, ws.sub_root, ws.ndepth, ws.ctr_x, ws.ctr_y,
                                                              ws.ctr_z, ws.neigh, stride, ws.parent, ws.enc, ws.xsol,
                                                              ws.root_poly, ws.cap_poly);
     // depth after depth: candidates (children of the live nodes above, then the roots of this
@@ -1797,25 +1847,25 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
         if (e != cudaSuccess) return e;
     }
     // the live depth-D cells carry every record from here on, indexed by their live index
-    k_sub_live_neigh<<<2 * ws.num_sms, kBlock, 0, s>>>(c, D, A, ws.lv_nb, dstride, na);
+    k_sub_live_neigh<<<PSR_GRID(ws, 2 * ws.num_sms), kBlock, 0, s>>>(c, D, A, ws.lv_nb, dstride, na);
     // s_vtx / s_edge need no clearing: every slot of a live cell is written by the owner of
     // that vertex / edge
-    k_sub_vertex_owner<<<gl, kBlock, 0, s>>>(c, D, A, ws.lv_nb, dstride, ws.s_vmask);
+    k_sub_vertex_owner<<<PSR_GRID(ws, gl), kBlock, 0, s>>>(c, D, A, ws.lv_nb, dstride, ws.s_vmask);
     e = launch_scan<2>(PopcLoad8{ws.s_vmask},
                        SubVertexStore{ws.s_vmask, c, D, A, ws.sv_x, ws.sv_y, ws.sv_z, ws.sv_owner, ws.sv_kind,
                                       8 * ws.cap.sub_dnodes, err},
                        &c->n_sub_dnodes, 0, ws.scan, total, err, s, ScanCount{&c->n_sub_vertices, 8 * ws.cap.sub_dnodes},
                        1);
     if (e != cudaSuccess) return e;
-    k_sub_vertex_maintain<<<gl, kBlock, 0, s>>>(c, ws.lv_nb, dstride, ws.sv_owner, ws.sv_kind, ws.s_vtx);
-    k_sub_edge_owner<<<gl, kBlock, 0, s>>>(c, D, A, ws.lv_nb, dstride, ws.s_emask);
+    k_sub_vertex_maintain<<<PSR_GRID(ws, gl), kBlock, 0, s>>>(c, ws.lv_nb, dstride, ws.sv_owner, ws.sv_kind, ws.s_vtx);
+    k_sub_edge_owner<<<PSR_GRID(ws, gl), kBlock, 0, s>>>(c, D, A, ws.lv_nb, dstride, ws.s_emask);
     e = launch_scan<2>(PopcLoad16{ws.s_emask},
                        SubEdgeStore{ws.s_emask, ws.se_owner, ws.se_kind, mb.edge_of_dnode, 12 * ws.cap.sub_dnodes, err},
                        &c->n_sub_dnodes, 0, ws.scan, total, err, s, ScanCount{&c->n_sub_edges, 12 * ws.cap.sub_dnodes},
                        1);
     if (e != cudaSuccess) return e;
-    k_sub_edge_maintain<<<gl, kBlock, 0, s>>>(c, ws.lv_nb, dstride, ws.se_owner, ws.se_kind, ws.s_edge);
-    k_sub_vertex_values<<<4 * ws.num_sms, kBlock, 0, s>>>(
+    k_sub_edge_maintain<<<PSR_GRID(ws, gl), kBlock, 0, s>>>(c, ws.lv_nb, dstride, ws.se_owner, ws.se_kind, ws.s_edge);
+    k_sub_vertex_values<<<PSR_GRID(ws, 4 * ws.num_sms), kBlock, 0, s>>>(
         c, D, ws.sv_x, ws.sv_y, ws.sv_z, ws.sv_owner, ws.neigh, stride, ws.parent, mb.groups, ws.root_self, A, ws.enc,
         ws.xsol, ws.sv_value, na);
     // crossings: staged after the main part's vertices
@@ -1829,7 +1879,7 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
                        StoreExclusive{mb.tri_of_dnode}, &c->n_sub_dnodes, 0, ws.scan, total, err, s,
                        ScanCount{&c->n_sub_tri, ws.part_cap_t}, 1);
     if (e != cudaSuccess) return e;
-    k_part_table<<<grid_for(ws, 1 << 16), kBlock, 0, s>>>(c, D, mb.groups, ws.lv_vnode, mb.edge_of_dnode, ws.se_cross,
+    k_part_table<<<PSR_GRID(ws, grid_for(ws, 1 << 16)), kBlock, 0, s>>>(c, D, mb.groups, ws.lv_vnode, mb.edge_of_dnode, ws.se_cross,
                                                           mb.tri_of_dnode, mb.group_cross0, mb.parts);
     e = launch_scan<2>(SubCubeLoad{ws.s_vtx, dstride, ws.sv_value, ws.s_cube_class, err},
                        SubCubeStore{ws.s_cube_class, ws.s_edge, dstride, ws.se_cross, mb.group_cross0, c, D, A,
@@ -1840,7 +1890,7 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
     int* n_parts = mb.misc;
     int* n_staged_v = mb.misc + 1;
     int* n_staged_t = mb.misc + 2;
-    k_count_parts<<<1, 1, 0, s>>>(c, n_parts, n_staged_v, n_staged_t, ws.part_cap_v, ws.part_cap_t);
+    k_count_parts<<<PSR_GRID(ws, 1), 1, 0, s>>>(c, n_parts, n_staged_v, n_staged_t, ws.part_cap_v, ws.part_cap_t);
     e = launch_scan(KeepVertexLoad{ws.part_v},
                     KeepVertexStore{ws.part_v, ws.mesh_v, mb.kept_prefix, ws.cap.mesh_vertices, err}, n_staged_v, 0,
                     ws.scan, total, err, s, ScanCount{&c->n_mesh_vertices, ws.cap.mesh_vertices}, 1);

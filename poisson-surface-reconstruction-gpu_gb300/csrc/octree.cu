@@ -14,6 +14,7 @@ namespace psr {
 // bounding box (mesh/BuildOctree.cu:51-133) and normalisation parameters (:619-631)
 // ------------------------------------------------------------------------------------
 __global__ void k_reset_counters(Counters* c, const int* params) {
+    PSR_CLOUD(c, params);
     static_assert(sizeof(Counters) % 4 == 0, "Counters is cleared word by word");
     unsigned* w = (unsigned*)c;
     for (int i = threadIdx.x; i < (int)(sizeof(Counters) / 4); i += blockDim.x) w[i] = 0u;
@@ -33,6 +34,7 @@ __global__ void k_reset_counters(Counters* c, const int* params) {
 }
 
 __global__ void __launch_bounds__(kBlock) k_bbox(const float* xyz, const float* nrm, Counters* c) {
+    PSR_CLOUD(xyz, nrm, c);
     const int n = c->n_points;
     float mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX}, mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX};
     bool bad = false;
@@ -68,6 +70,7 @@ __global__ void __launch_bounds__(kBlock) k_bbox(const float* xyz, const float* 
 }
 
 __global__ void k_bbox_finalize(Counters* c, float scale) {
+    PSR_CLOUD(c);
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     float mx[3], mn[3];
     for (int a = 0; a < 3; ++a) {
@@ -99,6 +102,7 @@ __device__ __forceinline__ float normalise_coord(float v, float ctr, float edge)
 // D-l, so the code equals the reference key's upper 32 bits.
 __global__ void __launch_bounds__(kBlock) k_encode(const float* xyz, const Counters* c, int depth,
                                                    unsigned* code, unsigned* sidx) {
+    PSR_CLOUD(xyz, c, code, sidx);
     const int n = c->n_points;
     const float c0 = c->center[0], c1 = c->center[1], c2 = c->center[2], e = c->max_edge;
     PSR_GRID_STRIDE(i, n) {
@@ -126,6 +130,7 @@ __global__ void __launch_bounds__(kBlock) k_gather(const float* xyz, const float
                                                    const unsigned* scode, const unsigned* sidx, const Counters* c,
                                                    int depth, float* px, float* py, float* pz, float* nx, float* ny,
                                                    float* nz, float* cr, float* cg, float* cb, unsigned* head) {
+    PSR_CLOUD(xyz, nrm, rgb, scode, sidx, c, px, py, pz, nx, ny, nz, cr, cg, cb, head);
     const int n = c->n_points;
     const float c0 = c->center[0], c1 = c->center[1], c2 = c->center[2], e = c->max_edge;
     const float nscale = (float)(2 << depth);
@@ -164,9 +169,11 @@ struct HeadStore {
         puid[i] = u;
         if (v) { ucode[u] = scode[i]; ufirst[u] = i; }
     }
+    __device__ void rebase() { PSR_CLOUD(scode, puid, ucode, ufirst); }   // to cloud blockIdx.y
 };
 
 __global__ void k_after_unique(Counters* c, int* ufirst, const unsigned* total) {
+    PSR_CLOUD(c, ufirst, total);
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         c->n_unique = (int)*total;
         ufirst[c->n_unique] = c->n_points;
@@ -179,9 +186,11 @@ struct LeafGroupLoad {
     __device__ unsigned operator()(int u) const {
         return (u == 0) ? 0u : (((ucode[u - 1] >> 3) != (ucode[u] >> 3)) ? 8u : 0u);
     }
+    __device__ void rebase() { PSR_CLOUD(ucode); }   // to cloud blockIdx.y
 };
 
 __global__ void k_after_leaf_groups(Counters* c, const unsigned* total, int depth, int node_cap) {
+    PSR_CLOUD(c, total);
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         int md = (int)*total + 8;
         if (c->n_unique == 0) md = 0;
@@ -195,6 +204,7 @@ __global__ void k_after_leaf_groups(Counters* c, const unsigned* total, int dept
 // level initialisation: D level gets dnum = 1, didx = slot (:294-300), others zero
 __global__ void __launch_bounds__(kBlock) k_init_level(const Counters* c, int d, int depth, int* tkey, int* tpidx,
                                                        int* tpnum, int* tdidx, int* tdnum, int* tchild) {
+    PSR_CLOUD(c, tkey, tpidx, tpnum, tdidx, tdnum, tchild);
     const int m = c->level_count[d];
     const int off = c->level_tmp_off[d];
     PSR_GRID_STRIDE(i, m) {
@@ -211,6 +221,7 @@ __global__ void __launch_bounds__(kBlock) k_init_level(const Counters* c, int d,
 __global__ void __launch_bounds__(kBlock) k_place_leaves(const Counters* c, const unsigned* ucode, const int* ufirst,
                                                          const unsigned* uaddr, int* uslot, int* tkey, int* tpidx,
                                                          int* tpnum) {
+    PSR_CLOUD(c, ucode, ufirst, uaddr, uslot, tkey, tpidx, tpnum);
     const int u_n = c->n_unique;
     PSR_GRID_STRIDE(u, u_n) {
         int s = (int)uaddr[u] + (int)(ucode[u] & 7u);
@@ -223,6 +234,7 @@ __global__ void __launch_bounds__(kBlock) k_place_leaves(const Counters* c, cons
 }
 __global__ void __launch_bounds__(kBlock) k_point2node(const Counters* c, const int* puid, const int* uslot,
                                                        int* point2node) {
+    PSR_CLOUD(c, puid, uslot, point2node);
     const int n = c->n_points;
     PSR_GRID_STRIDE(i, n) point2node[i] = uslot[puid[i]];
 }
@@ -232,6 +244,7 @@ __global__ void __launch_bounds__(kBlock) k_group_aggregate(Counters* c, int d, 
                                                             const int* tpidx, const int* tpnum, const int* tdidx,
                                                             const int* tdnum, int* gkey, int* gpidx, int* gpnum,
                                                             int* gdidx, int* gdnum) {
+    PSR_CLOUD(c, tkey, tpidx, tpnum, tdidx, tdnum, gkey, gpidx, gpnum, gdidx, gdnum);
     const int m = c->level_count[d];
     const int off = c->level_tmp_off[d];
     const int G = m / 8;
@@ -267,9 +280,11 @@ struct FatherGroupLoad {
     __device__ unsigned operator()(int g) const {
         return (g == 0) ? 0u : (((gkey[g - 1] >> sh2) != (gkey[g] >> sh2)) ? 8u : 0u);
     }
+    __device__ void rebase() { PSR_CLOUD(gkey); }   // to cloud blockIdx.y
 };
 
 __global__ void k_after_father_groups(Counters* c, int d, const unsigned* total, int node_cap) {
+    PSR_CLOUD(c, total);
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         int m = (d > 1) ? (int)*total + 8 : 1;
         int off = c->level_tmp_off[d] + c->level_count[d];
@@ -285,6 +300,7 @@ __global__ void __launch_bounds__(kBlock) k_place_fathers(const Counters* c, int
                                                           const int* gdnum, const unsigned* gaddr, int* tkey,
                                                           int* tpidx, int* tpnum, int* tdidx, int* tdnum, int* tchild,
                                                           int* tparent_slot) {
+    PSR_CLOUD(c, gkey, gpidx, gpnum, gdidx, gdnum, gaddr, tkey, tpidx, tpnum, tdidx, tdnum, tchild, tparent_slot);
     const int G = c->n_groups;
     const int off_parent = c->level_tmp_off[d - 1];
     const int off_group = c->level_tmp_off[d] / 8;
@@ -341,6 +357,7 @@ __global__ void __launch_bounds__(kLevelBlock) k_levels_block(Counters* c, int d
                                                               int* tpnum, int* tdidx, int* tdnum, int* tchild,
                                                               int* tparent_slot, int* gkey, int* gpidx, int* gpnum,
                                                               int* gdidx, int* gdnum, unsigned* gaddr, int node_cap) {
+    PSR_CLOUD(c, tkey, tpidx, tpnum, tdidx, tdnum, tchild, tparent_slot, gkey, gpidx, gpnum, gdidx, gdnum, gaddr);
     __shared__ unsigned s_warp[33];
     const int t = threadIdx.x;
     for (int d = dtop; d >= 1; --d) {
@@ -427,6 +444,7 @@ __global__ void __launch_bounds__(kLevelBlock) k_levels_block(Counters* c, int d
 __global__ void __launch_bounds__(kLevelBlock) k_neighbours_block(const Counters* c, int dmax, int depth,
                                                                   const int* key, const int* parent,
                                                                   const int* first_child, int* neigh, size_t stride) {
+    PSR_CLOUD(c, key, parent, first_child, neigh);
     for (int d = 1; d <= dmax; ++d) {
         const int m = c->level_count[d];
         const int b = c->level_base[d];
@@ -446,6 +464,7 @@ __global__ void __launch_bounds__(kLevelBlock) k_neighbours_block(const Counters
 }
 
 __global__ void k_levels_done(Counters* c, int depth) {
+    PSR_CLOUD(c);
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         int b = 0;
         for (int d = 0; d <= depth; ++d) {
@@ -463,6 +482,7 @@ __global__ void __launch_bounds__(kBlock) k_finalize_nodes(const Counters* c, in
                                                            const int* tparent_slot, int* key, int* pidx, int* pnum,
                                                            int* parent, int* first_child, int* didx, int* dnum,
                                                            int* ndepth, int* enc, float* cx, float* cy, float* cz) {
+    PSR_CLOUD(c, tkey, tpidx, tpnum, tdidx, tdnum, tchild, tparent_slot, key, pidx, pnum, parent, first_child, didx, dnum, ndepth, enc, cx, cy, cz);
     const int M = c->n_nodes;
     PSR_GRID_STRIDE(i, M) {
         int d = 0;
@@ -534,6 +554,7 @@ __global__ void __launch_bounds__(kBlock) k_finalize_nodes(const Counters* c, in
 __global__ void __launch_bounds__(kBlock) k_neighbours(const Counters* c, int d, int depth, const int* key,
                                                        const int* parent, const int* first_child, int* neigh,
                                                        size_t stride) {
+    PSR_CLOUD(c, key, parent, first_child, neigh);
     const int m = c->level_count[d];
     const int b = c->level_base[d];
     PSR_GRID_STRIDE(li, m) {
@@ -549,6 +570,7 @@ __global__ void __launch_bounds__(kBlock) k_neighbours(const Counters* c, int d,
 }
 
 __global__ void k_root_neighbours(int* neigh, size_t stride) {
+    PSR_CLOUD(neigh);
     int k = threadIdx.x;
     if (k < 27) neigh[(size_t)k * stride] = (k == 13) ? 0 : -1;
 }
@@ -561,9 +583,9 @@ cudaError_t encode_sort_points(Workspace& ws, const float* xyz, int depth, const
     cudaStream_t s = ws.stream;
     Counters* c = ws.cnt;
     const int gp = grid_for(ws, ws.cap.points);
-    k_bbox<<<gp, kBlock, 0, s>>>(xyz, xyz, c);
-    k_bbox_finalize<<<1, 1, 0, s>>>(c, 1.25f);
-    k_encode<<<gp, kBlock, 0, s>>>(xyz, c, depth, ws.code, ws.sidx);
+    k_bbox<<<PSR_GRID(ws, gp), kBlock, 0, s>>>(xyz, xyz, c);
+    k_bbox_finalize<<<PSR_GRID(ws, 1), 1, 0, s>>>(c, 1.25f);
+    k_encode<<<PSR_GRID(ws, gp), kBlock, 0, s>>>(xyz, c, depth, ws.code, ws.sidx);
     bool alt = false;
     cudaError_t e = radix_sort_pairs(ws.code, ws.sidx, &c->n_points, 3 * depth, ws.sort, &c->error, s, &alt);
     if (e != cudaSuccess) return e;
@@ -579,61 +601,61 @@ cudaError_t octree_build(Workspace& ws) {
     unsigned* err = &c->error;
     unsigned* total = (unsigned*)&c->scan_total;
     const int gp = grid_for(ws, ws.cap.points);
-    k_reset_counters<<<1, 256, 0, s>>>(c, ws.d_params);
-    k_bbox<<<gp, kBlock, 0, s>>>(ws.in_xyz, ws.in_nrm, c);
-    k_bbox_finalize<<<1, 1, 0, s>>>(c, 1.25f);
-    k_encode<<<gp, kBlock, 0, s>>>(ws.in_xyz, c, D, ws.code, ws.sidx);
+    k_reset_counters<<<PSR_GRID(ws, 1), 256, 0, s>>>(c, ws.d_params);
+    k_bbox<<<PSR_GRID(ws, gp), kBlock, 0, s>>>(ws.in_xyz, ws.in_nrm, c);
+    k_bbox_finalize<<<PSR_GRID(ws, 1), 1, 0, s>>>(c, 1.25f);
+    k_encode<<<PSR_GRID(ws, gp), kBlock, 0, s>>>(ws.in_xyz, c, D, ws.code, ws.sidx);
     bool alt = false;
     cudaError_t e = radix_sort_pairs(ws.code, ws.sidx, &c->n_points, 3 * D, ws.sort, err, s, &alt);
     if (e != cudaSuccess) return e;
     const unsigned* scode = alt ? ws.sort.keys_alt : ws.code;
     const unsigned* sidx = alt ? ws.sort.vals_alt : ws.sidx;
     unsigned* head = alt ? ws.code : ws.sort.keys_alt;   // free buffer of N words
-    k_gather<<<gp, kBlock, 0, s>>>(ws.in_xyz, ws.in_nrm, ws.in_rgb, scode, sidx, c, D, ws.px, ws.py, ws.pz, ws.nx,
+    k_gather<<<PSR_GRID(ws, gp), kBlock, 0, s>>>(ws.in_xyz, ws.in_nrm, ws.in_rgb, scode, sidx, c, D, ws.px, ws.py, ws.pz, ws.nx,
                                    ws.ny, ws.nz, ws.cr, ws.cg, ws.cb, head);
     e = launch_scan(LoadArray{head}, HeadStore{scode, ws.puid, ws.ucode, ws.ufirst}, &c->n_points, 0, ws.scan, total,
                     err, s, ScanCount{}, 1);
     if (e != cudaSuccess) return e;
-    k_after_unique<<<1, 1, 0, s>>>(c, ws.ufirst, total);
+    k_after_unique<<<PSR_GRID(ws, 1), 1, 0, s>>>(c, ws.ufirst, total);
     e = launch_scan(LeafGroupLoad{ws.ucode}, StoreInclusive{ws.uaddr}, &c->n_unique, 0, ws.scan, total, err, s,
                     ScanCount{}, 1);
     if (e != cudaSuccess) return e;
-    k_after_leaf_groups<<<1, 1, 0, s>>>(c, total, D, ws.cap.dnodes);
+    k_after_leaf_groups<<<PSR_GRID(ws, 1), 1, 0, s>>>(c, total, D, ws.cap.dnodes);
     const int gn = grid_for(ws, ws.cap.dnodes);
-    k_init_level<<<gn, kBlock, 0, s>>>(c, D, D, ws.tkey, ws.tpidx, ws.tpnum, ws.tdidx, ws.tdnum, ws.tchild);
-    k_place_leaves<<<gp, kBlock, 0, s>>>(c, ws.ucode, ws.ufirst, ws.uaddr, ws.uslot, ws.tkey, ws.tpidx, ws.tpnum);
-    k_point2node<<<gp, kBlock, 0, s>>>(c, ws.puid, ws.uslot, ws.point2node);
+    k_init_level<<<PSR_GRID(ws, gn), kBlock, 0, s>>>(c, D, D, ws.tkey, ws.tpidx, ws.tpnum, ws.tdidx, ws.tdnum, ws.tchild);
+    k_place_leaves<<<PSR_GRID(ws, gp), kBlock, 0, s>>>(c, ws.ucode, ws.ufirst, ws.uaddr, ws.uslot, ws.tkey, ws.tpidx, ws.tpnum);
+    k_point2node<<<PSR_GRID(ws, gp), kBlock, 0, s>>>(c, ws.puid, ws.uslot, ws.point2node);
     // levels D .. dfuse+1 level by level across the GPU, the small levels near the root in
     // one CTA
     const int dfuse = D - 3;
     for (int d = D; d >= 1 && d > dfuse; --d) {
         const int gg = grid_for(ws, ws.cap.dnodes / 8 + 1);
-        k_group_aggregate<<<gg, kBlock, 0, s>>>(c, d, D, ws.tkey, ws.tpidx, ws.tpnum, ws.tdidx, ws.tdnum, ws.gkey,
+        k_group_aggregate<<<PSR_GRID(ws, gg), kBlock, 0, s>>>(c, d, D, ws.tkey, ws.tpidx, ws.tpnum, ws.tdidx, ws.tdnum, ws.gkey,
                                                 ws.gpidx, ws.gpnum, ws.gdidx, ws.gdnum);
         e = launch_scan(FatherGroupLoad{ws.gkey, 3 * (D - d + 2)}, StoreInclusive{ws.gaddr}, &c->n_groups, 0, ws.scan,
                         total, err, s, ScanCount{}, 1);
         if (e != cudaSuccess) return e;
-        k_after_father_groups<<<1, 1, 0, s>>>(c, d, total, ws.cap.nodes);
-        k_init_level<<<gg, kBlock, 0, s>>>(c, d - 1, D, ws.tkey, ws.tpidx, ws.tpnum, ws.tdidx, ws.tdnum, ws.tchild);
-        k_place_fathers<<<gg, kBlock, 0, s>>>(c, d, D, ws.gkey, ws.gpidx, ws.gpnum, ws.gdidx, ws.gdnum, ws.gaddr,
+        k_after_father_groups<<<PSR_GRID(ws, 1), 1, 0, s>>>(c, d, total, ws.cap.nodes);
+        k_init_level<<<PSR_GRID(ws, gg), kBlock, 0, s>>>(c, d - 1, D, ws.tkey, ws.tpidx, ws.tpnum, ws.tdidx, ws.tdnum, ws.tchild);
+        k_place_fathers<<<PSR_GRID(ws, gg), kBlock, 0, s>>>(c, d, D, ws.gkey, ws.gpidx, ws.gpnum, ws.gdidx, ws.gdnum, ws.gaddr,
                                               ws.tkey, ws.tpidx, ws.tpnum, ws.tdidx, ws.tdnum, ws.tchild,
                                               ws.tparent_slot);
     }
     if (dfuse >= 1)
-        k_levels_block<<<1, kLevelBlock, 0, s>>>(c, dfuse, D, ws.tkey, ws.tpidx, ws.tpnum, ws.tdidx, ws.tdnum, ws.tchild,
+        k_levels_block<<<PSR_GRID(ws, 1), kLevelBlock, 0, s>>>(c, dfuse, D, ws.tkey, ws.tpidx, ws.tpnum, ws.tdidx, ws.tdnum, ws.tchild,
                                                  ws.tparent_slot, ws.gkey, ws.gpidx, ws.gpnum, ws.gdidx, ws.gdnum,
                                                  ws.gaddr, ws.cap.nodes);
-    k_levels_done<<<1, 1, 0, s>>>(c, D);
+    k_levels_done<<<PSR_GRID(ws, 1), 1, 0, s>>>(c, D);
     const int gm = grid_for(ws, ws.cap.nodes);
-    k_finalize_nodes<<<gm, kBlock, 0, s>>>(c, D, ws.tkey, ws.tpidx, ws.tpnum, ws.tdidx, ws.tdnum, ws.tchild,
+    k_finalize_nodes<<<PSR_GRID(ws, gm), kBlock, 0, s>>>(c, D, ws.tkey, ws.tpidx, ws.tpnum, ws.tdidx, ws.tdnum, ws.tchild,
                                            ws.tparent_slot, ws.key, ws.pidx, ws.pnum, ws.parent, ws.first_child,
                                            ws.didx, ws.dnum, ws.ndepth, ws.enc, ws.ctr_x, ws.ctr_y, ws.ctr_z);
     const size_t stride = (size_t)ws.cap.nodes;
-    k_root_neighbours<<<1, 32, 0, s>>>(ws.neigh, stride);
+    k_root_neighbours<<<PSR_GRID(ws, 1), 32, 0, s>>>(ws.neigh, stride);
     if (dfuse >= 1)
-        k_neighbours_block<<<1, kLevelBlock, 0, s>>>(c, dfuse, D, ws.key, ws.parent, ws.first_child, ws.neigh, stride);
+        k_neighbours_block<<<PSR_GRID(ws, 1), kLevelBlock, 0, s>>>(c, dfuse, D, ws.key, ws.parent, ws.first_child, ws.neigh, stride);
     for (int d = (dfuse >= 1 ? dfuse + 1 : 1); d <= D; ++d)
-        k_neighbours<<<gm, kBlock, 0, s>>>(c, d, D, ws.key, ws.parent, ws.first_child, ws.neigh, stride);
+        k_neighbours<<<PSR_GRID(ws, gm), kBlock, 0, s>>>(c, d, D, ws.key, ws.parent, ws.first_child, ws.neigh, stride);
     return cudaGetLastError();
 }
 

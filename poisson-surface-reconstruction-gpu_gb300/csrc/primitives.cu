@@ -19,6 +19,7 @@ int scan_grid(int max_tiles, int blocks_per_sm) {
 // Per-tile digit histogram, digit-major layout hist[digit * max_tiles + tile].
 __global__ void __launch_bounds__(kBlock) k_sort_hist(const unsigned* keys, const int* count_ptr, int shift,
                                                       unsigned* hist, int max_tiles, unsigned* err) {
+    PSR_CLOUD(keys, count_ptr, hist, err);
     __shared__ unsigned s_h[kRadix];
     const int n = *count_ptr;
     const int ntiles = (n + kSortTile - 1) / kSortTile;
@@ -49,6 +50,7 @@ struct HistLoad {
         int d = i / nt, t = i - d * nt;
         return hist[(size_t)d * max_tiles + t];
     }
+    __device__ void rebase() { PSR_CLOUD(hist, count_ptr); }   // to cloud blockIdx.y
 };
 struct HistStore {
     unsigned* hist;
@@ -59,10 +61,12 @@ struct HistStore {
         int d = i / nt, t = i - d * nt;
         hist[(size_t)d * max_tiles + t] = pre;
     }
+    __device__ void rebase() { PSR_CLOUD(hist, count_ptr); }   // to cloud blockIdx.y
 };
 
 // number of histogram entries to scan = kRadix * ntiles, written to *n_out
 __global__ void k_sort_hist_count(const int* count_ptr, int* n_out) {
+    PSR_CLOUD(count_ptr, n_out);
     int n = *count_ptr;
     *n_out = kRadix * ((n + kSortTile - 1) / kSortTile);
 }
@@ -74,6 +78,7 @@ __global__ void __launch_bounds__(kBlock) k_sort_scatter(const unsigned* keys_in
                                                          unsigned* keys_out, unsigned* vals_out,
                                                          const int* count_ptr, int shift, const unsigned* offs,
                                                          int max_tiles) {
+    PSR_CLOUD(keys_in, vals_in, keys_out, vals_out, count_ptr, offs);
     __shared__ unsigned s_cnt[kBlock / 32][kRadix];
     const int n = *count_ptr;
     const int ntiles = (n + kSortTile - 1) / kSortTile;
@@ -129,19 +134,34 @@ __global__ void __launch_bounds__(kBlock) k_sort_scatter(const unsigned* keys_in
     }
 }
 
+// p[0 .. n) = v, in every cloud of the launch
+__global__ void __launch_bounds__(kBlock) k_fill_words(unsigned* p, unsigned v, long long n) {
+    PSR_CLOUD(p);
+    for (long long i = blockIdx.x * (long long)kBlock + threadIdx.x; i < n; i += (long long)gridDim.x * kBlock) p[i] = v;
+}
+
+cudaError_t fill_words(unsigned* p, unsigned v, long long n, int clouds, cudaStream_t stream) {
+    const long long g = (n + kBlock - 1) / kBlock;
+    const int cap = scan_grid(1 << 30, 4);
+    const int gx = (int)(g < cap ? (g < 1 ? 1 : g) : cap);
+    k_fill_words<<<dim3(cloud_blocks(clouds, gx), clouds), kBlock, 0, stream>>>(p, v, n);
+    return cudaGetLastError();
+}
+
 cudaError_t radix_sort_pairs(unsigned* keys, unsigned* vals, const int* count_ptr, int key_bits, SortScratch sc,
                              unsigned* err, cudaStream_t stream, bool* result_in_alt) {
     int passes = (key_bits + kRadixBits - 1) / kRadixBits;
     if (passes < 1) passes = 1;
     unsigned *ki = keys, *vi = vals, *ko = sc.keys_alt, *vo = sc.vals_alt;
-    const int grid = scan_grid(sc.max_tiles);
+    const int nb = sc.scan.batch;
+    const dim3 grid(cloud_blocks(nb, scan_grid(sc.max_tiles)), nb);
     // the histogram scan length lives in the last int of the hist scratch area
     int* n_hist = (int*)(sc.hist + (size_t)kRadix * sc.max_tiles);
     unsigned* total = (unsigned*)(n_hist + 1);
     for (int p = 0; p < passes; ++p) {
         const int shift = p * kRadixBits;
         k_sort_hist<<<grid, kBlock, 0, stream>>>(ki, count_ptr, shift, sc.hist, sc.max_tiles, err);
-        k_sort_hist_count<<<1, 1, 0, stream>>>(count_ptr, n_hist);
+        k_sort_hist_count<<<dim3(1, nb), 1, 0, stream>>>(count_ptr, n_hist);
         cudaError_t e = launch_scan(HistLoad{sc.hist, count_ptr, sc.max_tiles}, HistStore{sc.hist, count_ptr, sc.max_tiles},
                                     n_hist, 0, sc.scan, total, err, stream, ScanCount{}, 1);
         if (e != cudaSuccess) return e;

@@ -18,6 +18,8 @@ constexpr int kScanMinTile = kBlock;             // smallest tile (1 item per th
 struct ScanScratch {
     unsigned long long* words;
     int max_tiles;
+    int batch = 1;   // clouds of the launch (host side: the grid's y extent)
+    __device__ void rebase() { PSR_CLOUD(words); }   // to cloud blockIdx.y
 };
 constexpr int kScanHeader = 3;
 
@@ -25,6 +27,7 @@ constexpr int kScanHeader = 3;
 struct ScanCount {
     int* dst = nullptr;
     int cap = 0;
+    __device__ void rebase() { PSR_CLOUD(dst); }   // to cloud blockIdx.y
 };
 
 // Store functors may define `void done(unsigned total) const`: the scan calls it once, after
@@ -80,6 +83,7 @@ __device__ __forceinline__ unsigned block_exclusive_scan(unsigned v, unsigned& e
 template <int kItems, class Load, class Store>
 __global__ void __launch_bounds__(kBlock) k_scan(Load load, Store store, const int* count_ptr, int count_add,
                                                  ScanScratch sc, unsigned* total, unsigned* err, ScanCount cnt) {
+    PSR_CLOUD(load, store, count_ptr, sc, total, err, cnt);
     constexpr int kTile = kBlock * kItems;
     __shared__ unsigned s_warp[kBlock / 32 + 1];
     __shared__ int s_tile;
@@ -207,8 +211,8 @@ template <int kItems = kScanItems, class Load, class Store>
 inline cudaError_t launch_scan(Load load, Store store, const int* count_ptr, int count_add, ScanScratch sc,
                                unsigned* total, unsigned* err, cudaStream_t stream, ScanCount cnt = ScanCount{},
                                int blocks_per_sm = 4) {
-    k_scan<kItems, Load, Store><<<scan_grid(sc.max_tiles, blocks_per_sm), kBlock, 0, stream>>>(
-        load, store, count_ptr, count_add, sc, total, err, cnt);
+    const dim3 grid(cloud_blocks(sc.batch, scan_grid(sc.max_tiles, blocks_per_sm)), sc.batch);
+    k_scan<kItems, Load, Store><<<grid, kBlock, 0, stream>>>(load, store, count_ptr, count_add, sc, total, err, cnt);
     return cudaGetLastError();
 }
 
@@ -216,14 +220,17 @@ inline cudaError_t launch_scan(Load load, Store store, const int* count_ptr, int
 struct LoadArray {
     const unsigned* a;
     __device__ unsigned operator()(int i) const { return a[i]; }
+    __device__ void rebase() { PSR_CLOUD(a); }   // to cloud blockIdx.y
 };
 struct StoreExclusive {
     unsigned* out;
     __device__ void operator()(int i, unsigned pre, unsigned) const { out[i] = pre; }
+    __device__ void rebase() { PSR_CLOUD(out); }   // to cloud blockIdx.y
 };
 struct StoreInclusive {
     unsigned* out;
     __device__ void operator()(int i, unsigned pre, unsigned v) const { out[i] = pre + v; }
+    __device__ void rebase() { PSR_CLOUD(out); }   // to cloud blockIdx.y
 };
 
 // ---- radix sort ------------------------------------------------------------------------
@@ -239,6 +246,10 @@ struct SortScratch {
     int max_tiles;
     ScanScratch scan;
 };
+
+// n 32-bit words at p set to v, in each of `clouds` clouds (a memset that multi-cloud
+// launches can take: every cloud's copy of the buffer)
+cudaError_t fill_words(unsigned* p, unsigned v, long long n, int clouds, cudaStream_t stream);
 
 cudaError_t radix_sort_pairs(unsigned* keys, unsigned* vals, const int* count_ptr, int key_bits, SortScratch sc,
                              unsigned* err, cudaStream_t stream, bool* result_in_alt);

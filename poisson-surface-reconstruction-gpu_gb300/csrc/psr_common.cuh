@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <cfloat>
 #include <cstdint>
+#include <cstdio>
 
 namespace psr {
 
@@ -68,7 +69,50 @@ struct ConstTables {
     int mc_count[256];
 };
 
+// ---- multi-cloud launches --------------------------------------------------------------
+// A batch handle keeps one complete workspace per cloud.  The workspaces sit in one
+// reserved address range, slot k at k * kCloudStride from slot 0, so a workspace pointer
+// of cloud 0 plus k * kCloudStride is the same buffer of cloud k.  Every kernel of the
+// pipeline is launched once for all the clouds of a batch with gridDim.y = clouds, and
+// first moves each of its workspace pointers (PSR_CLOUD) to cloud blockIdx.y; a one-cloud
+// launch has blockIdx.y = 0 and keeps them.  Null pointers (absent optional inputs) stay
+// null.  The range is aligned to kMaxBatchClouds * kCloudStride, so bits 35..40 of a
+// workspace address are its slot.
+constexpr unsigned long long kCloudStride = 1ull << 35;   // 32 GiB of address space per cloud
+constexpr int kMaxBatchClouds = 64;
+
+// blocks along x of a launch over `clouds` clouds whose one-cloud launch has gx blocks:
+// about twice the one-cloud grid in total (each cloud's blocks stride over its work), at
+// least one block per cloud
+inline int cloud_blocks(int clouds, int gx) {
+    if (clouds <= 1) return gx;
+    const int g = (2 * gx + clouds - 1) / clouds;
+    return g < 1 ? 1 : (g < gx ? g : gx);
+}
+
 #ifdef __CUDACC__
+template <class T>
+__device__ __forceinline__ void cloud_rebase_one(T*& p) {
+#ifdef PSR_CLOUD_CHECK
+    // diagnostic builds: a pointer handed to a multi-cloud launch must be slot 0's
+    if (blockIdx.y != 0 && p && ((((unsigned long long)p) >> 35) & (kMaxBatchClouds - 1)) != 0) {
+        if (threadIdx.x == 0 && blockIdx.x == 0)
+            printf("PSR_CLOUD_CHECK: cloud %u got a pointer outside slot 0: %p\n", blockIdx.y, (const void*)p);
+        return;
+    }
+#endif
+    if (p) p = (T*)((const char*)p + (unsigned long long)blockIdx.y * kCloudStride);
+}
+template <class S>
+__device__ __forceinline__ auto cloud_rebase_one(S& s) -> decltype(s.rebase(), void()) {
+    s.rebase();
+}
+template <class... T>
+__device__ __forceinline__ void cloud_rebase(T&... p) {
+    (cloud_rebase_one(p), ...);
+}
+#define PSR_CLOUD(...) ::psr::cloud_rebase(__VA_ARGS__)
+
 #define PSR_GRID_STRIDE(i, n) for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += gridDim.x * blockDim.x)
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }

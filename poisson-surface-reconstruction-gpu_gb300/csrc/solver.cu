@@ -94,14 +94,13 @@ static_assert(kCgSmemRows % 32 == 0, "whole warp slots");
 
 constexpr int kCgMaxRefine = 4;
 
-struct CgcArgs {
+// Workspace pointers of the CG; a multi-cloud launch moves them to the CTA's cloud (a
+// copy in registers: the launch parameters below stay where the launch put them).
+struct CgcVec {
     const Counters* c;
     Counters* cw;
-    int depth;
-    int first;          // depth of cluster / CTA 0; unit u solves depth first - u
     const int* neigh;
     const int* blk;     // block table: 64 entries per sibling group of depth >= 1
-    size_t stride;
     const float* stencil;
     const float* b;
     float* x;
@@ -109,6 +108,14 @@ struct CgcArgs {
     float* pa;
     float* pb;
     float* ap;
+    __device__ void rebase() { PSR_CLOUD(c, cw, neigh, blk, stencil, b, x, r, pa, pb, ap); }
+};
+
+struct CgcArgs {
+    CgcVec v;
+    int depth;
+    int first;          // depth of cluster / CTA 0; unit u solves depth first - u
+    size_t stride;
     float tol2;
     int max_iter;
     int res_period;     // > 0: true residual every res_period iterations; 0: only at
@@ -213,11 +220,11 @@ __device__ __forceinline__ void cg_start(CgcShared& sh, const CgcArgs& a, double
 }
 
 // Per-depth results of a finished solve (thread 0 of cluster CTA 0).
-__device__ __forceinline__ void cg_report(const CgcArgs& a, int d, const CgcShared& sh) {
-    a.cw->cg_rr[d] = sh.rr;
-    a.cw->cg_rr_true[d] = sh.rr_true;
-    a.cw->cg_checks[d] = sh.checks;
-    a.cw->cg_restarts[d] = sh.restarts;
+__device__ __forceinline__ void cg_report(const CgcVec& v, int d, const CgcShared& sh) {
+    v.cw->cg_rr[d] = sh.rr;
+    v.cw->cg_rr_true[d] = sh.rr_true;
+    v.cw->cg_checks[d] = sh.checks;
+    v.cw->cg_restarts[d] = sh.restarts;
 }
 
 // position of neighbour k (9 ox + 3 oy + oz) of sibling s (x = 4, y = 2, z = 1) in the
@@ -232,6 +239,7 @@ __device__ __forceinline__ int cg_spos(int s) { return 16 * ((s >> 2) & 1) + 4 *
 // 8 positions s, s + 8, ... as two contiguous int4.
 __global__ void __launch_bounds__(kBlock) k_cg_blocks(const Counters* c, const int* neigh, size_t stride,
                                                       int* blk) {
+    PSR_CLOUD(c, neigh, blk);
     const int ngroups = (c->n_nodes - 1) >> 3;
     PSR_GRID_STRIDE(t, ngroups * 64) {
         const int G = t >> 6, j = t & 63;
@@ -275,7 +283,7 @@ __device__ __forceinline__ float cg_ld_x(unsigned x_sa, unsigned desc) {
 // constant operand of the FMAs; U < 0: the stencil staged in shared memory.
 template <int U>
 __device__ __forceinline__ void cgc_resident(cg::cluster_group& cl, CgcShared& sh, const CgcArgs& a,
-                                             const CgUnit& u, int chunk, float2* rp0, float2* rp1, float* sap,
+                                             const CgcVec& v, const CgUnit& u, int chunk, float2* rp0, float2* rp1, float* sap,
                                              float* sx, float* sblk) {
     const unsigned me = cl.block_rank();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -294,7 +302,7 @@ __device__ __forceinline__ void cgc_resident(cg::cluster_group& cl, CgcShared& s
     // byte offset of the row inside that CTA's buffer (the zero row for an absent cell), so
     // an iteration reads a neighbour with one mapped load instead of locating its owner.
     // Only this CTA reads these groups' entries; the barrier below publishes them.
-    int* blkw = const_cast<int*>(a.blk);
+    int* blkw = const_cast<int*>(v.blk);
     for (int t = threadIdx.x; t < nloc * 8; t += kCgcBlock) {
         const size_t at = (size_t)gbase * 64 + t;
         const int nb = blkw[at];
@@ -317,7 +325,7 @@ __device__ __forceinline__ void cgc_resident(cg::cluster_group& cl, CgcShared& s
     // r0 = b, p_{-1} = 0, x0 = 0
     FF acc = ff_zero();
     for (int l = threadIdx.x; l < nloc; l += kCgcBlock) {
-        const float bi = a.b[mlo + l];
+        const float bi = v.b[mlo + l];
         rp0[l] = make_float2(bi, 0.0f);
         sx[l] = 0.0f;
         acc = ff_add(acc, ff_prod(bi, bi));
@@ -336,7 +344,7 @@ __device__ __forceinline__ void cgc_resident(cg::cluster_group& cl, CgcShared& s
         // slot is processed (they do not change between iterations)
         int4 q0 = make_int4(-1, -1, -1, -1), q1 = q0;
         if (warp < nslot && warp * 32 + lane < nloc) {
-            const int4* bp = reinterpret_cast<const int4*>(a.blk + (size_t)(gbase + ((warp * 32 + lane) >> 3)) * 64 + sib * 8);
+            const int4* bp = reinterpret_cast<const int4*>(v.blk + (size_t)(gbase + ((warp * 32 + lane) >> 3)) * 64 + sib * 8);
             q0 = bp[0];
             q1 = bp[1];
         }
@@ -347,7 +355,7 @@ __device__ __forceinline__ void cgc_resident(cg::cluster_group& cl, CgcShared& s
             const int ids[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
             const int ln = l + kCgWarps * 32;
             if (ln < nloc) {
-                const int4* bp = reinterpret_cast<const int4*>(a.blk + (size_t)(gbase + (ln >> 3)) * 64 + sib * 8);
+                const int4* bp = reinterpret_cast<const int4*>(v.blk + (size_t)(gbase + (ln >> 3)) * 64 + sib * 8);
                 q0 = bp[0];
                 q1 = bp[1];
             }
@@ -391,7 +399,7 @@ __device__ __forceinline__ void cgc_resident(cg::cluster_group& cl, CgcShared& s
         }
         cgc_allreduce(cl, sh, buf, acc, [&](double w) { cg_after_rr(sh, a, w, it); });
         ran = true;
-        if (me == 0 && threadIdx.x == 0) a.cw->cg_iters[u.d] = it;
+        if (me == 0 && threadIdx.x == 0) v.cw->cg_iters[u.d] = it;
         float2* t = cur;
         cur = nxt;
         nxt = t;
@@ -406,7 +414,7 @@ __device__ __forceinline__ void cgc_resident(cg::cluster_group& cl, CgcShared& s
                 const int l = sl * 32 + lane;
                 const bool mine = l < nloc;
                 if (mine) {
-                    const int4* bp = reinterpret_cast<const int4*>(a.blk + (size_t)(gbase + (l >> 3)) * 64 + sib * 8);
+                    const int4* bp = reinterpret_cast<const int4*>(v.blk + (size_t)(gbase + (l >> 3)) * 64 + sib * 8);
                     const int4 d0 = bp[0], d1 = bp[1];
                     const int ids[8] = {d0.x, d0.y, d0.z, d0.w, d1.x, d1.y, d1.z, d1.w};
                     float vals[8];
@@ -421,7 +429,7 @@ __device__ __forceinline__ void cgc_resident(cg::cluster_group& cl, CgcShared& s
 #pragma unroll
                     for (int k = 0; k < 27; ++k)
                         y = ff_add(y, ff_prod(U >= 0 ? a.stp[U < 0 ? 0 : U][k] : sh.st[k], myblk[spos + cg_kpos(k)]));
-                    const float ri = ff_to_float(ff_add(FF{a.b[mlo + l], 0.0f}, FF{-y.hi, -y.lo}));
+                    const float ri = ff_to_float(ff_add(FF{v.b[mlo + l], 0.0f}, FF{-y.hi, -y.lo}));
                     sap[l] = ri;
                     acc = ff_add(acc, ff_prod(ri, ri));
                 }
@@ -435,44 +443,44 @@ __device__ __forceinline__ void cgc_resident(cg::cluster_group& cl, CgcShared& s
         }
     }
     for (int l = threadIdx.x; l < nloc; l += kCgcBlock) {
-        a.x[mlo + l] = sx[l];
-        a.r[mlo + l] = cur[l].x;
+        v.x[mlo + l] = sx[l];
+        v.r[mlo + l] = cur[l].x;
     }
-    if (ran && me == 0 && threadIdx.x == 0) cg_report(a, u.d, sh);
+    if (ran && me == 0 && threadIdx.x == 0) cg_report(v, u.d, sh);
 }
 
 // Global-memory path (any size, any depth).
 __device__ __forceinline__ void cgc_global(cg::cluster_group& cl, CgcShared& sh, const CgcArgs& a,
-                                           const CgUnit& u) {
+                                           const CgcVec& v, const CgUnit& u) {
     const int tid = cl.block_rank() * blockDim.x + threadIdx.x;
     const int nthr = cl.num_blocks() * blockDim.x;
     FF acc = ff_zero();
     for (int i = u.row0 + tid; i < u.row1; i += nthr) {
-        const float bi = a.b[i];
-        a.r[i] = bi;
-        a.pa[i] = 0.0f;
-        a.x[i] = 0.0f;
+        const float bi = v.b[i];
+        v.r[i] = bi;
+        v.pa[i] = 0.0f;
+        v.x[i] = 0.0f;
         acc = ff_add(acc, ff_prod(bi, bi));
     }
     int buf = 0;
     cgc_allreduce(cl, sh, buf, acc, [&](double w) { cg_start(sh, a, w); });
     bool ran = false;
-    const float* pprev = a.pa;
-    float* pcur = a.pb;
+    const float* pprev = v.pa;
+    float* pcur = v.pb;
     int it = 1;
     while (sh.go) {
         const float beta = sh.beta;
         acc = ff_zero();
         for (int i = u.row0 + tid; i < u.row1; i += nthr) {
-            const float pi = fmaf(beta, pprev[i], a.r[i]);
+            const float pi = fmaf(beta, pprev[i], v.r[i]);
             float y = 0.0f;
 #pragma unroll 9
             for (int k = 0; k < 27; ++k) {
-                const int nb = __ldg(&a.neigh[(size_t)k * a.stride + i]);
-                if (nb >= 0) y = fmaf(sh.st[k], fmaf(beta, pprev[nb], a.r[nb]), y);
+                const int nb = __ldg(&v.neigh[(size_t)k * a.stride + i]);
+                if (nb >= 0) y = fmaf(sh.st[k], fmaf(beta, pprev[nb], v.r[nb]), y);
             }
             pcur[i] = pi;
-            a.ap[i] = y;
+            v.ap[i] = y;
             acc = ff_add(acc, ff_prod(pi, y));
         }
         cgc_allreduce(cl, sh, buf, acc, [&](double w) {
@@ -482,14 +490,14 @@ __device__ __forceinline__ void cgc_global(cg::cluster_group& cl, CgcShared& sh,
         const float alpha = sh.alpha;
         acc = ff_zero();
         for (int i = u.row0 + tid; i < u.row1; i += nthr) {
-            a.x[i] = fmaf(alpha, pcur[i], a.x[i]);
-            const float ri = fmaf(-alpha, a.ap[i], a.r[i]);
-            a.r[i] = ri;
+            v.x[i] = fmaf(alpha, pcur[i], v.x[i]);
+            const float ri = fmaf(-alpha, v.ap[i], v.r[i]);
+            v.r[i] = ri;
             acc = ff_add(acc, ff_prod(ri, ri));
         }
         cgc_allreduce(cl, sh, buf, acc, [&](double w) { cg_after_rr(sh, a, w, it); });
         ran = true;
-        if (cl.block_rank() == 0 && threadIdx.x == 0) a.cw->cg_iters[u.d] = it;
+        if (cl.block_rank() == 0 && threadIdx.x == 0) v.cw->cg_iters[u.d] = it;
         float* t = const_cast<float*>(pprev);
         pprev = pcur;
         pcur = t;
@@ -500,36 +508,36 @@ __device__ __forceinline__ void cgc_global(cg::cluster_group& cl, CgcShared& sh,
             for (int i = u.row0 + tid; i < u.row1; i += nthr) {
                 FF y = ff_zero();
                 for (int k = 0; k < 27; ++k) {
-                    const int nb = __ldg(&a.neigh[(size_t)k * a.stride + i]);
-                    if (nb >= 0) y = ff_add(y, ff_prod(sh.st[k], a.x[nb]));
+                    const int nb = __ldg(&v.neigh[(size_t)k * a.stride + i]);
+                    if (nb >= 0) y = ff_add(y, ff_prod(sh.st[k], v.x[nb]));
                 }
-                const float ri = ff_to_float(ff_add(FF{a.b[i], 0.0f}, FF{-y.hi, -y.lo}));
-                a.ap[i] = ri;   // staged; A p holds nothing live here
+                const float ri = ff_to_float(ff_add(FF{v.b[i], 0.0f}, FF{-y.hi, -y.lo}));
+                v.ap[i] = ri;   // staged; A p holds nothing live here
                 acc = ff_add(acc, ff_prod(ri, ri));
             }
             cgc_allreduce(cl, sh, buf, acc, [&](double w) { cg_after_true(sh, a, w, it); });
             if (sh.replace) {   // refinement restart: CG continues from the true residual
-                for (int i = u.row0 + tid; i < u.row1; i += nthr) a.r[i] = a.ap[i];
+                for (int i = u.row0 + tid; i < u.row1; i += nthr) v.r[i] = v.ap[i];
                 cl.sync();
             }
         }
     }
-    if (ran && cl.block_rank() == 0 && threadIdx.x == 0) cg_report(a, u.d, sh);
+    if (ran && cl.block_rank() == 0 && threadIdx.x == 0) cg_report(v, u.d, sh);
 }
 
 // one depth per cluster (a CTA when the launch has no cluster dimension); kClusterUnits:
 // the unit's stencil is a launch parameter
 template <bool kClusterUnits>
-__device__ __forceinline__ void cg_unit_body(const CgcArgs& a, int unit) {
+__device__ __forceinline__ void cg_unit_body(const CgcArgs& a, const CgcVec& v, int unit) {
     cg::cluster_group cl = cg::this_cluster();
     __shared__ CgcShared sh;
     extern __shared__ float4 cg_dyn[];
     const unsigned long long t_start = global_ns();
     CgUnit u;
     u.d = a.first - unit;
-    u.row0 = a.c->level_base[u.d];
-    u.row1 = (u.d < a.depth) ? a.c->level_base[u.d + 1] : a.c->n_nodes;
-    if (threadIdx.x < 27) sh.st[threadIdx.x] = a.stencil[u.d * 27 + threadIdx.x];
+    u.row0 = v.c->level_base[u.d];
+    u.row1 = (u.d < a.depth) ? v.c->level_base[u.d + 1] : v.c->n_nodes;
+    if (threadIdx.x < 27) sh.st[threadIdx.x] = v.stencil[u.d * 27 + threadIdx.x];
     __syncthreads();
     const int nblk = (int)cl.num_blocks();
     const int m = u.row1 - u.row0;
@@ -540,23 +548,29 @@ __device__ __forceinline__ void cg_unit_body(const CgcArgs& a, int unit) {
         float* sap = reinterpret_cast<float*>(rp1 + kCgSmemRows);
         float* sx = sap + kCgSmemRows;
         float* sblk = sx + kCgSmemRows;
-        if (kClusterUnits && unit == 0) cgc_resident<0>(cl, sh, a, u, chunk, rp0, rp1, sap, sx, sblk);
-        else if (kClusterUnits && unit == 1) cgc_resident<1>(cl, sh, a, u, chunk, rp0, rp1, sap, sx, sblk);
-        else if (kClusterUnits && unit == 2) cgc_resident<2>(cl, sh, a, u, chunk, rp0, rp1, sap, sx, sblk);
-        else cgc_resident<-1>(cl, sh, a, u, chunk, rp0, rp1, sap, sx, sblk);
+        if (kClusterUnits && unit == 0) cgc_resident<0>(cl, sh, a, v, u, chunk, rp0, rp1, sap, sx, sblk);
+        else if (kClusterUnits && unit == 1) cgc_resident<1>(cl, sh, a, v, u, chunk, rp0, rp1, sap, sx, sblk);
+        else if (kClusterUnits && unit == 2) cgc_resident<2>(cl, sh, a, v, u, chunk, rp0, rp1, sap, sx, sblk);
+        else cgc_resident<-1>(cl, sh, a, v, u, chunk, rp0, rp1, sap, sx, sblk);
     } else {
-        cgc_global(cl, sh, a, u);
+        cgc_global(cl, sh, a, v, u);
     }
     cl.sync();   // no CTA exits while others may still read its shared memory
-    if (cl.block_rank() == 0 && threadIdx.x == 0) a.cw->cg_depth_ns[u.d] = global_ns() - t_start;
+    if (cl.block_rank() == 0 && threadIdx.x == 0) v.cw->cg_depth_ns[u.d] = global_ns() - t_start;
 }
 
 __global__ void __launch_bounds__(kCgcBlock) k_cg_cluster(CgcArgs a) {
     cg::cluster_group cl = cg::this_cluster();
-    cg_unit_body<true>(a, (int)(blockIdx.x / cl.num_blocks()));
+    CgcVec v = a.v;
+    v.rebase();
+    cg_unit_body<true>(a, v, (int)(blockIdx.x / cl.num_blocks()));
 }
 
-__global__ void __launch_bounds__(kCgcBlock) k_cg_cta(CgcArgs a) { cg_unit_body<false>(a, (int)blockIdx.x); }
+__global__ void __launch_bounds__(kCgcBlock) k_cg_cta(CgcArgs a) {
+    CgcVec v = a.v;
+    v.rebase();
+    cg_unit_body<false>(a, v, (int)blockIdx.x);
+}
 
 // ---- implicit function at the sample points and the iso-value ----------------------
 __device__ __forceinline__ void decode3s(int e, int depth, int& ix, int& iy, int& iz) {
@@ -578,6 +592,7 @@ __global__ void __launch_bounds__(kBlock) k_point_poly(const Counters* c, int de
                                                        const float* ctr_y, const float* ctr_z, const int* neigh,
                                                        size_t stride, const int* parent, const int* enc,
                                                        const float* x, float* coef, size_t cstride) {
+    PSR_CLOUD(c, ctr_x, ctr_y, ctr_z, neigh, parent, enc, x, coef);
     const int d1 = depth - 1;
     const int n = c->level_count[d1];
     const int b = c->level_base[d1];
@@ -609,6 +624,7 @@ __global__ void __launch_bounds__(kBlock) k_point_values_coarse(const Counters* 
                                                                 const float* ctr_x, const float* ctr_y,
                                                                 const float* ctr_z, const float* coef,
                                                                 size_t cstride, float* out) {
+    PSR_CLOUD(c, px, py, pz, point2node, parent, ctr_x, ctr_y, ctr_z, coef, out);
     const int n = c->n_points;
     const int bD = c->level_base[depth];
     const int b1 = c->level_base[depth - 1];
@@ -632,33 +648,44 @@ __global__ void __launch_bounds__(kBlock) k_point_values_coarse(const Counters* 
     }
 }
 
+// The sample values are summed in chunks of kBlock points (chunk_sums[chunk]), then the
+// chunks in order: the iso-value's summation order depends only on the point count, not on
+// the launch's grid, so a cloud gets the same iso-value alone and in a multi-cloud launch.
 __global__ void __launch_bounds__(kBlock) k_point_values(const Counters* c, int depth, const float* px,
                                                          const float* py, const float* pz, const int* point2node,
                                                          const int* neigh, size_t stride, const int* enc,
-                                                         const float* x, float* out, double* block_sums) {
+                                                         const float* x, float* out, double* chunk_sums) {
+    PSR_CLOUD(c, px, py, pz, point2node, neigh, enc, x, out, chunk_sums);
     __shared__ double s_w[kBlock / 32];
     const int n = c->n_points;
     const int bD = c->level_base[depth];
-    double acc = 0.0;
-    PSR_GRID_STRIDE(i, n) {
-        const float v = level_terms(bD + point2node[i], out[i], px[i], py[i], pz[i], depth, neigh, stride, enc, x);
-        out[i] = v;
-        acc += (double)v;
-    }
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane_id() == 0) s_w[threadIdx.x >> 5] = acc;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double sum = 0.0;
-        for (int w = 0; w < kBlock / 32; ++w) sum += s_w[w];
-        block_sums[blockIdx.x] = sum;
+    const int nchunks = (n + kBlock - 1) / kBlock;
+    for (int ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+        const int i = ch * kBlock + threadIdx.x;
+        double acc = 0.0;
+        if (i < n) {
+            const float v = level_terms(bD + point2node[i], out[i], px[i], py[i], pz[i], depth, neigh, stride, enc, x);
+            out[i] = v;
+            acc = (double)v;
+        }
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane_id() == 0) s_w[threadIdx.x >> 5] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double sum = 0.0;
+            for (int w = 0; w < kBlock / 32; ++w) sum += s_w[w];
+            chunk_sums[ch] = sum;
+        }
+        __syncthreads();
     }
 }
 
-__global__ void k_iso_finalize(Counters* c, const double* block_sums, int nblocks) {
+__global__ void k_iso_finalize(Counters* c, const double* chunk_sums) {
+    PSR_CLOUD(c, chunk_sums);
     __shared__ double s_w[32];
+    const int nchunks = (c->n_points + kBlock - 1) / kBlock;
     double s = 0.0;
-    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) s += block_sums[b];
+    for (int b = threadIdx.x; b < nchunks; b += blockDim.x) s += chunk_sums[b];
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     if (lane_id() == 0) s_w[threadIdx.x >> 5] = s;
     __syncthreads();
@@ -704,10 +731,11 @@ void prepare_launch_configs(Workspace& ws) {
     (void)scan_grid(1 << 20);
 }
 
-static cudaError_t launch_cg(void (*kernel)(CgcArgs), CgcArgs& a, int grid, int cluster, cudaStream_t s) {
+// one cluster (or CTA) per depth and cloud: x spans the depths, y the clouds of the batch
+static cudaError_t launch_cg(void (*kernel)(CgcArgs), CgcArgs& a, int grid, int cluster, int clouds, cudaStream_t s) {
     void* args[] = {&a};
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(grid);
+    cfg.gridDim = dim3(grid, clouds);
     cfg.blockDim = dim3(kCgcBlock);
     cfg.dynamicSmemBytes = kCgSmemBytes;
     cfg.stream = s;
@@ -726,25 +754,25 @@ cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, 
     if (g_cg_cluster == 0) prepare_launch_configs(ws);
     const int D = ws.depth;
     CgcArgs a;
-    a.c = ws.cnt;
-    a.cw = ws.cnt;
+    a.v.c = ws.cnt;
+    a.v.cw = ws.cnt;
     a.depth = D;
-    a.neigh = ws.neigh;
-    a.blk = ws.cg_blk;
+    a.v.neigh = ws.neigh;
+    a.v.blk = ws.cg_blk;
     a.stride = (size_t)ws.cap.nodes;
-    a.stencil = ws.stencil;
-    a.b = ws.divg;
-    a.x = ws.xsol;
-    a.r = ws.cg_r;
-    a.pa = ws.cg_p;
-    a.pb = ws.cg_q;
-    a.ap = ws.cg_ap;
+    a.v.stencil = ws.stencil;
+    a.v.b = ws.divg;
+    a.v.x = ws.xsol;
+    a.v.r = ws.cg_r;
+    a.v.pa = ws.cg_p;
+    a.v.pb = ws.cg_q;
+    a.v.ap = ws.cg_ap;
     a.tol2 = cg_tol * cg_tol;
     // a fixed iteration count replaces the reference's max_iter (10000); the tolerance
     // test of the loop is kept (mesh/solver/CGAlgorithm.cu:36)
     a.max_iter = (cg_mode == 1 && cg_iters > 0) ? cg_iters : cg_max_iter;
     a.res_period = res_period;
-    k_cg_blocks<<<grid_for(ws, 1 << 20), kBlock, 0, s>>>(ws.cnt, ws.neigh, (size_t)ws.cap.nodes, ws.cg_blk);
+    k_cg_blocks<<<PSR_GRID(ws, grid_for(ws, 1 << 20)), kBlock, 0, s>>>(ws.cnt, ws.neigh, (size_t)ws.cap.nodes, ws.cg_blk);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     // The finest depths (D, D-1, and D-2 from depth 5 on; never the root) on clusters: depth
@@ -759,7 +787,7 @@ cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, 
     if (e == cudaSuccess && ncta > 0) {
         CgcArgs b = a;
         b.first = D - ncl;
-        e = launch_cg(k_cg_cta, b, ncta, 1, ws.aux);   // clusters of one CTA
+        e = launch_cg(k_cg_cta, b, ncta, 1, ws.batch, ws.aux);   // clusters of one CTA
     }
     if (e != cudaSuccess) return e;
     auto set_stencils = [&](CgcArgs& q) {
@@ -772,7 +800,7 @@ cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, 
         b.first = D - 1;
         set_stencils(b);
         const int cl2 = g_cg_cluster < 8 ? g_cg_cluster : 8;
-        e = launch_cg(k_cg_cluster, b, (ncl - 1) * cl2, cl2, ws.aux3);
+        e = launch_cg(k_cg_cluster, b, (ncl - 1) * cl2, cl2, ws.batch, ws.aux3);
         if (e == cudaSuccess) e = cudaEventRecord(ws.ev_join3, ws.aux3);
         if (e != cudaSuccess) return e;
     }
@@ -781,10 +809,10 @@ cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, 
     if (ncl > 1) e = cudaStreamWaitEvent(ws.aux, ws.ev_join3, 0);
     if (e == cudaSuccess) {
         const size_t cstride = (size_t)ws.cap.dnodes / 8 + 64;
-        k_point_poly<<<ws.num_sms * 4, kBlock, 0, ws.aux>>>(ws.cnt, D, ws.ctr_x, ws.ctr_y, ws.ctr_z, ws.neigh,
+        k_point_poly<<<PSR_GRID(ws, ws.num_sms * 4), kBlock, 0, ws.aux>>>(ws.cnt, D, ws.ctr_x, ws.ctr_y, ws.ctr_z, ws.neigh,
                                                             (size_t)ws.cap.nodes, ws.parent, ws.enc, ws.xsol,
                                                             ws.pv_coef, cstride);
-        k_point_values_coarse<<<ws.num_sms * 4, kBlock, 0, ws.aux>>>(ws.cnt, D, ws.px, ws.py, ws.pz, ws.point2node,
+        k_point_values_coarse<<<PSR_GRID(ws, ws.num_sms * 4), kBlock, 0, ws.aux>>>(ws.cnt, D, ws.px, ws.py, ws.pz, ws.point2node,
                                                                      ws.parent, ws.ctr_x, ws.ctr_y, ws.ctr_z,
                                                                      ws.pv_coef, cstride, ws.point_val);
         e = cudaEventRecord(ws.ev_join, ws.aux);
@@ -793,20 +821,20 @@ cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, 
     if (ncl > 0) {
         a.first = D;
         set_stencils(a);
-        e = launch_cg(k_cg_cluster, a, g_cg_cluster, g_cg_cluster, s);
+        e = launch_cg(k_cg_cluster, a, g_cg_cluster, g_cg_cluster, ws.batch, s);
         if (e != cudaSuccess) return e;
     }
     if (ws.ev_cg) {
-        e = cudaEventRecordWithFlags(ws.ev_cg, s, cudaEventRecordExternal);
+        e = cudaEventRecordWithFlags(ws.ev_cg, s, ws.ev_flags);
         if (e != cudaSuccess) return e;
     }
     e = cudaStreamWaitEvent(s, ws.ev_join, 0);
     if (e != cudaSuccess) return e;
     // iso-value: the depth-D terms complete the sample values
     const int nb = ws.num_sms * 4;
-    k_point_values<<<nb, kBlock, 0, s>>>(ws.cnt, ws.depth, ws.px, ws.py, ws.pz, ws.point2node, ws.neigh,
+    k_point_values<<<PSR_GRID(ws, nb), kBlock, 0, s>>>(ws.cnt, ws.depth, ws.px, ws.py, ws.pz, ws.point2node, ws.neigh,
                                          (size_t)ws.cap.nodes, ws.enc, ws.xsol, ws.point_val, ws.iso_partial);
-    k_iso_finalize<<<1, 256, 0, s>>>(ws.cnt, ws.iso_partial, nb);
+    k_iso_finalize<<<PSR_GRID(ws, 1), 256, 0, s>>>(ws.cnt, ws.iso_partial);
     return cudaGetLastError();
 }
 

@@ -33,6 +33,7 @@ __device__ __forceinline__ unsigned point_cell(int i, int depth, int g, int bD, 
 // the run's length), then one scan turns the counts into starts in place.
 __global__ void __launch_bounds__(kBlock) k_cell_count(Counters* c, int depth, int g, const int* key,
                                                        const int* point2node, int* count) {
+    PSR_CLOUD(c, key, point2node, count);
     const int n = c->n_points;
     const int bD = c->level_base[depth];
     if (blockIdx.x == 0 && threadIdx.x == 0) c->n_colour_cells = (1 << (3 * g)) + 1;
@@ -145,6 +146,7 @@ __global__ void __launch_bounds__(kBlock) k_colour_near(Counters* c, int g, cons
                                                         const float* py, const float* pz, const float* cr,
                                                         const float* cg, const float* cb, const int* cell_start,
                                                         int* far, float* out) {
+    PSR_CLOUD(c, mv, px, py, pz, cr, cg, cb, cell_start, far, out);
     __shared__ int s_off[kNearGroups][28];
     __shared__ int s_base[kNearGroups][27];
     const int V = c->n_mesh_vertices;
@@ -282,6 +284,7 @@ __global__ void __launch_bounds__(kFarThreads) k_colour(const Counters* c, int g
                                                        const float* px, const float* py, const float* pz,
                                                        const float* cr, const float* cg, const float* cb,
                                                        const int* cell_start, const int* far, float* out) {
+    PSR_CLOUD(c, mv, px, py, pz, cr, cg, cb, cell_start, far, out);
     __shared__ int s_off[28];
     __shared__ int s_base[27];
     __shared__ float s_cd[32];
@@ -365,6 +368,7 @@ __global__ void __launch_bounds__(kFarThreads) k_colour(const Counters* c, int g
 }
 
 __global__ void __launch_bounds__(kBlock) k_normals_zero(const Counters* c, double* acc, int* cnt) {
+    PSR_CLOUD(c, acc, cnt);
     const int V = c->n_mesh_vertices;
     PSR_GRID_STRIDE(v, V) {
         acc[3 * (size_t)v] = acc[3 * (size_t)v + 1] = acc[3 * (size_t)v + 2] = 0.0;
@@ -374,6 +378,7 @@ __global__ void __launch_bounds__(kBlock) k_normals_zero(const Counters* c, doub
 
 __global__ void __launch_bounds__(kBlock) k_triangle_normals(const Counters* c, const float* mv, const int* mt,
                                                              double* acc, int* cnt) {
+    PSR_CLOUD(c, mv, mt, acc, cnt);
     const int T = c->n_mesh_triangles;
     const int V = c->n_mesh_vertices;
     PSR_GRID_STRIDE(t, T) {
@@ -398,6 +403,7 @@ __global__ void __launch_bounds__(kBlock) k_triangle_normals(const Counters* c, 
 
 __global__ void __launch_bounds__(kBlock) k_vertex_normals(const Counters* c, const double* acc, const int* cnt,
                                                            float* out) {
+    PSR_CLOUD(c, acc, cnt, out);
     const int V = c->n_mesh_vertices;
     PSR_GRID_STRIDE(v, V) {
         const int n = cnt[v];
@@ -421,9 +427,9 @@ cudaError_t transfer_prepare(Workspace& ws, int with_colour) {
     if (!with_colour) return cudaSuccess;
     const int D = ws.depth;
     const int g = D < kColourGridLevel ? D : kColourGridLevel;
-    cudaError_t e = cudaMemsetAsync(ws.cell_start, 0, sizeof(int) * (((size_t)1 << (3 * g)) + 1), ws.stream);
+    cudaError_t e = fill_words((unsigned*)ws.cell_start, 0u, ((long long)1 << (3 * g)) + 1, ws.batch, ws.stream);
     if (e != cudaSuccess) return e;
-    k_cell_count<<<ws.num_sms * 4, kBlock, 0, ws.stream>>>(ws.cnt, D, g, ws.key, ws.point2node, ws.cell_start);
+    k_cell_count<<<PSR_GRID(ws, ws.num_sms * 4), kBlock, 0, ws.stream>>>(ws.cnt, D, g, ws.key, ws.point2node, ws.cell_start);
     unsigned* table = reinterpret_cast<unsigned*>(ws.cell_start);
     Counters* c = ws.cnt;
     return launch_scan(LoadArray{table}, StoreExclusive{table}, &c->n_colour_cells, 0, ws.scan,
@@ -437,16 +443,16 @@ cudaError_t transfer_build(Workspace& ws, int with_colour, int with_normals) {
     if (with_colour) {
         const int g = D < kColourGridLevel ? D : kColourGridLevel;
         int* cell_start = ws.cell_start;   // (1 << 3g) + 1 entries, from transfer_prepare
-        k_colour_near<<<grid, kBlock, 0, s>>>(ws.cnt, g, ws.mesh_v, ws.px, ws.py, ws.pz, ws.cr, ws.cg, ws.cb,
+        k_colour_near<<<PSR_GRID(ws, grid), kBlock, 0, s>>>(ws.cnt, g, ws.mesh_v, ws.px, ws.py, ws.pz, ws.cr, ws.cg, ws.cb,
                                               cell_start, ws.colour_far, ws.mesh_c);
-        k_colour<<<2 * ws.num_sms, kFarThreads, 0, s>>>(ws.cnt, g, ws.mesh_v, ws.px, ws.py, ws.pz, ws.cr, ws.cg,
+        k_colour<<<PSR_GRID(ws, 2 * ws.num_sms), kFarThreads, 0, s>>>(ws.cnt, g, ws.mesh_v, ws.px, ws.py, ws.pz, ws.cr, ws.cg,
                                                         ws.cb, cell_start, ws.colour_far, ws.mesh_c);
     }
     if (with_normals) {
         double* acc = ws.nacc;
-        k_normals_zero<<<grid, kBlock, 0, s>>>(ws.cnt, acc, ws.vcount);
-        k_triangle_normals<<<grid, kBlock, 0, s>>>(ws.cnt, ws.mesh_v, ws.mesh_t, acc, ws.vcount);
-        k_vertex_normals<<<grid, kBlock, 0, s>>>(ws.cnt, acc, ws.vcount, ws.mesh_n);
+        k_normals_zero<<<PSR_GRID(ws, grid), kBlock, 0, s>>>(ws.cnt, acc, ws.vcount);
+        k_triangle_normals<<<PSR_GRID(ws, grid), kBlock, 0, s>>>(ws.cnt, ws.mesh_v, ws.mesh_t, acc, ws.vcount);
+        k_vertex_normals<<<PSR_GRID(ws, grid), kBlock, 0, s>>>(ws.cnt, acc, ws.vcount, ws.mesh_n);
     }
     return cudaGetLastError();
 }

@@ -36,6 +36,7 @@ __device__ __forceinline__ bool weld_same(const unsigned* vb, int a, int b) {
 // at most `mask + 1` probes, the table being at least twice the vertex capacity
 __global__ void __launch_bounds__(kBlock) k_weld_insert(Counters* c, const float* mv, int* table, unsigned mask,
                                                         int* slot) {
+    PSR_CLOUD(c, mv, table, slot);
     const int V = c->n_mesh_vertices;
     const unsigned* vb = reinterpret_cast<const unsigned*>(mv);
     PSR_GRID_STRIDE(v, V) {
@@ -60,6 +61,7 @@ __global__ void __launch_bounds__(kBlock) k_weld_insert(Counters* c, const float
 
 // the smallest index of each class into its slot (any member's index is there already)
 __global__ void __launch_bounds__(kBlock) k_weld_min(const Counters* c, const int* slot, int* table) {
+    PSR_CLOUD(c, slot, table);
     const int V = c->n_mesh_vertices;
     PSR_GRID_STRIDE(v, V) atomicMin(&table[slot[v]], v);
 }
@@ -68,6 +70,7 @@ struct WeldLoad {
     const int* table;
     const int* slot;
     __device__ unsigned operator()(int v) const { return table[slot[v]] == v ? 1u : 0u; }
+    __device__ void rebase() { PSR_CLOUD(table, slot); }   // to cloud blockIdx.y
 };
 
 // representatives: new number and a compacted copy of the position
@@ -82,12 +85,14 @@ struct WeldStore {
         out_v[3 * (size_t)pre + 1] = mv[3 * (size_t)v + 1];
         out_v[3 * (size_t)pre + 2] = mv[3 * (size_t)v + 2];
     }
+    __device__ void rebase() { PSR_CLOUD(mv, out_v, newid); }   // to cloud blockIdx.y
 };
 
 // triangle corners -> the new number of their class's representative; welded positions back
 // into the mesh array; the vertex count becomes the welded one
 __global__ void __launch_bounds__(kBlock) k_weld_apply(Counters* c, const int* table, const int* slot,
                                                        const int* newid, const float* wv, float* mv, int* mt) {
+    PSR_CLOUD(c, table, slot, newid, wv, mv, mt);
     const int V = c->n_mesh_vertices;
     const int W = c->n_weld;
     const int T3 = 3 * c->n_mesh_triangles;
@@ -101,6 +106,7 @@ __global__ void __launch_bounds__(kBlock) k_weld_apply(Counters* c, const int* t
 }
 
 __global__ void k_weld_count(Counters* c) {
+    PSR_CLOUD(c);
     if (threadIdx.x == 0 && blockIdx.x == 0) c->n_mesh_vertices = c->n_weld;
 }
 
@@ -108,19 +114,19 @@ cudaError_t weld_build(Workspace& ws) {
     if (!ws.weld_table) return cudaSuccess;
     cudaStream_t s = ws.stream;
     Counters* c = ws.cnt;
-    cudaError_t e = cudaMemsetAsync(ws.weld_table, 0xff, sizeof(int) * ((size_t)ws.weld_mask + 1), s);
+    cudaError_t e = fill_words((unsigned*)ws.weld_table, 0xffffffffu, (long long)ws.weld_mask + 1, ws.batch, s);
     if (e != cudaSuccess) return e;
     const int g = grid_for(ws, ws.cap.mesh_vertices);
-    k_weld_insert<<<g, kBlock, 0, s>>>(c, ws.mesh_v, ws.weld_table, ws.weld_mask, ws.weld_slot);
-    k_weld_min<<<g, kBlock, 0, s>>>(c, ws.weld_slot, ws.weld_table);
+    k_weld_insert<<<PSR_GRID(ws, g), kBlock, 0, s>>>(c, ws.mesh_v, ws.weld_table, ws.weld_mask, ws.weld_slot);
+    k_weld_min<<<PSR_GRID(ws, g), kBlock, 0, s>>>(c, ws.weld_slot, ws.weld_table);
     e = launch_scan(WeldLoad{ws.weld_table, ws.weld_slot}, WeldStore{ws.mesh_v, ws.weld_v, ws.weld_newid},
                     &c->n_mesh_vertices, 0, ws.scan, (unsigned*)&c->scan_total, &c->error, s,
                     ScanCount{&c->n_weld, ws.cap.mesh_vertices}, 1);
     if (e != cudaSuccess) return e;
-    k_weld_apply<<<grid_for(ws, 3 * ws.cap.mesh_tris), kBlock, 0, s>>>(c, ws.weld_table, ws.weld_slot,
+    k_weld_apply<<<PSR_GRID(ws, grid_for(ws, 3 * ws.cap.mesh_tris)), kBlock, 0, s>>>(c, ws.weld_table, ws.weld_slot,
                                                                        ws.weld_newid, ws.weld_v, ws.mesh_v,
                                                                        ws.mesh_t);
-    k_weld_count<<<1, 32, 0, s>>>(c);
+    k_weld_count<<<PSR_GRID(ws, 1), 32, 0, s>>>(c);
     return cudaGetLastError();
 }
 

@@ -46,6 +46,7 @@ struct MeshBufs {
 };
 
 struct Workspace {
+    int batch = 1;          // clouds of the launches being issued (the grids' y extent)
     MeshBufs mb;
     Caps cap;
     int depth;
@@ -98,6 +99,7 @@ struct Workspace {
     float* divg;            // M
     float* xsol;            // M
     cudaEvent_t ev_cg = nullptr;   // recorded right after the CG kernel (stage timing)
+    unsigned ev_flags = 0;         // flags of the stage-timing event records (external in a capture)
     float *cg_r, *cg_p, *cg_q, *cg_ap;   // residual, two direction buffers, A p
     int* cg_blk;            // CG block table: 64 same-depth nodes per sibling group
     double* cg_partial;     // scratch: divergence chunk sums (float pairs, 8 bytes each)
@@ -181,6 +183,17 @@ struct Workspace {
 // sample grid of the colour search: 2^g cells per axis (128^3: a few samples per surface
 // cell at 200k points)
 constexpr int kColourGridLevel = 7;
+
+// launch grid for the clouds of the batch being issued (gx blocks for one cloud)
+#define PSR_GRID(ws, gx) dim3(::psr::cloud_blocks((ws).batch, (gx)), (ws).batch)
+
+// the clouds of the next launches (every scan scratch copy carries the count too)
+inline void set_batch(Workspace& ws, int clouds) {
+    ws.batch = clouds;
+    ws.scan.batch = clouds;
+    ws.scan_aux.batch = clouds;
+    ws.sort.scan.batch = clouds;
+}
 
 // grid of a grid-stride kernel over `work` items: enough blocks, at most 8 per SM
 inline int grid_for(const Workspace& ws, long long work) {

@@ -22,7 +22,8 @@ PSR_HOST, PSR_DEVICE = 0, 1
 # every function declared in include/psr/psr.h
 EXPORTED = ["psr_config_default", "psr_create", "psr_destroy", "psr_reconstruct", "psr_submit", "psr_poll",
             "psr_wait", "psr_memory_bytes", "psr_get_stats", "psr_debug_array", "psr_status_string",
-            "psr_last_error", "psr_surfels_to_points", "psr_morton_sort_noalloc", "psr_estimate_normals"]
+            "psr_last_error", "psr_surfels_to_points", "psr_morton_sort_noalloc", "psr_estimate_normals",
+            "psr_submit_batch", "psr_reconstruct_batch", "psr_get_batch_result"]
 
 
 class PsrConfig(ctypes.Structure):
@@ -33,7 +34,8 @@ class PsrConfig(ctypes.Structure):
                 ("compute_colors", ctypes.c_int), ("compute_normals", ctypes.c_int), ("device", ctypes.c_int),
                 ("laplacian_epsilon", ctypes.c_float), ("concurrent_stages", ctypes.c_int),
                 ("weld_vertices", ctypes.c_int), ("disable_graphs", ctypes.c_int),
-                ("root_poly_capacity", ctypes.c_int), ("cg_residual_period", ctypes.c_int)]
+                ("root_poly_capacity", ctypes.c_int), ("cg_residual_period", ctypes.c_int),
+                ("batch_clouds", ctypes.c_int)]
 
 
 class PsrPoints(ctypes.Structure):
@@ -85,6 +87,10 @@ def load_library(path=None):
     L.psr_reconstruct.argtypes = [ctypes.c_void_p, ctypes.POINTER(PsrPoints), ctypes.POINTER(PsrOptions),
                                   ctypes.POINTER(PsrMesh), ctypes.c_void_p]
     L.psr_submit.argtypes = L.psr_reconstruct.argtypes
+    L.psr_submit_batch.argtypes = [ctypes.c_void_p, ctypes.POINTER(PsrPoints), ctypes.c_int,
+                                   ctypes.POINTER(PsrOptions), ctypes.POINTER(PsrMesh), ctypes.c_void_p]
+    L.psr_reconstruct_batch.argtypes = L.psr_submit_batch.argtypes
+    L.psr_get_batch_result.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
     L.psr_poll.argtypes = [ctypes.c_void_p]
     L.psr_wait.argtypes = [ctypes.c_void_p]
     L.psr_memory_bytes.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t)]
@@ -142,7 +148,7 @@ class PoissonReconstruction:
     def __init__(self, max_depth=7, max_points=300000, max_triangles=1000000, max_mesh_vertices=300000,
                  compute_colors=False, compute_normals=False, cg_tolerance=1e-5, cg_max_iterations=10000,
                  max_nodes=0, max_subdivision_nodes=0, device=0, laplacian_epsilon=1e-6, concurrent_stages=True, weld_vertices=False,
-                 disable_graphs=False, root_poly_capacity=0, cg_residual_period=0):
+                 disable_graphs=False, root_poly_capacity=0, cg_residual_period=0, batch_clouds=1):
         self._lib = load_library()
         cfg = default_config()
         cfg.max_depth = max_depth
@@ -162,6 +168,7 @@ class PoissonReconstruction:
         cfg.disable_graphs = int(disable_graphs)
         cfg.root_poly_capacity = int(root_poly_capacity)
         cfg.cg_residual_period = int(cg_residual_period)
+        cfg.batch_clouds = int(batch_clouds)
         self.config = cfg
         h = ctypes.c_void_p()
         st = self._lib.psr_create(ctypes.byref(cfg), ctypes.byref(h))
@@ -219,6 +226,69 @@ class PoissonReconstruction:
         return self._mesh
 
     reconstruct = SolvePoissionReconstructionMesh
+
+    def _host_mesh(self):
+        vcap = int(self.config.max_mesh_vertices)
+        tcap = int(self.config.max_triangles)
+        v = np.empty((vcap, 3), np.float32)
+        t = np.empty((tcap, 3), np.int32)
+        c = np.empty((vcap, 3), np.float32) if self.config.compute_colors else None
+        nm = np.empty((vcap, 3), np.float32) if self.config.compute_normals else None
+        desc = PsrMesh(v.ctypes.data, t.ctypes.data, c.ctypes.data if c is not None else None,
+                       nm.ctypes.data if nm is not None else None, vcap, tcap, PSR_HOST, 0, 0)
+        return desc, (v, t, c, nm)
+
+    def reconstruct_batch(self, clouds, depth=0, cg_iterations=0):
+        """Reconstruct up to batch_clouds clouds of one depth in one multi-cloud pass
+        (psr_reconstruct_batch).  `clouds`: list of (xyz, normals, rgb or None) host arrays.
+        Returns one Mesh per cloud, or a PsrError for a cloud that failed."""
+        n = len(clouds)
+        keep = []
+        pts = (PsrPoints * n)()
+        meshes = (PsrMesh * n)()
+        bufs = []
+        for k, (xyz, nrm, rgb) in enumerate(clouds):
+            xyz = np.ascontiguousarray(xyz, np.float32)
+            nrm = np.ascontiguousarray(nrm, np.float32)
+            rgb = None if rgb is None else np.ascontiguousarray(rgb, np.uint8)
+            keep.append((xyz, nrm, rgb))
+            pts[k] = PsrPoints(xyz.ctypes.data, nrm.ctypes.data, rgb.ctypes.data if rgb is not None else None,
+                               int(xyz.shape[0]), PSR_HOST)
+            meshes[k], b = self._host_mesh()
+            bufs.append(b)
+        opt = PsrOptions(int(depth), int(cg_iterations))
+        st = self._lib.psr_reconstruct_batch(self._h, pts, n, ctypes.byref(opt), meshes, None)
+        if st != PSR_OK and self.batch_result(n - 1)[1].points == 0:
+            raise self._error(st, "psr_reconstruct_batch")   # the call itself failed: no per-cloud results
+        out = []
+        for k in range(n):
+            sk = self._lib.psr_get_batch_result(self._h, k, None)
+            if sk != PSR_OK:
+                out.append(PsrError(sk, f"cloud {k}: {self._lib.psr_status_string(sk).decode()}"))
+                continue
+            v, t, c, nm = bufs[k]
+            m = meshes[k]
+            nv, nt = m.vertex_count, m.triangle_count
+            out.append(Mesh(v[:nv].copy(), t[:nt].copy(), None if c is None else c[:nv].copy(),
+                            None if nm is None else nm[:nv].copy(), np.array(m.center[:], np.float32),
+                            float(m.scale)))
+        return out
+
+    def submit_batch_device(self, points, meshes, depth=0, cg_iterations=0, stream=None):
+        """Enqueue a multi-cloud pass: `points` a ctypes array of PsrPoints (device or pinned
+        host pointers), `meshes` a ctypes array of PsrMesh of the same length; returns at
+        once (collect with poll / wait, then batch_result)."""
+        self._pend = (points, PsrOptions(int(depth), int(cg_iterations)), meshes)
+        st = self._lib.psr_submit_batch(self._h, points, len(points), ctypes.byref(self._pend[1]), meshes, stream)
+        if st != PSR_OK:
+            self._pend = None
+            raise self._error(st, "psr_submit_batch")
+
+    def batch_result(self, index):
+        """(status, PsrStats) of cloud `index` of the last completed call."""
+        s = PsrStats()
+        st = self._lib.psr_get_batch_result(self._h, int(index), ctypes.byref(s))
+        return st, s
 
     def reconstruct_device(self, xyz_ptr, nrm_ptr, rgb_ptr, n, depth=0, cg_iterations=0, stream=None,
                            out=None):
