@@ -45,6 +45,10 @@ def parse():
     ap.add_argument("--workload", default="torus_ellipsoid200k")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--slots", type=int, default=8, help="concurrent reconstructions of the served leg")
+    ap.add_argument("--batch", type=int, default=16, help="clouds per multi-cloud launch in the batch leg")
+    ap.add_argument("--serve-seconds", type=float, default=15.0,
+                    help="open-loop duration of the serving-loop leg (Poisson arrivals, mixed sizes and depths)")
+    ap.add_argument("--no-serve-mix", action="store_true", help="skip the serving-loop leg")
     return ap.parse_args()
 
 
@@ -337,10 +341,11 @@ def main():
         pass
     peak_hbm = float(peaks.get("hbm_gbs", 6800.0))
     M = st.nodes
-    # algorithmic bytes of one CG row-iteration: 27 neighbour indices (108 B), the row's
+    # algorithmic bytes of one CG row-iteration of the matrix-free operator: the row's
     # residual and previous direction read (8 B), its new direction and residual written
-    # (8 B); the neighbours' values are the same vectors, counted once per row
-    row_bytes = 124
+    # (8 B), x read and written (8 B); the neighbours' values are the same vectors, counted
+    # once per row, and the neighbour / descriptor table is built once per solve
+    row_bytes = 24
     cg_bytes = 0
     for d in range(depth + 1):
         cg_bytes += st.level_count[d] * row_bytes * st.cg_iterations[d]
@@ -352,7 +357,11 @@ def main():
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s",
                 "algorithmic_bytes": cg_bytes, "launch_ms": cg_ms,
                 "note": "vectors resident in shared memory, descriptor table in L2 (DRAM traffic ~3 MB per "
-                        "reconstruction): latency bound"}
+                        "reconstruction): the HBM fraction does not bound it",
+                "limiter": "two cluster barriers and the distributed-shared-memory gathers of every iteration",
+                "us_per_iteration_depth_d": (1000.0 * st.cg_depth_ms[depth] / st.cg_iterations[depth]
+                                             if st.cg_iterations[depth] else None),
+                "sm_ms_per_recon": None}
     # DRAM traffic of one launch, from the committed ncu summary of the same kernel and workload
     try:
         for line in open(ROOT / "profiles" / "cg_cluster_torus200k_d7.md"):
@@ -363,9 +372,17 @@ def main():
         pass
     if roofline["achieved"]:
         roofline["frac"] = roofline["achieved"] / peak_hbm
+    # SM time of the CG per reconstruction: every depth's cluster or CTA holds its SMs for
+    # its own device time (one 1024-thread CTA per SM)
+    cl = 16 if depth >= 2 else 1
+    sm_ms = 0.0
+    for d in range(depth + 1):
+        ctas = cl if d == depth else (8 if d >= depth - 2 and depth >= 5 else 1)
+        sm_ms += ctas * st.cg_depth_ms[d]
+    roofline["sm_ms_per_recon"] = round(sm_ms, 3)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": tot_sdev / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 dots / reductions)", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (CG dots, norms and iso-value sums in f64 across warps / CTAs)", "data": "synthetic",
             "impl": "gpu",
             "config": {"workload": f"{args.workload} (N={n}, depth {depth}, colour, normals)",
                        "path": f"served: Server with {K} slots (handle + stream + CUDA graphs each), one host "
@@ -391,6 +408,17 @@ def main():
             "gpu_launches_per_recon": int(st_launches(server.slots[0].recon)) + 1,
             "roofline": roofline, "clocks": clocks}
     line.update(side_legs(psr, r, caps, d_xyz, d_nrm, d_rgb, n, depth, dev_mesh, stream, torch, st))
+    try:
+        line["batch"] = batch_leg(psr, caps, dclouds, args.steps, torch, dev, args.batch)
+        line["batch"]["vs_plain"] = line["batch"]["value"] / plain_value
+    except Exception as e:   # reported, not fatal: the headline legs are above
+        line["batch"] = {"error": str(e)}
+    if not args.no_serve_mix:
+        try:
+            import serve as serve_mod
+            line["serve_mix"] = serve_mix_leg(psr, serve_mod, syn, torch, dev, args.serve_seconds)
+        except Exception as e:
+            line["serve_mix"] = {"error": str(e)}
     if not args.no_cpu_baseline:
         try:
             line["cpu_baseline"] = cpu_baseline(xyz, nrm, rgb, depth)
@@ -479,6 +507,117 @@ def served_leg(server, clouds, steps, torch, dev):
     lat = np.array([1000.0 * (r.finished - r.admitted) for r in done])   # service time (no queueing)
     stages = np.mean([list(sl.recon.stats().stage_ms) for sl in server.slots], axis=0)
     return total_ms, lat, [round(float(x), 4) for x in stages]
+
+
+def batch_leg(psr, caps, clouds, steps, torch, dev, K):
+    """Multi-cloud launches (psr_submit_batch): K clouds of the workload per pass, one launch
+    of each kernel for all of them, device-resident inputs and outputs.  Device time = CUDA
+    events around `steps` passes on the launching stream (3 untimed passes first)."""
+    vcap, tcap = caps["max_mesh_vertices"], caps["max_triangles"]
+    with psr.PoissonReconstruction(batch_clouds=K, concurrent_stages=False, **caps) as r:
+        pts, meshes, outs = (psr.PsrPoints * K)(), (psr.PsrMesh * K)(), []
+        for k in range(K):
+            x, nrm, rgb, _ = clouds[k % len(clouds)]
+            o = [torch.empty((vcap, 3), dtype=torch.float32, device=dev), torch.empty((tcap, 3), dtype=torch.int32, device=dev),
+                 torch.empty((vcap, 3), dtype=torch.float32, device=dev), torch.empty((vcap, 3), dtype=torch.float32, device=dev)]
+            outs.append(o)
+            pts[k] = psr.PsrPoints(x.data_ptr(), nrm.data_ptr(), rgb.data_ptr() if rgb is not None else None,
+                                   x.shape[0], psr.PSR_DEVICE)
+            meshes[k] = psr.PsrMesh(o[0].data_ptr(), o[1].data_ptr(), o[2].data_ptr() if rgb is not None else None,
+                                    o[3].data_ptr(), vcap, tcap, psr.PSR_DEVICE, 0, 0)
+        stream = torch.cuda.current_stream(dev)
+        for _ in range(3):
+            r.submit_batch_device(pts, meshes, depth=clouds[0][3], stream=stream.cuda_stream)
+            r.wait()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        a.record(stream)
+        for _ in range(steps):
+            r.submit_batch_device(pts, meshes, depth=clouds[0][3], stream=stream.cuda_stream)
+            r.wait()
+        b.record(stream)
+        b.synchronize()
+        ms = a.elapsed_time(b)
+        st = [r.batch_result(k) for k in range(K)]
+        if any(x[0] != psr.PSR_OK for x in st):
+            raise RuntimeError("batch leg: a cloud failed")
+        return {"clouds_per_launch": K, "value": K * steps / (ms / 1000.0), "unit": UNIT,
+                "ms_per_pass": ms / steps, "kernel_launches_per_pass": int(st[0][1].kernel_launches),
+                "stage_ms": [round(float(v), 4) for v in st[0][1].stage_ms],
+                "memory_gb": round(r.memory_bytes() / 1e9, 2)}
+
+
+def serve_mix_leg(psr, serve, syn, torch, dev, seconds, rate=200.0, budget=40e9, pool=48, seed=11):
+    """The serving loop: Poisson arrivals at `rate` per second of clouds of the serving mix
+    (point counts log-uniform in [10k, 500k], depth uniform in 6..9, spheres, tori and
+    superquadrics randomly scaled and rotated, colour), admitted by footprint into slots of
+    two sizes under a device-memory budget; open loop for `seconds` after a 2 s warm-up.
+    Requests cycle over a pool of distinct seeded clouds resident on the device.  Reported:
+    completed reconstructions per second, arrival-to-completion p50 / p99, rejected
+    requests, and the plain path (one handle, one cloud at a time) on the same pool."""
+    from serve import Server, Request
+    clouds = []
+    for i in range(pool):
+        p, nr, rgb, d = syn.workload("serve", cloud=i)
+        clouds.append((torch.from_numpy(p).to(dev), torch.from_numpy(nr).to(dev), torch.from_numpy(rgb).to(dev), d))
+    big = dict(max_points=500000, max_depth=9, max_triangles=8000000, max_mesh_vertices=4000000,
+               max_subdivision_nodes=16000000)
+    small = dict(max_points=120000, max_depth=9, max_triangles=4000000, max_mesh_vertices=2000000,
+                 max_subdivision_nodes=8000000)
+    server = Server(classes=[dict(count=2, **big), dict(count=64, **small)], memory_budget=budget,
+                    compute_colors=True, compute_normals=True, laplacian_epsilon=0.0)
+    slots = {"large": sum(1 for s in server.slots if s.max_points == big["max_points"]),
+             "small": sum(1 for s in server.slots if s.max_points == small["max_points"])}
+    def open_loop(rate_s, secs, warm, seed_):
+        rng = np.random.default_rng(seed_)
+        n_req = int(rate_s * (secs + warm))
+        arrivals = np.cumsum(rng.exponential(1.0 / rate_s, n_req))
+        reqs = [Request(xyz=clouds[i % pool][0], normals=clouds[i % pool][1], rgb=clouds[i % pool][2],
+                        depth=clouds[i % pool][3]) for i in range(n_req)]
+        done = server.run(reqs, arrivals=list(arrivals))
+        t0 = min(r.arrival for r in done)
+        meas = [r for r in done if r.arrival - t0 >= warm]
+        ok = [r for r in meas if not r.error]
+        lat = np.array([r.latency_ms for r in ok])
+        span = max(r.finished for r in meas) - min(r.arrival for r in meas)
+        errors = sorted({r.error.split(":")[0] for r in meas if r.error})
+        return {"rate_per_s": round(rate_s, 2), "seconds": secs, "requests": len(meas), "completed": len(ok),
+                "rejected": sum(1 for r in meas if r.error), "errors": errors[:3],
+                "recons_per_s": len(ok) / span, "p50_ms": float(np.percentile(lat, 50)) if lat.size else None,
+                "p99_ms": float(np.percentile(lat, 99)) if lat.size else None}
+    # as configured (200 requests/s): completions per second are the loop's capacity when
+    # the arrivals exceed it, and latency is then mostly queueing; then an open loop at 70%
+    # of that capacity for latency under a sustainable load
+    out = open_loop(rate, seconds, 2.0, seed)
+    out.update(slots=slots, memory_gb=round(server.memory_bytes / 1e9, 2), budget_gb=budget / 1e9,
+               laplacian_epsilon=0.0)
+    if out["recons_per_s"] < 0.95 * rate:
+        out["sustainable"] = open_loop(0.7 * out["recons_per_s"], seconds, 2.0, seed + 1)
+    server.close()
+    # the plain path on the same pool: one handle sized for the largest cloud, one at a time
+    with psr.PoissonReconstruction(compute_colors=True, compute_normals=True, laplacian_epsilon=0.0, **big) as r:
+        vcap, tcap = big["max_mesh_vertices"], big["max_triangles"]
+        o = [torch.empty((vcap, 3), dtype=torch.float32, device=dev), torch.empty((tcap, 3), dtype=torch.int32, device=dev),
+             torch.empty((vcap, 3), dtype=torch.float32, device=dev), torch.empty((vcap, 3), dtype=torch.float32, device=dev)]
+        def one(c):
+            m = psr.PsrMesh(o[0].data_ptr(), o[1].data_ptr(), o[2].data_ptr(), o[3].data_ptr(), vcap, tcap,
+                            psr.PSR_DEVICE, 0, 0)
+            try:
+                r.reconstruct_device(c[0].data_ptr(), c[1].data_ptr(), c[2].data_ptr(), c[0].shape[0], depth=c[3],
+                                     out=m)
+                return True
+            except psr.PsrError:
+                return False
+        for c in clouds[:4]:
+            one(c)
+        torch.cuda.synchronize(dev)
+        t = time.perf_counter()
+        good = sum(one(c) for c in clouds)
+        torch.cuda.synchronize(dev)
+        out["plain"] = {"recons_per_s": good / (time.perf_counter() - t), "clouds": pool, "completed": good}
+    out["served_vs_plain"] = out["recons_per_s"] / out["plain"]["recons_per_s"]
+    return out
 
 
 def st_launches(r):

@@ -1,8 +1,9 @@
 // Header-only C++ shim over the C ABI (psr.h) with the reference's class and method names
 // (SparseSurfelFusion::PoissonReconstruction, mesh/PoissonReconstruction.h:63-184), so a
 // caller of the reference's data-parallel path can switch by changing the include and the
-// namespace.  It owns no device memory of its own except the optional surfel staging used
-// by the DepthSurfel overload.
+// namespace.  Besides the handle it owns one device buffer, allocated in the constructor
+// for max_points surfels, into which the DepthSurfel overload unpacks the surfels; no
+// reconstruction call allocates.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -42,6 +43,14 @@ public:
         cfg_ = c;
         psr_status s = psr_create(&c, &h_);
         if (s != PSR_OK) throw std::runtime_error(std::string("psr_create: ") + psr_status_string(s));
+        // SoA staging of the DepthSurfel overload: xyz, normals (floats) and rgb (bytes)
+        cudaError_t e = cudaMalloc(&staging_, 6 * sizeof(float) * (size_t)c.max_points + 3 * (size_t)c.max_points);
+        if (e != cudaSuccess) {
+            psr_destroy(h_);
+            h_ = nullptr;
+            throw std::runtime_error(std::string("surfel staging: ") + cudaGetErrorString(e));
+        }
+        staging_count_ = c.max_points;
     }
     ~PoissonReconstruction() {
         if (h_) psr_destroy(h_);
@@ -53,7 +62,7 @@ public:
     // Same role as the reference's SolvePoissionReconstructionMesh(DeviceArrayView<DepthSurfel>):
     // device-resident surfels in, mesh kept in the object (read with the getters below).
     void SolvePoissionReconstructionMesh(const DepthSurfel* device_surfels, int count, cudaStream_t stream = nullptr) {
-        ensure_staging(count);
+        if (count > staging_count_) throw std::runtime_error("more surfels than max_points");
         float* xyz = staging_;
         float* nrm = staging_ + 3 * (size_t)count;
         // colour from ColorAndTime.xyz when the handle transfers colours
@@ -69,12 +78,14 @@ public:
         vertices_.resize((size_t)cfg_.max_mesh_vertices);
         triangles_.resize((size_t)cfg_.max_triangles);
         colors_.resize(cfg_.compute_colors ? (size_t)cfg_.max_mesh_vertices : 0);
+        normals_.resize(cfg_.compute_normals ? (size_t)cfg_.max_mesh_vertices : 0);
         psr_points p{xyz, normals, rgb, count, location};
         psr_options o{depth, cg_iterations};
         psr_mesh m{};
         m.vertices = (float*)vertices_.data();
         m.triangles = (int32_t*)triangles_.data();
         m.colors = cfg_.compute_colors ? (float*)colors_.data() : nullptr;
+        m.normals = cfg_.compute_normals ? (float*)normals_.data() : nullptr;
         m.vertex_capacity = cfg_.max_mesh_vertices;
         m.triangle_capacity = cfg_.max_triangles;
         m.location = PSR_HOST;
@@ -84,6 +95,7 @@ public:
         vertices_.resize((size_t)m.vertex_count);
         triangles_.resize((size_t)m.triangle_count);
         if (cfg_.compute_colors) colors_.resize((size_t)m.vertex_count);
+        if (cfg_.compute_normals) normals_.resize((size_t)m.vertex_count);
         center_[0] = m.center[0]; center_[1] = m.center[1]; center_[2] = m.center[2];
         scale_ = m.scale;
     }
@@ -116,21 +128,12 @@ public:
     const std::vector<Point3D>& GetRebuildMeshVertices() const { return vertices_; }
     const std::vector<TriangleIndex>& GetRebuildMeshTriangleIndices() const { return triangles_; }
     const std::vector<Point3D>& GetRebuildMeshColors() const { return colors_; }
+    const std::vector<Point3D>& GetRebuildMeshNormals() const { return normals_; }
     const float* BoundingBoxOrigin() const { return center_; }
     float BoundingBoxEdge() const { return scale_; }
     psr_handle* handle() const { return h_; }
 
 private:
-    static void check(cudaError_t e) {
-        if (e != cudaSuccess) throw std::runtime_error(cudaGetErrorString(e));
-    }
-    void ensure_staging(int count) {
-        if (count <= staging_count_) return;
-        if (staging_) cudaFree(staging_);
-        staging_ = nullptr;
-        check(cudaMalloc(&staging_, 6 * sizeof(float) * (size_t)count + 3 * (size_t)count));
-        staging_count_ = count;
-    }
     psr_config cfg_{};
     psr_handle* h_ = nullptr;
     float* staging_ = nullptr;
@@ -138,6 +141,7 @@ private:
     std::vector<Point3D> vertices_;
     std::vector<TriangleIndex> triangles_;
     std::vector<Point3D> colors_;
+    std::vector<Point3D> normals_;
     float center_[3] = {0, 0, 0};
     float scale_ = 0;
 };

@@ -5,7 +5,8 @@ The reference reconstructs one cloud per blocking call (mesh/PoissonReconstructi
 one CUDA stream and one device-resident output mesh each -- and one host thread drives
 them through the non-blocking C ABI (psr_submit / psr_poll): a request that arrives while
 others are on the GPU is admitted as soon as a slot is free, and the slots' work overlaps
-on the device.  K is bounded by a device-memory budget (the handles' workspace sizes).
+on the device.  K is bounded by a device-memory budget (the handles' workspaces and output buffers); slots
+of several sizes admit each cloud by its footprint (point count and depth).
 Each slot's pipeline is one chain (concurrent_stages off): with K reconstructions
 already overlapping, a second stream per slot only adds contention.
 Results are the same as psr_reconstruct alone (the pipeline is deterministic per handle).
@@ -54,14 +55,30 @@ class _Slot:
     out: list
     mesh: object = None
     req: Request = None
+    max_points: int = 1 << 30     # the largest cloud and depth the slot's workspace takes
+    max_depth: int = 9
+    vcap: int = 0                 # output capacities (0: the server's)
+    tcap: int = 0
+
+    def fits(self, req):
+        return req.xyz.shape[0] <= self.max_points and (req.depth or self.max_depth) <= self.max_depth
 
 
 class Server:
-    """K concurrent reconstruction slots on one GPU, driven from one host thread."""
+    """Concurrent reconstruction slots on one GPU, driven from one host thread.
+
+    `slots` handles of one size (max_points, max_depth, output capacities), or `classes`:
+    a list of dicts, each {"count": n, "max_points": ..., "max_depth": ..., "max_triangles":
+    ..., "max_mesh_vertices": ...} (other handle settings as keyword arguments), for clouds
+    of uneven size: a request is admitted into the first free slot whose workspace takes its
+    point count and depth, so small clouds do not hold a workspace sized for the largest.
+    `memory_budget` (bytes) bounds the device memory of all slots: each slot costs its
+    handle's workspace plus its output buffers; slots of a class are created while the
+    budget allows, classes in the order given, at least one slot per class."""
 
     def __init__(self, slots=8, max_depth=7, max_points=300000, max_triangles=1000000, max_mesh_vertices=300000,
                  compute_colors=True, compute_normals=True, device=0, memory_budget=None, host_outputs=False,
-                 **caps):
+                 classes=None, **caps):
         import torch
         self.torch = torch
         self.dev = torch.device("cuda", device)
@@ -69,36 +86,50 @@ class Server:
         self.compute_colors, self.compute_normals = compute_colors, compute_normals
         self.host_outputs = host_outputs
         self.slots = []
-        for k in range(slots):
-            r = psr.PoissonReconstruction(max_depth=max_depth, max_points=max_points, max_triangles=max_triangles,
-                                          max_mesh_vertices=max_mesh_vertices, compute_colors=compute_colors,
-                                          compute_normals=compute_normals, device=device,
-                                          **{"concurrent_stages": False, **caps})
-            if memory_budget is not None and (k + 1) * self.slot_bytes(r) > memory_budget:
-                r.close()
-                if k == 0:
-                    raise ValueError(f"memory_budget {memory_budget} B is below one slot "
-                                     f"({self.slot_bytes(r)} B: workspace and output buffers)")
-                break
-            def buf(shape, dtype):
-                if host_outputs:
-                    return torch.empty(shape, dtype=dtype).pin_memory()
-                return torch.empty(shape, dtype=dtype, device=self.dev)
-            out = [buf((self.vcap, 3), torch.float32), buf((self.tcap, 3), torch.int32),
-                   buf((self.vcap, 3), torch.float32) if compute_colors else None,
-                   buf((self.vcap, 3), torch.float32) if compute_normals else None]
-            self.slots.append(_Slot(r, torch.cuda.Stream(self.dev), out))
+        self.rejected = []
+        if classes is None:
+            classes = [dict(count=slots, max_points=max_points, max_depth=max_depth, max_triangles=max_triangles,
+                            max_mesh_vertices=max_mesh_vertices)]
+        used = 0
+        for ci, cl in enumerate(classes):
+            cl = dict(cl)
+            count = cl.pop("count")
+            vcap, tcap = cl.get("max_mesh_vertices", max_mesh_vertices), cl.get("max_triangles", max_triangles)
+            for k in range(count):
+                r = psr.PoissonReconstruction(compute_colors=compute_colors, compute_normals=compute_normals,
+                                              device=device, **{"concurrent_stages": False, **caps, **cl})
+                cost = self.slot_bytes(r, vcap, tcap)
+                if memory_budget is not None and used + cost > memory_budget:
+                    r.close()
+                    if k == 0:
+                        self.close()
+                        raise ValueError(f"memory_budget {memory_budget} B leaves no slot of class {ci} "
+                                         f"({cost} B: workspace and output buffers)")
+                    break
+                used += cost
+                def buf(shape, dtype):
+                    if host_outputs:
+                        return torch.empty(shape, dtype=dtype).pin_memory()
+                    return torch.empty(shape, dtype=dtype, device=self.dev)
+                out = [buf((vcap, 3), torch.float32), buf((tcap, 3), torch.int32),
+                       buf((vcap, 3), torch.float32) if compute_colors else None,
+                       buf((vcap, 3), torch.float32) if compute_normals else None]
+                self.slots.append(_Slot(r, torch.cuda.Stream(self.dev), out, max_points=r.config.max_points,
+                                        max_depth=r.config.max_depth, vcap=vcap, tcap=tcap))
+        self.memory_bytes = used
         self.queue = []
         self.done = []
 
-    def slot_bytes(self, recon):
+    def slot_bytes(self, recon, vcap=None, tcap=None):
         """Device bytes of one slot: the handle's workspace plus its output mesh buffers
         (vertices, triangles, and colours / normals when computed; none on the device when
         outputs go to pinned host memory)."""
+        vcap = self.vcap if vcap is None else vcap
+        tcap = self.tcap if tcap is None else tcap
         out = 0
         if not self.host_outputs:
             per_vertex = 12 * (1 + int(self.compute_colors) + int(self.compute_normals))
-            out = per_vertex * self.vcap + 12 * self.tcap
+            out = per_vertex * vcap + 12 * tcap
         return recon.memory_bytes() + out
 
     def close(self):
@@ -111,13 +142,21 @@ class Server:
     def submit(self, req):
         if not req.arrival:
             req.arrival = time.perf_counter()
+        if not any(sl.fits(req) for sl in self.slots):
+            # no slot of this server takes the cloud: finished at once with an error
+            req.admitted = req.finished = time.perf_counter()
+            req.error = "rejected: no slot takes this cloud's point count and depth"
+            self.rejected.append(req)
+            self.done.append(req)
+            return
         self.queue.append(req)
 
     def _admit(self, sl, req):
         o = sl.out
+        vcap, tcap = (sl.vcap or self.vcap), (sl.tcap or self.tcap)
         sl.mesh = psr.PsrMesh(o[0].data_ptr(), o[1].data_ptr(),
                               o[2].data_ptr() if (o[2] is not None and req.rgb is not None) else None,
-                              o[3].data_ptr() if o[3] is not None else None, self.vcap, self.tcap,
+                              o[3].data_ptr() if o[3] is not None else None, vcap, tcap,
                               psr.PSR_HOST if self.host_outputs else psr.PSR_DEVICE, 0, 0)
         req.admitted = time.perf_counter()
         sl.req = req
@@ -148,7 +187,8 @@ class Server:
         self.done.append(req)
 
     def step(self):
-        """Collects finished slots and admits queued requests; returns the number of busy slots."""
+        """Collects finished slots and admits queued requests (the oldest request that fits
+        a free slot first); returns the number of busy slots."""
         busy = 0
         for sl in self.slots:
             if sl.req is not None:
@@ -160,7 +200,10 @@ class Server:
                 if fin:
                     self._finish(sl)
             if sl.req is None and self.queue:
-                self._admit(sl, self.queue.pop(0))
+                for qi, rq in enumerate(self.queue):
+                    if sl.fits(rq):
+                        self._admit(sl, self.queue.pop(qi))
+                        break
             busy += sl.req is not None
         return busy
 

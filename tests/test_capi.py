@@ -85,7 +85,7 @@ def test_cpp_shim_compiles(tmp_path):
     if not shutil.which("g++"):
         pytest.skip("no g++")
     src = tmp_path / "shim.cpp"
-    src.write_text('#include "psr/PoissonReconstruction.hpp"\n'
+    src.write_text('#include "psr/PoissonReconstruction.hpp"\n#include "psr/Server.hpp"\n'
                    'int main() { psr_gb300::PoissonReconstruction* p = nullptr; (void)p; return 0; }\n')
     cuda_inc = "/usr/local/cuda/include"
     r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", str(ROOT / "include"), "-I", cuda_inc, str(src)],

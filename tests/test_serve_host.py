@@ -59,7 +59,7 @@ def make_server(recons):
     for r in recons:
         out = [torch.zeros(16, 3), torch.zeros(16, 3, dtype=torch.int32), None, torch.zeros(16, 3)]
         s.slots.append(serve._Slot(r, FakeStream(), out))
-    s.queue, s.done = [], []
+    s.queue, s.done, s.rejected = [], [], []
     return s
 
 
@@ -115,3 +115,20 @@ def test_latency_summary_skips_failed_requests():
     s = serve.latency_summary([ok, bad])
     assert s["p99_ms"] == pytest.approx(2.0)
     assert serve.latency_summary([bad]) == {"p50_ms": None, "p99_ms": None}
+
+
+def test_footprint_classes_first_fit_and_rejection():
+    """Slots of two sizes: a large cloud waits for the large slot while small clouds queued
+    behind it go to the small slot; a cloud no slot takes is rejected at once."""
+    small, large = FakeRecon("small", polls=1), FakeRecon("large", polls=4)
+    s = make_server([small, large])
+    s.slots[0].max_points, s.slots[1].max_points = 100, 1000
+    reqs = [req(500, "big0"), req(600, "big1"), req(50, "s0"), req(60, "s1"), req(5000, "huge")]
+    done = s.run(reqs)
+    by = {r.tag: r for r in done}
+    assert "rejected" in by["huge"].error
+    assert s.rejected == [by["huge"]]
+    assert small.submitted == [50, 60] and large.submitted == [500, 600]
+    # the small clouds did not wait behind big1, which waited for the large slot
+    assert by["s1"].finished <= by["big1"].admitted + 1e-3
+    assert all(by[t].error == "" for t in ("big0", "big1", "s0", "s1"))
