@@ -297,8 +297,16 @@ def main():
                         torch.from_numpy(cc).pin_memory() if cc is not None else None, depth))
     caps = dict(max_depth=depth, max_points=max(300000, n), max_triangles=1000000, max_mesh_vertices=300000,
                 compute_colors=rgb is not None, compute_normals=True, device=local)
-    server = Server(slots=args.slots, **caps)
-    server_h = Server(slots=args.slots, host_outputs=True, **caps)
+    # launch shapes of the served slots chosen by the autotuner (CG cluster sizes)
+    import autotune
+    from serve import Request as _Req
+    def tune_requests():
+        return [_Req(xyz=c[0], normals=c[1], rgb=c[2], depth=c[3]) for _ in range(2) for c in dclouds]
+    tuned, tune_table = autotune.tune_served(lambda **kw: Server(slots=args.slots, **caps, **kw), tune_requests,
+                                             torch, dev)
+    tuned_kw = dict(cg_cluster_ctas=tuned[0], cg_cluster_ctas_fine=tuned[1])
+    server = Server(slots=args.slots, **caps, **tuned_kw)
+    server_h = Server(slots=args.slots, host_outputs=True, **caps, **tuned_kw)
     served_leg(server, dclouds, 2, torch, dev)
     served_leg(server_h, hclouds, 2, torch, dev)
     with ClockSampler(local) as clk:
@@ -406,10 +414,14 @@ def main():
             # nodes + the output copy kernel, K reconstructions per step
             "gpu_launches": (int(st_launches(server.slots[0].recon)) + 1) * K * args.steps,
             "gpu_launches_per_recon": int(st_launches(server.slots[0].recon)) + 1,
-            "roofline": roofline, "clocks": clocks}
+            "roofline": roofline, "clocks": clocks,
+            "autotune": {"chosen": {"cg_cluster_ctas": tuned[0], "cg_cluster_ctas_fine": tuned[1]},
+                         "served_recons_per_s": {f"{a}x{b}": (round(v, 1) if v else None)
+                                                 for (a, b), v in tune_table.items()},
+                         "plain": "cg_cluster_ctas 16 (the device's widest cluster), fine 8"}}
     line.update(side_legs(psr, r, caps, d_xyz, d_nrm, d_rgb, n, depth, dev_mesh, stream, torch, st))
     try:
-        line["batch"] = batch_leg(psr, caps, dclouds, args.steps, torch, dev, args.batch)
+        line["batch"] = batch_leg(psr, {**caps, **tuned_kw}, dclouds, args.steps, torch, dev, args.batch)
         line["batch"]["vs_plain"] = line["batch"]["value"] / plain_value
     except Exception as e:   # reported, not fatal: the headline legs are above
         line["batch"] = {"error": str(e)}

@@ -84,6 +84,11 @@ typedef struct psr_config {
                                   them (the clouds' data never mix; each result equals the
                                   one-cloud call's).  Device memory: K x psr_memory_bytes of a
                                   one-cloud handle */
+    int cg_cluster_ctas;       /* CTAs of the thread-block cluster that solves depth D (1..16;
+                                  0: the largest the device schedules, 16 on GB300).  Fewer
+                                  CTAs take more rows each: longer per call, less SM time, which
+                                  is what many concurrent reconstructions share */
+    int cg_cluster_ctas_fine;  /* the same for depths D-1 and D-2 (0: 8) */
 } psr_config;
 
 /* Oriented input cloud (the fields of DepthSurfel, base/CommonTypes.h:113-118, as SoA). */

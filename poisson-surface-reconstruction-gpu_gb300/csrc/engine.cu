@@ -411,7 +411,11 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     A.add(ws.mb.misc, 16);
     A.add(ws.d_params, 16);
 
-    if (cfg.batch_clouds > kMaxBatchClouds) { delete h; return PSR_INVALID_INPUT; }
+    if (cfg.batch_clouds > kMaxBatchClouds || cfg.cg_cluster_ctas < 0 || cfg.cg_cluster_ctas > 16 ||
+        cfg.cg_cluster_ctas_fine < 0 || cfg.cg_cluster_ctas_fine > 16) {
+        delete h;
+        return PSR_INVALID_INPUT;
+    }
     h->clouds = cfg.batch_clouds > 1 ? cfg.batch_clouds : 1;
     if (h->clouds == 1) {
         e = cudaMalloc(&h->arena, A.bytes);
@@ -424,6 +428,8 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     h->arena_bytes = A.bytes;
     A.assign((char*)h->arena);
     set_batch(ws, 1);
+    ws.cg_ctas = cfg.cg_cluster_ctas;
+    ws.cg_ctas_fine = cfg.cg_cluster_ctas_fine;
     ws.scan.max_tiles = cap.scan_tiles;
     // scan counters and epoch start at zero; the scans keep them consistent afterwards
     e = cudaMemset(ws.scan.words, 0, sizeof(unsigned long long) * ((size_t)cap.scan_tiles + kScanHeader));

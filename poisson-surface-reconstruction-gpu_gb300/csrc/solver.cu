@@ -175,8 +175,16 @@ __device__ __forceinline__ void cgc_allreduce(cg::cluster_group& cl, CgcShared& 
 
 // After the r.r reduction of an iteration (thread 0): beta, the continue flag and whether
 // the true residual is due.  `it` is the iteration just completed.
+// The step scalars are quotients of the FP64 sums rounded to float and divided in FP32 (within
+// 1.5 ulp of the FP64 quotient rounded to float): an FP64 division on the one thread that
+// finishes the sums sits on every iteration's critical path, and GB300 divides in FP64
+// slowly.
+__device__ __forceinline__ float cg_quot(double num, double den) {
+    return den != 0.0 ? __fdiv_rn((float)num, (float)den) : 0.0f;
+}
+
 __device__ __forceinline__ void cg_after_rr(CgcShared& sh, const CgcArgs& a, double w, int it) {
-    sh.beta = (sh.rr != 0.0) ? (float)(w / sh.rr) : 0.0f;
+    sh.beta = cg_quot(w, sh.rr);
     sh.rr_prev = sh.rr;
     sh.rr = w;
     const bool conv = !((float)w > a.tol2);   // the reference compares a float r.r (CGAlgorithm.cu:36)
@@ -382,7 +390,7 @@ __device__ __forceinline__ void cgc_resident(cg::cluster_group& cl, CgcShared& s
         }
         cgc_allreduce(cl, sh, buf, acc, [&](double w) {
             sh.pap = w;
-            sh.alpha = (w != 0.0) ? (float)(sh.rr / w) : 0.0f;
+            sh.alpha = cg_quot(sh.rr, w);
         });
         const float alpha = sh.alpha;
         // (B) x and r, r.r
@@ -485,7 +493,7 @@ __device__ __forceinline__ void cgc_global(cg::cluster_group& cl, CgcShared& sh,
         }
         cgc_allreduce(cl, sh, buf, acc, [&](double w) {
             sh.pap = w;
-            sh.alpha = (w != 0.0) ? (float)(sh.rr / w) : 0.0f;
+            sh.alpha = cg_quot(sh.rr, w);
         });
         const float alpha = sh.alpha;
         acc = ff_zero();
@@ -799,7 +807,8 @@ cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, 
         CgcArgs b = a;
         b.first = D - 1;
         set_stencils(b);
-        const int cl2 = g_cg_cluster < 8 ? g_cg_cluster : 8;
+        int cl2 = ws.cg_ctas_fine > 0 ? ws.cg_ctas_fine : 8;
+        if (cl2 > g_cg_cluster) cl2 = g_cg_cluster;
         e = launch_cg(k_cg_cluster, b, (ncl - 1) * cl2, cl2, ws.batch, ws.aux3);
         if (e == cudaSuccess) e = cudaEventRecord(ws.ev_join3, ws.aux3);
         if (e != cudaSuccess) return e;
@@ -821,7 +830,9 @@ cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, 
     if (ncl > 0) {
         a.first = D;
         set_stencils(a);
-        e = launch_cg(k_cg_cluster, a, g_cg_cluster, g_cg_cluster, ws.batch, s);
+        int cl1 = ws.cg_ctas > 0 ? ws.cg_ctas : g_cg_cluster;
+        if (cl1 > g_cg_cluster) cl1 = g_cg_cluster;
+        e = launch_cg(k_cg_cluster, a, cl1, cl1, ws.batch, s);
         if (e != cudaSuccess) return e;
     }
     if (ws.ev_cg) {

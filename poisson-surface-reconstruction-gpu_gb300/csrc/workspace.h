@@ -47,6 +47,8 @@ struct MeshBufs {
 
 struct Workspace {
     int batch = 1;          // clouds of the launches being issued (the grids' y extent)
+    int cg_ctas = 0;        // CTAs of the depth-D CG cluster (0: the largest the device runs, 16)
+    int cg_ctas_fine = 0;   // CTAs of each depth-(D-1), (D-2) CG cluster (0: 8)
     MeshBufs mb;
     Caps cap;
     int depth;

@@ -35,7 +35,8 @@ class PsrConfig(ctypes.Structure):
                 ("laplacian_epsilon", ctypes.c_float), ("concurrent_stages", ctypes.c_int),
                 ("weld_vertices", ctypes.c_int), ("disable_graphs", ctypes.c_int),
                 ("root_poly_capacity", ctypes.c_int), ("cg_residual_period", ctypes.c_int),
-                ("batch_clouds", ctypes.c_int)]
+                ("batch_clouds", ctypes.c_int), ("cg_cluster_ctas", ctypes.c_int),
+                ("cg_cluster_ctas_fine", ctypes.c_int)]
 
 
 class PsrPoints(ctypes.Structure):
@@ -148,7 +149,8 @@ class PoissonReconstruction:
     def __init__(self, max_depth=7, max_points=300000, max_triangles=1000000, max_mesh_vertices=300000,
                  compute_colors=False, compute_normals=False, cg_tolerance=1e-5, cg_max_iterations=10000,
                  max_nodes=0, max_subdivision_nodes=0, device=0, laplacian_epsilon=1e-6, concurrent_stages=True, weld_vertices=False,
-                 disable_graphs=False, root_poly_capacity=0, cg_residual_period=0, batch_clouds=1):
+                 disable_graphs=False, root_poly_capacity=0, cg_residual_period=0, batch_clouds=1,
+                 cg_cluster_ctas=0, cg_cluster_ctas_fine=0):
         self._lib = load_library()
         cfg = default_config()
         cfg.max_depth = max_depth
@@ -169,6 +171,8 @@ class PoissonReconstruction:
         cfg.root_poly_capacity = int(root_poly_capacity)
         cfg.cg_residual_period = int(cg_residual_period)
         cfg.batch_clouds = int(batch_clouds)
+        cfg.cg_cluster_ctas = int(cg_cluster_ctas)
+        cfg.cg_cluster_ctas_fine = int(cg_cluster_ctas_fine)
         self.config = cfg
         h = ctypes.c_void_p()
         st = self._lib.psr_create(ctypes.byref(cfg), ctypes.byref(h))

@@ -53,7 +53,7 @@ def test_struct_layouts_match_header(tmp_path):
     import shutil
     import subprocess
     import psr
-    assert ctypes.sizeof(psr.PsrConfig) == 19 * 4
+    assert ctypes.sizeof(psr.PsrConfig) == 21 * 4
     assert ctypes.sizeof(psr.PsrPoints) == 32
     assert ctypes.sizeof(psr.PsrOptions) == 8
     if not shutil.which("gcc"):
