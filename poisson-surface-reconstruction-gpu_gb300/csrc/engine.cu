@@ -65,6 +65,7 @@ struct psr_handle {
     bool pending = false;
     bool pend_batch = false;
     std::vector<psr_mesh> pend_meshes;        // copies of the callers' mesh descriptors
+    std::vector<char> pend_emitted;           // per cloud: outputs written by the GPU
     psr_mesh* pend_user_mesh = nullptr;       // single call: the caller's descriptor
     psr_mesh* pend_user_meshes = nullptr;     // batch call: the callers' descriptors
     int pend_depth = 0, pend_colour = 0, pend_normals = 0;
@@ -666,20 +667,43 @@ static cudaError_t stage_inputs(psr_handle* h, const psr_points* pts, int k, cud
     return e;
 }
 
-// Enqueues the count read-back of slot k and, for device-resident outputs, the copy of its
-// mesh into the caller's buffers (counts read on the device: no host wait).
+// Device address of a host output buffer the GPU can write (pinned or registered host
+// memory), else nullptr.  NULL stays NULL (output not asked for).
+static void* device_view(void* p, bool& ok) {
+    if (!p) return nullptr;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        (void)cudaGetLastError();
+        ok = false;
+        return nullptr;
+    }
+    if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) return p;
+    if (at.type == cudaMemoryTypeHost && at.devicePointer) return at.devicePointer;
+    ok = false;
+    return nullptr;
+}
+
+// Enqueues the count read-back of slot k and the copy of its mesh into the caller's
+// buffers by a kernel that reads the counts on the device (no host wait): for device
+// outputs, and for host outputs in pinned or registered memory, which the kernel writes
+// through their device addresses.  Other host outputs are copied when the work has
+// completed (*emitted = false).
 static cudaError_t stage_outputs(psr_handle* h, psr_mesh* mesh, int k, int want_colour, int want_normals,
-                                 cudaStream_t s) {
+                                 cudaStream_t s, bool* emitted) {
     Workspace& ws = h->ws;
     cudaError_t e =
         cudaMemcpyAsync(h->cnt_host_all + k, slot_ptr(ws.cnt, k), sizeof(Counters), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess && mesh->location == PSR_DEVICE) {
+    bool ok = true;
+    void* dv = device_view(mesh->vertices, ok);
+    void* dt = device_view(mesh->triangles, ok);
+    void* dc = want_colour ? device_view(mesh->colors, ok) : nullptr;
+    void* dn = want_normals ? device_view(mesh->normals, ok) : nullptr;
+    *emitted = ok;
+    if (e == cudaSuccess && ok) {
         k_emit_mesh<<<ws.num_sms * 4, kBlock, 0, s>>>(slot_ptr(ws.cnt, k), slot_ptr(ws.mesh_v, k),
                                                       slot_ptr(ws.mesh_t, k), slot_ptr(ws.mesh_c, k),
-                                                      slot_ptr(ws.mesh_n, k), mesh->vertices, mesh->triangles,
-                                                      want_colour ? mesh->colors : nullptr,
-                                                      want_normals ? mesh->normals : nullptr, mesh->vertex_capacity,
-                                                      mesh->triangle_capacity);
+                                                      slot_ptr(ws.mesh_n, k), (float*)dv, (int*)dt, (float*)dc,
+                                                      (float*)dn, mesh->vertex_capacity, mesh->triangle_capacity);
         e = cudaGetLastError();
     }
     return e;
@@ -722,7 +746,12 @@ static psr_status submit_clouds(psr_handle* h, const psr_points* pts, int count,
     for (int k = 0; k < count && e == cudaSuccess; ++k) e = stage_inputs(h, pts + k, k, s);
     if (e != cudaSuccess) return cuda_fail(h, e, "input copy");
     e = launch_pipeline(h, depth, cg_iters, want_colour, want_normals, has_rgb, count, s);
-    for (int k = 0; k < count && e == cudaSuccess; ++k) e = stage_outputs(h, meshes + k, k, want_colour, want_normals, s);
+    h->pend_emitted.assign(count, 0);
+    for (int k = 0; k < count && e == cudaSuccess; ++k) {
+        bool em = false;
+        e = stage_outputs(h, meshes + k, k, want_colour, want_normals, s, &em);
+        h->pend_emitted[k] = em;
+    }
     if (e == cudaSuccess) e = cudaEventRecord(h->done, s);
     if (e != cudaSuccess) return cuda_fail(h, e, "reconstruct");
     h->pending = true;
@@ -790,7 +819,7 @@ static psr_status finish_cloud(psr_handle* h, int k, const Counters& c, psr_stat
         h->last_error = "output mesh buffers too small";
         return PSR_OUT_OF_CAPACITY;
     }
-    if (mesh->location == PSR_DEVICE) return PSR_OK;   // written by k_emit_mesh
+    if (h->pend_emitted[k]) return PSR_OK;   // written by k_emit_mesh
     const cudaMemcpyKind ok = cudaMemcpyDeviceToHost;
     cudaError_t e = cudaSuccess;
     if (mesh->vertices && c.n_mesh_vertices)
@@ -818,7 +847,9 @@ static psr_status complete_impl(psr_handle* h) {
         h->batch_status[k] = st;
         if (st != PSR_OK && first == PSR_OK) first = st;
     }
-    const cudaError_t e = cudaStreamSynchronize(h->pend_stream);   // the host copies
+    bool copies = false;
+    for (int k = 0; k < count; ++k) copies = copies || (!h->pend_emitted[k] && h->batch_status[k] == PSR_OK);
+    const cudaError_t e = copies ? cudaStreamSynchronize(h->pend_stream) : cudaSuccess;   // the host copies
     if (h->pend_batch) {
         for (int k = 0; k < count; ++k) h->pend_user_meshes[k] = h->pend_meshes[k];
     } else {
