@@ -205,7 +205,8 @@ psr_status psr_submit_batch(psr_handle* h, const psr_points* points, int count, 
 psr_status psr_reconstruct_batch(psr_handle* h, const psr_points* points, int count, const psr_options* options,
                                  psr_mesh* meshes, void* stream);
 /* Status and statistics of cloud `index` of the last completed call (index 0 for a one-cloud
- * call); `out` may be NULL. */
+ * call); `out` may be NULL.  Returns PSR_INVALID_INPUT, leaving `out` untouched, when the
+ * last completed call had no cloud `index` (or no call has completed yet). */
 psr_status psr_get_batch_result(const psr_handle* h, int index, psr_stats* out);
 
 /* Input adaptor: device array of `count` DepthSurfel records (base/CommonTypes.h:113-118,
