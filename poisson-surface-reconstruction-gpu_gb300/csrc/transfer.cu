@@ -139,7 +139,7 @@ __device__ __forceinline__ unsigned spread3(unsigned v) {
 // away), spread over the group's lanes (flattened over the 27 cell ranges), each lane
 // keeping a sorted 4-list, merged by warp-minimum rounds within the group.  When 4 were
 // found and the 4th is closer than one width they are the exact 4 nearest and the colour
-// is written; otherwise the vertex goes to the far list for the wide search (k_colour).
+// is written; otherwise the vertex goes to the far list for the wide search (k_colour_far).
 constexpr int kNearLanes = 8;
 constexpr int kNearGroups = kBlock / kNearLanes;
 __global__ void __launch_bounds__(kBlock) k_colour_near(Counters* c, int g, const float* mv, const float* px,
@@ -227,143 +227,137 @@ __global__ void __launch_bounds__(kBlock) k_colour_near(Counters* c, int g, cons
     }
 }
 
-constexpr int kColourMaxShell = 12;   // widest block (2R+1 cells per axis) searched at one level
-
-// Far pass, one block of 256 threads per vertex of the far list.  The samples are
-// Morton-sorted, so the samples of a grid cell at any level g <= gmax form one contiguous
-// range, read from the level-gmax table at cell codes shifted by 3 (gmax - g).  At the
-// finest level the block gathers the samples of the 3x3x3 block of cells around the
-// vertex's cell (the 27 ranges flattened over the threads) and keeps the 4 nearest
-// (private sorted lists, merged by warp-minimum rounds).  Every sample
-// outside a block of radius R cells is at least R cell widths away, so:
-//   * 4 found and the 4th distance below 1 width: done;
-//   * 4 found otherwise: the 4th distance bounds the answer; the shell of cells between
-//     radius 2 and the radius R that exceeds it (one thread per cell) completes the search;
-//   * fewer than 4, or R too large: restart one level coarser.
-// the block's 4 nearest from its threads' sorted 4-lists: each warp merges its lanes, then
-// warp 0 merges the warps' 4 (one candidate per lane); every thread gets the result
-constexpr int kFarThreads = kBlock;
-static_assert(kFarThreads / 32 * 4 == 32, "one warp holds the candidates of all warps");
-__device__ __forceinline__ void knn_block_merge(const float (&bd)[4], const int (&bi)[4], float (&md)[4],
-                                                int (&mi)[4], float* s_cd, int* s_ci) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    float wd[4];
-    int wi[4];
-    knn_warp_merge(bd, bi, wd, wi);
-    if (lane == 0) {
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            s_cd[warp * 4 + q] = wd[q];
-            s_ci[warp * 4 + q] = wi[q];
-        }
-    }
-    __syncthreads();
-    if (warp == 0) {
-        const float cd[4] = {s_cd[lane], 1e6f, 1e6f, 1e6f};
-        const int ci[4] = {s_ci[lane], 0x7fffffff, 0x7fffffff, 0x7fffffff};
-        knn_warp_merge(cd, ci, wd, wi);
-    }
-    __syncthreads();   // every warp has read its candidates before they are replaced
-    if (threadIdx.x == 0) {
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            s_cd[q] = wd[q];
-            s_ci[q] = wi[q];
-        }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        md[q] = s_cd[q];
-        mi[q] = s_ci[q];
-    }
-    __syncthreads();   // read before the next merge writes
+// bits 0, 3, 6, ... of v gathered into the low bits (the inverse of spread3)
+__device__ __forceinline__ unsigned compact3(unsigned v) {
+    v &= 0x09249249u;
+    v = (v | (v >> 2)) & 0x030c30c3u;
+    v = (v | (v >> 4)) & 0x0300f00fu;
+    v = (v | (v >> 8)) & 0x030000ffu;
+    v = (v | (v >> 16)) & 0x3ffu;
+    return v;
 }
 
-__global__ void __launch_bounds__(kFarThreads) k_colour(const Counters* c, int gmax, const float* mv,
+// the sorted 4-list of the union of two sorted 4-lists over disjoint sample sets: four
+// rounds, each taking the smaller head and shifting that list (registers only)
+__device__ __forceinline__ void knn_merge4(float (&md)[4], int (&mi)[4], const float (&ld)[4], const int (&li)[4]) {
+    float ad[4] = {md[0], md[1], md[2], md[3]}, bd[4] = {ld[0], ld[1], ld[2], ld[3]};
+    int ai[4] = {mi[0], mi[1], mi[2], mi[3]}, bi[4] = {li[0], li[1], li[2], li[3]};
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const bool take_b = knn_less(bd[0], bi[0], ad[0], ai[0]);
+        md[r] = take_b ? bd[0] : ad[0];
+        mi[r] = take_b ? bi[0] : ai[0];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            ad[q] = take_b ? ad[q] : ad[q + 1];
+            ai[q] = take_b ? ai[q] : ai[q + 1];
+            bd[q] = take_b ? bd[q + 1] : bd[q];
+            bi[q] = take_b ? bi[q + 1] : bi[q];
+        }
+        ad[3] = take_b ? ad[3] : 1e6f;
+        ai[3] = take_b ? ai[3] : 0x7fffffff;
+        bd[3] = take_b ? 1e6f : bd[3];
+        bi[3] = take_b ? 0x7fffffff : bi[3];
+    }
+}
+
+// Far pass, one warp per vertex of the far list: a branch-and-bound descent of the grid's
+// cell hierarchy.  The samples are Morton-sorted, so the samples of a cell at any level
+// g <= gmax form one contiguous range, read from the level-gmax table at codes shifted by
+// 3 (gmax - g); the children of cell m are cells 8m .. 8m + 7 one level finer.  From the
+// root, a node is scanned when it is a finest-level cell or holds at most kFarLeaf samples
+// (the lanes split its samples, each keeping a sorted 4-list, merged by warp-minimum rounds
+// into the warp's 4 nearest so far); otherwise its non-empty children are pushed onto a
+// per-warp stack nearest box first.  A node whose box is farther than the 4th nearest so
+// far (with 1e-4 relative slack) is skipped: a sample's float distance is at least its
+// cell box's (the sample lies in the closed box and rounding is monotone).  So the result
+// is the exact 4 nearest under the (distance, index) order, whatever the distance.  The
+// stack holds at most 7 siblings per level plus 8 children: 7 gmax + 9 entries.
+constexpr int kFarWarps = kBlock / 32;
+constexpr int kFarLeaf = 32;
+constexpr int kFarStack = 64;
+static_assert(7 * kColourGridLevel + 9 <= kFarStack, "descent stack");
+
+__global__ void __launch_bounds__(kBlock) k_colour_far(const Counters* c, int gmax, const float* mv,
                                                        const float* px, const float* py, const float* pz,
                                                        const float* cr, const float* cg, const float* cb,
                                                        const int* cell_start, const int* far, float* out) {
     PSR_CLOUD(c, mv, px, py, pz, cr, cg, cb, cell_start, far, out);
-    __shared__ int s_off[28];
-    __shared__ int s_base[27];
-    __shared__ float s_cd[32];
-    __shared__ int s_ci[32];
+    __shared__ int s_node[kFarWarps][kFarStack];    // (level << 24) | cell code
+    __shared__ float s_dist[kFarWarps][kFarStack];  // squared distance to the cell's box
     const int nfar = c->n_colour_far;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int t = blockIdx.x; t < nfar; t += gridDim.x) {
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    int* stk = s_node[wib];
+    float* sdist = s_dist[wib];
+    for (int t = gw; t < nfar; t += nw) {
         const int v = far[t];
         const float qx = mv[3 * (size_t)v], qy = mv[3 * (size_t)v + 1], qz = mv[3 * (size_t)v + 2];
-        float md[4];
-        int mi[4];
-        for (int g = gmax; g >= 0; --g) {
-            const int G = 1 << g;
+        // the warp's 4 nearest so far, the same in every lane
+        float md[4] = {1e6f, 1e6f, 1e6f, 1e6f};
+        int mi[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
+        if (lane == 0) {
+            stk[0] = 0;   // the root: level 0, code 0
+            sdist[0] = 0.0f;
+        }
+        __syncwarp();
+        int top = 1;
+        while (top > 0) {
+            --top;
+            const int node = stk[top];
+            const float nd = sdist[top];
+            __syncwarp();   // every lane has read the entry before the slot is reused
+            if (mi[3] != 0x7fffffff && nd > md[3] * 1.0001f) continue;
+            const int g = node >> 24;
+            const unsigned m = (unsigned)node & 0xffffffu;
             const int shift = 3 * (gmax - g);
-            const int cx = min(max((int)floorf(qx * G), 0), G - 1);
-            const int cy = min(max((int)floorf(qy * G), 0), G - 1);
-            const int cz = min(max((int)floorf(qz * G), 0), G - 1);
-            if (warp == 0) {
-                int cnt = 0, base = 0;
-                if (lane < 27) {
-                    const int a = cx + lane / 9 - 1, b = cy + (lane / 3) % 3 - 1, z = cz + lane % 3 - 1;
-                    if (a >= 0 && a < G && b >= 0 && b < G && z >= 0 && z < G) {
-                        const unsigned m = morton3(a, b, z, g);
-                        base = cell_start[(size_t)m << shift];
-                        cnt = cell_start[(size_t)(m + 1) << shift] - base;
-                    }
-                }
-                int incl = cnt;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const int y = __shfl_up_sync(0xffffffffu, incl, o);
-                    if (lane >= o) incl += y;
-                }
-                if (lane < 27) {
-                    s_off[lane] = incl - cnt;
-                    s_base[lane] = base;
-                }
-                if (lane == 26) s_off[27] = incl;
+            const int s0 = cell_start[(size_t)m << shift], s1 = cell_start[(size_t)(m + 1) << shift];
+            if (g == gmax || s1 - s0 <= kFarLeaf) {
+                float bd[4] = {1e6f, 1e6f, 1e6f, 1e6f};
+                int bi[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
+                for (int j = s0 + lane; j < s1; j += 32) knn_visit(qx, qy, qz, px, py, pz, j, bd, bi);
+                float ld[4];
+                int li[4];
+                knn_warp_merge(bd, bi, ld, li);
+                knn_merge4(md, mi, ld, li);
+                continue;
             }
-            __syncthreads();
-            const int total = s_off[27];
-            float bd[4] = {1e6f, 1e6f, 1e6f, 1e6f};
-            int bi[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
-            int k = 0;
-            for (int i = tid; i < total; i += kFarThreads) {
-                while (s_off[k + 1] <= i) ++k;   // flattened index -> cell (increasing)
-                knn_visit(qx, qy, qz, px, py, pz, s_base[k] + (i - s_off[k]), bd, bi);
-            }
-            knn_block_merge(bd, bi, md, mi, s_cd, s_ci);
-            if (mi[3] == 0x7fffffff) continue;   // fewer than 4 samples in the block
-            const float w = 1.0f / (float)G;
-            if (md[3] < w * w) break;
-            int R = (int)(sqrtf(md[3]) * (float)G) + 1;
-            while (!(md[3] < __fmul_rn(R * w, R * w))) ++R;
-            if (R > kColourMaxShell && g > 0) continue;
-            // shell of cells with Chebyshev radius 2..R (thread-private lists continue)
-            const int side = 2 * R + 1;
-            const int ncell = side * side * side;
-            for (int i = tid; i < ncell; i += kFarThreads) {
-                const int ta = i / (side * side), tr = i - ta * side * side;
-                const int tb = tr / side, tz = tr - tb * side;
-                const int a = cx - R + ta, b = cy - R + tb, z = cz - R + tz;
-                if (a < 0 || a >= G || b < 0 || b >= G || z < 0 || z >= G) continue;
-                if (max(abs(a - cx), max(abs(b - cy), abs(z - cz))) <= 1) continue;
-                // a cell whose box is farther than the 4th nearest holds no closer sample
-                // (rounding is monotone: a sample's float distance is at least the box's)
+            // lanes 0..7: child (g + 1, 8 m + lane), its sample count and box distance
+            const int gc = g + 1;
+            const unsigned child = (m << 3) | (unsigned)(lane & 7);
+            const int cshift = 3 * (gmax - gc);
+            bool keep = false;
+            float d2 = 0.0f;
+            if (lane < 8) {
+                const int n0 = cell_start[(size_t)child << cshift], n1 = cell_start[(size_t)(child + 1) << cshift];
+                const float w = 1.0f / (float)(1 << gc);
+                const int a = (int)compact3(child >> 2), b = (int)compact3(child >> 1), z = (int)compact3(child);
                 const float gx = fmaxf(fmaxf(__fsub_rn(a * w, qx), __fsub_rn(qx, (a + 1) * w)), 0.0f);
                 const float gy = fmaxf(fmaxf(__fsub_rn(b * w, qy), __fsub_rn(qy, (b + 1) * w)), 0.0f);
                 const float gz = fmaxf(fmaxf(__fsub_rn(z * w, qz), __fsub_rn(qz, (z + 1) * w)), 0.0f);
-                const float mind2 = __fadd_rn(__fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy)), __fmul_rn(gz, gz));
-                if (mind2 > md[3] * 1.0001f) continue;
-                const unsigned m = morton3(a, b, z, g);
-                const int s0 = cell_start[(size_t)m << shift], s1 = cell_start[(size_t)(m + 1) << shift];
-                for (int j = s0; j < s1; ++j) knn_visit(qx, qy, qz, px, py, pz, j, bd, bi);
+                d2 = __fadd_rn(__fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy)), __fmul_rn(gz, gz));
+                keep = n1 > n0 && !(mi[3] != 0x7fffffff && d2 > md[3] * 1.0001f);
             }
-            knn_block_merge(bd, bi, md, mi, s_cd, s_ci);
-            break;
+            const unsigned kept = __ballot_sync(0xffffffffu, keep);
+            // rank among the kept children, nearest first (ties: lower child); pushed in
+            // reverse so the nearest is popped next
+            int rank = 0;
+#pragma unroll
+            for (int o = 0; o < 8; ++o) {
+                const float od = __shfl_sync(0xffffffffu, d2, o);
+                if (((kept >> o) & 1u) && (od < d2 || (od == d2 && o < lane))) ++rank;
+            }
+            const int nk = __popc(kept);
+            if (keep) {
+                stk[top + nk - 1 - rank] = (gc << 24) | (int)child;
+                sdist[top + nk - 1 - rank] = d2;
+            }
+            top += nk;
+            __syncwarp();
         }
-        if (tid == 0) colour_blend(md, mi, cr, cg, cb, &out[3 * (size_t)v]);
+        if (lane == 0) colour_blend(md, mi, cr, cg, cb, &out[3 * (size_t)v]);
+        __syncwarp();   // the stack is rewritten for the next vertex
     }
 }
 
@@ -374,6 +368,15 @@ __global__ void __launch_bounds__(kBlock) k_normals_zero(const Counters* c, doub
         acc[3 * (size_t)v] = acc[3 * (size_t)v + 1] = acc[3 * (size_t)v + 2] = 0.0;
         cnt[v] = 0;
     }
+}
+
+// a b - c d within 1.5 ulp (Kahan's difference of products: fma recovers the rounding error
+// of c d), so a sliver triangle's cross product keeps its direction instead of cancelling
+__device__ __forceinline__ float diff_of_products(float a, float b, float c, float d) {
+    const float w = __fmul_rn(c, d);
+    const float e = fmaf(-c, d, w);
+    const float f = fmaf(a, b, -w);
+    return f + e;
 }
 
 __global__ void __launch_bounds__(kBlock) k_triangle_normals(const Counters* c, const float* mv, const int* mt,
@@ -387,7 +390,8 @@ __global__ void __launch_bounds__(kBlock) k_triangle_normals(const Counters* c, 
         const float ox = mv[3 * (size_t)i0], oy = mv[3 * (size_t)i0 + 1], oz = mv[3 * (size_t)i0 + 2];
         const float ax = mv[3 * (size_t)i1] - ox, ay = mv[3 * (size_t)i1 + 1] - oy, az = mv[3 * (size_t)i1 + 2] - oz;
         const float bx = mv[3 * (size_t)i2] - ox, by = mv[3 * (size_t)i2 + 1] - oy, bz = mv[3 * (size_t)i2 + 2] - oz;
-        float nx = ay * bz - az * by, ny = az * bx - ax * bz, nz = ax * by - ay * bx;
+        float nx = diff_of_products(ay, bz, az, by), ny = diff_of_products(az, bx, ax, bz),
+              nz = diff_of_products(ax, by, ay, bx);
         const float l = sqrtf(nx * nx + ny * ny + nz * nz);
         if (l == 0.0f) { nx = ny = nz = 0.0f; }
         else { nx /= l; ny /= l; nz /= l; }
@@ -445,8 +449,8 @@ cudaError_t transfer_build(Workspace& ws, int with_colour, int with_normals) {
         int* cell_start = ws.cell_start;   // (1 << 3g) + 1 entries, from transfer_prepare
         k_colour_near<<<PSR_GRID(ws, grid), kBlock, 0, s>>>(ws.cnt, g, ws.mesh_v, ws.px, ws.py, ws.pz, ws.cr, ws.cg, ws.cb,
                                               cell_start, ws.colour_far, ws.mesh_c);
-        k_colour<<<PSR_GRID(ws, 2 * ws.num_sms), kFarThreads, 0, s>>>(ws.cnt, g, ws.mesh_v, ws.px, ws.py, ws.pz, ws.cr, ws.cg,
-                                                        ws.cb, cell_start, ws.colour_far, ws.mesh_c);
+        k_colour_far<<<PSR_GRID(ws, ws.num_sms * 4), kBlock, 0, s>>>(ws.cnt, g, ws.mesh_v, ws.px, ws.py, ws.pz, ws.cr,
+                                                                   ws.cg, ws.cb, cell_start, ws.colour_far, ws.mesh_c);
     }
     if (with_normals) {
         double* acc = ws.nacc;

@@ -147,6 +147,22 @@ def test_mix_rotated_scaled_clouds_depth7(recon, oracle_mod, cloud):
     assert len(mesh.triangles) > 1000
 
 
+@pytest.mark.parametrize("cloud", [38, 0])
+def test_colour_of_vertices_far_from_every_sample(oracle_mod, cloud):
+    """Serving-mix clouds whose meshes hold many vertices far from every sample: cloud 38
+    (405k points, depth 7) has about 5,900 mesh vertices whose 4th nearest sample lies
+    0.19-0.23 away in the unit cube, cloud 0 (12k points) about 37,000 beyond one colour-grid
+    cell.  Their colours come from the far pass's descent of the cell hierarchy; the whole
+    pipeline, colours included, against the oracle (exact 4 nearest by brute force)."""
+    import psr
+    p, nr, rgb, D = syn.workload("serve", cloud=cloud)
+    assert D == 7
+    caps = dict(max_depth=7, max_points=410000, compute_colors=True, compute_normals=True, laplacian_epsilon=1e-6)
+    with psr.PoissonReconstruction(**caps) as r:
+        mesh, o = full_check_arrays(r, oracle_mod, p, nr, rgb, D)
+    assert len(mesh.vertices) > 30000
+
+
 def test_laplacian_epsilon_is_applied(oracle_mod):
     # a drop threshold between the depth-6 stencil's edge (2.10e-5) and corner (2.48e-5)
     # entries: GPU and oracle drop the same entries (8 fixed CG iterations per depth)
