@@ -342,6 +342,8 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     A.add(ws.cg_r, (size_t)nodes); A.add(ws.cg_p, (size_t)nodes); A.add(ws.cg_q, (size_t)nodes);
     A.add(ws.cg_ap, (size_t)nodes);
     A.add(ws.cg_blk, (size_t)nodes * 8 + 64);
+    A.add(ws.cg_loop, (size_t)kMaxDepth + 1);
+    A.add(ws.cg_loop_part, (size_t)(kMaxDepth + 1) * kLoopMaxBlocks);
     A.add(ws.cg_partial, std::max((size_t)nodes, (size_t)4096 * (kMaxDepth + 1)));
     A.add(ws.point_val, (size_t)N);
     A.add(ws.pv_coef, 27 * ((size_t)dnodes / 8 + 64));
@@ -388,7 +390,7 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     A.add(ws.nacc, 3 * (size_t)cap.mesh_vertices);
     A.add(ws.vcount, (size_t)cap.mesh_vertices);
     A.add(ws.cell_start, ((size_t)1 << (3 * kColourGridLevel)) + 16);
-    A.add(ws.colour_far, (size_t)cap.mesh_vertices);
+    A.add(ws.colour_far, 2 * (size_t)cap.mesh_vertices);
     if (cfg.weld_vertices) {
         size_t slots = 1;
         while (slots < 2 * (size_t)cap.mesh_vertices) slots <<= 1;
@@ -437,6 +439,8 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     ws.scan_aux.max_tiles = cap.scan_tiles;
     if (e == cudaSuccess)
         e = cudaMemset(ws.scan_aux.words, 0, sizeof(unsigned long long) * ((size_t)cap.scan_tiles + kScanHeader));
+    // the device-loop CG's block tickets start at zero; each reduction leaves them at zero
+    if (e == cudaSuccess) e = cudaMemset(ws.cg_loop, 0, sizeof(CgLoopState) * (kMaxDepth + 1));
     ws.sort.max_tiles = sort_tiles;
     ws.sort.scan = ws.scan;   // sort shares the scan scratch (scans are sequential on one stream)
     e = cudaMallocHost(&h->cnt_host_all, sizeof(Counters) * (size_t)h->clouds);
@@ -453,6 +457,9 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ws.ev_join2, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ws.aux3, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ws.ev_join3, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ws.aux4, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ws.ev_join4, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ws.loop_body, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->done, cudaEventDisableTiming);
     // tables
     if (e == cudaSuccess) e = upload_tables_octree();
@@ -508,6 +515,9 @@ psr_status psr_destroy(psr_handle* h) {
     if (h->ws.ev_fork2) cudaEventDestroy(h->ws.ev_fork2);
     if (h->ws.ev_join2) cudaEventDestroy(h->ws.ev_join2);
     if (h->ws.ev_join3) cudaEventDestroy(h->ws.ev_join3);
+    if (h->ws.ev_join4) cudaEventDestroy(h->ws.ev_join4);
+    if (h->ws.aux4) cudaStreamDestroy(h->ws.aux4);
+    if (h->ws.loop_body) cudaStreamDestroy(h->ws.loop_body);
     if (h->ws.aux3) cudaStreamDestroy(h->ws.aux3);
     if (h->ws.aux2) cudaStreamDestroy(h->ws.aux2);
     if (h->ws.aux) cudaStreamDestroy(h->ws.aux);

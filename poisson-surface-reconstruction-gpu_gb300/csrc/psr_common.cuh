@@ -57,6 +57,20 @@ struct Counters {
     unsigned long long cg_depth_ns[kMaxDepth + 1];   // device time of each depth's CG
 };
 
+// State of one depth's CG when it runs as a device loop (a CUDA-graph while node whose
+// body launches one kernel per step over the whole GPU): the scalars the cluster solver
+// keeps in shared memory, in global memory between the kernels of an iteration.
+struct CgLoopState {
+    double rr, rr_prev, pap, floor2, rr_true;
+    float alpha, beta;
+    int go, check, replace, checks, restarts;
+    int active;              // the depth runs in the device loop (else a cluster solves it)
+    int it;                  // iterations done
+    unsigned ticket;         // blocks of the current kernel done (last-block reductions)
+    unsigned long long t0;   // global timer at the start of the solve
+};
+constexpr int kLoopMaxBlocks = 1024;   // blocks along x of a device-loop kernel (partials)
+
 // Look-up tables shared by the kernels (values derived in tables.cpp).
 struct ConstTables {
     int lut_parent[8][27];

@@ -20,6 +20,7 @@
 // Iso-value (:269-305): mean of the implicit function at the sample points, evaluated in
 // FP32 per point and averaged in FP64.
 #include <cooperative_groups.h>
+#include <vector>
 #include "workspace.h"
 #include "tables.cuh"
 
@@ -120,8 +121,16 @@ struct CgcArgs {
     int max_iter;
     int res_period;     // > 0: true residual every res_period iterations; 0: only at
                         // convergence; < 0: never (the recursive residual alone)
+    unsigned loop_mask; // depths the device loop solves when they do not fit the cluster
     float stp[3][27];   // stencils of units 0..2 of k_cg_cluster (depth first - u)
 };
+
+// The resident path holds a depth when its cluster's chunk of rows fits a CTA's shared
+// memory (the last row is the zero row); the root never does.
+__device__ __forceinline__ int cg_chunk(int m, int nblk) { return ((m + nblk - 1) / nblk + 7) & ~7; }
+__device__ __forceinline__ bool cg_fits_resident(int d, int m, int nblk) {
+    return d >= 1 && cg_chunk(m, nblk) < kCgSmemRows;
+}
 
 struct CgcShared {
     FF warp[kCgWarps];
@@ -183,7 +192,8 @@ __device__ __forceinline__ float cg_quot(double num, double den) {
     return den != 0.0 ? __fdiv_rn((float)num, (float)den) : 0.0f;
 }
 
-__device__ __forceinline__ void cg_after_rr(CgcShared& sh, const CgcArgs& a, double w, int it) {
+template <class St, class Ar>
+__device__ __forceinline__ void cg_after_rr(St& sh, const Ar& a, double w, int it) {
     sh.beta = cg_quot(w, sh.rr);
     sh.rr_prev = sh.rr;
     sh.rr = w;
@@ -200,7 +210,8 @@ __device__ __forceinline__ void cg_after_rr(CgcShared& sh, const CgcArgs& a, dou
 // has converged or has drifted more than 2x (in norm) below the true one; at most
 // kCgMaxRefine restarts, each one reducing the true r.r at least fourfold.  `it` is the
 // next iteration's number.
-__device__ __forceinline__ void cg_after_true(CgcShared& sh, const CgcArgs& a, double w, int it) {
+template <class St, class Ar>
+__device__ __forceinline__ void cg_after_true(St& sh, const Ar& a, double w, int it) {
     ++sh.checks;
     const double target = fmax((double)a.tol2, sh.floor2);
     const bool drift = w > 4.0 * fmax(sh.rr, sh.floor2);
@@ -216,7 +227,8 @@ __device__ __forceinline__ void cg_after_true(CgcShared& sh, const CgcArgs& a, d
 }
 
 // Start of a solve (thread 0): r0 = b, so r.r is also ||b||^2.
-__device__ __forceinline__ void cg_start(CgcShared& sh, const CgcArgs& a, double w) {
+template <class St, class Ar>
+__device__ __forceinline__ void cg_start(St& sh, const Ar& a, double w) {
     sh.rr = w;
     sh.beta = 0.0f;
     sh.go = ((float)w > a.tol2) && a.max_iter >= 1;
@@ -228,7 +240,8 @@ __device__ __forceinline__ void cg_start(CgcShared& sh, const CgcArgs& a, double
 }
 
 // Per-depth results of a finished solve (thread 0 of cluster CTA 0).
-__device__ __forceinline__ void cg_report(const CgcVec& v, int d, const CgcShared& sh) {
+template <class St>
+__device__ __forceinline__ void cg_report(const CgcVec& v, int d, const St& sh) {
     v.cw->cg_rr[d] = sh.rr;
     v.cw->cg_rr_true[d] = sh.rr_true;
     v.cw->cg_checks[d] = sh.checks;
@@ -549,8 +562,10 @@ __device__ __forceinline__ void cg_unit_body(const CgcArgs& a, const CgcVec& v, 
     __syncthreads();
     const int nblk = (int)cl.num_blocks();
     const int m = u.row1 - u.row0;
-    const int chunk = ((m + nblk - 1) / nblk + 7) & ~7;   // sibling-group aligned
-    if (u.d >= 1 && chunk < kCgSmemRows) {   // uniform over the cluster; the last row is the zero row
+    const int chunk = cg_chunk(m, nblk);   // sibling-group aligned
+    const bool fits = cg_fits_resident(u.d, m, nblk);   // uniform over the cluster
+    if (!fits && ((a.loop_mask >> u.d) & 1u)) return;    // the device loop solves this depth
+    if (fits) {
         float2* rp0 = reinterpret_cast<float2*>(cg_dyn);
         float2* rp1 = rp0 + kCgSmemRows;
         float* sap = reinterpret_cast<float*>(rp1 + kCgSmemRows);
@@ -578,6 +593,280 @@ __global__ void __launch_bounds__(kCgcBlock) k_cg_cta(CgcArgs a) {
     CgcVec v = a.v;
     v.rebase();
     cg_unit_body<false>(a, v, (int)blockIdx.x);
+}
+
+// ---- device-loop CG: the depths too large for a cluster's shared memory -----------------
+// A depth whose cluster chunk does not fit shared memory (cg_fits_resident false) is solved
+// by a loop of whole-GPU kernels inside a CUDA-graph while node: per iteration one kernel
+// for p and A p (p.Ap), one for x and r (r.r), one for the true residual when it is due,
+// one for a refinement restart, and one single-thread kernel that continues the loop while
+// any depth of any cloud goes on.  The iteration, the decisions after each reduction and
+// the precision (exact products, float-pair sums in a thread and a warp, FP64 across warps
+// and blocks, in a fixed order) are the cluster solver's; the scalars live in a
+// CgLoopState per depth.  Every reduction ends in the last block to finish (a ticket
+// counter after a fence), which sums the blocks' partials in block order.  The loop ends
+// after at most max_iter iterations per depth; no kernel waits on another block.
+// Operator: the block-table gathers of the resident path (8 per row: each lane of a warp
+// loads its sibling group's 8 block entries, the group's 64 values go to a per-warp shared
+// block, the 27-point stencil reads them there), from global memory.
+constexpr int kLoopBlock = 256;
+constexpr int kLoopWarps = kLoopBlock / 32;
+
+struct CgLoopArgs {
+    CgcVec v;
+    CgLoopState* st;     // per depth
+    double* part;        // per depth: kLoopMaxBlocks partial sums
+    int first;           // unit z (blockIdx.z) solves depth first - z
+    int ctas[kMaxDepth + 1];   // CTAs of the cluster launch that owns each depth
+    unsigned loop_mask;
+    float tol2;
+    int max_iter;
+    int res_period;
+    __device__ void rebase() {
+        v.rebase();
+        PSR_CLOUD(st, part);
+    }
+};
+
+struct LoopUnit {
+    int d, row0, m;
+    CgLoopState* st;
+    double* part;
+};
+
+__device__ __forceinline__ LoopUnit loop_unit(const CgLoopArgs& a) {
+    LoopUnit u;
+    u.d = a.first - (int)blockIdx.z;
+    u.row0 = a.v.c->level_base[u.d];
+    u.m = a.v.c->level_count[u.d];
+    u.st = a.st + u.d;
+    u.part = a.part + (size_t)u.d * kLoopMaxBlocks;
+    return u;
+}
+
+// Sum of every thread's `v` over the unit's blocks (FP64).  Returns true in the block that
+// finishes the sum, with the sum in `w` of thread 0 (the ticket is back at zero).
+__device__ __forceinline__ bool loop_reduce(FF v, const LoopUnit& u, double& w) {
+    __shared__ double s_w[kLoopWarps];
+    __shared__ int s_last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    v = ff_warp_sum(v);
+    if (lane == 0) s_w[warp] = ff_to_double(v);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = 0.0;
+        for (int k = 0; k < kLoopWarps; ++k) b += s_w[k];
+        u.part[blockIdx.x] = b;
+        __threadfence();
+        s_last = atomicAdd(&u.st->ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!s_last) return false;
+    __threadfence();
+    if (warp == 0) {
+        double t = 0.0;
+        for (int k = lane; k < (int)gridDim.x; k += 32) t += __ldcg(&u.part[k]);
+        t = dbl_warp_sum(t);
+        if (lane == 0) {
+            w = t;
+            u.st->ticket = 0u;
+        }
+    }
+    return true;
+}
+
+// r0 = b, p_{-1} = 0 (buffer pa), x0 = 0 for the depths the loop solves; the others are
+// marked inactive.
+__global__ void __launch_bounds__(kLoopBlock) k_cgl_init(CgLoopArgs a) {
+    a.rebase();
+    const LoopUnit u = loop_unit(a);
+    const bool active = ((a.loop_mask >> u.d) & 1u) && !cg_fits_resident(u.d, u.m, a.ctas[u.d]);
+    if (!active) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            u.st->active = 0;
+            u.st->go = 0;
+            u.st->check = 0;
+            u.st->replace = 0;
+        }
+        return;
+    }
+    FF acc = ff_zero();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < u.m; i += gridDim.x * blockDim.x) {
+        const float bi = a.v.b[u.row0 + i];
+        a.v.r[u.row0 + i] = bi;
+        a.v.pa[u.row0 + i] = 0.0f;
+        a.v.x[u.row0 + i] = 0.0f;
+        acc = ff_add(acc, ff_prod(bi, bi));
+    }
+    double w = 0.0;
+    if (loop_reduce(acc, u, w) && threadIdx.x == 0) {
+        cg_start(*u.st, a, w);
+        u.st->active = 1;
+        u.st->it = 0;
+        u.st->t0 = global_ns();
+    }
+}
+
+// the group's 64 block values (one per lane and entry e) into the warp's shared block
+__device__ __forceinline__ const int4* loop_blk(const CgLoopArgs& a, const LoopUnit& u, int l, int sib) {
+    return reinterpret_cast<const int4*>(a.v.blk + (size_t)(((u.row0 - 1) >> 3) + (l >> 3)) * 64 + sib * 8);
+}
+
+// p_k = r + beta p_{k-1}, A p_k, p.Ap; iteration it = st->it + 1 takes p_{k-1} from pa
+// when it is odd, from pb when it is even, and writes p_k to the other buffer
+__global__ void __launch_bounds__(kLoopBlock) k_cgl_spmv(CgLoopArgs a) {
+    a.rebase();
+    const LoopUnit u = loop_unit(a);
+    if (!u.st->active || !u.st->go) return;
+    __shared__ float s_st[27];
+    __shared__ float sblk[kLoopWarps * kCgWarpBlockFloats];
+    const int it = u.st->it + 1;
+    const float beta = u.st->beta;
+    const float* pprev = (it & 1) ? a.v.pa : a.v.pb;
+    float* pcur = (it & 1) ? a.v.pb : a.v.pa;
+    if (threadIdx.x < 27) s_st[threadIdx.x] = a.v.stencil[u.d * 27 + threadIdx.x];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int gi = lane >> 3, sib = lane & 7;
+    const int spos = cg_spos(sib);
+    float* myblk = sblk + warp * kCgWarpBlockFloats + gi * 80 + ((0x1a081200 >> (gi * 8)) & 0xff);
+    const int nslot = (u.m + 31) >> 5;
+    FF acc = ff_zero();
+    for (int sl = blockIdx.x * kLoopWarps + warp; sl < nslot; sl += gridDim.x * kLoopWarps) {
+        const int l = sl * 32 + lane;
+        const bool mine = l < u.m;   // whole groups: a group is all in or all out
+        if (mine) {
+            const int4* bp = loop_blk(a, u, l, sib);
+            const int4 q0 = bp[0], q1 = bp[1];
+            const int ids[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
+            float vals[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) vals[e] = ids[e] >= 0 ? fmaf(beta, pprev[ids[e]], a.v.r[ids[e]]) : 0.0f;
+#pragma unroll
+            for (int e = 0; e < 8; ++e) myblk[e * 8 + sib] = vals[e];
+        }
+        __syncwarp();
+        if (mine) {
+            float y = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 27; ++k) y = fmaf(s_st[k], myblk[spos + cg_kpos(k)], y);
+            const float pi = myblk[spos + cg_kpos(13)];   // the row itself
+            pcur[u.row0 + l] = pi;
+            a.v.ap[u.row0 + l] = y;
+            acc = ff_add(acc, ff_prod(pi, y));
+        }
+        __syncwarp();
+    }
+    double w = 0.0;
+    if (loop_reduce(acc, u, w) && threadIdx.x == 0) {
+        u.st->pap = w;
+        u.st->alpha = cg_quot(u.st->rr, w);
+    }
+}
+
+// x = x + alpha p, r = r - alpha A p, r.r and the decisions after it
+__global__ void __launch_bounds__(kLoopBlock) k_cgl_update(CgLoopArgs a) {
+    a.rebase();
+    const LoopUnit u = loop_unit(a);
+    if (!u.st->active || !u.st->go) return;
+    const int it = u.st->it + 1;
+    const float alpha = u.st->alpha;
+    const float* pcur = (it & 1) ? a.v.pb : a.v.pa;
+    FF acc = ff_zero();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < u.m; i += gridDim.x * blockDim.x) {
+        const int row = u.row0 + i;
+        a.v.x[row] = fmaf(alpha, pcur[row], a.v.x[row]);
+        const float ri = fmaf(-alpha, a.v.ap[row], a.v.r[row]);
+        a.v.r[row] = ri;
+        acc = ff_add(acc, ff_prod(ri, ri));
+    }
+    double w = 0.0;
+    if (loop_reduce(acc, u, w) && threadIdx.x == 0) {
+        cg_after_rr(*u.st, a, w, it);
+        u.st->it = it;
+        a.v.cw->cg_iters[u.d] = it;
+    }
+}
+
+// True residual b - A x when due (exact products, float-pair sums), staged in the
+// direction buffer the next iteration overwrites, and the refinement decision.
+__global__ void __launch_bounds__(kLoopBlock) k_cgl_true(CgLoopArgs a) {
+    a.rebase();
+    const LoopUnit u = loop_unit(a);
+    if (!u.st->active || !u.st->check) return;
+    __shared__ float s_st[27];
+    __shared__ float sblk[kLoopWarps * kCgWarpBlockFloats];
+    const int next = u.st->it + 1;
+    float* stage = (next & 1) ? a.v.pb : a.v.pa;
+    if (threadIdx.x < 27) s_st[threadIdx.x] = a.v.stencil[u.d * 27 + threadIdx.x];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int gi = lane >> 3, sib = lane & 7;
+    const int spos = cg_spos(sib);
+    float* myblk = sblk + warp * kCgWarpBlockFloats + gi * 80 + ((0x1a081200 >> (gi * 8)) & 0xff);
+    const int nslot = (u.m + 31) >> 5;
+    FF acc = ff_zero();
+    for (int sl = blockIdx.x * kLoopWarps + warp; sl < nslot; sl += gridDim.x * kLoopWarps) {
+        const int l = sl * 32 + lane;
+        const bool mine = l < u.m;
+        if (mine) {
+            const int4* bp = loop_blk(a, u, l, sib);
+            const int4 q0 = bp[0], q1 = bp[1];
+            const int ids[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
+            float vals[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) vals[e] = ids[e] >= 0 ? a.v.x[ids[e]] : 0.0f;
+#pragma unroll
+            for (int e = 0; e < 8; ++e) myblk[e * 8 + sib] = vals[e];
+        }
+        __syncwarp();
+        if (mine) {
+            FF y = ff_zero();
+#pragma unroll
+            for (int k = 0; k < 27; ++k) y = ff_add(y, ff_prod(s_st[k], myblk[spos + cg_kpos(k)]));
+            const float ri = ff_to_float(ff_add(FF{a.v.b[u.row0 + l], 0.0f}, FF{-y.hi, -y.lo}));
+            stage[u.row0 + l] = ri;
+            acc = ff_add(acc, ff_prod(ri, ri));
+        }
+        __syncwarp();
+    }
+    double w = 0.0;
+    if (loop_reduce(acc, u, w) && threadIdx.x == 0) cg_after_true(*u.st, a, w, next);
+}
+
+// refinement restart: the CG continues from the true residual
+__global__ void __launch_bounds__(kLoopBlock) k_cgl_replace(CgLoopArgs a) {
+    a.rebase();
+    const LoopUnit u = loop_unit(a);
+    if (!u.st->active || !u.st->replace) return;
+    const float* stage = ((u.st->it + 1) & 1) ? a.v.pb : a.v.pa;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < u.m; i += gridDim.x * blockDim.x)
+        a.v.r[u.row0 + i] = stage[u.row0 + i];
+}
+
+// one thread: clears the restart flags and continues the loop while any depth of any cloud
+// goes on (the state of cloud k sits k * kCloudStride after cloud 0's)
+__global__ void k_cgl_control(CgLoopState* st, int first, int units, int clouds, cudaGraphConditionalHandle cond) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    unsigned more = 0u;
+    for (int k = 0; k < clouds; ++k) {
+        CgLoopState* sk = (CgLoopState*)((char*)st + (unsigned long long)k * kCloudStride);
+        for (int z = 0; z < units; ++z) {
+            CgLoopState& q = sk[first - z];
+            q.replace = 0;
+            if (q.active && q.go) more = 1u;
+        }
+    }
+    cudaGraphSetConditional(cond, more);
+}
+
+// after the loop: the per-depth results the cluster solver reports
+__global__ void k_cgl_finish(CgLoopArgs a) {
+    a.rebase();
+    const LoopUnit u = loop_unit(a);
+    if (threadIdx.x != 0 || !u.st->active) return;
+    if (u.st->it > 0) cg_report(a.v, u.d, *u.st);
+    a.v.cw->cg_depth_ns[u.d] = global_ns() - u.st->t0;
 }
 
 // ---- implicit function at the sample points and the iso-value ----------------------
@@ -757,6 +1046,55 @@ static cudaError_t launch_cg(void (*kernel)(CgcArgs), CgcArgs& a, int grid, int 
     return cudaLaunchKernelExC(&cfg, (const void*)kernel, args);
 }
 
+// The device loop of the depths in L.loop_mask (units first .. first - units + 1), issued
+// on ws.aux4 while that stream is being captured: the initialisation kernel, then a while
+// node added to the captured graph, whose body is captured on ws.loop_body, then the report
+// kernel.  The body runs once even when no depth needs it (the control kernel then ends
+// the loop), so one graph serves every cloud size.
+static cudaError_t launch_cg_loop(Workspace& ws, CgLoopArgs& L, int units) {
+    const int nbx = 2 * ws.num_sms < kLoopMaxBlocks ? 2 * ws.num_sms : kLoopMaxBlocks;   // fixed: sums in a fixed order
+    const dim3 grid(nbx, ws.batch, units);
+    cudaStream_t s = ws.aux4;
+    k_cgl_init<<<grid, kLoopBlock, 0, s>>>(L);
+    cudaError_t e = cudaGetLastError();
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaGraph_t graph = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    if (e == cudaSuccess) e = cudaStreamGetCaptureInfo(s, &cs, nullptr, &graph, &deps, nullptr, &ndeps);
+    if (e == cudaSuccess && cs != cudaStreamCaptureStatusActive) e = cudaErrorStreamCaptureUnsupported;
+    if (e != cudaSuccess) return e;
+    std::vector<cudaGraphNode_t> dep(deps, deps + ndeps);
+    cudaGraphConditionalHandle cond = 0;
+    e = cudaGraphConditionalHandleCreate(&cond, graph, 1, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) return e;
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = cond;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t loop = nullptr;
+    e = cudaGraphAddNode(&loop, graph, dep.data(), nullptr, dep.size(), &np);
+    if (e != cudaSuccess) return e;
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    cudaStream_t b = ws.loop_body;
+    e = cudaStreamBeginCaptureToGraph(b, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    k_cgl_spmv<<<grid, kLoopBlock, 0, b>>>(L);
+    k_cgl_update<<<grid, kLoopBlock, 0, b>>>(L);
+    k_cgl_true<<<grid, kLoopBlock, 0, b>>>(L);
+    k_cgl_replace<<<grid, kLoopBlock, 0, b>>>(L);
+    k_cgl_control<<<1, 32, 0, b>>>(L.st, L.first, units, ws.batch, cond);
+    cudaError_t el = cudaGetLastError();
+    cudaGraph_t captured = nullptr;
+    e = cudaStreamEndCapture(b, &captured);
+    if (e == cudaSuccess) e = el;
+    if (e == cudaSuccess) e = cudaStreamUpdateCaptureDependencies(s, &loop, nullptr, 1, cudaStreamSetCaptureDependencies);
+    if (e != cudaSuccess) return e;
+    k_cgl_finish<<<dim3(1, ws.batch, units), 32, 0, s>>>(L);
+    return cudaGetLastError();
+}
+
 cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, int cg_max_iter, int res_period) {
     cudaStream_t s = ws.stream;
     if (g_cg_cluster == 0) prepare_launch_configs(ws);
@@ -789,9 +1127,37 @@ cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, 
     // each, on the second stream.  All three run concurrently.
     const int ncl = D < 2 ? D : (D >= 5 ? 3 : 2);
     const int ncta = D - ncl + 1;
+    int cl1 = ws.cg_ctas > 0 ? ws.cg_ctas : g_cg_cluster;
+    if (cl1 > g_cg_cluster) cl1 = g_cg_cluster;
+    int cl2 = ws.cg_ctas_fine > 0 ? ws.cg_ctas_fine : 8;
+    if (cl2 > g_cg_cluster) cl2 = g_cg_cluster;
+    // Depths 5 .. D may outgrow their cluster's shared memory (depths up to 4 have at most
+    // 4,096 rows); in a captured graph those are solved by the device loop, which decides
+    // per run from the row counts.  Issued directly (no graph), they take the global-memory
+    // path of their cluster.
+    const int loop_units = (ws.ev_flags == cudaEventRecordExternal && D >= 5) ? D - 4 : 0;
+    a.loop_mask = 0u;
+    for (int z = 0; z < loop_units; ++z) a.loop_mask |= 1u << (D - z);
     e = cudaEventRecord(ws.ev_fork, s);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(ws.aux, ws.ev_fork, 0);
     if (e == cudaSuccess && ncl > 1) e = cudaStreamWaitEvent(ws.aux3, ws.ev_fork, 0);
+    if (e == cudaSuccess && loop_units > 0) {
+        e = cudaStreamWaitEvent(ws.aux4, ws.ev_fork, 0);
+        CgLoopArgs L;
+        L.v = a.v;
+        L.st = ws.cg_loop;
+        L.part = ws.cg_loop_part;
+        L.first = D;
+        for (int d = 0; d <= kMaxDepth; ++d) L.ctas[d] = (d == D) ? cl1 : (d >= D - ncl + 1 ? cl2 : 1);
+        L.loop_mask = a.loop_mask;
+        L.tol2 = a.tol2;
+        L.max_iter = a.max_iter;
+        L.res_period = a.res_period;
+        if (e == cudaSuccess) e = launch_cg_loop(ws, L, loop_units);
+        if (e == cudaSuccess) e = cudaEventRecord(ws.ev_join4, ws.aux4);
+        // the coarse sample values and the depth-D terms wait for every depth's solution
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(ws.aux, ws.ev_join4, 0);
+    }
     if (e == cudaSuccess && ncta > 0) {
         CgcArgs b = a;
         b.first = D - ncl;
@@ -807,8 +1173,6 @@ cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, 
         CgcArgs b = a;
         b.first = D - 1;
         set_stencils(b);
-        int cl2 = ws.cg_ctas_fine > 0 ? ws.cg_ctas_fine : 8;
-        if (cl2 > g_cg_cluster) cl2 = g_cg_cluster;
         e = launch_cg(k_cg_cluster, b, (ncl - 1) * cl2, cl2, ws.batch, ws.aux3);
         if (e == cudaSuccess) e = cudaEventRecord(ws.ev_join3, ws.aux3);
         if (e != cudaSuccess) return e;
@@ -830,8 +1194,6 @@ cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, 
     if (ncl > 0) {
         a.first = D;
         set_stencils(a);
-        int cl1 = ws.cg_ctas > 0 ? ws.cg_ctas : g_cg_cluster;
-        if (cl1 > g_cg_cluster) cl1 = g_cg_cluster;
         e = launch_cg(k_cg_cluster, a, cl1, cl1, ws.batch, s);
         if (e != cudaSuccess) return e;
     }

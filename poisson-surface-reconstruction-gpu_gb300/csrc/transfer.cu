@@ -222,7 +222,11 @@ __global__ void __launch_bounds__(kBlock) k_colour_near(Counters* c, int g, cons
         }
         if (lane == 0) {
             if (mi[3] != 0x7fffffff && md[3] < w * w) colour_blend(md, mi, cr, cg, cb, &out[3 * (size_t)v]);
-            else far[atomicAdd(&c->n_colour_far, 1)] = v;
+            else {   // (vertex, the 4th squared distance found here: an upper bound, 1e6 if none)
+                const int slot = atomicAdd(&c->n_colour_far, 1);
+                far[2 * (size_t)slot] = v;
+                far[2 * (size_t)slot + 1] = __float_as_int(mi[3] != 0x7fffffff ? md[3] : 1e6f);
+            }
         }
     }
 }
@@ -264,15 +268,17 @@ __device__ __forceinline__ void knn_merge4(float (&md)[4], int (&mi)[4], const f
 // Far pass, one warp per vertex of the far list: a branch-and-bound descent of the grid's
 // cell hierarchy.  The samples are Morton-sorted, so the samples of a cell at any level
 // g <= gmax form one contiguous range, read from the level-gmax table at codes shifted by
-// 3 (gmax - g); the children of cell m are cells 8m .. 8m + 7 one level finer.  From the
-// root, a node is scanned when it is a finest-level cell or holds at most kFarLeaf samples
-// (the lanes split its samples, each keeping a sorted 4-list, merged by warp-minimum rounds
-// into the warp's 4 nearest so far); otherwise its non-empty children are pushed onto a
-// per-warp stack nearest box first.  A node whose box is farther than the 4th nearest so
-// far (with 1e-4 relative slack) is skipped: a sample's float distance is at least its
-// cell box's (the sample lies in the closed box and rounding is monotone).  So the result
-// is the exact 4 nearest under the (distance, index) order, whatever the distance.  The
-// stack holds at most 7 siblings per level plus 8 children: 7 gmax + 9 entries.
+// 3 (gmax - g); the children of cell m are cells 8m .. 8m + 7 one level finer.  Expanding
+// a node, the lanes 0..7 take its children: a child that is a finest-level cell or holds
+// at most kFarLeaf samples is scanned at once, together with its leaf siblings (their
+// samples flattened over the lanes, each lane keeping a sorted 4-list, merged by
+// warp-minimum rounds into the warp's 4 nearest so far); the other non-empty children are
+// pushed onto a per-warp stack, nearest box first.  A node whose box is farther than the
+// bound (the 4th nearest so far, or the near pass's 4th distance when smaller, with 1e-4
+// relative slack) is skipped: a sample's float distance is at least its cell box's (the
+// sample lies in the closed box and rounding is monotone).  So the result is the exact 4
+// nearest under the (distance, index) order, whatever the distance.  The stack holds at
+// most 7 siblings per level plus 8 children: 7 gmax + 9 entries.
 constexpr int kFarWarps = kBlock / 32;
 constexpr int kFarLeaf = 32;
 constexpr int kFarStack = 64;
@@ -285,16 +291,22 @@ __global__ void __launch_bounds__(kBlock) k_colour_far(const Counters* c, int gm
     PSR_CLOUD(c, mv, px, py, pz, cr, cg, cb, cell_start, far, out);
     __shared__ int s_node[kFarWarps][kFarStack];    // (level << 24) | cell code
     __shared__ float s_dist[kFarWarps][kFarStack];  // squared distance to the cell's box
+    __shared__ int s_loff[kFarWarps][9];            // leaf children scanned together: offsets
+    __shared__ int s_lbase[kFarWarps][8];           //   in the flattened range, first samples
     const int nfar = c->n_colour_far;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     int* stk = s_node[wib];
     float* sdist = s_dist[wib];
+    int* loff = s_loff[wib];
+    int* lbase = s_lbase[wib];
     for (int t = gw; t < nfar; t += nw) {
-        const int v = far[t];
+        const int v = far[2 * (size_t)t];
+        const float bound = __int_as_float(far[2 * (size_t)t + 1]);
         const float qx = mv[3 * (size_t)v], qy = mv[3 * (size_t)v + 1], qz = mv[3 * (size_t)v + 2];
-        // the warp's 4 nearest so far, the same in every lane
+        // the warp's 4 nearest so far, the same in every lane (1e6: a slot not yet filled;
+        // every squared distance in the unit cube is below 3)
         float md[4] = {1e6f, 1e6f, 1e6f, 1e6f};
         int mi[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
         if (lane == 0) {
@@ -308,52 +320,87 @@ __global__ void __launch_bounds__(kBlock) k_colour_far(const Counters* c, int gm
             const int node = stk[top];
             const float nd = sdist[top];
             __syncwarp();   // every lane has read the entry before the slot is reused
-            if (mi[3] != 0x7fffffff && nd > md[3] * 1.0001f) continue;
+            const float lim = fminf(bound, md[3]) * 1.0001f;
+            if (nd > lim) continue;
             const int g = node >> 24;
             const unsigned m = (unsigned)node & 0xffffffu;
-            const int shift = 3 * (gmax - g);
-            const int s0 = cell_start[(size_t)m << shift], s1 = cell_start[(size_t)(m + 1) << shift];
-            if (g == gmax || s1 - s0 <= kFarLeaf) {
-                float bd[4] = {1e6f, 1e6f, 1e6f, 1e6f};
-                int bi[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
-                for (int j = s0 + lane; j < s1; j += 32) knn_visit(qx, qy, qz, px, py, pz, j, bd, bi);
-                float ld[4];
-                int li[4];
-                knn_warp_merge(bd, bi, ld, li);
-                knn_merge4(md, mi, ld, li);
-                continue;
+            if (g == 0) {   // a small cloud: the root itself is a leaf
+                const int s1 = cell_start[(size_t)1 << (3 * gmax)];
+                if (s1 <= kFarLeaf) {
+                    float bd[4] = {1e6f, 1e6f, 1e6f, 1e6f};
+                    int bi[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
+                    for (int j = lane; j < s1; j += 32) knn_visit(qx, qy, qz, px, py, pz, j, bd, bi);
+                    float ld[4];
+                    int li[4];
+                    knn_warp_merge(bd, bi, ld, li);
+                    knn_merge4(md, mi, ld, li);
+                    continue;
+                }
             }
-            // lanes 0..7: child (g + 1, 8 m + lane), its sample count and box distance
+            // lanes 0..7: child (g + 1, 8 m + lane), its samples and box distance
             const int gc = g + 1;
             const unsigned child = (m << 3) | (unsigned)(lane & 7);
             const int cshift = 3 * (gmax - gc);
-            bool keep = false;
+            bool keep = false, leaf = false;
             float d2 = 0.0f;
+            int n0 = 0, cnt = 0;
             if (lane < 8) {
-                const int n0 = cell_start[(size_t)child << cshift], n1 = cell_start[(size_t)(child + 1) << cshift];
+                n0 = cell_start[(size_t)child << cshift];
+                cnt = cell_start[(size_t)(child + 1) << cshift] - n0;
                 const float w = 1.0f / (float)(1 << gc);
                 const int a = (int)compact3(child >> 2), b = (int)compact3(child >> 1), z = (int)compact3(child);
                 const float gx = fmaxf(fmaxf(__fsub_rn(a * w, qx), __fsub_rn(qx, (a + 1) * w)), 0.0f);
                 const float gy = fmaxf(fmaxf(__fsub_rn(b * w, qy), __fsub_rn(qy, (b + 1) * w)), 0.0f);
                 const float gz = fmaxf(fmaxf(__fsub_rn(z * w, qz), __fsub_rn(qz, (z + 1) * w)), 0.0f);
                 d2 = __fadd_rn(__fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy)), __fmul_rn(gz, gz));
-                keep = n1 > n0 && !(mi[3] != 0x7fffffff && d2 > md[3] * 1.0001f);
+                keep = cnt > 0 && !(d2 > lim);
+                leaf = gc == gmax || cnt <= kFarLeaf;
             }
-            const unsigned kept = __ballot_sync(0xffffffffu, keep);
-            // rank among the kept children, nearest first (ties: lower child); pushed in
+            if (__any_sync(0xffffffffu, keep && leaf)) {
+                // the kept leaf children's samples, flattened over the lanes
+                const int lc = (keep && leaf) ? cnt : 0;
+                int incl = lc;
+#pragma unroll
+                for (int o = 1; o < 8; o <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += y;
+                }
+                if (lane < 8) {
+                    loff[lane] = incl - lc;
+                    lbase[lane] = n0;
+                }
+                const int total = __shfl_sync(0xffffffffu, incl, 7);
+                if (lane == 0) loff[8] = total;
+                __syncwarp();
+                float bd[4] = {1e6f, 1e6f, 1e6f, 1e6f};
+                int bi[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
+                int k = 0;
+                for (int f = lane; f < total; f += 32) {
+                    while (loff[k + 1] <= f) ++k;   // flattened index -> child (increasing)
+                    knn_visit(qx, qy, qz, px, py, pz, lbase[k] + (f - loff[k]), bd, bi);
+                }
+                float ld[4];
+                int li[4];
+                knn_warp_merge(bd, bi, ld, li);
+                knn_merge4(md, mi, ld, li);
+                __syncwarp();   // the offsets are read before the next expansion rewrites them
+            }
+            // the kept inner children: rank by box distance (ties: lower child), pushed in
             // reverse so the nearest is popped next
+            const bool push = keep && !leaf;
+            const unsigned pm = __ballot_sync(0xffffffffu, push);
             int rank = 0;
 #pragma unroll
             for (int o = 0; o < 8; ++o) {
                 const float od = __shfl_sync(0xffffffffu, d2, o);
-                if (((kept >> o) & 1u) && (od < d2 || (od == d2 && o < lane))) ++rank;
+                if (((pm >> o) & 1u) && (od < d2 || (od == d2 && o < lane))) ++rank;
             }
-            const int nk = __popc(kept);
-            if (keep) {
-                stk[top + nk - 1 - rank] = (gc << 24) | (int)child;
-                sdist[top + nk - 1 - rank] = d2;
+            const int np = __popc(pm);
+            if (push) {
+                stk[top + np - 1 - rank] = (gc << 24) | (int)child;
+                sdist[top + np - 1 - rank] = d2;
             }
-            top += nk;
+            top += np;
             __syncwarp();
         }
         if (lane == 0) colour_blend(md, mi, cr, cg, cb, &out[3 * (size_t)v]);
@@ -449,7 +496,7 @@ cudaError_t transfer_build(Workspace& ws, int with_colour, int with_normals) {
         int* cell_start = ws.cell_start;   // (1 << 3g) + 1 entries, from transfer_prepare
         k_colour_near<<<PSR_GRID(ws, grid), kBlock, 0, s>>>(ws.cnt, g, ws.mesh_v, ws.px, ws.py, ws.pz, ws.cr, ws.cg, ws.cb,
                                               cell_start, ws.colour_far, ws.mesh_c);
-        k_colour_far<<<PSR_GRID(ws, ws.num_sms * 4), kBlock, 0, s>>>(ws.cnt, g, ws.mesh_v, ws.px, ws.py, ws.pz, ws.cr,
+        k_colour_far<<<PSR_GRID(ws, ws.num_sms * 8), kBlock, 0, s>>>(ws.cnt, g, ws.mesh_v, ws.px, ws.py, ws.pz, ws.cr,
                                                                    ws.cg, ws.cb, cell_start, ws.colour_far, ws.mesh_c);
     }
     if (with_normals) {

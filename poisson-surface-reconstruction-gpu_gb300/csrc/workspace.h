@@ -104,6 +104,8 @@ struct Workspace {
     unsigned ev_flags = 0;         // flags of the stage-timing event records (external in a capture)
     float *cg_r, *cg_p, *cg_q, *cg_ap;   // residual, two direction buffers, A p
     int* cg_blk;            // CG block table: 64 same-depth nodes per sibling group
+    CgLoopState* cg_loop;   // [D+1]: device-loop CG state per depth
+    double* cg_loop_part;   // [D+1][kLoopMaxBlocks]: its per-block partial sums
     double* cg_partial;     // scratch: divergence chunk sums (float pairs, 8 bytes each)
     float* point_val;       // N
     float* pv_coef;         // [27][cap.dnodes / 8 + 64]: per depth-(D-1) node, Bernstein coefficients
@@ -157,7 +159,7 @@ struct Workspace {
     double* nacc;           // per output vertex normal accumulator (3 doubles)
     int* vcount;            // per output vertex triangle count
     int* cell_start;        // sample grid for the colour search
-    int* colour_far;        // mesh vertices left to the wide colour search
+    int* colour_far;        // mesh vertices left to the wide colour search, with bounds
     // vertex welding (allocated only when the handle welds)
     int* weld_table = nullptr;   // hash slots: a vertex of the class, then its smallest index
     unsigned weld_mask = 0;      // slots - 1 (a power of two >= 2 x mesh vertex capacity)
@@ -179,6 +181,9 @@ struct Workspace {
     cudaEvent_t ev_fork2 = nullptr, ev_join2 = nullptr;
     cudaStream_t aux3 = nullptr;        // fourth stream: the CG of depths D-1 and D-2
     cudaEvent_t ev_join3 = nullptr;
+    cudaStream_t aux4 = nullptr;        // fifth stream: the device-loop CG of large depths
+    cudaEvent_t ev_join4 = nullptr;
+    cudaStream_t loop_body = nullptr;   // captures the body graph of the device loop
     int num_sms;
 };
 
