@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=15.0,
                     help="open-loop duration of the serving-loop leg (Poisson arrivals, mixed sizes and depths)")
     ap.add_argument("--no-serve-mix", action="store_true", help="skip the serving-loop leg")
+    ap.add_argument("--no-mix-batch", action="store_true", help="skip the 256-cloud multi-cloud mix leg")
+    ap.add_argument("--no-large", action="store_true", help="skip the 2M-point depth-9 leg")
     return ap.parse_args()
 
 
@@ -431,6 +433,16 @@ def main():
             line["serve_mix"] = serve_mix_leg(psr, serve_mod, syn, torch, dev, args.serve_seconds)
         except Exception as e:
             line["serve_mix"] = {"error": str(e)}
+    if not args.no_mix_batch:
+        try:
+            line["mix_batch"] = mix_batch_leg(psr, syn, torch, dev)
+        except Exception as e:
+            line["mix_batch"] = {"error": str(e)}
+    if not args.no_large:
+        try:
+            line["large"] = large_leg(psr, syn, torch, dev)
+        except Exception as e:
+            line["large"] = {"error": str(e)}
     if not args.no_cpu_baseline:
         try:
             line["cpu_baseline"] = cpu_baseline(xyz, nrm, rgb, depth)
@@ -557,6 +569,124 @@ def batch_leg(psr, caps, clouds, steps, torch, dev, K):
         return {"clouds_per_launch": K, "value": K * steps / (ms / 1000.0), "unit": UNIT,
                 "ms_per_pass": ms / steps, "kernel_launches_per_pass": int(st[0][1].kernel_launches),
                 "stage_ms": [round(float(v), 4) for v in st[0][1].stage_ms],
+                "memory_gb": round(r.memory_bytes() / 1e9, 2)}
+
+
+def mix_batch_leg(psr, syn, torch, dev, n_clouds=256, per_pass=16):
+    """The multi-cloud mix: 256 seeded clouds (point counts log-uniform in [5k, 150k];
+    spheres, tori and superquadrics randomly scaled and rotated; no colour; depth drawn from
+    6, 7, 8), grouped by depth into multi-cloud passes of up to `per_pass` clouds
+    (psr_submit_batch: one launch of each kernel per pass), against the plain path (one
+    handle, one psr_reconstruct per cloud) on the same clouds and capacities.  Inputs and
+    outputs device-resident; each form timed over one whole pass of the 256 clouds after an
+    untimed one (host clock, the device synchronised at both ends)."""
+    clouds = []
+    for i in range(n_clouds):
+        p, nr, _, d = syn.workload("mix", cloud=i)
+        clouds.append((torch.from_numpy(p).to(dev), torch.from_numpy(nr).to(dev), d))
+    caps = dict(max_points=150000, max_depth=8, max_triangles=1500000, max_mesh_vertices=800000,
+                max_subdivision_nodes=4000000, compute_colors=False, compute_normals=True)
+    vcap, tcap = caps["max_mesh_vertices"], caps["max_triangles"]
+    outs = [[torch.empty((vcap, 3), dtype=torch.float32, device=dev), torch.empty((tcap, 3), dtype=torch.int32, device=dev),
+             torch.empty((vcap, 3), dtype=torch.float32, device=dev)] for _ in range(per_pass)]
+    def mesh_of(k):
+        o = outs[k]
+        return psr.PsrMesh(o[0].data_ptr(), o[1].data_ptr(), None, o[2].data_ptr(), vcap, tcap, psr.PSR_DEVICE, 0, 0)
+    depths = sorted({c[2] for c in clouds})
+    groups = [[c for c in clouds if c[2] == d] for d in depths]
+    stream = torch.cuda.current_stream(dev)
+    out = {"clouds": n_clouds, "clouds_per_depth": {str(d): len(g) for d, g in zip(depths, groups)},
+           "clouds_per_pass": per_pass}
+    with psr.PoissonReconstruction(batch_clouds=per_pass, concurrent_stages=False, **caps) as r:
+        def run_all():
+            ok = 0
+            for g in groups:
+                for s0 in range(0, len(g), per_pass):
+                    part = g[s0:s0 + per_pass]
+                    pts, meshes = (psr.PsrPoints * len(part))(), (psr.PsrMesh * len(part))()
+                    for k, (x, nrm, _) in enumerate(part):
+                        pts[k] = psr.PsrPoints(x.data_ptr(), nrm.data_ptr(), None, x.shape[0], psr.PSR_DEVICE)
+                        meshes[k] = mesh_of(k)
+                    r.submit_batch_device(pts, meshes, depth=part[0][2], stream=stream.cuda_stream)
+                    try:
+                        r.wait()
+                    except psr.PsrError:
+                        pass
+                    for k in range(len(part)):
+                        stk = r.batch_result(k)[0]
+                        ok += stk == psr.PSR_OK
+                        if stk != psr.PSR_OK:
+                            name = psr.load_library().psr_status_string(stk).decode()
+                            failed[name] = failed.get(name, 0) + 1
+            return ok
+        failed = {}
+        run_all()   # graph capture of every (clouds, depth) shape
+        torch.cuda.synchronize(dev)
+        failed.clear()
+        t = time.perf_counter()
+        ok = run_all()
+        torch.cuda.synchronize(dev)
+        dt = time.perf_counter() - t
+        out.update(batched={"recons_per_s": ok / dt, "completed": ok, "seconds": dt, "failed": failed,
+                            "memory_gb": round(r.memory_bytes() / 1e9, 2)},
+                   failed_note="clouds the reference's algorithm cannot mesh at their depth (it reads unset "
+                               "vertex records: sparse clouds at depth 8) are rejected as invalid input by both "
+                               "forms")
+    with psr.PoissonReconstruction(**caps) as r:
+        def one(c):
+            try:
+                r.reconstruct_device(c[0].data_ptr(), c[1].data_ptr(), None, c[0].shape[0], depth=c[2], out=mesh_of(0))
+                return 1
+            except psr.PsrError:
+                return 0
+        for g in groups:
+            one(g[0])
+        torch.cuda.synchronize(dev)
+        t = time.perf_counter()
+        ok = sum(one(c) for c in clouds)
+        torch.cuda.synchronize(dev)
+        dt = time.perf_counter() - t
+        out["plain"] = {"recons_per_s": ok / dt, "completed": ok, "seconds": dt}
+    out["batched_vs_plain"] = out["batched"]["recons_per_s"] / out["plain"]["recons_per_s"]
+    return out
+
+
+def large_leg(psr, syn, torch, dev, reps=3):
+    """The precision-study cloud as a throughput case: 2,000,000 points on the superquadric
+    (sinusoidal displacement, jittered normals), depth 9, every Laplacian entry kept, one
+    cloud per call, inputs and outputs device-resident; median of `reps` timed calls after a
+    warm one (CUDA events on the calling stream)."""
+    p, nr, _, d = syn.workload("superquadric2m")
+    caps = dict(max_depth=9, max_points=p.shape[0], max_triangles=12000000, max_mesh_vertices=6000000,
+                max_subdivision_nodes=8000000, compute_colors=False, compute_normals=True, laplacian_epsilon=0.0)
+    x, n = torch.from_numpy(p).to(dev), torch.from_numpy(nr).to(dev)
+    vcap, tcap = caps["max_mesh_vertices"], caps["max_triangles"]
+    o = [torch.empty((vcap, 3), dtype=torch.float32, device=dev), torch.empty((tcap, 3), dtype=torch.int32, device=dev),
+         torch.empty((vcap, 3), dtype=torch.float32, device=dev)]
+    stream = torch.cuda.current_stream(dev)
+    with psr.PoissonReconstruction(**caps) as r:
+        def one():
+            m = psr.PsrMesh(o[0].data_ptr(), o[1].data_ptr(), None, o[2].data_ptr(), vcap, tcap, psr.PSR_DEVICE, 0, 0)
+            r.reconstruct_device(x.data_ptr(), n.data_ptr(), None, x.shape[0], depth=d, out=m, stream=stream.cuda_stream)
+            return m
+        one()
+        times = []
+        for _ in range(reps):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            m = one()
+            b.record(stream)
+            b.synchronize()
+            times.append(a.elapsed_time(b))
+        st = r.stats()
+        ms = float(np.median(times))
+        return {"workload": "superquadric2m (N=2,000,000, depth 9, normals, laplacian_epsilon 0)", "ms": ms,
+                "recons_per_s": 1000.0 / ms, "points_per_s": p.shape[0] / (ms / 1000.0),
+                "stage_ms": [round(float(v), 3) for v in st.stage_ms],
+                "cg_depth_ms": [round(float(v), 3) for v in st.cg_depth_ms[:d + 1]],
+                "cg_iterations": list(st.cg_iterations[:d + 1]), "nodes": int(st.nodes),
+                "mesh": {"vertices": int(m.vertex_count), "triangles": int(m.triangle_count)},
                 "memory_gb": round(r.memory_bytes() / 1e9, 2)}
 
 

@@ -344,6 +344,7 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     A.add(ws.cg_blk, (size_t)nodes * 8 + 64);
     A.add(ws.cg_loop, (size_t)kMaxDepth + 1);
     A.add(ws.cg_loop_part, (size_t)(kMaxDepth + 1) * kLoopMaxBlocks);
+    A.add(ws.cg_loop_ctl, (size_t)kLoopControlWords);
     A.add(ws.cg_partial, std::max((size_t)nodes, (size_t)4096 * (kMaxDepth + 1)));
     A.add(ws.point_val, (size_t)N);
     A.add(ws.pv_coef, 27 * ((size_t)dnodes / 8 + 64));

@@ -68,8 +68,9 @@ struct CgLoopState {
     int it;                  // iterations done
     unsigned ticket;         // blocks of the current kernel done (last-block reductions)
     unsigned long long t0;   // global timer at the start of the solve
+    unsigned long long t1;   // global timer at the end of its last step
 };
-constexpr int kLoopMaxBlocks = 1024;   // blocks along x of a device-loop kernel (partials)
+constexpr int kLoopMaxBlocks = 2048;   // virtual blocks of one depth of the device loop (partials)
 
 // Look-up tables shared by the kernels (values derived in tables.cpp).
 struct ConstTables {
@@ -94,6 +95,9 @@ struct ConstTables {
 // workspace address are its slot.
 constexpr unsigned long long kCloudStride = 1ull << 35;   // 32 GiB of address space per cloud
 constexpr int kMaxBatchClouds = 64;
+// words of the device loop's control block (pass and unit counts, the unit list, its
+// virtual-block offsets)
+constexpr int kLoopControlWords = 3 + 2 * kMaxBatchClouds * (kMaxDepth + 1);
 
 // blocks along x of a launch over `clouds` clouds whose one-cloud launch has gx blocks:
 // about twice the one-cloud grid in total (each cloud's blocks stride over its work), at

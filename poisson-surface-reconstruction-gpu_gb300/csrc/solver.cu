@@ -112,6 +112,12 @@ struct CgcVec {
     __device__ void rebase() { PSR_CLOUD(c, cw, neigh, blk, stencil, b, x, r, pa, pb, ap); }
 };
 
+// a workspace pointer of cloud 0 moved to cloud k (null stays null)
+template <class T>
+__device__ __forceinline__ T* at_cloud(T* p, int k) {
+    return p ? (T*)((const char*)p + (unsigned long long)k * kCloudStride) : p;
+}
+
 struct CgcArgs {
     CgcVec v;
     int depth;
@@ -597,56 +603,97 @@ __global__ void __launch_bounds__(kCgcBlock) k_cg_cta(CgcArgs a) {
 
 // ---- device-loop CG: the depths too large for a cluster's shared memory -----------------
 // A depth whose cluster chunk does not fit shared memory (cg_fits_resident false) is solved
-// by a loop of whole-GPU kernels inside a CUDA-graph while node: per iteration one kernel
-// for p and A p (p.Ap), one for x and r (r.r), one for the true residual when it is due,
-// one for a refinement restart, and one single-thread kernel that continues the loop while
-// any depth of any cloud goes on.  The iteration, the decisions after each reduction and
-// the precision (exact products, float-pair sums in a thread and a warp, FP64 across warps
-// and blocks, in a fixed order) are the cluster solver's; the scalars live in a
-// CgLoopState per depth.  Every reduction ends in the last block to finish (a ticket
-// counter after a fence), which sums the blocks' partials in block order.  The loop ends
-// after at most max_iter iterations per depth; no kernel waits on another block.
+// by a loop of whole-GPU kernels inside a CUDA-graph while node.  Body, per pass: twice the
+// true residual when it is due (k_cgl_true), p and A p with p.Ap (k_cgl_spmv), x and r with
+// r.r (k_cgl_update); then one thread lists the (depth, cloud) units that go on and ends
+// the loop when none does (k_cgl_control).  The iteration, the decisions after each
+// reduction and the precision (exact products, float-pair sums in a thread and a warp, FP64
+// across warps and blocks, in a fixed order) are the cluster solver's; the scalars live in
+// a CgLoopState per depth.  Each unit's work is split over virtual blocks, one per
+// kLoopRowsPerSplit rows, which the launch's blocks take in turn over the listed units, so
+// the sums keep one order whatever the number of clouds, and units that are done cost
+// nothing.  Every reduction
+// ends in the last virtual block to finish (a ticket counter after a fence), which sums the
+// virtual blocks' partials in order; every virtual block has read the state before it
+// takes its ticket, so the last one may clear a flag the kernel acted on.  The loop ends
+// after at most max_iter iterations per depth; no block waits on another.
 // Operator: the block-table gathers of the resident path (8 per row: each lane of a warp
 // loads its sibling group's 8 block entries, the group's 64 values go to a per-warp shared
 // block, the 27-point stencil reads them there), from global memory.
 constexpr int kLoopBlock = 256;
 constexpr int kLoopWarps = kLoopBlock / 32;
+constexpr int kLoopUnroll = 2;   // CG iterations per pass of the while node's body
+static_assert(kLoopMaxBlocks >= 1, "partials per unit");
 
 struct CgLoopArgs {
-    CgcVec v;
-    CgLoopState* st;     // per depth
-    double* part;        // per depth: kLoopMaxBlocks partial sums
-    int first;           // unit z (blockIdx.z) solves depth first - z
+    CgcVec v;            // cloud 0's workspace
+    CgLoopState* st;     // per depth (cloud 0)
+    double* part;        // per depth: kLoopMaxBlocks partial sums (cloud 0)
+    unsigned* ctl;       // CgLoopControl (cloud 0 only)
+    int first;           // unit z solves depth first - z
+    int units, clouds;
     int ctas[kMaxDepth + 1];   // CTAs of the cluster launch that owns each depth
     unsigned loop_mask;
     float tol2;
     int max_iter;
     int res_period;
-    __device__ void rebase() {
-        v.rebase();
-        PSR_CLOUD(st, part);
-    }
 };
 
+// Loop control of a launch: body passes run so far, the units (cloud << 8 | z) the next
+// pass works on, and the first virtual block of each (vstart[count]: their total).
+struct CgLoopControl {
+    unsigned passes;
+    unsigned count;
+    unsigned list[kMaxBatchClouds * (kMaxDepth + 1)];
+    unsigned vstart[kMaxBatchClouds * (kMaxDepth + 1) + 1];
+};
+static_assert(sizeof(CgLoopControl) == sizeof(unsigned) * kLoopControlWords, "control block words");
+constexpr int kLoopRowsPerSplit = 1024;   // rows per virtual block (below 2M rows)
+
+// virtual blocks of a unit of m rows: one per kLoopRowsPerSplit rows, at most
+// kLoopMaxBlocks (the sums' order depends on m alone)
+__device__ __forceinline__ unsigned loop_split(int m) {
+    const int v = (m + kLoopRowsPerSplit - 1) / kLoopRowsPerSplit;
+    return (unsigned)(v < 1 ? 1 : (v > kLoopMaxBlocks ? kLoopMaxBlocks : v));
+}
+
 struct LoopUnit {
-    int d, row0, m;
+    int d, row0, m, bx, split;
+    CgcVec v;
     CgLoopState* st;
     double* part;
 };
 
-__device__ __forceinline__ LoopUnit loop_unit(const CgLoopArgs& a) {
+// virtual block vb of the listed units: its unit (cloud's workspace) and index in the unit
+__device__ __forceinline__ LoopUnit loop_unit(const CgLoopArgs& a, const CgLoopControl* ctl, int vb) {
+    int lo = 0, hi = (int)ctl->count - 1;   // the unit i with vstart[i] <= vb < vstart[i + 1]
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if ((int)ctl->vstart[mid] <= vb) lo = mid;
+        else hi = mid - 1;
+    }
+    const unsigned e = ctl->list[lo];
+    const int k = (int)(e >> 8), z = (int)(e & 255u);
     LoopUnit u;
-    u.d = a.first - (int)blockIdx.z;
-    u.row0 = a.v.c->level_base[u.d];
-    u.m = a.v.c->level_count[u.d];
-    u.st = a.st + u.d;
-    u.part = a.part + (size_t)u.d * kLoopMaxBlocks;
+    u.bx = vb - (int)ctl->vstart[lo];
+    u.split = (int)(ctl->vstart[lo + 1] - ctl->vstart[lo]);
+    u.d = a.first - z;
+    u.v = a.v;
+    u.v.c = at_cloud(a.v.c, k); u.v.cw = at_cloud(a.v.cw, k); u.v.neigh = at_cloud(a.v.neigh, k);
+    u.v.blk = at_cloud(a.v.blk, k); u.v.stencil = at_cloud(a.v.stencil, k); u.v.b = at_cloud(a.v.b, k);
+    u.v.x = at_cloud(a.v.x, k); u.v.r = at_cloud(a.v.r, k); u.v.pa = at_cloud(a.v.pa, k);
+    u.v.pb = at_cloud(a.v.pb, k); u.v.ap = at_cloud(a.v.ap, k);
+    u.row0 = u.v.c->level_base[u.d];
+    u.m = u.v.c->level_count[u.d];
+    u.st = at_cloud(a.st, k) + u.d;
+    u.part = at_cloud(a.part, k) + (size_t)u.d * kLoopMaxBlocks;
     return u;
 }
 
-// Sum of every thread's `v` over the unit's blocks (FP64).  Returns true in the block that
-// finishes the sum, with the sum in `w` of thread 0 (the ticket is back at zero).
+// Sum of every thread's `v` over the unit's virtual blocks (FP64).  Returns true in the
+// block that finishes the sum, with the sum in `w` of thread 0 (the ticket is back at zero).
 __device__ __forceinline__ bool loop_reduce(FF v, const LoopUnit& u, double& w) {
+    const int split = u.split;
     __shared__ double s_w[kLoopWarps];
     __shared__ int s_last;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -656,217 +703,269 @@ __device__ __forceinline__ bool loop_reduce(FF v, const LoopUnit& u, double& w) 
     if (threadIdx.x == 0) {
         double b = 0.0;
         for (int k = 0; k < kLoopWarps; ++k) b += s_w[k];
-        u.part[blockIdx.x] = b;
+        u.part[u.bx] = b;
         __threadfence();
-        s_last = atomicAdd(&u.st->ticket, 1u) == gridDim.x - 1;
+        s_last = atomicAdd(&u.st->ticket, 1u) == (unsigned)split - 1;
     }
     __syncthreads();
-    if (!s_last) return false;
-    __threadfence();
-    if (warp == 0) {
-        double t = 0.0;
-        for (int k = lane; k < (int)gridDim.x; k += 32) t += __ldcg(&u.part[k]);
-        t = dbl_warp_sum(t);
-        if (lane == 0) {
-            w = t;
-            u.st->ticket = 0u;
+    const bool last = s_last;
+    if (last) {
+        __threadfence();
+        if (warp == 0) {
+            double t = 0.0;
+            for (int k = lane; k < split; k += 32) t += __ldcg(&u.part[k]);
+            t = dbl_warp_sum(t);
+            if (lane == 0) {
+                w = t;
+                u.st->ticket = 0u;
+            }
         }
     }
-    return true;
+    __syncthreads();   // s_w and s_last are reused by the next virtual block
+    return last;
 }
 
-// r0 = b, p_{-1} = 0 (buffer pa), x0 = 0 for the depths the loop solves; the others are
-// marked inactive.
+// One thread, before the loop: which depths of which clouds the loop solves (the others
+// are marked inactive), listed for the first pass.
+__global__ void k_cgl_plan(CgLoopArgs a) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    CgLoopControl* ctl = reinterpret_cast<CgLoopControl*>(a.ctl);
+    unsigned n = 0;
+    ctl->vstart[0] = 0u;
+    for (int k = 0; k < a.clouds; ++k) {
+        const Counters* c = at_cloud(a.v.c, k);
+        CgLoopState* st = at_cloud(a.st, k);
+        for (int z = 0; z < a.units; ++z) {
+            const int d = a.first - z;
+            const bool active = ((a.loop_mask >> d) & 1u) && !cg_fits_resident(d, c->level_count[d], a.ctas[d]);
+            st[d].active = active;
+            st[d].go = 0;
+            st[d].check = 0;
+            st[d].replace = 0;
+            st[d].it = 0;
+            if (active) {
+                ctl->list[n] = ((unsigned)k << 8) | (unsigned)z;
+                ctl->vstart[n + 1] = ctl->vstart[n] + loop_split(c->level_count[d]);
+                ++n;
+            }
+        }
+    }
+    ctl->count = n;
+    ctl->passes = 0u;
+}
+
+// r0 = b, p_{-1} = 0 (buffer pa), x0 = 0 for the listed depths
 __global__ void __launch_bounds__(kLoopBlock) k_cgl_init(CgLoopArgs a) {
-    a.rebase();
-    const LoopUnit u = loop_unit(a);
-    const bool active = ((a.loop_mask >> u.d) & 1u) && !cg_fits_resident(u.d, u.m, a.ctas[u.d]);
-    if (!active) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            u.st->active = 0;
-            u.st->go = 0;
-            u.st->check = 0;
-            u.st->replace = 0;
+    const CgLoopControl* ctl = reinterpret_cast<const CgLoopControl*>(a.ctl);
+    const int nv = (int)ctl->vstart[ctl->count];
+    for (int vb = blockIdx.x; vb < nv; vb += gridDim.x) {
+        const LoopUnit u = loop_unit(a, ctl, vb);
+        FF acc = ff_zero();
+        for (int i = u.bx * kLoopBlock + threadIdx.x; i < u.m; i += u.split * kLoopBlock) {
+            const float bi = u.v.b[u.row0 + i];
+            u.v.r[u.row0 + i] = bi;
+            u.v.pa[u.row0 + i] = 0.0f;
+            u.v.x[u.row0 + i] = 0.0f;
+            acc = ff_add(acc, ff_prod(bi, bi));
         }
-        return;
-    }
-    FF acc = ff_zero();
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < u.m; i += gridDim.x * blockDim.x) {
-        const float bi = a.v.b[u.row0 + i];
-        a.v.r[u.row0 + i] = bi;
-        a.v.pa[u.row0 + i] = 0.0f;
-        a.v.x[u.row0 + i] = 0.0f;
-        acc = ff_add(acc, ff_prod(bi, bi));
-    }
-    double w = 0.0;
-    if (loop_reduce(acc, u, w) && threadIdx.x == 0) {
-        cg_start(*u.st, a, w);
-        u.st->active = 1;
-        u.st->it = 0;
-        u.st->t0 = global_ns();
+        double w = 0.0;
+        if (loop_reduce(acc, u, w) && threadIdx.x == 0) {
+            cg_start(*u.st, a, w);
+            u.st->t0 = global_ns();
+            u.st->t1 = u.st->t0;
+        }
     }
 }
 
-// the group's 64 block values (one per lane and entry e) into the warp's shared block
-__device__ __forceinline__ const int4* loop_blk(const CgLoopArgs& a, const LoopUnit& u, int l, int sib) {
-    return reinterpret_cast<const int4*>(a.v.blk + (size_t)(((u.row0 - 1) >> 3) + (l >> 3)) * 64 + sib * 8);
+// the sibling group's block-table entries of lane (l, sib)
+__device__ __forceinline__ const int4* loop_blk(const LoopUnit& u, int l, int sib) {
+    return reinterpret_cast<const int4*>(u.v.blk + (size_t)(((u.row0 - 1) >> 3) + (l >> 3)) * 64 + sib * 8);
 }
 
-// p_k = r + beta p_{k-1}, A p_k, p.Ap; iteration it = st->it + 1 takes p_{k-1} from pa
-// when it is odd, from pb when it is even, and writes p_k to the other buffer
-__global__ void __launch_bounds__(kLoopBlock) k_cgl_spmv(CgLoopArgs a) {
-    a.rebase();
-    const LoopUnit u = loop_unit(a);
-    if (!u.st->active || !u.st->go) return;
+// True residual b - A x when due (exact products, float-pair sums), staged in the direction
+// buffer the next iteration writes, and the refinement decision.
+__global__ void __launch_bounds__(kLoopBlock) k_cgl_true(CgLoopArgs a) {
+    const CgLoopControl* ctl = reinterpret_cast<const CgLoopControl*>(a.ctl);
     __shared__ float s_st[27];
     __shared__ float sblk[kLoopWarps * kCgWarpBlockFloats];
-    const int it = u.st->it + 1;
-    const float beta = u.st->beta;
-    const float* pprev = (it & 1) ? a.v.pa : a.v.pb;
-    float* pcur = (it & 1) ? a.v.pb : a.v.pa;
-    if (threadIdx.x < 27) s_st[threadIdx.x] = a.v.stencil[u.d * 27 + threadIdx.x];
-    __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int gi = lane >> 3, sib = lane & 7;
     const int spos = cg_spos(sib);
     float* myblk = sblk + warp * kCgWarpBlockFloats + gi * 80 + ((0x1a081200 >> (gi * 8)) & 0xff);
-    const int nslot = (u.m + 31) >> 5;
-    FF acc = ff_zero();
-    for (int sl = blockIdx.x * kLoopWarps + warp; sl < nslot; sl += gridDim.x * kLoopWarps) {
-        const int l = sl * 32 + lane;
-        const bool mine = l < u.m;   // whole groups: a group is all in or all out
-        if (mine) {
-            const int4* bp = loop_blk(a, u, l, sib);
-            const int4 q0 = bp[0], q1 = bp[1];
-            const int ids[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
-            float vals[8];
+    const int nv = (int)ctl->vstart[ctl->count];
+    for (int vb = blockIdx.x; vb < nv; vb += gridDim.x) {
+        const LoopUnit u = loop_unit(a, ctl, vb);
+        if (!u.st->check) continue;   // uniform over the block
+        const int next = u.st->it + 1;
+        float* stage = (next & 1) ? u.v.pb : u.v.pa;
+        if (threadIdx.x < 27) s_st[threadIdx.x] = u.v.stencil[u.d * 27 + threadIdx.x];
+        __syncthreads();
+        const int nslot = (u.m + 31) >> 5;
+        FF acc = ff_zero();
+        for (int sl = u.bx * kLoopWarps + warp; sl < nslot; sl += u.split * kLoopWarps) {
+            const int l = sl * 32 + lane;
+            const bool mine = l < u.m;   // whole groups: a group is all in or all out
+            if (mine) {
+                const int4* bp = loop_blk(u, l, sib);
+                const int4 q0 = bp[0], q1 = bp[1];
+                const int ids[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
+                float vals[8];
 #pragma unroll
-            for (int e = 0; e < 8; ++e) vals[e] = ids[e] >= 0 ? fmaf(beta, pprev[ids[e]], a.v.r[ids[e]]) : 0.0f;
+                for (int e = 0; e < 8; ++e) vals[e] = ids[e] >= 0 ? u.v.x[ids[e]] : 0.0f;
 #pragma unroll
-            for (int e = 0; e < 8; ++e) myblk[e * 8 + sib] = vals[e];
+                for (int e = 0; e < 8; ++e) myblk[e * 8 + sib] = vals[e];
+            }
+            __syncwarp();
+            if (mine) {
+                FF y = ff_zero();
+#pragma unroll
+                for (int k = 0; k < 27; ++k) y = ff_add(y, ff_prod(s_st[k], myblk[spos + cg_kpos(k)]));
+                const float ri = ff_to_float(ff_add(FF{u.v.b[u.row0 + l], 0.0f}, FF{-y.hi, -y.lo}));
+                stage[u.row0 + l] = ri;
+                acc = ff_add(acc, ff_prod(ri, ri));
+            }
+            __syncwarp();
         }
-        __syncwarp();
-        if (mine) {
-            float y = 0.0f;
-#pragma unroll
-            for (int k = 0; k < 27; ++k) y = fmaf(s_st[k], myblk[spos + cg_kpos(k)], y);
-            const float pi = myblk[spos + cg_kpos(13)];   // the row itself
-            pcur[u.row0 + l] = pi;
-            a.v.ap[u.row0 + l] = y;
-            acc = ff_add(acc, ff_prod(pi, y));
+        double w = 0.0;
+        if (loop_reduce(acc, u, w) && threadIdx.x == 0) {
+            cg_after_true(*u.st, a, w, next);
+            u.st->check = 0;
+            u.st->t1 = global_ns();
         }
-        __syncwarp();
     }
-    double w = 0.0;
-    if (loop_reduce(acc, u, w) && threadIdx.x == 0) {
-        u.st->pap = w;
-        u.st->alpha = cg_quot(u.st->rr, w);
+}
+
+// p_k = r + beta p_{k-1}, A p_k, p.Ap.  Iteration it = st->it + 1 takes p_{k-1} from pa when
+// it is odd, from pb when it is even, and writes p_k to the other buffer.  After a
+// refinement restart (beta = 0) r is the true residual staged in that other buffer: each row
+// takes it into r, and p_k = fma(0, p_{k-1}, r) is that residual itself, so the rows that
+// overwrite the staged values with their p_k write the values already there.
+__global__ void __launch_bounds__(kLoopBlock) k_cgl_spmv(CgLoopArgs a) {
+    const CgLoopControl* ctl = reinterpret_cast<const CgLoopControl*>(a.ctl);
+    __shared__ float s_st[27];
+    __shared__ float sblk[kLoopWarps * kCgWarpBlockFloats];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int gi = lane >> 3, sib = lane & 7;
+    const int spos = cg_spos(sib);
+    float* myblk = sblk + warp * kCgWarpBlockFloats + gi * 80 + ((0x1a081200 >> (gi * 8)) & 0xff);
+    const int nv = (int)ctl->vstart[ctl->count];
+    for (int vb = blockIdx.x; vb < nv; vb += gridDim.x) {
+        const LoopUnit u = loop_unit(a, ctl, vb);
+        if (!u.st->go) continue;   // uniform over the block
+        const int it = u.st->it + 1;
+        const float beta = u.st->beta;
+        const bool restart = u.st->replace != 0;
+        const float* pprev = (it & 1) ? u.v.pa : u.v.pb;
+        float* pcur = (it & 1) ? u.v.pb : u.v.pa;
+        const float* rsrc = restart ? pcur : u.v.r;
+        if (threadIdx.x < 27) s_st[threadIdx.x] = u.v.stencil[u.d * 27 + threadIdx.x];
+        __syncthreads();
+        const int nslot = (u.m + 31) >> 5;
+        FF acc = ff_zero();
+        for (int sl = u.bx * kLoopWarps + warp; sl < nslot; sl += u.split * kLoopWarps) {
+            const int l = sl * 32 + lane;
+            const bool mine = l < u.m;
+            if (mine) {
+                const int4* bp = loop_blk(u, l, sib);
+                const int4 q0 = bp[0], q1 = bp[1];
+                const int ids[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
+                float vals[8];
+#pragma unroll
+                for (int e = 0; e < 8; ++e) vals[e] = ids[e] >= 0 ? fmaf(beta, pprev[ids[e]], rsrc[ids[e]]) : 0.0f;
+#pragma unroll
+                for (int e = 0; e < 8; ++e) myblk[e * 8 + sib] = vals[e];
+            }
+            __syncwarp();
+            if (mine) {
+                float y = 0.0f;
+#pragma unroll
+                for (int k = 0; k < 27; ++k) y = fmaf(s_st[k], myblk[spos + cg_kpos(k)], y);
+                const float pi = myblk[spos + cg_kpos(13)];   // the row itself
+                if (restart) u.v.r[u.row0 + l] = pi;
+                pcur[u.row0 + l] = pi;
+                u.v.ap[u.row0 + l] = y;
+                acc = ff_add(acc, ff_prod(pi, y));
+            }
+            __syncwarp();
+        }
+        double w = 0.0;
+        if (loop_reduce(acc, u, w) && threadIdx.x == 0) {
+            u.st->pap = w;
+            u.st->alpha = cg_quot(u.st->rr, w);
+            u.st->replace = 0;
+        }
     }
 }
 
 // x = x + alpha p, r = r - alpha A p, r.r and the decisions after it
 __global__ void __launch_bounds__(kLoopBlock) k_cgl_update(CgLoopArgs a) {
-    a.rebase();
-    const LoopUnit u = loop_unit(a);
-    if (!u.st->active || !u.st->go) return;
-    const int it = u.st->it + 1;
-    const float alpha = u.st->alpha;
-    const float* pcur = (it & 1) ? a.v.pb : a.v.pa;
-    FF acc = ff_zero();
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < u.m; i += gridDim.x * blockDim.x) {
-        const int row = u.row0 + i;
-        a.v.x[row] = fmaf(alpha, pcur[row], a.v.x[row]);
-        const float ri = fmaf(-alpha, a.v.ap[row], a.v.r[row]);
-        a.v.r[row] = ri;
-        acc = ff_add(acc, ff_prod(ri, ri));
-    }
-    double w = 0.0;
-    if (loop_reduce(acc, u, w) && threadIdx.x == 0) {
-        cg_after_rr(*u.st, a, w, it);
-        u.st->it = it;
-        a.v.cw->cg_iters[u.d] = it;
-    }
-}
-
-// True residual b - A x when due (exact products, float-pair sums), staged in the
-// direction buffer the next iteration overwrites, and the refinement decision.
-__global__ void __launch_bounds__(kLoopBlock) k_cgl_true(CgLoopArgs a) {
-    a.rebase();
-    const LoopUnit u = loop_unit(a);
-    if (!u.st->active || !u.st->check) return;
-    __shared__ float s_st[27];
-    __shared__ float sblk[kLoopWarps * kCgWarpBlockFloats];
-    const int next = u.st->it + 1;
-    float* stage = (next & 1) ? a.v.pb : a.v.pa;
-    if (threadIdx.x < 27) s_st[threadIdx.x] = a.v.stencil[u.d * 27 + threadIdx.x];
-    __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int gi = lane >> 3, sib = lane & 7;
-    const int spos = cg_spos(sib);
-    float* myblk = sblk + warp * kCgWarpBlockFloats + gi * 80 + ((0x1a081200 >> (gi * 8)) & 0xff);
-    const int nslot = (u.m + 31) >> 5;
-    FF acc = ff_zero();
-    for (int sl = blockIdx.x * kLoopWarps + warp; sl < nslot; sl += gridDim.x * kLoopWarps) {
-        const int l = sl * 32 + lane;
-        const bool mine = l < u.m;
-        if (mine) {
-            const int4* bp = loop_blk(a, u, l, sib);
-            const int4 q0 = bp[0], q1 = bp[1];
-            const int ids[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
-            float vals[8];
-#pragma unroll
-            for (int e = 0; e < 8; ++e) vals[e] = ids[e] >= 0 ? a.v.x[ids[e]] : 0.0f;
-#pragma unroll
-            for (int e = 0; e < 8; ++e) myblk[e * 8 + sib] = vals[e];
-        }
-        __syncwarp();
-        if (mine) {
-            FF y = ff_zero();
-#pragma unroll
-            for (int k = 0; k < 27; ++k) y = ff_add(y, ff_prod(s_st[k], myblk[spos + cg_kpos(k)]));
-            const float ri = ff_to_float(ff_add(FF{a.v.b[u.row0 + l], 0.0f}, FF{-y.hi, -y.lo}));
-            stage[u.row0 + l] = ri;
+    const CgLoopControl* ctl = reinterpret_cast<const CgLoopControl*>(a.ctl);
+    const int nv = (int)ctl->vstart[ctl->count];
+    for (int vb = blockIdx.x; vb < nv; vb += gridDim.x) {
+        const LoopUnit u = loop_unit(a, ctl, vb);
+        if (!u.st->go) continue;   // uniform over the block
+        const int it = u.st->it + 1;
+        const float alpha = u.st->alpha;
+        const float* pcur = (it & 1) ? u.v.pb : u.v.pa;
+        FF acc = ff_zero();
+        for (int i = u.bx * kLoopBlock + threadIdx.x; i < u.m; i += u.split * kLoopBlock) {
+            const int row = u.row0 + i;
+            u.v.x[row] = fmaf(alpha, pcur[row], u.v.x[row]);
+            const float ri = fmaf(-alpha, u.v.ap[row], u.v.r[row]);
+            u.v.r[row] = ri;
             acc = ff_add(acc, ff_prod(ri, ri));
         }
-        __syncwarp();
-    }
-    double w = 0.0;
-    if (loop_reduce(acc, u, w) && threadIdx.x == 0) cg_after_true(*u.st, a, w, next);
-}
-
-// refinement restart: the CG continues from the true residual
-__global__ void __launch_bounds__(kLoopBlock) k_cgl_replace(CgLoopArgs a) {
-    a.rebase();
-    const LoopUnit u = loop_unit(a);
-    if (!u.st->active || !u.st->replace) return;
-    const float* stage = ((u.st->it + 1) & 1) ? a.v.pb : a.v.pa;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < u.m; i += gridDim.x * blockDim.x)
-        a.v.r[u.row0 + i] = stage[u.row0 + i];
-}
-
-// one thread: clears the restart flags and continues the loop while any depth of any cloud
-// goes on (the state of cloud k sits k * kCloudStride after cloud 0's)
-__global__ void k_cgl_control(CgLoopState* st, int first, int units, int clouds, cudaGraphConditionalHandle cond) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    unsigned more = 0u;
-    for (int k = 0; k < clouds; ++k) {
-        CgLoopState* sk = (CgLoopState*)((char*)st + (unsigned long long)k * kCloudStride);
-        for (int z = 0; z < units; ++z) {
-            CgLoopState& q = sk[first - z];
-            q.replace = 0;
-            if (q.active && q.go) more = 1u;
+        double w = 0.0;
+        if (loop_reduce(acc, u, w) && threadIdx.x == 0) {
+            cg_after_rr(*u.st, a, w, it);
+            u.st->it = it;
+            u.st->t1 = global_ns();
+            u.v.cw->cg_iters[u.d] = it;
         }
     }
-    cudaGraphSetConditional(cond, more);
 }
 
-// after the loop: the per-depth results the cluster solver reports
+// One thread, last in the body: lists the units with an iteration or a true residual
+// pending for the next pass and continues the loop while there is one.  Whatever the states
+// say, it stops after max_iter + kCgMaxRefine + 2 passes (each depth iterates at most
+// max_iter times, at least once per pass while it goes on, and its checks ride on those
+// passes plus one after the last iteration) and then marks every cloud's counters as timed
+// out.
+__global__ void k_cgl_control(CgLoopArgs a, cudaGraphConditionalHandle cond) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    CgLoopControl* ctl = reinterpret_cast<CgLoopControl*>(a.ctl);
+    const unsigned n0 = ctl->count;
+    unsigned n = 0;
+    for (unsigned i = 0; i < n0; ++i) {   // in place: entry n <= i is written after i is read
+        const unsigned e = ctl->list[i];
+        const unsigned sp = ctl->vstart[i + 1] - ctl->vstart[i];
+        const CgLoopState& q = at_cloud(a.st, (int)(e >> 8))[a.first - (int)(e & 255u)];
+        if (q.go || q.check) {
+            ctl->list[n] = e;
+            ctl->vstart[n + 1] = ctl->vstart[n] + sp;
+            ++n;
+        }
+    }
+    const unsigned passes = ++ctl->passes;
+    if (n > 0 && passes > (unsigned)a.max_iter + kCgMaxRefine + 2u) {
+        n = 0;
+        ctl->vstart[0] = 0u;
+        for (int k = 0; k < a.clouds; ++k) atomicOr(&at_cloud(a.v.cw, k)->error, kErrSpinTimeout);
+    }
+    ctl->count = n;
+    cudaGraphSetConditional(cond, n > 0 ? 1u : 0u);
+}
+
+// after the loop: the per-depth results the cluster solver reports (one thread per unit)
 __global__ void k_cgl_finish(CgLoopArgs a) {
-    a.rebase();
-    const LoopUnit u = loop_unit(a);
-    if (threadIdx.x != 0 || !u.st->active) return;
-    if (u.st->it > 0) cg_report(a.v, u.d, *u.st);
-    a.v.cw->cg_depth_ns[u.d] = global_ns() - u.st->t0;
+    if (threadIdx.x != 0) return;
+    const int k = (int)blockIdx.y, d = a.first - (int)blockIdx.z;
+    const CgLoopState& q = at_cloud(a.st, k)[d];
+    if (!q.active) return;
+    CgcVec v = a.v;
+    v.cw = at_cloud(a.v.cw, k);
+    if (q.it > 0) cg_report(v, d, q);
+    v.cw->cg_depth_ns[d] = q.t1 - q.t0;
 }
 
 // ---- implicit function at the sample points and the iso-value ----------------------
@@ -1051,10 +1150,12 @@ static cudaError_t launch_cg(void (*kernel)(CgcArgs), CgcArgs& a, int grid, int 
 // node added to the captured graph, whose body is captured on ws.loop_body, then the report
 // kernel.  The body runs once even when no depth needs it (the control kernel then ends
 // the loop), so one graph serves every cloud size.
-static cudaError_t launch_cg_loop(Workspace& ws, CgLoopArgs& L, int units) {
-    const int nbx = 2 * ws.num_sms < kLoopMaxBlocks ? 2 * ws.num_sms : kLoopMaxBlocks;   // fixed: sums in a fixed order
-    const dim3 grid(nbx, ws.batch, units);
+static cudaError_t launch_cg_loop(Workspace& ws, CgLoopArgs& L) {
+    // the launches' blocks (8 resident blocks of 256 threads per SM) take the listed units'
+    // virtual blocks in turn
+    const int grid = 8 * ws.num_sms;
     cudaStream_t s = ws.aux4;
+    k_cgl_plan<<<1, 32, 0, s>>>(L);
     k_cgl_init<<<grid, kLoopBlock, 0, s>>>(L);
     cudaError_t e = cudaGetLastError();
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -1080,18 +1181,19 @@ static cudaError_t launch_cg_loop(Workspace& ws, CgLoopArgs& L, int units) {
     cudaStream_t b = ws.loop_body;
     e = cudaStreamBeginCaptureToGraph(b, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return e;
-    k_cgl_spmv<<<grid, kLoopBlock, 0, b>>>(L);
-    k_cgl_update<<<grid, kLoopBlock, 0, b>>>(L);
-    k_cgl_true<<<grid, kLoopBlock, 0, b>>>(L);
-    k_cgl_replace<<<grid, kLoopBlock, 0, b>>>(L);
-    k_cgl_control<<<1, 32, 0, b>>>(L.st, L.first, units, ws.batch, cond);
+    for (int rep = 0; rep < kLoopUnroll; ++rep) {   // a depth that is done skips the rest of the pass
+        k_cgl_true<<<grid, kLoopBlock, 0, b>>>(L);
+        k_cgl_spmv<<<grid, kLoopBlock, 0, b>>>(L);
+        k_cgl_update<<<grid, kLoopBlock, 0, b>>>(L);
+    }
+    k_cgl_control<<<1, 32, 0, b>>>(L, cond);
     cudaError_t el = cudaGetLastError();
     cudaGraph_t captured = nullptr;
     e = cudaStreamEndCapture(b, &captured);
     if (e == cudaSuccess) e = el;
     if (e == cudaSuccess) e = cudaStreamUpdateCaptureDependencies(s, &loop, nullptr, 1, cudaStreamSetCaptureDependencies);
     if (e != cudaSuccess) return e;
-    k_cgl_finish<<<dim3(1, ws.batch, units), 32, 0, s>>>(L);
+    k_cgl_finish<<<dim3(1, ws.batch, L.units), 32, 0, s>>>(L);
     return cudaGetLastError();
 }
 
@@ -1132,10 +1234,13 @@ cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, 
     int cl2 = ws.cg_ctas_fine > 0 ? ws.cg_ctas_fine : 8;
     if (cl2 > g_cg_cluster) cl2 = g_cg_cluster;
     // Depths 5 .. D may outgrow their cluster's shared memory (depths up to 4 have at most
-    // 4,096 rows); in a captured graph those are solved by the device loop, which decides
-    // per run from the row counts.  Issued directly (no graph), they take the global-memory
-    // path of their cluster.
-    const int loop_units = (ws.ev_flags == cudaEventRecordExternal && D >= 5) ? D - 4 : 0;
+    // 4,096 rows).  For trees of depth 8 and 9, whose finest depths usually do, a captured
+    // graph solves those depths by the device loop, which decides per run from the row
+    // counts.  Shallower trees, and pipelines issued directly (no graph), leave them to the
+    // global-memory path of their cluster: their depths fit the clusters up to dense clouds
+    // of millions of points, and a graph holding a while node cannot be profiled kernel by
+    // kernel (Nsight Compute profiles such a graph only as a whole).
+    const int loop_units = (ws.ev_flags == cudaEventRecordExternal && D >= 8) ? D - 4 : 0;
     a.loop_mask = 0u;
     for (int z = 0; z < loop_units; ++z) a.loop_mask |= 1u << (D - z);
     e = cudaEventRecord(ws.ev_fork, s);
@@ -1147,13 +1252,16 @@ cudaError_t solve_build(Workspace& ws, int cg_mode, int cg_iters, float cg_tol, 
         L.v = a.v;
         L.st = ws.cg_loop;
         L.part = ws.cg_loop_part;
+        L.ctl = ws.cg_loop_ctl;
         L.first = D;
+        L.units = loop_units;
+        L.clouds = ws.batch;
         for (int d = 0; d <= kMaxDepth; ++d) L.ctas[d] = (d == D) ? cl1 : (d >= D - ncl + 1 ? cl2 : 1);
         L.loop_mask = a.loop_mask;
         L.tol2 = a.tol2;
         L.max_iter = a.max_iter;
         L.res_period = a.res_period;
-        if (e == cudaSuccess) e = launch_cg_loop(ws, L, loop_units);
+        if (e == cudaSuccess) e = launch_cg_loop(ws, L);
         if (e == cudaSuccess) e = cudaEventRecord(ws.ev_join4, ws.aux4);
         // the coarse sample values and the depth-D terms wait for every depth's solution
         if (e == cudaSuccess) e = cudaStreamWaitEvent(ws.aux, ws.ev_join4, 0);

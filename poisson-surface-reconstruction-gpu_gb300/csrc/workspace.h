@@ -106,6 +106,7 @@ struct Workspace {
     int* cg_blk;            // CG block table: 64 same-depth nodes per sibling group
     CgLoopState* cg_loop;   // [D+1]: device-loop CG state per depth
     double* cg_loop_part;   // [D+1][kLoopMaxBlocks]: its per-block partial sums
+    unsigned* cg_loop_ctl;  // loop control of a launch (passes, listed units; cloud 0's copy)
     double* cg_partial;     // scratch: divergence chunk sums (float pairs, 8 bytes each)
     float* point_val;       // N
     float* pv_coef;         // [27][cap.dnodes / 8 + 64]: per depth-(D-1) node, Bernstein coefficients

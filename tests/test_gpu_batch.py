@@ -67,3 +67,32 @@ def test_batch_isolates_a_failing_cloud():
         # a one-cloud call on a batch handle runs in its first slot
         one = r.SolvePoissionReconstructionMesh(*clouds[0], depth=7)
     same(ref[0], one)
+
+
+def test_batch_depth8_device_loop_equals_alone():
+    """Depth 8: the finest depths of the larger clouds outgrow their clusters' shared memory
+    and are solved by the device loop (a CUDA-graph while node); one loop serves every
+    cloud of the pass, each cloud's depths ending on their own iteration counts.  Each mesh
+    is bit-identical to the one-cloud call's, and the per-depth CG results too."""
+    import psr
+    # the four largest of the first 16 (the reference's algorithm cannot mesh the sparsest
+    # clouds at depth 8: it reads unset vertex records, which both paths reject)
+    clouds = sorted(mix_clouds(16), key=lambda c: -c[0].shape[0])[:4]
+    caps = dict(CAPS, max_depth=8, max_points=160000, max_mesh_vertices=1000000, max_triangles=2000000,
+                max_subdivision_nodes=4000000)
+    ref, ref_st = [], []
+    with psr.PoissonReconstruction(**caps) as r:
+        for p, nr, rgb in clouds:
+            ref.append(r.SolvePoissionReconstructionMesh(p, nr, rgb, depth=8))
+            ref_st.append(r.stats())
+    # the largest cloud's depth 8 has more rows than a 16-CTA cluster holds
+    assert ref_st[0].level_count[8] > 16 * 7168
+    with psr.PoissonReconstruction(batch_clouds=4, **caps) as r:
+        got = r.reconstruct_batch(clouds, depth=8)
+        for i in range(len(clouds)):
+            st, s = r.batch_result(i)
+            assert st == psr.PSR_OK
+            assert list(s.cg_iterations) == list(ref_st[i].cg_iterations)
+            assert list(s.cg_residual) == list(ref_st[i].cg_residual)
+    for a, b in zip(ref, got):
+        same(a, b)
