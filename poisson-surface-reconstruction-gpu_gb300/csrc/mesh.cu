@@ -1429,6 +1429,7 @@ __global__ void __launch_bounds__(kBlock) k_sub_vertex_values(const Counters* c,
     __shared__ int s_node[kSvWarps][kSvMaxLevels];   // slot (subdivision) or octree node
     __shared__ int s_o[kSvWarps][kSvMaxLevels][3];   // function index of the level's node
     __shared__ float s_t[kSvWarps][kSvMaxLevels * 27];
+    __shared__ float s_b[kSvWarps][kSvMaxLevels][9];  // a level's 3 basis values per axis
     const int V = c->n_sub_vertices;
     const float iso = c->iso;
     const int lb = c->sub_lbase[depth];
@@ -1472,6 +1473,12 @@ __global__ void __launch_bounds__(kBlock) k_sub_vertex_values(const Counters* c,
             s_o[w][lane][2] = oz;
         }
         __syncwarp();
+        // the 27 translates of a level share 3 basis values per axis: 9 evaluations per level
+        for (int t = lane; t < nlev * 9; t += 32) {
+            const int l = t / 9, r = t - 9 * l, a = r / 3;
+            s_b[w][l][r] = basis32(s_o[w][l][a] - 1 + (r - 3 * a), a == 0 ? qx : (a == 1 ? qy : qz));
+        }
+        __syncwarp();
         for (int t = lane; t < nlev * 27; t += 32) {
             const int l = t / 27, k = t - 27 * l;
             const int nd = s_node[w][l];
@@ -1479,9 +1486,9 @@ __global__ void __launch_bounds__(kBlock) k_sub_vertex_values(const Counters* c,
             if (nb >= na) nb = sub_value_node(nb, na, G, root_self);
             float term = 0.0f;
             if (nb >= 0) {
-                const float bxk = basis32(s_o[w][l][0] - 1 + k / 9, qx);
-                const float byk = basis32(s_o[w][l][1] - 1 + (k / 3) % 3, qy);
-                const float bzk = basis32(s_o[w][l][2] - 1 + k % 3, qz);
+                const float bxk = s_b[w][l][k / 9];
+                const float byk = s_b[w][l][3 + (k / 3) % 3];
+                const float bzk = s_b[w][l][6 + k % 3];
                 term = __fmul_rn(__fmul_rn(__fmul_rn(x[nb], bxk), byk), bzk);
             }
             s_t[w][t] = term;

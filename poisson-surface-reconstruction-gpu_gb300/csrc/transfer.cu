@@ -379,10 +379,15 @@ __global__ void __launch_bounds__(kBlock) k_colour_far(const Counters* c, int gm
                     while (loff[k + 1] <= f) ++k;   // flattened index -> child (increasing)
                     knn_visit(qx, qy, qz, px, py, pz, lbase[k] + (f - loff[k]), bd, bi);
                 }
-                float ld[4];
-                int li[4];
-                knn_warp_merge(bd, bi, ld, li);
-                knn_merge4(md, mi, ld, li);
+                // merged only when some lane found a sample that enters the 4 nearest so far
+                // (each lane's list is sorted: its head decides; most batches of a far
+                // search bring none)
+                if (__any_sync(0xffffffffu, knn_less(bd[0], bi[0], md[3], mi[3]))) {
+                    float ld[4];
+                    int li[4];
+                    knn_warp_merge(bd, bi, ld, li);
+                    knn_merge4(md, mi, ld, li);
+                }
                 __syncwarp();   // the offsets are read before the next expansion rewrites them
             }
             // the kept inner children: rank by box distance (ties: lower child), pushed in
