@@ -105,6 +105,16 @@ __device__ __forceinline__ void knn_visit(float qx, float qy, float qz, const fl
     knn_insert(bd, bi, d2, i);
 }
 
+// the same, keeping only samples that precede (d4, i4), the 4th nearest found so far: the
+// others cannot be among the 4 nearest
+__device__ __forceinline__ void knn_visit_below(float qx, float qy, float qz, const float* px, const float* py,
+                                                const float* pz, int i, float d4, int i4, float (&bd)[4],
+                                                int (&bi)[4]) {
+    const float dx = __fsub_rn(qx, px[i]), dy = __fsub_rn(qy, py[i]), dz = __fsub_rn(qz, pz[i]);
+    const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+    if (knn_less(d2, i, d4, i4)) knn_insert(bd, bi, d2, i);
+}
+
 // colour of a vertex from its 4 nearest (fewer than 4 samples: the reference's unfilled
 // slots, distance 1e6 and sample 0); weights grow with the squared distance
 __device__ __forceinline__ void colour_blend(const float (&md)[4], const int (&mi)[4], const float* cr,
@@ -377,7 +387,7 @@ __global__ void __launch_bounds__(kBlock) k_colour_far(const Counters* c, int gm
                 int k = 0;
                 for (int f = lane; f < total; f += 32) {
                     while (loff[k + 1] <= f) ++k;   // flattened index -> child (increasing)
-                    knn_visit(qx, qy, qz, px, py, pz, lbase[k] + (f - loff[k]), bd, bi);
+                    knn_visit_below(qx, qy, qz, px, py, pz, lbase[k] + (f - loff[k]), md[3], mi[3], bd, bi);
                 }
                 // merged only when some lane found a sample that enters the 4 nearest so far
                 // (each lane's list is sorted: its head decides; most batches of a far
