@@ -1413,33 +1413,37 @@ __global__ void __launch_bounds__(kBlock) k_sub_edge_maintain(const Counters* c,
 // own plus the slot offset.  A subdivision node's own index comes from its centre
 // ((off + 1/2) / 2^d exactly).  The value is the sum, level after level from the owner's
 // nearest contributing node up to the root and then 27 neighbour terms in slot order, of
-// ((x Fx) Fy) Fz.  One warp per vertex: lane 0 finds the levels (subdivision nodes through
-// the jump links, then the octree ancestors), the lanes gather the coefficients and form
-// the terms in parallel, and lane 0 adds them in that order (absent neighbours as +0, which
-// leaves such a sum unchanged): the chain's dependent loads are paid once per level instead
-// of once per term.
-constexpr int kSvWarps = kBlock / 32;
+// ((x Fx) Fy) Fz.  Eight lanes per vertex (four vertices per warp, whose chains of
+// dependent loads overlap): the group's first lane finds the levels (subdivision nodes
+// through the jump links, then the octree ancestors), the lanes evaluate the 3 basis values
+// per axis of each level and form the terms in parallel, and the first lane adds them in
+// that order (absent neighbours as +0, which leaves such a sum unchanged): the chain's
+// dependent loads are paid once per level instead of once per term.
+constexpr int kSvLanes = 8;
+constexpr int kSvBlock = 128;
+constexpr int kSvGroups = kSvBlock / kSvLanes;
 constexpr int kSvMaxLevels = kMaxDepth + 1;
-__global__ void __launch_bounds__(kBlock) k_sub_vertex_values(const Counters* c, int depth, const float* vx,
-                                                              const float* vy, const float* vz, const int* vowner,
-                                                              const int* neigh, size_t stride, const int* parent,
-                                                              const int* groups, const int* root_self, SubArrays A,
-                                                              const int* enc, const float* x, float* vvalue, int na) {
+__global__ void __launch_bounds__(kSvBlock) k_sub_vertex_values(const Counters* c, int depth, const float* vx,
+                                                                const float* vy, const float* vz, const int* vowner,
+                                                                const int* neigh, size_t stride, const int* parent,
+                                                                const int* groups, const int* root_self, SubArrays A,
+                                                                const int* enc, const float* x, float* vvalue, int na) {
     PSR_CLOUD(c, vx, vy, vz, vowner, neigh, parent, groups, root_self, A, enc, x, vvalue);
-    __shared__ int s_node[kSvWarps][kSvMaxLevels];   // slot (subdivision) or octree node
-    __shared__ int s_o[kSvWarps][kSvMaxLevels][3];   // function index of the level's node
-    __shared__ float s_t[kSvWarps][kSvMaxLevels * 27];
-    __shared__ float s_b[kSvWarps][kSvMaxLevels][9];  // a level's 3 basis values per axis
+    __shared__ int s_node[kSvGroups][kSvMaxLevels];   // slot (subdivision) or octree node
+    __shared__ int s_o[kSvGroups][kSvMaxLevels][3];   // function index of the level's node
+    __shared__ float s_t[kSvGroups][kSvMaxLevels * 27];
+    __shared__ float s_b[kSvGroups][kSvMaxLevels][9];  // a level's 3 basis values per axis
     const int V = c->n_sub_vertices;
     const float iso = c->iso;
     const int lb = c->sub_lbase[depth];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int v = blockIdx.x * kSvWarps + w; v < V; v += gridDim.x * kSvWarps) {
+    const int gl = threadIdx.x & (kSvLanes - 1), w = threadIdx.x / kSvLanes;
+    const unsigned gmask = 0xffu << (threadIdx.x & 24);   // the group's lanes in its warp
+    for (int v = blockIdx.x * kSvGroups + w; v < V; v += gridDim.x * kSvGroups) {
         const float qx = vx[v], qy = vy[v], qz = vz[v];
         const int own = A.live[lb + vowner[v]];
         const int* G = groups + (size_t)A.group[own] * kGroupRec;
         int nsub = 0, nlev = 0;
-        if (lane == 0) {
+        if (gl == 0) {
             // levels whose 27 neighbours are all zero-valued subdivision nodes add nothing:
             // the jump links skip them
             int sn = A.jump[own], now = -1;
@@ -1452,13 +1456,13 @@ __global__ void __launch_bounds__(kBlock) k_sub_vertex_values(const Counters* c,
             nlev = nsub;
             for (; now != -1 && nlev < kSvMaxLevels; now = parent[now]) s_node[w][nlev++] = now;
         }
-        nsub = __shfl_sync(0xffffffffu, nsub, 0);
-        nlev = __shfl_sync(0xffffffffu, nlev, 0);
-        __syncwarp();
-        if (lane < nlev) {
-            const int nd = s_node[w][lane];
+        nsub = __shfl_sync(gmask, nsub, 0, kSvLanes);
+        nlev = __shfl_sync(gmask, nlev, 0, kSvLanes);
+        __syncwarp(gmask);
+        for (int l = gl; l < nlev; l += kSvLanes) {
+            const int nd = s_node[w][l];
             int ox, oy, oz;
-            if (lane < nsub) {
+            if (l < nsub) {
                 const int d = A.depth[nd];
                 const float sc = (float)(1 << d);
                 const int base = (1 << d) - 1;
@@ -1468,18 +1472,18 @@ __global__ void __launch_bounds__(kBlock) k_sub_vertex_values(const Counters* c,
             } else {
                 decode_fn_index(enc[nd], depth, ox, oy, oz);
             }
-            s_o[w][lane][0] = ox;
-            s_o[w][lane][1] = oy;
-            s_o[w][lane][2] = oz;
+            s_o[w][l][0] = ox;
+            s_o[w][l][1] = oy;
+            s_o[w][l][2] = oz;
         }
-        __syncwarp();
+        __syncwarp(gmask);
         // the 27 translates of a level share 3 basis values per axis: 9 evaluations per level
-        for (int t = lane; t < nlev * 9; t += 32) {
+        for (int t = gl; t < nlev * 9; t += kSvLanes) {
             const int l = t / 9, r = t - 9 * l, a = r / 3;
             s_b[w][l][r] = basis32(s_o[w][l][a] - 1 + (r - 3 * a), a == 0 ? qx : (a == 1 ? qy : qz));
         }
-        __syncwarp();
-        for (int t = lane; t < nlev * 27; t += 32) {
+        __syncwarp(gmask);
+        for (int t = gl; t < nlev * 27; t += kSvLanes) {
             const int l = t / 27, k = t - 27 * l;
             const int nd = s_node[w][l];
             int nb = (l < nsub) ? A.neigh[(size_t)k * A.cstride + nd] : neigh[(size_t)k * stride + nd];
@@ -1493,8 +1497,8 @@ __global__ void __launch_bounds__(kBlock) k_sub_vertex_values(const Counters* c,
             }
             s_t[w][t] = term;
         }
-        __syncwarp();
-        if (lane == 0) {
+        __syncwarp(gmask);
+        if (gl == 0) {
             float val = 0.0f;
             for (int l = 0; l < nlev; ++l) {
 #pragma unroll
@@ -1502,7 +1506,7 @@ __global__ void __launch_bounds__(kBlock) k_sub_vertex_values(const Counters* c,
             }
             vvalue[v] = __fsub_rn(val, iso);
         }
-        __syncwarp();
+        __syncwarp(gmask);
     }
 }
 
@@ -1872,7 +1876,7 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
                        1);
     if (e != cudaSuccess) return e;
     k_sub_edge_maintain<<<PSR_GRID(ws, gl), kBlock, 0, s>>>(c, ws.lv_nb, dstride, ws.se_owner, ws.se_kind, ws.s_edge);
-    k_sub_vertex_values<<<PSR_GRID(ws, 4 * ws.num_sms), kBlock, 0, s>>>(
+    k_sub_vertex_values<<<PSR_GRID(ws, 16 * ws.num_sms), kSvBlock, 0, s>>>(
         c, D, ws.sv_x, ws.sv_y, ws.sv_z, ws.sv_owner, ws.neigh, stride, ws.parent, mb.groups, ws.root_self, A, ws.enc,
         ws.xsol, ws.sv_value, na);
     // crossings: staged after the main part's vertices
