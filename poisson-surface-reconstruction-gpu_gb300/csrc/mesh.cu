@@ -1837,8 +1837,11 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
     const size_t stride = (size_t)ws.cap.nodes;
     const size_t dstride = (size_t)ws.cap.sub_dnodes;
     const int na = ws.cap.nodes;
-    // kernels over live depth-D cells (few: one block per SM, grid-stride beyond)
-    const int gl = ws.num_sms;
+    // kernels over live depth-D cells and the scans of the subdivision: sized for a few
+    // thousand live cells (one block per SM, grid-stride beyond) up to depth 7; the trees of
+    // depth 8 and 9 have hundreds of thousands to millions, four blocks per SM
+    const int gl = D >= 8 ? 4 * ws.num_sms : ws.num_sms;
+    const int sbps = D >= 8 ? 4 : 1;
     cudaError_t e;
     SubArrays A{ws.c_vnode, ws.c_key, ws.c_group, ws.c_parent, ws.c_jump, ws.c_depth, ws.c_cx, ws.c_cy, ws.c_cz,
                 ws.c_neigh, (size_t)ws.cap.sub_nodes, ws.c_live, ws.c_poly, ws.c_touch, ws.lv_vnode,
@@ -1854,11 +1857,11 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
                                         ws.neigh, stride, ws.first_child, ws.parent, mb.ov_group, mb.ov_sub, ws.enc,
                                         ws.xsol, ws.root_poly, ws.cap_poly, A},
                            SubLevelStore{c, d, D, A, err}, &c->sub_cand[d], 0, ws.scan, total, err, s, ScanCount{},
-                           1);
+                           sbps);
         if (e != cudaSuccess) return e;
     }
     // the live depth-D cells carry every record from here on, indexed by their live index
-    k_sub_live_neigh<<<PSR_GRID(ws, 2 * ws.num_sms), kBlock, 0, s>>>(c, D, A, ws.lv_nb, dstride, na);
+    k_sub_live_neigh<<<PSR_GRID(ws, 2 * gl), kBlock, 0, s>>>(c, D, A, ws.lv_nb, dstride, na);
     // s_vtx / s_edge need no clearing: every slot of a live cell is written by the owner of
     // that vertex / edge
     k_sub_vertex_owner<<<PSR_GRID(ws, gl), kBlock, 0, s>>>(c, D, A, ws.lv_nb, dstride, ws.s_vmask);
@@ -1866,14 +1869,14 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
                        SubVertexStore{ws.s_vmask, c, D, A, ws.sv_x, ws.sv_y, ws.sv_z, ws.sv_owner, ws.sv_kind,
                                       8 * ws.cap.sub_dnodes, err},
                        &c->n_sub_dnodes, 0, ws.scan, total, err, s, ScanCount{&c->n_sub_vertices, 8 * ws.cap.sub_dnodes},
-                       1);
+                       sbps);
     if (e != cudaSuccess) return e;
     k_sub_vertex_maintain<<<PSR_GRID(ws, gl), kBlock, 0, s>>>(c, ws.lv_nb, dstride, ws.sv_owner, ws.sv_kind, ws.s_vtx);
     k_sub_edge_owner<<<PSR_GRID(ws, gl), kBlock, 0, s>>>(c, D, A, ws.lv_nb, dstride, ws.s_emask);
     e = launch_scan<2>(PopcLoad16{ws.s_emask},
                        SubEdgeStore{ws.s_emask, ws.se_owner, ws.se_kind, mb.edge_of_dnode, 12 * ws.cap.sub_dnodes, err},
                        &c->n_sub_dnodes, 0, ws.scan, total, err, s, ScanCount{&c->n_sub_edges, 12 * ws.cap.sub_dnodes},
-                       1);
+                       sbps);
     if (e != cudaSuccess) return e;
     k_sub_edge_maintain<<<PSR_GRID(ws, gl), kBlock, 0, s>>>(c, ws.lv_nb, dstride, ws.se_owner, ws.se_kind, ws.s_edge);
     k_sub_vertex_values<<<PSR_GRID(ws, 16 * ws.num_sms), kSvBlock, 0, s>>>(
@@ -1883,19 +1886,19 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
     e = launch_scan<2>(SubCrossLoad{ws.se_owner, ws.se_kind, ws.s_vtx, dstride, ws.sv_value, err},
                        SubCrossStore{ws.se_owner, ws.se_kind, ws.s_vtx, dstride, ws.sv_value, ws.sv_x, ws.sv_y,
                                      ws.sv_z, ws.se_cross, ws.part_v, &c->n_cross, ws.part_cap_v, err},
-                       &c->n_sub_edges, 0, ws.scan, total, err, s, ScanCount{&c->n_sub_cross, ws.part_cap_v}, 1);
+                       &c->n_sub_edges, 0, ws.scan, total, err, s, ScanCount{&c->n_sub_cross, ws.part_cap_v}, sbps);
     if (e != cudaSuccess) return e;
     // triangle prefix per live cell
     e = launch_scan<2>(SubCubeLoad{ws.s_vtx, dstride, ws.sv_value, ws.s_cube_class, err},
                        StoreExclusive{mb.tri_of_dnode}, &c->n_sub_dnodes, 0, ws.scan, total, err, s,
-                       ScanCount{&c->n_sub_tri, ws.part_cap_t}, 1);
+                       ScanCount{&c->n_sub_tri, ws.part_cap_t}, sbps);
     if (e != cudaSuccess) return e;
     k_part_table<<<PSR_GRID(ws, grid_for(ws, 1 << 16)), kBlock, 0, s>>>(c, D, mb.groups, ws.lv_vnode, mb.edge_of_dnode, ws.se_cross,
                                                           mb.tri_of_dnode, mb.group_cross0, mb.parts);
     e = launch_scan<2>(SubCubeLoad{ws.s_vtx, dstride, ws.sv_value, ws.s_cube_class, err},
                        SubCubeStore{ws.s_cube_class, ws.s_edge, dstride, ws.se_cross, mb.group_cross0, c, D, A,
                                     ws.part_t, &c->n_tri, ws.part_cap_t, err},
-                       &c->n_sub_dnodes, 0, ws.scan, total, err, s, ScanCount{}, 1);
+                       &c->n_sub_dnodes, 0, ws.scan, total, err, s, ScanCount{}, sbps);
     if (e != cudaSuccess) return e;
     // insertion of all parts
     int* n_parts = mb.misc;
@@ -1904,12 +1907,12 @@ cudaError_t mesh_build_sub(Workspace& ws, const MeshBufs& mb) {
     k_count_parts<<<PSR_GRID(ws, 1), 1, 0, s>>>(c, n_parts, n_staged_v, n_staged_t, ws.part_cap_v, ws.part_cap_t);
     e = launch_scan(KeepVertexLoad{ws.part_v},
                     KeepVertexStore{ws.part_v, ws.mesh_v, mb.kept_prefix, ws.cap.mesh_vertices, err}, n_staged_v, 0,
-                    ws.scan, total, err, s, ScanCount{&c->n_mesh_vertices, ws.cap.mesh_vertices}, 1);
+                    ws.scan, total, err, s, ScanCount{&c->n_mesh_vertices, ws.cap.mesh_vertices}, sbps);
     if (e != cudaSuccess) return e;
     e = launch_scan<1>(KeepTriLoad{ws.part_t, mb.parts, n_parts},
                     KeepTriStore{ws.part_t, mb.parts, n_parts, mb.kept_prefix, n_staged_v, &c->n_mesh_vertices,
                                  ws.mesh_t, ws.cap.mesh_tris, err},
-                    n_staged_t, 0, ws.scan, total, err, s, ScanCount{&c->n_mesh_triangles, ws.cap.mesh_tris}, 1);
+                    n_staged_t, 0, ws.scan, total, err, s, ScanCount{&c->n_mesh_triangles, ws.cap.mesh_tris}, sbps);
     if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }
