@@ -392,6 +392,7 @@ psr_status psr_create(const psr_config* cfg_in, psr_handle** out) {
     A.add(ws.vcount, (size_t)cap.mesh_vertices);
     A.add(ws.cell_start, ((size_t)1 << (3 * kColourGridLevel)) + 16);
     A.add(ws.colour_far, 2 * (size_t)cap.mesh_vertices);
+    A.add(ws.colour_far2, 2 * (size_t)cap.mesh_vertices);
     if (cfg.weld_vertices) {
         size_t slots = 1;
         while (slots < 2 * (size_t)cap.mesh_vertices) slots <<= 1;

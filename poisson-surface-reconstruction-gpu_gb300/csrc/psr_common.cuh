@@ -38,7 +38,8 @@ struct Counters {
     int n_sub_dnodes;             // live depth-D subdivision cells
     int n_sub_vertices, n_sub_edges, n_sub_cross, n_sub_tri;
     int n_mesh_vertices, n_mesh_triangles;
-    int n_colour_far;             // mesh vertices whose 4 nearest samples need the wide search
+    int n_colour_far;             // mesh vertices whose 4 nearest samples the near pass left
+    int n_colour_far2;            //   and of those, the ones the coarser pass left
     int n_colour_cells;           // entries of the colour cell table
     int n_weld;                   // mesh vertices left by welding
     int scan_total;               // scratch total written by scans

@@ -152,22 +152,31 @@ __device__ __forceinline__ unsigned spread3(unsigned v) {
 // is written; otherwise the vertex goes to the far list for the wide search (k_colour_far).
 constexpr int kNearLanes = 8;
 constexpr int kNearGroups = kBlock / kNearLanes;
-__global__ void __launch_bounds__(kBlock) k_colour_near(Counters* c, int g, const float* mv, const float* px,
+constexpr int kNearCoarseCap = 512;   // samples the coarser pass scans per vertex at most
+// The same search one or two levels coarser (g < gt, the table's level: cell m of level g
+// is the range of table entries m << 3 (gt - g) .. (m + 1) << 3 (gt - g)) serves the vertices
+// a finer pass left (`in`: (vertex, bound) pairs, *in_count of them), when their block holds
+// at most `cap` samples; the ones it does not settle go on to `out` with the smaller bound.
+__global__ void __launch_bounds__(kBlock) k_colour_near(Counters* c, int g, int gt, const float* mv, const float* px,
                                                         const float* py, const float* pz, const float* cr,
                                                         const float* cg, const float* cb, const int* cell_start,
-                                                        int* far, float* out) {
-    PSR_CLOUD(c, mv, px, py, pz, cr, cg, cb, cell_start, far, out);
+                                                        const int* in, const int* in_count, int cap, int* far,
+                                                        int* far_count, float* out) {
+    PSR_CLOUD(c, mv, px, py, pz, cr, cg, cb, cell_start, in, in_count, far, far_count, out);
     __shared__ int s_off[kNearGroups][28];
     __shared__ int s_base[kNearGroups][27];
-    const int V = c->n_mesh_vertices;
+    const int V = in ? *in_count : c->n_mesh_vertices;
     const int G = 1 << g;
+    const int shift = 3 * (gt - g);
     const float w = 1.0f / (float)G;
     const int lane = threadIdx.x & (kNearLanes - 1);
     const int gib = threadIdx.x / kNearLanes;
     const unsigned gmask = 0xffu << (threadIdx.x & 24);   // the group's lanes in its warp
     const int group = (blockIdx.x * blockDim.x + threadIdx.x) / kNearLanes;
     const int ngroups = (gridDim.x * blockDim.x) / kNearLanes;
-    for (int v = group; v < V; v += ngroups) {
+    for (int t = group; t < V; t += ngroups) {
+        const int v = in ? in[2 * (size_t)t] : t;
+        const float prev = in ? __int_as_float(in[2 * (size_t)t + 1]) : 1e6f;
         const float qx = mv[3 * (size_t)v], qy = mv[3 * (size_t)v + 1], qz = mv[3 * (size_t)v + 2];
         const int cx = min(max((int)floorf(qx * G), 0), G - 1);
         const int cy = min(max((int)floorf(qy * G), 0), G - 1);
@@ -182,8 +191,8 @@ __global__ void __launch_bounds__(kBlock) k_colour_near(Counters* c, int g, cons
                 const int a = cx + k / 9 - 1, b = cy + (k / 3) % 3 - 1, z = cz + k % 3 - 1;
                 if (a >= 0 && a < G && b >= 0 && b < G && z >= 0 && z < G) {
                     const unsigned m = (spread3((unsigned)a) << 2) | (spread3((unsigned)b) << 1) | spread3((unsigned)z);
-                    base = cell_start[m];
-                    cnt = cell_start[m + 1] - base;
+                    base = cell_start[(size_t)m << shift];
+                    cnt = cell_start[(size_t)(m + 1) << shift] - base;
                 }
             }
             int incl = cnt;
@@ -200,6 +209,14 @@ __global__ void __launch_bounds__(kBlock) k_colour_near(Counters* c, int g, cons
         }
         if (lane == 0) s_off[gib][27] = running;
         __syncwarp(gmask);
+        if (cap > 0 && running > cap) {   // a crowded block: left to the wide search as it is
+            if (lane == 0) {
+                const int slot = atomicAdd(far_count, 1);
+                far[2 * (size_t)slot] = v;
+                far[2 * (size_t)slot + 1] = __float_as_int(prev);
+            }
+            continue;
+        }
         float bd[4] = {1e6f, 1e6f, 1e6f, 1e6f};
         int bi[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
         int k = 0;
@@ -232,10 +249,10 @@ __global__ void __launch_bounds__(kBlock) k_colour_near(Counters* c, int g, cons
         }
         if (lane == 0) {
             if (mi[3] != 0x7fffffff && md[3] < w * w) colour_blend(md, mi, cr, cg, cb, &out[3 * (size_t)v]);
-            else {   // (vertex, the 4th squared distance found here: an upper bound, 1e6 if none)
-                const int slot = atomicAdd(&c->n_colour_far, 1);
+            else {   // (vertex, the 4th squared distance found so far: an upper bound, 1e6 if none)
+                const int slot = atomicAdd(far_count, 1);
                 far[2 * (size_t)slot] = v;
-                far[2 * (size_t)slot + 1] = __float_as_int(mi[3] != 0x7fffffff ? md[3] : 1e6f);
+                far[2 * (size_t)slot + 1] = __float_as_int(mi[3] != 0x7fffffff ? fminf(md[3], prev) : prev);
             }
         }
     }
@@ -297,13 +314,14 @@ static_assert(7 * kColourGridLevel + 9 <= kFarStack, "descent stack");
 __global__ void __launch_bounds__(kBlock) k_colour_far(const Counters* c, int gmax, const float* mv,
                                                        const float* px, const float* py, const float* pz,
                                                        const float* cr, const float* cg, const float* cb,
-                                                       const int* cell_start, const int* far, float* out) {
-    PSR_CLOUD(c, mv, px, py, pz, cr, cg, cb, cell_start, far, out);
+                                                       const int* cell_start, const int* far, const int* far_count,
+                                                       float* out) {
+    PSR_CLOUD(c, mv, px, py, pz, cr, cg, cb, cell_start, far, far_count, out);
     __shared__ int s_node[kFarWarps][kFarStack];    // (level << 24) | cell code
     __shared__ float s_dist[kFarWarps][kFarStack];  // squared distance to the cell's box
     __shared__ int s_loff[kFarWarps][9];            // leaf children scanned together: offsets
     __shared__ int s_lbase[kFarWarps][8];           //   in the flattened range, first samples
-    const int nfar = c->n_colour_far;
+    const int nfar = *far_count;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
@@ -509,10 +527,24 @@ cudaError_t transfer_build(Workspace& ws, int with_colour, int with_normals) {
     if (with_colour) {
         const int g = D < kColourGridLevel ? D : kColourGridLevel;
         int* cell_start = ws.cell_start;   // (1 << 3g) + 1 entries, from transfer_prepare
-        k_colour_near<<<PSR_GRID(ws, grid), kBlock, 0, s>>>(ws.cnt, g, ws.mesh_v, ws.px, ws.py, ws.pz, ws.cr, ws.cg, ws.cb,
-                                              cell_start, ws.colour_far, ws.mesh_c);
+        k_colour_near<<<PSR_GRID(ws, grid), kBlock, 0, s>>>(ws.cnt, g, g, ws.mesh_v, ws.px, ws.py, ws.pz, ws.cr, ws.cg,
+                                                          ws.cb, cell_start, nullptr, nullptr, 0, ws.colour_far,
+                                                          &ws.cnt->n_colour_far, ws.mesh_c);
+        // the vertices it leaves: the same search two levels coarser (a sparse cloud's
+        // vertices find their 4 samples there), then the wide search for the rest
+        const int* far_list = ws.colour_far;
+        const int* far_count = &ws.cnt->n_colour_far;
+        if (D >= 8) {
+            k_colour_near<<<PSR_GRID(ws, grid), kBlock, 0, s>>>(ws.cnt, g - 2, g, ws.mesh_v, ws.px, ws.py, ws.pz, ws.cr,
+                                                              ws.cg, ws.cb, cell_start, ws.colour_far,
+                                                              &ws.cnt->n_colour_far, kNearCoarseCap, ws.colour_far2,
+                                                              &ws.cnt->n_colour_far2, ws.mesh_c);
+            far_list = ws.colour_far2;
+            far_count = &ws.cnt->n_colour_far2;
+        }
         k_colour_far<<<PSR_GRID(ws, ws.num_sms * 8), kBlock, 0, s>>>(ws.cnt, g, ws.mesh_v, ws.px, ws.py, ws.pz, ws.cr,
-                                                                   ws.cg, ws.cb, cell_start, ws.colour_far, ws.mesh_c);
+                                                                   ws.cg, ws.cb, cell_start, far_list, far_count,
+                                                                   ws.mesh_c);
     }
     if (with_normals) {
         double* acc = ws.nacc;

@@ -160,7 +160,8 @@ struct Workspace {
     double* nacc;           // per output vertex normal accumulator (3 doubles)
     int* vcount;            // per output vertex triangle count
     int* cell_start;        // sample grid for the colour search
-    int* colour_far;        // mesh vertices left to the wide colour search, with bounds
+    int* colour_far;        // (vertex, bound) pairs the near colour search left
+    int* colour_far2;       // those the coarser search left (trees of depth 8 and 9)
     // vertex welding (allocated only when the handle welds)
     int* weld_table = nullptr;   // hash slots: a vertex of the class, then its smallest index
     unsigned weld_mask = 0;      // slots - 1 (a power of two >= 2 x mesh vertex capacity)
