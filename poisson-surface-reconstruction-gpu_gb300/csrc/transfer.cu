@@ -307,7 +307,7 @@ __device__ __forceinline__ void knn_merge4(float (&md)[4], int (&mi)[4], const f
 // nearest under the (distance, index) order, whatever the distance.  The stack holds at
 // most 7 siblings per level plus 8 children: 7 gmax + 9 entries.
 constexpr int kFarWarps = kBlock / 32;
-constexpr int kFarLeaf = 32;
+constexpr int kFarLeaf = 128;
 constexpr int kFarStack = 64;
 static_assert(7 * kColourGridLevel + 9 <= kFarStack, "descent stack");
 
