@@ -65,8 +65,13 @@ typedef struct psr_config {
                                   normals come from the welded mesh.  0 (default): as the
                                   reference */
     int disable_graphs;        /* 0 (default): each (depth, options) pipeline is captured once
-                                  into a CUDA graph and replayed; 1: kernels are issued one by
-                                  one on every call (same results; for inspection) */
+                                  into a CUDA graph and replayed; for depths 8 and 9 the graph
+                                  solves the CG systems too large for a cluster's shared memory
+                                  in a device loop (a while node; such a graph is profiled by
+                                  Nsight Compute only as a whole).  1: kernels are issued one by
+                                  one on every call, those systems on the clusters' global-memory
+                                  path (meshes within the CG tolerance of the graph's; for
+                                  inspection and per-kernel profiling) */
     int root_poly_capacity;    /* 0 (default): max(65536, nodes / 16).  Subdivision roots beyond
                                   this many evaluate the levels above them by walking their
                                   octree chain instead of from one cached polynomial per root

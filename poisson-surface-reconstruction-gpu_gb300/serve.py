@@ -11,7 +11,11 @@ Each slot's pipeline is one chain (concurrent_stages off): with K reconstruction
 already overlapping, a second stream per slot only adds contention.
 Results are the same as psr_reconstruct alone (the pipeline is deterministic per handle).
 
-Device buffers for the slots' outputs come from PyTorch (plumbing only).
+Device buffers for the slots' outputs come from PyTorch (plumbing only).  With host
+outputs, each slot writes its meshes into a ring of `host_out_sets` pinned buffer sets
+(the GPU writes them directly) and a finished request holds views of its set, not copies:
+they stay valid until its slot starts the host_out_sets-th request after it (copy them to
+keep them longer).
 """
 import time
 from dataclasses import dataclass
@@ -33,8 +37,8 @@ class Request:
     tag: object = None
     arrival: float = 0.0          # host clock (time.perf_counter) when it arrived
     # filled on completion
-    vertices: object = None       # device tensor V x 3 (unit cube)
-    triangles: object = None      # device tensor T x 3
+    vertices: object = None       # V x 3 (unit cube): a device tensor, or with host outputs a
+    triangles: object = None      # T x 3     view of the slot's pinned buffers (see above)
     colors: object = None
     normals_out: object = None
     center: tuple = ()
@@ -52,8 +56,10 @@ class Request:
 class _Slot:
     recon: object
     stream: object
-    out: list
+    out: list                     # output buffers [vertices, triangles, colours, normals]
     mesh: object = None
+    ring: list = None             # host outputs: the pinned buffer sets `out` rotates over
+    ring_at: int = 0
     req: Request = None
     max_points: int = 1 << 30     # the largest cloud and depth the slot's workspace takes
     max_depth: int = 9
@@ -78,7 +84,7 @@ class Server:
 
     def __init__(self, slots=8, max_depth=7, max_points=300000, max_triangles=1000000, max_mesh_vertices=300000,
                  compute_colors=True, compute_normals=True, device=0, memory_budget=None, host_outputs=False,
-                 classes=None, **caps):
+                 classes=None, host_out_sets=2, **caps):
         import torch
         self.torch = torch
         self.dev = torch.device("cuda", device)
@@ -111,11 +117,14 @@ class Server:
                     if host_outputs:
                         return torch.empty(shape, dtype=dtype).pin_memory()
                     return torch.empty(shape, dtype=dtype, device=self.dev)
-                out = [buf((vcap, 3), torch.float32), buf((tcap, 3), torch.int32),
-                       buf((vcap, 3), torch.float32) if compute_colors else None,
-                       buf((vcap, 3), torch.float32) if compute_normals else None]
-                self.slots.append(_Slot(r, torch.cuda.Stream(self.dev), out, max_points=r.config.max_points,
-                                        max_depth=r.config.max_depth, vcap=vcap, tcap=tcap))
+                def out_set():
+                    return [buf((vcap, 3), torch.float32), buf((tcap, 3), torch.int32),
+                            buf((vcap, 3), torch.float32) if compute_colors else None,
+                            buf((vcap, 3), torch.float32) if compute_normals else None]
+                ring = [out_set() for _ in range(max(2, host_out_sets))] if host_outputs else None
+                self.slots.append(_Slot(r, torch.cuda.Stream(self.dev), ring[0] if ring else out_set(), ring=ring,
+                                        max_points=r.config.max_points, max_depth=r.config.max_depth, vcap=vcap,
+                                        tcap=tcap))
         self.memory_bytes = used
         self.queue = []
         self.done = []
@@ -173,14 +182,25 @@ class Server:
         req.finished = time.perf_counter()
         req.error = error
         if not error:
-            with self.torch.cuda.stream(sl.stream):   # device copies stay ordered before the slot's next run
-                nv, nt = m.vertex_count, m.triangle_count
-                req.vertices = sl.out[0][:nv].clone()
-                req.triangles = sl.out[1][:nt].clone()
-                req.colors = sl.out[2][:nv].clone() if (sl.out[2] is not None and m.colors) else None
-                req.normals_out = sl.out[3][:nv].clone() if sl.out[3] is not None else None
-            if not self.host_outputs:
-                sl.stream.synchronize()   # only the copies above are left on the slot's stream
+            nv, nt = m.vertex_count, m.triangle_count
+            if sl.ring:
+                # host outputs: the GPU wrote them into this set; the request keeps views and
+                # the slot's next request writes the next set of the ring
+                o = sl.out
+                req.vertices = o[0][:nv]
+                req.triangles = o[1][:nt]
+                req.colors = o[2][:nv] if (o[2] is not None and m.colors) else None
+                req.normals_out = o[3][:nv] if o[3] is not None else None
+                sl.ring_at = (sl.ring_at + 1) % len(sl.ring)
+                sl.out = sl.ring[sl.ring_at]
+            else:
+                with self.torch.cuda.stream(sl.stream):   # device copies stay ordered before the slot's next run
+                    req.vertices = sl.out[0][:nv].clone()
+                    req.triangles = sl.out[1][:nt].clone()
+                    req.colors = sl.out[2][:nv].clone() if (sl.out[2] is not None and m.colors) else None
+                    req.normals_out = sl.out[3][:nv].clone() if sl.out[3] is not None else None
+                if not self.host_outputs:
+                    sl.stream.synchronize()   # only the copies above are left on the slot's stream
             req.center = tuple(m.center)
             req.scale = m.scale
         sl.req = None

@@ -56,6 +56,40 @@ def test_served_matches_alone():
                 assert r.scale == pytest.approx(m.scale, rel=0, abs=0)
 
 
+def test_served_host_io_matches_alone():
+    """Host-resident inputs (pinned) and outputs: the GPU reads the clouds and writes the
+    meshes in pinned memory; each finished request holds views of its slot's output set,
+    valid until the slot starts the host_out_sets-th request after it (here four sets for
+    four requests, whichever slots take them)."""
+    import torch
+    import psr
+    from serve import Request, Server
+
+    cl = clouds()[:4]
+    caps = dict(max_depth=7, max_points=60000, max_triangles=400000, max_mesh_vertices=200000,
+                max_subdivision_nodes=4000000)
+    srv = Server(slots=2, host_outputs=True, host_out_sets=4, **caps)
+    try:
+        reqs = [Request(xyz=torch.from_numpy(p).pin_memory(), normals=torch.from_numpy(nr).pin_memory(),
+                        rgb=torch.from_numpy(rgb).pin_memory() if rgb is not None else None, depth=d, tag=i)
+                for i, (p, nr, rgb, d) in enumerate(cl)]
+        done = srv.run(reqs)
+        assert all(not r.error for r in done), [r.error for r in done]
+        by_tag = {r.tag: r for r in done}
+        with psr.PoissonReconstruction(compute_colors=True, compute_normals=True, **caps) as alone:
+            for i, (p, nr, rgb, d) in enumerate(cl):
+                m = alone.SolvePoissionReconstructionMesh(p, nr, rgb, depth=d)
+                r = by_tag[i]
+                assert not r.vertices.is_cuda and r.vertices.is_pinned()
+                np.testing.assert_array_equal(r.vertices.numpy(), m.vertices)
+                np.testing.assert_array_equal(r.triangles.numpy(), m.triangles)
+                np.testing.assert_array_equal(r.normals_out.numpy(), m.normals)
+                if rgb is not None:
+                    np.testing.assert_array_equal(r.colors.numpy(), m.colors)
+    finally:
+        srv.close()
+
+
 def test_submit_poll_wait_states():
     import torch
     import psr

@@ -132,3 +132,21 @@ def test_footprint_classes_first_fit_and_rejection():
     # the small clouds did not wait behind big1, which waited for the large slot
     assert by["s1"].finished <= by["big1"].admitted + 1e-3
     assert all(by[t].error == "" for t in ("big0", "big1", "s0", "s1"))
+
+
+def test_host_output_ring_hands_out_views_of_alternating_sets():
+    """With host outputs a finished request keeps views of the pinned set its slot wrote
+    (no copy), and the slot's next request writes the next set of its ring."""
+    a = FakeRecon("a", polls=1)
+    s = make_server([a])
+    s.host_outputs = True
+    ring = [[torch.zeros(16, 3), torch.zeros(16, 3, dtype=torch.int32), None, torch.zeros(16, 3)] for _ in range(2)]
+    sl = s.slots[0]
+    sl.ring, sl.ring_at, sl.out = ring, 0, ring[0]
+    done = s.run([req(4, k) for k in range(4)])
+    assert [r.tag for r in done] == [0, 1, 2, 3]
+    for k, r in enumerate(done):
+        assert r.error == ""
+        assert r.vertices.untyped_storage().data_ptr() == ring[k % 2][0].untyped_storage().data_ptr()
+        assert r.triangles.untyped_storage().data_ptr() == ring[k % 2][1].untyped_storage().data_ptr()
+    assert sl.out is ring[0] and sl.ring_at == 0
