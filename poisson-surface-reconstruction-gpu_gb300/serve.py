@@ -11,11 +11,11 @@ Each slot's pipeline is one chain (concurrent_stages off): with K reconstruction
 already overlapping, a second stream per slot only adds contention.
 Results are the same as psr_reconstruct alone (the pipeline is deterministic per handle).
 
-Device buffers for the slots' outputs come from PyTorch (plumbing only).  With host
-outputs, each slot writes its meshes into a ring of `host_out_sets` pinned buffer sets
-(the GPU writes them directly) and a finished request holds views of its set, not copies:
-they stay valid until its slot starts the host_out_sets-th request after it (copy them to
-keep them longer).
+Output buffers come from PyTorch (plumbing only): device memory, or pinned host memory
+with `host_outputs` (the GPU writes the meshes there directly).  Each slot writes its
+meshes into a ring of `out_sets` buffer sets and a finished request holds views of its set,
+not copies: they stay valid until its slot starts the out_sets-th request after it (copy
+them to keep them longer).
 """
 import time
 from dataclasses import dataclass
@@ -37,8 +37,8 @@ class Request:
     tag: object = None
     arrival: float = 0.0          # host clock (time.perf_counter) when it arrived
     # filled on completion
-    vertices: object = None       # V x 3 (unit cube): a device tensor, or with host outputs a
-    triangles: object = None      # T x 3     view of the slot's pinned buffers (see above)
+    vertices: object = None       # V x 3 (unit cube), T x 3: views of the slot's output
+    triangles: object = None      # buffers (device, or pinned host memory; see above)
     colors: object = None
     normals_out: object = None
     center: tuple = ()
@@ -58,7 +58,7 @@ class _Slot:
     stream: object
     out: list                     # output buffers [vertices, triangles, colours, normals]
     mesh: object = None
-    ring: list = None             # host outputs: the pinned buffer sets `out` rotates over
+    ring: list = None             # the output buffer sets `out` rotates over
     ring_at: int = 0
     req: Request = None
     max_points: int = 1 << 30     # the largest cloud and depth the slot's workspace takes
@@ -84,7 +84,7 @@ class Server:
 
     def __init__(self, slots=8, max_depth=7, max_points=300000, max_triangles=1000000, max_mesh_vertices=300000,
                  compute_colors=True, compute_normals=True, device=0, memory_budget=None, host_outputs=False,
-                 classes=None, host_out_sets=2, **caps):
+                 classes=None, out_sets=2, **caps):
         import torch
         self.torch = torch
         self.dev = torch.device("cuda", device)
@@ -104,7 +104,7 @@ class Server:
             for k in range(count):
                 r = psr.PoissonReconstruction(compute_colors=compute_colors, compute_normals=compute_normals,
                                               device=device, **{"concurrent_stages": False, **caps, **cl})
-                cost = self.slot_bytes(r, vcap, tcap)
+                cost = self.slot_bytes(r, vcap, tcap, out_sets)
                 if memory_budget is not None and used + cost > memory_budget:
                     r.close()
                     if k == 0:
@@ -121,16 +121,16 @@ class Server:
                     return [buf((vcap, 3), torch.float32), buf((tcap, 3), torch.int32),
                             buf((vcap, 3), torch.float32) if compute_colors else None,
                             buf((vcap, 3), torch.float32) if compute_normals else None]
-                ring = [out_set() for _ in range(max(2, host_out_sets))] if host_outputs else None
-                self.slots.append(_Slot(r, torch.cuda.Stream(self.dev), ring[0] if ring else out_set(), ring=ring,
+                ring = [out_set() for _ in range(max(2, out_sets))]
+                self.slots.append(_Slot(r, torch.cuda.Stream(self.dev), ring[0], ring=ring,
                                         max_points=r.config.max_points, max_depth=r.config.max_depth, vcap=vcap,
                                         tcap=tcap))
         self.memory_bytes = used
         self.queue = []
         self.done = []
 
-    def slot_bytes(self, recon, vcap=None, tcap=None):
-        """Device bytes of one slot: the handle's workspace plus its output mesh buffers
+    def slot_bytes(self, recon, vcap=None, tcap=None, out_sets=2):
+        """Device bytes of one slot: the handle's workspace plus its output mesh buffer sets
         (vertices, triangles, and colours / normals when computed; none on the device when
         outputs go to pinned host memory)."""
         vcap = self.vcap if vcap is None else vcap
@@ -138,7 +138,7 @@ class Server:
         out = 0
         if not self.host_outputs:
             per_vertex = 12 * (1 + int(self.compute_colors) + int(self.compute_normals))
-            out = per_vertex * vcap + 12 * tcap
+            out = max(2, out_sets) * (per_vertex * vcap + 12 * tcap)
         return recon.memory_bytes() + out
 
     def close(self):
@@ -183,24 +183,16 @@ class Server:
         req.error = error
         if not error:
             nv, nt = m.vertex_count, m.triangle_count
+            # the reconstruction wrote its mesh into this set before its completion event: the
+            # request keeps views and the slot's next request writes the next set of the ring
+            o = sl.out
+            req.vertices = o[0][:nv]
+            req.triangles = o[1][:nt]
+            req.colors = o[2][:nv] if (o[2] is not None and m.colors) else None
+            req.normals_out = o[3][:nv] if o[3] is not None else None
             if sl.ring:
-                # host outputs: the GPU wrote them into this set; the request keeps views and
-                # the slot's next request writes the next set of the ring
-                o = sl.out
-                req.vertices = o[0][:nv]
-                req.triangles = o[1][:nt]
-                req.colors = o[2][:nv] if (o[2] is not None and m.colors) else None
-                req.normals_out = o[3][:nv] if o[3] is not None else None
                 sl.ring_at = (sl.ring_at + 1) % len(sl.ring)
                 sl.out = sl.ring[sl.ring_at]
-            else:
-                with self.torch.cuda.stream(sl.stream):   # device copies stay ordered before the slot's next run
-                    req.vertices = sl.out[0][:nv].clone()
-                    req.triangles = sl.out[1][:nt].clone()
-                    req.colors = sl.out[2][:nv].clone() if (sl.out[2] is not None and m.colors) else None
-                    req.normals_out = sl.out[3][:nv].clone() if sl.out[3] is not None else None
-                if not self.host_outputs:
-                    sl.stream.synchronize()   # only the copies above are left on the slot's stream
             req.center = tuple(m.center)
             req.scale = m.scale
         sl.req = None

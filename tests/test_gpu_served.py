@@ -31,7 +31,7 @@ def test_served_matches_alone():
     cl = clouds()
     caps = dict(max_depth=7, max_points=60000, max_triangles=400000, max_mesh_vertices=200000,
                 max_subdivision_nodes=4000000)
-    srv = Server(slots=3, **caps)
+    srv = Server(slots=3, out_sets=10, **caps)   # results kept until the end: no set is reused
     try:
         reqs = [Request(xyz=torch.from_numpy(p).to(dev), normals=torch.from_numpy(nr).to(dev),
                         rgb=torch.from_numpy(rgb).to(dev) if rgb is not None else None, depth=d, tag=i)
@@ -59,8 +59,8 @@ def test_served_matches_alone():
 def test_served_host_io_matches_alone():
     """Host-resident inputs (pinned) and outputs: the GPU reads the clouds and writes the
     meshes in pinned memory; each finished request holds views of its slot's output set,
-    valid until the slot starts the host_out_sets-th request after it (here four sets for
-    four requests, whichever slots take them)."""
+    valid until the slot starts the out_sets-th request after it (here four sets for four
+    requests, whichever slots take them)."""
     import torch
     import psr
     from serve import Request, Server
@@ -68,7 +68,7 @@ def test_served_host_io_matches_alone():
     cl = clouds()[:4]
     caps = dict(max_depth=7, max_points=60000, max_triangles=400000, max_mesh_vertices=200000,
                 max_subdivision_nodes=4000000)
-    srv = Server(slots=2, host_outputs=True, host_out_sets=4, **caps)
+    srv = Server(slots=2, host_outputs=True, out_sets=4, **caps)
     try:
         reqs = [Request(xyz=torch.from_numpy(p).pin_memory(), normals=torch.from_numpy(nr).pin_memory(),
                         rgb=torch.from_numpy(rgb).pin_memory() if rgb is not None else None, depth=d, tag=i)

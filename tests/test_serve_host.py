@@ -135,8 +135,8 @@ def test_footprint_classes_first_fit_and_rejection():
 
 
 def test_host_output_ring_hands_out_views_of_alternating_sets():
-    """With host outputs a finished request keeps views of the pinned set its slot wrote
-    (no copy), and the slot's next request writes the next set of its ring."""
+    """A finished request keeps views of the output set its slot wrote (no copy), and the
+    slot's next request writes the next set of its ring."""
     a = FakeRecon("a", polls=1)
     s = make_server([a])
     s.host_outputs = True
