@@ -298,14 +298,15 @@ __device__ __forceinline__ void knn_merge4(float (&md)[4], int (&mi)[4], const f
 // 3 (gmax - g); the children of cell m are cells 8m .. 8m + 7 one level finer.  Expanding
 // a node, the lanes 0..7 take its children: a child that is a finest-level cell or holds
 // at most kFarLeaf samples is scanned at once, together with its leaf siblings (their
-// samples flattened over the lanes, each lane keeping a sorted 4-list, merged by
-// warp-minimum rounds into the warp's 4 nearest so far); the other non-empty children are
-// pushed onto a per-warp stack, nearest box first.  A node whose box is farther than the
-// bound (the 4th nearest so far, or the near pass's 4th distance when smaller, with 1e-4
-// relative slack) is skipped: a sample's float distance is at least its cell box's (the
-// sample lies in the closed box and rounding is monotone).  So the result is the exact 4
-// nearest under the (distance, index) order, whatever the distance.  The stack holds at
-// most 7 siblings per level plus 8 children: 7 gmax + 9 entries.
+// samples flattened over the lanes, each lane keeping a sorted 4-list of the samples ahead
+// of the warp's 4th nearest so far, merged by warp-minimum rounds into the warp's 4 nearest
+// only when some lane holds one); the other non-empty children are pushed onto a per-warp
+// stack, nearest box first.  A node whose box is farther than the bound (the 4th nearest
+// so far, or the near passes' 4th distance when smaller, with 1e-4 relative slack) is
+// skipped: a sample's float distance is at least its cell box's (the sample lies in the
+// closed box and rounding is monotone).  So the result is the exact 4 nearest under the
+// (distance, index) order, whatever the distance.  The stack holds at most 7 siblings per
+// level plus 8 children: 7 gmax + 9 entries.
 constexpr int kFarWarps = kBlock / 32;
 constexpr int kFarLeaf = 128;
 constexpr int kFarStack = 64;
